@@ -1,0 +1,266 @@
+"""CPU checkers for the GMM hot path -- TEST INFRASTRUCTURE ONLY.
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` may use
+this package, and only as the checker (or, in bench.py, as the timed CPU baseline). The
+product package ``gmm_gb300`` never imports it.
+
+Two libraries, both built by ``oracle/Makefile``:
+
+* ``_build/liboracle.so`` -- the C restatement in ``gmm_oracle.c``: ``*32`` functions follow
+  the reference CPU estimator's float semantics operation by operation (the "port"), ``*64``
+  functions are the FP64 oracle. Builds on any host.
+* ``_ref/libgmmref.so`` -- the reference's own CPU estimator and ``CModelAdapt`` compiled from
+  the reference sources (only where those sources are present). Used to pin the port.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libgmmref.so")
+REF_SRC = "/root/reference/GMM/lib_bmssr"
+
+ACC_MEAN, ACC_VAR, ACC_PROBS_ONLY = 1, 2, 4
+
+
+class _Opts(C.Structure):
+    _fields_ = [("minLogLike", C.c_float), ("minGamma", C.c_float),
+                ("min_var", C.c_float), ("threads", C.c_int)]
+
+
+def build(ref: bool | None = None) -> None:
+    """Compile the port (always) and the reference library (when its sources exist)."""
+    subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
+    if ref is None:
+        ref = os.path.isdir(REF_SRC)
+    if ref:
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_ROOT={REF_SRC}"], check=True)
+
+
+_lib = None
+_ref = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build(ref=False)
+        _lib = C.CDLL(LIB_PATH)
+    return _lib
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_PATH)
+
+
+def ref():
+    global _ref
+    if _ref is None:
+        _ref = C.CDLL(REF_PATH)
+        _ref.ref_last_error.restype = C.c_char_p
+    return _ref
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _opts(threads=1, minLogLike=-1e20, minGamma=1e-4, min_var=1e-6):
+    return _Opts(minLogLike, minGamma, min_var, threads)
+
+
+def rearrange_order(w):
+    w = _f32(w)
+    order = np.zeros(len(w), np.int32)
+    nz = lib().orc_rearrange_order(len(w), _p(w), _p(order))
+    return order, nz
+
+
+def loglikes32(X, w, mu, var, threads=1, **kw):
+    X, w, mu, var = map(_f32, (X, w, mu, var))
+    N, D = X.shape
+    out = np.zeros(N, np.float32)
+    trouble = C.c_int(0)
+    o = _opts(threads, **kw)
+    rc = lib().orc32_loglikes(_p(X), C.c_longlong(N), D, len(w), _p(w), _p(mu), _p(var),
+                              C.byref(o), _p(out), C.byref(trouble))
+    if rc:
+        raise RuntimeError(f"orc32_loglikes failed ({rc})")
+    return out
+
+
+def accumulate32(X, w, mu, var, flags=ACC_MEAN | ACC_VAR, threads=1, **kw):
+    X, w, mu, var = map(_f32, (X, w, mu, var))
+    N, D = X.shape
+    M = len(w)
+    n, F, S = np.zeros(M), np.zeros((M, D)), np.zeros((M, D))
+    tl, tn = C.c_double(0.0), C.c_longlong(0)
+    o = _opts(threads, **kw)
+    rc = lib().orc32_accumulate(_p(X), C.c_longlong(N), D, M, _p(w), _p(mu), _p(var),
+                                C.byref(o), flags, _p(n), _p(F), _p(S), C.byref(tl), C.byref(tn))
+    if rc:
+        raise RuntimeError(f"orc32_accumulate failed ({rc})")
+    return dict(n=n, F=F, S=S, totLL=tl.value, totN=tn.value)
+
+
+def loglikes64(X, w, mu, var, **kw):
+    X, w, mu, var = map(_f32, (X, w, mu, var))
+    N, D = X.shape
+    out = np.zeros(N)
+    o = _opts(1, **kw)
+    rc = lib().orc64_loglikes(_p(X), C.c_longlong(N), D, len(w), _p(w), _p(mu), _p(var),
+                              C.byref(o), _p(out))
+    if rc:
+        raise RuntimeError(f"orc64_loglikes failed ({rc})")
+    return out
+
+
+def accumulate64(X, w, mu, var, flags=ACC_MEAN | ACC_VAR, **kw):
+    X, w, mu, var = map(_f32, (X, w, mu, var))
+    N, D = X.shape
+    M = len(w)
+    n, F, S = np.zeros(M), np.zeros((M, D)), np.zeros((M, D))
+    tl, tn = C.c_double(0.0), C.c_longlong(0)
+    o = _opts(1, **kw)
+    rc = lib().orc64_accumulate(_p(X), C.c_longlong(N), D, M, _p(w), _p(mu), _p(var),
+                                C.byref(o), flags, _p(n), _p(F), _p(S), C.byref(tl), C.byref(tn))
+    if rc:
+        raise RuntimeError(f"orc64_accumulate failed ({rc})")
+    return dict(n=n, F=F, S=S, totLL=tl.value, totN=tn.value)
+
+
+def em_update(w, mu, var, st, upW=True, upM=True, upV=True, min_var=1e-6):
+    w, mu, var = _f32(w).copy(), _f32(mu).copy(), _f32(var).copy()
+    M, D = mu.shape
+    n, F, S = (np.ascontiguousarray(st[k], np.float64) for k in ("n", "F", "S"))
+    alive = lib().orc_em_update(M, D, _p(w), _p(mu), _p(var), _p(n), _p(F), _p(S),
+                                C.c_longlong(st["totN"]), int(upW), int(upM), int(upV),
+                                C.c_float(min_var))
+    return w, mu, var, alive
+
+
+def em_update64(w, st, upW=True, upM=True, upV=True, min_var=1e-6):
+    w = _f32(w)
+    M, D = st["F"].shape
+    n, F, S = (np.ascontiguousarray(st[k], np.float64) for k in ("n", "F", "S"))
+    ow, omu, ovar = np.zeros(M), np.zeros((M, D)), np.zeros((M, D))
+    alive = lib().orc64_em_update(M, D, _p(w), _p(n), _p(F), _p(S), C.c_longlong(st["totN"]),
+                                  int(upW), int(upM), int(upV), C.c_double(min_var),
+                                  _p(ow), _p(omu), _p(ovar))
+    return ow, omu, ovar, alive
+
+
+def map_update(ubm_w, ubm_mu, ubm_var, st, tau, w=None, mu=None, var=None,
+               upW=False, upM=True, upV=False, min_var=1e-6):
+    ubm_w, ubm_mu, ubm_var = map(_f32, (ubm_w, ubm_mu, ubm_var))
+    w = (ubm_w if w is None else _f32(w)).copy()
+    mu = (ubm_mu if mu is None else _f32(mu)).copy()
+    var = (ubm_var if var is None else _f32(var)).copy()
+    M, D = mu.shape
+    n, F, S = (np.ascontiguousarray(st[k], np.float64) for k in ("n", "F", "S"))
+    lib().orc_map_update(M, D, _p(w), _p(mu), _p(var), _p(ubm_w), _p(ubm_mu), _p(ubm_var),
+                         _p(n), _p(F), _p(S), C.c_longlong(st["totN"]), int(tau),
+                         int(upW), int(upM), int(upV), C.c_float(min_var))
+    return w, mu, var
+
+
+def mllr_w(mu, var, st, ubm_mu=None, ubm_var=None, ubm_init=False, min_var=1e-6):
+    mu, var = _f32(mu), _f32(var)
+    M, D = mu.shape
+    ubm_mu = mu if ubm_mu is None else _f32(ubm_mu)
+    ubm_var = var if ubm_var is None else _f32(ubm_var)
+    n, F = (np.ascontiguousarray(st[k], np.float64) for k in ("n", "F"))
+    W = np.zeros((D, D + 1))
+    rc = lib().orc_mllr_w(M, D, _p(mu), _p(var), _p(ubm_mu), _p(ubm_var), _p(n), _p(F),
+                          int(ubm_init), C.c_float(min_var), _p(W))
+    if rc:
+        raise RuntimeError(f"orc_mllr_w failed ({rc}): MLLR invertibility conditions not met")
+    return W
+
+
+def mllr_apply(mu, W):
+    mu = _f32(mu)
+    M, D = mu.shape
+    W = np.ascontiguousarray(W, np.float64)
+    out = np.zeros_like(mu)
+    lib().orc_mllr_apply(M, D, _p(mu), _p(W), _p(out))
+    return out
+
+
+# ------------------------------------------------------------------ reference library
+
+def ref_loglikes(X, w, mu, var, threads=1, sse=False):
+    X, w, mu, var = map(_f32, (X, w, mu, var))
+    N, D = X.shape
+    out = np.zeros(N, np.float32)
+    rc = ref().ref_loglikes(_p(X), C.c_long(N), D, len(w), _p(w), _p(mu), _p(var),
+                            threads, int(sse), _p(out))
+    if rc:
+        raise RuntimeError(ref().ref_last_error().decode())
+    return out
+
+
+def ref_accumulate(X, w, mu, var, flags=ACC_MEAN | ACC_VAR, threads=1, sse=False):
+    X, w, mu, var = map(_f32, (X, w, mu, var))
+    N, D = X.shape
+    M = len(w)
+    n, F, S = np.zeros(M), np.zeros((M, D)), np.zeros((M, D))
+    tl, tn = C.c_double(0.0), C.c_uint(0)
+    order = np.zeros(M, np.int32)
+    rc = ref().ref_accumulate(_p(X), C.c_long(N), D, M, _p(w), _p(mu), _p(var), threads,
+                              int(sse), flags, _p(n), _p(F), _p(S), C.byref(tl), C.byref(tn),
+                              _p(order))
+    if rc:
+        raise RuntimeError(ref().ref_last_error().decode())
+    return dict(n=n, F=F, S=S, totLL=tl.value, totN=tn.value, order=order)
+
+
+def ref_em(X, w, mu, var, iters, upW=True, upM=True, upV=True, threads=1, sse=False):
+    X = _f32(X)
+    w, mu, var = _f32(w).copy(), _f32(mu).copy(), _f32(var).copy()
+    N, D = X.shape
+    M = len(w)
+    ll = np.zeros(iters)
+    order = np.zeros(M, np.int32)
+    rc = ref().ref_em(_p(X), C.c_long(N), D, M, _p(w), _p(mu), _p(var), iters, int(upW),
+                      int(upM), int(upV), threads, int(sse), _p(ll), _p(order))
+    if rc:
+        raise RuntimeError(ref().ref_last_error().decode())
+    return w, mu, var, ll
+
+
+def ref_map(X, w, mu, var, tau, iters=1, upW=False, upM=True, upV=False, threads=1, sse=False):
+    X, w, mu, var = map(_f32, (X, w, mu, var))
+    N, D = X.shape
+    M = len(w)
+    ow, omu, ovar = np.zeros_like(w), np.zeros_like(mu), np.zeros_like(var)
+    ll = np.zeros(iters)
+    rc = ref().ref_map(_p(X), C.c_long(N), D, M, _p(w), _p(mu), _p(var), int(tau), iters,
+                       int(upW), int(upM), int(upV), threads, int(sse), _p(ow), _p(omu),
+                       _p(ovar), _p(ll))
+    if rc:
+        raise RuntimeError(ref().ref_last_error().decode())
+    return ow, omu, ovar, ll
+
+
+def ref_mllr(X, w, mu, var, iters=1, ubm_init=False, threads=1, sse=False):
+    X, w, mu, var = map(_f32, (X, w, mu, var))
+    N, D = X.shape
+    M = len(w)
+    W = np.zeros((D, D + 1))
+    omu = np.zeros_like(mu)
+    rc = ref().ref_mllr(_p(X), C.c_long(N), D, M, _p(w), _p(mu), _p(var), iters,
+                        int(ubm_init), threads, int(sse), _p(W), _p(omu))
+    if rc:
+        raise RuntimeError(ref().ref_last_error().decode())
+    return W, omu

@@ -1,0 +1,622 @@
+/*
+ * CPU oracle for the GMM hot path -- TEST INFRASTRUCTURE ONLY (see gmm_oracle.h).
+ * Compiled with -ffp-contract=off so that every float expression rounds exactly as in an
+ * x86-64 build of the reference estimator, on any host.
+ *
+ * Reference anchors (paths inside GMMTeam/GMM/GMM/lib_bmssr):
+ *   model precompute      trainer/OL_GMMStatsEstimator.cpp:234-313 (insertModel)
+ *   component log-like    trainer/OL_GMMStatsEstimator.cpp:563-588 (computeMixLogLike)
+ *   frame log-like        trainer/OL_GMMStatsEstimator.cpp:444-510 (getLikeAndGammas)
+ *   log-add               trainer/OL_GMMStatsEstimator.cpp:1449-1458 (addLog, LPDIF = 15)
+ *   posteriors            trainer/OL_GMMStatsEstimator.cpp:515-558 (compGammas)
+ *   stat accumulation     trainer/OL_GMMStatsEstimator.cpp:1334-1378 (accumulateStats(vec))
+ *   frame loop + totals   trainer/OL_GMMStatsEstimator.cpp:1105-1193 (accumulateStats(batch))
+ *   thread split + merge  trainer/OL_GMMStatsEstimator.cpp:884-971 (accumulateStatsMT),
+ *                         model/OL_GMMStats.cpp:99-145 (operator+=)
+ */
+#include "gmm_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define MINUS_LOG_2PI (-1.837877066409345)
+#define LPDIF 15.0f
+#define MIN_FRAMES_FOR_THREAD 100
+#define MIN_IND_SAMPLES 2.0
+
+int orc_rearrange_order(int M, const float* w, int* order) {
+  int nz = 0, z = 1;
+  for (int m = 0; m < M; ++m) {
+    if (w[m] > 0) order[nz++] = m;
+    else order[M - z++] = m;
+  }
+  return nz;
+}
+
+/* ---------------------------------------------------------------- float port ---------- */
+
+typedef struct {
+  int M, D;
+  const float* w;
+  const float* mu;
+  float* icov;      /* M*D, 1/var */
+  float* logGconst; /* M */
+  float* logW;      /* M */
+  const orc_opts* o;
+} model32;
+
+static int prep32(model32* m, int M, int D, const float* w, const float* mu, const float* var,
+                  const orc_opts* o) {
+  m->M = M;
+  m->D = D;
+  m->w = w;
+  m->mu = mu;
+  m->o = o;
+  m->icov = (float*)malloc(sizeof(float) * (size_t)M * D);
+  m->logGconst = (float*)malloc(sizeof(float) * (size_t)M);
+  m->logW = (float*)malloc(sizeof(float) * (size_t)M);
+  for (int c = 0; c < M; ++c) {
+    float wc = w[c];
+    m->logW[c] = (wc > 0) ? logf(wc) : o->minLogLike;
+    if (!(wc > 0)) { m->logGconst[c] = 0.0f; continue; }
+    float acc = 0.0f;
+    for (int d = 0; d < D; ++d) {
+      float v = var[(size_t)c * D + d];
+      if (v < o->min_var) return 1;
+      m->icov[(size_t)c * D + d] = 1.0f / v;
+      acc += logf(v);
+    }
+    m->logGconst[c] = (float)(MINUS_LOG_2PI * D / 2 - acc / 2);
+  }
+  return 0;
+}
+
+static void free32(model32* m) {
+  free(m->icov);
+  free(m->logGconst);
+  free(m->logW);
+}
+
+static inline void add_log(float* p1, float p2) {
+  if (*p1 - LPDIF > p2) return;
+  if (*p1 > p2) *p1 = *p1 + logf(1.0f + expf(p2 - *p1));
+  else *p1 = p2 + logf(1.0f + expf(*p1 - p2));
+}
+
+static inline float mix_loglike(const model32* m, int c, const float* x) {
+  const float* mean = m->mu + (size_t)c * m->D;
+  const float* ic = m->icov + (size_t)c * m->D;
+  float e = 0.0f;
+  for (int d = 0; d < m->D; ++d) {
+    float diff = x[d] - mean[d];
+    float t = diff * diff;
+    t = t * ic[d];
+    e = e + t;
+  }
+  float ll = m->logGconst[c] - 0.5f * e;
+  if (!isfinite(ll)) return m->o->minLogLike;
+  return ll;
+}
+
+/* getLikeAndGammas: g[c] = unnormalised log posterior; returns frame log-likelihood. */
+static float like_and_gammas(const model32* m, const float* x, float* g, int* trouble) {
+  float minLL = m->o->minLogLike;
+  float maxLL = minLL, sumLL = minLL;
+  for (int c = 0; c < m->M; ++c) {
+    if (!(m->w[c] > 0)) continue;
+    if (m->logW[c] == minLL) { g[c] = minLL; continue; }
+    g[c] = mix_loglike(m, c, x) + m->logW[c];
+    if (maxLL < g[c]) maxLL = g[c];
+    add_log(&sumLL, g[c]);
+  }
+  if (maxLL == minLL) { *trouble = 1; return minLL; }
+  return sumLL;
+}
+
+static int count_active(int M, const float* w) {
+  int k = 0;
+  for (int c = 0; c < M; ++c) k += (w[c] > 0);
+  return k;
+}
+
+/* compGammas */
+static float comp_gammas(const model32* m, const float* x, float* g, int nactive, int* trouble) {
+  float ll = like_and_gammas(m, x, g, trouble);
+  if (nactive == 1) {
+    for (int c = 0; c < m->M; ++c)
+      if (m->w[c] > 0) { g[c] = 1.0f; break; }
+    return ll;
+  }
+  float minLL = m->o->minLogLike;
+  if (ll == minLL) {
+    for (int c = 0; c < m->M; ++c)
+      if (m->w[c] > 0) g[c] = m->o->minGamma;
+  } else {
+    for (int c = 0; c < m->M; ++c) {
+      if (!(m->w[c] > 0)) continue;
+      g[c] = (float)(g[c] > minLL) * expf(g[c] - ll);
+    }
+  }
+  return ll;
+}
+
+typedef struct {
+  const model32* m;
+  const float* X;
+  long long first, count;
+  int flags;
+  double *n, *F, *S;
+  double totLL;
+  long long totN;
+  float* out;
+  int trouble;
+  int nactive;
+} job32;
+
+static void acc_range(job32* j) {
+  const model32* m = j->m;
+  int D = m->D, M = m->M;
+  float* g = (float*)malloc(sizeof(float) * (size_t)(M > 0 ? M : 1));
+  int fm = (j->flags & ORC_ACC_MEAN) != 0, fv = (j->flags & ORC_ACC_VAR) != 0;
+  int probsOnly = (j->flags & ORC_ACC_PROBS_ONLY) != 0;
+  float minGamma = m->o->minGamma;
+  for (long long i = 0; i < j->count; ++i) {
+    const float* x = j->X + (size_t)(j->first + i) * D;
+    float ll = comp_gammas(m, x, g, j->nactive, &j->trouble);
+    j->totLL += (double)ll;
+    for (int c = 0; c < M; ++c) {
+      if (!(m->w[c] > 0)) continue;
+      float gc = g[c];
+      if (gc <= minGamma) continue;
+      j->n[c] += (double)gc;
+      if (probsOnly) continue;
+      for (int k = 0; k < D; ++k) {
+        if (fm) j->F[(size_t)c * D + k] += (double)(gc * x[k]);
+        if (fv) {
+          float t = gc * x[k];
+          t = t * x[k];
+          j->S[(size_t)c * D + k] += (double)t;
+        }
+      }
+    }
+  }
+  j->totN += j->count;
+  free(g);
+}
+
+static void ll_range(job32* j) {
+  const model32* m = j->m;
+  float* g = (float*)malloc(sizeof(float) * (size_t)(m->M > 0 ? m->M : 1));
+  for (long long i = 0; i < j->count; ++i) {
+    const float* x = j->X + (size_t)(j->first + i) * m->D;
+    j->out[j->first + i] = like_and_gammas(m, x, g, &j->trouble);
+  }
+  free(g);
+}
+
+static void* acc_thread(void* p) { acc_range((job32*)p); return NULL; }
+static void* ll_thread(void* p) { ll_range((job32*)p); return NULL; }
+
+/* Split exactly as accumulateStatsMT / compVecsLogLikeMT: T = min(N/100, threads) workers,
+ * N/T frames each, the last takes the remainder. */
+static int split_threads(long long N, int threads) {
+  long long t = N / MIN_FRAMES_FOR_THREAD;
+  if (t > threads) t = threads;
+  return (int)t;
+}
+
+int orc32_loglikes(const float* X, long long N, int D, int M, const float* w, const float* mu,
+                   const float* var, const orc_opts* o, float* out, int* stability_trouble) {
+  if (N < 0 || D <= 0 || M <= 0) return 2;
+  model32 m;
+  int rc = prep32(&m, M, D, w, mu, var, o);
+  if (rc) { free32(&m); return rc; }
+  int T = split_threads(N, o->threads);
+  int trouble = 0;
+  if (T < 2) {
+    job32 j = {&m, X, 0, N, 0, 0, 0, 0, 0.0, 0, out, 0, 0};
+    ll_range(&j);
+    trouble = j.trouble;
+  } else {
+    job32* jobs = (job32*)calloc((size_t)T, sizeof(job32));
+    pthread_t* th = (pthread_t*)calloc((size_t)T, sizeof(pthread_t));
+    long long part = N / T, shift = 0;
+    for (int t = 0; t < T; ++t) {
+      long long cnt = (t + 1 == T) ? N - shift : part;
+      job32 j = {&m, X, shift, cnt, 0, 0, 0, 0, 0.0, 0, out, 0, 0};
+      jobs[t] = j;
+      shift += cnt;
+      pthread_create(&th[t], NULL, ll_thread, &jobs[t]);
+    }
+    for (int t = 0; t < T; ++t) { pthread_join(th[t], NULL); trouble |= jobs[t].trouble; }
+    free(jobs);
+    free(th);
+  }
+  if (stability_trouble) *stability_trouble = trouble;
+  free32(&m);
+  return 0;
+}
+
+int orc32_accumulate(const float* X, long long N, int D, int M, const float* w, const float* mu,
+                     const float* var, const orc_opts* o, int flags, double* n, double* F,
+                     double* S, double* totLL, long long* totN) {
+  if (N < 0 || D <= 0 || M <= 0) return 2;
+  model32 m;
+  int rc = prep32(&m, M, D, w, mu, var, o);
+  if (rc) { free32(&m); return rc; }
+  int nactive = count_active(M, w);
+  size_t MD = (size_t)M * D;
+  int T = split_threads(N, o->threads);
+  if (T < 2) {
+    job32 j = {&m, X, 0, N, flags, n, F, S, *totLL, *totN, NULL, 0, nactive};
+    acc_range(&j);
+    *totLL = j.totLL;
+    *totN = j.totN;
+  } else {
+    job32* jobs = (job32*)calloc((size_t)T, sizeof(job32));
+    pthread_t* th = (pthread_t*)calloc((size_t)T, sizeof(pthread_t));
+    long long part = N / T, shift = 0;
+    for (int t = 0; t < T; ++t) {
+      long long cnt = (t + 1 == T) ? N - shift : part;
+      job32 j = {&m, X, shift, cnt, flags, n, F, S, *totLL, *totN, NULL, 0, nactive};
+      if (t > 0) {
+        j.n = (double*)calloc((size_t)M, sizeof(double));
+        j.F = (double*)calloc(MD, sizeof(double));
+        j.S = (double*)calloc(MD, sizeof(double));
+        j.totLL = 0.0;
+        j.totN = 0;
+      }
+      jobs[t] = j;
+      shift += cnt;
+      pthread_create(&th[t], NULL, acc_thread, &jobs[t]);
+    }
+    pthread_join(th[0], NULL);
+    int fm = (flags & (ORC_ACC_MEAN | ORC_ACC_VAR)) != 0, fv = (flags & ORC_ACC_VAR) != 0;
+    /* GMMStats::operator+= in thread order: per component mixProb, then per dim mean, var */
+    for (int t = 1; t < T; ++t) {
+      pthread_join(th[t], NULL);
+      for (int c = 0; c < M; ++c) {
+        n[c] += jobs[t].n[c];
+        for (int k = 0; k < D; ++k) {
+          if (fm) F[(size_t)c * D + k] += jobs[t].F[(size_t)c * D + k];
+          if (fv) S[(size_t)c * D + k] += jobs[t].S[(size_t)c * D + k];
+        }
+      }
+      jobs[0].totN += jobs[t].totN;
+      jobs[0].totLL += jobs[t].totLL;
+      free(jobs[t].n);
+      free(jobs[t].F);
+      free(jobs[t].S);
+    }
+    *totLL = jobs[0].totLL;
+    *totN = jobs[0].totN;
+    free(jobs);
+    free(th);
+  }
+  free32(&m);
+  return 0;
+}
+
+/* ---------------------------------------------------------------- FP64 oracle --------- */
+
+typedef struct {
+  int M, D;
+  const float* w;
+  const float* mu;
+  const float* var;
+  double* logc; /* log w - D/2 log 2pi - 1/2 sum log var */
+} model64;
+
+static int prep64(model64* m, int M, int D, const float* w, const float* mu, const float* var,
+                  const orc_opts* o) {
+  m->M = M; m->D = D; m->w = w; m->mu = mu; m->var = var;
+  m->logc = (double*)malloc(sizeof(double) * (size_t)M);
+  for (int c = 0; c < M; ++c) {
+    if (!(w[c] > 0)) { m->logc[c] = 0; continue; }
+    double s = 0;
+    for (int d = 0; d < D; ++d) {
+      double v = var[(size_t)c * D + d];
+      if (v < o->min_var) return 1;
+      s += log(v);
+    }
+    m->logc[c] = log((double)w[c]) + MINUS_LOG_2PI * D / 2.0 - 0.5 * s;
+  }
+  return 0;
+}
+
+/* returns frame LL (or -inf if no active component); g[c] = log joint, -inf for skipped */
+static double frame64(const model64* m, const float* x, double* g) {
+  double mx = -INFINITY;
+  for (int c = 0; c < m->M; ++c) {
+    if (!(m->w[c] > 0)) { g[c] = -INFINITY; continue; }
+    const float* mean = m->mu + (size_t)c * m->D;
+    const float* v = m->var + (size_t)c * m->D;
+    double e = 0;
+    for (int d = 0; d < m->D; ++d) {
+      double diff = (double)x[d] - (double)mean[d];
+      e += diff * diff / (double)v[d];
+    }
+    g[c] = m->logc[c] - 0.5 * e;
+    if (g[c] > mx) mx = g[c];
+  }
+  if (mx == -INFINITY) return mx;
+  double s = 0;
+  for (int c = 0; c < m->M; ++c)
+    if (g[c] > -INFINITY) s += exp(g[c] - mx);
+  return mx + log(s);
+}
+
+int orc64_loglikes(const float* X, long long N, int D, int M, const float* w, const float* mu,
+                   const float* var, const orc_opts* o, double* out) {
+  model64 m;
+  int rc = prep64(&m, M, D, w, mu, var, o);
+  if (rc) { free(m.logc); return rc; }
+  double* g = (double*)malloc(sizeof(double) * (size_t)M);
+  for (long long i = 0; i < N; ++i) out[i] = frame64(&m, X + (size_t)i * D, g);
+  free(g);
+  free(m.logc);
+  return 0;
+}
+
+int orc64_accumulate(const float* X, long long N, int D, int M, const float* w, const float* mu,
+                     const float* var, const orc_opts* o, int flags, double* n, double* F,
+                     double* S, double* totLL, long long* totN) {
+  model64 m;
+  int rc = prep64(&m, M, D, w, mu, var, o);
+  if (rc) { free(m.logc); return rc; }
+  int nactive = count_active(M, w);
+  double* g = (double*)malloc(sizeof(double) * (size_t)M);
+  int fm = (flags & ORC_ACC_MEAN) != 0, fv = (flags & ORC_ACC_VAR) != 0;
+  int probsOnly = (flags & ORC_ACC_PROBS_ONLY) != 0;
+  double tl = *totLL;
+  for (long long i = 0; i < N; ++i) {
+    const float* x = X + (size_t)i * D;
+    double ll = frame64(&m, x, g);
+    if (ll == -INFINITY) { tl += (double)o->minLogLike; continue; }
+    tl += ll;
+    for (int c = 0; c < M; ++c) {
+      if (!(w[c] > 0)) continue;
+      double gc = (nactive == 1) ? 1.0 : exp(g[c] - ll);
+      if (gc <= (double)o->minGamma) continue;
+      n[c] += gc;
+      if (probsOnly) continue;
+      for (int k = 0; k < D; ++k) {
+        double xv = x[k];
+        if (fm) F[(size_t)c * D + k] += gc * xv;
+        if (fv) S[(size_t)c * D + k] += gc * xv * xv;
+      }
+    }
+  }
+  *totLL = tl;
+  *totN += N;
+  free(g);
+  free(m.logc);
+  return 0;
+}
+
+/* ---------------------------------------------------------------- M-step ------------- */
+
+static float reset_var_value(void) {
+  /* GMMMixture::Reset (OL_GMModel.cpp:73-83) fills diagonal variances with memset(.., 1, ..):
+   * every byte 0x01. */
+  unsigned int bits = 0x01010101u;
+  float f;
+  memcpy(&f, &bits, sizeof f);
+  return f;
+}
+
+int orc_em_update(int M, int D, float* w, float* mu, float* var, const double* n,
+                  const double* F, const double* S, long long totN, int upW, int upM, int upV,
+                  float min_var) {
+  int changed = 0, nzero = 0;
+  double corr = 0.0;
+  float* mean = (float*)malloc(sizeof(float) * (size_t)D);
+  float rv = reset_var_value();
+  unsigned int tot = (unsigned int)totN; /* GMMStats::_totalAccSamples is unsigned int */
+  for (int j = 0; j < M; ++j) {
+    if (w[j] == 0.0f) { ++nzero; continue; }
+    double mp = n[j];
+    if (mp < MIN_IND_SAMPLES) {
+      for (int k = 0; k < D; ++k) { mu[(size_t)j * D + k] = 0.0f; var[(size_t)j * D + k] = rv; }
+      w[j] = 0.0f;
+      changed = 1;
+      continue;
+    }
+    if (upW) {
+      w[j] = (float)(mp / tot);
+      changed = 1;
+    }
+    corr += w[j];
+    if (upM || upV) {
+      for (int k = 0; k < D; ++k) mean[k] = (float)(F[(size_t)j * D + k] / mp);
+      if (upV) {
+        for (int k = 0; k < D; ++k) {
+          float v = (float)(S[(size_t)j * D + k] / mp - pow((double)mean[k], 2));
+          if (v < min_var) v = min_var;
+          var[(size_t)j * D + k] = v;
+        }
+      }
+      if (upM) memcpy(mu + (size_t)j * D, mean, sizeof(float) * (size_t)D);
+    }
+  }
+  if (changed && corr > 0.0)
+    for (int j = 0; j < M; ++j) w[j] = (float)(w[j] / corr);
+  free(mean);
+  return M - nzero;
+}
+
+int orc64_em_update(int M, int D, const float* w, const double* n, const double* F,
+                    const double* S, long long totN, int upW, int upM, int upV, double min_var,
+                    double* ow, double* omu, double* ovar) {
+  int nzero = 0;
+  double corr = 0.0;
+  for (int j = 0; j < M; ++j) {
+    ow[j] = w[j];
+    if (w[j] == 0.0f) { ++nzero; continue; }
+    double mp = n[j];
+    if (mp < MIN_IND_SAMPLES) { ow[j] = 0.0; continue; }
+    if (upW) ow[j] = mp / (double)totN;
+    corr += ow[j];
+    for (int k = 0; k < D; ++k) {
+      double mk = F[(size_t)j * D + k] / mp;
+      if (upM) omu[(size_t)j * D + k] = mk;
+      if (upV) {
+        double v = S[(size_t)j * D + k] / mp - mk * mk;
+        ovar[(size_t)j * D + k] = v < min_var ? min_var : v;
+      }
+    }
+  }
+  if (corr > 0.0)
+    for (int j = 0; j < M; ++j) ow[j] /= corr;
+  return M - nzero;
+}
+
+void orc_map_update(int M, int D, float* w, float* mu, float* var, const float* ubm_w,
+                    const float* ubm_mu, const float* ubm_var, const double* n, const double* F,
+                    const double* S, long long totN, int tau, int upW, int upM, int upV,
+                    float min_var) {
+  double corr = 0.0;
+  unsigned int tot = (unsigned int)totN;
+  float* am = (float*)malloc(sizeof(float) * (size_t)D);
+  float* av = (float*)malloc(sizeof(float) * (size_t)D);
+  for (int j = 0; j < M; ++j) {
+    if (ubm_w[j] == 0) continue;
+    double mp = n[j];
+    if (!(mp > 0.0f)) continue;
+    const float* um = ubm_mu + (size_t)j * D;
+    const float* uv = ubm_var + (size_t)j * D;
+    double alfa = mp / (mp + tau);
+    if (upW && tot > 0) {
+      float aw = (float)(alfa * (mp / tot) + (1 - alfa) * ubm_w[j]);
+      w[j] = aw;
+      corr += aw;
+    }
+    if (upM || upV) {
+      for (int k = 0; k < D; ++k)
+        am[k] = (float)(alfa * F[(size_t)j * D + k] / mp + (1 - alfa) * um[k]);
+      if (upV) {
+        for (int k = 0; k < D; ++k) {
+          float second = uv[k] + um[k] * um[k];
+          float msq = am[k] * am[k];
+          av[k] = (float)(alfa * S[(size_t)j * D + k] / mp + (1 - alfa) * second - msq);
+          if (av[k] < min_var) av[k] = min_var;
+        }
+      }
+      memcpy(mu + (size_t)j * D, am, sizeof(float) * (size_t)D);
+      if (upV) memcpy(var + (size_t)j * D, av, sizeof(float) * (size_t)D);
+    }
+  }
+  if (upW && corr != 0) {
+    float fc = (float)corr;
+    for (int j = 0; j < M; ++j) w[j] = w[j] / fc;
+  }
+  free(am);
+  free(av);
+}
+
+void orc_gj_invert(int n, double* a) {
+  for (int k = 0; k < n; ++k) {
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j)
+        if (i != k && j != k) a[i * n + j] -= a[k * n + j] * a[i * n + k] / a[k * n + k];
+    for (int j = 0; j < n; ++j)
+      if (j != k) a[k * n + j] = -a[k * n + j] / a[k * n + k];
+    for (int i = 0; i < n; ++i)
+      if (i != k) a[i * n + k] = a[i * n + k] / a[k * n + k];
+    a[k * n + k] = 1.0 / a[k * n + k];
+  }
+}
+
+int orc_mllr_w(int M, int D, const float* mu, const float* var, const float* ubm_mu,
+               const float* ubm_var, const double* n, const double* F, int ubm_init,
+               float min_var, double* W) {
+  int E = D + 1;
+  if (M < E) return 3;
+  int active = 0;
+  double occ = 0.0;
+  for (int m = 0; m < M; ++m)
+    if (n[m] > 0) { ++active; occ += n[m]; }
+  if (active < E) return 3;
+  if (occ * D < (double)D * E) return 3;
+  double* G = (double*)malloc(sizeof(double) * (size_t)E * E);
+  double* k = (double*)malloc(sizeof(double) * (size_t)E);
+  double* G0 = NULL;
+  double* k0 = NULL;
+  if (ubm_init) {
+    /* prepareKiGiInitMatrices: per row i, prior terms from every UBM component */
+    G0 = (double*)calloc((size_t)D * E * E, sizeof(double));
+    k0 = (double*)calloc((size_t)D * E, sizeof(double));
+    for (int m = 0; m < M; ++m) {
+      const float* v = ubm_var + (size_t)m * D;
+      const float* me = ubm_mu + (size_t)m * D;
+      for (int r = 0; r < D; ++r) {
+        double cG = (v[r] < min_var) ? (double)(1 / min_var) : (double)(1 / v[r]);
+        double ck = me[r] * cG;
+        double* Gr = G0 + (size_t)r * E * E;
+        double* kr = k0 + (size_t)r * E;
+        for (int d = 0; d < D; ++d) {
+          kr[d] += ck * me[d];
+          Gr[D * E + d] += cG * me[d];
+          Gr[d * E + D] += cG * me[d];
+          for (int dd = 0; dd < D; ++dd) Gr[d * E + dd] += cG * me[d] * me[dd];
+          Gr[d * E + d] += cG * v[d];
+        }
+        Gr[E * E - 1] += cG;
+        kr[D] += ck;
+      }
+    }
+  }
+  for (int i = 0; i < D; ++i) {
+    if (ubm_init) {
+      memcpy(G, G0 + (size_t)i * E * E, sizeof(double) * (size_t)E * E);
+      memcpy(k, k0 + (size_t)i * E, sizeof(double) * (size_t)E);
+    } else {
+      memset(G, 0, sizeof(double) * (size_t)E * E);
+      memset(k, 0, sizeof(double) * (size_t)E);
+    }
+    for (int m = 0; m < M; ++m) {
+      double mp = n[m];
+      if (!(mp > 0)) continue;
+      const float* mv = var + (size_t)m * D;
+      const float* mm = mu + (size_t)m * D;
+      double cm = F[(size_t)m * D + i] / mv[i];
+      double cv = mp / mv[i];
+      for (int a = 0; a < D; ++a) {
+        k[a] += cm * mm[a];
+        for (int b = a; b < D; ++b) {
+          G[a * E + b] += cv * mm[a] * mm[b];
+          G[b * E + a] = G[a * E + b];
+        }
+        G[a * E + D] += cv * mm[a];
+        G[D * E + a] = G[a * E + D];
+      }
+      k[D] += cm;
+      G[D * E + D] += cv;
+    }
+    orc_gj_invert(E, G);
+    for (int a = 0; a < E; ++a) {
+      double s = 0.0;
+      for (int b = 0; b < E; ++b) s += G[a * E + b] * k[b];
+      W[(size_t)i * E + a] = s;
+    }
+  }
+  free(G);
+  free(k);
+  free(G0);
+  free(k0);
+  return 0;
+}
+
+void orc_mllr_apply(int M, int D, const float* mu, const double* W, float* omu) {
+  int E = D + 1;
+  for (int m = 0; m < M; ++m) {
+    const float* x = mu + (size_t)m * D;
+    for (int k = 0; k < D; ++k) {
+      double v = 0.0;
+      for (int kk = 0; kk < D; ++kk) v += W[(size_t)k * E + kk] * x[kk];
+      omu[(size_t)m * D + k] = (float)(v + W[(size_t)k * E + D]);
+    }
+  }
+}

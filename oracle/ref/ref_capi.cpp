@@ -1,0 +1,262 @@
+// Test-only C entry points around the reference's own CPU estimator and re-estimation
+// driver, compiled unmodified from the reference sources (GMM/lib_bmssr) by oracle/Makefile.
+// The resulting oracle/_ref/libgmmref.so is a checker used by tests and by the fixture
+// generator in tests/golden; nothing in the product links or loads it.
+//
+// The reference classes keep the routines the tests need (UpdateModelEM, IterEM, IterMAP,
+// IterW_MLLR, the _stats member) protected or private, so this translation unit opens
+// them up with the preprocessor before including the headers. No reference code is
+// changed; the calls below go through the same member functions trainGMM uses:
+//   - E-step:   GMMStatsEstimator{,_SSE}<double>::accumulateStatsMT
+//               (lib_bmssr/trainer/OL_GMMStatsEstimator.cpp:884-971)
+//   - scoring:  compVecsLogLikeMT (OL_GMMStatsEstimator.cpp:811-879)
+//   - EM loop:  CModelAdapt::IterEM / UpdateModelEM (OL_ModelAdapt.cpp:1276-1296, 823-949)
+//   - MAP loop: CModelAdapt::IterMAP / UpdateModelMAP (OL_ModelAdapt.cpp:1298-1317, 993-1106)
+//   - MLLR:     CModelAdapt::IterW_MLLR / AdaptModelMLLR (OL_ModelAdapt.cpp:1365-1415, 1583-1612)
+#include <cstring>
+#include <cstdio>
+#include <vector>
+#include <string>
+#include <stdexcept>
+// Standard headers first, so the access override below only reaches the reference classes.
+#include <sstream>
+#include <fstream>
+#include <iostream>
+#include <iomanip>
+#include <list>
+#include <map>
+#include <new>
+#include <limits>
+#include <thread>
+#include <mutex>
+#include <functional>
+#include <ext/hash_map>
+#include <hash_map>
+#include <boost/thread.hpp>
+#include <boost/program_options.hpp>
+
+#define private public
+#define protected public
+#include "general/my_inttypes.h"
+#include "general/Exception.h"
+#include "trainer/OL_ModelAdapt.h"
+#include "trainer/OL_GMMStatsEstimator_SSE.h"
+#undef private
+#undef protected
+
+namespace {
+
+// Builds a diagonal GMModel from flat arrays (w[M], mu[M*D], var[M*D]).
+GMModel* make_model(int M, int D, const float* w, const float* mu, const float* var) {
+  GMModel* g = new GMModel(D, M, false);
+  for (int m = 0; m < M; ++m)
+    g->SetMixParam(m, const_cast<float*>(mu + (size_t)m * D), const_cast<float*>(var + (size_t)m * D), w[m]);
+  return g;
+}
+
+void read_model(GMModel* g, int M, int D, float* w, float* mu, float* var) {
+  for (int m = 0; m < M; ++m) {
+    w[m] = g->GetMixtureWeight(m);
+    memcpy(mu + (size_t)m * D, g->GetMixtureMean(m), sizeof(float) * D);
+    memcpy(var + (size_t)m * D, g->GetMixtureVar(m), sizeof(float) * D);
+  }
+}
+
+std::vector<float*> rows(const float* X, long N, int D) {
+  std::vector<float*> r((size_t)N);
+  for (long i = 0; i < N; ++i) r[(size_t)i] = const_cast<float*>(X + (size_t)i * D);
+  return r;
+}
+
+GMMStatsEstimator<double>* make_estimator(int sse, int threads) {
+  GMMStatsEstimator<double>* e;
+  if (sse) e = new GMMStatsEstimator_SSE<double>;
+  else e = new GMMStatsEstimator<double>;
+  e->_numThreads = threads;
+  e->_verbosity = 0;
+  return e;
+}
+
+thread_local std::string g_err;
+
+void fill_param(Param& p, const float* X, long N, int D) {
+  std::vector<float*> r = rows(X, N, D);
+  std::vector<float> cf((size_t)N, 1.0f);
+  p.ExportInternal<float>(r.data(), (unsigned)N, (unsigned)D, cf.data());
+}
+
+CModelAdapt::OPTIONS base_options(int threads, int sse) {
+  CModelAdapt::OPTIONS opt;
+  opt._numThreads = threads;
+  opt._SSEacc = sse != 0;
+  opt._verbosity = 0;
+  opt._saveMixOcc = false;
+  opt._delMix = 0.0f;
+  return opt;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* ref_last_error() { return g_err.c_str(); }
+
+// Per-frame log-likelihoods (a11). Returns 0 on success.
+int ref_loglikes(const float* X, long N, int D, int M, const float* w, const float* mu,
+                 const float* var, int threads, int sse, float* out) {
+  try {
+    GMModel* g = make_model(M, D, w, mu, var);
+    GMMStatsEstimator<double>* e = make_estimator(sse, threads);
+    e->insertModel(*g);
+    std::vector<float*> r = rows(X, N, D);
+    e->compVecsLogLikeMT(r.data(), (unsigned)N, (unsigned)D, out);
+    delete e;
+    delete g;
+    return 0;
+  } catch (std::exception& ex) { g_err = ex.what(); return 1; }
+}
+
+// One E-step (a2-a6). flags: bit0 mean stats, bit1 var stats, bit2 occupancies only.
+// order[k] receives the original index of the component stored at position k after
+// GMModel::RearrangeMixtures; the statistics are returned in that (rearranged) order.
+int ref_accumulate(const float* X, long N, int D, int M, const float* w, const float* mu,
+                   const float* var, int threads, int sse, int flags, double* n, double* F,
+                   double* S, double* totLL, unsigned* totSamples, int* order) {
+  try {
+    std::vector<float> wtag(w, w + M);
+    GMModel* g = make_model(M, D, w, mu, var);
+    // Tag each component with its original index through its first mean coordinate copy.
+    std::vector<float*> before((size_t)M);
+    for (int m = 0; m < M; ++m) before[(size_t)m] = g->GetMixtureMean(m);
+    GMMStatsEstimator<double>* e = make_estimator(sse, threads);
+    e->insertModel(*g);
+    for (int k = 0; k < M; ++k) {
+      order[k] = -1;
+      for (int m = 0; m < M; ++m)
+        if (g->GetMixtureMean(k) == before[(size_t)m]) order[k] = m;
+    }
+    bool probsOnly = (flags & 4) != 0;
+    bool fm = (flags & 1) != 0, fv = (flags & 2) != 0;
+    GMMStats<double> st(D, M, fm || fv, fv, false, false);
+    st.reset();
+    e->setAccFlags(probsOnly, fm, fv, false, false);
+    std::vector<float*> r = rows(X, N, D);
+    e->accumulateStatsMT(r.data(), (unsigned)N, (unsigned)D, st);
+    for (int m = 0; m < M; ++m) {
+      n[m] = st.getProb(m);
+      for (int d = 0; d < D; ++d) {
+        if (F) F[(size_t)m * D + d] = (fm || fv) ? st.getMean(m)[d] : 0.0;
+        if (S) S[(size_t)m * D + d] = fv ? st.getVar(m)[d] : 0.0;
+      }
+    }
+    *totLL = st.getTotLogLike();
+    *totSamples = st.getTotAccSamples();
+    delete e;
+    delete g;
+    return 0;
+  } catch (std::exception& ex) { g_err = ex.what(); return 1; }
+}
+
+// `iters` EM iterations through CModelAdapt::IterEM (tau = 0 MAP-type driver, which is the
+// trainGMM --type 2 --tau 0 route). Model arrays are updated in place (component order after
+// the reference's rearrangement). ll[i] = total log-likelihood accumulated in iteration i.
+int ref_em(const float* X, long N, int D, int M, float* w, float* mu, float* var, int iters,
+           int upW, int upM, int upV, int threads, int sse, double* ll, int* order) {
+  try {
+    GMModel* ubm = make_model(M, D, w, mu, var);
+    std::vector<float*> before((size_t)M);
+    for (int m = 0; m < M; ++m) before[(size_t)m] = ubm->GetMixtureMean(m);
+    CModelAdapt cm;
+    CModelAdapt::OPTIONS opt = base_options(threads, sse);
+    opt._adaptType = MAP;
+    opt._tau = 0;
+    opt._iterCountEM = iters;
+    opt._iterCountMAP = 0;
+    opt._AdaptWeightBool = upW != 0;
+    opt._AdaptMeanBool = upM != 0;
+    opt._AdaptVarBool = upV != 0;
+    cm.SetOptions(opt);
+    Param p;
+    fill_param(p, X, N, D);
+    cm.InsertData(p, false);
+    cm.Initialize(ubm);
+    GMModel* model = new GMModel(ubm);
+    for (int it = 0; it < iters; ++it) {
+      cm.IterEM(model, 1);
+      ll[it] = cm._stats.getTotLogLike();
+    }
+    // the estimator rearranged `model` in place; report the permutation relative to input
+    for (int k = 0; k < M; ++k) order[k] = k;
+    read_model(model, M, D, w, mu, var);
+    delete model;
+    delete ubm;
+    return 0;
+  } catch (std::exception& ex) { g_err = ex.what(); return 1; }
+  catch (Exception* ex) { g_err = ex->m_strDescription; delete ex; return 2; }
+}
+
+// MAP adaptation through CModelAdapt::IterMAP with relevance factor tau (a9).
+int ref_map(const float* X, long N, int D, int M, const float* w, const float* mu, const float* var,
+            int tau, int iters, int upW, int upM, int upV, int threads, int sse, float* ow,
+            float* omu, float* ovar, double* ll) {
+  try {
+    GMModel* ubm = make_model(M, D, w, mu, var);
+    CModelAdapt cm;
+    CModelAdapt::OPTIONS opt = base_options(threads, sse);
+    opt._adaptType = MAP;
+    opt._tau = tau;
+    opt._iterCountEM = 0;
+    opt._iterCountMAP = iters;
+    opt._AdaptWeightBool = upW != 0;
+    opt._AdaptMeanBool = upM != 0;
+    opt._AdaptVarBool = upV != 0;
+    cm.SetOptions(opt);
+    Param p;
+    fill_param(p, X, N, D);
+    cm.InsertData(p, false);
+    cm.Initialize(ubm);
+    GMModel* model = new GMModel(ubm);
+    for (int it = 0; it < iters; ++it) {
+      cm.IterMAP(model, 1);
+      if (ll) ll[it] = cm._stats.getTotLogLike();
+    }
+    read_model(model, M, D, ow, omu, ovar);
+    delete model;
+    delete ubm;
+    return 0;
+  } catch (std::exception& ex) { g_err = ex.what(); return 1; }
+  catch (Exception* ex) { g_err = ex->m_strDescription; delete ex; return 2; }
+}
+
+// Global MLLR mean transform (a10): W is D x (D+1) row-major; omu receives A*mu+b.
+int ref_mllr(const float* X, long N, int D, int M, const float* w, const float* mu, const float* var,
+             int iters, int ubm_init, int threads, int sse, double* W, float* omu) {
+  try {
+    GMModel* ubm = make_model(M, D, w, mu, var);
+    CModelAdapt cm;
+    CModelAdapt::OPTIONS opt = base_options(threads, sse);
+    opt._adaptType = MLLR;
+    opt._iterMLLR = iters;
+    opt._mllrUBMInit = ubm_init != 0;
+    opt._applyTransforms = true;
+    cm.SetOptions(opt);
+    Param p;
+    fill_param(p, X, N, D);
+    cm.InsertData(p, false);
+    cm.Initialize(ubm);
+    cm._UBM = ubm;
+    MATRIX* Wm = cm.IterW_MLLR(ubm, iters, NULL);
+    for (int i = 0; i < D; ++i)
+      for (int j = 0; j <= D; ++j) W[(size_t)i * (D + 1) + j] = Wm->GetXY(i, j);
+    GMModel* ad = cm.AdaptModelMLLR(ubm, Wm);
+    for (int m = 0; m < M; ++m) memcpy(omu + (size_t)m * D, ad->GetMixtureMean(m), sizeof(float) * D);
+    delete ad;
+    Wm->Delete();
+    delete Wm;
+    delete ubm;
+    return 0;
+  } catch (std::exception& ex) { g_err = ex.what(); return 1; }
+  catch (Exception* ex) { g_err = ex->m_strDescription; delete ex; return 2; }
+}
+
+}  // extern "C"
