@@ -1,0 +1,238 @@
+"""ctypes binding of the C ABI in include/gmm_gb300.h.
+
+The shared library is built in-tree by ``gmm_gb300.build`` (``gmm_gb300/_build``). If it is
+missing, importing this module raises: there is no CPU fallback for any entry point.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libgmm_gb300.so")
+
+OK, ERR_ARG, ERR_CUDA, ERR_STATE, ERR_MODEL, ERR_NOMEM, ERR_UNSUPPORTED, ERR_MLLR, ERR_TIMEOUT = range(9)
+PREC_FP32, PREC_TC = 0, 1
+ACC_MEAN, ACC_VAR, ACC_PROBS_ONLY = 1, 2, 4
+
+# Every symbol the header declares, with (restype, argtypes).
+_vp, _i, _ll, _f, _d, _sz = C.c_void_p, C.c_int, C.c_longlong, C.c_float, C.c_double, C.c_size_t
+SIGNATURES = {
+    "gmm_create": (_i, [_i, C.POINTER(_vp)]),
+    "gmm_destroy": (_i, [_vp]),
+    "gmm_last_error": (C.c_char_p, [_vp]),
+    "gmm_set_options": (_i, [_vp, _f, _f, _f]),
+    "gmm_set_precision": (_i, [_vp, _i]),
+    "gmm_set_memory_budget": (_i, [_vp, _sz]),
+    "gmm_get_stream": (_i, [_vp, C.POINTER(_vp)]),
+    "gmm_upload_model": (_i, [_vp, _i, _i, _vp, _vp, _vp]),
+    "gmm_set_prior": (_i, [_vp, _vp, _vp, _vp]),
+    "gmm_read_model": (_i, [_vp, _vp, _vp, _vp]),
+    "gmm_upload_features": (_i, [_vp, _vp, _ll, _i]),
+    "gmm_upload_features_device": (_i, [_vp, _vp, _ll, _i]),
+    "gmm_accumulate": (_i, [_vp, _i, _vp, _vp, _vp, C.POINTER(_d), C.POINTER(_ll)]),
+    "gmm_accumulate_device": (_i, [_vp, _i]),
+    "gmm_read_stats": (_i, [_vp, _vp, _vp, _vp, C.POINTER(_d), C.POINTER(_ll)]),
+    "gmm_loglikes": (_i, [_vp, _vp]),
+    "gmm_em_update": (_i, [_vp, _i, _i, _i, C.POINTER(_i)]),
+    "gmm_map_update": (_i, [_vp, _i, _i, _i, _i]),
+    "gmm_em_iterate": (_i, [_vp, _i, _i, _i, _i, _vp, C.POINTER(_i)]),
+    "gmm_mllr_estimate": (_i, [_vp, _i, _vp]),
+    "gmm_mllr_apply": (_i, [_vp, _vp]),
+    "gmm_profile_enable": (_i, [_vp, _i]),
+    "gmm_profile_reset": (_i, [_vp]),
+    "gmm_profile_read": (_i, [_vp, _i, C.POINTER(C.c_char_p), _vp, _vp]),
+    "gmm_launch_count": (_ll, [_vp]),
+}
+
+_lib = None
+
+
+def load():
+    """Load the library (once). Raises if it was not built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(
+                f"gmm_gb300 CUDA library not found at {LIB_PATH}; build it with "
+                "`python -m gmm_gb300.build` (there is no CPU fallback)")
+        lib = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+class GMMError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"[gmm status {code}] {msg}")
+        self.code = code
+
+
+def ptr(a):
+    if a is None:
+        return None
+    if isinstance(a, int):
+        return a
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    return a.ctypes.data
+
+
+class Handle:
+    """One engine handle (one stream on one device)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        h = C.c_void_p()
+        rc = self.lib.gmm_create(device, C.byref(h))
+        if rc:
+            raise GMMError(rc, self.lib.gmm_last_error(None).decode())
+        self.h = h
+        self.M = self.D = 0
+        self.N = 0
+
+    def check(self, rc):
+        if rc:
+            raise GMMError(rc, self.lib.gmm_last_error(self.h).decode())
+        return rc
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.gmm_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- configuration
+    def set_options(self, min_loglike=-1e20, min_gamma=1e-4, min_var=1e-6):
+        self.check(self.lib.gmm_set_options(self.h, min_loglike, min_gamma, min_var))
+
+    def set_precision(self, mode):
+        self.check(self.lib.gmm_set_precision(self.h, mode))
+
+    def set_memory_budget(self, nbytes):
+        self.check(self.lib.gmm_set_memory_budget(self.h, nbytes))
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        self.check(self.lib.gmm_get_stream(self.h, C.byref(s)))
+        return s.value or 0
+
+    # -- model / features
+    def upload_model(self, w, mu, var):
+        w = np.ascontiguousarray(w, np.float32)
+        mu = np.ascontiguousarray(mu, np.float32)
+        var = np.ascontiguousarray(var, np.float32)
+        M, D = mu.shape
+        self.check(self.lib.gmm_upload_model(self.h, M, D, ptr(w), ptr(mu), ptr(var)))
+        self.M, self.D = M, D
+
+    def set_prior(self, w=None, mu=None, var=None):
+        if w is None:
+            self.check(self.lib.gmm_set_prior(self.h, None, None, None))
+            return
+        w = np.ascontiguousarray(w, np.float32)
+        mu = np.ascontiguousarray(mu, np.float32)
+        var = np.ascontiguousarray(var, np.float32)
+        self.check(self.lib.gmm_set_prior(self.h, ptr(w), ptr(mu), ptr(var)))
+
+    def read_model(self):
+        w = np.zeros(self.M, np.float32)
+        mu = np.zeros((self.M, self.D), np.float32)
+        var = np.zeros((self.M, self.D), np.float32)
+        self.check(self.lib.gmm_read_model(self.h, ptr(w), ptr(mu), ptr(var)))
+        return w, mu, var
+
+    def upload_features(self, X):
+        X = np.ascontiguousarray(X, np.float32)
+        N, D = X.shape
+        self.check(self.lib.gmm_upload_features(self.h, ptr(X), N, D))
+        self.N, self.D = N, D
+
+    def upload_features_device(self, dptr: int, N: int, D: int):
+        self.check(self.lib.gmm_upload_features_device(self.h, dptr, N, D))
+        self.N, self.D = N, D
+
+    # -- E-step
+    def accumulate(self, flags=ACC_MEAN | ACC_VAR):
+        n = np.zeros(self.M)
+        F = np.zeros((self.M, self.D))
+        S = np.zeros((self.M, self.D))
+        tl, tn = C.c_double(), C.c_longlong()
+        self.check(self.lib.gmm_accumulate(self.h, flags, ptr(n), ptr(F), ptr(S),
+                                           C.byref(tl), C.byref(tn)))
+        return dict(n=n, F=F, S=S, totLL=tl.value, totN=tn.value)
+
+    def accumulate_device(self, flags=ACC_MEAN | ACC_VAR):
+        self.check(self.lib.gmm_accumulate_device(self.h, flags))
+
+    def read_stats(self):
+        n = np.zeros(self.M)
+        F = np.zeros((self.M, self.D))
+        S = np.zeros((self.M, self.D))
+        tl, tn = C.c_double(), C.c_longlong()
+        self.check(self.lib.gmm_read_stats(self.h, ptr(n), ptr(F), ptr(S), C.byref(tl), C.byref(tn)))
+        return dict(n=n, F=F, S=S, totLL=tl.value, totN=tn.value)
+
+    def loglikes(self):
+        out = np.zeros(self.N, np.float32)
+        self.check(self.lib.gmm_loglikes(self.h, ptr(out)))
+        return out
+
+    # -- M-step
+    def em_update(self, upW=True, upM=True, upV=True):
+        a = C.c_int()
+        self.check(self.lib.gmm_em_update(self.h, int(upW), int(upM), int(upV), C.byref(a)))
+        return a.value
+
+    def map_update(self, tau, upW=False, upM=True, upV=False):
+        self.check(self.lib.gmm_map_update(self.h, int(tau), int(upW), int(upM), int(upV)))
+
+    def em_iterate(self, iters, upW=True, upM=True, upV=True):
+        ll = np.zeros(max(iters, 1))
+        a = C.c_int()
+        self.check(self.lib.gmm_em_iterate(self.h, iters, int(upW), int(upM), int(upV),
+                                           ptr(ll), C.byref(a)))
+        return ll[:iters], a.value
+
+    def mllr_estimate(self, ubm_init=False):
+        W = np.zeros((self.D, self.D + 1))
+        self.check(self.lib.gmm_mllr_estimate(self.h, int(ubm_init), ptr(W)))
+        return W
+
+    def mllr_apply(self, W):
+        W = np.ascontiguousarray(W, np.float64)
+        self.check(self.lib.gmm_mllr_apply(self.h, ptr(W)))
+
+    # -- profiling
+    def profile(self, on=True):
+        self.check(self.lib.gmm_profile_enable(self.h, int(on)))
+
+    def profile_reset(self):
+        self.check(self.lib.gmm_profile_reset(self.h))
+
+    def profile_read(self):
+        cap = 64
+        names = (C.c_char_p * cap)()
+        ms = np.zeros(cap)
+        cnt = np.zeros(cap, np.int64)
+        n = self.lib.gmm_profile_read(self.h, cap, names, ptr(ms), ptr(cnt))
+        return {names[i].decode(): (float(ms[i]), int(cnt[i])) for i in range(min(n, cap))}
+
+    def launch_count(self) -> int:
+        return int(self.lib.gmm_launch_count(self.h))

@@ -1,0 +1,543 @@
+// C ABI of the GB300 GMM statistics engine (declared in include/gmm_gb300.h).
+//
+// A handle owns one non-blocking CUDA stream and keeps the model, the features, the FP64
+// statistics and all scratch resident on its device. Host round trips happen only where a
+// result is returned to the caller; gmm_em_iterate runs the whole EM loop on the device.
+#include <string.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <new>
+#include <string>
+
+#include "gmm_internal.cuh"
+
+namespace gmm {
+
+static std::string g_create_err;
+
+int fail(Ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  else g_create_err = msg;
+  return code;
+}
+
+int cuda_fail(Ctx* c, cudaError_t e, const char* what) {
+  std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+  cudaGetLastError();  // clear a non-sticky error
+  return fail(c, e == cudaErrorMemoryAllocation ? GMM_ERR_NOMEM : GMM_ERR_CUDA, m);
+}
+
+int dalloc(Ctx* c, void** p, size_t bytes, const char* what) {
+  *p = nullptr;
+  if (bytes == 0) return GMM_OK;
+  if (c->budget && c->allocated + bytes > c->budget)
+    return fail(c, GMM_ERR_NOMEM, std::string(what) + ": over the handle's device-memory budget");
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    return cuda_fail(c, e, what);
+  }
+  c->allocated += bytes;
+  return GMM_OK;
+}
+
+void dfree(Ctx* c, void* p, size_t bytes) {
+  if (!p) return;
+  cudaFree(p);
+  c->allocated = c->allocated >= bytes ? c->allocated - bytes : 0;
+}
+
+int sync(Ctx* c, const char* what) {
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, what);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(c, e, what);
+  return GMM_OK;
+}
+
+LaunchScope::LaunchScope(Ctx* ctx, const char* name) : c(ctx) {
+  ++c->launches;
+  if (!c->profile) return;
+  for (auto& k : c->timers)
+    if (k.name == name) { t = &k; break; }
+  if (!t) {
+    c->timers.emplace_back();
+    t = &c->timers.back();
+    t->name = name;
+  }
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  cudaEventRecord(a, c->stream);
+}
+
+LaunchScope::~LaunchScope() {
+  if (!t) return;
+  cudaEventRecord(b, c->stream);
+  t->pending.emplace_back(a, b);
+  t->launches++;
+}
+
+static void drain_timers(Ctx* c) {
+  for (auto& k : c->timers) {
+    for (auto& ev : k.pending) {
+      cudaEventSynchronize(ev.second);
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, ev.first, ev.second);
+      k.ms += ms;
+      cudaEventDestroy(ev.first);
+      cudaEventDestroy(ev.second);
+    }
+    k.pending.clear();
+  }
+}
+
+static void free_model(Ctx* c) {
+  size_t md = sizeof(float) * (size_t)c->M * c->D, m1 = sizeof(float) * (size_t)c->M;
+  dfree(c, c->w, m1); dfree(c, c->mu, md); dfree(c, c->var, md);
+  dfree(c, c->icov, md); dfree(c, c->logG, m1); dfree(c, c->logW, m1);
+  dfree(c, c->act, sizeof(int) * (size_t)c->M);
+  dfree(c, c->pw, m1); dfree(c, c->pmu, md); dfree(c, c->pvar, md);
+  dfree(c, c->bw, m1); dfree(c, c->bmu, md); dfree(c, c->bvar, md);
+  dfree(c, c->stats, sizeof(double) * ((size_t)c->M * (1 + 2 * c->D) + 2));
+  c->w = c->mu = c->var = c->icov = c->logG = c->logW = nullptr;
+  c->pw = c->pmu = c->pvar = c->bw = c->bmu = c->bvar = nullptr;
+  c->act = nullptr;
+  c->stats = nullptr;
+  c->have_prior = false;
+  c->stats_valid = false;
+}
+
+static int ensure_model(Ctx* c, int M, int D) {
+  if (c->w && c->M == M && c->D == D) return GMM_OK;
+  free_model(c);
+  c->M = M;
+  c->D = D;
+  size_t md = sizeof(float) * (size_t)M * D, m1 = sizeof(float) * (size_t)M;
+  int rc = 0;
+  rc |= dalloc(c, (void**)&c->w, m1, "model weights");
+  if (!rc) rc |= dalloc(c, (void**)&c->mu, md, "model means");
+  if (!rc) rc |= dalloc(c, (void**)&c->var, md, "model variances");
+  if (!rc) rc |= dalloc(c, (void**)&c->icov, md, "inverse variances");
+  if (!rc) rc |= dalloc(c, (void**)&c->logG, m1, "log constants");
+  if (!rc) rc |= dalloc(c, (void**)&c->logW, m1, "log weights");
+  if (!rc) rc |= dalloc(c, (void**)&c->act, sizeof(int) * (size_t)M, "active list");
+  if (!rc) rc |= dalloc(c, (void**)&c->bw, m1, "model backup");
+  if (!rc) rc |= dalloc(c, (void**)&c->bmu, md, "model backup");
+  if (!rc) rc |= dalloc(c, (void**)&c->bvar, md, "model backup");
+  if (!rc) rc |= dalloc(c, (void**)&c->stats, sizeof(double) * ((size_t)M * (1 + 2 * D) + 2), "statistics");
+  if (rc) { int code = rc; free_model(c); c->M = c->D = 0; return code; }
+  c->tcx_valid = c->tcx_valid && (c->tcx.K != 0);
+  return GMM_OK;
+}
+
+static void free_features(Ctx* c) {
+  dfree(c, c->Xown, sizeof(float) * (size_t)c->N * c->Dx);
+  c->Xown = nullptr;
+  c->X = nullptr;
+  dfree(c, c->ll, c->ll_cap);
+  c->ll = nullptr;
+  c->ll_cap = 0;
+  dfree(c, c->llpart, c->llpart_cap * sizeof(double));
+  c->llpart = nullptr;
+  c->llpart_cap = 0;
+  c->N = 0;
+  c->tcx_valid = false;
+}
+
+static int alloc_frame_buffers(Ctx* c, long long N) {
+  size_t llb = sizeof(float) * (size_t)(N + 256);
+  int rc = dalloc(c, (void**)&c->ll, llb, "per-frame log-likelihoods");
+  if (rc) return rc;
+  c->ll_cap = llb;
+  size_t np = (size_t)((N + 255) / 256) + 1024;
+  rc = dalloc(c, (void**)&c->llpart, np * sizeof(double), "log-likelihood partial sums");
+  if (rc) return rc;
+  c->llpart_cap = np;
+  return GMM_OK;
+}
+
+static int estep(Ctx* c, int flags, bool want_stats, float* ll_dev) {
+  if (!c->w) return fail(c, GMM_ERR_STATE, "no model uploaded");
+  if (!c->X) return fail(c, GMM_ERR_STATE, "no features uploaded");
+  if (c->Dx != c->D)
+    return fail(c, GMM_ERR_ARG, "Inconsistent model & feature vector - different dimensions");
+  int rc;
+  if (c->model_dirty) {
+    rc = plain_precompute(c);
+    if (rc) return rc;
+  }
+  if (c->precision == GMM_PREC_TC) return tc_estep(c, flags, want_stats, ll_dev);
+  return plain_estep(c, flags, want_stats, ll_dev);
+}
+
+static int accumulate_device(Ctx* c, int flags) {
+  if (!c->w) return fail(c, GMM_ERR_STATE, "no model uploaded");
+  if (!c->X) return fail(c, GMM_ERR_STATE, "no features uploaded");
+  cudaError_t e = cudaMemsetAsync(c->stats, 0, sizeof(double) * ((size_t)c->M * (1 + 2 * c->D) + 2),
+                                  c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "cudaMemsetAsync(stats)");
+  c->stats_valid = false;
+  int rc = estep(c, flags, true, nullptr);
+  if (rc) return rc;
+  c->tot_frames = c->N;
+  c->acc_flags = flags;
+  c->stats_valid = true;
+  return GMM_OK;
+}
+
+static int stage(Ctx* c, size_t bytes) {
+  if (bytes <= c->hstage_cap) return GMM_OK;
+  if (c->hstage) cudaFreeHost(c->hstage);
+  c->hstage = nullptr;
+  c->hstage_cap = 0;
+  cudaError_t e = cudaMallocHost((void**)&c->hstage, bytes);
+  if (e != cudaSuccess) return cuda_fail(c, e, "cudaMallocHost(staging)");
+  c->hstage_cap = bytes;
+  return GMM_OK;
+}
+
+static int read_stats(Ctx* c, double* n, double* F, double* S, double* tl, long long* tn) {
+  if (!c->stats_valid) return fail(c, GMM_ERR_STATE, "no statistics accumulated");
+  size_t cnt = (size_t)c->M * (1 + 2 * c->D) + 1;
+  int rc = stage(c, cnt * sizeof(double));
+  if (rc) return rc;
+  cudaError_t e = cudaMemcpyAsync(c->hstage, c->stats, cnt * sizeof(double),
+                                  cudaMemcpyDeviceToHost, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "cudaMemcpyAsync(stats)");
+  rc = sync(c, "read statistics");
+  if (rc) return rc;
+  const size_t M = c->M, MD = (size_t)c->M * c->D;
+  if (n) memcpy(n, c->hstage, M * sizeof(double));
+  if (F) memcpy(F, c->hstage + M, MD * sizeof(double));
+  if (S) memcpy(S, c->hstage + M + MD, MD * sizeof(double));
+  if (tl) *tl = c->hstage[M + 2 * MD];
+  if (tn) *tn = c->tot_frames;
+  return GMM_OK;
+}
+
+}  // namespace gmm
+
+using namespace gmm;
+
+extern "C" {
+
+int gmm_create(int device, gmm_handle* out) {
+  if (!out) return fail(nullptr, GMM_ERR_ARG, "gmm_create: null output pointer");
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0)
+    return fail(nullptr, GMM_ERR_CUDA, "gmm_create: no CUDA device is available");
+  if (device < 0 || device >= n) return fail(nullptr, GMM_ERR_ARG, "gmm_create: device id out of range");
+  e = cudaSetDevice(device);
+  if (e != cudaSuccess) return fail(nullptr, GMM_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+  gmm_ctx* c = new (std::nothrow) gmm_ctx();
+  if (!c) return fail(nullptr, GMM_ERR_NOMEM, "gmm_create: out of host memory");
+  c->device = device;
+  e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) { delete c; return fail(nullptr, GMM_ERR_CUDA, "cudaStreamCreate failed"); }
+  if (dalloc(c, (void**)&c->flag, 16 * sizeof(int), "flags") ||
+      cudaMallocHost((void**)&c->hflag, 16 * sizeof(int)) != cudaSuccess) {
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return fail(nullptr, GMM_ERR_NOMEM, "gmm_create: flag allocation failed");
+  }
+  cudaMemset(c->flag, 0, 16 * sizeof(int));
+  *out = c;
+  return GMM_OK;
+}
+
+int gmm_destroy(gmm_handle h) {
+  if (!h) return GMM_OK;
+  gmm_ctx* c = h;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  drain_timers(c);
+  free_model(c);
+  free_features(c);
+  dfree(c, c->logits, c->logits_cap);
+  dfree(c, c->part, c->part_cap);
+  dfree(c, c->tcpart, c->tcpart_cap);
+  dfree(c, c->tcm.planes, 0);
+  dfree(c, c->tcm.comp_of_row, 0);
+  dfree(c, c->tcm.ll2, 0);
+  dfree(c, c->tcx.planes, 0);
+  dfree(c, c->tc_err, 0);
+  dfree(c, c->tc_llpart, 0);
+  dfree(c, c->flag, 0);
+  if (c->hflag) cudaFreeHost(c->hflag);
+  if (c->hstage) cudaFreeHost(c->hstage);
+  cudaStreamDestroy(c->stream);
+  delete c;
+  return GMM_OK;
+}
+
+const char* gmm_last_error(gmm_handle h) { return h ? h->err.c_str() : g_create_err.c_str(); }
+
+int gmm_set_options(gmm_handle h, float min_loglike, float min_gamma, float min_var) {
+  if (!h) return GMM_ERR_ARG;
+  h->minLL = min_loglike;
+  h->minGamma = min_gamma;
+  h->min_var = min_var;
+  h->model_dirty = true;
+  return GMM_OK;
+}
+
+int gmm_set_precision(gmm_handle h, int mode) {
+  if (!h) return GMM_ERR_ARG;
+  if (mode != GMM_PREC_FP32 && mode != GMM_PREC_TC) return fail(h, GMM_ERR_ARG, "unknown precision mode");
+  if (mode == GMM_PREC_TC && h->D > 0 && !tc_supported(h->D))
+    return fail(h, GMM_ERR_UNSUPPORTED, "tensor-core path supports 1 <= D <= 63");
+  h->precision = mode;
+  return GMM_OK;
+}
+
+int gmm_set_memory_budget(gmm_handle h, size_t bytes) {
+  if (!h) return GMM_ERR_ARG;
+  h->budget = bytes;
+  return GMM_OK;
+}
+
+int gmm_get_stream(gmm_handle h, void** stream) {
+  if (!h || !stream) return GMM_ERR_ARG;
+  *stream = (void*)h->stream;
+  return GMM_OK;
+}
+
+int gmm_upload_model(gmm_handle h, int M, int D, const float* w, const float* mu, const float* var) {
+  if (!h) return GMM_ERR_ARG;
+  Ctx* c = h;
+  if (!w || !mu || !var) return fail(c, GMM_ERR_ARG, "gmm_upload_model: null array");
+  if (M < 1 || M > kMaxMix || D < 1 || D > kMaxDim)
+    return fail(c, GMM_ERR_ARG, "gmm_upload_model: M must be in [1, 32767] and D in [1, 1024]");
+  if (c->precision == GMM_PREC_TC && !tc_supported(D))
+    return fail(c, GMM_ERR_UNSUPPORTED, "tensor-core path supports 1 <= D <= 63");
+  cudaSetDevice(c->device);
+  int rc = ensure_model(c, M, D);
+  if (rc) return rc;
+  size_t md = sizeof(float) * (size_t)M * D;
+  cudaMemcpyAsync(c->w, w, sizeof(float) * M, cudaMemcpyHostToDevice, c->stream);
+  cudaMemcpyAsync(c->mu, mu, md, cudaMemcpyHostToDevice, c->stream);
+  cudaMemcpyAsync(c->var, var, md, cudaMemcpyHostToDevice, c->stream);
+  c->stats_valid = false;
+  c->model_dirty = true;
+  return plain_precompute(c);
+}
+
+int gmm_set_prior(gmm_handle h, const float* w, const float* mu, const float* var) {
+  if (!h) return GMM_ERR_ARG;
+  Ctx* c = h;
+  if (!c->w) return fail(c, GMM_ERR_STATE, "upload a model before its prior");
+  size_t md = sizeof(float) * (size_t)c->M * c->D, m1 = sizeof(float) * (size_t)c->M;
+  if (!c->pw) {
+    int rc = dalloc(c, (void**)&c->pw, m1, "prior weights");
+    if (!rc) rc = dalloc(c, (void**)&c->pmu, md, "prior means");
+    if (!rc) rc = dalloc(c, (void**)&c->pvar, md, "prior variances");
+    if (rc) return rc;
+  }
+  if (w && mu && var) {
+    cudaMemcpyAsync(c->pw, w, m1, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(c->pmu, mu, md, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(c->pvar, var, md, cudaMemcpyHostToDevice, c->stream);
+  } else {  // NULLs: the current resident model becomes the prior
+    cudaMemcpyAsync(c->pw, c->w, m1, cudaMemcpyDeviceToDevice, c->stream);
+    cudaMemcpyAsync(c->pmu, c->mu, md, cudaMemcpyDeviceToDevice, c->stream);
+    cudaMemcpyAsync(c->pvar, c->var, md, cudaMemcpyDeviceToDevice, c->stream);
+  }
+  c->have_prior = true;
+  return sync(c, "gmm_set_prior");
+}
+
+int gmm_read_model(gmm_handle h, float* w, float* mu, float* var) {
+  if (!h) return GMM_ERR_ARG;
+  Ctx* c = h;
+  if (!c->w) return fail(c, GMM_ERR_STATE, "no model uploaded");
+  size_t md = sizeof(float) * (size_t)c->M * c->D;
+  if (w) cudaMemcpyAsync(w, c->w, sizeof(float) * c->M, cudaMemcpyDeviceToHost, c->stream);
+  if (mu) cudaMemcpyAsync(mu, c->mu, md, cudaMemcpyDeviceToHost, c->stream);
+  if (var) cudaMemcpyAsync(var, c->var, md, cudaMemcpyDeviceToHost, c->stream);
+  return sync(c, "gmm_read_model");
+}
+
+int gmm_upload_features(gmm_handle h, const float* X, long long N, int D) {
+  if (!h) return GMM_ERR_ARG;
+  Ctx* c = h;
+  if (!X && N > 0) return fail(c, GMM_ERR_ARG, "gmm_upload_features: null array");
+  if (N < 0 || D < 1 || D > kMaxDim) return fail(c, GMM_ERR_ARG, "gmm_upload_features: bad N or D");
+  cudaSetDevice(c->device);
+  size_t bytes = sizeof(float) * (size_t)N * D;
+  int rc = GMM_OK;
+  const bool reuse = c->Xown && c->N == N && c->Dx == D && c->ll;
+  if (!reuse) {
+    free_features(c);
+    rc = dalloc(c, (void**)&c->Xown, bytes, "features");
+    if (rc) return rc;
+  }
+  c->tcx_valid = false;
+  if (bytes) {
+    cudaError_t e = cudaMemcpyAsync(c->Xown, X, bytes, cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaMemcpyAsync(features)");
+  }
+  c->X = c->Xown;
+  c->N = N;
+  c->Dx = D;
+  if (!reuse) {
+    rc = alloc_frame_buffers(c, N);
+    if (rc) return rc;
+  }
+  c->stats_valid = false;
+  return sync(c, "gmm_upload_features");
+}
+
+int gmm_upload_features_device(gmm_handle h, const float* dX, long long N, int D) {
+  if (!h) return GMM_ERR_ARG;
+  Ctx* c = h;
+  if (!dX && N > 0) return fail(c, GMM_ERR_ARG, "gmm_upload_features_device: null array");
+  if (N < 0 || D < 1 || D > kMaxDim) return fail(c, GMM_ERR_ARG, "gmm_upload_features_device: bad N or D");
+  cudaSetDevice(c->device);
+  free_features(c);
+  c->X = dX;
+  c->N = N;
+  c->Dx = D;
+  c->stats_valid = false;
+  return alloc_frame_buffers(c, N);
+}
+
+int gmm_accumulate_device(gmm_handle h, int flags) {
+  if (!h) return GMM_ERR_ARG;
+  cudaSetDevice(h->device);
+  int rc = accumulate_device(h, flags);
+  if (rc) return rc;
+  return sync(h, "gmm_accumulate");
+}
+
+int gmm_read_stats(gmm_handle h, double* n, double* F, double* S, double* tl, long long* tn) {
+  if (!h) return GMM_ERR_ARG;
+  return read_stats(h, n, F, S, tl, tn);
+}
+
+int gmm_accumulate(gmm_handle h, int flags, double* n, double* F, double* S, double* tl,
+                   long long* tn) {
+  if (!h) return GMM_ERR_ARG;
+  cudaSetDevice(h->device);
+  int rc = accumulate_device(h, flags);
+  if (rc) return rc;
+  return read_stats(h, n, F, S, tl, tn);
+}
+
+int gmm_loglikes(gmm_handle h, float* out) {
+  if (!h) return GMM_ERR_ARG;
+  Ctx* c = h;
+  if (!out && c->N > 0) return fail(c, GMM_ERR_ARG, "gmm_loglikes: null output");
+  cudaSetDevice(c->device);
+  int rc = estep(c, 0, false, c->ll);
+  if (rc) return rc;
+  if (c->N > 0) {
+    cudaError_t e = cudaMemcpyAsync(out, c->ll, sizeof(float) * (size_t)c->N,
+                                    cudaMemcpyDeviceToHost, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaMemcpyAsync(loglikes)");
+  }
+  return sync(c, "gmm_loglikes");
+}
+
+int gmm_em_update(gmm_handle h, int upW, int upM, int upV, int* alive) {
+  if (!h) return GMM_ERR_ARG;
+  cudaSetDevice(h->device);
+  int a = 0;
+  int rc = mstep_em(h, upW, upM, upV, &a);
+  if (rc) return rc;
+  if (alive) *alive = a;
+  return GMM_OK;
+}
+
+int gmm_map_update(gmm_handle h, int tau, int upW, int upM, int upV) {
+  if (!h) return GMM_ERR_ARG;
+  if (tau < 0) return fail(h, GMM_ERR_ARG, "tau must be >= 0");
+  cudaSetDevice(h->device);
+  if (tau == 0) return gmm_em_update(h, upW, upM, upV, nullptr);
+  int rc = mstep_map(h, tau, upW, upM, upV);
+  if (rc) return rc;
+  return sync(h, "gmm_map_update");
+}
+
+int gmm_em_iterate(gmm_handle h, int iters, int upW, int upM, int upV, double* ll, int* alive) {
+  if (!h) return GMM_ERR_ARG;
+  Ctx* c = h;
+  if (iters < 0) return fail(c, GMM_ERR_ARG, "iters must be >= 0");
+  cudaSetDevice(c->device);
+  const int flags = (upM ? GMM_ACC_MEAN : 0) | (upV ? GMM_ACC_VAR : 0) |
+                    ((upW && !upM && !upV) ? GMM_ACC_PROBS_ONLY : 0);
+  const size_t md = sizeof(float) * (size_t)c->M * c->D, m1 = sizeof(float) * (size_t)c->M;
+  const size_t tot_idx = (size_t)c->M * (1 + 2 * c->D);
+  int last_alive = 0;
+  for (int it = 0; it < iters; ++it) {
+    // insertModel: zero-weight components move behind the others (GMModel::RearrangeMixtures)
+    int rc = mstep_rearrange(c);
+    if (rc) return rc;
+    rc = plain_precompute(c);
+    if (rc) return rc;
+    rc = accumulate_device(c, flags);
+    if (rc) return rc;
+    if (ll) {
+      rc = sync(c, "EM iteration");
+      if (rc) return rc;
+      cudaMemcpy(&ll[it], c->stats + tot_idx, sizeof(double), cudaMemcpyDeviceToHost);
+    }
+    // IterEM keeps a copy of the model; UpdateModelMAP restores it if no component survives
+    cudaMemcpyAsync(c->bw, c->w, m1, cudaMemcpyDeviceToDevice, c->stream);
+    cudaMemcpyAsync(c->bmu, c->mu, md, cudaMemcpyDeviceToDevice, c->stream);
+    cudaMemcpyAsync(c->bvar, c->var, md, cudaMemcpyDeviceToDevice, c->stream);
+    rc = mstep_em(c, upW, upM, upV, &last_alive);
+    if (rc) return rc;
+    if (last_alive == 0) {
+      cudaMemcpyAsync(c->w, c->bw, m1, cudaMemcpyDeviceToDevice, c->stream);
+      cudaMemcpyAsync(c->mu, c->bmu, md, cudaMemcpyDeviceToDevice, c->stream);
+      cudaMemcpyAsync(c->var, c->bvar, md, cudaMemcpyDeviceToDevice, c->stream);
+    }
+  }
+  if (alive) *alive = last_alive;
+  return sync(c, "gmm_em_iterate");
+}
+
+int gmm_mllr_estimate(gmm_handle h, int ubm_init, double* W) {
+  if (!h || !W) return GMM_ERR_ARG;
+  cudaSetDevice(h->device);
+  return mstep_mllr(h, ubm_init, W);
+}
+
+int gmm_mllr_apply(gmm_handle h, const double* W) {
+  if (!h || !W) return GMM_ERR_ARG;
+  if (!h->w) return fail(h, GMM_ERR_STATE, "no model uploaded");
+  cudaSetDevice(h->device);
+  return mstep_mllr_apply(h, W);
+}
+
+int gmm_profile_enable(gmm_handle h, int on) {
+  if (!h) return GMM_ERR_ARG;
+  h->profile = on != 0;
+  return GMM_OK;
+}
+
+int gmm_profile_reset(gmm_handle h) {
+  if (!h) return GMM_ERR_ARG;
+  drain_timers(h);
+  h->timers.clear();
+  return GMM_OK;
+}
+
+int gmm_profile_read(gmm_handle h, int cap, const char** names, double* ms, long long* launches) {
+  if (!h) return -GMM_ERR_ARG;
+  drain_timers(h);
+  int n = (int)h->timers.size();
+  for (int i = 0; i < n && i < cap; ++i) {
+    if (names) names[i] = h->timers[i].name.c_str();
+    if (ms) ms[i] = h->timers[i].ms;
+    if (launches) launches[i] = h->timers[i].launches;
+  }
+  return n;
+}
+
+long long gmm_launch_count(gmm_handle h) { return h ? h->launches : 0; }
+
+}  // extern "C"

@@ -1,0 +1,151 @@
+// Internal declarations shared by the gmm_gb300 translation units.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "gmm_gb300.h"
+
+namespace gmm {
+
+constexpr double kMinusLog2Pi = -1.837877066409345;  // OL_GMMStatsEstimator.h:280
+constexpr int kMaxMix = 32767;                        // GMModel::NumMixes is __int16
+constexpr int kMaxDim = 1024;
+
+// ------------------------------------------------------------------ error plumbing
+struct Error {
+  int code;
+  std::string msg;
+};
+
+// ------------------------------------------------------------------ per-kernel timing
+struct KernelTimer {
+  std::string name;
+  double ms = 0.0;
+  long long launches = 0;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;
+};
+
+// ------------------------------------------------------------------ tensor-core model planes
+struct TcModel {
+  int K = 0;            // padded contraction length (multiple of 16) of [x, x^2, 1, ...]
+  int Mpad = 0;         // active components padded to the component tile
+  uint16_t* planes = nullptr;  // 3 bf16 planes of W~ in the UMMA K-major tile layout
+  int* comp_of_row = nullptr;  // row r of the padded active list -> caller component index
+  float* ll2 = nullptr;        // per-frame log2-domain LSE of the current E-step
+};
+
+struct TcFeatures {
+  int K = 0;
+  long long Npad = 0;
+  uint16_t* planes = nullptr;  // 3 bf16 planes of Z = [x, x^2, 1, ...] per frame tile
+};
+
+struct Ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+
+  float minLL = -1e20f, minGamma = 1e-4f, min_var = 1e-6f;
+  int precision = GMM_PREC_FP32;
+  size_t budget = 0, allocated = 0;
+
+  // model (caller order), device
+  int M = 0, D = 0, Mact = 0;
+  float *w = nullptr, *mu = nullptr, *var = nullptr;
+  float *icov = nullptr, *logG = nullptr, *logW = nullptr;
+  int* act = nullptr;      // active component indices in order (w > 0)
+  int* flag = nullptr;     // device flags: [0] bad variance, [1] stability trouble, [2] alive,
+                           // [3] timeout, [4] active count
+  int* hflag = nullptr;    // pinned mirror of flag
+  float *pw = nullptr, *pmu = nullptr, *pvar = nullptr;  // MAP prior
+  bool have_prior = false;
+  bool model_dirty = true;  // precompute needed
+
+  // features
+  long long N = 0;
+  int Dx = 0;  // feature dimension (checked against the model's at each E-step)
+  const float* X = nullptr;
+  float* Xown = nullptr;
+
+  // statistics (FP64, caller order): n[M], F[M*D], S[M*D], then totLL, and frames as double
+  double* stats = nullptr;
+  double* llpart = nullptr;  // per-block log-likelihood partial sums
+  size_t llpart_cap = 0;
+  long long tot_frames = 0;
+  int acc_flags = 0;
+  bool stats_valid = false;
+
+  // scratch
+  float* logits = nullptr;  // plain path: [Mact][chunk] raw log posteriors
+  size_t logits_cap = 0;
+  float* ll = nullptr;      // per-frame log-likelihood, N floats
+  size_t ll_cap = 0;
+  double* part = nullptr;   // plain path: per (slice, component) partial statistics
+  size_t part_cap = 0;
+  double* hstage = nullptr; size_t hstage_cap = 0;  // pinned staging for results
+
+  // model backup for the all-components-killed fallback of IterEM
+  float *bw = nullptr, *bmu = nullptr, *bvar = nullptr;
+
+  // tensor-core path
+  TcModel tcm;
+  TcFeatures tcx;
+  bool tcx_valid = false;
+  double* tcpart = nullptr;  // per-CTA FP64 partial statistics
+  size_t tcpart_cap = 0;
+  CUtensorMap tm_z128, tm_zft, tm_w128, tm_wct;  // TMA maps over the operand planes
+  int* tc_err = nullptr;                          // bounded-wait expiry flag
+  double* tc_llpart = nullptr;                    // per-thread log-likelihood partials
+  size_t tc_llpart_cap = 0;
+  int sms = 0;
+
+  // timing
+  bool profile = false;
+  std::vector<KernelTimer> timers;
+  long long launches = 0;
+};
+
+// device allocation through the handle's budget
+int dalloc(Ctx* c, void** p, size_t bytes, const char* what);
+void dfree(Ctx* c, void* p, size_t bytes);
+int fail(Ctx* c, int code, const std::string& msg);
+int cuda_fail(Ctx* c, cudaError_t e, const char* what);
+
+// kernel timing around a launch
+struct LaunchScope {
+  Ctx* c;
+  KernelTimer* t = nullptr;
+  cudaEvent_t a = nullptr, b = nullptr;
+  LaunchScope(Ctx* c, const char* name);
+  ~LaunchScope();
+};
+#define GMM_LAUNCH(ctx, name) ::gmm::LaunchScope _ls_##__LINE__((ctx), (name))
+
+// ------------------------------------------------------------------ plain FP32 path
+int plain_precompute(Ctx* c);
+int plain_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev);
+
+// ------------------------------------------------------------------ M-step
+int mstep_em(Ctx* c, int upW, int upM, int upV, int* alive);
+int mstep_map(Ctx* c, int tau, int upW, int upM, int upV);
+int mstep_rearrange(Ctx* c);
+int mstep_mllr(Ctx* c, int ubm_init, double* W_host);
+int mstep_mllr_apply(Ctx* c, const double* W_host);
+
+// ------------------------------------------------------------------ tensor-core path
+int tc_supported(int D);
+int tc_prepare_features(Ctx* c);
+int tc_prepare_model(Ctx* c);
+int tc_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev);
+
+int sync(Ctx* c, const char* what);
+
+}  // namespace gmm
+
+// The opaque handle type of the C ABI is the context itself.
+struct gmm_ctx : public gmm::Ctx {};

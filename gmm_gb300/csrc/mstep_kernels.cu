@@ -1,0 +1,394 @@
+// M-step on the device: EM, MAP and global-MLLR re-estimation from the FP64 statistics.
+//
+// The model stays device-resident between E-steps; nothing goes through the host per EM
+// iteration. Arithmetic follows the reference's CModelAdapt (GMM/lib_bmssr/trainer/
+// OL_ModelAdapt.cpp) expression by expression -- FP64 math, float stores, the same
+// sequential sums for the weight normalisers -- and uses explicit round-to-nearest intrinsics
+// so no multiply-add is fused. Given the same statistics the updates are bit-identical to the
+// reference's.
+#include <math.h>
+
+#include "gmm_internal.cuh"
+
+namespace gmm {
+
+namespace {
+
+__device__ __forceinline__ float reset_var_value() {
+  // GMMMixture::Reset (OL_GMModel.cpp:73-83) fills diagonal variances with memset(.., 1, ..)
+  return __int_as_float(0x01010101);
+}
+
+// UpdateModelEM per component (OL_ModelAdapt.cpp:858-921). flag[5] <- weights changed,
+// flag[6] <- number of components that had zero weight before the update.
+__global__ void em_comp_kernel(int M, int D, float* __restrict__ w, float* __restrict__ mu,
+                               float* __restrict__ var, const double* __restrict__ stats,
+                               unsigned int tot, int upW, int upM, int upV, float min_var,
+                               int* __restrict__ flag) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= M) return;
+  const double* n = stats;
+  const double* F = stats + M;
+  const double* S = stats + M + (size_t)M * D;
+  if (w[j] == 0.0f) { atomicAdd(&flag[6], 1); return; }
+  double mp = n[j];
+  float* mj = mu + (size_t)j * D;
+  float* vj = var + (size_t)j * D;
+  if (mp < 2.0) {  // _MIN_IND_SAMPLES_ (OL_ModelAdapt.h:54)
+    for (int k = 0; k < D; ++k) { mj[k] = 0.0f; vj[k] = reset_var_value(); }
+    w[j] = 0.0f;
+    atomicExch(&flag[5], 1);
+    return;
+  }
+  if (upW) {
+    w[j] = (float)__ddiv_rn(mp, (double)tot);
+    atomicExch(&flag[5], 1);
+  }
+  if (upM || upV) {
+    for (int k = 0; k < D; ++k) {
+      float mean = (float)__ddiv_rn(F[(size_t)j * D + k], mp);
+      if (upV) {
+        double m2 = __dmul_rn((double)mean, (double)mean);
+        float v = (float)__dsub_rn(__ddiv_rn(S[(size_t)j * D + k], mp), m2);
+        if (v < min_var) v = min_var;
+        vj[k] = v;
+      }
+      if (upM) mj[k] = mean;
+    }
+  }
+}
+
+// Weight renormalisation (OL_ModelAdapt.cpp:928-931): sequential FP64 sum in component order.
+__global__ void em_norm_kernel(int M, float* __restrict__ w, int* __restrict__ flag) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double corr = 0.0;
+  for (int j = 0; j < M; ++j) corr = __dadd_rn(corr, (double)w[j]);
+  if (flag[5] && corr > 0.0)
+    for (int j = 0; j < M; ++j) w[j] = (float)__ddiv_rn((double)w[j], corr);
+  flag[2] = M - flag[6];
+}
+
+// UpdateModelMAP, tau > 0 (OL_ModelAdapt.cpp:1024-1099), one thread per component.
+__global__ void map_comp_kernel(int M, int D, float* __restrict__ w, float* __restrict__ mu,
+                                float* __restrict__ var, const float* __restrict__ uw,
+                                const float* __restrict__ umu, const float* __restrict__ uvar,
+                                const double* __restrict__ stats, unsigned int tot, int tau,
+                                int upW, int upM, int upV, float min_var,
+                                float* __restrict__ adapted_w) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= M) return;
+  adapted_w[j] = 0.0f;
+  if (uw[j] == 0.0f) return;
+  const double* n = stats;
+  const double* F = stats + M;
+  const double* S = stats + M + (size_t)M * D;
+  double mp = n[j];
+  if (!(mp > 0.0)) return;
+  double alfa = __ddiv_rn(mp, __dadd_rn(mp, (double)tau));
+  double one_m = __dsub_rn(1.0, alfa);
+  if (upW && tot > 0) {
+    double t1 = __dmul_rn(alfa, __ddiv_rn(mp, (double)tot));
+    float aw = (float)__dadd_rn(t1, __dmul_rn(one_m, (double)uw[j]));
+    w[j] = aw;
+    adapted_w[j] = aw;
+  }
+  if (upM || upV) {
+    const float* um = umu + (size_t)j * D;
+    const float* uv = uvar + (size_t)j * D;
+    for (int k = 0; k < D; ++k) {
+      double a1 = __ddiv_rn(__dmul_rn(alfa, F[(size_t)j * D + k]), mp);
+      float am = (float)__dadd_rn(a1, __dmul_rn(one_m, (double)um[k]));
+      if (upV) {
+        float second = __fadd_rn(uv[k], __fmul_rn(um[k], um[k]));
+        float msq = __fmul_rn(am, am);
+        double b1 = __ddiv_rn(__dmul_rn(alfa, S[(size_t)j * D + k]), mp);
+        double b2 = __dadd_rn(b1, __dmul_rn(one_m, (double)second));
+        float av = (float)__dsub_rn(b2, (double)msq);
+        if (av < min_var) av = min_var;
+        var[(size_t)j * D + k] = av;
+      }
+      mu[(size_t)j * D + k] = am;
+    }
+  }
+}
+
+__global__ void map_norm_kernel(int M, float* __restrict__ w, const float* __restrict__ adapted_w,
+                                const float* __restrict__ uw, const double* __restrict__ stats,
+                                int upW, unsigned int tot) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (!upW) return;
+  double corr = 0.0;
+  for (int j = 0; j < M; ++j)
+    if (uw[j] != 0.0f && stats[j] > 0.0 && tot > 0) corr = __dadd_rn(corr, (double)adapted_w[j]);
+  if (corr != 0.0) {
+    float fc = (float)corr;
+    for (int j = 0; j < M; ++j) w[j] = __fdiv_rn(w[j], fc);
+  }
+}
+
+// GMModel::RearrangeMixtures (OL_GMModel.cpp:857-885), single block: non-zero-weight
+// components keep their order, the k-th zero-weight one goes to slot M-1-k.
+__global__ void rearrange_kernel(int M, int D, float* __restrict__ w, float* __restrict__ mu,
+                                 float* __restrict__ var, float* __restrict__ tw,
+                                 float* __restrict__ tmu, float* __restrict__ tvar,
+                                 int* __restrict__ order) {
+  __shared__ int s_nz;
+  if (threadIdx.x == 0) {
+    int nz = 0, z = 1;
+    for (int m = 0; m < M; ++m) {
+      if (w[m] > 0.0f) order[nz++] = m;
+      else order[M - z++] = m;
+    }
+    s_nz = nz;
+  }
+  __syncthreads();
+  for (size_t e = threadIdx.x; e < (size_t)M * D; e += blockDim.x) {
+    tmu[e] = mu[e];
+    tvar[e] = var[e];
+  }
+  for (int m = threadIdx.x; m < M; m += blockDim.x) tw[m] = w[m];
+  __syncthreads();
+  for (size_t e = threadIdx.x; e < (size_t)M * D; e += blockDim.x) {
+    int k = (int)(e / D), d = (int)(e - (size_t)k * D);
+    mu[e] = tmu[(size_t)order[k] * D + d];
+    var[e] = tvar[(size_t)order[k] * D + d];
+  }
+  for (int m = threadIdx.x; m < M; m += blockDim.x) w[m] = tw[order[m]];
+}
+
+// CheckInvertibility sums (OL_ModelAdapt.cpp:1857-1866): sequential, component order.
+__global__ void mllr_check_kernel(int M, const double* __restrict__ n, double* __restrict__ out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int act = 0;
+  double occ = 0.0;
+  for (int m = 0; m < M; ++m)
+    if (n[m] > 0.0) { ++act; occ = __dadd_rn(occ, n[m]); }
+  out[0] = act;
+  out[1] = occ;
+}
+
+// One block per transform row i: G_i, k_i (ComputeKiGi_MLLR :1525-1581, with the
+// prepareKiGiInitMatrices prior :1484-1523), pivot-free Gauss-Jordan inverse
+// (MATRIX::_Invert_Gen, Matrix4_LMa.cpp:2232-2300), w_i = G_i^-1 k_i (MATRIX::Mult).
+// Shared memory: (D+1)^2 + (D+1) doubles.
+__global__ void mllr_row_kernel(int M, int D, const float* __restrict__ mu,
+                                const float* __restrict__ var, const float* __restrict__ umu,
+                                const float* __restrict__ uvar, const double* __restrict__ stats,
+                                int ubm_init, float min_var, double* __restrict__ W) {
+  extern __shared__ double sm[];
+  const int E = D + 1;
+  const int i = blockIdx.x;
+  double* G = sm;
+  double* kv = sm + E * E;
+  const double* n = stats;
+  const double* F = stats + M;
+  // each thread owns entries (a, b) of the upper triangle incl. the last column, plus k[a]
+  for (int e = threadIdx.x; e < E * E; e += blockDim.x) {
+    int a = e / E, b = e - a * E;
+    if (a > b) continue;
+    double g = 0.0;
+    if (ubm_init) {
+      // prior terms over all UBM components, accumulated in the reference's order
+      for (int m = 0; m < M; ++m) {
+        const float* v = uvar + (size_t)m * D;
+        const float* me = umu + (size_t)m * D;
+        double cG = (v[i] < min_var) ? (double)__fdiv_rn(1.0f, min_var) : (double)__fdiv_rn(1.0f, v[i]);
+        if (a < D && b < D) {
+          g = __dadd_rn(g, __dmul_rn(__dmul_rn(cG, (double)me[a]), (double)me[b]));
+          if (a == b) g = __dadd_rn(g, __dmul_rn(cG, (double)v[a]));
+        } else if (a < D) {
+          g = __dadd_rn(g, __dmul_rn(cG, (double)me[a]));
+        } else {
+          g = __dadd_rn(g, cG);
+        }
+      }
+    }
+    for (int m = 0; m < M; ++m) {
+      double mp = n[m];
+      if (!(mp > 0.0)) continue;
+      const float* mm = mu + (size_t)m * D;
+      double cv = __ddiv_rn(mp, (double)var[(size_t)m * D + i]);
+      if (a < D && b < D) g = __dadd_rn(g, __dmul_rn(__dmul_rn(cv, (double)mm[a]), (double)mm[b]));
+      else if (a < D) g = __dadd_rn(g, __dmul_rn(cv, (double)mm[a]));
+      else g = __dadd_rn(g, cv);
+    }
+    G[a * E + b] = g;
+  }
+  for (int a = threadIdx.x; a < E; a += blockDim.x) {
+    double k = 0.0;
+    if (ubm_init) {
+      for (int m = 0; m < M; ++m) {
+        const float* v = uvar + (size_t)m * D;
+        const float* me = umu + (size_t)m * D;
+        double cG = (v[i] < min_var) ? (double)__fdiv_rn(1.0f, min_var) : (double)__fdiv_rn(1.0f, v[i]);
+        double ck = __dmul_rn((double)me[i], cG);
+        k = __dadd_rn(k, a < D ? __dmul_rn(ck, (double)me[a]) : ck);
+      }
+    }
+    for (int m = 0; m < M; ++m) {
+      double mp = n[m];
+      if (!(mp > 0.0)) continue;
+      double cm = __ddiv_rn(F[(size_t)m * D + i], (double)var[(size_t)m * D + i]);
+      k = __dadd_rn(k, a < D ? __dmul_rn(cm, (double)mu[(size_t)m * D + a]) : cm);
+    }
+    kv[a] = k;
+  }
+  __syncthreads();
+  // the reference mirrors the upper triangle into the lower one as it accumulates
+  for (int e = threadIdx.x; e < E * E; e += blockDim.x) {
+    int a = e / E, b = e - a * E;
+    if (a > b) G[a * E + b] = G[b * E + a];
+  }
+  __syncthreads();
+  for (int k = 0; k < E; ++k) {
+    const double piv = G[k * E + k];
+    for (int e = threadIdx.x; e < E * E; e += blockDim.x) {
+      int a = e / E, b = e - a * E;
+      if (a != k && b != k)
+        G[e] = __dsub_rn(G[e], __ddiv_rn(__dmul_rn(G[k * E + b], G[a * E + k]), piv));
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < E; e += blockDim.x) {
+      if (e != k) {
+        G[k * E + e] = __ddiv_rn(-G[k * E + e], piv);
+        G[e * E + k] = __ddiv_rn(G[e * E + k], piv);
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) G[k * E + k] = __ddiv_rn(1.0, piv);
+    __syncthreads();
+  }
+  for (int a = threadIdx.x; a < E; a += blockDim.x) {
+    double s = 0.0;
+    for (int b = 0; b < E; ++b) s = __dadd_rn(s, __dmul_rn(G[a * E + b], kv[b]));
+    W[(size_t)i * E + a] = s;
+  }
+}
+
+// AdaptModelMLLR (OL_ModelAdapt.cpp:1597-1608): one block per component.
+__global__ void mllr_apply_kernel(int M, int D, float* __restrict__ mu, const double* __restrict__ W) {
+  extern __shared__ float row[];
+  const int m = blockIdx.x;
+  const int E = D + 1;
+  for (int k = threadIdx.x; k < D; k += blockDim.x) row[k] = mu[(size_t)m * D + k];
+  __syncthreads();
+  for (int k = threadIdx.x; k < D; k += blockDim.x) {
+    double v = 0.0;
+    for (int kk = 0; kk < D; ++kk) v = __dadd_rn(v, __dmul_rn(W[(size_t)k * E + kk], (double)row[kk]));
+    mu[(size_t)m * D + k] = (float)__dadd_rn(v, W[(size_t)k * E + D]);
+  }
+}
+
+}  // namespace
+
+int mstep_em(Ctx* c, int upW, int upM, int upV, int* alive) {
+  if (!c->stats_valid) return fail(c, GMM_ERR_STATE, "no statistics accumulated");
+  cudaMemsetAsync(c->flag + 5, 0, 2 * sizeof(int), c->stream);
+  unsigned int tot = (unsigned int)c->tot_frames;
+  {
+    GMM_LAUNCH(c, "em_comp_kernel");
+    em_comp_kernel<<<(c->M + 127) / 128, 128, 0, c->stream>>>(
+        c->M, c->D, c->w, c->mu, c->var, c->stats, tot, upW, upM, upV, c->min_var, c->flag);
+  }
+  {
+    GMM_LAUNCH(c, "em_norm_kernel");
+    em_norm_kernel<<<1, 32, 0, c->stream>>>(c->M, c->w, c->flag);
+  }
+  c->model_dirty = true;
+  c->tcx_valid = c->tcx_valid;  // features unaffected
+  if (alive) {
+    cudaError_t e = cudaMemcpyAsync(c->hflag, c->flag, 8 * sizeof(int), cudaMemcpyDeviceToHost,
+                                    c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaMemcpyAsync(flags)");
+    int rc = sync(c, "EM update");
+    if (rc) return rc;
+    *alive = c->hflag[2];
+  }
+  return GMM_OK;
+}
+
+int mstep_map(Ctx* c, int tau, int upW, int upM, int upV) {
+  if (!c->stats_valid) return fail(c, GMM_ERR_STATE, "no statistics accumulated");
+  if (!c->have_prior) return fail(c, GMM_ERR_STATE, "MAP needs a prior model (gmm_set_prior)");
+  unsigned int tot = (unsigned int)c->tot_frames;
+  // adapted weights scratch: reuse the logW buffer (recomputed by the next precompute)
+  {
+    GMM_LAUNCH(c, "map_comp_kernel");
+    map_comp_kernel<<<(c->M + 127) / 128, 128, 0, c->stream>>>(
+        c->M, c->D, c->w, c->mu, c->var, c->pw, c->pmu, c->pvar, c->stats, tot, tau, upW, upM,
+        upV, c->min_var, c->logW);
+  }
+  {
+    GMM_LAUNCH(c, "map_norm_kernel");
+    map_norm_kernel<<<1, 32, 0, c->stream>>>(c->M, c->w, c->logW, c->pw, c->stats, upW, tot);
+  }
+  c->model_dirty = true;
+  return GMM_OK;
+}
+
+int mstep_rearrange(Ctx* c) {
+  GMM_LAUNCH(c, "rearrange_kernel");
+  rearrange_kernel<<<1, 1024, 0, c->stream>>>(c->M, c->D, c->w, c->mu, c->var, c->bw, c->bmu,
+                                               c->bvar, c->act);
+  c->model_dirty = true;
+  return GMM_OK;
+}
+
+int mstep_mllr(Ctx* c, int ubm_init, double* W_host) {
+  if (!c->stats_valid) return fail(c, GMM_ERR_STATE, "no statistics accumulated");
+  if (!(c->acc_flags & GMM_ACC_MEAN)) return fail(c, GMM_ERR_STATE, "MLLR needs mean statistics");
+  const int D = c->D, M = c->M, E = D + 1;
+  if (ubm_init && !c->have_prior) return fail(c, GMM_ERR_STATE, "MLLR UBM init needs a prior model");
+  double* dW = nullptr;
+  int rc = dalloc(c, (void**)&dW, sizeof(double) * ((size_t)D * E + 2), "MLLR transform");
+  if (rc) return rc;
+  {
+    GMM_LAUNCH(c, "mllr_check_kernel");
+    mllr_check_kernel<<<1, 32, 0, c->stream>>>(M, c->stats, dW + (size_t)D * E);
+  }
+  double chk[2];
+  cudaMemcpyAsync(chk, dW + (size_t)D * E, sizeof(chk), cudaMemcpyDeviceToHost, c->stream);
+  rc = sync(c, "MLLR check");
+  if (rc) { dfree(c, dW, sizeof(double) * ((size_t)D * E + 2)); return rc; }
+  if (M < E || chk[0] < E || chk[1] * D < (double)D * E) {
+    dfree(c, dW, sizeof(double) * ((size_t)D * E + 2));
+    return fail(c, GMM_ERR_MLLR, "CheckInvertibility(): not enough components or data for a D x (D+1) MLLR transform");
+  }
+  size_t smem = sizeof(double) * ((size_t)E * E + E);
+  if (smem > 200 * 1024) {
+    dfree(c, dW, sizeof(double) * ((size_t)D * E + 2));
+    return fail(c, GMM_ERR_UNSUPPORTED, "MLLR: D too large for the shared-memory solve");
+  }
+  cudaFuncSetAttribute(mllr_row_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  {
+    GMM_LAUNCH(c, "mllr_row_kernel");
+    const float* umu = c->have_prior ? c->pmu : c->mu;
+    const float* uvar = c->have_prior ? c->pvar : c->var;
+    mllr_row_kernel<<<D, 256, smem, c->stream>>>(M, D, c->mu, c->var, umu, uvar, c->stats,
+                                                 ubm_init, c->min_var, dW);
+  }
+  cudaError_t e = cudaMemcpyAsync(W_host, dW, sizeof(double) * (size_t)D * E,
+                                  cudaMemcpyDeviceToHost, c->stream);
+  if (e != cudaSuccess) { dfree(c, dW, 0); return cuda_fail(c, e, "cudaMemcpyAsync(W)"); }
+  rc = sync(c, "MLLR solve");
+  dfree(c, dW, sizeof(double) * ((size_t)D * E + 2));
+  return rc;
+}
+
+int mstep_mllr_apply(Ctx* c, const double* W_host) {
+  const int D = c->D, E = D + 1;
+  double* dW = nullptr;
+  int rc = dalloc(c, (void**)&dW, sizeof(double) * (size_t)D * E, "MLLR transform");
+  if (rc) return rc;
+  cudaMemcpyAsync(dW, W_host, sizeof(double) * (size_t)D * E, cudaMemcpyHostToDevice, c->stream);
+  {
+    GMM_LAUNCH(c, "mllr_apply_kernel");
+    mllr_apply_kernel<<<c->M, 64, sizeof(float) * D, c->stream>>>(c->M, D, c->mu, dW);
+  }
+  rc = sync(c, "MLLR apply");
+  dfree(c, dW, sizeof(double) * (size_t)D * E);
+  c->model_dirty = true;
+  return rc;
+}
+
+}  // namespace gmm

@@ -1,0 +1,797 @@
+// Tensor-core (tcgen05) E-step for sm_103a.
+//
+// The diagonal-covariance log-likelihood is a contraction:
+//   s_fm = sum_k Z_fk W_km,  Z_f = [x_f, x_f^2, 1, 0...],
+//   W_m  = log2(e) * [mu_m / var_m, -1 / (2 var_m), log w_m - D/2 log 2pi - 1/2 sum log var_m, 0...]
+// (log2 units), K = 2D+1 padded to a multiple of 16. Z and W are each held as three bf16 planes
+// (v = p1 + p2 + p3, each plane the bf16 rounding of what the previous ones left), and the
+// contraction sums the six plane products p_i q_j with i + j <= 4 into an FP32 TMEM
+// accumulator: every operand is represented to ~2^-24 relative, so the logits carry FP32-level
+// error from the accumulation alone.
+//
+// Two kernels per E-step, both with one TMA-producer warp, one MMA-issuer warp and four
+// epilogue warps (one per TMEM lane quadrant):
+//   ll_kernel  (frame-tile major, persistent): S[128 frames x CT comps] per component chunk,
+//              online log2-sum-exp over all chunks in the epilogue -> per-frame log-likelihood.
+//   acc_kernel (component-chunk major): the chunk's W planes stay in shared memory; Z tiles
+//              stream through a 2-stage TMA ring. The MMA computes S^T[128 comps x FT frames];
+//              the epilogue turns it in place into posteriors gamma = 2^(s - ll) (pruned at
+//              minGamma, split into bf16 hi + lo) and the next MMA uses those TMEM columns as
+//              its A operand: D2[comps x K] += Gamma^T [Z1, Z2] (hi*Z1 + hi*Z2 + lo*Z1), i.e. the
+//              n, F, S statistics in one [1, x, x^2] product. Posteriors never leave TMEM.
+//              D2 is double-buffered and flushed into per-CTA FP64 partials every `flush_every`
+//              tiles; a final kernel reduces the partials over CTAs in a fixed order.
+// Every mbarrier wait is bounded (~2 s); on expiry the kernel raises an error flag, drains its
+// own copies and MMAs (bounded), frees TMEM and returns.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cudaTypedefs.h>
+#include <math.h>
+
+#include "gmm_internal.cuh"
+#include "tc_ptx.cuh"
+
+namespace gmm {
+
+using namespace ptx;
+
+namespace {
+
+constexpr double kLog2e = 1.4426950408889634;
+constexpr float kLn2 = 0.69314718055994531f;
+constexpr long long kWaitLimit = 4000000000LL;  // clock cycles (~2 s)
+constexpr int kThreads = 192;                    // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
+
+__host__ __device__ constexpr int tile_frames(int K) { return K <= 96 ? 128 : 64; }
+
+// ------------------------------------------------------------------ operand preparation
+
+__device__ __forceinline__ void split3f(float v, uint16_t& a, uint16_t& b, uint16_t& c) {
+  __nv_bfloat16 h1 = __float2bfloat16_rn(v);
+  float r = v - __bfloat162float(h1);  // exact
+  __nv_bfloat16 h2 = __float2bfloat16_rn(r);
+  r = r - __bfloat162float(h2);  // exact
+  __nv_bfloat16 h3 = __float2bfloat16_rn(r);
+  a = __bfloat16_as_ushort(h1);
+  b = __bfloat16_as_ushort(h2);
+  c = __bfloat16_as_ushort(h3);
+}
+
+__device__ __forceinline__ void split3d(double v, uint16_t& a, uint16_t& b, uint16_t& c) {
+  __nv_bfloat16 h1 = __float2bfloat16_rn((float)v);
+  double r = v - (double)__bfloat162float(h1);
+  __nv_bfloat16 h2 = __float2bfloat16_rn((float)r);
+  r = r - (double)__bfloat162float(h2);
+  __nv_bfloat16 h3 = __float2bfloat16_rn((float)r);
+  a = __bfloat16_as_ushort(h1);
+  b = __bfloat16_as_ushort(h2);
+  c = __bfloat16_as_ushort(h3);
+}
+
+// Z planes [3][Npad][K]: row f = [x, x^2, 1, 0...] (zero rows past N).
+__global__ void features_kernel(const float* __restrict__ X, long long N, long long Npad, int D,
+                                int K, uint16_t* __restrict__ planes) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= Npad * K) return;
+  const long long f = t / K;
+  const int k = (int)(t - f * K);
+  float v = 0.0f;
+  if (f < N) {
+    if (k < D) v = X[f * D + k];
+    else if (k < 2 * D) { float x = X[f * D + k - D]; v = x * x; }
+    else if (k == 2 * D) v = 1.0f;
+  }
+  uint16_t a, b, c;
+  split3f(v, a, b, c);
+  const size_t plane = (size_t)Npad * K;
+  planes[t] = a;
+  planes[plane + t] = b;
+  planes[2 * plane + t] = c;
+}
+
+// W planes [3][Mpad][K] over the active components (log2 units); padded rows carry a
+// constant of -1e30 so they never contribute.
+__global__ void model_kernel(int D, int K, int Mact, int Mpad, const int* __restrict__ act,
+                             const float* __restrict__ w, const float* __restrict__ mu,
+                             const float* __restrict__ var, uint16_t* __restrict__ planes,
+                             int* __restrict__ comp_of_row) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)Mpad * K) return;
+  const int r = (int)(t / K), k = (int)(t - (long long)r * K);
+  double v = 0.0;
+  if (r < Mact) {
+    const int m = act[r];
+    const float* mm = mu + (size_t)m * D;
+    const float* vv = var + (size_t)m * D;
+    if (k < D) v = kLog2e * (double)mm[k] / (double)vv[k];
+    else if (k < 2 * D) v = -0.5 * kLog2e / (double)vv[k - D];
+    else if (k == 2 * D) {
+      double s = 0.0;
+      for (int d = 0; d < D; ++d) s += log((double)vv[d]);
+      v = kLog2e * (log((double)w[m]) + kMinusLog2Pi * D / 2.0 - 0.5 * s);
+    }
+  } else if (k == 2 * D) {
+    v = -1e30;
+  }
+  uint16_t a, b, c;
+  split3d(v, a, b, c);
+  const size_t plane = (size_t)Mpad * K;
+  planes[t] = a;
+  planes[plane + t] = b;
+  planes[2 * plane + t] = c;
+  if (k == 0) comp_of_row[r] = r < Mact ? act[r] : -1;
+}
+
+// ------------------------------------------------------------------ shared helpers
+
+__device__ __forceinline__ uint8_t* align1024(uint8_t* p) {
+  return reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(p) + 1023) & ~(uintptr_t)1023);
+}
+
+// Wait without the abort short-cut (used to drain in-flight work on the exit path).
+__device__ __forceinline__ void mbar_drain(uint64_t* bar, uint32_t parity) {
+  const long long t0 = clock64();
+  while (!mbar_try_wait(bar, parity))
+    if (clock64() - t0 > kWaitLimit) break;
+}
+
+// Plane products (Z plane, W plane) with i + j <= 4 (1-based), small terms first.
+__device__ __constant__ int kProdZ[6] = {2, 1, 0, 1, 0, 0};
+__device__ __constant__ int kProdW[6] = {0, 1, 2, 0, 1, 0};
+
+// ------------------------------------------------------------------ log-likelihood kernel
+
+template <int K, int CT>
+struct LlCfg {
+  static constexpr int KC = K / 8;
+  static constexpr int Z_PLANE = 128 * K * 2;
+  static constexpr int W_PLANE = CT * K * 2;
+  static constexpr int Z_BYTES = 3 * Z_PLANE;
+  static constexpr int W_STAGE = 3 * W_PLANE;
+  static constexpr int OFF_Z = 0;
+  static constexpr int OFF_W = Z_BYTES;
+  static constexpr int OFF_BAR = OFF_W + 2 * W_STAGE;
+  static constexpr int OFF_MISC = OFF_BAR + 16 * 8;
+  static constexpr int SMEM = (OFF_MISC + 64 + 1024) > 120 * 1024 ? (OFF_MISC + 64 + 1024) : 120 * 1024;
+};
+
+template <int K, int CT>
+__global__ void __launch_bounds__(kThreads, 1)
+    ll_kernel(const __grid_constant__ CUtensorMap zmap, const __grid_constant__ CUtensorMap wmap,
+              long long N, int n_tiles, int n_chunks, float trouble2, float minLL,
+              float* __restrict__ ll2_out, float* __restrict__ ll_out,
+              double* __restrict__ llpart, int* __restrict__ err) {
+  using C = LlCfg<K, CT>;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = align1024(smem_raw);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + C::OFF_BAR);
+  uint64_t* z_full = bars + 0;
+  uint64_t* z_empty = bars + 1;
+  uint64_t* w_full = bars + 2;   // [2]
+  uint64_t* w_empty = bars + 4;  // [2]
+  uint64_t* s_full = bars + 6;   // [2]
+  uint64_t* s_empty = bars + 8;  // [2]
+  uint64_t* mma_done = bars + 10;
+  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(smem + C::OFF_MISC);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + C::OFF_MISC + 8);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    mbar_init(z_full, 1);
+    mbar_init(z_empty, 1);
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&w_full[i], 1);
+      mbar_init(&w_empty[i], 1);
+      mbar_init(&s_full[i], 1);
+      mbar_init(&s_empty[i], 4);
+    }
+    mbar_init(mma_done, 1);
+    *abort_flag = 0;
+    fence_mbar_init();
+  }
+  if (warp == 1) {
+    tmem_alloc(tmem_holder, 256);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_holder;
+  // tiles of this CTA: blockIdx.x, blockIdx.x + gridDim.x, ...
+  const int my_tiles = (n_tiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
+
+  if (warp == 0) {
+    if (lane == 0 && my_tiles > 0) {
+      prefetch_tmap(&zmap);
+      prefetch_tmap(&wmap);
+      int j = 0;
+      bool ok = true;
+      for (int it = 0; it < my_tiles && ok; ++it) {
+        const int tile = (int)blockIdx.x + it * (int)gridDim.x;
+        if (!mbar_wait(z_empty, (it & 1) ^ 1, abort_flag, kWaitLimit)) { ok = false; break; }
+        mbar_arrive_expect_tx(z_full, C::Z_BYTES);
+        for (int p = 0; p < 3; ++p)
+          for (int c = 0; c < C::KC; ++c)
+            tma_load_3d(smem + C::OFF_Z + p * C::Z_PLANE + c * 128 * 16, &zmap, 8 * c, tile * 128, p, z_full);
+        for (int ch = 0; ch < n_chunks; ++ch, ++j) {
+          const int ws = j & 1;
+          if (!mbar_wait(&w_empty[ws], ((j >> 1) & 1) ^ 1, abort_flag, kWaitLimit)) { ok = false; break; }
+          mbar_arrive_expect_tx(&w_full[ws], C::W_STAGE);
+          uint8_t* dst = smem + C::OFF_W + ws * C::W_STAGE;
+          for (int p = 0; p < 3; ++p)
+            for (int c = 0; c < C::KC; ++c)
+              tma_load_3d(dst + p * C::W_PLANE + c * CT * 16, &wmap, 8 * c, ch * CT, p, &w_full[ws]);
+        }
+      }
+      // drain: every issued copy must land before the CTA exits
+      if (!ok) {
+        mbar_drain(z_full, 0);
+        mbar_drain(z_full, 1);
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0 && my_tiles > 0) {
+      const uint32_t idesc = idesc_bf16(128, CT, false, false);
+      const uint32_t zb = smem_u32(smem + C::OFF_Z);
+      const uint32_t wb0 = smem_u32(smem + C::OFF_W);
+      int j = 0;
+      bool ok = true;
+      for (int it = 0; it < my_tiles && ok; ++it) {
+        if (!mbar_wait(z_full, it & 1, abort_flag, kWaitLimit)) { ok = false; break; }
+        for (int ch = 0; ch < n_chunks; ++ch, ++j) {
+          const int ws = j & 1, b = j & 1;
+          if (!mbar_wait(&w_full[ws], (j >> 1) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
+          if (!mbar_wait(&s_empty[b], ((j >> 1) & 1) ^ 1, abort_flag, kWaitLimit)) { ok = false; break; }
+          tc_fence_after();
+          const uint32_t wb = wb0 + ws * C::W_STAGE;
+          const uint32_t d = tmem + b * CT;
+          int acc = 0;
+#pragma unroll 1
+          for (int pr = 0; pr < 6; ++pr) {
+#pragma unroll
+            for (int q = 0; q < K / 16; ++q) {
+              const uint64_t a = smem_desc(zb + kProdZ[pr] * C::Z_PLANE + q * 2 * 128 * 16, 128 * 16, 128);
+              const uint64_t bd = smem_desc(wb + kProdW[pr] * C::W_PLANE + q * 2 * CT * 16, CT * 16, 128);
+              mma_ss(d, a, bd, idesc, acc);
+              acc = 1;
+            }
+          }
+          mma_commit(&s_full[b]);
+          mma_commit(&w_empty[ws]);
+          if (ch == n_chunks - 1) mma_commit(z_empty);
+        }
+      }
+      mma_commit(mma_done);
+      mbar_drain(mma_done, 0);
+    }
+  } else {
+    // epilogue: thread = frame row of the tile
+    const int q4 = warp & 3;
+    const int row = q4 * 32 + lane;
+    const uint32_t lane_off = (uint32_t)(q4 * 32) << 16;
+    double llsum = 0.0;
+    int j = 0;
+    bool ok = true;
+    for (int it = 0; it < my_tiles && ok; ++it) {
+      const int tile = (int)blockIdx.x + it * (int)gridDim.x;
+      float m = -INFINITY, sum = 0.0f;
+      for (int ch = 0; ch < n_chunks; ++ch, ++j) {
+        const int b = j & 1;
+        if (!mbar_wait(&s_full[b], (j >> 1) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
+        tc_fence_after();
+#pragma unroll
+        for (int sub = 0; sub < CT / 32; ++sub) {
+          uint32_t v[32];
+          tmem_ld32(tmem + lane_off + b * CT + 32 * sub, v);
+          tmem_ld_wait();
+          float mx = __uint_as_float(v[0]);
+#pragma unroll
+          for (int k = 1; k < 32; ++k) mx = fmaxf(mx, __uint_as_float(v[k]));
+          const float mn = fmaxf(m, mx);
+          if (mn > -INFINITY) {
+            float s = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 32; ++k) s += ex2(__uint_as_float(v[k]) - mn);
+            sum = sum * ex2(m - mn) + s;
+            m = mn;
+          }
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&s_empty[b]);
+      }
+      if (!ok) break;
+      const long long f = (long long)tile * 128 + row;
+      float l2 = m + lg2(sum);
+      const bool trouble = !(m > trouble2) || !isfinite(l2);
+      if (f < N) {
+        if (trouble) l2 = -INFINITY;
+        ll2_out[f] = l2;
+        const float lnat = trouble ? minLL : l2 * kLn2;
+        if (ll_out) ll_out[f] = lnat;
+        llsum += (double)lnat;
+      } else {
+        ll2_out[f] = __int_as_float(0x7fc00000);  // padding marker (NaN)
+      }
+    }
+    llpart[(size_t)blockIdx.x * 128 + row] = llsum;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && *abort_flag) atomicExch(err, 1);
+  if (warp == 1) {
+    tc_fence_after();
+    tmem_dealloc(tmem, 256);
+  }
+}
+
+// ------------------------------------------------------------------ statistics kernel
+
+template <int K, int FT>
+struct AccCfg {
+  static constexpr int KC = K / 8;
+  static constexpr int W_PLANE = 128 * K * 2;
+  static constexpr int Z_PLANE = FT * K * 2;
+  static constexpr int W_BYTES = 3 * W_PLANE;
+  static constexpr int Z_STAGE = 3 * Z_PLANE;
+  static constexpr int LL_STAGE = FT * 4;
+  static constexpr int OFF_W = 0;
+  static constexpr int OFF_Z = W_BYTES;
+  static constexpr int OFF_LL = OFF_Z + 2 * Z_STAGE;
+  static constexpr int OFF_BAR = OFF_LL + 2 * LL_STAGE;
+  static constexpr int OFF_MISC = OFF_BAR + 16 * 8;
+  static constexpr int SMEM = (OFF_MISC + 64 + 1024) > 120 * 1024 ? (OFF_MISC + 64 + 1024) : 120 * 1024;
+  static constexpr int D2_COL = 256;  // D2 buffers at 256 + 128 d
+};
+
+__device__ __forceinline__ float posterior(float s2, float l2, float minGamma, int single_comp) {
+  if (single_comp) return isnan(l2) ? 0.0f : 1.0f;
+  if (!isfinite(l2)) return 0.0f;
+  const float g = ex2(s2 - l2);
+  return g > minGamma ? g : 0.0f;
+}
+
+template <int K, int FT>
+__global__ void __launch_bounds__(kThreads, 1)
+    acc_kernel(const __grid_constant__ CUtensorMap zmap, const __grid_constant__ CUtensorMap wmap,
+               const float* __restrict__ ll2, int n_tiles, int n_chunks, int slices, int flush_every,
+               float minGamma, int single_comp, double* __restrict__ part, int* __restrict__ err) {
+  using C = AccCfg<K, FT>;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = align1024(smem_raw);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + C::OFF_BAR);
+  uint64_t* w_full = bars + 0;
+  uint64_t* z_full = bars + 1;   // [2]
+  uint64_t* z_empty = bars + 3;  // [2]
+  uint64_t* s_full = bars + 5;   // [2]
+  uint64_t* g_full = bars + 7;   // [2]
+  uint64_t* d_full = bars + 9;   // [2]
+  uint64_t* d_empty = bars + 11; // [2]
+  uint64_t* mma_done = bars + 13;
+  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(smem + C::OFF_MISC);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + C::OFF_MISC + 8);
+  float* ll_s = reinterpret_cast<float*>(smem + C::OFF_LL);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int chunk = (int)blockIdx.x % n_chunks, slice = (int)blockIdx.x / n_chunks;
+  const int per = (n_tiles + slices - 1) / slices;
+  const int t0 = slice * per;
+  const int nt = max(0, min(n_tiles, t0 + per) - t0);
+
+  if (threadIdx.x == 0) {
+    mbar_init(w_full, 1);
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&z_full[i], 1);
+      mbar_init(&z_empty[i], 1);
+      mbar_init(&s_full[i], 1);
+      mbar_init(&g_full[i], 4);
+      mbar_init(&d_full[i], 1);
+      mbar_init(&d_empty[i], 4);
+    }
+    mbar_init(mma_done, 1);
+    *abort_flag = 0;
+    fence_mbar_init();
+  }
+  if (warp == 1) {
+    tmem_alloc(tmem_holder, 512);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_holder;
+
+  if (warp == 0) {
+    if (lane == 0 && nt > 0) {
+      prefetch_tmap(&zmap);
+      prefetch_tmap(&wmap);
+      mbar_arrive_expect_tx(w_full, C::W_BYTES);
+      for (int p = 0; p < 3; ++p)
+        for (int c = 0; c < C::KC; ++c)
+          tma_load_3d(smem + C::OFF_W + p * C::W_PLANE + c * 128 * 16, &wmap, 8 * c, chunk * 128, p, w_full);
+      int issued = 0;
+      for (int i = 0; i < nt; ++i) {
+        const int s = i & 1;
+        if (!mbar_wait(&z_empty[s], ((i >> 1) & 1) ^ 1, abort_flag, kWaitLimit)) break;
+        mbar_arrive_expect_tx(&z_full[s], C::Z_STAGE + C::LL_STAGE);
+        uint8_t* zs = smem + C::OFF_Z + s * C::Z_STAGE;
+        const int row = (t0 + i) * FT;
+        for (int p = 0; p < 3; ++p)
+          for (int c = 0; c < C::KC; ++c)
+            tma_load_3d(zs + p * C::Z_PLANE + c * FT * 16, &zmap, 8 * c, row, p, &z_full[s]);
+        bulk_load(ll_s + s * FT, ll2 + row, FT * 4, &z_full[s]);
+        issued = i + 1;
+      }
+      if (*abort_flag) {  // drain the copies of the last two issued tiles
+        mbar_drain(w_full, 0);
+        for (int i = max(0, issued - 2); i < issued; ++i) mbar_drain(&z_full[i & 1], (i >> 1) & 1);
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0 && nt > 0) {
+      const uint32_t idesc_l = idesc_bf16(128, FT, false, false);
+      const uint32_t idesc_s = idesc_bf16(128, K, false, true);
+      const uint32_t wb = smem_u32(smem + C::OFF_W);
+      const uint32_t zb0 = smem_u32(smem + C::OFF_Z);
+      bool ok = mbar_wait(w_full, 0, abort_flag, kWaitLimit);
+      auto logits = [&](int i) {
+        const uint32_t zb = zb0 + (i & 1) * C::Z_STAGE;
+        const uint32_t d = tmem + (i & 1) * FT;
+        int acc = 0;
+#pragma unroll 1
+        for (int pr = 0; pr < 6; ++pr) {
+#pragma unroll
+          for (int q = 0; q < K / 16; ++q) {
+            const uint64_t a = smem_desc(wb + kProdW[pr] * C::W_PLANE + q * 2 * 128 * 16, 128 * 16, 128);
+            const uint64_t bd = smem_desc(zb + kProdZ[pr] * C::Z_PLANE + q * 2 * FT * 16, FT * 16, 128);
+            mma_ss(d, a, bd, idesc_l, acc);
+            acc = 1;
+          }
+        }
+        mma_commit(&s_full[i & 1]);
+      };
+      auto stats = [&](int j) -> bool {
+        const int b = j & 1;
+        if (!mbar_wait(&g_full[b], (j >> 1) & 1, abort_flag, kWaitLimit)) return false;
+        tc_fence_after();
+        const int period = j / flush_every, dsel = period & 1;
+        const bool fresh = (j % flush_every) == 0;
+        if (fresh) {
+          if (!mbar_wait(&d_empty[dsel], ((period >> 1) & 1) ^ 1, abort_flag, kWaitLimit)) return false;
+          tc_fence_after();
+        }
+        const uint32_t dcol = tmem + C::D2_COL + 128 * dsel;
+        const uint32_t gb = tmem + b * FT;
+        const uint32_t zb = zb0 + (j & 1) * C::Z_STAGE;
+        int acc = fresh ? 0 : 1;
+#pragma unroll
+        for (int q = 0; q < FT / 16; ++q) {
+          const uint32_t hi = gb + 32 * (q >> 1) + 8 * (q & 1);
+          const uint32_t lo = hi + 16;
+          // B = Z as [N = K columns] x [K' = frames], MN-major: LBO along frames, SBO along columns
+          const uint64_t z1 = smem_desc(zb + 0 * C::Z_PLANE + q * 2 * 128, 128, FT * 16);
+          const uint64_t z2 = smem_desc(zb + 1 * C::Z_PLANE + q * 2 * 128, 128, FT * 16);
+          mma_ts(dcol, lo, z1, idesc_s, acc);
+          acc = 1;
+          mma_ts(dcol, hi, z2, idesc_s, 1);
+          mma_ts(dcol, hi, z1, idesc_s, 1);
+        }
+        mma_commit(&z_empty[j & 1]);
+        if ((j % flush_every) == flush_every - 1 || j == nt - 1) mma_commit(&d_full[dsel]);
+        return true;
+      };
+      for (int i = 0; i < nt && ok; ++i) {
+        if (!mbar_wait(&z_full[i & 1], (i >> 1) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
+        tc_fence_after();
+        logits(i);
+        if (i > 0 && !stats(i - 1)) { ok = false; break; }
+      }
+      if (ok) stats(nt - 1);
+      mma_commit(mma_done);
+      mbar_drain(mma_done, 0);
+    }
+  } else if (nt > 0) {
+    const int q4 = warp & 3;
+    const int row = q4 * 32 + lane;
+    const uint32_t lane_off = (uint32_t)(q4 * 32) << 16;
+    double* mypart = part + ((size_t)blockIdx.x * 128 + row) * K;
+    bool first_flush = true;
+    for (int i = 0; i < nt; ++i) {
+      const int b = i & 1;
+      if (!mbar_wait(&z_full[i & 1], (i >> 1) & 1, abort_flag, kWaitLimit)) break;
+      if (!mbar_wait(&s_full[b], (i >> 1) & 1, abort_flag, kWaitLimit)) break;
+      tc_fence_after();
+      const float* lls = ll_s + (i & 1) * FT;
+#pragma unroll 1
+      for (int c = 0; c < FT / 32; ++c) {
+        uint32_t v[32];
+        tmem_ld32(tmem + lane_off + b * FT + 32 * c, v);
+        tmem_ld_wait();
+        uint32_t hi[16], lo[16];
+#pragma unroll
+        for (int k = 0; k < 32; k += 2) {
+          const float g0 = posterior(__uint_as_float(v[k]), lls[32 * c + k], minGamma, single_comp);
+          const float g1 = posterior(__uint_as_float(v[k + 1]), lls[32 * c + k + 1], minGamma, single_comp);
+          const uint32_t h = pack_bf16(g0, g1);
+          const float h0 = __uint_as_float(h << 16), h1 = __uint_as_float(h & 0xffff0000u);
+          hi[k >> 1] = h;
+          lo[k >> 1] = pack_bf16(g0 - h0, g1 - h1);
+        }
+        tmem_st16(tmem + lane_off + b * FT + 32 * c, hi);
+        tmem_st16(tmem + lane_off + b * FT + 32 * c + 16, lo);
+      }
+      tmem_st_wait();
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&g_full[b]);
+      if ((i % flush_every) == flush_every - 1 || i == nt - 1) {
+        const int p = i / flush_every, dsel = p & 1;
+        if (!mbar_wait(&d_full[dsel], (p >> 1) & 1, abort_flag, kWaitLimit)) break;
+        tc_fence_after();
+#pragma unroll 1
+        for (int c = 0; c < K / 16; ++c) {
+          uint32_t r[16];
+          tmem_ld16(tmem + lane_off + C::D2_COL + 128 * dsel + 16 * c, r);
+          tmem_ld_wait();
+#pragma unroll
+          for (int k = 0; k < 16; ++k) {
+            const double v = (double)__uint_as_float(r[k]);
+            if (first_flush) mypart[16 * c + k] = v;
+            else mypart[16 * c + k] += v;
+          }
+        }
+        first_flush = false;
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&d_empty[dsel]);
+      }
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && *abort_flag) atomicExch(err, 1);
+  if (warp == 1) {
+    tc_fence_after();
+    tmem_dealloc(tmem, 512);
+  }
+}
+
+// part [cta][128][K] -> stats (caller order), summing CTAs of each chunk in slice order.
+__global__ void reduce_kernel(int M, int D, int K, int Mact, int n_chunks, int slices, int n_tiles,
+                              const int* __restrict__ comp_of_row, const double* __restrict__ part,
+                              int flags, double* __restrict__ stats) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)Mact * K) return;
+  const int r = (int)(t / K), e = (int)(t - (long long)r * K);
+  if (e > 2 * D) return;
+  const int ch = r / 128, rr = r - ch * 128;
+  const int per = (n_tiles + slices - 1) / slices;
+  double s = 0.0;
+  for (int sl = 0; sl < slices; ++sl) {
+    if (sl * per >= n_tiles) break;
+    s += part[(((size_t)sl * n_chunks + ch) * 128 + rr) * K + e];
+  }
+  const int m = comp_of_row[r];
+  if (e == 2 * D) stats[m] += s;
+  else if (e < D) { if (flags & GMM_ACC_MEAN) stats[(size_t)M + (size_t)m * D + e] += s; }
+  else if (flags & GMM_ACC_VAR) stats[(size_t)M + (size_t)M * D + (size_t)m * D + (e - D)] += s;
+}
+
+__global__ void ll_total_kernel(int n, const double* __restrict__ llpart, double* __restrict__ tot) {
+  __shared__ double red[32];
+  double v = 0.0;
+  for (int k = threadIdx.x; k < n; k += blockDim.x) v += llpart[k];
+  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += red[k];
+    *tot += s;
+  }
+}
+
+// ------------------------------------------------------------------ host side
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    cudaDriverEntryPointQueryResult q;
+    void* p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+// 3-D map over [3 planes][rows][K] bf16 with a box of 8 columns x box_rows rows x 1 plane:
+// each copy lands as box_rows consecutive 16-byte rows, i.e. one K-chunk column of the
+// no-swizzle core-matrix layout.
+int make_map(Ctx* c, CUtensorMap* map, const uint16_t* base, long long rows, int K, int box_rows) {
+  auto fn = encode_fn();
+  if (!fn) return fail(c, GMM_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+  cuuint64_t dims[3] = {(cuuint64_t)K, (cuuint64_t)rows, 3};
+  cuuint64_t strides[2] = {(cuuint64_t)K * 2, (cuuint64_t)rows * K * 2};
+  cuuint32_t box[3] = {8, (cuuint32_t)box_rows, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, (void*)base, dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(c, GMM_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+  return GMM_OK;
+}
+
+template <int K>
+int launch_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
+  constexpr int FT = tile_frames(K);
+  constexpr int CT = tile_frames(K);
+  using LC = LlCfg<K, CT>;
+  using AC = AccCfg<K, FT>;
+  const long long Npad = c->tcx.Npad;
+  const int n_tiles_ll = (int)(Npad / 128);
+  const int n_chunks_ll = c->tcm.Mpad / CT;
+  int grid_ll = std::min(n_tiles_ll, c->sms);
+  if (grid_ll < 1) grid_ll = 1;
+  size_t need = (size_t)grid_ll * 128;
+  if (need > c->tc_llpart_cap) {
+    dfree(c, c->tc_llpart, c->tc_llpart_cap * sizeof(double));
+    c->tc_llpart = nullptr;
+    int rc = dalloc(c, (void**)&c->tc_llpart, need * sizeof(double), "tc llpart");
+    if (rc) return rc;
+    c->tc_llpart_cap = need;
+  }
+  static bool attr_set_ll = false, attr_set_acc = false;
+  if (!attr_set_ll) {
+    cudaFuncSetAttribute(ll_kernel<K, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize, LC::SMEM);
+    attr_set_ll = true;
+  }
+  const float trouble2 = (float)(c->minLL * kLog2e);
+  {
+    GMM_LAUNCH(c, "tc_ll_kernel");
+    ll_kernel<K, CT><<<grid_ll, kThreads, LC::SMEM, c->stream>>>(
+        c->tm_z128, c->tm_wct, c->N, n_tiles_ll, n_chunks_ll, trouble2, c->minLL, c->tcm.ll2,
+        ll_out_dev, c->tc_llpart, c->tc_err);
+  }
+  if (!want_stats) return GMM_OK;
+  {
+    GMM_LAUNCH(c, "tc_ll_total_kernel");
+    ll_total_kernel<<<1, 1024, 0, c->stream>>>(grid_ll * 128, c->tc_llpart,
+                                                c->stats + (size_t)c->M * (1 + 2 * c->D));
+  }
+  const int n_tiles = (int)(Npad / FT);
+  const int n_chunks = c->tcm.Mpad / 128;
+  int slices = c->sms / n_chunks;
+  if (slices < 1) slices = 1;
+  if (slices > n_tiles) slices = n_tiles;
+  const int grid = n_chunks * slices;
+  size_t pneed = (size_t)grid * 128 * K * sizeof(double);
+  if (pneed > c->tcpart_cap) {
+    dfree(c, c->tcpart, c->tcpart_cap);
+    c->tcpart = nullptr;
+    c->tcpart_cap = 0;
+    int rc = dalloc(c, (void**)&c->tcpart, pneed, "tc partial statistics");
+    if (rc) return rc;
+    c->tcpart_cap = pneed;
+  }
+  if (!attr_set_acc) {
+    cudaFuncSetAttribute(acc_kernel<K, FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, AC::SMEM);
+    attr_set_acc = true;
+  }
+  {
+    GMM_LAUNCH(c, "tc_acc_kernel");
+    acc_kernel<K, FT><<<grid, kThreads, AC::SMEM, c->stream>>>(
+        c->tm_zft, c->tm_w128, c->tcm.ll2, n_tiles, n_chunks, slices, 16, c->minGamma, c->Mact == 1,
+        c->tcpart, c->tc_err);
+  }
+  {
+    GMM_LAUNCH(c, "tc_reduce_kernel");
+    long long tot = (long long)c->Mact * K;
+    reduce_kernel<<<(int)((tot + 255) / 256), 256, 0, c->stream>>>(
+        c->M, c->D, K, c->Mact, n_chunks, slices, n_tiles, c->tcm.comp_of_row, c->tcpart, flags, c->stats);
+  }
+  return GMM_OK;
+}
+
+}  // namespace
+
+int tc_supported(int D) { return D >= 1 && D <= 63; }
+
+static int tc_K(int D) { return (2 * D + 1 + 15) / 16 * 16; }
+
+int tc_prepare_features(Ctx* c) {
+  const int K = tc_K(c->D);
+  const long long Npad = (c->N + 127) / 128 * 128;
+  const size_t bytes = (size_t)3 * Npad * K * sizeof(uint16_t);
+  if (c->tcx.planes == nullptr || c->tcx.Npad != Npad || c->tcx.K != K) {
+    dfree(c, c->tcx.planes, (size_t)3 * c->tcx.Npad * c->tcx.K * sizeof(uint16_t));
+    c->tcx.planes = nullptr;
+    int rc = dalloc(c, (void**)&c->tcx.planes, bytes, "tensor-core feature planes");
+    if (rc) return rc;
+    c->tcx.Npad = Npad;
+    c->tcx.K = K;
+    dfree(c, c->tcm.ll2, 0);
+    c->tcm.ll2 = nullptr;
+    rc = dalloc(c, (void**)&c->tcm.ll2, sizeof(float) * (size_t)Npad, "tensor-core frame LSE");
+    if (rc) return rc;
+  }
+  {
+    GMM_LAUNCH(c, "tc_features_kernel");
+    const long long tot = Npad * K;
+    features_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(c->X, c->N, Npad, c->D, K,
+                                                                         c->tcx.planes);
+  }
+  int rc = make_map(c, &c->tm_z128, c->tcx.planes, Npad, K, 128);
+  if (!rc) rc = make_map(c, &c->tm_zft, c->tcx.planes, Npad, K, tile_frames(K));
+  if (rc) return rc;
+  c->tcx_valid = true;
+  return GMM_OK;
+}
+
+int tc_prepare_model(Ctx* c) {
+  const int K = tc_K(c->D);
+  const int Mpad = (c->Mact + 127) / 128 * 128;
+  if (c->tcm.planes == nullptr || c->tcm.Mpad != Mpad || c->tcm.K != K) {
+    dfree(c, c->tcm.planes, 0);
+    dfree(c, c->tcm.comp_of_row, 0);
+    c->tcm.planes = nullptr;
+    c->tcm.comp_of_row = nullptr;
+    int rc = dalloc(c, (void**)&c->tcm.planes, (size_t)3 * Mpad * K * sizeof(uint16_t), "tensor-core model planes");
+    if (!rc) rc = dalloc(c, (void**)&c->tcm.comp_of_row, sizeof(int) * Mpad, "row map");
+    if (rc) return rc;
+    c->tcm.Mpad = Mpad;
+    c->tcm.K = K;
+  }
+  {
+    GMM_LAUNCH(c, "tc_model_kernel");
+    const long long tot = (long long)Mpad * K;
+    model_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(
+        c->D, K, c->Mact, Mpad, c->act, c->w, c->mu, c->var, c->tcm.planes, c->tcm.comp_of_row);
+  }
+  int rc = make_map(c, &c->tm_w128, c->tcm.planes, Mpad, K, 128);
+  if (!rc) rc = make_map(c, &c->tm_wct, c->tcm.planes, Mpad, K, tile_frames(K));
+  return rc;
+}
+
+int tc_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
+  if (!tc_supported(c->D)) return fail(c, GMM_ERR_UNSUPPORTED, "tensor-core path supports 1 <= D <= 63");
+  if (c->N == 0) return GMM_OK;
+  if (!c->tc_err) {
+    int rc = dalloc(c, (void**)&c->tc_err, sizeof(int), "tc error flag");
+    if (rc) return rc;
+    cudaMemsetAsync(c->tc_err, 0, sizeof(int), c->stream);
+    int dev;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, dev);
+  }
+  int rc;
+  if (!c->tcx_valid || c->tcx.planes == nullptr) {
+    rc = tc_prepare_features(c);
+    if (rc) return rc;
+  }
+  rc = tc_prepare_model(c);  // model may change every iteration
+  if (rc) return rc;
+  switch (c->tcm.K) {
+    case 16: rc = launch_estep<16>(c, flags, want_stats, ll_out_dev); break;
+    case 32: rc = launch_estep<32>(c, flags, want_stats, ll_out_dev); break;
+    case 48: rc = launch_estep<48>(c, flags, want_stats, ll_out_dev); break;
+    case 64: rc = launch_estep<64>(c, flags, want_stats, ll_out_dev); break;
+    case 80: rc = launch_estep<80>(c, flags, want_stats, ll_out_dev); break;
+    case 96: rc = launch_estep<96>(c, flags, want_stats, ll_out_dev); break;
+    case 112: rc = launch_estep<112>(c, flags, want_stats, ll_out_dev); break;
+    case 128: rc = launch_estep<128>(c, flags, want_stats, ll_out_dev); break;
+    default: return fail(c, GMM_ERR_UNSUPPORTED, "tensor-core path: unsupported K");
+  }
+  if (rc) return rc;
+  // surface a bounded-wait expiry as an error status (the context stays usable)
+  int herr = 0;
+  cudaMemcpyAsync(&herr, c->tc_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  rc = sync(c, "tensor-core E-step");
+  if (rc) return rc;
+  if (herr) {
+    cudaMemsetAsync(c->tc_err, 0, sizeof(int), c->stream);
+    return fail(c, GMM_ERR_TIMEOUT, "tensor-core E-step: a bounded device wait expired");
+  }
+  return GMM_OK;
+}
+
+}  // namespace gmm

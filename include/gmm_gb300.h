@@ -1,0 +1,133 @@
+/*
+ * gmm_gb300 -- C ABI of the GB300 (sm_103a) GMM statistics engine.
+ *
+ * One handle = one CUDA stream on one device with a device-resident model, feature block,
+ * statistics and scratch. Every entry point returns a status (GMM_OK = 0); on failure
+ * gmm_last_error(h) gives the message. Calls on one handle must not run concurrently from
+ * several host threads; different handles are independent. All calls are synchronous from the
+ * caller's point of view (they return after the device work finished) unless stated otherwise.
+ *
+ * The entry points replace the reference's thin GPU layer GMMStatsEstimator_GPU
+ * (GMM/lib_bmssr/trainer/CU_GMMStatsEstimator_CUDA.h:125-183) and the host estimator above it
+ * (GMMStatsEstimator_CUDA, OL_GMMStatsEstimator_CUDA.h:39-105); the re-estimation entry points
+ * replace CModelAdapt's UpdateModelEM / UpdateModelMAP / MLLR routines
+ * (GMM/lib_bmssr/trainer/OL_ModelAdapt.cpp). Citations below give the exact member each one
+ * stands in for.
+ *
+ * Layouts: features X are row-major float32 [N][D]; a model is w[M], mu[M][D], var[M][D]
+ * (diagonal covariances) in the caller's component order. Components with w <= 0 are skipped,
+ * which is what the reference does after GMModel::RearrangeMixtures moved them behind the
+ * others; statistics come back in the caller's order (zero for skipped components).
+ */
+#ifndef GMM_GB300_H
+#define GMM_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gmm_ctx* gmm_handle;
+
+/* status codes */
+#define GMM_OK 0
+#define GMM_ERR_ARG 1         /* bad argument (null pointer, size out of range) */
+#define GMM_ERR_CUDA 2        /* CUDA runtime error; the message names the call */
+#define GMM_ERR_STATE 3       /* call out of order (e.g. no model or features uploaded) */
+#define GMM_ERR_MODEL 4       /* a variance below min_var (insertModel throws, OL_GMMStatsEstimator.cpp:287-296) */
+#define GMM_ERR_NOMEM 5       /* device allocation refused, or over the handle's memory budget */
+#define GMM_ERR_UNSUPPORTED 6 /* configuration outside the implemented range (e.g. D too large) */
+#define GMM_ERR_MLLR 7        /* MLLR invertibility conditions fail (OL_ModelAdapt.cpp:1851-1878) */
+#define GMM_ERR_TIMEOUT 8     /* a bounded device-side wait expired */
+
+/* precision modes */
+#define GMM_PREC_FP32 0 /* plain FP32 replica of the reference CPU arithmetic */
+#define GMM_PREC_TC 1   /* tcgen05 tensor-core fused path, split-bf16 operands, FP32 accumulate */
+
+/* accumulation flags (GMMStatsEstimator::setAccFlags, OL_GMMStatsEstimator.h:107-113) */
+#define GMM_ACC_MEAN 1
+#define GMM_ACC_VAR 2
+#define GMM_ACC_PROBS_ONLY 4
+
+/* Create a handle on `device` (GMMStatsEstimator_GPU::GMMStatsEstimator_GPU(int GPU_id),
+ * CU_GMMStatsEstimator_CUDA.cu; context creation :977-1016). */
+int gmm_create(int device, gmm_handle* out);
+int gmm_destroy(gmm_handle h);
+/* Message of the last failed call on h (or of the last failed gmm_create when h is NULL). */
+const char* gmm_last_error(gmm_handle h);
+
+/* Estimator knobs: GMMStatsEstimator::_minLogLike, _minGamma, _min_var
+ * (OL_GMMStatsEstimator.h:59-61; defaults -1e20, 1e-4, 1e-6). */
+int gmm_set_options(gmm_handle h, float min_loglike, float min_gamma, float min_var);
+int gmm_set_precision(gmm_handle h, int mode);
+/* Device-memory budget for this handle in bytes (0 = unlimited); allocations past it fail with
+ * GMM_ERR_NOMEM (the reference pre-checks memory in getNSamples2GPU,
+ * CU_GMMStatsEstimator_CUDA.cu:1136-1225). */
+int gmm_set_memory_budget(gmm_handle h, size_t bytes);
+/* The handle's cudaStream_t, for callers that time or order work around it. */
+int gmm_get_stream(gmm_handle h, void** stream);
+
+/* Model upload and precompute: insertModel (OL_GMMStatsEstimator.cpp:234-313) +
+ * GMMStatsEstimator_GPU::uploadModel (CU_GMMStatsEstimator_CUDA.cu:284-318). */
+int gmm_upload_model(gmm_handle h, int M, int D, const float* w, const float* mu, const float* var);
+/* Prior model for MAP (the UBM argument of CModelAdapt::UpdateModelMAP, OL_ModelAdapt.cpp:993). */
+int gmm_set_prior(gmm_handle h, const float* w, const float* mu, const float* var);
+/* Copy the device-resident model back (w[M], mu[M*D], var[M*D]). */
+int gmm_read_model(gmm_handle h, float* w, float* mu, float* var);
+
+/* Feature upload: alignVectors + uploadParam (OL_GMMStatsEstimator_CUDA.cpp:291-328,
+ * CU_GMMStatsEstimator_CUDA.cu:431-470). The host variant copies from host memory; the device
+ * variant keeps a reference to caller-owned device memory (it must outlive its use). */
+int gmm_upload_features(gmm_handle h, const float* X, long long N, int D);
+int gmm_upload_features_device(gmm_handle h, const float* dX, long long N, int D);
+
+/* E-step over the resident features: accumulateStatsMT (OL_GMMStatsEstimator.cpp:884-971) /
+ * GMMStatsEstimator_CUDA::accumulateStatsMT (OL_GMMStatsEstimator_CUDA.cpp:395-511).
+ * Statistics are zeroed first and returned in FP64: n[M], F[M*D], S[M*D] (any of them may be
+ * NULL), the total log-likelihood and the number of frames. */
+int gmm_accumulate(gmm_handle h, int flags, double* n, double* F, double* S, double* tot_loglike,
+                   long long* tot_frames);
+/* Same E-step, statistics left on the device for the M-step entry points below. */
+int gmm_accumulate_device(gmm_handle h, int flags);
+int gmm_read_stats(gmm_handle h, double* n, double* F, double* S, double* tot_loglike,
+                   long long* tot_frames);
+
+/* Per-frame log-likelihoods: compVecsLogLikeMT (OL_GMMStatsEstimator.cpp:811-879) /
+ * compLogLikes + getLogLikes (CU_GMMStatsEstimator_CUDA.cu:606-643). out: N floats (host). */
+int gmm_loglikes(gmm_handle h, float* out);
+
+/* M-step on the device statistics (FP64 math, float model), in place on the resident model:
+ * CModelAdapt::UpdateModelEM (OL_ModelAdapt.cpp:823-949). *alive = components left with
+ * non-zero weight. */
+int gmm_em_update(gmm_handle h, int up_weight, int up_mean, int up_var, int* alive);
+/* CModelAdapt::UpdateModelMAP with tau > 0 (OL_ModelAdapt.cpp:1024-1106) against the prior. */
+int gmm_map_update(gmm_handle h, int tau, int up_weight, int up_mean, int up_var);
+/* `iters` EM iterations entirely on the device (CModelAdapt::IterEM with tau = 0,
+ * OL_ModelAdapt.cpp:1276-1296): each iteration moves zero-weight components behind the others
+ * as insertModel does, accumulates and updates. ll[i] = total log-likelihood of iteration i.
+ * The resident model is left in the reference's final component order. */
+int gmm_em_iterate(gmm_handle h, int iters, int up_weight, int up_mean, int up_var, double* ll,
+                   int* alive);
+
+/* Global MLLR mean transform from the device statistics (mean statistics required):
+ * CModelAdapt::ComputeW_MLLR + ComputeKiGi_MLLR + MATRIX::Invert (OL_ModelAdapt.cpp:1417-1581,
+ * Matrix4_LMa.cpp:2232-2300), with the UBM-based initialisation of prepareKiGiInitMatrices
+ * (:1484-1523) from the prior when ubm_init != 0. W: D x (D+1) row-major FP64 (host). */
+int gmm_mllr_estimate(gmm_handle h, int ubm_init, double* W);
+/* CModelAdapt::AdaptModelMLLR (OL_ModelAdapt.cpp:1583-1612): resident means <- A mu + b. */
+int gmm_mllr_apply(gmm_handle h, const double* W);
+
+/* Per-kernel device time accounting (CUDA events on the handle's stream; the reference's
+ * GPU_CUDA_TIMER, CU_GMMStatsEstimator_CUDA.cu:50-55). gmm_profile_read fills up to `cap`
+ * entries of names/milliseconds/launch counts and returns the number of kernels seen. */
+int gmm_profile_enable(gmm_handle h, int on);
+int gmm_profile_reset(gmm_handle h);
+int gmm_profile_read(gmm_handle h, int cap, const char** names, double* ms, long long* launches);
+/* Number of kernel launches this handle issued since creation (all kernels). */
+long long gmm_launch_count(gmm_handle h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,111 @@
+"""Generates the golden fixtures in this directory from the reference itself.
+
+Run where the reference sources are present (they are read in place, never copied):
+
+    python tests/golden/make_golden.py [--ref-root /root/reference/GMM]
+
+It builds ``oracle/_ref/libgmmref.so`` (the reference CPU estimator and CModelAdapt compiled
+from their own sources, see oracle/Makefile) and records its outputs on small inputs:
+
+* ``example.npz``  -- the first 1000 frames of the reference's example/data.bin, the
+  example/myModel.gmm model, the matching 6-digit values of example/data.logL, and the
+  reference's full-precision per-frame log-likelihoods and E-step statistics (1 and 4 threads).
+* ``em_small.npz`` -- seeded C1-style data (N=2048, D=39, 16 components): three EM iterations
+  of CModelAdapt::IterEM (per-iteration total log-likelihood and final model), and the first
+  E-step's statistics at 4 threads.
+* ``edge.npz``     -- zero-weight components (reordering), a single-component model, N < 100
+  (single-thread path), an outlier frame (numerical-stability branch), D = 1, and an EM update
+  that kills an under-occupied component.
+* ``map_mllr.npz`` -- mean-only MAP (tau = 16) and one global MLLR transform, with and without
+  the UBM-based initialisation.
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import oracle as O  # noqa: E402
+from gmm_gb300 import formats, synth  # noqa: E402
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref-root", default="/root/reference/GMM")
+    a = ap.parse_args()
+    O.REF_SRC = os.path.join(a.ref_root, "lib_bmssr")
+    O.build(ref=True)
+
+    # ---- example/ ---------------------------------------------------------------
+    ex = os.path.join(a.ref_root, "example")
+    X = formats.read_raw(os.path.join(ex, "data.bin"))[:1000]
+    g = formats.read_gmm_txt(os.path.join(ex, "myModel.gmm"))
+    with open(os.path.join(ex, "data.logL")) as f:
+        f.readline()
+        ll_file = np.array(f.read().split()[:1000], np.float64)
+    ll_ref = O.ref_loglikes(X, g.w, g.mu, g.var, threads=4)
+    s1 = O.ref_accumulate(X, g.w, g.mu, g.var, threads=1)
+    s4 = O.ref_accumulate(X, g.w, g.mu, g.var, threads=4)
+    np.savez_compressed(os.path.join(HERE, "example.npz"), X=X, w=g.w, mu=g.mu, var=g.var,
+                        ll_file=ll_file, ll_ref=ll_ref,
+                        n1=s1["n"], F1=s1["F"], S1=s1["S"], totLL1=s1["totLL"],
+                        n4=s4["n"], F4=s4["F"], S4=s4["S"], totLL4=s4["totLL"])
+
+    # ---- EM on seeded C1-style data --------------------------------------------
+    X, w, mu, var = synth.config_em(11, 2048, 39, 16, 16)
+    st = O.ref_accumulate(X, w, mu, var, threads=4)
+    ew, emu, evar, ell = O.ref_em(X, w, mu, var, 3, threads=4)
+    np.savez_compressed(os.path.join(HERE, "em_small.npz"), X=X, w=w, mu=mu, var=var,
+                        n=st["n"], F=st["F"], S=st["S"], totLL=st["totLL"],
+                        em_ll=ell, em_w=ew, em_mu=emu, em_var=evar)
+
+    # ---- edge cases -------------------------------------------------------------
+    out = {}
+    gw, gmu, gvar = synth.generator_gmm(21, 8, 6)
+    Xe = synth.sample_gmm(22, gw, gmu, gvar, 600)
+    wz = gw.copy(); wz[[1, 5]] = 0.0
+    wz /= wz.sum()
+    s = O.ref_accumulate(Xe, wz, gmu, gvar, threads=3)
+    out.update(zw_X=Xe, zw_w=wz, zw_mu=gmu, zw_var=gvar, zw_order=s["order"], zw_n=s["n"],
+               zw_F=s["F"], zw_S=s["S"], zw_totLL=s["totLL"])
+    s = O.ref_accumulate(Xe, gw[:1] * 0 + 1, gmu[:1], gvar[:1], threads=2)
+    out.update(m1_n=s["n"], m1_F=s["F"], m1_S=s["S"], m1_totLL=s["totLL"])
+    s = O.ref_accumulate(Xe[:50], gw, gmu, gvar, threads=4)
+    out.update(n50_n=s["n"], n50_F=s["F"], n50_S=s["S"], n50_totLL=s["totLL"])
+    Xo = Xe[:200].copy(); Xo[17] = 1e19
+    s = O.ref_accumulate(Xo, gw, gmu, gvar, threads=2)
+    out.update(out_X=Xo, out_n=s["n"], out_F=s["F"], out_S=s["S"], out_totLL=s["totLL"])
+    out.update(out_ll=O.ref_loglikes(Xo, gw, gmu, gvar, threads=2))
+    X1 = Xe[:, :1].copy()
+    s = O.ref_accumulate(X1, gw, gmu[:, :1], gvar[:, :1], threads=2)
+    out.update(d1_n=s["n"], d1_F=s["F"], d1_S=s["S"], d1_totLL=s["totLL"])
+    # an init whose last component sits far from the data: EM kills it (occupancy < 2)
+    Xk, wk, muk, vark = synth.config_em(23, 800, 6, 4, 5)
+    muk[4] = 50.0
+    kw, kmu, kvar, kll = O.ref_em(Xk, wk, muk, vark, 2, threads=2)
+    out.update(kill_X=Xk, kill_w0=wk, kill_mu0=muk, kill_var0=vark, kill_w=kw, kill_mu=kmu,
+               kill_var=kvar, kill_ll=kll)
+    np.savez_compressed(os.path.join(HERE, "edge.npz"), **out)
+
+    # ---- MAP and MLLR -----------------------------------------------------------
+    uw, umu, uvar = synth.generator_gmm(31, 32, 12)
+    Xs = synth.sample_gmm(32, uw, umu + 0.3, uvar, 4000)
+    mw, mmu, mvar, mll = O.ref_map(Xs, uw, umu, uvar, 16, iters=1, upM=True, threads=2)
+    W0, amu0 = O.ref_mllr(Xs, uw, umu, uvar, ubm_init=False, threads=2)
+    W1, amu1 = O.ref_mllr(Xs, uw, umu, uvar, ubm_init=True, threads=2)
+    np.savez_compressed(os.path.join(HERE, "map_mllr.npz"), X=Xs, w=uw, mu=umu, var=uvar,
+                        map_w=mw, map_mu=mmu, map_var=mvar, map_ll=mll,
+                        mllr_W0=W0, mllr_mu0=amu0, mllr_W1=W1, mllr_mu1=amu1)
+    for fn in sorted(os.listdir(HERE)):
+        if fn.endswith(".npz"):
+            print(fn, os.path.getsize(os.path.join(HERE, fn)))
+
+
+if __name__ == "__main__":
+    main()
