@@ -2,7 +2,8 @@
 //
 // The diagonal-covariance log-likelihood is a contraction:
 //   s_fm = sum_k Z_fk W_km,  Z_f = [x_f, x_f^2, 1, 0...],
-//   W_m  = log2(e) * [mu_m / var_m, -1 / (2 var_m), log w_m - D/2 log 2pi - 1/2 sum log var_m, 0...]
+//   W_m  = log2(e) * [mu_m / var_m, -1 / (2 var_m), c_m, 0...],
+//   c_m  = log w_m - D/2 log 2pi - 1/2 sum log var_m - 1/2 sum mu_m^2 / var_m
 // (log2 units), K = 2D+1 padded to a multiple of 16. Z and W are each held as three bf16 planes
 // (v = p1 + p2 + p3, each plane the bf16 rounding of what the previous ones left), and the
 // contraction sums the six plane products p_i q_j with i + j <= 4 into an FP32 TMEM
@@ -106,9 +107,13 @@ __global__ void model_kernel(int D, int K, int Mact, int Mpad, const int* __rest
     if (k < D) v = kLog2e * (double)mm[k] / (double)vv[k];
     else if (k < 2 * D) v = -0.5 * kLog2e / (double)vv[k - D];
     else if (k == 2 * D) {
-      double s = 0.0;
-      for (int d = 0; d < D; ++d) s += log((double)vv[d]);
-      v = kLog2e * (log((double)w[m]) + kMinusLog2Pi * D / 2.0 - 0.5 * s);
+      // constant of the expanded quadratic: log w - D/2 log 2pi - 1/2 sum log var - 1/2 sum mu^2/var
+      double s = 0.0, q = 0.0;
+      for (int d = 0; d < D; ++d) {
+        s += log((double)vv[d]);
+        q += (double)mm[d] * (double)mm[d] / (double)vv[d];
+      }
+      v = kLog2e * (log((double)w[m]) + kMinusLog2Pi * D / 2.0 - 0.5 * s - 0.5 * q);
     }
   } else if (k == 2 * D) {
     v = -1e30;

@@ -1,0 +1,111 @@
+"""Tensor-core (tcgen05) path against the FP64 oracle.
+
+The TC path evaluates the log-likelihood as a split-bf16 contraction with FP32 accumulation
+and exact-in-FP32 operand splits, so it is compared with the FP64 oracle (not with the float
+replica). Tolerances, written per quantity:
+  per-frame log-likelihood   |diff| <= 2e-4 + 2e-6 |ll|
+  total log-likelihood       rel <= 1e-6
+  statistics                 |diff| <= 1e-3 * (scale of the component's statistic) -- posteriors
+                             near the minGamma cut may land on the other side, which moves a
+                             statistic by at most minGamma * |x| per frame
+  EM update (means/vars)     rel <= 1e-4 after one iteration at these small sizes (the 1e-5
+                             target of the full-size workload is measured by bench.py)
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def tc_handle(glib):
+    h = glib.Handle(0)
+    h.set_precision(glib.PREC_TC)
+    return h
+
+
+def check_stats(s, o, rel=1e-3):
+    for k in ("n", "F", "S"):
+        scale = np.maximum(np.abs(o[k]), np.abs(o["n"])[:, None] if k != "n" else 1.0) + 1.0
+        err = np.abs(s[k] - o[k]) / scale
+        assert err.max() <= rel, (k, err.max())
+
+
+@pytest.mark.parametrize("D,M,N", [(39, 16, 2048), (39, 200, 3000), (6, 8, 1000), (20, 4, 777),
+                                   (60, 130, 2500), (1, 5, 640), (47, 64, 1536)])
+def test_tc_matches_fp64(glib, oracle, D, M, N):
+    from gmm_gb300 import synth
+    X, w, mu, var = synth.config_em(100 + D, N, D, max(2, M // 2), M)
+    h = tc_handle(glib)
+    h.upload_model(w, mu, var)
+    h.upload_features(X)
+    ll = h.loglikes()
+    o_ll = oracle.loglikes64(X, w, mu, var)
+    assert np.all(np.abs(ll - o_ll) <= 2e-4 + 2e-6 * np.abs(o_ll)), np.abs(ll - o_ll).max()
+    s = h.accumulate()
+    o = oracle.accumulate64(X, w, mu, var)
+    assert abs(s["totLL"] - o["totLL"]) <= 1e-6 * abs(o["totLL"])
+    check_stats(s, o)
+    h.close()
+
+
+def test_tc_zero_weights_and_single_component(glib, oracle, golden):
+    e = golden("edge.npz")
+    h = tc_handle(glib)
+    h.upload_model(e["zw_w"], e["zw_mu"], e["zw_var"])
+    h.upload_features(e["zw_X"])
+    s = h.accumulate()
+    o = oracle.accumulate64(e["zw_X"], e["zw_w"], e["zw_mu"], e["zw_var"])
+    check_stats(s, o)
+    assert s["n"][1] == 0 and s["n"][5] == 0
+    h.upload_model(np.ones(1, np.float32), e["zw_mu"][:1], e["zw_var"][:1])
+    s = h.accumulate()
+    assert np.allclose(s["n"], [len(e["zw_X"])])
+    o = oracle.accumulate64(e["zw_X"], np.ones(1, np.float32), e["zw_mu"][:1], e["zw_var"][:1])
+    check_stats(s, o, rel=1e-5)
+    h.close()
+
+
+def test_tc_outlier_frame(glib, oracle, golden):
+    from gmm_gb300 import synth
+    e = golden("edge.npz")
+    w, mu, var = synth.generator_gmm(21, 8, 6)
+    h = tc_handle(glib)
+    h.upload_model(w, mu, var)
+    h.upload_features(e["out_X"])
+    ll = h.loglikes()
+    assert ll[17] == np.float32(-1e20)
+    s = h.accumulate()
+    assert s["totLL"] == pytest.approx(float(e["out_totLL"]), rel=1e-9)
+    h.close()
+
+
+def test_tc_em_iteration_close_to_fp64(glib, oracle, golden):
+    g = golden("em_small.npz")
+    h = tc_handle(glib)
+    h.upload_model(g["w"], g["mu"], g["var"])
+    h.upload_features(g["X"])
+    ll, alive = h.em_iterate(1)
+    o = oracle.accumulate64(g["X"], g["w"], g["mu"], g["var"])
+    ow, omu, ovar, _ = oracle.em_update64(g["w"], o)
+    w, mu, var = h.read_model()
+    assert abs(ll[0] - o["totLL"]) <= 1e-6 * abs(o["totLL"])
+    assert np.allclose(w, ow, rtol=1e-4)
+    assert np.allclose(mu, omu, rtol=1e-4, atol=1e-4)
+    assert np.allclose(var, ovar, rtol=1e-4)
+    h.close()
+
+
+def test_tc_c1_full_size(glib, oracle):
+    """Config C1 at full size through the TC path, against the FP64 oracle."""
+    from gmm_gb300 import synth
+    X, w, mu, var = synth.c1(seed=1)
+    h = tc_handle(glib)
+    h.upload_model(w, mu, var)
+    h.upload_features(X)
+    s = h.accumulate()
+    o = oracle.accumulate64(X, w, mu, var)
+    assert abs(s["totLL"] - o["totLL"]) <= 1e-6 * abs(o["totLL"])
+    check_stats(s, o)
+    # the kept posterior mass per frame never exceeds one
+    assert s["n"].sum() <= len(X) * (1 + 1e-6)
+    h.close()
