@@ -45,6 +45,7 @@ SIGNATURES = {
     "gmm_profile_reset": (_i, [_vp]),
     "gmm_profile_read": (_i, [_vp, _i, C.POINTER(C.c_char_p), _vp, _vp]),
     "gmm_launch_count": (_ll, [_vp]),
+    "gmm_accumulate_noalloc": (_i, [_vp, _ll, _i, _i, _vp, _vp, _vp, _f, _f, _f, _i, _vp, _vp]),
 }
 
 _lib = None

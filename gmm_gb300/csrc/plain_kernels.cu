@@ -425,3 +425,147 @@ int plain_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
 }
 
 }  // namespace gmm
+
+// ---------------------------------------------------------------------------------------------
+// Allocation-free E-step (gmm_accumulate_noalloc). Some callers cannot let this library call
+// cudaMalloc: an application whose framework owns the whole device-memory pool, or a
+// latency-critical loop where an allocation (and the implicit device synchronisation of a
+// cudaFree) is not allowed once it runs. For them the plain FP32 E-step below works entirely in
+// one fixed scratch array that lives in this file for the life of the process.
+// ---------------------------------------------------------------------------------------------
+namespace gmm {
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = (size_t)32 << 20;  // 32 MiB per device
+constexpr int kNoAllocMaxMix = 4096;
+constexpr int kNoAllocMaxDim = 128;
+constexpr size_t kNoAllocPartBytes = (size_t)4 << 20;       // per-slice partial statistics
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kMaxDevices = 64;
+static void* g_noalloc_ptr[kMaxDevices];
+static bool g_noalloc_ready[kMaxDevices];
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+}  // namespace
+}  // namespace gmm
+
+extern "C" int gmm_accumulate_noalloc(const float* dX, long long N, int D, int M, const float* dw,
+                                      const float* dmu, const float* dvar, float min_loglike,
+                                      float min_gamma, float min_var, int flags, double* d_stats,
+                                      void* stream) {
+  using namespace gmm;
+  if (N < 0 || M < 1 || D < 1 || !dw || !dmu || !dvar || !d_stats || (N > 0 && !dX))
+    return fail(nullptr, GMM_ERR_ARG, "gmm_accumulate_noalloc: bad argument");
+  if (M > kNoAllocMaxMix || D > kNoAllocMaxDim)
+    return fail(nullptr, GMM_ERR_UNSUPPORTED,
+                "gmm_accumulate_noalloc: at most 4096 components and 128 dimensions "
+                "(fixed 32 MiB scratch)");
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+    return fail(nullptr, GMM_ERR_CUDA, "gmm_accumulate_noalloc: no current CUDA device");
+  // once per device, with that device current: the device address of the scratch array
+  if (!g_noalloc_ready[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return fail(nullptr, GMM_ERR_CUDA,
+                  std::string("gmm_accumulate_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    }
+    g_noalloc_ptr[dev] = p;
+    g_noalloc_ready[dev] = true;
+  }
+  unsigned char* base = static_cast<unsigned char*>(g_noalloc_ptr[dev]);
+  const int E = 1 + 2 * D;
+
+  // carve the scratch: flags | active list | icov | logG | logW | partials | LL | LL partials | posteriors
+  size_t off = 0;
+  Ctx c;
+  c.device = dev;
+  c.stream = static_cast<cudaStream_t>(stream);
+  c.minLL = min_loglike;
+  c.minGamma = min_gamma;
+  c.min_var = min_var;
+  c.M = M;
+  c.D = D;
+  c.Dx = D;
+  c.N = N;
+  c.X = dX;
+  c.w = const_cast<float*>(dw);
+  c.mu = const_cast<float*>(dmu);
+  c.var = const_cast<float*>(dvar);
+  c.stats = d_stats;
+  int hflag[16] = {0};
+  c.hflag = hflag;
+  c.flag = reinterpret_cast<int*>(base + off); off = align_up(off + 16 * sizeof(int), 256);
+  c.act = reinterpret_cast<int*>(base + off); off = align_up(off + sizeof(int) * M, 256);
+  c.icov = reinterpret_cast<float*>(base + off); off = align_up(off + sizeof(float) * (size_t)M * D, 256);
+  c.logG = reinterpret_cast<float*>(base + off); off = align_up(off + sizeof(float) * M, 256);
+  c.logW = reinterpret_cast<float*>(base + off); off = align_up(off + sizeof(float) * M, 256);
+  c.part = reinterpret_cast<double*>(base + off); off = align_up(off + kNoAllocPartBytes, 256);
+  const size_t rest = kNoAllocScratchBytes - off;
+
+  // calls share the scratch: clear what must start at zero (flags) and the caller's output
+  e = cudaMemsetAsync(c.flag, 0, 16 * sizeof(int), c.stream);
+  if (e == cudaSuccess)
+    e = cudaMemsetAsync(d_stats, 0, sizeof(double) * ((size_t)M * E + 1), c.stream);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "gmm_accumulate_noalloc: cudaMemsetAsync");
+  int rc = plain_precompute(&c);
+  if (rc) return fail(nullptr, rc, c.err);
+  if (c.Mact <= 0) return fail(nullptr, GMM_ERR_STATE, "gmm_accumulate_noalloc: no component with non-zero weight");
+
+  // frame chunk: posteriors [Mact][chunk] + LL [chunk] + LL partials [chunk / 256] in `rest`
+  long long chunk = (long long)(rest / (sizeof(float) * (size_t)c.Mact + sizeof(float) + sizeof(double)));
+  chunk = chunk / 256 * 256 - 256;
+  if (chunk < 256) return fail(nullptr, GMM_ERR_UNSUPPORTED, "gmm_accumulate_noalloc: model too large for the scratch");
+  if (chunk > N) chunk = (N + 255) / 256 * 256;
+  if (chunk < 256) chunk = 256;
+  c.logits = reinterpret_cast<float*>(base + off); off = align_up(off + sizeof(float) * (size_t)c.Mact * chunk, 256);
+  c.ll = reinterpret_cast<float*>(base + off); off = align_up(off + sizeof(float) * (size_t)chunk, 256);
+  c.llpart = reinterpret_cast<double*>(base + off); off = align_up(off + sizeof(double) * (size_t)(chunk / 256 + 1), 256);
+  if (off > kNoAllocScratchBytes) return fail(nullptr, GMM_ERR_UNSUPPORTED, "gmm_accumulate_noalloc: scratch layout overflow");
+  c.llpart_cap = (size_t)(chunk / 256 + 1);
+
+  for (long long f0 = 0; f0 < N; f0 += chunk) {
+    const long long nf = (N - f0 < chunk) ? N - f0 : chunk;
+    const int blocks = (int)((nf + 255) / 256);
+    // per-chunk frame index space: the kernels address X and LL as [f0 + i]; the LL buffer
+    // holds one chunk, so point it one chunk back
+    float* llbuf = c.ll - f0;
+    if (D <= 16) launch_ll<16>(&c, f0, nf, c.logits, chunk, llbuf, blocks);
+    else if (D <= 32) launch_ll<32>(&c, f0, nf, c.logits, chunk, llbuf, blocks);
+    else if (D <= 40) launch_ll<40>(&c, f0, nf, c.logits, chunk, llbuf, blocks);
+    else if (D <= 64) launch_ll<64>(&c, f0, nf, c.logits, chunk, llbuf, blocks);
+    else launch_ll<128>(&c, f0, nf, c.logits, chunk, llbuf, blocks);
+    ll_total_kernel<<<1, 1024, 0, c.stream>>>(blocks, c.llpart, c.stats + (size_t)M * E);
+    long long slices = 152LL * 64 / c.Mact;
+    if (slices > nf / 256) slices = nf / 256;
+    const long long max_slices = (long long)(kNoAllocPartBytes / (sizeof(double) * (size_t)c.Mact * E));
+    if (slices > max_slices) slices = max_slices;
+    if (slices < 1) slices = 1;
+    slices = slices / 4 * 4 > 0 ? slices / 4 * 4 : slices;
+    long long slice_len = (nf + slices - 1) / slices;
+    slice_len = (slice_len + 31) / 32 * 32;
+    // the statistics kernel reads LL as ll[f0 + i] from c.ll
+    c.ll = llbuf;
+    const int DW = (D + 31) / 32;
+    switch (DW) {
+      case 1: launch_stats<1>(&c, f0, nf, chunk, flags, (int)slices, slice_len); break;
+      case 2: launch_stats<2>(&c, f0, nf, chunk, flags, (int)slices, slice_len); break;
+      case 3: launch_stats<3>(&c, f0, nf, chunk, flags, (int)slices, slice_len); break;
+      default: launch_stats<4>(&c, f0, nf, chunk, flags, (int)slices, slice_len); break;
+    }
+    c.ll = llbuf + f0;
+    const long long tot = (long long)c.Mact * E;
+    reduce_kernel<<<(int)((tot + 255) / 256), 256, 0, c.stream>>>(M, D, c.Mact, c.act, (int)slices,
+                                                                  c.part, c.stats);
+  }
+  e = cudaStreamSynchronize(c.stream);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "gmm_accumulate_noalloc");
+  return GMM_OK;
+}

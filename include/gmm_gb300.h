@@ -118,6 +118,24 @@ int gmm_mllr_estimate(gmm_handle h, int ubm_init, double* W);
 /* CModelAdapt::AdaptModelMLLR (OL_ModelAdapt.cpp:1583-1612): resident means <- A mu + b. */
 int gmm_mllr_apply(gmm_handle h, const double* W);
 
+/* Allocation-free E-step. No counterpart in the reference: it exists for callers that cannot let
+ * this library allocate device memory -- an application whose framework owns the whole device
+ * memory pool, or a latency-critical loop in which a cudaMalloc/cudaFree (and the device
+ * synchronisation a cudaFree implies) is not allowed once it runs. It computes what
+ * gmm_accumulate computes with the plain FP32 path, from caller-owned device arrays
+ * (dX [N][D], dw [M], dmu [M][D], dvar [M][D]) into the caller-owned device array
+ * d_stats = n[M] | F[M*D] | S[M*D] | total log-likelihood (FP64, zeroed first), on `stream`
+ * (a cudaStream_t; NULL = legacy default stream), and returns after the work finished.
+ * Working memory is one fixed 32 MiB array compiled into the library; every GPU that loads the
+ * library keeps it until the process exits. Limits: M <= 4096, D <= 128 (GMM_ERR_UNSUPPORTED
+ * beyond). The first call on a device looks up the array's device address (no allocation); make
+ * that first call before any stream capture. All calls share the array, so calls that overlap
+ * on the GPU (different streams or threads at the same time) race; serialise them. Errors are
+ * reported through gmm_last_error(NULL). */
+int gmm_accumulate_noalloc(const float* dX, long long N, int D, int M, const float* dw,
+                           const float* dmu, const float* dvar, float min_loglike, float min_gamma,
+                           float min_var, int flags, double* d_stats, void* stream);
+
 /* Per-kernel device time accounting (CUDA events on the handle's stream; the reference's
  * GPU_CUDA_TIMER, CU_GMMStatsEstimator_CUDA.cu:50-55). gmm_profile_read fills up to `cap`
  * entries of names/milliseconds/launch counts and returns the number of kernels seen. */
