@@ -98,7 +98,7 @@ struct Ctx {
   bool tcx_valid = false;
   double* tcpart = nullptr;  // per-CTA FP64 partial statistics
   size_t tcpart_cap = 0;
-  CUtensorMap tm_z128, tm_zft, tm_w128, tm_wct;  // TMA maps over the operand planes
+  CUtensorMap tm_zfull, tm_zhalf, tm_wfull, tm_whalf;  // TMA maps over the operand images
   int* tc_err = nullptr;                          // bounded-wait expiry flag
   double* tc_llpart = nullptr;                    // per-thread log-likelihood partials
   size_t tc_llpart_cap = 0;

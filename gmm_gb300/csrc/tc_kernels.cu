@@ -10,8 +10,13 @@
 // accumulator: every operand is represented to ~2^-24 relative, so the logits carry FP32-level
 // error from the accumulation alone.
 //
-// Two kernels per E-step, both with one TMA-producer warp, one MMA-issuer warp and four
-// epilogue warps (one per TMEM lane quadrant):
+// Operand planes live in HBM as core-matrix tile images: for each plane and each 128-row tile,
+// [K/8 column chunks][128 rows][8 bf16], i.e. exactly the no-swizzle UMMA layout, contiguous
+// (K x 256 bytes). A tile reaches shared memory in one cp.async.bulk.tensor.2d copy per plane over a
+// [rows][128 elements] view (256-byte rows); 64-row half tiles take one 1 KB copy per column chunk.
+//
+// Two kernels per E-step, both with one TMA-producer warp, one MMA-issuer warp and eight
+// epilogue warps (two per TMEM lane quadrant, each taking half of the accumulator columns):
 //   ll_kernel  (frame-tile major, persistent): S[128 frames x CT comps] per component chunk,
 //              online log2-sum-exp over all chunks in the epilogue -> per-frame log-likelihood.
 //   acc_kernel (component-chunk major): the chunk's W planes stay in shared memory; Z tiles
@@ -41,7 +46,7 @@ namespace {
 constexpr double kLog2e = 1.4426950408889634;
 constexpr float kLn2 = 0.69314718055994531f;
 constexpr long long kWaitLimit = 4000000000LL;  // clock cycles (~2 s)
-constexpr int kThreads = 192;                    // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
+constexpr int kThreads = 320;                    // warp 0 TMA, warp 1 MMA, warps 2-9 epilogue
 
 __host__ __device__ constexpr int tile_frames(int K) { return K <= 96 ? 128 : 64; }
 
@@ -69,36 +74,48 @@ __device__ __forceinline__ void split3d(double v, uint16_t& a, uint16_t& b, uint
   c = __bfloat16_as_ushort(h3);
 }
 
-// Z planes [3][Npad][K]: row f = [x, x^2, 1, 0...] (zero rows past N).
-__global__ void features_kernel(const float* __restrict__ X, long long N, long long Npad, int D,
+// Z planes as tile images: element (frame f, column k) of plane p sits at
+// ((p * nT + f / 128) * K/8 + k / 8) * 1024 + (f % 128) * 8 + k % 8; row f = [x, x^2, 1, 0...]
+// (zero rows past N). One thread per element, in image order (coalesced stores).
+__global__ void features_kernel(const float* __restrict__ X, long long N, long long nT, int D,
                                 int K, uint16_t* __restrict__ planes) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= Npad * K) return;
-  const long long f = t / K;
-  const int k = (int)(t - f * K);
+  const int KC = K / 8;
+  if (t >= nT * 128 * K) return;
+  const int e = (int)(t & 7), r = (int)((t >> 3) & 127);
+  const long long blk = t >> 10;
+  const int c = (int)(blk % KC);
+  const long long T = blk / KC;
+  const long long f = T * 128 + r;
+  const int k = c * 8 + e;
   float v = 0.0f;
   if (f < N) {
     if (k < D) v = X[f * D + k];
     else if (k < 2 * D) { float x = X[f * D + k - D]; v = x * x; }
     else if (k == 2 * D) v = 1.0f;
   }
-  uint16_t a, b, c;
-  split3f(v, a, b, c);
-  const size_t plane = (size_t)Npad * K;
+  uint16_t a, b, cc;
+  split3f(v, a, b, cc);
+  const size_t plane = (size_t)nT * 128 * K;
   planes[t] = a;
   planes[plane + t] = b;
-  planes[2 * plane + t] = c;
+  planes[2 * plane + t] = cc;
 }
 
-// W planes [3][Mpad][K] over the active components (log2 units); padded rows carry a
-// constant of -1e30 so they never contribute.
+// W planes as tile images (same layout as Z, rows = active components padded to 128, log2
+// units); padded rows carry a constant of -1e30 so they never contribute.
 __global__ void model_kernel(int D, int K, int Mact, int Mpad, const int* __restrict__ act,
                              const float* __restrict__ w, const float* __restrict__ mu,
                              const float* __restrict__ var, uint16_t* __restrict__ planes,
                              int* __restrict__ comp_of_row) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int KC = K / 8;
   if (t >= (long long)Mpad * K) return;
-  const int r = (int)(t / K), k = (int)(t - (long long)r * K);
+  const int e = (int)(t & 7), rr = (int)((t >> 3) & 127);
+  const long long blk = t >> 10;
+  const int cchunk = (int)(blk % KC);
+  const int r = (int)(blk / KC) * 128 + rr;
+  const int k = cchunk * 8 + e;
   double v = 0.0;
   if (r < Mact) {
     const int m = act[r];
@@ -108,12 +125,12 @@ __global__ void model_kernel(int D, int K, int Mact, int Mpad, const int* __rest
     else if (k < 2 * D) v = -0.5 * kLog2e / (double)vv[k - D];
     else if (k == 2 * D) {
       // constant of the expanded quadratic: log w - D/2 log 2pi - 1/2 sum log var - 1/2 sum mu^2/var
-      double s = 0.0, q = 0.0;
+      double sl = 0.0, q = 0.0;
       for (int d = 0; d < D; ++d) {
-        s += log((double)vv[d]);
+        sl += log((double)vv[d]);
         q += (double)mm[d] * (double)mm[d] / (double)vv[d];
       }
-      v = kLog2e * (log((double)w[m]) + kMinusLog2Pi * D / 2.0 - 0.5 * s - 0.5 * q);
+      v = kLog2e * (log((double)w[m]) + kMinusLog2Pi * D / 2.0 - 0.5 * sl - 0.5 * q);
     }
   } else if (k == 2 * D) {
     v = -1e30;
@@ -140,6 +157,23 @@ __device__ __forceinline__ void mbar_drain(uint64_t* bar, uint32_t parity) {
     if (clock64() - t0 > kWaitLimit) break;
 }
 
+// Copy one plane of one tile image into shared memory. half < 0: the whole 128-row image
+// (one copy of K x 256 bytes); half = 0/1: rows [64 half, 64 half + 64) of every column chunk
+// (K/8 copies of 1 KB) into a 64-row image.
+__device__ __forceinline__ void load_image(uint8_t* dst, const CUtensorMap* full, const CUtensorMap* halfm,
+                                           int plane, int nT, int K, int tile, int half, uint64_t* bar) {
+  const int y0 = (plane * nT + tile) * K;
+  if (half < 0) {
+    tma_load_2d(dst, full, 0, y0, bar);
+  } else {
+    for (int c = 0; c < K / 8; ++c) tma_load_2d(dst + c * 1024, halfm, 0, y0 + c * 8 + half * 4, bar);
+  }
+}
+
+__device__ __forceinline__ void named_sync(int id, int nthreads) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
 // Plane products (Z plane, W plane) with i + j <= 4 (1-based), small terms first.
 __device__ __constant__ int kProdZ[6] = {2, 1, 0, 1, 0, 0};
 __device__ __constant__ int kProdW[6] = {0, 1, 2, 0, 1, 0};
@@ -148,24 +182,24 @@ __device__ __constant__ int kProdW[6] = {0, 1, 2, 0, 1, 0};
 
 template <int K, int CT>
 struct LlCfg {
-  static constexpr int KC = K / 8;
   static constexpr int Z_PLANE = 128 * K * 2;
   static constexpr int W_PLANE = CT * K * 2;
   static constexpr int Z_BYTES = 3 * Z_PLANE;
   static constexpr int W_STAGE = 3 * W_PLANE;
   static constexpr int OFF_Z = 0;
   static constexpr int OFF_W = Z_BYTES;
-  static constexpr int OFF_BAR = OFF_W + 2 * W_STAGE;
+  static constexpr int OFF_RED = OFF_W + 2 * W_STAGE;  // [128] max, [128] sum, [4] stop flags
+  static constexpr int OFF_BAR = OFF_RED + 2 * 128 * 4 + 64;
   static constexpr int OFF_MISC = OFF_BAR + 16 * 8;
   static constexpr int SMEM = (OFF_MISC + 64 + 1024) > 120 * 1024 ? (OFF_MISC + 64 + 1024) : 120 * 1024;
 };
 
 template <int K, int CT>
 __global__ void __launch_bounds__(kThreads, 1)
-    ll_kernel(const __grid_constant__ CUtensorMap zmap, const __grid_constant__ CUtensorMap wmap,
-              long long N, int n_tiles, int n_chunks, float trouble2, float minLL,
-              float* __restrict__ ll2_out, float* __restrict__ ll_out,
-              double* __restrict__ llpart, int* __restrict__ err) {
+    ll_kernel(const __grid_constant__ CUtensorMap zfull, const __grid_constant__ CUtensorMap wfull,
+              const __grid_constant__ CUtensorMap whalf, long long N, int nTz, int nTw,
+              int n_tiles, int n_chunks, float trouble2, float minLL, float* __restrict__ ll2_out,
+              float* __restrict__ ll_out, double* __restrict__ llpart, int* __restrict__ err) {
   using C = LlCfg<K, CT>;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
@@ -179,6 +213,9 @@ __global__ void __launch_bounds__(kThreads, 1)
   uint64_t* mma_done = bars + 10;
   uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(smem + C::OFF_MISC);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + C::OFF_MISC + 8);
+  float* red_m = reinterpret_cast<float*>(smem + C::OFF_RED);
+  float* red_s = red_m + 128;
+  volatile int* stop_s = reinterpret_cast<volatile int*>(red_m + 256);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
@@ -188,7 +225,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       mbar_init(&w_full[i], 1);
       mbar_init(&w_empty[i], 1);
       mbar_init(&s_full[i], 1);
-      mbar_init(&s_empty[i], 4);
+      mbar_init(&s_empty[i], 8);
     }
     mbar_init(mma_done, 1);
     *abort_flag = 0;
@@ -207,8 +244,9 @@ __global__ void __launch_bounds__(kThreads, 1)
 
   if (warp == 0) {
     if (lane == 0 && my_tiles > 0) {
-      prefetch_tmap(&zmap);
-      prefetch_tmap(&wmap);
+      prefetch_tmap(&zfull);
+      prefetch_tmap(&wfull);
+      prefetch_tmap(&whalf);
       int j = 0;
       bool ok = true;
       for (int it = 0; it < my_tiles && ok; ++it) {
@@ -216,16 +254,16 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (!mbar_wait(z_empty, (it & 1) ^ 1, abort_flag, kWaitLimit)) { ok = false; break; }
         mbar_arrive_expect_tx(z_full, C::Z_BYTES);
         for (int p = 0; p < 3; ++p)
-          for (int c = 0; c < C::KC; ++c)
-            tma_load_3d(smem + C::OFF_Z + p * C::Z_PLANE + c * 128 * 16, &zmap, 8 * c, tile * 128, p, z_full);
+          load_image(smem + C::OFF_Z + p * C::Z_PLANE, &zfull, &zfull, p, nTz, K, tile, -1, z_full);
         for (int ch = 0; ch < n_chunks; ++ch, ++j) {
           const int ws = j & 1;
           if (!mbar_wait(&w_empty[ws], ((j >> 1) & 1) ^ 1, abort_flag, kWaitLimit)) { ok = false; break; }
           mbar_arrive_expect_tx(&w_full[ws], C::W_STAGE);
           uint8_t* dst = smem + C::OFF_W + ws * C::W_STAGE;
-          for (int p = 0; p < 3; ++p)
-            for (int c = 0; c < C::KC; ++c)
-              tma_load_3d(dst + p * C::W_PLANE + c * CT * 16, &wmap, 8 * c, ch * CT, p, &w_full[ws]);
+          for (int p = 0; p < 3; ++p) {
+            if (CT == 128) load_image(dst + p * C::W_PLANE, &wfull, &whalf, p, nTw, K, ch, -1, &w_full[ws]);
+            else load_image(dst + p * C::W_PLANE, &wfull, &whalf, p, nTw, K, ch >> 1, ch & 1, &w_full[ws]);
+          }
         }
       }
       // drain: every issued copy must land before the CTA exits
@@ -270,34 +308,39 @@ __global__ void __launch_bounds__(kThreads, 1)
       mbar_drain(mma_done, 0);
     }
   } else {
-    // epilogue: thread = frame row of the tile
+    // epilogue: thread = frame row of the tile; the two warps of a lane quadrant take the two
+    // halves of every component chunk and merge their partial sums at the end of the tile
     const int q4 = warp & 3;
+    const int hf = (warp - 2) >> 2;
     const int row = q4 * 32 + lane;
     const uint32_t lane_off = (uint32_t)(q4 * 32) << 16;
     double llsum = 0.0;
     int j = 0;
     bool ok = true;
-    for (int it = 0; it < my_tiles && ok; ++it) {
+    for (int it = 0; it < my_tiles; ++it) {
       const int tile = (int)blockIdx.x + it * (int)gridDim.x;
       float m = -INFINITY, sum = 0.0f;
-      for (int ch = 0; ch < n_chunks; ++ch, ++j) {
+      for (int ch = 0; ch < n_chunks && ok; ++ch, ++j) {
         const int b = j & 1;
         if (!mbar_wait(&s_full[b], (j >> 1) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
         tc_fence_after();
 #pragma unroll
-        for (int sub = 0; sub < CT / 32; ++sub) {
+        for (int sub = 0; sub < CT / 64; ++sub) {
           uint32_t v[32];
-          tmem_ld32(tmem + lane_off + b * CT + 32 * sub, v);
+          tmem_ld32(tmem + lane_off + b * CT + hf * (CT / 2) + 32 * sub, v);
           tmem_ld_wait();
           float mx = __uint_as_float(v[0]);
 #pragma unroll
           for (int k = 1; k < 32; ++k) mx = fmaxf(mx, __uint_as_float(v[k]));
           const float mn = fmaxf(m, mx);
           if (mn > -INFINITY) {
-            float s = 0.0f;
+            float s0 = 0.0f, s1 = 0.0f;
 #pragma unroll
-            for (int k = 0; k < 32; ++k) s += ex2(__uint_as_float(v[k]) - mn);
-            sum = sum * ex2(m - mn) + s;
+            for (int k = 0; k < 32; k += 2) {
+              s0 += ex2(__uint_as_float(v[k]) - mn);
+              s1 += ex2(__uint_as_float(v[k + 1]) - mn);
+            }
+            sum = sum * ex2(m - mn) + (s0 + s1);
             m = mn;
           }
         }
@@ -305,21 +348,34 @@ __global__ void __launch_bounds__(kThreads, 1)
         __syncwarp();
         if (lane == 0) mbar_arrive(&s_empty[b]);
       }
-      if (!ok) break;
-      const long long f = (long long)tile * 128 + row;
-      float l2 = m + lg2(sum);
-      const bool trouble = !(m > trouble2) || !isfinite(l2);
-      if (f < N) {
-        if (trouble) l2 = -INFINITY;
-        ll2_out[f] = l2;
-        const float lnat = trouble ? minLL : l2 * kLn2;
-        if (ll_out) ll_out[f] = lnat;
-        llsum += (double)lnat;
-      } else {
-        ll2_out[f] = __int_as_float(0x7fc00000);  // padding marker (NaN)
+      // merge the two column halves of each row. Both warps of the pair reach both barriers on
+      // every path, and leave the tile loop together: the stop decision is one snapshot of the
+      // abort flag (raised by any failed wait) taken between the barriers.
+      if (hf == 1) { red_m[row] = m; red_s[row] = sum; }
+      named_sync(1 + q4, 64);
+      if (hf == 0 && lane == 0) stop_s[q4] = *abort_flag;
+      if (hf == 0 && ok && !*abort_flag) {
+        const float m1 = red_m[row], s1 = red_s[row];
+        const float M = fmaxf(m, m1);
+        float S = 0.0f;
+        if (M > -INFINITY) S = sum * ex2(m - M) + s1 * ex2(m1 - M);
+        const long long f = (long long)tile * 128 + row;
+        float l2 = M + lg2(S);
+        const bool trouble = !(M > trouble2) || !isfinite(l2);
+        if (f < N) {
+          // trouble frames carry +inf (every posterior prunes to 0), padding carries NaN
+          ll2_out[f] = trouble ? INFINITY : l2;
+          const float lnat = trouble ? minLL : l2 * kLn2;
+          if (ll_out) ll_out[f] = lnat;
+          llsum += (double)lnat;
+        } else {
+          ll2_out[f] = __int_as_float(0x7fc00000);
+        }
       }
+      named_sync(1 + q4, 64);
+      if (stop_s[q4]) break;
     }
-    llpart[(size_t)blockIdx.x * 128 + row] = llsum;
+    if (hf == 0) llpart[(size_t)blockIdx.x * 128 + row] = llsum;
   }
   __syncthreads();
   if (threadIdx.x == 0 && *abort_flag) atomicExch(err, 1);
@@ -333,7 +389,6 @@ __global__ void __launch_bounds__(kThreads, 1)
 
 template <int K, int FT>
 struct AccCfg {
-  static constexpr int KC = K / 8;
   static constexpr int W_PLANE = 128 * K * 2;
   static constexpr int Z_PLANE = FT * K * 2;
   static constexpr int W_BYTES = 3 * W_PLANE;
@@ -348,18 +403,12 @@ struct AccCfg {
   static constexpr int D2_COL = 256;  // D2 buffers at 256 + 128 d
 };
 
-__device__ __forceinline__ float posterior(float s2, float l2, float minGamma, int single_comp) {
-  if (single_comp) return isnan(l2) ? 0.0f : 1.0f;
-  if (!isfinite(l2)) return 0.0f;
-  const float g = ex2(s2 - l2);
-  return g > minGamma ? g : 0.0f;
-}
-
 template <int K, int FT>
 __global__ void __launch_bounds__(kThreads, 1)
-    acc_kernel(const __grid_constant__ CUtensorMap zmap, const __grid_constant__ CUtensorMap wmap,
-               const float* __restrict__ ll2, int n_tiles, int n_chunks, int slices, int flush_every,
-               float minGamma, int single_comp, double* __restrict__ part, int* __restrict__ err) {
+    acc_kernel(const __grid_constant__ CUtensorMap zfull, const __grid_constant__ CUtensorMap zhalf,
+               const __grid_constant__ CUtensorMap wfull, int nTz, int nTw, const float* __restrict__ ll2,
+               int n_tiles, int n_chunks, int slices, int flush_every, float minGamma, int single_comp,
+               double* __restrict__ part, int* __restrict__ err) {
   using C = AccCfg<K, FT>;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
@@ -388,9 +437,9 @@ __global__ void __launch_bounds__(kThreads, 1)
       mbar_init(&z_full[i], 1);
       mbar_init(&z_empty[i], 1);
       mbar_init(&s_full[i], 1);
-      mbar_init(&g_full[i], 4);
+      mbar_init(&g_full[i], 8);
       mbar_init(&d_full[i], 1);
-      mbar_init(&d_empty[i], 4);
+      mbar_init(&d_empty[i], 8);
     }
     mbar_init(mma_done, 1);
     *abort_flag = 0;
@@ -407,23 +456,24 @@ __global__ void __launch_bounds__(kThreads, 1)
 
   if (warp == 0) {
     if (lane == 0 && nt > 0) {
-      prefetch_tmap(&zmap);
-      prefetch_tmap(&wmap);
+      prefetch_tmap(&zfull);
+      prefetch_tmap(&zhalf);
+      prefetch_tmap(&wfull);
       mbar_arrive_expect_tx(w_full, C::W_BYTES);
       for (int p = 0; p < 3; ++p)
-        for (int c = 0; c < C::KC; ++c)
-          tma_load_3d(smem + C::OFF_W + p * C::W_PLANE + c * 128 * 16, &wmap, 8 * c, chunk * 128, p, w_full);
+        load_image(smem + C::OFF_W + p * C::W_PLANE, &wfull, &wfull, p, nTw, K, chunk, -1, w_full);
       int issued = 0;
       for (int i = 0; i < nt; ++i) {
         const int s = i & 1;
         if (!mbar_wait(&z_empty[s], ((i >> 1) & 1) ^ 1, abort_flag, kWaitLimit)) break;
         mbar_arrive_expect_tx(&z_full[s], C::Z_STAGE + C::LL_STAGE);
         uint8_t* zs = smem + C::OFF_Z + s * C::Z_STAGE;
-        const int row = (t0 + i) * FT;
-        for (int p = 0; p < 3; ++p)
-          for (int c = 0; c < C::KC; ++c)
-            tma_load_3d(zs + p * C::Z_PLANE + c * FT * 16, &zmap, 8 * c, row, p, &z_full[s]);
-        bulk_load(ll_s + s * FT, ll2 + row, FT * 4, &z_full[s]);
+        const int t = t0 + i;
+        for (int p = 0; p < 3; ++p) {
+          if (FT == 128) load_image(zs + p * C::Z_PLANE, &zfull, &zhalf, p, nTz, K, t, -1, &z_full[s]);
+          else load_image(zs + p * C::Z_PLANE, &zfull, &zhalf, p, nTz, K, t >> 1, t & 1, &z_full[s]);
+        }
+        bulk_load(ll_s + s * FT, ll2 + (size_t)t * FT, FT * 4, &z_full[s]);
         issued = i + 1;
       }
       if (*abort_flag) {  // drain the copies of the last two issued tiles
@@ -495,10 +545,16 @@ __global__ void __launch_bounds__(kThreads, 1)
       mbar_drain(mma_done, 0);
     }
   } else if (nt > 0) {
+    // epilogue: thread = component row; the two warps of a lane quadrant take the two halves of
+    // the tile's frames (and of the statistic columns at a flush)
     const int q4 = warp & 3;
+    const int hf = (warp - 2) >> 2;
     const int row = q4 * 32 + lane;
     const uint32_t lane_off = (uint32_t)(q4 * 32) << 16;
     double* mypart = part + ((size_t)blockIdx.x * 128 + row) * K;
+    constexpr int NCH = FT / 64;          // 32-frame chunks per warp
+    constexpr int KCH = K / 16;           // 16-column chunks of the statistics
+    const int kc0 = hf ? (KCH + 1) / 2 : 0, kc1 = hf ? KCH : (KCH + 1) / 2;
     bool first_flush = true;
     for (int i = 0; i < nt; ++i) {
       const int b = i & 1;
@@ -507,19 +563,39 @@ __global__ void __launch_bounds__(kThreads, 1)
       tc_fence_after();
       const float* lls = ll_s + (i & 1) * FT;
 #pragma unroll 1
-      for (int c = 0; c < FT / 32; ++c) {
+      for (int cc = 0; cc < NCH; ++cc) {
+        const int c = hf * NCH + cc;
         uint32_t v[32];
         tmem_ld32(tmem + lane_off + b * FT + 32 * c, v);
         tmem_ld_wait();
         uint32_t hi[16], lo[16];
+        if (!single_comp) {
 #pragma unroll
-        for (int k = 0; k < 32; k += 2) {
-          const float g0 = posterior(__uint_as_float(v[k]), lls[32 * c + k], minGamma, single_comp);
-          const float g1 = posterior(__uint_as_float(v[k + 1]), lls[32 * c + k + 1], minGamma, single_comp);
-          const uint32_t h = pack_bf16(g0, g1);
-          const float h0 = __uint_as_float(h << 16), h1 = __uint_as_float(h & 0xffff0000u);
-          hi[k >> 1] = h;
-          lo[k >> 1] = pack_bf16(g0 - h0, g1 - h1);
+          for (int k = 0; k < 32; k += 4) {
+            const float4 l4 = *reinterpret_cast<const float4*>(lls + 32 * c + k);
+            float g0 = ex2(__uint_as_float(v[k + 0]) - l4.x);
+            float g1 = ex2(__uint_as_float(v[k + 1]) - l4.y);
+            float g2 = ex2(__uint_as_float(v[k + 2]) - l4.z);
+            float g3 = ex2(__uint_as_float(v[k + 3]) - l4.w);
+            g0 = g0 > minGamma ? g0 : 0.0f;  // NaN (padding) and 0 (trouble: +inf LSE) prune
+            g1 = g1 > minGamma ? g1 : 0.0f;
+            g2 = g2 > minGamma ? g2 : 0.0f;
+            g3 = g3 > minGamma ? g3 : 0.0f;
+            const uint32_t h01 = pack_bf16(g0, g1), h23 = pack_bf16(g2, g3);
+            hi[k >> 1] = h01;
+            hi[(k >> 1) + 1] = h23;
+            lo[k >> 1] = pack_bf16(g0 - __uint_as_float(h01 << 16), g1 - __uint_as_float(h01 & 0xffff0000u));
+            lo[(k >> 1) + 1] = pack_bf16(g2 - __uint_as_float(h23 << 16), g3 - __uint_as_float(h23 & 0xffff0000u));
+          }
+        } else {
+          // one component: every real frame has posterior 1 (padding 0)
+#pragma unroll
+          for (int k = 0; k < 32; k += 2) {
+            const float g0 = isnan(lls[32 * c + k]) ? 0.0f : 1.0f;
+            const float g1 = isnan(lls[32 * c + k + 1]) ? 0.0f : 1.0f;
+            hi[k >> 1] = pack_bf16(g0, g1);
+            lo[k >> 1] = 0u;
+          }
         }
         tmem_st16(tmem + lane_off + b * FT + 32 * c, hi);
         tmem_st16(tmem + lane_off + b * FT + 32 * c + 16, lo);
@@ -533,7 +609,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (!mbar_wait(&d_full[dsel], (p >> 1) & 1, abort_flag, kWaitLimit)) break;
         tc_fence_after();
 #pragma unroll 1
-        for (int c = 0; c < K / 16; ++c) {
+        for (int c = kc0; c < kc1; ++c) {
           uint32_t r[16];
           tmem_ld16(tmem + lane_off + C::D2_COL + 128 * dsel + 16 * c, r);
           tmem_ld_wait();
@@ -609,17 +685,16 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-// 3-D map over [3 planes][rows][K] bf16 with a box of 8 columns x box_rows rows x 1 plane:
-// each copy lands as box_rows consecutive 16-byte rows, i.e. one K-chunk column of the
-// no-swizzle core-matrix layout.
-int make_map(Ctx* c, CUtensorMap* map, const uint16_t* base, long long rows, int K, int box_rows) {
+// 2-D map over the plane images viewed as [rows][128 bf16] (256-byte rows): a box of
+// 128 x box_rows lands box_rows * 256 contiguous bytes in shared memory.
+int make_map(Ctx* c, CUtensorMap* map, const uint16_t* base, long long total_elems, int box_rows) {
   auto fn = encode_fn();
   if (!fn) return fail(c, GMM_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
-  cuuint64_t dims[3] = {(cuuint64_t)K, (cuuint64_t)rows, 3};
-  cuuint64_t strides[2] = {(cuuint64_t)K * 2, (cuuint64_t)rows * K * 2};
-  cuuint32_t box[3] = {8, (cuuint32_t)box_rows, 1};
-  cuuint32_t estr[3] = {1, 1, 1};
-  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, (void*)base, dims, strides, box, estr,
+  cuuint64_t dims[2] = {128, (cuuint64_t)(total_elems / 128)};
+  cuuint64_t strides[1] = {256};
+  cuuint32_t box[2] = {128, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)base, dims, strides, box, estr,
                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return fail(c, GMM_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
@@ -633,6 +708,7 @@ int launch_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
   using LC = LlCfg<K, CT>;
   using AC = AccCfg<K, FT>;
   const long long Npad = c->tcx.Npad;
+  const int nTz = (int)(Npad / 128), nTw = c->tcm.Mpad / 128;
   const int n_tiles_ll = (int)(Npad / 128);
   const int n_chunks_ll = c->tcm.Mpad / CT;
   int grid_ll = std::min(n_tiles_ll, c->sms);
@@ -654,8 +730,8 @@ int launch_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
   {
     GMM_LAUNCH(c, "tc_ll_kernel");
     ll_kernel<K, CT><<<grid_ll, kThreads, LC::SMEM, c->stream>>>(
-        c->tm_z128, c->tm_wct, c->N, n_tiles_ll, n_chunks_ll, trouble2, c->minLL, c->tcm.ll2,
-        ll_out_dev, c->tc_llpart, c->tc_err);
+        c->tm_zfull, c->tm_wfull, c->tm_whalf, c->N, nTz, nTw, n_tiles_ll, n_chunks_ll, trouble2,
+        c->minLL, c->tcm.ll2, ll_out_dev, c->tc_llpart, c->tc_err);
   }
   if (!want_stats) return GMM_OK;
   {
@@ -685,8 +761,8 @@ int launch_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
   {
     GMM_LAUNCH(c, "tc_acc_kernel");
     acc_kernel<K, FT><<<grid, kThreads, AC::SMEM, c->stream>>>(
-        c->tm_zft, c->tm_w128, c->tcm.ll2, n_tiles, n_chunks, slices, 16, c->minGamma, c->Mact == 1,
-        c->tcpart, c->tc_err);
+        c->tm_zfull, c->tm_zhalf, c->tm_wfull, nTz, nTw, c->tcm.ll2, n_tiles, n_chunks, slices, 16,
+        c->minGamma, c->Mact == 1, c->tcpart, c->tc_err);
   }
   {
     GMM_LAUNCH(c, "tc_reduce_kernel");
@@ -722,11 +798,11 @@ int tc_prepare_features(Ctx* c) {
   {
     GMM_LAUNCH(c, "tc_features_kernel");
     const long long tot = Npad * K;
-    features_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(c->X, c->N, Npad, c->D, K,
+    features_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(c->X, c->N, Npad / 128, c->D, K,
                                                                          c->tcx.planes);
   }
-  int rc = make_map(c, &c->tm_z128, c->tcx.planes, Npad, K, 128);
-  if (!rc) rc = make_map(c, &c->tm_zft, c->tcx.planes, Npad, K, tile_frames(K));
+  int rc = make_map(c, &c->tm_zfull, c->tcx.planes, 3 * Npad * K, K);
+  if (!rc) rc = make_map(c, &c->tm_zhalf, c->tcx.planes, 3 * Npad * K, 4);
   if (rc) return rc;
   c->tcx_valid = true;
   return GMM_OK;
@@ -752,8 +828,8 @@ int tc_prepare_model(Ctx* c) {
     model_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(
         c->D, K, c->Mact, Mpad, c->act, c->w, c->mu, c->var, c->tcm.planes, c->tcm.comp_of_row);
   }
-  int rc = make_map(c, &c->tm_w128, c->tcm.planes, Mpad, K, 128);
-  if (!rc) rc = make_map(c, &c->tm_wct, c->tcm.planes, Mpad, K, tile_frames(K));
+  int rc = make_map(c, &c->tm_wfull, c->tcm.planes, 3LL * Mpad * K, K);
+  if (!rc) rc = make_map(c, &c->tm_whalf, c->tcm.planes, 3LL * Mpad * K, 4);
   return rc;
 }
 
