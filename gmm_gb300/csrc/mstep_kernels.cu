@@ -58,14 +58,21 @@ __global__ void em_comp_kernel(int M, int D, float* __restrict__ w, float* __res
   }
 }
 
-// Weight renormalisation (OL_ModelAdapt.cpp:928-931): sequential FP64 sum in component order.
+// Weight renormalisation (OL_ModelAdapt.cpp:928-931): the normaliser is the sequential FP64
+// sum in component order (one thread, as the reference adds them); the divisions are
+// independent and run across the block.
 __global__ void em_norm_kernel(int M, float* __restrict__ w, int* __restrict__ flag) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double corr = 0.0;
-  for (int j = 0; j < M; ++j) corr = __dadd_rn(corr, (double)w[j]);
+  __shared__ double s_corr;
+  if (threadIdx.x == 0) {
+    double corr = 0.0;
+    for (int j = 0; j < M; ++j) corr = __dadd_rn(corr, (double)w[j]);
+    s_corr = corr;
+    flag[2] = M - flag[6];
+  }
+  __syncthreads();
+  const double corr = s_corr;
   if (flag[5] && corr > 0.0)
-    for (int j = 0; j < M; ++j) w[j] = (float)__ddiv_rn((double)w[j], corr);
-  flag[2] = M - flag[6];
+    for (int j = threadIdx.x; j < M; j += blockDim.x) w[j] = (float)__ddiv_rn((double)w[j], corr);
 }
 
 // UpdateModelMAP, tau > 0 (OL_ModelAdapt.cpp:1024-1099), one thread per component.
@@ -115,14 +122,18 @@ __global__ void map_comp_kernel(int M, int D, float* __restrict__ w, float* __re
 __global__ void map_norm_kernel(int M, float* __restrict__ w, const float* __restrict__ adapted_w,
                                 const float* __restrict__ uw, const double* __restrict__ stats,
                                 int upW, unsigned int tot) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  __shared__ double s_corr;
   if (!upW) return;
-  double corr = 0.0;
-  for (int j = 0; j < M; ++j)
-    if (uw[j] != 0.0f && stats[j] > 0.0 && tot > 0) corr = __dadd_rn(corr, (double)adapted_w[j]);
-  if (corr != 0.0) {
-    float fc = (float)corr;
-    for (int j = 0; j < M; ++j) w[j] = __fdiv_rn(w[j], fc);
+  if (threadIdx.x == 0) {
+    double corr = 0.0;
+    for (int j = 0; j < M; ++j)
+      if (uw[j] != 0.0f && stats[j] > 0.0 && tot > 0) corr = __dadd_rn(corr, (double)adapted_w[j]);
+    s_corr = corr;
+  }
+  __syncthreads();
+  if (s_corr != 0.0) {
+    const float fc = (float)s_corr;
+    for (int j = threadIdx.x; j < M; j += blockDim.x) w[j] = __fdiv_rn(w[j], fc);
   }
 }
 
@@ -292,7 +303,7 @@ int mstep_em(Ctx* c, int upW, int upM, int upV, int* alive) {
   }
   {
     GMM_LAUNCH(c, "em_norm_kernel");
-    em_norm_kernel<<<1, 32, 0, c->stream>>>(c->M, c->w, c->flag);
+    em_norm_kernel<<<1, 1024, 0, c->stream>>>(c->M, c->w, c->flag);
   }
   c->model_dirty = true;
   c->tcx_valid = c->tcx_valid;  // features unaffected
@@ -320,7 +331,7 @@ int mstep_map(Ctx* c, int tau, int upW, int upM, int upV) {
   }
   {
     GMM_LAUNCH(c, "map_norm_kernel");
-    map_norm_kernel<<<1, 32, 0, c->stream>>>(c->M, c->w, c->logW, c->pw, c->stats, upW, tot);
+    map_norm_kernel<<<1, 1024, 0, c->stream>>>(c->M, c->w, c->logW, c->pw, c->stats, upW, tot);
   }
   c->model_dirty = true;
   return GMM_OK;

@@ -178,39 +178,71 @@ __device__ __forceinline__ void named_sync(int id, int nthreads) {
 __device__ __constant__ int kProdZ[6] = {2, 1, 0, 1, 0, 0};
 __device__ __constant__ int kProdW[6] = {0, 1, 2, 0, 1, 0};
 
+// Copies row `r` of one 128-row tile image (all three planes) from HBM into TMEM, laid out as
+// a tcgen05 A operand: lane = row, each 32-bit column holds two consecutive bf16 of K. Plane p
+// occupies columns [col + p K/2, col + (p+1) K/2). Called by a whole warp (lane = row within
+// its 32-lane quadrant); `valid` false stores zeros.
+__device__ __forceinline__ void image_row_to_tmem(const uint16_t* __restrict__ planes, int nT, int K,
+                                                  int tile, int r, uint32_t taddr, bool valid) {
+  const int KC = K / 8;
+  for (int p = 0; p < 3; ++p) {
+    const uint4* src = reinterpret_cast<const uint4*>(planes + ((size_t)(p * nT + tile) * KC) * 1024 + (size_t)r * 8);
+    for (int c = 0; c < KC; c += 2) {
+      uint4 u0 = make_uint4(0, 0, 0, 0), u1 = make_uint4(0, 0, 0, 0);
+      if (valid) {
+        u0 = __ldg(src + (size_t)c * 128);
+        u1 = __ldg(src + (size_t)(c + 1) * 128);
+      }
+      const uint32_t w[8] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z, u1.w};
+      tmem_st8(taddr + p * (K / 2) + c * 4, w);
+    }
+  }
+}
+
 // ------------------------------------------------------------------ log-likelihood kernel
 
-template <int K, int CT>
+// Z tiles (the A operand: 128 frames x K, 3 planes) live in TMEM, double-buffered when it fits;
+// W chunks (128 components) stream through an NW-stage shared-memory ring. The MMAs read only W
+// from shared memory (A from TMEM), which leaves shared-memory bandwidth for the TMA ring.
+__host__ __device__ constexpr int cmax(int a, int b) { return a > b ? a : b; }
+__host__ __device__ constexpr int ll_zb(int K) { return K <= 80 ? 2 : 1; }
+__host__ __device__ constexpr int ll_nw(int K) { return K <= 96 ? 3 : 2; }
+
+template <int K>
 struct LlCfg {
-  static constexpr int Z_PLANE = 128 * K * 2;
-  static constexpr int W_PLANE = CT * K * 2;
-  static constexpr int Z_BYTES = 3 * Z_PLANE;
+  static constexpr int ZB = ll_zb(K), NW = ll_nw(K);
+  static constexpr int W_PLANE = 128 * K * 2;
   static constexpr int W_STAGE = 3 * W_PLANE;
-  static constexpr int OFF_Z = 0;
-  static constexpr int OFF_W = Z_BYTES;
-  static constexpr int OFF_RED = OFF_W + 2 * W_STAGE;  // [128] max, [128] sum, [4] stop flags
+  static constexpr int ZCOLS = 3 * K / 2;  // TMEM columns of one Z tile
+  static constexpr int S_COL = 0;          // 2 accumulator buffers of 128 columns
+  static constexpr int Z_COL = 256;        // Z buffers
+  static constexpr int OFF_W = 0;
+  static constexpr int OFF_RED = OFF_W + NW * W_STAGE;  // [128] max, [128] sum, [4] stop flags
   static constexpr int OFF_BAR = OFF_RED + 2 * 128 * 4 + 64;
   static constexpr int OFF_MISC = OFF_BAR + 16 * 8;
-  static constexpr int SMEM = (OFF_MISC + 64 + 1024) > 120 * 1024 ? (OFF_MISC + 64 + 1024) : 120 * 1024;
+  static constexpr int SMEM = cmax(OFF_MISC + 64 + 1024, 120 * 1024);
+  static_assert(Z_COL + ZB * ZCOLS <= 512, "TMEM budget");
 };
+constexpr int kLlThreads = 448;  // warp 0 TMA, 1 MMA, 2-9 epilogue, 10-13 Z loaders
 
-template <int K, int CT>
-__global__ void __launch_bounds__(kThreads, 1)
-    ll_kernel(const __grid_constant__ CUtensorMap zfull, const __grid_constant__ CUtensorMap wfull,
-              const __grid_constant__ CUtensorMap whalf, long long N, int nTz, int nTw,
-              int n_tiles, int n_chunks, float trouble2, float minLL, float* __restrict__ ll2_out,
-              float* __restrict__ ll_out, double* __restrict__ llpart, int* __restrict__ err) {
-  using C = LlCfg<K, CT>;
+template <int K>
+__global__ void __launch_bounds__(kLlThreads, 1)
+    ll_kernel(const __grid_constant__ CUtensorMap wfull, const uint16_t* __restrict__ zplanes,
+              long long N, int nTz, int nTw, int n_tiles, int n_chunks, float trouble2, float minLL,
+              float* __restrict__ ll2_out, float* __restrict__ ll_out, double* __restrict__ llpart,
+              int* __restrict__ err) {
+  using C = LlCfg<K>;
+  constexpr int ZB = C::ZB, NW = C::NW;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + C::OFF_BAR);
-  uint64_t* z_full = bars + 0;
-  uint64_t* z_empty = bars + 1;
-  uint64_t* w_full = bars + 2;   // [2]
-  uint64_t* w_empty = bars + 4;  // [2]
-  uint64_t* s_full = bars + 6;   // [2]
-  uint64_t* s_empty = bars + 8;  // [2]
-  uint64_t* mma_done = bars + 10;
+  uint64_t* z_full = bars + 0;   // [ZB <= 2]
+  uint64_t* z_empty = bars + 2;  // [ZB]
+  uint64_t* w_full = bars + 4;   // [NW <= 3]
+  uint64_t* w_empty = bars + 7;  // [NW]
+  uint64_t* s_full = bars + 10;  // [2]
+  uint64_t* s_empty = bars + 12; // [2]
+  uint64_t* mma_done = bars + 14;
   uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(smem + C::OFF_MISC);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + C::OFF_MISC + 8);
   float* red_m = reinterpret_cast<float*>(smem + C::OFF_RED);
@@ -219,11 +251,15 @@ __global__ void __launch_bounds__(kThreads, 1)
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
-    mbar_init(z_full, 1);
-    mbar_init(z_empty, 1);
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < ZB; ++i) {
+      mbar_init(&z_full[i], 4);
+      mbar_init(&z_empty[i], 1);
+    }
+    for (int i = 0; i < NW; ++i) {
       mbar_init(&w_full[i], 1);
       mbar_init(&w_empty[i], 1);
+    }
+    for (int i = 0; i < 2; ++i) {
       mbar_init(&s_full[i], 1);
       mbar_init(&s_empty[i], 8);
     }
@@ -232,84 +268,91 @@ __global__ void __launch_bounds__(kThreads, 1)
     fence_mbar_init();
   }
   if (warp == 1) {
-    tmem_alloc(tmem_holder, 256);
+    tmem_alloc(tmem_holder, 512);
     tmem_relinquish();
   }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_holder;
-  // tiles of this CTA: blockIdx.x, blockIdx.x + gridDim.x, ...
   const int my_tiles = (n_tiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
 
   if (warp == 0) {
     if (lane == 0 && my_tiles > 0) {
-      prefetch_tmap(&zfull);
       prefetch_tmap(&wfull);
-      prefetch_tmap(&whalf);
       int j = 0;
       bool ok = true;
       for (int it = 0; it < my_tiles && ok; ++it) {
-        const int tile = (int)blockIdx.x + it * (int)gridDim.x;
-        if (!mbar_wait(z_empty, (it & 1) ^ 1, abort_flag, kWaitLimit)) { ok = false; break; }
-        mbar_arrive_expect_tx(z_full, C::Z_BYTES);
-        for (int p = 0; p < 3; ++p)
-          load_image(smem + C::OFF_Z + p * C::Z_PLANE, &zfull, &zfull, p, nTz, K, tile, -1, z_full);
         for (int ch = 0; ch < n_chunks; ++ch, ++j) {
-          const int ws = j & 1;
-          if (!mbar_wait(&w_empty[ws], ((j >> 1) & 1) ^ 1, abort_flag, kWaitLimit)) { ok = false; break; }
+          const int ws = j % NW;
+          if (!mbar_wait(&w_empty[ws], ((j / NW) & 1) ^ 1, abort_flag, kWaitLimit)) { ok = false; break; }
           mbar_arrive_expect_tx(&w_full[ws], C::W_STAGE);
           uint8_t* dst = smem + C::OFF_W + ws * C::W_STAGE;
-          for (int p = 0; p < 3; ++p) {
-            if (CT == 128) load_image(dst + p * C::W_PLANE, &wfull, &whalf, p, nTw, K, ch, -1, &w_full[ws]);
-            else load_image(dst + p * C::W_PLANE, &wfull, &whalf, p, nTw, K, ch >> 1, ch & 1, &w_full[ws]);
-          }
+          for (int p = 0; p < 3; ++p)
+            load_image(dst + p * C::W_PLANE, &wfull, &wfull, p, nTw, K, ch, -1, &w_full[ws]);
         }
       }
-      // drain: every issued copy must land before the CTA exits
-      if (!ok) {
-        mbar_drain(z_full, 0);
-        mbar_drain(z_full, 1);
+      if (!ok) {  // drain the copies still in flight
+        const int last = j;
+        for (int k = max(0, last - NW); k < last; ++k) mbar_drain(&w_full[k % NW], (k / NW) & 1);
       }
     }
   } else if (warp == 1) {
     if (lane == 0 && my_tiles > 0) {
-      const uint32_t idesc = idesc_bf16(128, CT, false, false);
-      const uint32_t zb = smem_u32(smem + C::OFF_Z);
+      const uint32_t idesc = idesc_bf16(128, 128, false, false);
       const uint32_t wb0 = smem_u32(smem + C::OFF_W);
       int j = 0;
       bool ok = true;
       for (int it = 0; it < my_tiles && ok; ++it) {
-        if (!mbar_wait(z_full, it & 1, abort_flag, kWaitLimit)) { ok = false; break; }
+        const int zb = it % ZB;
+        if (!mbar_wait(&z_full[zb], (it / ZB) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
+        const uint32_t za = tmem + C::Z_COL + zb * C::ZCOLS;
         for (int ch = 0; ch < n_chunks; ++ch, ++j) {
-          const int ws = j & 1, b = j & 1;
-          if (!mbar_wait(&w_full[ws], (j >> 1) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
+          const int ws = j % NW, b = j & 1;
+          if (!mbar_wait(&w_full[ws], (j / NW) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
           if (!mbar_wait(&s_empty[b], ((j >> 1) & 1) ^ 1, abort_flag, kWaitLimit)) { ok = false; break; }
           tc_fence_after();
           const uint32_t wb = wb0 + ws * C::W_STAGE;
-          const uint32_t d = tmem + b * CT;
+          const uint32_t d = tmem + C::S_COL + b * 128;
           int acc = 0;
 #pragma unroll 1
           for (int pr = 0; pr < 6; ++pr) {
+            const uint32_t a_pl = za + kProdZ[pr] * (K / 2);
+            const uint32_t w_pl = wb + kProdW[pr] * C::W_PLANE;
 #pragma unroll
             for (int q = 0; q < K / 16; ++q) {
-              const uint64_t a = smem_desc(zb + kProdZ[pr] * C::Z_PLANE + q * 2 * 128 * 16, 128 * 16, 128);
-              const uint64_t bd = smem_desc(wb + kProdW[pr] * C::W_PLANE + q * 2 * CT * 16, CT * 16, 128);
-              mma_ss(d, a, bd, idesc, acc);
+              const uint64_t bd = smem_desc(w_pl + q * 2 * 128 * 16, 128 * 16, 128);
+              mma_ts(d, a_pl + q * 8, bd, idesc, acc);
               acc = 1;
             }
           }
           mma_commit(&s_full[b]);
           mma_commit(&w_empty[ws]);
-          if (ch == n_chunks - 1) mma_commit(z_empty);
+          if (ch == n_chunks - 1) mma_commit(&z_empty[zb]);
         }
       }
       mma_commit(mma_done);
       mbar_drain(mma_done, 0);
     }
+  } else if (warp >= 10) {
+    // Z loaders: thread = frame row of the tile; fill the next TMEM Z buffer from HBM
+    const int q4 = warp & 3;
+    const int row = q4 * 32 + lane;
+    const uint32_t lane_off = (uint32_t)(q4 * 32) << 16;
+    for (int it = 0; it < my_tiles; ++it) {
+      const int zb = it % ZB;
+      const int tile = (int)blockIdx.x + it * (int)gridDim.x;
+      if (!mbar_wait(&z_empty[zb], ((it / ZB) & 1) ^ 1, abort_flag, kWaitLimit)) break;
+      tc_fence_after();
+      image_row_to_tmem(zplanes, nTz, K, tile, row, tmem + lane_off + C::Z_COL + zb * C::ZCOLS, tile < nTz);
+      tmem_st_wait();
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&z_full[zb]);
+    }
   } else {
-    // epilogue: thread = frame row of the tile; the two warps of a lane quadrant take the two
-    // halves of every component chunk and merge their partial sums at the end of the tile
+    // epilogue: thread = frame row; the two warps of a lane quadrant take the two 64-column
+    // halves of each chunk and merge their partial sums at the end of the tile
     const int q4 = warp & 3;
     const int hf = (warp - 2) >> 2;
     const int row = q4 * 32 + lane;
@@ -325,9 +368,9 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (!mbar_wait(&s_full[b], (j >> 1) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
         tc_fence_after();
 #pragma unroll
-        for (int sub = 0; sub < CT / 64; ++sub) {
+        for (int sub = 0; sub < 2; ++sub) {
           uint32_t v[32];
-          tmem_ld32(tmem + lane_off + b * CT + hf * (CT / 2) + 32 * sub, v);
+          tmem_ld32(tmem + lane_off + C::S_COL + b * 128 + hf * 64 + 32 * sub, v);
           tmem_ld_wait();
           float mx = __uint_as_float(v[0]);
 #pragma unroll
@@ -349,19 +392,19 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (lane == 0) mbar_arrive(&s_empty[b]);
       }
       // merge the two column halves of each row. Both warps of the pair reach both barriers on
-      // every path, and leave the tile loop together: the stop decision is one snapshot of the
+      // every path and leave the tile loop together: the stop decision is one snapshot of the
       // abort flag (raised by any failed wait) taken between the barriers.
       if (hf == 1) { red_m[row] = m; red_s[row] = sum; }
       named_sync(1 + q4, 64);
       if (hf == 0 && lane == 0) stop_s[q4] = *abort_flag;
       if (hf == 0 && ok && !*abort_flag) {
         const float m1 = red_m[row], s1 = red_s[row];
-        const float M = fmaxf(m, m1);
-        float S = 0.0f;
-        if (M > -INFINITY) S = sum * ex2(m - M) + s1 * ex2(m1 - M);
+        const float M2 = fmaxf(m, m1);
+        float S2 = 0.0f;
+        if (M2 > -INFINITY) S2 = sum * ex2(m - M2) + s1 * ex2(m1 - M2);
         const long long f = (long long)tile * 128 + row;
-        float l2 = M + lg2(S);
-        const bool trouble = !(M > trouble2) || !isfinite(l2);
+        float l2 = M2 + lg2(S2);
+        const bool trouble = !(M2 > trouble2) || !isfinite(l2);
         if (f < N) {
           // trouble frames carry +inf (every posterior prunes to 0), padding carries NaN
           ll2_out[f] = trouble ? INFINITY : l2;
@@ -381,46 +424,55 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (threadIdx.x == 0 && *abort_flag) atomicExch(err, 1);
   if (warp == 1) {
     tc_fence_after();
-    tmem_dealloc(tmem, 256);
+    tmem_dealloc(tmem, 512);
   }
 }
 
 // ------------------------------------------------------------------ statistics kernel
 
-template <int K, int FT>
+// The component chunk's W planes are stored into TMEM once (A operand of the logits MMA); Z tiles
+// stream through an NZ-stage shared-memory ring; posteriors go from the logits accumulator into
+// TMEM in place and feed the statistics MMA; one statistics accumulator, flushed to FP64
+// partials every FLUSH tiles.
+__host__ __device__ constexpr int acc_ft(int K) { return K <= 96 ? 128 : 64; }
+__host__ __device__ constexpr int acc_nz(int K) { return K <= 96 ? 3 : 4; }
+
+template <int K>
 struct AccCfg {
-  static constexpr int W_PLANE = 128 * K * 2;
+  static constexpr int FT = acc_ft(K), NZ = acc_nz(K);
   static constexpr int Z_PLANE = FT * K * 2;
-  static constexpr int W_BYTES = 3 * W_PLANE;
   static constexpr int Z_STAGE = 3 * Z_PLANE;
   static constexpr int LL_STAGE = FT * 4;
-  static constexpr int OFF_W = 0;
-  static constexpr int OFF_Z = W_BYTES;
-  static constexpr int OFF_LL = OFF_Z + 2 * Z_STAGE;
-  static constexpr int OFF_BAR = OFF_LL + 2 * LL_STAGE;
+  static constexpr int S_COL = 0;               // 2 posterior buffers of FT columns
+  static constexpr int W_COL = 2 * FT;          // W planes, 3 K/2 columns
+  static constexpr int D_COL = (W_COL + 3 * K / 2 + 15) / 16 * 16;  // statistics accumulator
+  static constexpr int OFF_Z = 0;
+  static constexpr int OFF_LL = OFF_Z + NZ * Z_STAGE;
+  static constexpr int OFF_BAR = OFF_LL + NZ * LL_STAGE;
   static constexpr int OFF_MISC = OFF_BAR + 16 * 8;
-  static constexpr int SMEM = (OFF_MISC + 64 + 1024) > 120 * 1024 ? (OFF_MISC + 64 + 1024) : 120 * 1024;
-  static constexpr int D2_COL = 256;  // D2 buffers at 256 + 128 d
+  static constexpr int SMEM = cmax(OFF_MISC + 64 + 1024, 120 * 1024);
+  static constexpr int FLUSH = 64 * 128 / FT;   // tiles per FP64 flush (8192 frames)
+  static_assert(D_COL + K <= 512, "TMEM budget");
 };
 
-template <int K, int FT>
+template <int K>
 __global__ void __launch_bounds__(kThreads, 1)
-    acc_kernel(const __grid_constant__ CUtensorMap zfull, const __grid_constant__ CUtensorMap zhalf,
-               const __grid_constant__ CUtensorMap wfull, int nTz, int nTw, const float* __restrict__ ll2,
-               int n_tiles, int n_chunks, int slices, int flush_every, float minGamma, int single_comp,
-               double* __restrict__ part, int* __restrict__ err) {
-  using C = AccCfg<K, FT>;
+    acc_kernel(const __grid_constant__ CUtensorMap zmap, const uint16_t* __restrict__ wplanes,
+               int nTz, int nTw, const float* __restrict__ ll2, int n_tiles, int n_chunks, int slices,
+               float minGamma, int single_comp, double* __restrict__ part, int* __restrict__ err) {
+  using C = AccCfg<K>;
+  constexpr int FT = C::FT, NZ = C::NZ, FLUSH = C::FLUSH;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + C::OFF_BAR);
   uint64_t* w_full = bars + 0;
-  uint64_t* z_full = bars + 1;   // [2]
-  uint64_t* z_empty = bars + 3;  // [2]
-  uint64_t* s_full = bars + 5;   // [2]
-  uint64_t* g_full = bars + 7;   // [2]
-  uint64_t* d_full = bars + 9;   // [2]
-  uint64_t* d_empty = bars + 11; // [2]
-  uint64_t* mma_done = bars + 13;
+  uint64_t* z_full = bars + 1;   // [NZ <= 4]
+  uint64_t* z_empty = bars + 5;  // [NZ]
+  uint64_t* s_full = bars + 9;   // [2]
+  uint64_t* g_full = bars + 11;  // [2]
+  uint64_t* d_full = bars + 13;
+  uint64_t* d_empty = bars + 14;
+  uint64_t* mma_done = bars + 15;
   uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(smem + C::OFF_MISC);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + C::OFF_MISC + 8);
   float* ll_s = reinterpret_cast<float*>(smem + C::OFF_LL);
@@ -432,15 +484,17 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int nt = max(0, min(n_tiles, t0 + per) - t0);
 
   if (threadIdx.x == 0) {
-    mbar_init(w_full, 1);
-    for (int i = 0; i < 2; ++i) {
+    mbar_init(w_full, 8);
+    for (int i = 0; i < NZ; ++i) {
       mbar_init(&z_full[i], 1);
       mbar_init(&z_empty[i], 1);
+    }
+    for (int i = 0; i < 2; ++i) {
       mbar_init(&s_full[i], 1);
       mbar_init(&g_full[i], 8);
-      mbar_init(&d_full[i], 1);
-      mbar_init(&d_empty[i], 8);
     }
+    mbar_init(d_full, 1);
+    mbar_init(d_empty, 8);
     mbar_init(mma_done, 1);
     *abort_flag = 0;
     fence_mbar_init();
@@ -456,49 +510,43 @@ __global__ void __launch_bounds__(kThreads, 1)
 
   if (warp == 0) {
     if (lane == 0 && nt > 0) {
-      prefetch_tmap(&zfull);
-      prefetch_tmap(&zhalf);
-      prefetch_tmap(&wfull);
-      mbar_arrive_expect_tx(w_full, C::W_BYTES);
-      for (int p = 0; p < 3; ++p)
-        load_image(smem + C::OFF_W + p * C::W_PLANE, &wfull, &wfull, p, nTw, K, chunk, -1, w_full);
+      prefetch_tmap(&zmap);
       int issued = 0;
       for (int i = 0; i < nt; ++i) {
-        const int s = i & 1;
-        if (!mbar_wait(&z_empty[s], ((i >> 1) & 1) ^ 1, abort_flag, kWaitLimit)) break;
+        const int s = i % NZ;
+        if (!mbar_wait(&z_empty[s], ((i / NZ) & 1) ^ 1, abort_flag, kWaitLimit)) break;
         mbar_arrive_expect_tx(&z_full[s], C::Z_STAGE + C::LL_STAGE);
         uint8_t* zs = smem + C::OFF_Z + s * C::Z_STAGE;
         const int t = t0 + i;
         for (int p = 0; p < 3; ++p) {
-          if (FT == 128) load_image(zs + p * C::Z_PLANE, &zfull, &zhalf, p, nTz, K, t, -1, &z_full[s]);
-          else load_image(zs + p * C::Z_PLANE, &zfull, &zhalf, p, nTz, K, t >> 1, t & 1, &z_full[s]);
+          if (FT == 128) load_image(zs + p * C::Z_PLANE, &zmap, &zmap, p, nTz, K, t, -1, &z_full[s]);
+          else load_image(zs + p * C::Z_PLANE, &zmap, &zmap, p, nTz, K, t >> 1, t & 1, &z_full[s]);
         }
         bulk_load(ll_s + s * FT, ll2 + (size_t)t * FT, FT * 4, &z_full[s]);
         issued = i + 1;
       }
-      if (*abort_flag) {  // drain the copies of the last two issued tiles
-        mbar_drain(w_full, 0);
-        for (int i = max(0, issued - 2); i < issued; ++i) mbar_drain(&z_full[i & 1], (i >> 1) & 1);
-      }
+      if (*abort_flag)  // drain the copies still in flight
+        for (int i = max(0, issued - NZ); i < issued; ++i) mbar_drain(&z_full[i % NZ], (i / NZ) & 1);
     }
   } else if (warp == 1) {
     if (lane == 0 && nt > 0) {
       const uint32_t idesc_l = idesc_bf16(128, FT, false, false);
       const uint32_t idesc_s = idesc_bf16(128, K, false, true);
-      const uint32_t wb = smem_u32(smem + C::OFF_W);
       const uint32_t zb0 = smem_u32(smem + C::OFF_Z);
+      const uint32_t wa = tmem + C::W_COL;
       bool ok = mbar_wait(w_full, 0, abort_flag, kWaitLimit);
       auto logits = [&](int i) {
-        const uint32_t zb = zb0 + (i & 1) * C::Z_STAGE;
-        const uint32_t d = tmem + (i & 1) * FT;
+        const uint32_t zb = zb0 + (i % NZ) * C::Z_STAGE;
+        const uint32_t d = tmem + C::S_COL + (i & 1) * FT;
         int acc = 0;
 #pragma unroll 1
         for (int pr = 0; pr < 6; ++pr) {
+          const uint32_t a_pl = wa + kProdW[pr] * (K / 2);
+          const uint32_t z_pl = zb + kProdZ[pr] * C::Z_PLANE;
 #pragma unroll
           for (int q = 0; q < K / 16; ++q) {
-            const uint64_t a = smem_desc(wb + kProdW[pr] * C::W_PLANE + q * 2 * 128 * 16, 128 * 16, 128);
-            const uint64_t bd = smem_desc(zb + kProdZ[pr] * C::Z_PLANE + q * 2 * FT * 16, FT * 16, 128);
-            mma_ss(d, a, bd, idesc_l, acc);
+            const uint64_t bd = smem_desc(z_pl + q * 2 * FT * 16, FT * 16, 128);
+            mma_ts(d, a_pl + q * 8, bd, idesc_l, acc);
             acc = 1;
           }
         }
@@ -508,15 +556,15 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int b = j & 1;
         if (!mbar_wait(&g_full[b], (j >> 1) & 1, abort_flag, kWaitLimit)) return false;
         tc_fence_after();
-        const int period = j / flush_every, dsel = period & 1;
-        const bool fresh = (j % flush_every) == 0;
+        const int period = j / FLUSH;
+        const bool fresh = (j % FLUSH) == 0;
         if (fresh) {
-          if (!mbar_wait(&d_empty[dsel], ((period >> 1) & 1) ^ 1, abort_flag, kWaitLimit)) return false;
+          if (!mbar_wait(d_empty, (period & 1) ^ 1, abort_flag, kWaitLimit)) return false;
           tc_fence_after();
         }
-        const uint32_t dcol = tmem + C::D2_COL + 128 * dsel;
-        const uint32_t gb = tmem + b * FT;
-        const uint32_t zb = zb0 + (j & 1) * C::Z_STAGE;
+        const uint32_t dcol = tmem + C::D_COL;
+        const uint32_t gb = tmem + C::S_COL + b * FT;
+        const uint32_t zb = zb0 + (j % NZ) * C::Z_STAGE;
         int acc = fresh ? 0 : 1;
 #pragma unroll
         for (int q = 0; q < FT / 16; ++q) {
@@ -530,12 +578,12 @@ __global__ void __launch_bounds__(kThreads, 1)
           mma_ts(dcol, hi, z2, idesc_s, 1);
           mma_ts(dcol, hi, z1, idesc_s, 1);
         }
-        mma_commit(&z_empty[j & 1]);
-        if ((j % flush_every) == flush_every - 1 || j == nt - 1) mma_commit(&d_full[dsel]);
+        mma_commit(&z_empty[j % NZ]);
+        if ((j % FLUSH) == FLUSH - 1 || j == nt - 1) mma_commit(d_full);
         return true;
       };
       for (int i = 0; i < nt && ok; ++i) {
-        if (!mbar_wait(&z_full[i & 1], (i >> 1) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
+        if (!mbar_wait(&z_full[i % NZ], (i / NZ) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
         tc_fence_after();
         logits(i);
         if (i > 0 && !stats(i - 1)) { ok = false; break; }
@@ -545,28 +593,45 @@ __global__ void __launch_bounds__(kThreads, 1)
       mbar_drain(mma_done, 0);
     }
   } else if (nt > 0) {
-    // epilogue: thread = component row; the two warps of a lane quadrant take the two halves of
-    // the tile's frames (and of the statistic columns at a flush)
+    // epilogue: thread = component row; the two warps of a lane quadrant split the work
     const int q4 = warp & 3;
     const int hf = (warp - 2) >> 2;
     const int row = q4 * 32 + lane;
     const uint32_t lane_off = (uint32_t)(q4 * 32) << 16;
+    // the chunk's W planes into TMEM (A operand of the logits MMA): planes 0-1 by one warp of
+    // the pair, plane 2 by the other
+    {
+      const int KC = K / 8;
+      for (int p = (hf ? 2 : 0); p < (hf ? 3 : 2); ++p) {
+        const uint4* src = reinterpret_cast<const uint4*>(wplanes + ((size_t)(p * nTw + chunk) * KC) * 1024 + (size_t)row * 8);
+        for (int c = 0; c < KC; c += 2) {
+          const uint4 u0 = __ldg(src + (size_t)c * 128), u1 = __ldg(src + (size_t)(c + 1) * 128);
+          const uint32_t w[8] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z, u1.w};
+          tmem_st8(tmem + lane_off + C::W_COL + p * (K / 2) + c * 4, w);
+        }
+      }
+      tmem_st_wait();
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(w_full);
+    }
     double* mypart = part + ((size_t)blockIdx.x * 128 + row) * K;
-    constexpr int NCH = FT / 64;          // 32-frame chunks per warp
-    constexpr int KCH = K / 16;           // 16-column chunks of the statistics
+    constexpr int NCH = FT / 64;  // 32-frame chunks per warp
+    constexpr int KCH = K / 16;   // 16-column chunks of the statistics
     const int kc0 = hf ? (KCH + 1) / 2 : 0, kc1 = hf ? KCH : (KCH + 1) / 2;
     bool first_flush = true;
     for (int i = 0; i < nt; ++i) {
       const int b = i & 1;
-      if (!mbar_wait(&z_full[i & 1], (i >> 1) & 1, abort_flag, kWaitLimit)) break;
+      if (!mbar_wait(&z_full[i % NZ], (i / NZ) & 1, abort_flag, kWaitLimit)) break;
       if (!mbar_wait(&s_full[b], (i >> 1) & 1, abort_flag, kWaitLimit)) break;
       tc_fence_after();
-      const float* lls = ll_s + (i & 1) * FT;
+      const float* lls = ll_s + (i % NZ) * FT;
 #pragma unroll 1
       for (int cc = 0; cc < NCH; ++cc) {
         const int c = hf * NCH + cc;
+        const uint32_t col = tmem + lane_off + C::S_COL + b * FT + 32 * c;
         uint32_t v[32];
-        tmem_ld32(tmem + lane_off + b * FT + 32 * c, v);
+        tmem_ld32(col, v);
         tmem_ld_wait();
         uint32_t hi[16], lo[16];
         if (!single_comp) {
@@ -597,33 +662,33 @@ __global__ void __launch_bounds__(kThreads, 1)
             lo[k >> 1] = 0u;
           }
         }
-        tmem_st16(tmem + lane_off + b * FT + 32 * c, hi);
-        tmem_st16(tmem + lane_off + b * FT + 32 * c + 16, lo);
+        tmem_st16(col, hi);
+        tmem_st16(col + 16, lo);
       }
       tmem_st_wait();
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&g_full[b]);
-      if ((i % flush_every) == flush_every - 1 || i == nt - 1) {
-        const int p = i / flush_every, dsel = p & 1;
-        if (!mbar_wait(&d_full[dsel], (p >> 1) & 1, abort_flag, kWaitLimit)) break;
+      if ((i % FLUSH) == FLUSH - 1 || i == nt - 1) {
+        const int p = i / FLUSH;
+        if (!mbar_wait(d_full, p & 1, abort_flag, kWaitLimit)) break;
         tc_fence_after();
 #pragma unroll 1
         for (int c = kc0; c < kc1; ++c) {
           uint32_t r[16];
-          tmem_ld16(tmem + lane_off + C::D2_COL + 128 * dsel + 16 * c, r);
+          tmem_ld16(tmem + lane_off + C::D_COL + 16 * c, r);
           tmem_ld_wait();
 #pragma unroll
           for (int k = 0; k < 16; ++k) {
-            const double v = (double)__uint_as_float(r[k]);
-            if (first_flush) mypart[16 * c + k] = v;
-            else mypart[16 * c + k] += v;
+            const double dv = (double)__uint_as_float(r[k]);
+            if (first_flush) mypart[16 * c + k] = dv;
+            else mypart[16 * c + k] += dv;
           }
         }
         first_flush = false;
         tc_fence_before();
         __syncwarp();
-        if (lane == 0) mbar_arrive(&d_empty[dsel]);
+        if (lane == 0) mbar_arrive(d_empty);
       }
     }
   }
@@ -703,14 +768,12 @@ int make_map(Ctx* c, CUtensorMap* map, const uint16_t* base, long long total_ele
 
 template <int K>
 int launch_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
-  constexpr int FT = tile_frames(K);
-  constexpr int CT = tile_frames(K);
-  using LC = LlCfg<K, CT>;
-  using AC = AccCfg<K, FT>;
+  using LC = LlCfg<K>;
+  using AC = AccCfg<K>;
   const long long Npad = c->tcx.Npad;
   const int nTz = (int)(Npad / 128), nTw = c->tcm.Mpad / 128;
-  const int n_tiles_ll = (int)(Npad / 128);
-  const int n_chunks_ll = c->tcm.Mpad / CT;
+  const int n_tiles_ll = nTz;
+  const int n_chunks = nTw;
   int grid_ll = std::min(n_tiles_ll, c->sms);
   if (grid_ll < 1) grid_ll = 1;
   size_t need = (size_t)grid_ll * 128;
@@ -723,15 +786,15 @@ int launch_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
   }
   static bool attr_set_ll = false, attr_set_acc = false;
   if (!attr_set_ll) {
-    cudaFuncSetAttribute(ll_kernel<K, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize, LC::SMEM);
+    cudaFuncSetAttribute(ll_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, LC::SMEM);
     attr_set_ll = true;
   }
   const float trouble2 = (float)(c->minLL * kLog2e);
   {
     GMM_LAUNCH(c, "tc_ll_kernel");
-    ll_kernel<K, CT><<<grid_ll, kThreads, LC::SMEM, c->stream>>>(
-        c->tm_zfull, c->tm_wfull, c->tm_whalf, c->N, nTz, nTw, n_tiles_ll, n_chunks_ll, trouble2,
-        c->minLL, c->tcm.ll2, ll_out_dev, c->tc_llpart, c->tc_err);
+    ll_kernel<K><<<grid_ll, kLlThreads, LC::SMEM, c->stream>>>(
+        c->tm_wfull, c->tcx.planes, c->N, nTz, nTw, n_tiles_ll, n_chunks, trouble2, c->minLL,
+        c->tcm.ll2, ll_out_dev, c->tc_llpart, c->tc_err);
   }
   if (!want_stats) return GMM_OK;
   {
@@ -739,8 +802,7 @@ int launch_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
     ll_total_kernel<<<1, 1024, 0, c->stream>>>(grid_ll * 128, c->tc_llpart,
                                                 c->stats + (size_t)c->M * (1 + 2 * c->D));
   }
-  const int n_tiles = (int)(Npad / FT);
-  const int n_chunks = c->tcm.Mpad / 128;
+  const int n_tiles = (int)(Npad / AC::FT);
   int slices = c->sms / n_chunks;
   if (slices < 1) slices = 1;
   if (slices > n_tiles) slices = n_tiles;
@@ -755,14 +817,15 @@ int launch_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
     c->tcpart_cap = pneed;
   }
   if (!attr_set_acc) {
-    cudaFuncSetAttribute(acc_kernel<K, FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, AC::SMEM);
+    cudaFuncSetAttribute(acc_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, AC::SMEM);
     attr_set_acc = true;
   }
   {
     GMM_LAUNCH(c, "tc_acc_kernel");
-    acc_kernel<K, FT><<<grid, kThreads, AC::SMEM, c->stream>>>(
-        c->tm_zfull, c->tm_zhalf, c->tm_wfull, nTz, nTw, c->tcm.ll2, n_tiles, n_chunks, slices, 16,
-        c->minGamma, c->Mact == 1, c->tcpart, c->tc_err);
+    const CUtensorMap& zm = AC::FT == 128 ? c->tm_zfull : c->tm_zhalf;
+    acc_kernel<K><<<grid, kThreads, AC::SMEM, c->stream>>>(
+        zm, c->tcm.planes, nTz, nTw, c->tcm.ll2, n_tiles, n_chunks, slices, c->minGamma,
+        c->Mact == 1, c->tcpart, c->tc_err);
   }
   {
     GMM_LAUNCH(c, "tc_reduce_kernel");
