@@ -1,18 +1,24 @@
-"""Benchmark of the GMM EM iteration on GB300 (frames x components per second).
+"""Benchmark of the GMM hot path on GB300 (frames x components per second).
 
-Workload (default): UBM EM at scale -- N = 10,000,000 frames, D = 39, fitted with M = 2048
-diagonal components (features drawn from a seeded 512-component generator GMM; random-frame
-initialisation). One step = one full EM iteration over all N frames: E-step (log-likelihood,
-log-sum-exp posteriors, n/F/S statistics reduced in FP64) and the M-step update, with the
-features resident in HBM. The features (1.56 GB) are larger than L2 (129 MB).
+Workloads (--workload):
+  ubm-em     (default, the headline line) UBM EM at scale -- N = 10,000,000 frames, D = 39,
+             fitted with M = 2048 diagonal components (features drawn from a seeded
+             512-component generator GMM; random-frame initialisation). One step = one full EM
+             iteration over all N frames: E-step (log-likelihood, log-sum-exp posteriors,
+             n/F/S statistics reduced in FP64) and the M-step update, features resident in HBM
+             (1.56 GB, larger than the 129 MB L2).
+  map-batch  batched mean-only MAP adaptation -- a UBM with M = 1024, D = 60 and 1000 speakers,
+             each a seeded 16-component shift of the UBM, frame counts lognormal clipped to
+             200..30000 (4.8M frames, 1.15 GB), relevance factor 16. One step = one MAP
+             iteration of every speaker (statistics over the UBM + UpdateModelMAP), in one call.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--precision tc|fp32]
-    python bench.py --impl reference ...   # the reference CPU path on the host cores
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--precision tc|fp32] [--workload ...]
+    python bench.py --impl reference ...   # the reference CPU algorithm on the host cores
 
-Under torchrun each rank runs an independent replica on its own GPU (the E-step shards by
-frames only through a sum of statistics; one GPU per process, no collective on the data path);
-`value` is the sum over ranks of the frames x components processed divided by the slowest
-rank's time. Rank 0 prints one JSON line.
+With --precision fp32 the same steps run on the plain FP32 kernels (for map-batch: one speaker
+after the other, as the reference adapts them). Under torchrun each rank runs an independent
+replica on its own GPU (no collective on the data path); `value` is the sum over ranks of the
+frames x components processed divided by the slowest rank's time. Rank 0 prints one JSON line.
 """
 from __future__ import annotations
 
@@ -29,7 +35,6 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "frames·components/s per EM iter"
 UNIT = "frame·comp/s"
 
 
@@ -39,16 +44,25 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="ubm-em", choices=["ubm-em", "map-batch"])
     ap.add_argument("--precision", default=os.environ.get("GMM_BENCH_PRECISION", "tc"),
                     choices=["tc", "fp32"])
-    ap.add_argument("--frames", type=int, default=10_000_000)
-    ap.add_argument("--mix", type=int, default=2048)
-    ap.add_argument("--dim", type=int, default=39)
+    ap.add_argument("--frames", type=int, default=None, help="ubm-em: N (default 10M)")
+    ap.add_argument("--mix", type=int, default=None, help="M (default 2048 / 1024)")
+    ap.add_argument("--dim", type=int, default=None, help="D (default 39 / 60)")
     ap.add_argument("--gen-mix", type=int, default=512)
-    ap.add_argument("--seed", type=int, default=2)
+    ap.add_argument("--speakers", type=int, default=1000)
+    ap.add_argument("--tau", type=int, default=16)
+    ap.add_argument("--seed", type=int, default=None)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
-    return ap.parse_args()
+    a = ap.parse_args()
+    em = a.workload == "ubm-em"
+    a.frames = a.frames or 10_000_000
+    a.mix = a.mix or (2048 if em else 1024)
+    a.dim = a.dim or (39 if em else 60)
+    a.seed = a.seed if a.seed is not None else (2 if em else 3)
+    return a
 
 
 def dist_env():
@@ -75,7 +89,7 @@ class ClockSampler:
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+                 "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
         return self
@@ -120,55 +134,188 @@ def measured_peaks():
     return 6800.0, 1900.0, 1700.0, "fallback"
 
 
-def cpu_reference(args, X, w, mu, var, seconds, threads):
-    """The reference CPU algorithm (the oracle port of the reference estimator, all host
-    threads) on a bounded sample of the workload. Returns (fc/s, sample description)."""
-    import oracle
-    oracle.build(ref=False)
-    n0 = min(len(X), 20000)
-    t = time.perf_counter()
-    st = oracle.accumulate32(X[:n0], w, mu, var, threads=threads)
-    oracle.em_update(w, mu, var, st)
-    dt = time.perf_counter() - t
-    n = int(min(len(X), max(n0, n0 * seconds / max(dt, 1e-3))))
-    t = time.perf_counter()
-    st = oracle.accumulate32(X[:n], w, mu, var, threads=threads)
-    oracle.em_update(w, mu, var, st)
-    dt = time.perf_counter() - t
-    return n * len(w) / dt, n, dt
+# ------------------------------------------------------------------ workloads
 
+class UbmEm:
+    """One EM iteration of an M-component UBM over N resident frames."""
+    metric = "frames·components/s per EM iter"
+
+    def __init__(self, args, rank, gen_frames=None):
+        from gmm_gb300 import synth
+        self.a = args
+        self.N, self.M, self.D = args.frames, args.mix, args.dim
+        n = self.N if gen_frames is None else min(self.N, gen_frames)
+        self.X, self.w, self.mu, self.var = synth.config_em(args.seed + rank, n, self.D,
+                                                            args.gen_mix, self.M)
+        self.fc = self.N * self.M
+
+    def describe(self):
+        return {"workload": f"UBM EM iteration, N={self.N} frames, M={self.M}, D={self.D} "
+                            f"(seeded {self.a.gen_mix}-component generator)",
+                "frames": self.N, "components": self.M, "dim": self.D,
+                "l2": f"inputs larger than L2 (features {self.N * self.D * 4 / 1e9:.2f} GB)"}
+
+    def setup(self, dev, lib, torch, device):
+        self.dev, self.lib = dev, lib
+        self.Xpin = torch.from_numpy(self.X).pin_memory()
+        self.dX = self.Xpin.to(device)
+        dev.upload_model(self.w, self.mu, self.var)
+        dev.upload_features_device(self.dX.data_ptr(), self.N, self.D)
+
+    def step(self):
+        self.dev.accumulate_device(self.lib.ACC_MEAN | self.lib.ACC_VAR)
+        self.dev.em_update(True, True, True)
+
+    def flop_per_fc(self, kernel):
+        D = self.D
+        if kernel.startswith("tc_"):
+            return 2 * (2 * D + 1) * (2 if "acc" in kernel else 1)
+        return 2 * (2 * D + 1)
+
+    def e2e_prepare(self, torch):
+        M, D = self.M, self.D
+        self.Xhost = self.Xpin.numpy()
+        self.out = [torch.empty(s, dtype=torch.float32).pin_memory().numpy() for s in (M, (M, D), (M, D))]
+        self.dev.upload_model(self.w, self.mu, self.var)
+        return int(self.X.nbytes), int(sum(o.nbytes for o in self.out))
+
+    def e2e_step(self):
+        dev = self.dev
+        dev.upload_features(self.Xhost)
+        dev.accumulate_device(self.lib.ACC_MEAN | self.lib.ACC_VAR)
+        dev.em_update(True, True, True)
+        wb, mub, varb = self.out
+        dev.check(dev.lib.gmm_read_model(dev.h, wb.ctypes.data, mub.ctypes.data, varb.ctypes.data))
+
+    def cpu_rate(self, seconds, threads):
+        """The reference CPU algorithm (the oracle port: accumulateStatsMT + UpdateModelEM, all
+        host threads) on a bounded prefix of the frames."""
+        import oracle
+        oracle.build(ref=False)
+        X, w, mu, var = self.X, self.w, self.mu, self.var
+        n0 = min(len(X), 20000)
+        t = time.perf_counter()
+        st = oracle.accumulate32(X[:n0], w, mu, var, threads=threads)
+        oracle.em_update(w, mu, var, st)
+        dt = time.perf_counter() - t
+        n = int(min(len(X), 400_000, max(n0, n0 * seconds / max(dt, 1e-3))))
+        t = time.perf_counter()
+        st = oracle.accumulate32(X[:n], w, mu, var, threads=threads)
+        oracle.em_update(w, mu, var, st)
+        dt = time.perf_counter() - t
+        return n * self.M / dt, (f"{n} frames x {self.M} components (E-step + EM update) of the "
+                                  f"same workload, {dt:.1f} s")
+
+
+class MapBatch:
+    """One mean-only MAP iteration for every speaker of a batch against a resident UBM."""
+    metric = "frames·components/s per MAP iter (batched speakers)"
+
+    def __init__(self, args, rank):
+        from gmm_gb300 import synth
+        self.a = args
+        self.M, self.D, self.S = args.mix, args.dim, args.speakers
+        self.X, self.offs, (self.uw, self.umu, self.uvar) = synth.c3(args.seed + rank, self.S,
+                                                                     self.M, self.D)
+        self.N = int(self.offs[-1])
+        self.fc = self.N * self.M
+
+    def describe(self):
+        lens = np.diff(self.offs)
+        return {"workload": f"batched mean-only MAP, {self.S} speakers x {lens.min()}-{lens.max()} "
+                            f"frames (N={self.N}), UBM M={self.M}, D={self.D}, tau={self.a.tau}",
+                "frames": self.N, "speakers": self.S, "components": self.M, "dim": self.D,
+                "tau": self.a.tau,
+                "l2": f"inputs larger than L2 (features {self.X.nbytes / 1e9:.2f} GB)"}
+
+    def setup(self, dev, lib, torch, device):
+        self.dev, self.lib, self.torch = dev, lib, torch
+        self.Xpin = torch.from_numpy(self.X).pin_memory()
+        self.dX = self.Xpin.to(device)
+        dev.upload_model(self.uw, self.umu, self.uvar)
+        dev.upload_features_device(self.dX.data_ptr(), self.N, self.D)
+        self.d_mu = torch.empty((self.S, self.M, self.D), dtype=torch.float32, device=device)
+        self.d_ll = torch.empty(self.S, dtype=torch.float64, device=device)
+
+    def step(self):
+        self.dev.map_batch_device(self.offs, self.a.tau, 0, 1, 0, d_mu=self.d_mu.data_ptr(),
+                                  d_ll=self.d_ll.data_ptr())
+
+    def flop_per_fc(self, kernel):
+        D = self.D
+        if kernel == "tc_acc_kernel":
+            return 2 * (2 * D + 1) + 2 * (D + 1)  # logits + mean-only statistics
+        return 2 * (2 * D + 1)
+
+    def e2e_prepare(self, torch):
+        self.Xhost = self.Xpin.numpy()
+        self.mu_out = torch.empty((self.S, self.M, self.D), dtype=torch.float32).pin_memory().numpy()
+        self.ll_out = torch.empty(self.S, dtype=torch.float64).pin_memory().numpy()
+        return int(self.X.nbytes), int(self.mu_out.nbytes + self.ll_out.nbytes)
+
+    def e2e_step(self):
+        dev = self.dev
+        dev.upload_features(self.Xhost)
+        offs = np.ascontiguousarray(self.offs, np.int64)
+        dev.check(dev.lib.gmm_map_batch(dev.h, self.S, offs.ctypes.data, self.a.tau, 0, 1, 0, None,
+                                        self.mu_out.ctypes.data, None, self.ll_out.ctypes.data))
+
+    def cpu_rate(self, seconds, threads):
+        """The reference CPU algorithm per speaker (the oracle port: accumulateStatsMT with all
+        host threads + UpdateModelMAP), over as many speakers as fit the time budget."""
+        import oracle
+        oracle.build(ref=False)
+        t = time.perf_counter()
+        frames = 0
+        s = 0
+        while s < self.S and (time.perf_counter() - t) < seconds:
+            Xs = self.X[self.offs[s]:self.offs[s + 1]]
+            st = oracle.accumulate32(Xs, self.uw, self.umu, self.uvar, flags=oracle.ACC_MEAN,
+                                     threads=threads)
+            oracle.map_update(self.uw, self.umu, self.uvar, st, self.a.tau)
+            frames += len(Xs)
+            s += 1
+        dt = time.perf_counter() - t
+        return frames * self.M / dt, (f"first {s} speakers ({frames} frames) x {self.M} components "
+                                      f"(mean-only MAP: E-step + update), {dt:.1f} s")
+
+
+WORKLOADS = {"ubm-em": UbmEm, "map-batch": MapBatch}
+
+
+# ------------------------------------------------------------------ reference arm
 
 def run_reference(args):
+    """The reference's CPU implementation of the path (the oracle port of its estimator and
+    update), all host threads, bounded samples of the same workload per step."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    from gmm_gb300 import synth
     threads = os.cpu_count() or 1
-    X, w, mu, var = synth.config_em(args.seed, min(args.frames, 400_000), args.dim,
-                                    args.gen_mix, args.mix)
+    wl = UbmEm(args, 0, gen_frames=400_000) if args.workload == "ubm-em" else MapBatch(args, 0)
     per_step = max(1.0, 60.0 / max(1, args.steps + args.warmup))
     rates = []
     for i in range(args.warmup + args.steps):
-        r, n, dt = cpu_reference(args, X, w, mu, var, per_step, threads)
+        r, sample = wl.cpu_rate(per_step, threads)
         if i >= args.warmup:
-            rates.append((r, n, dt))
-    value = statistics.median([r for r, _, _ in rates])
-    n = rates[-1][1]
+            rates.append((r, sample))
+    value = statistics.median([r for r, _ in rates])
+    cfg = {k: v for k, v in wl.describe().items() if k != "l2"}
     out = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "impl": "reference", "metric": wl.metric, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * args.frames * args.mix / value, "higher_is_better": True,
+        "ms_per_step": 1e3 * wl.fc / value, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"UBM EM, N={args.frames} frames, M={args.mix}, D={args.dim}",
-                   "frames": args.frames, "components": args.mix, "dim": args.dim,
-                   "timed_sample_frames": n},
+        "config": cfg,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{n} frames x {args.mix} components per step (E-step + EM "
-                                   "update), reference CPU algorithm (oracle port), all host threads"},
+                         "sample": rates[-1][1] + " per step; reference CPU algorithm (oracle port), "
+                                                  "all host threads"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out), flush=True)
 
+
+# ------------------------------------------------------------------ GPU arm
 
 def main():
     args = parse()
@@ -180,23 +327,16 @@ def main():
         import torch.distributed as dist
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
-    from gmm_gb300 import _lib, synth
+    from gmm_gb300 import _lib
     _lib.load()
 
-    N, M, D = args.frames, args.mix, args.dim
-    X, w, mu, var = synth.config_em(args.seed + rank, N, D, args.gen_mix, M)
-    dev = _lib.Handle(local if world > 1 else 0)
+    gpu = local if world > 1 else 0
+    wl = WORKLOADS[args.workload](args, rank)
+    dev = _lib.Handle(gpu)
     prec = _lib.PREC_TC if args.precision == "tc" else _lib.PREC_FP32
     dev.set_precision(prec)
-    Xpin = torch.from_numpy(X).pin_memory()
-    dX = Xpin.to(f"cuda:{local if world > 1 else 0}", non_blocking=False)
-    dev.upload_model(w, mu, var)
-    dev.upload_features_device(dX.data_ptr(), N, D)
+    wl.setup(dev, _lib, torch, f"cuda:{gpu}")
     stream = torch.cuda.ExternalStream(dev.stream())
-
-    def step():
-        dev.accumulate_device(_lib.ACC_MEAN | _lib.ACC_VAR)
-        dev.em_update(True, True, True)
 
     def barrier():
         torch.cuda.synchronize()
@@ -204,19 +344,19 @@ def main():
             torch.distributed.barrier()
 
     for _ in range(args.warmup):
-        step()
+        wl.step()
     # kernel timing (CUDA events on the engine's stream) over the timed region
     dev.profile(True)
     dev.profile_reset()
     launches0 = dev.launch_count()
     barrier()
-    with ClockSampler(local if world > 1 else 0) as clk:
+    with ClockSampler(gpu) as clk:
         with torch.cuda.stream(stream):
             t0 = torch.cuda.Event(enable_timing=True)
             t1 = torch.cuda.Event(enable_timing=True)
             t0.record(stream)
             for _ in range(args.steps):
-                step()
+                wl.step()
             t1.record(stream)
         barrier()
     ms = t0.elapsed_time(t1) / args.steps
@@ -227,38 +367,28 @@ def main():
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
-    value = world * N * M / (ms / 1e3)
+    value = world * wl.fc / (ms / 1e3)
 
-    # end-to-end through the public API: host (pinned) features -> device, EM iteration,
-    # updated model back to the host, every step
+    # end-to-end through the public API: pinned host features -> device, the step, the result
+    # back to the host, every step
     e2e = None
     if not args.no_e2e:
-        Xhost = Xpin.numpy()
-        wb, mub, varb = np.empty(M, np.float32), np.empty((M, D), np.float32), np.empty((M, D), np.float32)
-
-        def e2e_step():
-            dev.upload_features(Xhost)
-            dev.accumulate_device(_lib.ACC_MEAN | _lib.ACC_VAR)
-            dev.em_update(True, True, True)
-            dev.lib.gmm_read_model(dev.h, wb.ctypes.data, mub.ctypes.data, varb.ctypes.data)
-
-        dev.upload_model(w, mu, var)
+        h2d, d2h = wl.e2e_prepare(torch)
         for _ in range(2):
-            e2e_step()
+            wl.e2e_step()
         barrier()
         te = time.perf_counter()
         ke = max(2, args.steps // 2)
         for _ in range(ke):
-            e2e_step()
+            wl.e2e_step()
         barrier()
         e2e_ms = (time.perf_counter() - te) * 1e3 / ke
         if world > 1:
             t = torch.tensor([e2e_ms], device="cuda")
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
             e2e_ms = float(t.item())
-        e2e = {"value": world * N * M / (e2e_ms / 1e3), "unit": UNIT,
-               "h2d_bytes_per_step": int(X.nbytes), "d2h_bytes_per_step": int(wb.nbytes + mub.nbytes + varb.nbytes),
-               "ms_per_step": e2e_ms}
+        e2e = {"value": world * wl.fc / (e2e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms}
 
     if rank != 0:
         if world > 1:
@@ -267,40 +397,34 @@ def main():
 
     hbm, bf16, bf16s, peak_kind = measured_peaks()
     # dominant kernel: largest share of device time in the timed region
-    top = max(prof.items(), key=lambda kv: kv[1][0]) if prof else ("none", (0.0, 1))
-    name, (kms, kcnt) = top
-    fc_per_launch = N * M / max(1, kcnt // args.steps) if kcnt else 0
-    if name.startswith("tc_"):
-        flop_fc = 2 * (2 * D + 1) * (2 if "acc" in name else 1)
-    else:
-        flop_fc = 2 * (2 * D + 1) if "ll" in name else 2 * (2 * D + 1)
+    name, (kms, kcnt) = max(prof.items(), key=lambda kv: kv[1][0]) if prof else ("none", (0.0, 0))
     per_launch_ms = kms / max(1, kcnt)
-    achieved = flop_fc * fc_per_launch / (per_launch_ms / 1e3) / 1e12 if kcnt else 0.0
+    launches_per_step = max(1, kcnt // args.steps) if kcnt else 1
+    flop_fc = wl.flop_per_fc(name)
+    achieved = flop_fc * (wl.fc / launches_per_step) / (per_launch_ms / 1e3) / 1e12 if kcnt else 0.0
     peak = bf16s if bf16s else bf16
     roofline = {"bound": "tensor", "kernel": name, "achieved": achieved, "peak": peak,
                 "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
-                "algorithmic_flop_per_fc": flop_fc, "peak_source": f"{peak_kind} (bf16 sustained)",
+                "algorithmic_flop_per_fc": flop_fc,
+                "peak_source": f"{peak_kind} (bf16 sustained, MEASURED_PEAKS.json)",
                 "kernel_ms_per_launch": per_launch_ms,
                 "kernel_share": kms / max(1e-9, sum(v[0] for v in prof.values()))}
 
-    cpu = None
-    if world == 1 or rank == 0:
-        threads = os.cpu_count() or 1
-        r, n, dt = cpu_reference(args, X[:400_000], w, mu, var, args.cpu_seconds, threads)
-        cpu = {"value": r, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"{n} frames x {M} components (E-step + EM update) of the same workload, "
-                         f"{dt:.1f} s, reference CPU algorithm (oracle port)"}
+    threads = os.cpu_count() or 1
+    r, sample = wl.cpu_rate(args.cpu_seconds, threads)
+    cpu = {"value": r, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": sample + "; reference CPU algorithm (oracle port)"}
 
+    cfg = wl.describe()
+    cfg.update({"precision": args.precision, "parallelism": f"replicas x{world}"})
     out = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "metric": wl.metric, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32" if prec == _lib.PREC_FP32 else "bf16x3 split (tcgen05), f32 accumulate, f64 reduce",
-        "data": "synthetic",
-        "config": {"workload": f"UBM EM iteration, N={N} frames, M={M}, D={D} (seeded {args.gen_mix}-component generator)",
-                   "frames": N, "components": M, "dim": D, "precision": args.precision,
-                   "l2": "inputs larger than L2 (features 1.56 GB)", "parallelism": f"replicas x{world}"},
-        "clocks": clk.summary(), "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
-        "cpu_baseline": cpu, "kernels": {k: {"ms": v[0], "launches": v[1]} for k, v in prof.items()},
+        "vs_baseline": None,
+        "dtype": "f32" if prec == _lib.PREC_FP32 else "bf16x3 split (tcgen05), f32 accumulate, f64 reduce",
+        "data": "synthetic", "config": cfg, "clocks": clk.summary(), "e2e": e2e,
+        "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
+        "kernels": {k: {"ms": v[0], "launches": v[1]} for k, v in prof.items()},
     }
     print(json.dumps(out), flush=True)
     if world > 1:

@@ -39,6 +39,8 @@ SIGNATURES = {
     "gmm_em_update": (_i, [_vp, _i, _i, _i, C.POINTER(_i)]),
     "gmm_map_update": (_i, [_vp, _i, _i, _i, _i]),
     "gmm_em_iterate": (_i, [_vp, _i, _i, _i, _i, _vp, C.POINTER(_i)]),
+    "gmm_map_batch": (_i, [_vp, _i, _vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp]),
+    "gmm_map_batch_device": (_i, [_vp, _i, _vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp]),
     "gmm_mllr_estimate": (_i, [_vp, _i, _vp]),
     "gmm_mllr_apply": (_i, [_vp, _vp]),
     "gmm_profile_enable": (_i, [_vp, _i]),
@@ -203,6 +205,26 @@ class Handle:
 
     def map_update(self, tau, upW=False, upM=True, upV=False):
         self.check(self.lib.gmm_map_update(self.h, int(tau), int(upW), int(upM), int(upV)))
+
+    def map_batch(self, offs, tau, upW=False, upM=True, upV=False):
+        """One MAP iteration per speaker against the resident model (the UBM); speaker s owns the
+        resident frames offs[s]:offs[s+1]. Returns (w [S,M], mu [S,M,D], var [S,M,D], ll [S])."""
+        offs = np.ascontiguousarray(offs, np.int64)
+        S = len(offs) - 1
+        w = np.zeros((S, self.M), np.float32)
+        mu = np.zeros((S, self.M, self.D), np.float32)
+        var = np.zeros((S, self.M, self.D), np.float32)
+        ll = np.zeros(S)
+        self.check(self.lib.gmm_map_batch(self.h, S, ptr(offs), int(tau), int(upW), int(upM),
+                                          int(upV), ptr(w), ptr(mu), ptr(var), ptr(ll)))
+        return w, mu, var, ll
+
+    def map_batch_device(self, offs, tau, upW, upM, upV, d_w=0, d_mu=0, d_var=0, d_ll=0):
+        """map_batch into caller-owned device arrays (integer device pointers, 0 = not wanted)."""
+        offs = np.ascontiguousarray(offs, np.int64)
+        self.check(self.lib.gmm_map_batch_device(self.h, len(offs) - 1, ptr(offs), int(tau),
+                                                 int(upW), int(upM), int(upV), d_w or None,
+                                                 d_mu or None, d_var or None, d_ll or None))
 
     def em_iterate(self, iters, upW=True, upM=True, upV=True):
         ll = np.zeros(max(iters, 1))

@@ -461,6 +461,83 @@ int gmm_map_update(gmm_handle h, int tau, int upW, int upM, int upV) {
   return sync(h, "gmm_map_update");
 }
 
+static int map_batch(Ctx* c, int S, const long long* offs, int tau, int upW, int upM, int upV,
+                     float* w, float* mu, float* var, double* ll, bool dev_out) {
+  if (S < 0 || (S > 0 && !offs)) return fail(c, GMM_ERR_ARG, "gmm_map_batch: bad speaker count or offsets");
+  if (tau < 1) return fail(c, GMM_ERR_ARG, "gmm_map_batch: tau must be >= 1");
+  if (!c->w) return fail(c, GMM_ERR_STATE, "no model uploaded");
+  if (!c->X && c->N > 0) return fail(c, GMM_ERR_STATE, "no features uploaded");
+  if (c->Dx != c->D && c->N > 0)
+    return fail(c, GMM_ERR_ARG, "Inconsistent model & feature vector - different dimensions");
+  if (S == 0) return GMM_OK;
+  if (offs[0] < 0 || offs[S] > c->N) return fail(c, GMM_ERR_ARG, "gmm_map_batch: offsets outside the resident frames");
+  for (int s = 0; s < S; ++s)
+    if (offs[s + 1] < offs[s]) return fail(c, GMM_ERR_ARG, "gmm_map_batch: offsets must be non-decreasing");
+  cudaSetDevice(c->device);
+  int rc;
+  if (c->model_dirty) {
+    rc = plain_precompute(c);
+    if (rc) return rc;
+  }
+  const int M = c->M, D = c->D;
+  const size_t bw = sizeof(float) * (size_t)S * M, bmu = bw * D, bll = sizeof(double) * S;
+  const size_t boffs = sizeof(long long) * (S + 1);
+  MapBatch b;
+  b.S = S;
+  b.tau = tau;
+  b.upW = upW;
+  b.upM = upM;
+  b.upV = upV;
+  b.flags = (upM ? GMM_ACC_MEAN : 0) | (upV ? GMM_ACC_VAR : 0) | ((upW && !upM && !upV) ? GMM_ACC_PROBS_ONLY : 0);
+  b.offs = offs;
+  long long* d_offs = nullptr;
+  float *ow = nullptr, *omu = nullptr, *ovar = nullptr;
+  double* oll = nullptr;
+  rc = dalloc(c, (void**)&d_offs, boffs, "speaker offsets");
+  if (!rc) rc = dalloc(c, (void**)&b.aw, bw, "adapted weight scratch");
+  // device staging for host outputs; weights and log-likelihoods are always computed
+  if (!rc && !(dev_out && w)) rc = dalloc(c, (void**)&ow, bw, "adapted weights");
+  if (!rc && !dev_out && mu) rc = dalloc(c, (void**)&omu, bmu, "adapted means");
+  if (!rc && !dev_out && var) rc = dalloc(c, (void**)&ovar, bmu, "adapted variances");
+  if (!rc && !(dev_out && ll)) rc = dalloc(c, (void**)&oll, bll, "speaker log-likelihoods");
+  if (!rc) {
+    b.d_offs = d_offs;
+    b.w = ow ? ow : w;
+    b.mu = dev_out ? mu : omu;
+    b.var = dev_out ? var : ovar;
+    b.ll = oll ? oll : ll;
+    cudaMemcpyAsync(d_offs, offs, boffs, cudaMemcpyHostToDevice, c->stream);
+    rc = c->precision == GMM_PREC_TC ? tc_map_batch(c, b) : plain_map_batch(c, b);
+  }
+  if (!rc && !dev_out) {
+    if (w) cudaMemcpyAsync(w, b.w, bw, cudaMemcpyDeviceToHost, c->stream);
+    if (mu) cudaMemcpyAsync(mu, b.mu, bmu, cudaMemcpyDeviceToHost, c->stream);
+    if (var) cudaMemcpyAsync(var, b.var, bmu, cudaMemcpyDeviceToHost, c->stream);
+    if (ll) cudaMemcpyAsync(ll, b.ll, bll, cudaMemcpyDeviceToHost, c->stream);
+  }
+  if (!rc) rc = sync(c, "gmm_map_batch");
+  cudaStreamSynchronize(c->stream);
+  dfree(c, d_offs, boffs);
+  dfree(c, b.aw, bw);
+  dfree(c, ow, bw);
+  dfree(c, omu, bmu);
+  dfree(c, ovar, bmu);
+  dfree(c, oll, bll);
+  return rc;
+}
+
+int gmm_map_batch(gmm_handle h, int S, const long long* offs, int tau, int upW, int upM, int upV,
+                  float* w, float* mu, float* var, double* ll) {
+  if (!h) return GMM_ERR_ARG;
+  return map_batch(h, S, offs, tau, upW, upM, upV, w, mu, var, ll, false);
+}
+
+int gmm_map_batch_device(gmm_handle h, int S, const long long* offs, int tau, int upW, int upM,
+                         int upV, float* d_w, float* d_mu, float* d_var, double* d_ll) {
+  if (!h) return GMM_ERR_ARG;
+  return map_batch(h, S, offs, tau, upW, upM, upV, d_w, d_mu, d_var, d_ll, true);
+}
+
 int gmm_em_iterate(gmm_handle h, int iters, int upW, int upM, int upV, double* ll, int* alive) {
   if (!h) return GMM_ERR_ARG;
   Ctx* c = h;

@@ -143,6 +143,26 @@ int tc_prepare_features(Ctx* c);
 int tc_prepare_model(Ctx* c);
 int tc_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev);
 
+// One MAP iteration for S speakers against the resident model (the UBM); speaker s owns the
+// resident frames [offs[s], offs[s+1]).
+struct MapBatch {
+  int S = 0, tau = 0, upW = 0, upM = 0, upV = 0, flags = 0;
+  const long long* offs = nullptr;    // host, S + 1 entries
+  const long long* d_offs = nullptr;  // the same on the device
+  float* w = nullptr;                 // device outputs: [S][M] weights, [S][M][D] means, variances
+  float* mu = nullptr;
+  float* var = nullptr;
+  float* aw = nullptr;                // device scratch [S][M]
+  double* ll = nullptr;               // device output [S]: per-speaker total log-likelihood
+};
+// statistics layouts read by mstep_map_batch
+constexpr int kStatsSlots = 0;  // tensor-core partials: [speaker][chunk][K cols][128 rows], rows via row_of_comp
+constexpr int kStatsPlain = 1;  // [speaker][n (M) | F (M x D) | S (M x D) | totLL | pad]
+int mstep_map_batch(Ctx* c, const MapBatch& b, const double* stats, int layout, int K, int n_chunks,
+                    const int* row_of_comp);
+int tc_map_batch(Ctx* c, const MapBatch& b);
+int plain_map_batch(Ctx* c, const MapBatch& b);
+
 int sync(Ctx* c, const char* what);
 
 }  // namespace gmm

@@ -290,6 +290,98 @@ __global__ void mllr_apply_kernel(int M, int D, float* __restrict__ mu, const do
   }
 }
 
+// CModelAdapt::UpdateModelMAP (OL_ModelAdapt.cpp:1024-1099) for every (speaker, component),
+// with the resident model as both the starting point and the prior: AdaptModelMAP copies the UBM
+// (:1259-1260) and the first MAP iteration adapts that copy towards the statistics. Same
+// expression order as map_comp_kernel. One warp per (speaker, component), lanes over the
+// dimensions (coalesced rows). Statistics come in one of two layouts (kStatsSlots /
+// kStatsPlain); in the plain layout the speaker's total log-likelihood is copied out as well.
+__global__ void map_batch_kernel(int S, int M, int D, int layout, const double* __restrict__ stats,
+                                 int K, int n_chunks, const int* __restrict__ row_of_comp,
+                                 const long long* __restrict__ offs, const float* __restrict__ uw,
+                                 const float* __restrict__ umu, const float* __restrict__ uvar,
+                                 int tau, int upW, int upM, int upV, float min_var,
+                                 float* __restrict__ ow, float* __restrict__ omu,
+                                 float* __restrict__ ovar, float* __restrict__ adapted_w,
+                                 double* __restrict__ ll) {
+  const long long t = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (t >= (long long)S * M) return;
+  const int s = (int)(t / M), m = (int)(t - (long long)s * M);
+  const float* um = umu + (size_t)m * D;
+  const float* uv = uvar + (size_t)m * D;
+  float* om = omu ? omu + (size_t)t * D : nullptr;
+  float* ov = ovar ? ovar + (size_t)t * D : nullptr;
+  const double *pn = nullptr, *pF = nullptr, *pS = nullptr;
+  size_t cs = 1;  // stride between the columns of one component's statistics
+  if (layout == kStatsSlots) {
+    const int r = row_of_comp[m];
+    if (r >= 0) {  // inactive components were never accumulated
+      const double* st = stats + ((size_t)s * n_chunks + r / 128) * K * 128 + (r % 128);
+      cs = 128;
+      pF = st;
+      pS = st + (size_t)D * 128;
+      pn = st + (size_t)2 * D * 128;
+    }
+  } else {
+    const double* st = stats + (size_t)s * ((size_t)M * (1 + 2 * D) + 2);
+    if (m == 0 && lane == 0) ll[s] = st[(size_t)M * (1 + 2 * D)];
+    pn = st + m;
+    pF = st + M + (size_t)m * D;
+    pS = st + M + (size_t)M * D + (size_t)m * D;
+  }
+  const double mp = pn ? *pn : 0.0;
+  const bool adapt = uw[m] != 0.0f && mp > 0.0;
+  const unsigned int tot = (unsigned int)(offs[s + 1] - offs[s]);
+  const double alfa = adapt ? __ddiv_rn(mp, __dadd_rn(mp, (double)tau)) : 0.0;
+  const double one_m = __dsub_rn(1.0, alfa);
+  if (lane == 0) {
+    float aw = 0.0f;
+    const bool wset = adapt && upW && tot > 0;
+    if (wset) {
+      const double t1 = __dmul_rn(alfa, __ddiv_rn(mp, (double)tot));
+      aw = (float)__dadd_rn(t1, __dmul_rn(one_m, (double)uw[m]));
+    }
+    ow[t] = wset ? aw : uw[m];
+    adapted_w[t] = aw;
+  }
+  for (int k = lane; k < D; k += 32) {
+    float am = um[k], av = uv[k];
+    if (adapt && (upM || upV)) {
+      const double a1 = __ddiv_rn(__dmul_rn(alfa, pF[k * cs]), mp);
+      am = (float)__dadd_rn(a1, __dmul_rn(one_m, (double)um[k]));
+      if (upV) {
+        const float second = __fadd_rn(uv[k], __fmul_rn(um[k], um[k]));
+        const float msq = __fmul_rn(am, am);
+        const double b1 = __ddiv_rn(__dmul_rn(alfa, pS[k * cs]), mp);
+        const double b2 = __dadd_rn(b1, __dmul_rn(one_m, (double)second));
+        av = (float)__dsub_rn(b2, (double)msq);
+        if (av < min_var) av = min_var;
+      }
+    }
+    if (om) om[k] = am;
+    if (ov) ov[k] = av;
+  }
+}
+
+// Weight renormalisation per speaker (OL_ModelAdapt.cpp:1100-1104): one warp per speaker, the
+// FP64 sum taken sequentially in component order by lane 0 (entries of components that were not
+// adapted are +0.0 and leave it unchanged, as in map_norm_kernel), the divisions by all lanes.
+__global__ void map_batch_norm_kernel(int S, int M, const float* __restrict__ adapted_w,
+                                      float* __restrict__ ow) {
+  const int s = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (s >= S) return;
+  double corr = 0.0;
+  if (lane == 0)
+    for (int m = 0; m < M; ++m) corr = __dadd_rn(corr, (double)adapted_w[(size_t)s * M + m]);
+  corr = __shfl_sync(0xffffffffu, corr, 0);
+  if (corr != 0.0) {
+    const float fc = (float)corr;
+    for (int m = lane; m < M; m += 32) ow[(size_t)s * M + m] = __fdiv_rn(ow[(size_t)s * M + m], fc);
+  }
+}
+
 }  // namespace
 
 int mstep_em(Ctx* c, int upW, int upM, int upV, int* alive) {
@@ -400,6 +492,23 @@ int mstep_mllr_apply(Ctx* c, const double* W_host) {
   dfree(c, dW, sizeof(double) * (size_t)D * E);
   c->model_dirty = true;
   return rc;
+}
+
+int mstep_map_batch(Ctx* c, const MapBatch& b, const double* stats, int layout, int K, int n_chunks,
+                    const int* row_of_comp) {
+  const long long tot = (long long)b.S * c->M;
+  if (tot == 0) return GMM_OK;
+  {
+    GMM_LAUNCH(c, "map_batch_kernel");
+    map_batch_kernel<<<(unsigned)((tot + 7) / 8), 256, 0, c->stream>>>(
+        b.S, c->M, c->D, layout, stats, K, n_chunks, row_of_comp, b.d_offs, c->w, c->mu, c->var,
+        b.tau, b.upW, b.upM, b.upV, c->min_var, b.w, b.mu, b.var, b.aw, b.ll);
+  }
+  if (b.upW) {
+    GMM_LAUNCH(c, "map_batch_norm_kernel");
+    map_batch_norm_kernel<<<(b.S + 7) / 8, 256, 0, c->stream>>>(b.S, c->M, b.aw, b.w);
+  }
+  return GMM_OK;
 }
 
 }  // namespace gmm

@@ -424,6 +424,36 @@ int plain_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
   return GMM_OK;
 }
 
+// Batched MAP with FP32 statistics: one plain E-step per speaker over its frame range (the
+// reference's one-speaker-at-a-time AdaptModelMAP loop, OL_ModelAdapt.cpp:1165-1205), each into
+// its own statistics block, then one M-step launch for all speakers.
+int plain_map_batch(Ctx* c, const MapBatch& b) {
+  const int M = c->M, D = c->D;
+  const size_t stride = (size_t)M * (1 + 2 * D) + 2;
+  const size_t bytes = sizeof(double) * stride * (size_t)(b.S > 0 ? b.S : 1);
+  double* d_stats = nullptr;
+  int rc = dalloc(c, (void**)&d_stats, bytes, "per-speaker statistics");
+  if (rc) return rc;
+  cudaMemsetAsync(d_stats, 0, bytes, c->stream);
+  const float* X0 = c->X;
+  const long long N0 = c->N;
+  double* stats0 = c->stats;
+  for (int s = 0; s < b.S && !rc; ++s) {
+    c->X = X0 + (size_t)b.offs[s] * D;
+    c->N = b.offs[s + 1] - b.offs[s];
+    c->stats = d_stats + (size_t)s * stride;
+    if (c->N > 0) rc = plain_estep(c, b.flags, true, nullptr);
+  }
+  c->X = X0;
+  c->N = N0;
+  c->stats = stats0;
+  if (!rc) rc = mstep_map_batch(c, b, d_stats, kStatsPlain, 0, 0, nullptr);
+  if (!rc) rc = sync(c, "batched MAP (FP32 statistics)");
+  cudaStreamSynchronize(c->stream);
+  dfree(c, d_stats, bytes);
+  return rc;
+}
+
 }  // namespace gmm
 
 // ---------------------------------------------------------------------------------------------

@@ -15,24 +15,37 @@
 // (K x 256 bytes). A tile reaches shared memory in one cp.async.bulk.tensor.2d copy per plane over a
 // [rows][128 elements] view (256-byte rows); 64-row half tiles take one 1 KB copy per column chunk.
 //
-// Two kernels per E-step, both with one TMA-producer warp, one MMA-issuer warp and eight
-// epilogue warps (two per TMEM lane quadrant, each taking half of the accumulator columns):
-//   ll_kernel  (frame-tile major, persistent): S[128 frames x CT comps] per component chunk,
-//              online log2-sum-exp over all chunks in the epilogue -> per-frame log-likelihood.
-//   acc_kernel (component-chunk major): the chunk's W planes stay in shared memory; Z tiles
-//              stream through a 2-stage TMA ring. The MMA computes S^T[128 comps x FT frames];
+// Two kernels per E-step. Each has one TMA-producer warp, one MMA-issuer thread and eight
+// epilogue warps (two per TMEM lane quadrant); the MMAs take their A operand from TMEM
+// (tcgen05.mma ... [a_tmem], b_desc), so only B is read from shared memory and the TMA ring keeps
+// shared-memory bandwidth to itself.
+//   ll_kernel  (frame-tile major, persistent): four loader warps copy the 128-frame Z tile into
+//              TMEM (double-buffered where it fits); 128-component W chunks stream through a
+//              3-stage TMA ring; S[128 frames x 128 comps] accumulates in one of two TMEM
+//              buffers; the epilogue releases each buffer as soon as it has read it and runs an
+//              online log2-sum-exp over all chunks -> per-frame log-likelihood.
+//   acc_kernel (component-chunk major): the chunk's W planes are stored into TMEM once; Z tiles
+//              stream through a 3-deep TMA ring. The MMA computes S^T[128 comps x FT frames];
 //              the epilogue turns it in place into posteriors gamma = 2^(s - ll) (pruned at
-//              minGamma, split into bf16 hi + lo) and the next MMA uses those TMEM columns as
-//              its A operand: D2[comps x K] += Gamma^T [Z1, Z2] (hi*Z1 + hi*Z2 + lo*Z1), i.e. the
-//              n, F, S statistics in one [1, x, x^2] product. Posteriors never leave TMEM.
-//              D2 is double-buffered and flushed into per-CTA FP64 partials every `flush_every`
-//              tiles; a final kernel reduces the partials over CTAs in a fixed order.
+//              minGamma, split into bf16 hi + lo) and the statistics MMA uses those TMEM
+//              columns as its A operand: D2[comps x K] += Gamma^T Z with the five products
+//              hi*Z1 + hi*Z2 + hi*Z3 + lo*Z1 + lo*Z2 (x and x^2 need all three planes: two
+//              leave a 2^-17 relative error that the variance update S/n - mu^2 magnifies), i.e.
+//              the n, F, S statistics in one [x, x^2, 1] product. Posteriors never leave TMEM.
+//              D2 holds one tile's sums: the tensor core's FP32 accumulation over many tiles
+//              loses low bits steadily, so the epilogue reads D2 every tile (one tile late, off
+//              the MMA's critical path), sums tiles in FP32 registers with round-to-nearest and
+//              moves them into FP64 partials every 8192 frames; a final kernel reduces the
+//              partials over CTAs in a fixed order.
 // Every mbarrier wait is bounded (~2 s); on expiry the kernel raises an error flag, drains its
 // own copies and MMAs (bounded), frees TMEM and returns.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
 #include <math.h>
+
+#include <algorithm>
+#include <vector>
 
 #include "gmm_internal.cuh"
 #include "tc_ptx.cuh"
@@ -47,8 +60,6 @@ constexpr double kLog2e = 1.4426950408889634;
 constexpr float kLn2 = 0.69314718055994531f;
 constexpr long long kWaitLimit = 4000000000LL;  // clock cycles (~2 s)
 constexpr int kThreads = 320;                    // warp 0 TMA, warp 1 MMA, warps 2-9 epilogue
-
-__host__ __device__ constexpr int tile_frames(int K) { return K <= 96 ? 128 : 64; }
 
 // ------------------------------------------------------------------ operand preparation
 
@@ -74,32 +85,44 @@ __device__ __forceinline__ void split3d(double v, uint16_t& a, uint16_t& b, uint
   c = __bfloat16_as_ushort(h3);
 }
 
-// Z planes as tile images: element (frame f, column k) of plane p sits at
+// Z planes as tile images: element (row f, column k) of plane p sits at
 // ((p * nT + f / 128) * K/8 + k / 8) * 1024 + (f % 128) * 8 + k % 8; row f = [x, x^2, 1, 0...]
-// (zero rows past N). One thread per element, in image order (coalesced stores).
+// of frame row_frame[f] (identity when row_frame is null), zero for padding rows (past N, or
+// row_frame < 0). One thread per 8-column group of a row: it writes one 16-byte chunk per
+// plane, and a warp covers 32 consecutive rows of a group (512 contiguous bytes per plane).
 __global__ void features_kernel(const float* __restrict__ X, long long N, long long nT, int D,
-                                int K, uint16_t* __restrict__ planes) {
+                                int K, const long long* __restrict__ row_frame,
+                                uint16_t* __restrict__ planes) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int KC = K / 8;
-  if (t >= nT * 128 * K) return;
-  const int e = (int)(t & 7), r = (int)((t >> 3) & 127);
-  const long long blk = t >> 10;
+  if (t >= nT * 128 * KC) return;
+  const int r = (int)(t & 127);
+  const long long blk = t >> 7;  // (tile, column group) in image order
   const int c = (int)(blk % KC);
   const long long T = blk / KC;
-  const long long f = T * 128 + r;
-  const int k = c * 8 + e;
-  float v = 0.0f;
-  if (f < N) {
-    if (k < D) v = X[f * D + k];
-    else if (k < 2 * D) { float x = X[f * D + k - D]; v = x * x; }
-    else if (k == 2 * D) v = 1.0f;
+  const long long row = T * 128 + r;
+  const long long f = row_frame ? row_frame[row] : (row < N ? row : -1);
+  uint16_t a[8], b[8], cc[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    const int k = c * 8 + e;
+    float v = 0.0f;
+    if (f >= 0) {
+      if (k < D) v = X[f * D + k];
+      else if (k < 2 * D) { const float x = X[f * D + k - D]; v = x * x; }
+      else if (k == 2 * D) v = 1.0f;
+    }
+    split3f(v, a[e], b[e], cc[e]);
   }
-  uint16_t a, b, cc;
-  split3f(v, a, b, cc);
   const size_t plane = (size_t)nT * 128 * K;
-  planes[t] = a;
-  planes[plane + t] = b;
-  planes[2 * plane + t] = cc;
+  const size_t off = (size_t)t * 8;  // == (T * KC + c) * 1024 + r * 8
+  auto pack = [](const uint16_t* h) {
+    return make_uint4(h[0] | ((uint32_t)h[1] << 16), h[2] | ((uint32_t)h[3] << 16),
+                      h[4] | ((uint32_t)h[5] << 16), h[6] | ((uint32_t)h[7] << 16));
+  };
+  *reinterpret_cast<uint4*>(planes + off) = pack(a);
+  *reinterpret_cast<uint4*>(planes + plane + off) = pack(b);
+  *reinterpret_cast<uint4*>(planes + 2 * plane + off) = pack(cc);
 }
 
 // W planes as tile images (same layout as Z, rows = active components padded to 128, log2
@@ -228,7 +251,8 @@ constexpr int kLlThreads = 448;  // warp 0 TMA, 1 MMA, 2-9 epilogue, 10-13 Z loa
 template <int K>
 __global__ void __launch_bounds__(kLlThreads, 1)
     ll_kernel(const __grid_constant__ CUtensorMap wfull, const uint16_t* __restrict__ zplanes,
-              long long N, int nTz, int nTw, int n_tiles, int n_chunks, float trouble2, float minLL,
+              long long N, const long long* __restrict__ row_frame, int nTz, int nTw, int n_tiles,
+              int n_chunks, float trouble2, float minLL,
               float* __restrict__ ll2_out, float* __restrict__ ll_out, double* __restrict__ llpart,
               int* __restrict__ err) {
   using C = LlCfg<K>;
@@ -367,11 +391,18 @@ __global__ void __launch_bounds__(kLlThreads, 1)
         const int b = j & 1;
         if (!mbar_wait(&s_full[b], (j >> 1) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
         tc_fence_after();
+        // read both 32-column halves, then hand the accumulator back to the MMA issuer before
+        // doing the arithmetic: the issuer waits on this release, so it comes as early as possible
+        uint32_t vv[2][32];
+        tmem_ld32(tmem + lane_off + C::S_COL + b * 128 + hf * 64, vv[0]);
+        tmem_ld32(tmem + lane_off + C::S_COL + b * 128 + hf * 64 + 32, vv[1]);
+        tmem_ld_wait();
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&s_empty[b]);
 #pragma unroll
         for (int sub = 0; sub < 2; ++sub) {
-          uint32_t v[32];
-          tmem_ld32(tmem + lane_off + C::S_COL + b * 128 + hf * 64 + 32 * sub, v);
-          tmem_ld_wait();
+          const uint32_t* v = vv[sub];
           float mx = __uint_as_float(v[0]);
 #pragma unroll
           for (int k = 1; k < 32; ++k) mx = fmaxf(mx, __uint_as_float(v[k]));
@@ -387,9 +418,6 @@ __global__ void __launch_bounds__(kLlThreads, 1)
             m = mn;
           }
         }
-        tc_fence_before();
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&s_empty[b]);
       }
       // merge the two column halves of each row. Both warps of the pair reach both barriers on
       // every path and leave the tile loop together: the stop decision is one snapshot of the
@@ -402,14 +430,15 @@ __global__ void __launch_bounds__(kLlThreads, 1)
         const float M2 = fmaxf(m, m1);
         float S2 = 0.0f;
         if (M2 > -INFINITY) S2 = sum * ex2(m - M2) + s1 * ex2(m1 - M2);
-        const long long f = (long long)tile * 128 + row;
+        const long long f = (long long)tile * 128 + row;  // padded row
+        const long long fr = row_frame ? row_frame[f] : (f < N ? f : -1);
         float l2 = M2 + lg2(S2);
         const bool trouble = !(M2 > trouble2) || !isfinite(l2);
-        if (f < N) {
+        if (fr >= 0) {
           // trouble frames carry +inf (every posterior prunes to 0), padding carries NaN
           ll2_out[f] = trouble ? INFINITY : l2;
           const float lnat = trouble ? minLL : l2 * kLn2;
-          if (ll_out) ll_out[f] = lnat;
+          if (ll_out) ll_out[fr] = lnat;
           llsum += (double)lnat;
         } else {
           ll2_out[f] = __int_as_float(0x7fc00000);
@@ -429,6 +458,25 @@ __global__ void __launch_bounds__(kLlThreads, 1)
 }
 
 // ------------------------------------------------------------------ statistics kernel
+
+// Accumulation periods of one CTA's tile range, identical for the MMA issuer and the epilogue:
+// begin(j) must be called for j = 0, 1, 2, ... in order.
+struct Periods {
+  const int* slot;
+  int t0, nt, defslot;
+  int run_start = 0, period = -1;
+  __device__ Periods(const int* s, int t0_, int nt_, int d) : slot(s), t0(t0_), nt(nt_), defslot(d) {}
+  __device__ int slot_of(int j) const { return slot ? slot[t0 + j] : defslot; }
+  __device__ bool begin(int j, int flush) {
+    if (j == 0 || slot_of(j) != slot_of(j - 1)) run_start = j;
+    const bool fresh = ((j - run_start) % flush) == 0;
+    if (fresh) ++period;
+    return fresh;
+  }
+  __device__ bool end(int j, int flush) const {
+    return j == nt - 1 || slot_of(j + 1) != slot_of(j) || ((j + 1 - run_start) % flush) == 0;
+  }
+};
 
 // The component chunk's W planes are stored into TMEM once (A operand of the logits MMA); Z tiles
 // stream through an NZ-stage shared-memory ring; posteriors go from the logits accumulator into
@@ -459,6 +507,7 @@ template <int K>
 __global__ void __launch_bounds__(kThreads, 1)
     acc_kernel(const __grid_constant__ CUtensorMap zmap, const uint16_t* __restrict__ wplanes,
                int nTz, int nTw, const float* __restrict__ ll2, int n_tiles, int n_chunks, int slices,
+               const int* __restrict__ tile_slot, const int* __restrict__ slice_t0,
                float minGamma, int single_comp, double* __restrict__ part, int* __restrict__ err) {
   using C = AccCfg<K>;
   constexpr int FT = C::FT, NZ = C::NZ, FLUSH = C::FLUSH;
@@ -479,9 +528,19 @@ __global__ void __launch_bounds__(kThreads, 1)
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int chunk = (int)blockIdx.x % n_chunks, slice = (int)blockIdx.x / n_chunks;
-  const int per = (n_tiles + slices - 1) / slices;
-  const int t0 = slice * per;
-  const int nt = max(0, min(n_tiles, t0 + per) - t0);
+  int t0, nt;
+  if (slice_t0) {
+    t0 = slice_t0[slice];
+    nt = slice_t0[slice + 1] - t0;
+  } else {
+    const int per = (n_tiles + slices - 1) / slices;
+    t0 = slice * per;
+    nt = max(0, min(n_tiles, t0 + per) - t0);
+  }
+  // Statistics go to "slots": one per speaker with tile_slot (slices never split a speaker, so
+  // each (slot, chunk) has one owner), else one per slice. An accumulation period ends at a
+  // slot change or after FLUSH tiles of the same slot.
+  Periods per(tile_slot, t0, nt, slice);
 
   if (threadIdx.x == 0) {
     mbar_init(w_full, 8);
@@ -556,16 +615,13 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int b = j & 1;
         if (!mbar_wait(&g_full[b], (j >> 1) & 1, abort_flag, kWaitLimit)) return false;
         tc_fence_after();
-        const int period = j / FLUSH;
-        const bool fresh = (j % FLUSH) == 0;
-        if (fresh) {
-          if (!mbar_wait(d_empty, (period & 1) ^ 1, abort_flag, kWaitLimit)) return false;
-          tc_fence_after();
-        }
+        // D2 holds one tile: wait until the epilogue has read out tile j - 1
+        if (j > 0 && !mbar_wait(d_empty, (j - 1) & 1, abort_flag, kWaitLimit)) return false;
+        tc_fence_after();
         const uint32_t dcol = tmem + C::D_COL;
         const uint32_t gb = tmem + C::S_COL + b * FT;
         const uint32_t zb = zb0 + (j % NZ) * C::Z_STAGE;
-        int acc = fresh ? 0 : 1;
+        int acc = 0;
 #pragma unroll
         for (int q = 0; q < FT / 16; ++q) {
           const uint32_t hi = gb + 32 * (q >> 1) + 8 * (q & 1);
@@ -573,13 +629,17 @@ __global__ void __launch_bounds__(kThreads, 1)
           // B = Z as [N = K columns] x [K' = frames], MN-major: LBO along frames, SBO along columns
           const uint64_t z1 = smem_desc(zb + 0 * C::Z_PLANE + q * 2 * 128, 128, FT * 16);
           const uint64_t z2 = smem_desc(zb + 1 * C::Z_PLANE + q * 2 * 128, 128, FT * 16);
-          mma_ts(dcol, lo, z1, idesc_s, acc);
+          const uint64_t z3 = smem_desc(zb + 2 * C::Z_PLANE + q * 2 * 128, 128, FT * 16);
+          // gamma (hi + lo) x Z (z1 + z2 + z3): the five products above 2^-18, smallest first
+          mma_ts(dcol, lo, z2, idesc_s, acc);
           acc = 1;
+          mma_ts(dcol, hi, z3, idesc_s, 1);
+          mma_ts(dcol, lo, z1, idesc_s, 1);
           mma_ts(dcol, hi, z2, idesc_s, 1);
           mma_ts(dcol, hi, z1, idesc_s, 1);
         }
         mma_commit(&z_empty[j % NZ]);
-        if ((j % FLUSH) == FLUSH - 1 || j == nt - 1) mma_commit(d_full);
+        mma_commit(d_full);
         return true;
       };
       for (int i = 0; i < nt && ok; ++i) {
@@ -615,15 +675,62 @@ __global__ void __launch_bounds__(kThreads, 1)
       __syncwarp();
       if (lane == 0) mbar_arrive(w_full);
     }
-    double* mypart = part + ((size_t)blockIdx.x * 128 + row) * K;
-    constexpr int NCH = FT / 64;  // 32-frame chunks per warp
-    constexpr int KCH = K / 16;   // 16-column chunks of the statistics
-    const int kc0 = hf ? (KCH + 1) / 2 : 0, kc1 = hf ? KCH : (KCH + 1) / 2;
-    bool first_flush = true;
+    constexpr int NCH = FT / 64;         // 32-frame chunks per warp
+    constexpr int KCH = K / 16;          // 16-column chunks of the statistics
+    constexpr int KH = (KCH + 1) / 2;    // chunks per warp of a pair
+    const int kc0 = hf ? KH : 0, kc1 = hf ? KCH : KH;
+    // The statistics MMA leaves one tile's sums in D2. The epilogue reads them one tile late
+    // (after the next tile's posteriors, so that it never waits on the MMA), adds them into
+    // FP32 registers with round-to-nearest, and moves the registers into the FP64 partials at
+    // the end of each accumulation period (FLUSH tiles of one slot).
+    float dacc[KH * 16];
+#pragma unroll
+    for (int k = 0; k < KH * 16; ++k) dacc[k] = 0.0f;
+    int last_slot = -1;
+    auto readout = [&](int t, bool flush, int slot) -> bool {
+      if (!mbar_wait(d_full, t & 1, abort_flag, kWaitLimit)) return false;
+      tc_fence_after();
+#pragma unroll
+      for (int cc = 0; cc < KH; ++cc) {
+        if (kc0 + cc < kc1) {
+          uint32_t r[16];
+          tmem_ld16(tmem + lane_off + C::D_COL + 16 * (kc0 + cc), r);
+          tmem_ld_wait();
+#pragma unroll
+          for (int k = 0; k < 16; ++k) dacc[cc * 16 + k] += __uint_as_float(r[k]);
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(d_empty);
+      if (flush) {
+        double* mypart = part + ((size_t)slot * n_chunks + chunk) * K * 128 + row;  // [col][row]
+        const bool first_flush = slot != last_slot;
+        last_slot = slot;
+#pragma unroll
+        for (int cc = 0; cc < KH; ++cc) {
+          if (kc0 + cc < kc1) {
+#pragma unroll
+            for (int k = 0; k < 16; ++k) {
+              double* dst = mypart + (size_t)(16 * (kc0 + cc) + k) * 128;
+              if (first_flush) *dst = (double)dacc[cc * 16 + k];
+              else *dst += (double)dacc[cc * 16 + k];
+              dacc[cc * 16 + k] = 0.0f;
+            }
+          }
+        }
+      }
+      return true;
+    };
+    bool ok = true;
     for (int i = 0; i < nt; ++i) {
       const int b = i & 1;
-      if (!mbar_wait(&z_full[i % NZ], (i / NZ) & 1, abort_flag, kWaitLimit)) break;
-      if (!mbar_wait(&s_full[b], (i >> 1) & 1, abort_flag, kWaitLimit)) break;
+      // period bookkeeping of the previous tile, before begin(i) moves the run start
+      const bool end_prev = i > 0 && per.end(i - 1, FLUSH);
+      const int slot_prev = i > 0 ? per.slot_of(i - 1) : 0;
+      per.begin(i, FLUSH);
+      if (!mbar_wait(&z_full[i % NZ], (i / NZ) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
+      if (!mbar_wait(&s_full[b], (i >> 1) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
       tc_fence_after();
       const float* lls = ll_s + (i % NZ) * FT;
 #pragma unroll 1
@@ -669,28 +776,9 @@ __global__ void __launch_bounds__(kThreads, 1)
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&g_full[b]);
-      if ((i % FLUSH) == FLUSH - 1 || i == nt - 1) {
-        const int p = i / FLUSH;
-        if (!mbar_wait(d_full, p & 1, abort_flag, kWaitLimit)) break;
-        tc_fence_after();
-#pragma unroll 1
-        for (int c = kc0; c < kc1; ++c) {
-          uint32_t r[16];
-          tmem_ld16(tmem + lane_off + C::D_COL + 16 * c, r);
-          tmem_ld_wait();
-#pragma unroll
-          for (int k = 0; k < 16; ++k) {
-            const double dv = (double)__uint_as_float(r[k]);
-            if (first_flush) mypart[16 * c + k] = dv;
-            else mypart[16 * c + k] += dv;
-          }
-        }
-        first_flush = false;
-        tc_fence_before();
-        __syncwarp();
-        if (lane == 0) mbar_arrive(d_empty);
-      }
+      if (i > 0 && !readout(i - 1, end_prev, slot_prev)) { ok = false; break; }
     }
+    if (ok && !*abort_flag) readout(nt - 1, true, per.slot_of(nt - 1));
   }
   __syncthreads();
   if (threadIdx.x == 0 && *abort_flag) atomicExch(err, 1);
@@ -700,20 +788,21 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
 }
 
-// part [cta][128][K] -> stats (caller order), summing CTAs of each chunk in slice order.
+// part [cta][K][128] -> stats (caller order), summing CTAs of each chunk in slice order.
 __global__ void reduce_kernel(int M, int D, int K, int Mact, int n_chunks, int slices, int n_tiles,
                               const int* __restrict__ comp_of_row, const double* __restrict__ part,
                               int flags, double* __restrict__ stats) {
+  // thread order = partial layout order [chunk][col][row] (coalesced reads)
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)Mact * K) return;
-  const int r = (int)(t / K), e = (int)(t - (long long)r * K);
-  if (e > 2 * D) return;
-  const int ch = r / 128, rr = r - ch * 128;
+  if (t >= (long long)n_chunks * K * 128) return;
+  const int rr = (int)(t & 127), e = (int)((t >> 7) % K), ch = (int)(t / (128LL * K));
+  const int r = ch * 128 + rr;
+  if (r >= Mact || e > 2 * D) return;
   const int per = (n_tiles + slices - 1) / slices;
   double s = 0.0;
   for (int sl = 0; sl < slices; ++sl) {
     if (sl * per >= n_tiles) break;
-    s += part[(((size_t)sl * n_chunks + ch) * 128 + rr) * K + e];
+    s += part[(((size_t)sl * n_chunks + ch) * K + e) * 128 + rr];
   }
   const int m = comp_of_row[r];
   if (e == 2 * D) stats[m] += s;
@@ -733,6 +822,70 @@ __global__ void ll_total_kernel(int n, const double* __restrict__ llpart, double
     for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += red[k];
     *tot += s;
   }
+}
+
+// ------------------------------------------------------------------ batched MAP support
+
+// row_of_comp[m] = row of component m in the padded active list, -1 when m is inactive.
+__global__ void row_of_comp_kernel(int M, int Mpad, const int* __restrict__ comp_of_row,
+                                   int* __restrict__ row_of_comp) {
+  for (int m = threadIdx.x; m < M; m += blockDim.x) row_of_comp[m] = -1;
+  __syncthreads();
+  for (int r = threadIdx.x; r < Mpad; r += blockDim.x)
+    if (comp_of_row[r] >= 0) row_of_comp[comp_of_row[r]] = r;
+}
+
+// Per-speaker total log-likelihood: FP64 sum of the speaker's frame log-likelihoods (strided
+// per thread, then a fixed warp and block tree).
+__global__ void seg_sum_kernel(const long long* __restrict__ offs, const float* __restrict__ ll,
+                               double* __restrict__ out) {
+  __shared__ double red[32];
+  const int s = blockIdx.x;
+  double v = 0.0;
+  for (long long f = offs[s] + threadIdx.x; f < offs[s + 1]; f += blockDim.x) v += (double)ll[f];
+  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[k];
+    out[s] = t;
+  }
+}
+
+template <int K>
+int map_batch_launch(Ctx* c, long long Rpad, const long long* d_row_frame, const int* d_tile_slot,
+                     const int* d_slice_t0, int slices, double* d_part) {
+  using LC = LlCfg<K>;
+  using AC = AccCfg<K>;
+  const int nTz = (int)(Rpad / 128), nTw = c->tcm.Mpad / 128;
+  int grid_ll = std::min(nTz, c->sms);
+  if (grid_ll < 1) grid_ll = 1;
+  const size_t need = (size_t)grid_ll * 128;
+  if (need > c->tc_llpart_cap) {
+    dfree(c, c->tc_llpart, c->tc_llpart_cap * sizeof(double));
+    c->tc_llpart = nullptr;
+    c->tc_llpart_cap = 0;
+    int rc = dalloc(c, (void**)&c->tc_llpart, need * sizeof(double), "tc llpart");
+    if (rc) return rc;
+    c->tc_llpart_cap = need;
+  }
+  cudaFuncSetAttribute(ll_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, LC::SMEM);
+  cudaFuncSetAttribute(acc_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, AC::SMEM);
+  {
+    GMM_LAUNCH(c, "tc_ll_kernel");
+    ll_kernel<K><<<grid_ll, kLlThreads, LC::SMEM, c->stream>>>(
+        c->tm_wfull, c->tcx.planes, c->N, d_row_frame, nTz, nTw, nTz, nTw,
+        (float)(c->minLL * kLog2e), c->minLL, c->tcm.ll2, c->ll, c->tc_llpart, c->tc_err);
+  }
+  {
+    GMM_LAUNCH(c, "tc_acc_kernel");
+    const CUtensorMap& zm = AC::FT == 128 ? c->tm_zfull : c->tm_zhalf;
+    acc_kernel<K><<<nTw * slices, kThreads, AC::SMEM, c->stream>>>(
+        zm, c->tcm.planes, nTz, nTw, c->tcm.ll2, (int)(Rpad / AC::FT), nTw, slices, d_tile_slot,
+        d_slice_t0, c->minGamma, c->Mact == 1, d_part, c->tc_err);
+  }
+  return GMM_OK;
 }
 
 // ------------------------------------------------------------------ host side
@@ -793,7 +946,7 @@ int launch_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
   {
     GMM_LAUNCH(c, "tc_ll_kernel");
     ll_kernel<K><<<grid_ll, kLlThreads, LC::SMEM, c->stream>>>(
-        c->tm_wfull, c->tcx.planes, c->N, nTz, nTw, n_tiles_ll, n_chunks, trouble2, c->minLL,
+        c->tm_wfull, c->tcx.planes, c->N, nullptr, nTz, nTw, n_tiles_ll, n_chunks, trouble2, c->minLL,
         c->tcm.ll2, ll_out_dev, c->tc_llpart, c->tc_err);
   }
   if (!want_stats) return GMM_OK;
@@ -824,12 +977,12 @@ int launch_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
     GMM_LAUNCH(c, "tc_acc_kernel");
     const CUtensorMap& zm = AC::FT == 128 ? c->tm_zfull : c->tm_zhalf;
     acc_kernel<K><<<grid, kThreads, AC::SMEM, c->stream>>>(
-        zm, c->tcm.planes, nTz, nTw, c->tcm.ll2, n_tiles, n_chunks, slices, c->minGamma,
-        c->Mact == 1, c->tcpart, c->tc_err);
+        zm, c->tcm.planes, nTz, nTw, c->tcm.ll2, n_tiles, n_chunks, slices, nullptr, nullptr,
+        c->minGamma, c->Mact == 1, c->tcpart, c->tc_err);
   }
   {
     GMM_LAUNCH(c, "tc_reduce_kernel");
-    long long tot = (long long)c->Mact * K;
+    long long tot = (long long)n_chunks * K * 128;
     reduce_kernel<<<(int)((tot + 255) / 256), 256, 0, c->stream>>>(
         c->M, c->D, K, c->Mact, n_chunks, slices, n_tiles, c->tcm.comp_of_row, c->tcpart, flags, c->stats);
   }
@@ -848,21 +1001,21 @@ int tc_prepare_features(Ctx* c) {
   const size_t bytes = (size_t)3 * Npad * K * sizeof(uint16_t);
   if (c->tcx.planes == nullptr || c->tcx.Npad != Npad || c->tcx.K != K) {
     dfree(c, c->tcx.planes, (size_t)3 * c->tcx.Npad * c->tcx.K * sizeof(uint16_t));
+    dfree(c, c->tcm.ll2, sizeof(float) * (size_t)c->tcx.Npad);
     c->tcx.planes = nullptr;
+    c->tcm.ll2 = nullptr;
+    c->tcx.Npad = 0;
     int rc = dalloc(c, (void**)&c->tcx.planes, bytes, "tensor-core feature planes");
+    if (!rc) rc = dalloc(c, (void**)&c->tcm.ll2, sizeof(float) * (size_t)Npad, "tensor-core frame LSE");
     if (rc) return rc;
     c->tcx.Npad = Npad;
     c->tcx.K = K;
-    dfree(c, c->tcm.ll2, 0);
-    c->tcm.ll2 = nullptr;
-    rc = dalloc(c, (void**)&c->tcm.ll2, sizeof(float) * (size_t)Npad, "tensor-core frame LSE");
-    if (rc) return rc;
   }
   {
     GMM_LAUNCH(c, "tc_features_kernel");
-    const long long tot = Npad * K;
+    const long long tot = Npad * (K / 8);
     features_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(c->X, c->N, Npad / 128, c->D, K,
-                                                                         c->tcx.planes);
+                                                                         nullptr, c->tcx.planes);
   }
   int rc = make_map(c, &c->tm_zfull, c->tcx.planes, 3 * Npad * K, K);
   if (!rc) rc = make_map(c, &c->tm_zhalf, c->tcx.planes, 3 * Npad * K, 4);
@@ -875,8 +1028,8 @@ int tc_prepare_model(Ctx* c) {
   const int K = tc_K(c->D);
   const int Mpad = (c->Mact + 127) / 128 * 128;
   if (c->tcm.planes == nullptr || c->tcm.Mpad != Mpad || c->tcm.K != K) {
-    dfree(c, c->tcm.planes, 0);
-    dfree(c, c->tcm.comp_of_row, 0);
+    dfree(c, c->tcm.planes, (size_t)3 * c->tcm.Mpad * c->tcm.K * sizeof(uint16_t));
+    dfree(c, c->tcm.comp_of_row, sizeof(int) * (size_t)c->tcm.Mpad);
     c->tcm.planes = nullptr;
     c->tcm.comp_of_row = nullptr;
     int rc = dalloc(c, (void**)&c->tcm.planes, (size_t)3 * Mpad * K * sizeof(uint16_t), "tensor-core model planes");
@@ -936,6 +1089,130 @@ int tc_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
     return fail(c, GMM_ERR_TIMEOUT, "tensor-core E-step: a bounded device wait expired");
   }
   return GMM_OK;
+}
+
+
+// Batched MAP, tensor-core statistics: every speaker's frames are laid out from a 128-row tile
+// boundary (padding rows carry no frame), the logits kernel runs once over all tiles, and the
+// statistics kernel gives each (speaker, component chunk) its own FP64 accumulator slot; its
+// frame-tile slices are cut at speaker boundaries so that every slot has one writer.
+int tc_map_batch(Ctx* c, const MapBatch& b) {
+  if (!tc_supported(c->D)) return fail(c, GMM_ERR_UNSUPPORTED, "tensor-core path supports 1 <= D <= 63");
+  if (!c->tc_err) {
+    int rc = dalloc(c, (void**)&c->tc_err, sizeof(int), "tc error flag");
+    if (rc) return rc;
+    cudaMemsetAsync(c->tc_err, 0, sizeof(int), c->stream);
+    int dev;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, dev);
+  }
+  const int S = b.S, M = c->M, D = c->D, K = tc_K(D);
+  const long long* offs = b.offs;
+  int rc = tc_prepare_model(c);
+  if (rc) return rc;
+  const int FT = acc_ft(K);
+  const int n_chunks = c->tcm.Mpad / 128;
+  // padded row layout: speaker s starts at row pad[s], a multiple of 128
+  std::vector<long long> pad((size_t)S + 1, 0);
+  for (int s = 0; s < S; ++s) pad[s + 1] = pad[s] + (offs[s + 1] - offs[s] + 127) / 128 * 128;
+  const long long Rpad = pad[S] > 0 ? pad[S] : 128;
+  std::vector<long long> row_frame((size_t)Rpad, -1);
+  for (int s = 0; s < S; ++s)
+    for (long long f = offs[s]; f < offs[s + 1]; ++f) row_frame[(size_t)(pad[s] + f - offs[s])] = f;
+  const long long ntiles = Rpad / FT;
+  std::vector<int> tile_slot((size_t)ntiles, 0);
+  for (int s = 0; s < S; ++s)
+    for (long long t = pad[s] / FT; t < pad[s + 1] / FT; ++t) tile_slot[(size_t)t] = s;
+  // slices: contiguous speaker ranges of about equal tile counts, one CTA per (slice, chunk)
+  const int want = std::max(1, std::min<int>((int)ntiles, c->sms / n_chunks));
+  std::vector<int> slice_t0(1, 0);
+  {
+    const double target = (double)ntiles / want;
+    for (int s = 0; s + 1 < S && (int)slice_t0.size() < want; ++s)
+      if ((double)(pad[s + 1] / FT) >= target * (double)slice_t0.size() && pad[s + 1] / FT > slice_t0.back())
+        slice_t0.push_back((int)(pad[s + 1] / FT));
+    slice_t0.push_back((int)ntiles);
+  }
+  const int slices = (int)slice_t0.size() - 1;
+  const size_t part_bytes = (size_t)S * n_chunks * 128 * K * sizeof(double);
+  const size_t rf_bytes = sizeof(long long) * (size_t)Rpad, ts_bytes = sizeof(int) * (size_t)ntiles;
+  const size_t st_bytes = sizeof(int) * (size_t)(slices + 1), roc_bytes = sizeof(int) * (size_t)M;
+  long long* d_rf = nullptr;
+  int *d_ts = nullptr, *d_st = nullptr, *d_roc = nullptr;
+  double* d_part = nullptr;
+  rc = dalloc(c, (void**)&d_rf, rf_bytes, "row map");
+  if (!rc) rc = dalloc(c, (void**)&d_ts, ts_bytes, "tile slots");
+  if (!rc) rc = dalloc(c, (void**)&d_st, st_bytes, "slice ranges");
+  if (!rc) rc = dalloc(c, (void**)&d_roc, roc_bytes, "component rows");
+  if (!rc) rc = dalloc(c, (void**)&d_part, part_bytes, "per-speaker statistics");
+  if (!rc) {
+    // operand planes in the padded layout; the next regular E-step rebuilds its own
+    const size_t pbytes = (size_t)3 * Rpad * K * sizeof(uint16_t);
+    if (c->tcx.planes == nullptr || c->tcx.Npad != Rpad || c->tcx.K != K) {
+      dfree(c, c->tcx.planes, (size_t)3 * c->tcx.Npad * c->tcx.K * sizeof(uint16_t));
+      dfree(c, c->tcm.ll2, sizeof(float) * (size_t)c->tcx.Npad);
+      c->tcx.planes = nullptr;
+      c->tcm.ll2 = nullptr;
+      c->tcx.Npad = 0;
+      rc = dalloc(c, (void**)&c->tcx.planes, pbytes, "tensor-core feature planes");
+      if (!rc) rc = dalloc(c, (void**)&c->tcm.ll2, sizeof(float) * (size_t)Rpad, "tensor-core frame LSE");
+      if (!rc) {
+        c->tcx.Npad = Rpad;
+        c->tcx.K = K;
+      }
+    }
+    c->tcx_valid = false;
+  }
+  if (!rc) {
+    cudaMemcpyAsync(d_rf, row_frame.data(), rf_bytes, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(d_ts, tile_slot.data(), ts_bytes, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(d_st, slice_t0.data(), st_bytes, cudaMemcpyHostToDevice, c->stream);
+    cudaMemsetAsync(d_part, 0, part_bytes, c->stream);
+    GMM_LAUNCH(c, "tc_features_kernel");
+    features_kernel<<<(unsigned)((Rpad * (K / 8) + 255) / 256), 256, 0, c->stream>>>(
+        c->X, c->N, Rpad / 128, D, K, d_rf, c->tcx.planes);
+  }
+  if (!rc) rc = make_map(c, &c->tm_zfull, c->tcx.planes, 3 * Rpad * K, K);
+  if (!rc) rc = make_map(c, &c->tm_zhalf, c->tcx.planes, 3 * Rpad * K, 4);
+  if (!rc) {
+    switch (K) {
+      case 16: rc = map_batch_launch<16>(c, Rpad, d_rf, d_ts, d_st, slices, d_part); break;
+      case 32: rc = map_batch_launch<32>(c, Rpad, d_rf, d_ts, d_st, slices, d_part); break;
+      case 48: rc = map_batch_launch<48>(c, Rpad, d_rf, d_ts, d_st, slices, d_part); break;
+      case 64: rc = map_batch_launch<64>(c, Rpad, d_rf, d_ts, d_st, slices, d_part); break;
+      case 80: rc = map_batch_launch<80>(c, Rpad, d_rf, d_ts, d_st, slices, d_part); break;
+      case 96: rc = map_batch_launch<96>(c, Rpad, d_rf, d_ts, d_st, slices, d_part); break;
+      case 112: rc = map_batch_launch<112>(c, Rpad, d_rf, d_ts, d_st, slices, d_part); break;
+      default: rc = map_batch_launch<128>(c, Rpad, d_rf, d_ts, d_st, slices, d_part); break;
+    }
+  }
+  if (!rc) {
+    {
+      GMM_LAUNCH(c, "row_of_comp_kernel");
+      row_of_comp_kernel<<<1, 1024, 0, c->stream>>>(M, c->tcm.Mpad, c->tcm.comp_of_row, d_roc);
+    }
+    if (S > 0) {
+      GMM_LAUNCH(c, "seg_sum_kernel");
+      seg_sum_kernel<<<S, 256, 0, c->stream>>>(b.d_offs, c->ll, b.ll);
+    }
+    rc = mstep_map_batch(c, b, d_part, kStatsSlots, K, n_chunks, d_roc);
+  }
+  if (!rc) {
+    int herr = 0;
+    cudaMemcpyAsync(&herr, c->tc_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+    rc = sync(c, "batched MAP (tensor-core statistics)");
+    if (!rc && herr) {
+      cudaMemsetAsync(c->tc_err, 0, sizeof(int), c->stream);
+      rc = fail(c, GMM_ERR_TIMEOUT, "batched MAP: a bounded device wait expired");
+    }
+  }
+  cudaStreamSynchronize(c->stream);
+  dfree(c, d_rf, rf_bytes);
+  dfree(c, d_ts, ts_bytes);
+  dfree(c, d_st, st_bytes);
+  dfree(c, d_roc, roc_bytes);
+  dfree(c, d_part, part_bytes);
+  return rc;
 }
 
 }  // namespace gmm

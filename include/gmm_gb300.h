@@ -103,6 +103,21 @@ int gmm_loglikes(gmm_handle h, float* out);
 int gmm_em_update(gmm_handle h, int up_weight, int up_mean, int up_var, int* alive);
 /* CModelAdapt::UpdateModelMAP with tau > 0 (OL_ModelAdapt.cpp:1024-1106) against the prior. */
 int gmm_map_update(gmm_handle h, int tau, int up_weight, int up_mean, int up_var);
+/* One MAP iteration for S speakers in one call: the per-speaker loop of Model_ADAPT
+ * (projects/Model_ADAPT/Model_ADAPT.cpp:170-240) around CModelAdapt::AdaptModel with
+ * adaptType MAP and one MAP iteration (OL_ModelAdapt.cpp:1163-1174, AdaptModelMAP :1250-1274,
+ * IterMAP :1298-1316, UpdateModelMAP :1024-1106). The resident model is the UBM; the resident
+ * features hold every speaker's frames back to back, speaker s owning rows
+ * [offs[s], offs[s+1]) (offs: S + 1 non-decreasing entries, offs[S] <= N). With GMM_PREC_TC one
+ * fused E-step covers all speakers; with GMM_PREC_FP32 the speakers run one after the other.
+ * Outputs (host, any may be NULL): w [S][M], mu [S][M][D], var [S][M][D], ll [S] (each speaker's
+ * total log-likelihood under the UBM). tau >= 1. The resident model is not changed. */
+int gmm_map_batch(gmm_handle h, int S, const long long* offs, int tau, int up_weight, int up_mean,
+                  int up_var, float* w, float* mu, float* var, double* ll);
+/* The same with device outputs (d_w, d_mu, d_var, d_ll on the handle's device; any may be NULL). */
+int gmm_map_batch_device(gmm_handle h, int S, const long long* offs, int tau, int up_weight,
+                         int up_mean, int up_var, float* d_w, float* d_mu, float* d_var,
+                         double* d_ll);
 /* `iters` EM iterations entirely on the device (CModelAdapt::IterEM with tau = 0,
  * OL_ModelAdapt.cpp:1276-1296): each iteration moves zero-weight components behind the others
  * as insertModel does, accumulates and updates. ll[i] = total log-likelihood of iteration i.

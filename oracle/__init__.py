@@ -125,13 +125,13 @@ def loglikes64(X, w, mu, var, **kw):
     return out
 
 
-def accumulate64(X, w, mu, var, flags=ACC_MEAN | ACC_VAR, **kw):
+def accumulate64(X, w, mu, var, flags=ACC_MEAN | ACC_VAR, threads=1, **kw):
     X, w, mu, var = map(_f32, (X, w, mu, var))
     N, D = X.shape
     M = len(w)
     n, F, S = np.zeros(M), np.zeros((M, D)), np.zeros((M, D))
     tl, tn = C.c_double(0.0), C.c_longlong(0)
-    o = _opts(1, **kw)
+    o = _opts(threads, **kw)
     rc = lib().orc64_accumulate(_p(X), C.c_longlong(N), D, M, _p(w), _p(mu), _p(var),
                                 C.byref(o), flags, _p(n), _p(F), _p(S), C.byref(tl), C.byref(tn))
     if rc:

@@ -360,38 +360,95 @@ int orc64_loglikes(const float* X, long long N, int D, int M, const float* w, co
   return 0;
 }
 
+typedef struct {
+  const model64* m;
+  const float* X;
+  long long f0, f1;
+  int D, M, nactive, fm, fv, probsOnly;
+  const orc_opts* o;
+  double *n, *F, *S, tl;
+} acc64_job;
+
+static void* acc64_thread(void* arg) {
+  acc64_job* j = (acc64_job*)arg;
+  const model64* m = j->m;
+  const int M = j->M, D = j->D;
+  double* g = (double*)malloc(sizeof(double) * (size_t)M);
+  for (long long i = j->f0; i < j->f1; ++i) {
+    const float* x = j->X + (size_t)i * D;
+    double ll = frame64(m, x, g);
+    if (ll == -INFINITY) { j->tl += (double)j->o->minLogLike; continue; }
+    j->tl += ll;
+    for (int c = 0; c < M; ++c) {
+      if (!(m->w[c] > 0)) continue;
+      double gc = (j->nactive == 1) ? 1.0 : exp(g[c] - ll);
+      if (gc <= (double)j->o->minGamma) continue;
+      j->n[c] += gc;
+      if (j->probsOnly) continue;
+      for (int k = 0; k < D; ++k) {
+        double xv = x[k];
+        if (j->fm) j->F[(size_t)c * D + k] += gc * xv;
+        if (j->fv) j->S[(size_t)c * D + k] += gc * xv * xv;
+      }
+    }
+  }
+  free(g);
+  return NULL;
+}
+
+/* FP64 statistics. With o->threads = T > 1 the frames are split into T contiguous ranges whose
+ * private sums are added in range order (a precision reference: only the FP64 summation order
+ * depends on T). */
 int orc64_accumulate(const float* X, long long N, int D, int M, const float* w, const float* mu,
                      const float* var, const orc_opts* o, int flags, double* n, double* F,
                      double* S, double* totLL, long long* totN) {
   model64 m;
   int rc = prep64(&m, M, D, w, mu, var, o);
   if (rc) { free(m.logc); return rc; }
-  int nactive = count_active(M, w);
-  double* g = (double*)malloc(sizeof(double) * (size_t)M);
-  int fm = (flags & ORC_ACC_MEAN) != 0, fv = (flags & ORC_ACC_VAR) != 0;
-  int probsOnly = (flags & ORC_ACC_PROBS_ONLY) != 0;
-  double tl = *totLL;
-  for (long long i = 0; i < N; ++i) {
-    const float* x = X + (size_t)i * D;
-    double ll = frame64(&m, x, g);
-    if (ll == -INFINITY) { tl += (double)o->minLogLike; continue; }
-    tl += ll;
-    for (int c = 0; c < M; ++c) {
-      if (!(w[c] > 0)) continue;
-      double gc = (nactive == 1) ? 1.0 : exp(g[c] - ll);
-      if (gc <= (double)o->minGamma) continue;
-      n[c] += gc;
-      if (probsOnly) continue;
-      for (int k = 0; k < D; ++k) {
-        double xv = x[k];
-        if (fm) F[(size_t)c * D + k] += gc * xv;
-        if (fv) S[(size_t)c * D + k] += gc * xv * xv;
-      }
+  int T = o->threads < 1 ? 1 : o->threads;
+  if (N < (long long)T * 64) T = 1;
+  acc64_job* jobs = (acc64_job*)calloc((size_t)T, sizeof(acc64_job));
+  pthread_t* th = (pthread_t*)calloc((size_t)T, sizeof(pthread_t));
+  for (int t = 0; t < T; ++t) {
+    acc64_job* j = &jobs[t];
+    j->m = &m; j->X = X; j->D = D; j->M = M; j->o = o;
+    j->f0 = N * t / T; j->f1 = N * (t + 1) / T;
+    j->nactive = count_active(M, w);
+    j->fm = (flags & ORC_ACC_MEAN) != 0;
+    j->fv = (flags & ORC_ACC_VAR) != 0;
+    j->probsOnly = (flags & ORC_ACC_PROBS_ONLY) != 0;
+    if (T == 1) {
+      j->n = n; j->F = F; j->S = S; j->tl = *totLL;
+    } else {
+      j->n = (double*)calloc((size_t)M, sizeof(double));
+      j->F = (double*)calloc((size_t)M * D, sizeof(double));
+      j->S = (double*)calloc((size_t)M * D, sizeof(double));
+      j->tl = 0.0;
     }
   }
-  *totLL = tl;
+  if (T == 1) {
+    acc64_thread(&jobs[0]);
+    *totLL = jobs[0].tl;
+  } else {
+    for (int t = 0; t < T; ++t) pthread_create(&th[t], NULL, acc64_thread, &jobs[t]);
+    for (int t = 0; t < T; ++t) pthread_join(th[t], NULL);
+    double tl = *totLL;
+    for (int t = 0; t < T; ++t) {
+      for (int c = 0; c < M; ++c) n[c] += jobs[t].n[c];
+      for (size_t e = 0; e < (size_t)M * D; ++e) {
+        F[e] += jobs[t].F[e];
+        S[e] += jobs[t].S[e];
+      }
+      tl += jobs[t].tl;
+      free(jobs[t].n);
+      free(jobs[t].F);
+      free(jobs[t].S);
+    }
+    *totLL = tl;
+  }
   *totN += N;
-  free(g);
+  free(jobs);
+  free(th);
   free(m.logc);
   return 0;
 }
