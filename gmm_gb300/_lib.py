@@ -48,7 +48,21 @@ SIGNATURES = {
     "gmm_profile_read": (_i, [_vp, _i, C.POINTER(C.c_char_p), _vp, _vp]),
     "gmm_launch_count": (_ll, [_vp]),
     "gmm_accumulate_noalloc": (_i, [_vp, _ll, _i, _i, _vp, _vp, _vp, _f, _f, _f, _i, _vp, _vp]),
+    "gmm_server_create": (_i, [_i, _i, _i, _i, _sz, C.POINTER(_vp)]),
+    "gmm_server_destroy": (_i, [_vp]),
+    "gmm_server_last_error": (C.c_char_p, [_vp]),
+    "gmm_server_set_options": (_i, [_vp, _f, _f, _f, _i]),
+    "gmm_server_add_model": (_i, [_vp, _vp, _vp, _vp, C.POINTER(_i)]),
+    "gmm_server_submit": (_i, [_vp, _i, _i, _vp, _ll, _i, _i, _i, _i, _i, C.POINTER(_ll)]),
+    "gmm_server_poll": (_i, [_vp, _ll, C.POINTER(_i)]),
+    "gmm_server_wait": (_i, [_vp, _ll, _i]),
+    "gmm_server_result": (_i, [_vp, _ll, C.POINTER(_d), _vp, _vp, _vp, _vp, C.POINTER(_d)]),
+    "gmm_server_stats": (_i, [_vp, C.POINTER(_ll), C.POINTER(_ll), C.POINTER(_ll), C.POINTER(_sz)]),
 }
+
+REQ_SCORE, REQ_MAP = 0, 1
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
+SUBMIT_FRAME_LL, SUBMIT_NO_COPY = 1, 2
 
 _lib = None
 
@@ -259,3 +273,100 @@ class Handle:
 
     def launch_count(self) -> int:
         return int(self.lib.gmm_launch_count(self.h))
+
+
+class Server:
+    """Continuous-batching request server (gmm_server_*): resident models, scoring and MAP
+    requests. submit() returns a ticket; result() waits and returns the request's outputs."""
+
+    def __init__(self, device: int, D: int, M: int, max_models: int, request_bytes: int):
+        self.lib = load()
+        h = C.c_void_p()
+        rc = self.lib.gmm_server_create(device, D, M, max_models, request_bytes, C.byref(h))
+        if rc:
+            raise GMMError(rc, self.lib.gmm_server_last_error(None).decode())
+        self.h, self.D, self.M = h, D, M
+        self._keep = {}
+
+    def check(self, rc):
+        if rc:
+            raise GMMError(rc, self.lib.gmm_server_last_error(self.h).decode())
+        return rc
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.gmm_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_options(self, min_loglike=-1e20, min_gamma=1e-4, min_var=1e-6, max_batch=4096):
+        self.check(self.lib.gmm_server_set_options(self.h, min_loglike, min_gamma, min_var, max_batch))
+
+    def add_model(self, w, mu, var) -> int:
+        w = np.ascontiguousarray(w, np.float32)
+        mu = np.ascontiguousarray(mu, np.float32)
+        var = np.ascontiguousarray(var, np.float32)
+        mid = C.c_int()
+        self.check(self.lib.gmm_server_add_model(self.h, ptr(w), ptr(mu), ptr(var), C.byref(mid)))
+        return mid.value
+
+    def submit(self, kind, model, X, tau=16, upW=0, upM=1, upV=0, frame_ll=False, no_copy=False) -> int:
+        """no_copy: X must stay alive and unchanged until result() (the server keeps a reference)."""
+        X = np.ascontiguousarray(X, np.float32)
+        t = C.c_longlong()
+        opts = (SUBMIT_FRAME_LL if frame_ll else 0) | (SUBMIT_NO_COPY if no_copy else 0)
+        self.check(self.lib.gmm_server_submit(self.h, kind, model, ptr(X), len(X), tau, upW, upM, upV,
+                                              opts, C.byref(t)))
+        if no_copy:
+            self._keep[t.value] = X
+        self._n = getattr(self, "_n", {})
+        self._n[t.value] = (kind, len(X), bool(frame_ll))
+        return t.value
+
+    def poll(self, ticket) -> int:
+        st = C.c_int()
+        self.check(self.lib.gmm_server_poll(self.h, ticket, C.byref(st)))
+        return st.value
+
+    def wait(self, ticket, timeout_ms=-1):
+        self.check(self.lib.gmm_server_wait(self.h, ticket, timeout_ms))
+
+    def result(self, ticket, timeout_ms=-1):
+        """Waits for the request; returns dict(ll, latency_ms, frame_ll?, w/mu/var for MAP)."""
+        self.wait(ticket, timeout_ms)
+        kind, n, want_fll = self._n.pop(ticket)
+        ll, lat = C.c_double(), C.c_double()
+        out = {}
+        fll = np.zeros(n, np.float32) if want_fll else None
+        w = mu = var = None
+        if kind == REQ_MAP:
+            w = np.zeros(self.M, np.float32)
+            mu = np.zeros((self.M, self.D), np.float32)
+            var = np.zeros((self.M, self.D), np.float32)
+        rc = self.lib.gmm_server_result(self.h, ticket, C.byref(ll), ptr(fll) if fll is not None else None,
+                                        ptr(w) if w is not None else None, ptr(mu) if mu is not None else None,
+                                        ptr(var) if var is not None else None, C.byref(lat))
+        self._keep.pop(ticket, None)
+        self.check(rc)
+        out.update(ll=ll.value, latency_ms=lat.value)
+        if fll is not None:
+            out["frame_ll"] = fll
+        if kind == REQ_MAP:
+            out.update(w=w, mu=mu, var=var)
+        return out
+
+    def stats(self):
+        b, c, f, p = C.c_longlong(), C.c_longlong(), C.c_longlong(), C.c_size_t()
+        self.check(self.lib.gmm_server_stats(self.h, C.byref(b), C.byref(c), C.byref(f), C.byref(p)))
+        return dict(batches=b.value, completed=c.value, failed=f.value, peak_batch_bytes=p.value)

@@ -163,6 +163,39 @@ int mstep_map_batch(Ctx* c, const MapBatch& b, const double* stats, int layout, 
 int tc_map_batch(Ctx* c, const MapBatch& b);
 int plain_map_batch(Ctx* c, const MapBatch& b);
 
+// One tensor-core E-step over a batch of requests that may use different resident models (all
+// with the same D and chunk count): feature planes for the batch's padded row layout, the
+// logits / log-sum-exp kernel over every row (W chunks from the tile's model), and the
+// statistics kernel over explicit work items. Device pointers; launched on c->stream.
+struct TcBatch {
+  int D = 0, K = 0;
+  int n_chunks = 0;                   // W chunks per model
+  int w_chunks_total = 0;             // W chunks in the shared planes
+  const uint16_t* wplanes = nullptr;  // shared W planes (tile images)
+  const CUtensorMap* wmap = nullptr;  // 2-D map over wplanes, box = K rows
+  const float* X = nullptr;           // batch frames [N][D]
+  long long N = 0, Rpad = 0;          // frames, padded rows (multiple of 128)
+  const long long* row_frame = nullptr;  // [Rpad]
+  const int* tile_wbase = nullptr;       // [Rpad / 128] first W chunk of the row tile's model
+  uint16_t* zplanes = nullptr;        // [3][Rpad][K]
+  float* ll2 = nullptr;               // [Rpad]
+  float* ll = nullptr;                // [N] per-frame log-likelihood
+  double* llpart = nullptr;           // [>= sms * 128]
+  int n_work = 0;                     // statistics CTAs (0: log-likelihoods only)
+  const int4* work = nullptr;         // {W chunk, chunk in model, first FT tile, FT tiles}
+  const int* tile_slot = nullptr;     // [Rpad / FT] statistics slot of each FT tile
+  double* part = nullptr;             // [slots][n_chunks][K][128]
+  int single_comp = 0;
+};
+int tc_stats_ft(int K);  // frames per statistics tile for K
+int tc_flush_tiles(int K);  // statistics tiles per FP64 flush
+int tc_k(int D);
+int tc_run_batch(Ctx* c, const TcBatch& b);
+int tc_make_wmap(Ctx* c, CUtensorMap* map, const uint16_t* planes, long long rows, int K);
+int tc_build_model(Ctx* c, int D, int K, int Mact, int Mpad, long long plane_rows, long long row0,
+                   const int* act, const float* w, const float* mu, const float* var,
+                   uint16_t* planes, int* comp_of_row);
+
 int sync(Ctx* c, const char* what);
 
 }  // namespace gmm

@@ -127,10 +127,12 @@ __global__ void features_kernel(const float* __restrict__ X, long long N, long l
 
 // W planes as tile images (same layout as Z, rows = active components padded to 128, log2
 // units); padded rows carry a constant of -1e30 so they never contribute.
-__global__ void model_kernel(int D, int K, int Mact, int Mpad, const int* __restrict__ act,
-                             const float* __restrict__ w, const float* __restrict__ mu,
-                             const float* __restrict__ var, uint16_t* __restrict__ planes,
-                             int* __restrict__ comp_of_row) {
+// The model occupies rows [row0, row0 + Mpad) of planes that hold plane_rows rows each (several
+// models can share one set of planes, each starting on a 128-row tile).
+__global__ void model_kernel(int D, int K, int Mact, int Mpad, long long plane_rows, long long row0,
+                             const int* __restrict__ act, const float* __restrict__ w,
+                             const float* __restrict__ mu, const float* __restrict__ var,
+                             uint16_t* __restrict__ planes, int* __restrict__ comp_of_row) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int KC = K / 8;
   if (t >= (long long)Mpad * K) return;
@@ -160,10 +162,11 @@ __global__ void model_kernel(int D, int K, int Mact, int Mpad, const int* __rest
   }
   uint16_t a, b, c;
   split3d(v, a, b, c);
-  const size_t plane = (size_t)Mpad * K;
-  planes[t] = a;
-  planes[plane + t] = b;
-  planes[2 * plane + t] = c;
+  const size_t plane = (size_t)plane_rows * K;
+  const size_t o = (size_t)row0 * K + t;
+  planes[o] = a;
+  planes[plane + o] = b;
+  planes[2 * plane + o] = c;
   if (k == 0) comp_of_row[r] = r < Mact ? act[r] : -1;
 }
 
@@ -251,8 +254,8 @@ constexpr int kLlThreads = 448;  // warp 0 TMA, 1 MMA, 2-9 epilogue, 10-13 Z loa
 template <int K>
 __global__ void __launch_bounds__(kLlThreads, 1)
     ll_kernel(const __grid_constant__ CUtensorMap wfull, const uint16_t* __restrict__ zplanes,
-              long long N, const long long* __restrict__ row_frame, int nTz, int nTw, int n_tiles,
-              int n_chunks, float trouble2, float minLL,
+              long long N, const long long* __restrict__ row_frame, const int* __restrict__ tile_wbase,
+              int nTz, int nTw, int n_tiles, int n_chunks, float trouble2, float minLL,
               float* __restrict__ ll2_out, float* __restrict__ ll_out, double* __restrict__ llpart,
               int* __restrict__ err) {
   using C = LlCfg<K>;
@@ -307,13 +310,15 @@ __global__ void __launch_bounds__(kLlThreads, 1)
       int j = 0;
       bool ok = true;
       for (int it = 0; it < my_tiles && ok; ++it) {
+        // first W chunk of the tile's model (one model unless a per-tile base is given)
+        const int wbase = tile_wbase ? tile_wbase[(int)blockIdx.x + it * (int)gridDim.x] : 0;
         for (int ch = 0; ch < n_chunks; ++ch, ++j) {
           const int ws = j % NW;
           if (!mbar_wait(&w_empty[ws], ((j / NW) & 1) ^ 1, abort_flag, kWaitLimit)) { ok = false; break; }
           mbar_arrive_expect_tx(&w_full[ws], C::W_STAGE);
           uint8_t* dst = smem + C::OFF_W + ws * C::W_STAGE;
           for (int p = 0; p < 3; ++p)
-            load_image(dst + p * C::W_PLANE, &wfull, &wfull, p, nTw, K, ch, -1, &w_full[ws]);
+            load_image(dst + p * C::W_PLANE, &wfull, &wfull, p, nTw, K, wbase + ch, -1, &w_full[ws]);
         }
       }
       if (!ok) {  // drain the copies still in flight
@@ -508,7 +513,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     acc_kernel(const __grid_constant__ CUtensorMap zmap, const uint16_t* __restrict__ wplanes,
                int nTz, int nTw, const float* __restrict__ ll2, int n_tiles, int n_chunks, int slices,
                const int* __restrict__ tile_slot, const int* __restrict__ slice_t0,
-               float minGamma, int single_comp, double* __restrict__ part, int* __restrict__ err) {
+               const int4* __restrict__ work, float minGamma, int single_comp,
+               double* __restrict__ part, int* __restrict__ err) {
   using C = AccCfg<K>;
   constexpr int FT = C::FT, NZ = C::NZ, FLUSH = C::FLUSH;
   extern __shared__ uint8_t smem_raw[];
@@ -527,9 +533,17 @@ __global__ void __launch_bounds__(kThreads, 1)
   float* ll_s = reinterpret_cast<float*>(smem + C::OFF_LL);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int chunk = (int)blockIdx.x % n_chunks, slice = (int)blockIdx.x / n_chunks;
+  int chunk = (int)blockIdx.x % n_chunks, slice = (int)blockIdx.x / n_chunks;
+  int wchunk = chunk;  // W chunk in the planes (several models may share them)
   int t0, nt;
-  if (slice_t0) {
+  if (work) {
+    // explicit work item: {W chunk in the planes, chunk within its model, first tile, tiles}
+    const int4 wi = work[blockIdx.x];
+    wchunk = wi.x;
+    chunk = wi.y;
+    t0 = wi.z;
+    nt = wi.w;
+  } else if (slice_t0) {
     t0 = slice_t0[slice];
     nt = slice_t0[slice + 1] - t0;
   } else {
@@ -663,7 +677,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     {
       const int KC = K / 8;
       for (int p = (hf ? 2 : 0); p < (hf ? 3 : 2); ++p) {
-        const uint4* src = reinterpret_cast<const uint4*>(wplanes + ((size_t)(p * nTw + chunk) * KC) * 1024 + (size_t)row * 8);
+        const uint4* src = reinterpret_cast<const uint4*>(wplanes + ((size_t)(p * nTw + wchunk) * KC) * 1024 + (size_t)row * 8);
         for (int c = 0; c < KC; c += 2) {
           const uint4 u0 = __ldg(src + (size_t)c * 128), u1 = __ldg(src + (size_t)(c + 1) * 128);
           const uint32_t w[8] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z, u1.w};
@@ -875,7 +889,7 @@ int map_batch_launch(Ctx* c, long long Rpad, const long long* d_row_frame, const
   {
     GMM_LAUNCH(c, "tc_ll_kernel");
     ll_kernel<K><<<grid_ll, kLlThreads, LC::SMEM, c->stream>>>(
-        c->tm_wfull, c->tcx.planes, c->N, d_row_frame, nTz, nTw, nTz, nTw,
+        c->tm_wfull, c->tcx.planes, c->N, d_row_frame, nullptr, nTz, nTw, nTz, nTw,
         (float)(c->minLL * kLog2e), c->minLL, c->tcm.ll2, c->ll, c->tc_llpart, c->tc_err);
   }
   {
@@ -883,7 +897,7 @@ int map_batch_launch(Ctx* c, long long Rpad, const long long* d_row_frame, const
     const CUtensorMap& zm = AC::FT == 128 ? c->tm_zfull : c->tm_zhalf;
     acc_kernel<K><<<nTw * slices, kThreads, AC::SMEM, c->stream>>>(
         zm, c->tcm.planes, nTz, nTw, c->tcm.ll2, (int)(Rpad / AC::FT), nTw, slices, d_tile_slot,
-        d_slice_t0, c->minGamma, c->Mact == 1, d_part, c->tc_err);
+        d_slice_t0, nullptr, c->minGamma, c->Mact == 1, d_part, c->tc_err);
   }
   return GMM_OK;
 }
@@ -946,7 +960,7 @@ int launch_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
   {
     GMM_LAUNCH(c, "tc_ll_kernel");
     ll_kernel<K><<<grid_ll, kLlThreads, LC::SMEM, c->stream>>>(
-        c->tm_wfull, c->tcx.planes, c->N, nullptr, nTz, nTw, n_tiles_ll, n_chunks, trouble2, c->minLL,
+        c->tm_wfull, c->tcx.planes, c->N, nullptr, nullptr, nTz, nTw, n_tiles_ll, n_chunks, trouble2, c->minLL,
         c->tcm.ll2, ll_out_dev, c->tc_llpart, c->tc_err);
   }
   if (!want_stats) return GMM_OK;
@@ -978,7 +992,7 @@ int launch_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
     const CUtensorMap& zm = AC::FT == 128 ? c->tm_zfull : c->tm_zhalf;
     acc_kernel<K><<<grid, kThreads, AC::SMEM, c->stream>>>(
         zm, c->tcm.planes, nTz, nTw, c->tcm.ll2, n_tiles, n_chunks, slices, nullptr, nullptr,
-        c->minGamma, c->Mact == 1, c->tcpart, c->tc_err);
+        nullptr, c->minGamma, c->Mact == 1, c->tcpart, c->tc_err);
   }
   {
     GMM_LAUNCH(c, "tc_reduce_kernel");
@@ -1042,7 +1056,7 @@ int tc_prepare_model(Ctx* c) {
     GMM_LAUNCH(c, "tc_model_kernel");
     const long long tot = (long long)Mpad * K;
     model_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(
-        c->D, K, c->Mact, Mpad, c->act, c->w, c->mu, c->var, c->tcm.planes, c->tcm.comp_of_row);
+        c->D, K, c->Mact, Mpad, Mpad, 0, c->act, c->w, c->mu, c->var, c->tcm.planes, c->tcm.comp_of_row);
   }
   int rc = make_map(c, &c->tm_wfull, c->tcm.planes, 3LL * Mpad * K, K);
   if (!rc) rc = make_map(c, &c->tm_whalf, c->tcm.planes, 3LL * Mpad * K, 4);
@@ -1213,6 +1227,76 @@ int tc_map_batch(Ctx* c, const MapBatch& b) {
   dfree(c, d_roc, roc_bytes);
   dfree(c, d_part, part_bytes);
   return rc;
+}
+
+// ------------------------------------------------------------------ request batches
+
+int tc_stats_ft(int K) { return acc_ft(K); }
+int tc_flush_tiles(int K) { return 64 * 128 / acc_ft(K); }
+int tc_k(int D) { return tc_K(D); }
+
+int tc_make_wmap(Ctx* c, CUtensorMap* map, const uint16_t* planes, long long rows, int K) {
+  return make_map(c, map, planes, 3 * rows * K, K);
+}
+
+int tc_build_model(Ctx* c, int D, int K, int Mact, int Mpad, long long plane_rows, long long row0,
+                   const int* act, const float* w, const float* mu, const float* var,
+                   uint16_t* planes, int* comp_of_row) {
+  GMM_LAUNCH(c, "tc_model_kernel");
+  const long long tot = (long long)Mpad * K;
+  model_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(D, K, Mact, Mpad, plane_rows, row0, act,
+                                                                     w, mu, var, planes, comp_of_row);
+  return GMM_OK;
+}
+
+namespace {
+template <int K>
+void run_batch_k(Ctx* c, const TcBatch& b, const CUtensorMap& zfull, const CUtensorMap& zhalf) {
+  using LC = LlCfg<K>;
+  using AC = AccCfg<K>;
+  const int nTz = (int)(b.Rpad / 128);
+  const int grid_ll = std::max(1, std::min(nTz, c->sms));
+  cudaFuncSetAttribute(ll_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, LC::SMEM);
+  cudaFuncSetAttribute(acc_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, AC::SMEM);
+  {
+    GMM_LAUNCH(c, "tc_ll_kernel");
+    ll_kernel<K><<<grid_ll, kLlThreads, LC::SMEM, c->stream>>>(
+        *b.wmap, b.zplanes, b.N, b.row_frame, b.tile_wbase, nTz, b.w_chunks_total, nTz, b.n_chunks,
+        (float)(c->minLL * kLog2e), c->minLL, b.ll2, b.ll, b.llpart, c->tc_err);
+  }
+  if (b.n_work > 0) {
+    GMM_LAUNCH(c, "tc_acc_kernel");
+    const CUtensorMap& zm = AC::FT == 128 ? zfull : zhalf;
+    acc_kernel<K><<<b.n_work, kThreads, AC::SMEM, c->stream>>>(
+        zm, b.wplanes, nTz, b.w_chunks_total, b.ll2, (int)(b.Rpad / AC::FT), b.n_chunks, 1, b.tile_slot,
+        nullptr, b.work, c->minGamma, b.single_comp, b.part, c->tc_err);
+  }
+}
+}  // namespace
+
+int tc_run_batch(Ctx* c, const TcBatch& b) {
+  if (b.Rpad <= 0) return GMM_OK;
+  {
+    GMM_LAUNCH(c, "tc_features_kernel");
+    features_kernel<<<(unsigned)((b.Rpad * (b.K / 8) + 255) / 256), 256, 0, c->stream>>>(
+        b.X, b.N, b.Rpad / 128, b.D, b.K, b.row_frame, b.zplanes);
+  }
+  CUtensorMap zfull, zhalf;
+  int rc = make_map(c, &zfull, b.zplanes, 3 * b.Rpad * b.K, b.K);
+  if (!rc) rc = make_map(c, &zhalf, b.zplanes, 3 * b.Rpad * b.K, 4);
+  if (rc) return rc;
+  switch (b.K) {
+    case 16: run_batch_k<16>(c, b, zfull, zhalf); break;
+    case 32: run_batch_k<32>(c, b, zfull, zhalf); break;
+    case 48: run_batch_k<48>(c, b, zfull, zhalf); break;
+    case 64: run_batch_k<64>(c, b, zfull, zhalf); break;
+    case 80: run_batch_k<80>(c, b, zfull, zhalf); break;
+    case 96: run_batch_k<96>(c, b, zfull, zhalf); break;
+    case 112: run_batch_k<112>(c, b, zfull, zhalf); break;
+    case 128: run_batch_k<128>(c, b, zfull, zhalf); break;
+    default: return fail(c, GMM_ERR_UNSUPPORTED, "tensor-core path: unsupported K");
+  }
+  return GMM_OK;
 }
 
 }  // namespace gmm

@@ -160,6 +160,51 @@ int gmm_profile_read(gmm_handle h, int cap, const char** names, double* ms, long
 /* Number of kernel launches this handle issued since creation (all kernels). */
 long long gmm_launch_count(gmm_handle h);
 
+/* ------------------------------------------------------------------ request server
+ * Continuous-batching server for scoring and MAP-adaptation requests against resident GMMs. It
+ * replaces the reference's one-request-at-a-time tools: getLogLike's per-file scoring
+ * (projects/GetLogLikeGMM/main.cpp:119-180 -> compVecsLogLikeMT, OL_GMMStatsEstimator.cpp:811-879)
+ * and Model_ADAPT's per-speaker MAP loop (projects/Model_ADAPT/Model_ADAPT.cpp:170-240 ->
+ * CModelAdapt::AdaptModel / AdaptModelMAP, OL_ModelAdapt.cpp:1163-1274). All models of a server
+ * have the same M and D (1 <= D <= 63, tensor-core path). A worker thread admits queued requests
+ * in arrival order while their device footprint fits one of two request arenas of
+ * request_bytes / 2 each, runs each batch as one fused E-step, and overlaps the next batch's
+ * preparation and upload with the running one. A request's result does not depend on what else
+ * is in its batch (bit-identical). */
+typedef struct gmm_server_s* gmm_server;
+#define GMM_REQ_SCORE 0  /* total (and optionally per-frame) log-likelihood under the model */
+#define GMM_REQ_MAP 1    /* one MAP iteration against the model (the model is the UBM) */
+#define GMM_REQ_QUEUED 0
+#define GMM_REQ_RUNNING 1
+#define GMM_REQ_DONE 2
+#define GMM_REQ_FAILED 3
+int gmm_server_create(int device, int D, int M, int max_models, size_t request_bytes, gmm_server* out);
+int gmm_server_destroy(gmm_server s);
+const char* gmm_server_last_error(gmm_server s); /* NULL server: the last create error */
+/* minLogLike, minGamma, min_var as in gmm_set_options; max_batch = most requests per batch. */
+int gmm_server_set_options(gmm_server s, float min_loglike, float min_gamma, float min_var, int max_batch);
+/* Makes a model resident (w [M], mu [M][D], var [M][D]); *model_id receives its id. */
+int gmm_server_add_model(gmm_server s, const float* w, const float* mu, const float* var, int* model_id);
+/* Queues a request on frames [N][D] (host). By default the frames are copied at submit, so the
+ * caller may reuse them; with GMM_SUBMIT_NO_COPY they must stay valid until gmm_server_result
+ * (page-locked memory is then copied to the device directly). GMM_SUBMIT_FRAME_LL keeps the
+ * per-frame log-likelihoods. For GMM_REQ_MAP, tau >= 1 and up_* select the adapted parameters
+ * (as gmm_map_batch). */
+#define GMM_SUBMIT_FRAME_LL 1
+#define GMM_SUBMIT_NO_COPY 2
+int gmm_server_submit(gmm_server s, int kind, int model_id, const float* frames, long long N, int tau,
+                      int up_weight, int up_mean, int up_var, int options, long long* ticket);
+int gmm_server_poll(gmm_server s, long long ticket, int* state); /* GMM_REQ_* state */
+/* Blocks until the request finished (timeout_ms < 0: no limit; GMM_ERR_TIMEOUT on expiry). */
+int gmm_server_wait(gmm_server s, long long ticket, int timeout_ms);
+/* Copies a finished request's results (any pointer may be NULL: total_ll; frame_ll [N];
+ * w [M], mu [M][D], var [M][D] for MAP; latency from submit to completion in ms) and releases
+ * the ticket. Returns the request's own status. */
+int gmm_server_result(gmm_server s, long long ticket, double* total_ll, float* frame_ll, float* w, float* mu,
+                      float* var, double* latency_ms);
+int gmm_server_stats(gmm_server s, long long* batches, long long* completed, long long* failed,
+                     size_t* peak_batch_bytes);
+
 #ifdef __cplusplus
 }
 #endif
