@@ -60,7 +60,7 @@ struct Req {
   double ll = 0.0;
   std::vector<float> frame_ll, w, mu, var;
   double t_submit = 0.0, t_admit = 0.0, t_done = 0.0;
-  size_t foot = 0;
+  size_t foot = 0, hin_foot = 0, hout_foot = 0;  // device, pinned input, pinned output bytes
   // batch layout
   long long row0 = 0, rows = 0, x0 = 0;
   int piece0 = 0, pieces = 0;
@@ -356,7 +356,12 @@ bool plan(Server* s, Batch& b) {
   b.ovar = d.take<float>((size_t)R_map * s->M * s->D);
   const size_t out1 = d.off;
   b.oaw = d.take<float>((size_t)R_map * s->M);
-  if (d.off > d.cap || in_bytes > s->hin_bytes) return false;
+  // staging holds the layout arrays and the frames of the requests that were copied at submit
+  size_t staged_end = b.meta_bytes;
+  for (const Req* r : b.reqs)
+    if (!r->src) staged_end = std::max(staged_end, (size_t)((const char*)(b.X + (size_t)(r->x0 + r->N) * s->D) - s->arena[b.slot]));
+  (void)in_bytes;
+  if (d.off > d.cap || staged_end > s->hin_bytes) return false;
   b.dev_bytes = d.off;
   // host staging: same offsets as the device block for the inputs
   char* h = s->hin[b.slot];
@@ -541,11 +546,12 @@ void worker_loop(Server* s) {
       if (!have_running) s->cv_work.wait(lk, [&] { return s->stop || !s->pending.empty(); });
       if (s->stop && s->pending.empty() && !have_running) return;
       // admission: arrival order, while the footprint fits the free arena
-      size_t used = 0;
+      size_t used = 0, hin = 0, hout = 0;
       const double t = now_ms();
       while (!s->pending.empty() && (int)next.reqs.size() < s->max_batch) {
         Req* r = s->pending.front();
-        if (r->foot > s->arena_bytes - kArenaSlack) {  // can never fit
+        if (r->foot > s->arena_bytes - kArenaSlack || r->hin_foot > s->hin_bytes - kArenaSlack ||
+            r->hout_foot > s->hout_bytes - kArenaSlack) {  // can never fit
           s->pending.pop_front();
           r->state = GMM_REQ_FAILED;
           r->status = GMM_ERR_NOMEM;
@@ -555,8 +561,12 @@ void worker_loop(Server* s) {
           s->cv_done.notify_all();
           continue;
         }
-        if (used + r->foot > s->arena_bytes - kArenaSlack) break;
+        if (used + r->foot > s->arena_bytes - kArenaSlack || hin + r->hin_foot > s->hin_bytes - kArenaSlack ||
+            hout + r->hout_foot > s->hout_bytes - kArenaSlack)
+          break;
         used += r->foot;
+        hin += r->hin_foot;
+        hout += r->hout_foot;
         s->pending.pop_front();
         r->state = GMM_REQ_RUNNING;
         r->t_admit = t;
@@ -663,8 +673,10 @@ int gmm_server_create(int device, int D, int M, int max_models, size_t request_b
     cudaMemsetAsync(s->wplanes, 0, (size_t)3 * wrows * s->K * 2, c->stream);
     rc = gmm::tc_make_wmap(c, &s->wmap, s->wplanes, wrows, s->K);
   }
-  s->hin_bytes = s->arena_bytes;
-  s->hout_bytes = s->arena_bytes;
+  // pinned staging: the inputs are at most about a third of a request's device footprint
+  // (frames and row maps, not the operand planes), the outputs a quarter of it
+  s->hin_bytes = s->arena_bytes / 2;
+  s->hout_bytes = s->arena_bytes / 4;
   for (int i = 0; i < 2 && !rc; ++i) {
     if (cudaMallocHost((void**)&s->hin[i], s->hin_bytes) != cudaSuccess ||
         cudaMallocHost((void**)&s->hout[i], s->hout_bytes) != cudaSuccess)
@@ -786,6 +798,12 @@ int gmm_server_submit(gmm_server s, int kind, int model_id, const float* frames,
   r->upV = up_v;
   r->want_frame_ll = (options & GMM_SUBMIT_FRAME_LL) != 0;
   r->foot = gmm::footprint(s, N, kind);
+  {
+    const size_t rows = (size_t)((N + 127) / 128 * 128);
+    r->hin_foot = gmm::align256((r->src ? 0 : (size_t)N * s->D * 4) + rows * 8 + rows / 128 * 4 + rows / s->FT * 4) + 1024;
+    r->hout_foot = gmm::align256(8 + (size_t)N * 4 +
+                                 (kind == GMM_REQ_MAP ? (size_t)s->M * 4 * (2 + 2 * s->D) : 0)) + 1024;
+  }
   r->t_submit = gmm::now_ms();
   {
     std::lock_guard<std::mutex> lk(s->mu);
