@@ -41,6 +41,7 @@ SIGNATURES = {
     "gmm_em_iterate": (_i, [_vp, _i, _i, _i, _i, _vp, C.POINTER(_i)]),
     "gmm_map_batch": (_i, [_vp, _i, _vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp]),
     "gmm_map_batch_device": (_i, [_vp, _i, _vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp]),
+    "gmm_mllr_batch": (_i, [_vp, _i, _vp, _i, _vp, _vp, _vp, _vp]),
     "gmm_mllr_estimate": (_i, [_vp, _i, _vp]),
     "gmm_mllr_apply": (_i, [_vp, _vp]),
     "gmm_profile_enable": (_i, [_vp, _i]),
@@ -239,6 +240,19 @@ class Handle:
         self.check(self.lib.gmm_map_batch_device(self.h, len(offs) - 1, ptr(offs), int(tau),
                                                  int(upW), int(upM), int(upV), d_w or None,
                                                  d_mu or None, d_var or None, d_ll or None))
+
+    def mllr_batch(self, offs, ubm_init=False, means=True):
+        """Global MLLR transform per speaker against the resident model (the UBM). Returns
+        (W [S, D, D+1], status [S], adapted means [S, M, D] or None, ll [S])."""
+        offs = np.ascontiguousarray(offs, np.int64)
+        S = len(offs) - 1
+        W = np.zeros((S, self.D, self.D + 1))
+        st = np.zeros(S, np.int32)
+        mu = np.zeros((S, self.M, self.D), np.float32) if means else None
+        ll = np.zeros(S)
+        self.check(self.lib.gmm_mllr_batch(self.h, S, ptr(offs), int(ubm_init), ptr(W), ptr(st),
+                                           ptr(mu) if mu is not None else None, ptr(ll)))
+        return W, st, mu, ll
 
     def em_iterate(self, iters, upW=True, upM=True, upV=True):
         ll = np.zeros(max(iters, 1))

@@ -461,24 +461,28 @@ int gmm_map_update(gmm_handle h, int tau, int upW, int upM, int upV) {
   return sync(h, "gmm_map_update");
 }
 
-static int map_batch(Ctx* c, int S, const long long* offs, int tau, int upW, int upM, int upV,
-                     float* w, float* mu, float* var, double* ll, bool dev_out) {
-  if (S < 0 || (S > 0 && !offs)) return fail(c, GMM_ERR_ARG, "gmm_map_batch: bad speaker count or offsets");
-  if (tau < 1) return fail(c, GMM_ERR_ARG, "gmm_map_batch: tau must be >= 1");
+// Common checks of the batched entry points: speakers own resident frame ranges.
+static int check_speakers(Ctx* c, const char* fn, int S, const long long* offs) {
+  const std::string f(fn);
+  if (S < 0 || (S > 0 && !offs)) return fail(c, GMM_ERR_ARG, f + ": bad speaker count or offsets");
   if (!c->w) return fail(c, GMM_ERR_STATE, "no model uploaded");
   if (!c->X && c->N > 0) return fail(c, GMM_ERR_STATE, "no features uploaded");
   if (c->Dx != c->D && c->N > 0)
     return fail(c, GMM_ERR_ARG, "Inconsistent model & feature vector - different dimensions");
   if (S == 0) return GMM_OK;
-  if (offs[0] < 0 || offs[S] > c->N) return fail(c, GMM_ERR_ARG, "gmm_map_batch: offsets outside the resident frames");
+  if (offs[0] < 0 || offs[S] > c->N) return fail(c, GMM_ERR_ARG, f + ": offsets outside the resident frames");
   for (int s = 0; s < S; ++s)
-    if (offs[s + 1] < offs[s]) return fail(c, GMM_ERR_ARG, "gmm_map_batch: offsets must be non-decreasing");
+    if (offs[s + 1] < offs[s]) return fail(c, GMM_ERR_ARG, f + ": offsets must be non-decreasing");
   cudaSetDevice(c->device);
-  int rc;
-  if (c->model_dirty) {
-    rc = plain_precompute(c);
-    if (rc) return rc;
-  }
+  if (c->model_dirty) return plain_precompute(c);
+  return GMM_OK;
+}
+
+static int map_batch(Ctx* c, int S, const long long* offs, int tau, int upW, int upM, int upV,
+                     float* w, float* mu, float* var, double* ll, bool dev_out) {
+  if (tau < 1) return fail(c, GMM_ERR_ARG, "gmm_map_batch: tau must be >= 1");
+  int rc = check_speakers(c, "gmm_map_batch", S, offs);
+  if (rc || S == 0) return rc;
   const int M = c->M, D = c->D;
   const size_t bw = sizeof(float) * (size_t)S * M, bmu = bw * D, bll = sizeof(double) * S;
   const size_t boffs = sizeof(long long) * (S + 1);
@@ -536,6 +540,56 @@ int gmm_map_batch_device(gmm_handle h, int S, const long long* offs, int tau, in
                          int upV, float* d_w, float* d_mu, float* d_var, double* d_ll) {
   if (!h) return GMM_ERR_ARG;
   return map_batch(h, S, offs, tau, upW, upM, upV, d_w, d_mu, d_var, d_ll, true);
+}
+
+int gmm_mllr_batch(gmm_handle h, int S, const long long* offs, int ubm_init, double* W, int* status,
+                   float* mu_out, double* ll) {
+  if (!h) return GMM_ERR_ARG;
+  Ctx* c = h;
+  int rc = check_speakers(c, "gmm_mllr_batch", S, offs);
+  if (rc || S == 0) return rc;
+  const int M = c->M, D = c->D, E = D + 1;
+  const size_t bW = sizeof(double) * (size_t)S * D * E, bst = sizeof(int) * S, bmu = sizeof(float) * (size_t)S * M * D;
+  const size_t bll = sizeof(double) * S, boffs = sizeof(long long) * (S + 1);
+  double *dW = nullptr, *dll = nullptr;
+  int* dst = nullptr;
+  float* dmu = nullptr;
+  long long* doffs = nullptr;
+  rc = dalloc(c, (void**)&dW, bW, "MLLR transforms");
+  if (!rc) rc = dalloc(c, (void**)&dst, bst, "MLLR status");
+  if (!rc) rc = dalloc(c, (void**)&dll, bll, "speaker log-likelihoods");
+  if (!rc) rc = dalloc(c, (void**)&doffs, boffs, "speaker offsets");
+  if (!rc && mu_out) rc = dalloc(c, (void**)&dmu, bmu, "MLLR adapted means");
+  if (!rc) {
+    cudaMemcpyAsync(doffs, offs, boffs, cudaMemcpyHostToDevice, c->stream);
+    if (c->precision == GMM_PREC_TC) {
+      SpeakerStats ss;
+      rc = tc_speaker_stats(c, S, offs, doffs, dll, &ss);
+      if (!rc) rc = mstep_mllr_batch(c, S, nullptr, &ss, ubm_init, dW, dst, dmu, nullptr);
+      tc_free_speaker_stats(c, &ss);
+    } else {
+      double* stats = nullptr;
+      size_t bytes = 0;
+      rc = plain_speaker_stats(c, S, offs, GMM_ACC_MEAN, &stats, &bytes);
+      if (!rc) rc = mstep_mllr_batch(c, S, stats, nullptr, ubm_init, dW, dst, dmu, dll);
+      cudaStreamSynchronize(c->stream);
+      dfree(c, stats, bytes);
+    }
+  }
+  if (!rc) {
+    if (W) cudaMemcpyAsync(W, dW, bW, cudaMemcpyDeviceToHost, c->stream);
+    if (status) cudaMemcpyAsync(status, dst, bst, cudaMemcpyDeviceToHost, c->stream);
+    if (mu_out) cudaMemcpyAsync(mu_out, dmu, bmu, cudaMemcpyDeviceToHost, c->stream);
+    if (ll) cudaMemcpyAsync(ll, dll, bll, cudaMemcpyDeviceToHost, c->stream);
+    rc = sync(c, "gmm_mllr_batch");
+  }
+  cudaStreamSynchronize(c->stream);
+  dfree(c, dW, bW);
+  dfree(c, dst, bst);
+  dfree(c, dll, bll);
+  dfree(c, doffs, boffs);
+  dfree(c, dmu, bmu);
+  return rc;
 }
 
 int gmm_em_iterate(gmm_handle h, int iters, int upW, int upM, int upV, double* ll, int* alive) {

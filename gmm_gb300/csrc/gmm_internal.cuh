@@ -155,13 +155,30 @@ struct MapBatch {
   float* aw = nullptr;                // device scratch [S][M]
   double* ll = nullptr;               // device output [S]: per-speaker total log-likelihood
 };
-// statistics layouts read by mstep_map_batch
-constexpr int kStatsSlots = 0;  // tensor-core partials: [speaker][chunk][K cols][128 rows], rows via row_of_comp
-constexpr int kStatsPlain = 1;  // [speaker][n (M) | F (M x D) | S (M x D) | totLL | pad]
-int mstep_map_batch(Ctx* c, const MapBatch& b, const double* stats, int layout, int K, int n_chunks,
-                    const int* row_of_comp);
+// Per-speaker statistics from the tensor-core path: FP64 partials of pieces of at most 8192
+// frames, [piece][chunk][K cols][128 rows] (columns x | x^2 | 1, rows = padded active list);
+// speaker s owns pieces [piece0[s], piece0[s] + npieces[s]), summed in piece order.
+struct SpeakerStats {
+  int S = 0, n_chunks = 0, K = 0, pieces = 0;
+  double* part = nullptr;
+  int* piece0 = nullptr;       // [S]
+  int* npieces = nullptr;      // [S]
+  int* row_of_comp = nullptr;  // [M], -1 for inactive components
+  size_t part_bytes = 0;
+};
+int tc_speaker_stats(Ctx* c, int S, const long long* offs, const long long* d_offs, double* d_ll,
+                     SpeakerStats* ss);
+void tc_free_speaker_stats(Ctx* c, SpeakerStats* ss);
+// Per-speaker statistics from the plain path: [speaker][n (M) | F (M x D) | S (M x D) | totLL | pad]
+// MAP update for all speakers from either form (exactly one of plain / ss is non-null).
+int mstep_map_batch(Ctx* c, const MapBatch& b, const double* plain, const SpeakerStats* ss);
 int tc_map_batch(Ctx* c, const MapBatch& b);
 int plain_map_batch(Ctx* c, const MapBatch& b);
+// Plain FP32 per-speaker statistics in the plain layout (one E-step per speaker); *out is a
+// device array the caller frees with dfree(c, *out, *bytes).
+int plain_speaker_stats(Ctx* c, int S, const long long* offs, int flags, double** out, size_t* bytes);
+int mstep_mllr_batch(Ctx* c, int S, const double* plain, const SpeakerStats* ss, int ubm_init, double* dW,
+                     int* dstatus, float* dmu_out, double* dll);
 
 // One tensor-core E-step over a batch of requests that may use different resident models (all
 // with the same D and chunk count): feature planes for the batch's padded row layout, the

@@ -296,8 +296,10 @@ __global__ void mllr_apply_kernel(int M, int D, float* __restrict__ mu, const do
 // expression order as map_comp_kernel. One warp per (speaker, component), lanes over the
 // dimensions (coalesced rows). Statistics come in one of two layouts (kStatsSlots /
 // kStatsPlain); in the plain layout the speaker's total log-likelihood is copied out as well.
-__global__ void map_batch_kernel(int S, int M, int D, int layout, const double* __restrict__ stats,
-                                 int K, int n_chunks, const int* __restrict__ row_of_comp,
+__global__ void map_batch_kernel(int S, int M, int D, const double* __restrict__ plain,
+                                 const double* __restrict__ part, int K, int n_chunks,
+                                 const int* __restrict__ piece0, const int* __restrict__ npieces,
+                                 const int* __restrict__ row_of_comp,
                                  const long long* __restrict__ offs, const float* __restrict__ uw,
                                  const float* __restrict__ umu, const float* __restrict__ uvar,
                                  int tau, int upW, int upM, int upV, float min_var,
@@ -312,25 +314,26 @@ __global__ void map_batch_kernel(int S, int M, int D, int layout, const double* 
   const float* uv = uvar + (size_t)m * D;
   float* om = omu ? omu + (size_t)t * D : nullptr;
   float* ov = ovar ? ovar + (size_t)t * D : nullptr;
-  const double *pn = nullptr, *pF = nullptr, *pS = nullptr;
-  size_t cs = 1;  // stride between the columns of one component's statistics
-  if (layout == kStatsSlots) {
-    const int r = row_of_comp[m];
-    if (r >= 0) {  // inactive components were never accumulated
-      const double* st = stats + ((size_t)s * n_chunks + r / 128) * K * 128 + (r % 128);
-      cs = 128;
-      pF = st;
-      pS = st + (size_t)D * 128;
-      pn = st + (size_t)2 * D * 128;
+  // statistic e (columns x | x^2 | 1 of the tensor-core partials, or n / F / S of the plain
+  // layout) of component m for speaker s
+  const int row = plain ? 0 : row_of_comp[m];
+  const double* pst = plain ? plain + (size_t)s * ((size_t)M * (1 + 2 * D) + 2) : nullptr;
+  if (plain && m == 0 && lane == 0) ll[s] = pst[(size_t)M * (1 + 2 * D)];
+  auto stat = [&](int e) -> double {  // e in [0, 2D]: F_k = e < D, S_k = D + k, n = 2D
+    if (plain) {
+      if (e == 2 * D) return pst[m];
+      if (e < D) return pst[M + (size_t)m * D + e];
+      return pst[M + (size_t)M * D + (size_t)m * D + (e - D)];
     }
-  } else {
-    const double* st = stats + (size_t)s * ((size_t)M * (1 + 2 * D) + 2);
-    if (m == 0 && lane == 0) ll[s] = st[(size_t)M * (1 + 2 * D)];
-    pn = st + m;
-    pF = st + M + (size_t)m * D;
-    pS = st + M + (size_t)M * D + (size_t)m * D;
-  }
-  const double mp = pn ? *pn : 0.0;
+    if (row < 0) return 0.0;  // inactive components were never accumulated
+    double v = 0.0;
+    for (int p = 0; p < npieces[s]; ++p) {
+      const double x = part[((size_t)(piece0[s] + p) * n_chunks + row / 128) * K * 128 + (size_t)e * 128 + (row % 128)];
+      v = p == 0 ? x : __dadd_rn(v, x);
+    }
+    return v;
+  };
+  const double mp = stat(2 * D);
   const bool adapt = uw[m] != 0.0f && mp > 0.0;
   const unsigned int tot = (unsigned int)(offs[s + 1] - offs[s]);
   const double alfa = adapt ? __ddiv_rn(mp, __dadd_rn(mp, (double)tau)) : 0.0;
@@ -348,12 +351,12 @@ __global__ void map_batch_kernel(int S, int M, int D, int layout, const double* 
   for (int k = lane; k < D; k += 32) {
     float am = um[k], av = uv[k];
     if (adapt && (upM || upV)) {
-      const double a1 = __ddiv_rn(__dmul_rn(alfa, pF[k * cs]), mp);
+      const double a1 = __ddiv_rn(__dmul_rn(alfa, stat(k)), mp);
       am = (float)__dadd_rn(a1, __dmul_rn(one_m, (double)um[k]));
       if (upV) {
         const float second = __fadd_rn(uv[k], __fmul_rn(um[k], um[k]));
         const float msq = __fmul_rn(am, am);
-        const double b1 = __ddiv_rn(__dmul_rn(alfa, pS[k * cs]), mp);
+        const double b1 = __ddiv_rn(__dmul_rn(alfa, stat(D + k)), mp);
         const double b2 = __dadd_rn(b1, __dmul_rn(one_m, (double)second));
         av = (float)__dsub_rn(b2, (double)msq);
         if (av < min_var) av = min_var;
@@ -379,6 +382,263 @@ __global__ void map_batch_norm_kernel(int S, int M, const float* __restrict__ ad
   if (corr != 0.0) {
     const float fc = (float)corr;
     for (int m = lane; m < M; m += 32) ow[(size_t)s * M + m] = __fdiv_rn(ow[(size_t)s * M + m], fc);
+  }
+}
+
+// ------------------------------------------------------------------ batched MLLR
+
+__host__ __device__ inline int tri_index(int a, int b, int E) { return a * E - a * (a - 1) / 2 + (b - a); }
+
+// Dense per-speaker mean statistics of MLLR (n [S][M], F [S][M][D], FP64) from either the plain
+// layout or the tensor-core pieces. One warp per (speaker, component).
+__global__ void mllr_gather_kernel(int S, int M, int D, const double* __restrict__ plain,
+                                   const double* __restrict__ part, int K, int n_chunks,
+                                   const int* __restrict__ piece0, const int* __restrict__ npieces,
+                                   const int* __restrict__ row_of_comp, double* __restrict__ n_out,
+                                   double* __restrict__ F_out, double* __restrict__ ll_out) {
+  const long long t = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (t >= (long long)S * M) return;
+  const int s = (int)(t / M), m = (int)(t - (long long)s * M);
+  const int row = plain ? 0 : row_of_comp[m];
+  const double* pst = plain ? plain + (size_t)s * ((size_t)M * (1 + 2 * D) + 2) : nullptr;
+  auto stat = [&](int e) -> double {
+    if (plain) return e == 2 * D ? pst[m] : pst[M + (size_t)m * D + e];
+    if (row < 0) return 0.0;
+    double v = 0.0;
+    for (int p = 0; p < npieces[s]; ++p) {
+      const double x = part[((size_t)(piece0[s] + p) * n_chunks + row / 128) * K * 128 + (size_t)e * 128 + (row % 128)];
+      v = p == 0 ? x : __dadd_rn(v, x);
+    }
+    return v;
+  };
+  if (lane == 0) n_out[t] = stat(2 * D);
+  if (plain && ll_out && m == 0 && lane == 0) ll_out[s] = pst[(size_t)M * (1 + 2 * D)];
+  for (int k = lane; k < D; k += 32) F_out[(size_t)t * D + k] = stat(k);
+}
+
+// CheckInvertibility (OL_ModelAdapt.cpp:1851-1878) per speaker: enough components and data for a
+// D x (D+1) transform. One warp per speaker.
+__global__ void mllr_batch_check_kernel(int S, int M, int D, const double* __restrict__ n,
+                                        int* __restrict__ status) {
+  const int s = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (s >= S) return;
+  int act = 0;
+  double occ = 0.0;
+  if (lane == 0)
+    for (int m = 0; m < M; ++m) {
+      const double v = n[(size_t)s * M + m];
+      if (v > 0.0) { ++act; occ = __dadd_rn(occ, v); }
+    }
+  if (lane == 0) {
+    const int E = D + 1;
+    status[s] = (M < E || act < E || occ * D < (double)D * E) ? GMM_ERR_MLLR : GMM_OK;
+  }
+}
+
+// xi_m xi_m^T over the upper triangle (incl. diagonal), xi_m = [mu_m; 1]: B[m][tri(a, b)] (float).
+__global__ void mllr_outer_kernel(int M, int D, const float* __restrict__ mu, float* __restrict__ B) {
+  const int E = D + 1, T = E * (E + 1) / 2;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)M * T) return;
+  const int m = (int)(t / T);
+  int e = (int)(t - (long long)m * T), a = 0;
+  while (e >= E - a) { e -= E - a; ++a; }
+  const int b = a + e;
+  const float xa = a < D ? mu[(size_t)m * D + a] : 1.0f, xb = b < D ? mu[(size_t)m * D + b] : 1.0f;
+  B[t] = (float)((double)xa * (double)xb);
+}
+
+// xi_m = [mu_m; 1] as floats: X[m][a].
+__global__ void mllr_xi_kernel(int M, int D, const float* __restrict__ mu, float* __restrict__ X) {
+  const int E = D + 1;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)M * E) return;
+  const int m = (int)(t / E), a = (int)(t - (long long)m * E);
+  X[t] = a < D ? mu[(size_t)m * D + a] : 1.0f;
+}
+
+// The data terms of ComputeKiGi_MLLR (OL_ModelAdapt.cpp:1525-1581) for all speakers and rows as
+// GEMMs over the components: out[s][i][c] = sum_m (coef(s, m) / var[m][i]) * B[m][c], with
+// coef = n (G, c = upper-triangle pair) or coef = F[.][.][i] (k, c = a, B = xi). FP32 operands
+// (coef * 1/var rounded to float) and products in 64 x 64 tiles, FP32 sums over 128 components at
+// a time, added into FP64.
+__global__ void __launch_bounds__(256) mllr_gemm_kernel(int S, int M, int D, int C, const double* __restrict__ coef,
+                                                         long long cs_s, long long cs_m, int coef_i_stride,
+                                                         const float* __restrict__ var,
+                                                         const float* __restrict__ B, int ldb,
+                                                         double* __restrict__ out) {
+  __shared__ float As[32][65];
+  __shared__ float Bs[32][64];
+  const int i = blockIdx.z;
+  const int s0 = blockIdx.y * 64, c0 = blockIdx.x * 64;
+  const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
+  float acc[4][4];
+  double dacc[4][4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) { acc[u][v] = 0.0f; dacc[u][v] = 0.0; }
+  for (int m0 = 0; m0 < M; m0 += 32) {
+    for (int e = tid; e < 32 * 64; e += 256) {
+      const int mm = e >> 6, ss = e & 63;
+      const int m = m0 + mm, s = s0 + ss;
+      float a = 0.0f;
+      if (m < M && s < S)
+        a = __fmul_rn((float)coef[(size_t)s * cs_s + (size_t)m * cs_m + (size_t)i * coef_i_stride],
+                      __frcp_rn(var[(size_t)m * D + i]));
+      As[mm][ss] = a;
+      const int cc = e & 63;
+      const int c = c0 + cc;
+      Bs[mm][cc] = (m < M && c < C) ? B[(size_t)m * ldb + c] : 0.0f;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int mm = 0; mm < 32; ++mm) {
+      float av[4], bv[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) av[u] = As[mm][ty * 4 + u];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) bv[v] = Bs[mm][tx * 4 + v];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] = fmaf(av[u], bv[v], acc[u][v]);
+    }
+    __syncthreads();
+    if (((m0 + 32) & 127) == 0 || m0 + 32 >= M) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) { dacc[u][v] += (double)acc[u][v]; acc[u][v] = 0.0f; }
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int s = s0 + ty * 4 + u;
+    if (s >= S) continue;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int c = c0 + tx * 4 + v;
+      if (c < C) out[((size_t)s * D + i) * C + c] = dacc[u][v];
+    }
+  }
+}
+
+// The prior terms of prepareKiGiInitMatrices (OL_ModelAdapt.cpp:1484-1523), the same for every
+// speaker: Gp[i][tri(a, b)], kp[i][a], accumulated over the UBM components in order. One block
+// per row i.
+__global__ void mllr_prior_kernel(int M, int D, const float* __restrict__ umu, const float* __restrict__ uvar,
+                                  float min_var, double* __restrict__ Gp, double* __restrict__ kp) {
+  const int E = D + 1, T = E * (E + 1) / 2;
+  const int i = blockIdx.x;
+  for (int e = threadIdx.x; e < T + E; e += blockDim.x) {
+    double g = 0.0;
+    if (e < T) {
+      int r = e, a = 0;
+      while (r >= E - a) { r -= E - a; ++a; }
+      const int b = a + r;
+      for (int m = 0; m < M; ++m) {
+        const float* v = uvar + (size_t)m * D;
+        const float* me = umu + (size_t)m * D;
+        const double cG = (v[i] < min_var) ? (double)__fdiv_rn(1.0f, min_var) : (double)__fdiv_rn(1.0f, v[i]);
+        if (a < D && b < D) {
+          g = __dadd_rn(g, __dmul_rn(__dmul_rn(cG, (double)me[a]), (double)me[b]));
+          if (a == b) g = __dadd_rn(g, __dmul_rn(cG, (double)v[a]));
+        } else if (a < D) {
+          g = __dadd_rn(g, __dmul_rn(cG, (double)me[a]));
+        } else {
+          g = __dadd_rn(g, cG);
+        }
+      }
+      Gp[(size_t)i * T + e] = g;
+    } else {
+      const int a = e - T;
+      for (int m = 0; m < M; ++m) {
+        const float* v = uvar + (size_t)m * D;
+        const float* me = umu + (size_t)m * D;
+        const double cG = (v[i] < min_var) ? (double)__fdiv_rn(1.0f, min_var) : (double)__fdiv_rn(1.0f, v[i]);
+        const double ck = __dmul_rn((double)me[i], cG);
+        g = __dadd_rn(g, a < D ? __dmul_rn(ck, (double)me[a]) : ck);
+      }
+      kp[(size_t)i * E + a] = g;
+    }
+  }
+}
+
+// w_i = G_i^-1 k_i per (speaker, row): the pivot-free Gauss-Jordan inverse of MATRIX::_Invert_Gen
+// (Matrix4_LMa.cpp:2232-2300) in FP64, as mllr_row_kernel. One block per (row i, speaker s).
+__global__ void mllr_solve_kernel(int S, int D, const double* __restrict__ Gd, const double* __restrict__ kd,
+                                  const double* __restrict__ Gp, const double* __restrict__ kp,
+                                  const int* __restrict__ status, double* __restrict__ W) {
+  extern __shared__ double sm[];
+  const int E = D + 1, T = E * (E + 1) / 2;
+  const int i = blockIdx.x, s = blockIdx.y;
+  double* G = sm;
+  double* kv = sm + E * E;
+  double* Wr = W + ((size_t)s * D + i) * E;
+  if (status[s] != GMM_OK) {
+    for (int a = threadIdx.x; a < E; a += blockDim.x) Wr[a] = 0.0;
+    return;
+  }
+  for (int e = threadIdx.x; e < E * E; e += blockDim.x) {
+    const int a = e / E, b = e - a * E;
+    const int ti = a <= b ? tri_index(a, b, E) : tri_index(b, a, E);
+    double g = Gd[((size_t)s * D + i) * T + ti];
+    if (Gp) g = __dadd_rn(Gp[(size_t)i * T + ti], g);
+    G[e] = g;
+  }
+  for (int a = threadIdx.x; a < E; a += blockDim.x) {
+    double k = kd[((size_t)s * D + i) * E + a];
+    if (kp) k = __dadd_rn(kp[(size_t)i * E + a], k);
+    kv[a] = k;
+  }
+  __syncthreads();
+  for (int k = 0; k < E; ++k) {
+    const double piv = G[k * E + k];
+    for (int e = threadIdx.x; e < E * E; e += blockDim.x) {
+      const int a = e / E, b = e - a * E;
+      if (a != k && b != k) G[e] = __dsub_rn(G[e], __ddiv_rn(__dmul_rn(G[k * E + b], G[a * E + k]), piv));
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < E; e += blockDim.x) {
+      if (e != k) {
+        G[k * E + e] = __ddiv_rn(-G[k * E + e], piv);
+        G[e * E + k] = __ddiv_rn(G[e * E + k], piv);
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) G[k * E + k] = __ddiv_rn(1.0, piv);
+    __syncthreads();
+  }
+  for (int a = threadIdx.x; a < E; a += blockDim.x) {
+    double v = 0.0;
+    for (int b = 0; b < E; ++b) v = __dadd_rn(v, __dmul_rn(G[a * E + b], kv[b]));
+    Wr[a] = v;
+  }
+}
+
+// AdaptModelMLLR (OL_ModelAdapt.cpp:1597-1608) for every (speaker, component): mu' = A mu + b.
+// One warp per (speaker, component); speakers whose transform failed keep the UBM means.
+__global__ void mllr_batch_apply_kernel(int S, int M, int D, const float* __restrict__ mu,
+                                        const double* __restrict__ W, const int* __restrict__ status,
+                                        float* __restrict__ out) {
+  const long long t = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (t >= (long long)S * M) return;
+  const int s = (int)(t / M), m = (int)(t - (long long)s * M);
+  const int E = D + 1;
+  const float* row = mu + (size_t)m * D;
+  for (int k = lane; k < D; k += 32) {
+    float r = row[k];
+    if (status[s] == GMM_OK) {
+      const double* Wk = W + ((size_t)s * D + k) * E;
+      double v = 0.0;
+      for (int kk = 0; kk < D; ++kk) v = __dadd_rn(v, __dmul_rn(Wk[kk], (double)row[kk]));
+      r = (float)__dadd_rn(v, Wk[D]);
+    }
+    out[(size_t)t * D + k] = r;
   }
 }
 
@@ -494,21 +754,105 @@ int mstep_mllr_apply(Ctx* c, const double* W_host) {
   return rc;
 }
 
-int mstep_map_batch(Ctx* c, const MapBatch& b, const double* stats, int layout, int K, int n_chunks,
-                    const int* row_of_comp) {
+int mstep_map_batch(Ctx* c, const MapBatch& b, const double* plain, const SpeakerStats* ss) {
   const long long tot = (long long)b.S * c->M;
   if (tot == 0) return GMM_OK;
   {
     GMM_LAUNCH(c, "map_batch_kernel");
     map_batch_kernel<<<(unsigned)((tot + 7) / 8), 256, 0, c->stream>>>(
-        b.S, c->M, c->D, layout, stats, K, n_chunks, row_of_comp, b.d_offs, c->w, c->mu, c->var,
-        b.tau, b.upW, b.upM, b.upV, c->min_var, b.w, b.mu, b.var, b.aw, b.ll);
+        b.S, c->M, c->D, plain, ss ? ss->part : nullptr, ss ? ss->K : 0, ss ? ss->n_chunks : 0,
+        ss ? ss->piece0 : nullptr, ss ? ss->npieces : nullptr, ss ? ss->row_of_comp : nullptr, b.d_offs,
+        c->w, c->mu, c->var, b.tau, b.upW, b.upM, b.upV, c->min_var, b.w, b.mu, b.var, b.aw, b.ll);
   }
   if (b.upW) {
     GMM_LAUNCH(c, "map_batch_norm_kernel");
     map_batch_norm_kernel<<<(b.S + 7) / 8, 256, 0, c->stream>>>(b.S, c->M, b.aw, b.w);
   }
   return GMM_OK;
+}
+
+// Batched global MLLR: per-speaker statistics (plain layout or tensor-core pieces) -> dense n, F
+// -> invertibility check -> G and k data terms as FP32-product GEMMs with FP64 sums (+ the UBM
+// prior terms when ubm_init) -> FP64 Gauss-Jordan solves -> optional adapted means. The resident
+// model is the UBM. dW [S][D][D+1], dstatus [S], dmu_out [S][M][D] or null.
+int mstep_mllr_batch(Ctx* c, int S, const double* plain, const SpeakerStats* ss, int ubm_init, double* dW,
+                     int* dstatus, float* dmu_out, double* dll) {
+  const int M = c->M, D = c->D, E = D + 1, T = E * (E + 1) / 2;
+  if (S == 0) return GMM_OK;
+  const float* umu = c->mu;
+  const float* uvar = c->var;
+  double *n = nullptr, *F = nullptr, *Gd = nullptr, *kd = nullptr, *Gp = nullptr, *kp = nullptr;
+  float *B = nullptr, *Xi = nullptr;
+  const size_t bn = sizeof(double) * (size_t)S * M, bF = bn * D, bG = sizeof(double) * (size_t)S * D * T;
+  const size_t bk = sizeof(double) * (size_t)S * D * E, bB = sizeof(float) * (size_t)M * T;
+  const size_t bXi = sizeof(float) * (size_t)M * E;
+  const size_t bGp = sizeof(double) * (size_t)D * T, bkp = sizeof(double) * (size_t)D * E;
+  int rc = dalloc(c, (void**)&n, bn, "MLLR n");
+  if (!rc) rc = dalloc(c, (void**)&F, bF, "MLLR F");
+  if (!rc) rc = dalloc(c, (void**)&Gd, bG, "MLLR G");
+  if (!rc) rc = dalloc(c, (void**)&kd, bk, "MLLR k");
+  if (!rc) rc = dalloc(c, (void**)&B, bB, "MLLR outer products");
+  if (!rc) rc = dalloc(c, (void**)&Xi, bXi, "MLLR extended means");
+  if (!rc && ubm_init) rc = dalloc(c, (void**)&Gp, bGp, "MLLR prior G");
+  if (!rc && ubm_init) rc = dalloc(c, (void**)&kp, bkp, "MLLR prior k");
+  const size_t smem = sizeof(double) * ((size_t)E * E + E);
+  if (!rc && smem > 200 * 1024) rc = fail(c, GMM_ERR_UNSUPPORTED, "MLLR: D too large for the shared-memory solve");
+  if (!rc) {
+    const long long tot = (long long)S * M;
+    {
+      GMM_LAUNCH(c, "mllr_gather_kernel");
+      mllr_gather_kernel<<<(unsigned)((tot + 7) / 8), 256, 0, c->stream>>>(
+          S, M, D, plain, ss ? ss->part : nullptr, ss ? ss->K : 0, ss ? ss->n_chunks : 0, ss ? ss->piece0 : nullptr,
+          ss ? ss->npieces : nullptr, ss ? ss->row_of_comp : nullptr, n, F, dll);
+    }
+    {
+      GMM_LAUNCH(c, "mllr_batch_check_kernel");
+      mllr_batch_check_kernel<<<(S + 7) / 8, 256, 0, c->stream>>>(S, M, D, n, dstatus);
+    }
+    {
+      GMM_LAUNCH(c, "mllr_outer_kernel");
+      mllr_outer_kernel<<<(unsigned)(((long long)M * T + 255) / 256), 256, 0, c->stream>>>(M, D, umu, B);
+    }
+    {
+      GMM_LAUNCH(c, "mllr_xi_kernel");
+      mllr_xi_kernel<<<(unsigned)(((long long)M * E + 255) / 256), 256, 0, c->stream>>>(M, D, umu, Xi);
+    }
+    {
+      // G data term: coef = n[s][m]
+      GMM_LAUNCH(c, "mllr_gemm_kernel");
+      dim3 grid((T + 63) / 64, (S + 63) / 64, D);
+      mllr_gemm_kernel<<<grid, 256, 0, c->stream>>>(S, M, D, T, n, (long long)M, 1, 0, uvar, B, T, Gd);
+    }
+    {
+      // k data term: coef = F[s][m][i]
+      GMM_LAUNCH(c, "mllr_gemm_kernel");
+      dim3 grid((E + 63) / 64, (S + 63) / 64, D);
+      mllr_gemm_kernel<<<grid, 256, 0, c->stream>>>(S, M, D, E, F, (long long)M * D, D, 1, uvar, Xi, E, kd);
+    }
+    if (ubm_init) {
+      GMM_LAUNCH(c, "mllr_prior_kernel");
+      mllr_prior_kernel<<<D, 256, 0, c->stream>>>(M, D, umu, uvar, c->min_var, Gp, kp);
+    }
+    cudaFuncSetAttribute(mllr_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    {
+      GMM_LAUNCH(c, "mllr_solve_kernel");
+      mllr_solve_kernel<<<dim3(D, S), 128, smem, c->stream>>>(S, D, Gd, kd, Gp, kp, dstatus, dW);
+    }
+    if (dmu_out) {
+      GMM_LAUNCH(c, "mllr_batch_apply_kernel");
+      mllr_batch_apply_kernel<<<(unsigned)((tot + 7) / 8), 256, 0, c->stream>>>(S, M, D, umu, dW, dstatus, dmu_out);
+    }
+    rc = sync(c, "batched MLLR");
+  }
+  dfree(c, n, bn);
+  dfree(c, F, bF);
+  dfree(c, Gd, bG);
+  dfree(c, kd, bk);
+  dfree(c, B, bB);
+  dfree(c, Xi, bXi);
+  dfree(c, Gp, bGp);
+  dfree(c, kp, bkp);
+  return rc;
 }
 
 }  // namespace gmm

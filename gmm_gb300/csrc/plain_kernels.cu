@@ -424,30 +424,45 @@ int plain_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
   return GMM_OK;
 }
 
-// Batched MAP with FP32 statistics: one plain E-step per speaker over its frame range (the
-// reference's one-speaker-at-a-time AdaptModelMAP loop, OL_ModelAdapt.cpp:1165-1205), each into
-// its own statistics block, then one M-step launch for all speakers.
-int plain_map_batch(Ctx* c, const MapBatch& b) {
+// Per-speaker FP32-path statistics: one plain E-step per speaker over its frame range (the
+// reference's one-speaker-at-a-time AdaptModel loop, projects/Model_ADAPT/Model_ADAPT.cpp:170-240),
+// each into its own block [n (M) | F (M x D) | S (M x D) | totLL | pad].
+int plain_speaker_stats(Ctx* c, int S, const long long* offs, int flags, double** out, size_t* bytes) {
   const int M = c->M, D = c->D;
   const size_t stride = (size_t)M * (1 + 2 * D) + 2;
-  const size_t bytes = sizeof(double) * stride * (size_t)(b.S > 0 ? b.S : 1);
-  double* d_stats = nullptr;
-  int rc = dalloc(c, (void**)&d_stats, bytes, "per-speaker statistics");
+  *bytes = sizeof(double) * stride * (size_t)(S > 0 ? S : 1);
+  *out = nullptr;
+  int rc = dalloc(c, (void**)out, *bytes, "per-speaker statistics");
   if (rc) return rc;
-  cudaMemsetAsync(d_stats, 0, bytes, c->stream);
+  double* d_stats = *out;
+  cudaMemsetAsync(d_stats, 0, *bytes, c->stream);
   const float* X0 = c->X;
   const long long N0 = c->N;
   double* stats0 = c->stats;
-  for (int s = 0; s < b.S && !rc; ++s) {
-    c->X = X0 + (size_t)b.offs[s] * D;
-    c->N = b.offs[s + 1] - b.offs[s];
+  for (int s = 0; s < S && !rc; ++s) {
+    c->X = X0 + (size_t)offs[s] * D;
+    c->N = offs[s + 1] - offs[s];
     c->stats = d_stats + (size_t)s * stride;
-    if (c->N > 0) rc = plain_estep(c, b.flags, true, nullptr);
+    if (c->N > 0) rc = plain_estep(c, flags, true, nullptr);
   }
   c->X = X0;
   c->N = N0;
   c->stats = stats0;
-  if (!rc) rc = mstep_map_batch(c, b, d_stats, kStatsPlain, 0, 0, nullptr);
+  if (rc) {
+    cudaStreamSynchronize(c->stream);
+    dfree(c, *out, *bytes);
+    *out = nullptr;
+  }
+  return rc;
+}
+
+// Batched MAP with FP32 statistics: the per-speaker plain E-steps, then one M-step launch for all.
+int plain_map_batch(Ctx* c, const MapBatch& b) {
+  double* d_stats = nullptr;
+  size_t bytes = 0;
+  int rc = plain_speaker_stats(c, b.S, b.offs, b.flags, &d_stats, &bytes);
+  if (rc) return rc;
+  rc = mstep_map_batch(c, b, d_stats, nullptr);
   if (!rc) rc = sync(c, "batched MAP (FP32 statistics)");
   cudaStreamSynchronize(c->stream);
   dfree(c, d_stats, bytes);

@@ -512,8 +512,8 @@ template <int K>
 __global__ void __launch_bounds__(kThreads, 1)
     acc_kernel(const __grid_constant__ CUtensorMap zmap, const uint16_t* __restrict__ wplanes,
                int nTz, int nTw, const float* __restrict__ ll2, int n_tiles, int n_chunks, int slices,
-               const int* __restrict__ tile_slot, const int* __restrict__ slice_t0,
-               const int4* __restrict__ work, float minGamma, int single_comp,
+               const int* __restrict__ tile_slot, const int4* __restrict__ work, float minGamma,
+               int single_comp,
                double* __restrict__ part, int* __restrict__ err) {
   using C = AccCfg<K>;
   constexpr int FT = C::FT, NZ = C::NZ, FLUSH = C::FLUSH;
@@ -543,9 +543,6 @@ __global__ void __launch_bounds__(kThreads, 1)
     chunk = wi.y;
     t0 = wi.z;
     nt = wi.w;
-  } else if (slice_t0) {
-    t0 = slice_t0[slice];
-    nt = slice_t0[slice + 1] - t0;
   } else {
     const int per = (n_tiles + slices - 1) / slices;
     t0 = slice * per;
@@ -867,41 +864,6 @@ __global__ void seg_sum_kernel(const long long* __restrict__ offs, const float* 
   }
 }
 
-template <int K>
-int map_batch_launch(Ctx* c, long long Rpad, const long long* d_row_frame, const int* d_tile_slot,
-                     const int* d_slice_t0, int slices, double* d_part) {
-  using LC = LlCfg<K>;
-  using AC = AccCfg<K>;
-  const int nTz = (int)(Rpad / 128), nTw = c->tcm.Mpad / 128;
-  int grid_ll = std::min(nTz, c->sms);
-  if (grid_ll < 1) grid_ll = 1;
-  const size_t need = (size_t)grid_ll * 128;
-  if (need > c->tc_llpart_cap) {
-    dfree(c, c->tc_llpart, c->tc_llpart_cap * sizeof(double));
-    c->tc_llpart = nullptr;
-    c->tc_llpart_cap = 0;
-    int rc = dalloc(c, (void**)&c->tc_llpart, need * sizeof(double), "tc llpart");
-    if (rc) return rc;
-    c->tc_llpart_cap = need;
-  }
-  cudaFuncSetAttribute(ll_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, LC::SMEM);
-  cudaFuncSetAttribute(acc_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, AC::SMEM);
-  {
-    GMM_LAUNCH(c, "tc_ll_kernel");
-    ll_kernel<K><<<grid_ll, kLlThreads, LC::SMEM, c->stream>>>(
-        c->tm_wfull, c->tcx.planes, c->N, d_row_frame, nullptr, nTz, nTw, nTz, nTw,
-        (float)(c->minLL * kLog2e), c->minLL, c->tcm.ll2, c->ll, c->tc_llpart, c->tc_err);
-  }
-  {
-    GMM_LAUNCH(c, "tc_acc_kernel");
-    const CUtensorMap& zm = AC::FT == 128 ? c->tm_zfull : c->tm_zhalf;
-    acc_kernel<K><<<nTw * slices, kThreads, AC::SMEM, c->stream>>>(
-        zm, c->tcm.planes, nTz, nTw, c->tcm.ll2, (int)(Rpad / AC::FT), nTw, slices, d_tile_slot,
-        d_slice_t0, nullptr, c->minGamma, c->Mact == 1, d_part, c->tc_err);
-  }
-  return GMM_OK;
-}
-
 // ------------------------------------------------------------------ host side
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
@@ -992,7 +954,7 @@ int launch_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
     const CUtensorMap& zm = AC::FT == 128 ? c->tm_zfull : c->tm_zhalf;
     acc_kernel<K><<<grid, kThreads, AC::SMEM, c->stream>>>(
         zm, c->tcm.planes, nTz, nTw, c->tcm.ll2, n_tiles, n_chunks, slices, nullptr, nullptr,
-        nullptr, c->minGamma, c->Mact == 1, c->tcpart, c->tc_err);
+        c->minGamma, c->Mact == 1, c->tcpart, c->tc_err);
   }
   {
     GMM_LAUNCH(c, "tc_reduce_kernel");
@@ -1106,11 +1068,14 @@ int tc_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
 }
 
 
-// Batched MAP, tensor-core statistics: every speaker's frames are laid out from a 128-row tile
-// boundary (padding rows carry no frame), the logits kernel runs once over all tiles, and the
-// statistics kernel gives each (speaker, component chunk) its own FP64 accumulator slot; its
-// frame-tile slices are cut at speaker boundaries so that every slot has one writer.
-int tc_map_batch(Ctx* c, const MapBatch& b) {
+// Per-speaker statistics of S speakers in one fused E-step over the resident features (speaker s
+// owns frames [offs[s], offs[s+1])). Every speaker starts on a 128-row tile of a padded row
+// layout; its frames are cut into pieces of one FP64 flush period (8192 frames), each piece with
+// its own FP64 slot, and the statistics kernel runs over work items (component chunk x range of
+// whole pieces) of about equal size. A speaker's sums are the piece slots added in piece order.
+int tc_speaker_stats(Ctx* c, int S, const long long* offs, const long long* d_offs, double* d_ll,
+                     SpeakerStats* ss) {
+  *ss = SpeakerStats();
   if (!tc_supported(c->D)) return fail(c, GMM_ERR_UNSUPPORTED, "tensor-core path supports 1 <= D <= 63");
   if (!c->tc_err) {
     int rc = dalloc(c, (void**)&c->tc_err, sizeof(int), "tc error flag");
@@ -1120,13 +1085,12 @@ int tc_map_batch(Ctx* c, const MapBatch& b) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, dev);
   }
-  const int S = b.S, M = c->M, D = c->D, K = tc_K(D);
-  const long long* offs = b.offs;
+  const int M = c->M, D = c->D, K = tc_K(D);
   int rc = tc_prepare_model(c);
   if (rc) return rc;
-  const int FT = acc_ft(K);
+  const int FT = acc_ft(K), FLUSH = 64 * 128 / FT;
   const int n_chunks = c->tcm.Mpad / 128;
-  // padded row layout: speaker s starts at row pad[s], a multiple of 128
+  // padded row layout and pieces
   std::vector<long long> pad((size_t)S + 1, 0);
   for (int s = 0; s < S; ++s) pad[s + 1] = pad[s] + (offs[s + 1] - offs[s] + 127) / 128 * 128;
   const long long Rpad = pad[S] > 0 ? pad[S] : 128;
@@ -1134,31 +1098,53 @@ int tc_map_batch(Ctx* c, const MapBatch& b) {
   for (int s = 0; s < S; ++s)
     for (long long f = offs[s]; f < offs[s + 1]; ++f) row_frame[(size_t)(pad[s] + f - offs[s])] = f;
   const long long ntiles = Rpad / FT;
-  std::vector<int> tile_slot((size_t)ntiles, 0);
-  for (int s = 0; s < S; ++s)
-    for (long long t = pad[s] / FT; t < pad[s + 1] / FT; ++t) tile_slot[(size_t)t] = s;
-  // slices: contiguous speaker ranges of about equal tile counts, one CTA per (slice, chunk)
-  const int want = std::max(1, std::min<int>((int)ntiles, c->sms / n_chunks));
-  std::vector<int> slice_t0(1, 0);
-  {
-    const double target = (double)ntiles / want;
-    for (int s = 0; s + 1 < S && (int)slice_t0.size() < want; ++s)
-      if ((double)(pad[s + 1] / FT) >= target * (double)slice_t0.size() && pad[s + 1] / FT > slice_t0.back())
-        slice_t0.push_back((int)(pad[s + 1] / FT));
-    slice_t0.push_back((int)ntiles);
+  std::vector<int> tile_slot((size_t)ntiles, 0), piece0((size_t)S, 0), npieces((size_t)S, 0);
+  int pieces = 0;
+  for (int s = 0; s < S; ++s) {
+    const long long t0 = pad[s] / FT, t1 = pad[s + 1] / FT;
+    piece0[s] = pieces;
+    npieces[s] = (int)((t1 - t0 + FLUSH - 1) / FLUSH);
+    for (long long t = t0; t < t1; ++t) tile_slot[(size_t)t] = pieces + (int)((t - t0) / FLUSH);
+    pieces += npieces[s];
   }
-  const int slices = (int)slice_t0.size() - 1;
-  const size_t part_bytes = (size_t)S * n_chunks * 128 * K * sizeof(double);
+  // work items: ranges of whole pieces of about equal tile counts, one CTA per (range, chunk)
+  std::vector<int4> work;
+  {
+    const long long target = std::max<long long>(FLUSH / 4, ntiles * n_chunks / std::max(1, c->sms));
+    long long t0 = 0, acc = 0, cur = 0;
+    for (int s = 0; s < S; ++s) {
+      const long long rt = (pad[s + 1] - pad[s]) / FT;
+      for (int p = 0; p < npieces[s]; ++p) {
+        const long long pt = std::min<long long>(FLUSH, rt - (long long)p * FLUSH);
+        acc += pt;
+        cur += pt;
+        if (acc >= target) {
+          for (int ch = 0; ch < n_chunks; ++ch) work.push_back(make_int4(ch, ch, (int)t0, (int)(cur - t0)));
+          t0 = cur;
+          acc = 0;
+        }
+      }
+    }
+    if (cur > t0)
+      for (int ch = 0; ch < n_chunks; ++ch) work.push_back(make_int4(ch, ch, (int)t0, (int)(cur - t0)));
+  }
   const size_t rf_bytes = sizeof(long long) * (size_t)Rpad, ts_bytes = sizeof(int) * (size_t)ntiles;
-  const size_t st_bytes = sizeof(int) * (size_t)(slices + 1), roc_bytes = sizeof(int) * (size_t)M;
+  const size_t wk_bytes = sizeof(int4) * std::max<size_t>(1, work.size());
   long long* d_rf = nullptr;
-  int *d_ts = nullptr, *d_st = nullptr, *d_roc = nullptr;
-  double* d_part = nullptr;
+  int* d_ts = nullptr;
+  int4* d_wk = nullptr;
+  ss->S = S;
+  ss->n_chunks = n_chunks;
+  ss->K = K;
+  ss->pieces = pieces;
+  ss->part_bytes = (size_t)std::max(pieces, 1) * n_chunks * K * 128 * sizeof(double);
   rc = dalloc(c, (void**)&d_rf, rf_bytes, "row map");
   if (!rc) rc = dalloc(c, (void**)&d_ts, ts_bytes, "tile slots");
-  if (!rc) rc = dalloc(c, (void**)&d_st, st_bytes, "slice ranges");
-  if (!rc) rc = dalloc(c, (void**)&d_roc, roc_bytes, "component rows");
-  if (!rc) rc = dalloc(c, (void**)&d_part, part_bytes, "per-speaker statistics");
+  if (!rc) rc = dalloc(c, (void**)&d_wk, wk_bytes, "work items");
+  if (!rc) rc = dalloc(c, (void**)&ss->part, ss->part_bytes, "per-speaker statistics");
+  if (!rc) rc = dalloc(c, (void**)&ss->piece0, sizeof(int) * std::max(S, 1), "speaker pieces");
+  if (!rc) rc = dalloc(c, (void**)&ss->npieces, sizeof(int) * std::max(S, 1), "speaker pieces");
+  if (!rc) rc = dalloc(c, (void**)&ss->row_of_comp, sizeof(int) * M, "component rows");
   if (!rc) {
     // operand planes in the padded layout; the next regular E-step rebuilds its own
     const size_t pbytes = (size_t)3 * Rpad * K * sizeof(uint16_t);
@@ -1177,55 +1163,85 @@ int tc_map_batch(Ctx* c, const MapBatch& b) {
     }
     c->tcx_valid = false;
   }
+  const size_t need = (size_t)std::max(1, c->sms) * 128;
+  if (!rc && need > c->tc_llpart_cap) {
+    dfree(c, c->tc_llpart, c->tc_llpart_cap * sizeof(double));
+    c->tc_llpart = nullptr;
+    c->tc_llpart_cap = 0;
+    rc = dalloc(c, (void**)&c->tc_llpart, need * sizeof(double), "tc llpart");
+    if (!rc) c->tc_llpart_cap = need;
+  }
   if (!rc) {
     cudaMemcpyAsync(d_rf, row_frame.data(), rf_bytes, cudaMemcpyHostToDevice, c->stream);
     cudaMemcpyAsync(d_ts, tile_slot.data(), ts_bytes, cudaMemcpyHostToDevice, c->stream);
-    cudaMemcpyAsync(d_st, slice_t0.data(), st_bytes, cudaMemcpyHostToDevice, c->stream);
-    cudaMemsetAsync(d_part, 0, part_bytes, c->stream);
-    GMM_LAUNCH(c, "tc_features_kernel");
-    features_kernel<<<(unsigned)((Rpad * (K / 8) + 255) / 256), 256, 0, c->stream>>>(
-        c->X, c->N, Rpad / 128, D, K, d_rf, c->tcx.planes);
-  }
-  if (!rc) rc = make_map(c, &c->tm_zfull, c->tcx.planes, 3 * Rpad * K, K);
-  if (!rc) rc = make_map(c, &c->tm_zhalf, c->tcx.planes, 3 * Rpad * K, 4);
-  if (!rc) {
-    switch (K) {
-      case 16: rc = map_batch_launch<16>(c, Rpad, d_rf, d_ts, d_st, slices, d_part); break;
-      case 32: rc = map_batch_launch<32>(c, Rpad, d_rf, d_ts, d_st, slices, d_part); break;
-      case 48: rc = map_batch_launch<48>(c, Rpad, d_rf, d_ts, d_st, slices, d_part); break;
-      case 64: rc = map_batch_launch<64>(c, Rpad, d_rf, d_ts, d_st, slices, d_part); break;
-      case 80: rc = map_batch_launch<80>(c, Rpad, d_rf, d_ts, d_st, slices, d_part); break;
-      case 96: rc = map_batch_launch<96>(c, Rpad, d_rf, d_ts, d_st, slices, d_part); break;
-      case 112: rc = map_batch_launch<112>(c, Rpad, d_rf, d_ts, d_st, slices, d_part); break;
-      default: rc = map_batch_launch<128>(c, Rpad, d_rf, d_ts, d_st, slices, d_part); break;
+    if (!work.empty()) cudaMemcpyAsync(d_wk, work.data(), work.size() * sizeof(int4), cudaMemcpyHostToDevice, c->stream);
+    if (S > 0) {
+      cudaMemcpyAsync(ss->piece0, piece0.data(), sizeof(int) * S, cudaMemcpyHostToDevice, c->stream);
+      cudaMemcpyAsync(ss->npieces, npieces.data(), sizeof(int) * S, cudaMemcpyHostToDevice, c->stream);
     }
+    TcBatch t;
+    t.D = D;
+    t.K = K;
+    t.n_chunks = n_chunks;
+    t.w_chunks_total = n_chunks;
+    t.wplanes = c->tcm.planes;
+    t.wmap = &c->tm_wfull;
+    t.X = c->X;
+    t.N = c->N;
+    t.Rpad = Rpad;
+    t.row_frame = d_rf;
+    t.tile_wbase = nullptr;
+    t.zplanes = c->tcx.planes;
+    t.ll2 = c->tcm.ll2;
+    t.ll = c->ll;
+    t.llpart = c->tc_llpart;
+    t.n_work = (int)work.size();
+    t.work = d_wk;
+    t.tile_slot = d_ts;
+    t.part = ss->part;
+    t.single_comp = c->Mact == 1;
+    rc = tc_run_batch(c, t);
   }
   if (!rc) {
     {
       GMM_LAUNCH(c, "row_of_comp_kernel");
-      row_of_comp_kernel<<<1, 1024, 0, c->stream>>>(M, c->tcm.Mpad, c->tcm.comp_of_row, d_roc);
+      row_of_comp_kernel<<<1, 1024, 0, c->stream>>>(M, c->tcm.Mpad, c->tcm.comp_of_row, ss->row_of_comp);
     }
-    if (S > 0) {
+    if (S > 0 && d_ll) {
       GMM_LAUNCH(c, "seg_sum_kernel");
-      seg_sum_kernel<<<S, 256, 0, c->stream>>>(b.d_offs, c->ll, b.ll);
+      seg_sum_kernel<<<S, 256, 0, c->stream>>>(d_offs, c->ll, d_ll);
     }
-    rc = mstep_map_batch(c, b, d_part, kStatsSlots, K, n_chunks, d_roc);
-  }
-  if (!rc) {
     int herr = 0;
     cudaMemcpyAsync(&herr, c->tc_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
-    rc = sync(c, "batched MAP (tensor-core statistics)");
+    rc = sync(c, "per-speaker statistics (tensor-core path)");
     if (!rc && herr) {
       cudaMemsetAsync(c->tc_err, 0, sizeof(int), c->stream);
-      rc = fail(c, GMM_ERR_TIMEOUT, "batched MAP: a bounded device wait expired");
+      rc = fail(c, GMM_ERR_TIMEOUT, "per-speaker statistics: a bounded device wait expired");
     }
   }
   cudaStreamSynchronize(c->stream);
   dfree(c, d_rf, rf_bytes);
   dfree(c, d_ts, ts_bytes);
-  dfree(c, d_st, st_bytes);
-  dfree(c, d_roc, roc_bytes);
-  dfree(c, d_part, part_bytes);
+  dfree(c, d_wk, wk_bytes);
+  if (rc) tc_free_speaker_stats(c, ss);
+  return rc;
+}
+
+void tc_free_speaker_stats(Ctx* c, SpeakerStats* ss) {
+  dfree(c, ss->part, ss->part_bytes);
+  dfree(c, ss->piece0, sizeof(int) * std::max(ss->S, 1));
+  dfree(c, ss->npieces, sizeof(int) * std::max(ss->S, 1));
+  dfree(c, ss->row_of_comp, sizeof(int) * c->M);
+  *ss = SpeakerStats();
+}
+
+int tc_map_batch(Ctx* c, const MapBatch& b) {
+  SpeakerStats ss;
+  int rc = tc_speaker_stats(c, b.S, b.offs, b.d_offs, b.ll, &ss);
+  if (rc) return rc;
+  rc = mstep_map_batch(c, b, nullptr, &ss);
+  if (!rc) rc = sync(c, "batched MAP update");
+  tc_free_speaker_stats(c, &ss);
   return rc;
 }
 
@@ -1269,7 +1285,7 @@ void run_batch_k(Ctx* c, const TcBatch& b, const CUtensorMap& zfull, const CUten
     const CUtensorMap& zm = AC::FT == 128 ? zfull : zhalf;
     acc_kernel<K><<<b.n_work, kThreads, AC::SMEM, c->stream>>>(
         zm, b.wplanes, nTz, b.w_chunks_total, b.ll2, (int)(b.Rpad / AC::FT), b.n_chunks, 1, b.tile_slot,
-        nullptr, b.work, c->minGamma, b.single_comp, b.part, c->tc_err);
+        b.work, c->minGamma, b.single_comp, b.part, c->tc_err);
   }
 }
 }  // namespace

@@ -114,6 +114,19 @@ int gmm_map_update(gmm_handle h, int tau, int up_weight, int up_mean, int up_var
  * total log-likelihood under the UBM). tau >= 1. The resident model is not changed. */
 int gmm_map_batch(gmm_handle h, int S, const long long* offs, int tau, int up_weight, int up_mean,
                   int up_var, float* w, float* mu, float* var, double* ll);
+/* Global MLLR mean transforms for S speakers in one call (one regression class, one iteration):
+ * the per-speaker loop of Model_ADAPT around CModelAdapt::AdaptModel with adaptType MLLR
+ * (OL_ModelAdapt.cpp:1175-1184: IterW_MLLR -> ComputeW_MLLR :1417-1482, ComputeKiGi_MLLR
+ * :1525-1581, prepareKiGiInitMatrices :1484-1523 when ubm_init, CheckInvertibility :1851-1878,
+ * AdaptModelMLLR :1583-1612). Speakers own resident frame ranges as in gmm_map_batch; the
+ * resident model is the UBM. The G and k sums over components run as FP32-product GEMMs with FP64
+ * accumulation (the single-speaker gmm_mllr_estimate keeps the reference's FP64 sequence); each
+ * row is solved in FP64 with the reference's pivot-free Gauss-Jordan inverse. Outputs (host, any
+ * may be NULL): W [S][D][D+1] row-major, status [S] (GMM_OK or GMM_ERR_MLLR when the speaker has
+ * too few components or frames; its W is zero and its means stay the UBM's), mu_out [S][M][D]
+ * adapted means, ll [S]. */
+int gmm_mllr_batch(gmm_handle h, int S, const long long* offs, int ubm_init, double* W, int* status,
+                   float* mu_out, double* ll);
 /* The same with device outputs (d_w, d_mu, d_var, d_ll on the handle's device; any may be NULL). */
 int gmm_map_batch_device(gmm_handle h, int S, const long long* offs, int tau, int up_weight,
                          int up_mean, int up_var, float* d_w, float* d_mu, float* d_var,
