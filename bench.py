@@ -11,6 +11,11 @@ Workloads (--workload):
              each a seeded 16-component shift of the UBM, frame counts lognormal clipped to
              200..30000 (4.8M frames, 1.15 GB), relevance factor 16. One step = one MAP
              iteration of every speaker (statistics over the UBM + UpdateModelMAP), in one call.
+  mllr-batch batched global MLLR -- UBM M = 2048, D = 39, 500 speakers with frame counts uniform
+             in 1000..20000, features = a seeded random affine transform of UBM samples. One
+             step = one transform estimation for every speaker (mean statistics, G and k, FP64
+             solves), in one call.
+  serve      the request server under Poisson arrivals (see run_serve).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--precision tc|fp32] [--workload ...]
     python bench.py --impl reference ...   # the reference CPU algorithm on the host cores
@@ -44,7 +49,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="ubm-em", choices=["ubm-em", "map-batch", "serve"])
+    ap.add_argument("--workload", default="ubm-em", choices=["ubm-em", "map-batch", "mllr-batch", "serve"])
     ap.add_argument("--models", type=int, default=200, help="serve: resident models")
     ap.add_argument("--pool", type=int, default=256, help="serve: utterances per request kind")
     ap.add_argument("--rates", default="500,1000,2000,5000,10000,15000,20000", help="serve: arrival rates (req/s)")
@@ -63,11 +68,13 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     a = ap.parse_args()
-    em = a.workload == "ubm-em"
+    big = a.workload in ("ubm-em", "mllr-batch")  # M = 2048, D = 39 workloads
     a.frames = a.frames or 10_000_000
-    a.mix = a.mix or (2048 if em else 1024)
-    a.dim = a.dim or (39 if em else 60)
-    a.seed = a.seed if a.seed is not None else {"ubm-em": 2, "map-batch": 3, "serve": 5}[a.workload]
+    a.mix = a.mix or (2048 if big else 1024)
+    a.dim = a.dim or (39 if big else 60)
+    if a.workload == "mllr-batch" and a.speakers == 1000:
+        a.speakers = 500
+    a.seed = a.seed if a.seed is not None else {"ubm-em": 2, "map-batch": 3, "mllr-batch": 4, "serve": 5}[a.workload]
     return a
 
 
@@ -286,7 +293,75 @@ class MapBatch:
                                       f"(mean-only MAP: E-step + update), {dt:.1f} s")
 
 
-WORKLOADS = {"ubm-em": UbmEm, "map-batch": MapBatch}
+class MllrBatch:
+    """One global MLLR transform estimation for every speaker of a batch against a resident UBM."""
+    metric = "frames·components/s per MLLR iter (batched speakers)"
+
+    def __init__(self, args, rank):
+        from gmm_gb300 import synth
+        self.a = args
+        self.M, self.D, self.S = args.mix, args.dim, args.speakers
+        self.X, self.offs, (self.uw, self.umu, self.uvar), _ = synth.c4(args.seed + rank, self.S, self.M,
+                                                                        self.D)
+        self.N = int(self.offs[-1])
+        self.fc = self.N * self.M
+
+    def describe(self):
+        lens = np.diff(self.offs)
+        return {"workload": f"batched global MLLR, {self.S} speakers x {lens.min()}-{lens.max()} frames "
+                            f"(N={self.N}), UBM M={self.M}, D={self.D}, one regression class",
+                "frames": self.N, "speakers": self.S, "components": self.M, "dim": self.D,
+                "l2": f"inputs larger than L2 (features {self.X.nbytes / 1e9:.2f} GB)"}
+
+    def setup(self, dev, lib, torch, device):
+        self.dev, self.lib = dev, lib
+        self.Xpin = torch.from_numpy(self.X).pin_memory()
+        self.dX = self.Xpin.to(device)
+        dev.upload_model(self.uw, self.umu, self.uvar)
+        dev.upload_features_device(self.dX.data_ptr(), self.N, self.D)
+        self.W = np.zeros((self.S, self.D, self.D + 1))
+        self.st = np.zeros(self.S, np.int32)
+        self.o = np.ascontiguousarray(self.offs, np.int64)
+
+    def step(self):
+        dev = self.dev
+        dev.check(dev.lib.gmm_mllr_batch(dev.h, self.S, self.o.ctypes.data, 0, self.W.ctypes.data,
+                                         self.st.ctypes.data, None, None))
+
+    def flop_per_fc(self, kernel):
+        D = self.D
+        if kernel == "tc_acc_kernel":
+            return 2 * (2 * D + 1) + 2 * (D + 1)  # logits + mean-only statistics
+        return 2 * (2 * D + 1)
+
+    def e2e_prepare(self, torch):
+        self.Xhost = self.Xpin.numpy()
+        return int(self.X.nbytes), int(self.W.nbytes + self.st.nbytes)
+
+    def e2e_step(self):
+        self.dev.upload_features(self.Xhost)
+        self.step()
+
+    def cpu_rate(self, seconds, threads):
+        """The reference CPU algorithm per speaker (the oracle port: accumulateStatsMT with all
+        host threads + ComputeW_MLLR), over as many speakers as fit the time budget."""
+        import oracle
+        oracle.build(ref=False)
+        t = time.perf_counter()
+        frames = 0
+        s = 0
+        while s < self.S and (time.perf_counter() - t) < seconds:
+            Xs = self.X[self.offs[s]:self.offs[s + 1]]
+            st = oracle.accumulate32(Xs, self.uw, self.umu, self.uvar, flags=oracle.ACC_MEAN, threads=threads)
+            oracle.mllr_w(self.umu, self.uvar, st)
+            frames += len(Xs)
+            s += 1
+        dt = time.perf_counter() - t
+        return frames * self.M / dt, (f"first {s} speakers ({frames} frames) x {self.M} components "
+                                      f"(MLLR: E-step + G/k + solves), {dt:.1f} s")
+
+
+WORKLOADS = {"ubm-em": UbmEm, "map-batch": MapBatch, "mllr-batch": MllrBatch}
 
 
 # ------------------------------------------------------------------ served request loop
@@ -450,7 +525,7 @@ def run_reference(args):
     threads = os.cpu_count() or 1
     if args.workload == "serve":
         return run_serve_reference(args, threads)
-    wl = UbmEm(args, 0, gen_frames=400_000) if args.workload == "ubm-em" else MapBatch(args, 0)
+    wl = UbmEm(args, 0, gen_frames=400_000) if args.workload == "ubm-em" else WORKLOADS[args.workload](args, 0)
     per_step = max(1.0, 60.0 / max(1, args.steps + args.warmup))
     rates = []
     for i in range(args.warmup + args.steps):

@@ -426,11 +426,14 @@ __global__ void mllr_batch_check_kernel(int S, int M, int D, const double* __res
   if (s >= S) return;
   int act = 0;
   double occ = 0.0;
-  if (lane == 0)
-    for (int m = 0; m < M; ++m) {
-      const double v = n[(size_t)s * M + m];
-      if (v > 0.0) { ++act; occ = __dadd_rn(occ, v); }
-    }
+  for (int m = lane; m < M; m += 32) {
+    const double v = n[(size_t)s * M + m];
+    if (v > 0.0) { ++act; occ += v; }
+  }
+  for (int o = 16; o; o >>= 1) {
+    act += __shfl_xor_sync(0xffffffffu, act, o);
+    occ += __shfl_xor_sync(0xffffffffu, occ, o);
+  }
   if (lane == 0) {
     const int E = D + 1;
     status[s] = (M < E || act < E || occ * D < (double)D * E) ? GMM_ERR_MLLR : GMM_OK;
@@ -462,61 +465,64 @@ __global__ void mllr_xi_kernel(int M, int D, const float* __restrict__ mu, float
 // The data terms of ComputeKiGi_MLLR (OL_ModelAdapt.cpp:1525-1581) for all speakers and rows as
 // GEMMs over the components: out[s][i][c] = sum_m (coef(s, m) / var[m][i]) * B[m][c], with
 // coef = n (G, c = upper-triangle pair) or coef = F[.][.][i] (k, c = a, B = xi). FP32 operands
-// (coef * 1/var rounded to float) and products in 64 x 64 tiles, FP32 sums over 128 components at
-// a time, added into FP64.
+// (coef * 1/var rounded to float) and products in 128 x 64 tiles, FP32 sums over 128 components
+// at a time, added into FP64.
 __global__ void __launch_bounds__(256) mllr_gemm_kernel(int S, int M, int D, int C, const double* __restrict__ coef,
                                                          long long cs_s, long long cs_m, int coef_i_stride,
                                                          const float* __restrict__ var,
                                                          const float* __restrict__ B, int ldb,
                                                          double* __restrict__ out) {
-  __shared__ float As[32][65];
+  // 128 speakers x 64 columns per block, 8 x 4 outputs per thread
+  __shared__ float As[32][129];
   __shared__ float Bs[32][64];
   const int i = blockIdx.z;
-  const int s0 = blockIdx.y * 64, c0 = blockIdx.x * 64;
+  const int s0 = blockIdx.y * 128, c0 = blockIdx.x * 64;
   const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
-  float acc[4][4];
-  double dacc[4][4];
+  float acc[8][4];
+  double dacc[8][4];
 #pragma unroll
-  for (int u = 0; u < 4; ++u)
+  for (int u = 0; u < 8; ++u)
 #pragma unroll
     for (int v = 0; v < 4; ++v) { acc[u][v] = 0.0f; dacc[u][v] = 0.0; }
   for (int m0 = 0; m0 < M; m0 += 32) {
-    for (int e = tid; e < 32 * 64; e += 256) {
-      const int mm = e >> 6, ss = e & 63;
+    for (int e = tid; e < 32 * 128; e += 256) {
+      const int mm = e >> 7, ss = e & 127;
       const int m = m0 + mm, s = s0 + ss;
       float a = 0.0f;
       if (m < M && s < S)
         a = __fmul_rn((float)coef[(size_t)s * cs_s + (size_t)m * cs_m + (size_t)i * coef_i_stride],
                       __frcp_rn(var[(size_t)m * D + i]));
       As[mm][ss] = a;
-      const int cc = e & 63;
-      const int c = c0 + cc;
+    }
+    for (int e = tid; e < 32 * 64; e += 256) {
+      const int mm = e >> 6, cc = e & 63;
+      const int m = m0 + mm, c = c0 + cc;
       Bs[mm][cc] = (m < M && c < C) ? B[(size_t)m * ldb + c] : 0.0f;
     }
     __syncthreads();
-#pragma unroll 8
+#pragma unroll 4
     for (int mm = 0; mm < 32; ++mm) {
-      float av[4], bv[4];
+      float av[8], bv[4];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) av[u] = As[mm][ty * 4 + u];
+      for (int u = 0; u < 8; ++u) av[u] = As[mm][ty * 8 + u];
 #pragma unroll
       for (int v = 0; v < 4; ++v) bv[v] = Bs[mm][tx * 4 + v];
 #pragma unroll
-      for (int u = 0; u < 4; ++u)
+      for (int u = 0; u < 8; ++u)
 #pragma unroll
         for (int v = 0; v < 4; ++v) acc[u][v] = fmaf(av[u], bv[v], acc[u][v]);
     }
     __syncthreads();
     if (((m0 + 32) & 127) == 0 || m0 + 32 >= M) {
 #pragma unroll
-      for (int u = 0; u < 4; ++u)
+      for (int u = 0; u < 8; ++u)
 #pragma unroll
         for (int v = 0; v < 4; ++v) { dacc[u][v] += (double)acc[u][v]; acc[u][v] = 0.0f; }
     }
   }
 #pragma unroll
-  for (int u = 0; u < 4; ++u) {
-    const int s = s0 + ty * 4 + u;
+  for (int u = 0; u < 8; ++u) {
+    const int s = s0 + ty * 8 + u;
     if (s >= S) continue;
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
@@ -567,56 +573,57 @@ __global__ void mllr_prior_kernel(int M, int D, const float* __restrict__ umu, c
   }
 }
 
-// w_i = G_i^-1 k_i per (speaker, row): the pivot-free Gauss-Jordan inverse of MATRIX::_Invert_Gen
-// (Matrix4_LMa.cpp:2232-2300) in FP64, as mllr_row_kernel. One block per (row i, speaker s).
+// w_i = G_i^-1 k_i per (speaker, row), in FP64: Gaussian elimination without pivoting on the
+// augmented system [G_i | k_i] and back substitution -- the same elimination order as the
+// reference's pivot-free Gauss-Jordan inverse (MATRIX::_Invert_Gen, Matrix4_LMa.cpp:2232-2300)
+// followed by the product with k, without forming the inverse (a third of the work). One warp per
+// (row i, speaker s), lanes over the rows below the pivot; four systems per block.
+constexpr int kSolveWarps = 4;
 __global__ void mllr_solve_kernel(int S, int D, const double* __restrict__ Gd, const double* __restrict__ kd,
                                   const double* __restrict__ Gp, const double* __restrict__ kp,
                                   const int* __restrict__ status, double* __restrict__ W) {
   extern __shared__ double sm[];
-  const int E = D + 1, T = E * (E + 1) / 2;
-  const int i = blockIdx.x, s = blockIdx.y;
-  double* G = sm;
-  double* kv = sm + E * E;
+  const int E = D + 1, T = E * (E + 1) / 2, LD = E + 2;  // row stride: E columns + k + pad
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long sys = (long long)blockIdx.x * kSolveWarps + warp;
+  if (sys >= (long long)S * D) return;
+  const int s = (int)(sys / D), i = (int)(sys - (long long)s * D);
+  double* A = sm + (size_t)warp * E * LD;
   double* Wr = W + ((size_t)s * D + i) * E;
   if (status[s] != GMM_OK) {
-    for (int a = threadIdx.x; a < E; a += blockDim.x) Wr[a] = 0.0;
+    for (int a = lane; a < E; a += 32) Wr[a] = 0.0;
     return;
   }
-  for (int e = threadIdx.x; e < E * E; e += blockDim.x) {
+  for (int e = lane; e < E * E; e += 32) {
     const int a = e / E, b = e - a * E;
     const int ti = a <= b ? tri_index(a, b, E) : tri_index(b, a, E);
     double g = Gd[((size_t)s * D + i) * T + ti];
     if (Gp) g = __dadd_rn(Gp[(size_t)i * T + ti], g);
-    G[e] = g;
+    A[a * LD + b] = g;
   }
-  for (int a = threadIdx.x; a < E; a += blockDim.x) {
+  for (int a = lane; a < E; a += 32) {
     double k = kd[((size_t)s * D + i) * E + a];
     if (kp) k = __dadd_rn(kp[(size_t)i * E + a], k);
-    kv[a] = k;
+    A[a * LD + E] = k;
   }
-  __syncthreads();
+  __syncwarp();
   for (int k = 0; k < E; ++k) {
-    const double piv = G[k * E + k];
-    for (int e = threadIdx.x; e < E * E; e += blockDim.x) {
-      const int a = e / E, b = e - a * E;
-      if (a != k && b != k) G[e] = __dsub_rn(G[e], __ddiv_rn(__dmul_rn(G[k * E + b], G[a * E + k]), piv));
+    const double ipiv = __ddiv_rn(1.0, A[k * LD + k]);
+    for (int r = k + 1 + lane; r < E; r += 32) {
+      const double f = __dmul_rn(A[r * LD + k], ipiv);
+      for (int c = k + 1; c <= E; ++c) A[r * LD + c] = __dsub_rn(A[r * LD + c], __dmul_rn(f, A[k * LD + c]));
     }
-    __syncthreads();
-    for (int e = threadIdx.x; e < E; e += blockDim.x) {
-      if (e != k) {
-        G[k * E + e] = __ddiv_rn(-G[k * E + e], piv);
-        G[e * E + k] = __ddiv_rn(G[e * E + k], piv);
-      }
+    __syncwarp();
+  }
+  if (lane == 0) {
+    for (int r = E - 1; r >= 0; --r) {
+      double v = A[r * LD + E];
+      for (int c = r + 1; c < E; ++c) v = __dsub_rn(v, __dmul_rn(A[r * LD + c], A[c * LD + E]));
+      A[r * LD + E] = __ddiv_rn(v, A[r * LD + r]);
     }
-    __syncthreads();
-    if (threadIdx.x == 0) G[k * E + k] = __ddiv_rn(1.0, piv);
-    __syncthreads();
   }
-  for (int a = threadIdx.x; a < E; a += blockDim.x) {
-    double v = 0.0;
-    for (int b = 0; b < E; ++b) v = __dadd_rn(v, __dmul_rn(G[a * E + b], kv[b]));
-    Wr[a] = v;
-  }
+  __syncwarp();
+  for (int a = lane; a < E; a += 32) Wr[a] = A[a * LD + E];
 }
 
 // AdaptModelMLLR (OL_ModelAdapt.cpp:1597-1608) for every (speaker, component): mu' = A mu + b.
@@ -795,7 +802,7 @@ int mstep_mllr_batch(Ctx* c, int S, const double* plain, const SpeakerStats* ss,
   if (!rc) rc = dalloc(c, (void**)&Xi, bXi, "MLLR extended means");
   if (!rc && ubm_init) rc = dalloc(c, (void**)&Gp, bGp, "MLLR prior G");
   if (!rc && ubm_init) rc = dalloc(c, (void**)&kp, bkp, "MLLR prior k");
-  const size_t smem = sizeof(double) * ((size_t)E * E + E);
+  const size_t smem = sizeof(double) * (size_t)kSolveWarps * E * (E + 2);
   if (!rc && smem > 200 * 1024) rc = fail(c, GMM_ERR_UNSUPPORTED, "MLLR: D too large for the shared-memory solve");
   if (!rc) {
     const long long tot = (long long)S * M;
@@ -820,13 +827,13 @@ int mstep_mllr_batch(Ctx* c, int S, const double* plain, const SpeakerStats* ss,
     {
       // G data term: coef = n[s][m]
       GMM_LAUNCH(c, "mllr_gemm_kernel");
-      dim3 grid((T + 63) / 64, (S + 63) / 64, D);
+      dim3 grid((T + 63) / 64, (S + 127) / 128, D);
       mllr_gemm_kernel<<<grid, 256, 0, c->stream>>>(S, M, D, T, n, (long long)M, 1, 0, uvar, B, T, Gd);
     }
     {
       // k data term: coef = F[s][m][i]
       GMM_LAUNCH(c, "mllr_gemm_kernel");
-      dim3 grid((E + 63) / 64, (S + 63) / 64, D);
+      dim3 grid((E + 63) / 64, (S + 127) / 128, D);
       mllr_gemm_kernel<<<grid, 256, 0, c->stream>>>(S, M, D, E, F, (long long)M * D, D, 1, uvar, Xi, E, kd);
     }
     if (ubm_init) {
@@ -836,7 +843,9 @@ int mstep_mllr_batch(Ctx* c, int S, const double* plain, const SpeakerStats* ss,
     cudaFuncSetAttribute(mllr_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     {
       GMM_LAUNCH(c, "mllr_solve_kernel");
-      mllr_solve_kernel<<<dim3(D, S), 128, smem, c->stream>>>(S, D, Gd, kd, Gp, kp, dstatus, dW);
+      const long long nsys = (long long)S * D;
+      mllr_solve_kernel<<<(unsigned)((nsys + kSolveWarps - 1) / kSolveWarps), 32 * kSolveWarps, smem, c->stream>>>(
+          S, D, Gd, kd, Gp, kp, dstatus, dW);
     }
     if (dmu_out) {
       GMM_LAUNCH(c, "mllr_batch_apply_kernel");
