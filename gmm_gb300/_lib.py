@@ -49,6 +49,8 @@ SIGNATURES = {
     "gmm_profile_read": (_i, [_vp, _i, C.POINTER(C.c_char_p), _vp, _vp]),
     "gmm_launch_count": (_ll, [_vp]),
     "gmm_accumulate_noalloc": (_i, [_vp, _ll, _i, _i, _vp, _vp, _vp, _f, _f, _f, _i, _vp, _vp]),
+    "gmm_read_param": (_i, [C.c_char_p, _i, C.c_uint, _vp, _ll, C.POINTER(_ll), C.POINTER(_i)]),
+    "gmm_accumulate_files": (_i, [_vp, _i, _i, C.POINTER(C.c_char_p), _i, C.c_uint, _d, C.POINTER(_i)]),
     "gmm_server_create": (_i, [_i, _i, _i, _i, _sz, C.POINTER(_vp)]),
     "gmm_server_destroy": (_i, [_vp]),
     "gmm_server_last_error": (C.c_char_p, [_vp]),
@@ -61,6 +63,7 @@ SIGNATURES = {
     "gmm_server_stats": (_i, [_vp, C.POINTER(_ll), C.POINTER(_ll), C.POINTER(_ll), C.POINTER(_sz)]),
 }
 
+PRM_SVES, PRM_HTK, PRM_RAW = 0, 1, 2
 REQ_SCORE, REQ_MAP = 0, 1
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
 SUBMIT_FRAME_LL, SUBMIT_NO_COPY = 1, 2
@@ -185,6 +188,15 @@ class Handle:
     def upload_features_device(self, dptr: int, N: int, D: int):
         self.check(self.lib.gmm_upload_features_device(self.h, dptr, N, D))
         self.N, self.D = N, D
+
+    def accumulate_files(self, paths, prm_type, dwnsmp=1, buffer_gb=1.0, flags=ACC_MEAN | ACC_VAR):
+        """File-by-file accumulation; returns the number of files that contributed frames. The
+        statistics stay on the device (read_stats / the M-step entry points)."""
+        arr = (C.c_char_p * max(1, len(paths)))(*[p.encode() for p in paths])
+        used = C.c_int()
+        self.check(self.lib.gmm_accumulate_files(self.h, flags, len(paths), arr, prm_type, dwnsmp,
+                                                 buffer_gb, C.byref(used)))
+        return used.value
 
     # -- E-step
     def accumulate(self, flags=ACC_MEAN | ACC_VAR):
@@ -384,3 +396,18 @@ class Server:
         b, c, f, p = C.c_longlong(), C.c_longlong(), C.c_longlong(), C.c_size_t()
         self.check(self.lib.gmm_server_stats(self.h, C.byref(b), C.byref(c), C.byref(f), C.byref(p)))
         return dict(batches=b.value, completed=c.value, failed=f.value, peak_batch_bytes=p.value)
+
+
+def read_param(path: str, prm_type: int, dwnsmp: int = 1) -> np.ndarray:
+    """One feature file through the library's reader (gmm_read_param)."""
+    lib = load()
+    N, D = C.c_longlong(), C.c_int()
+    rc = lib.gmm_read_param(path.encode(), prm_type, dwnsmp, None, 0, C.byref(N), C.byref(D))
+    if rc:
+        raise GMMError(rc, f"gmm_read_param: cannot read {path}")
+    out = np.zeros((N.value, D.value), np.float32)
+    if out.size:
+        rc = lib.gmm_read_param(path.encode(), prm_type, dwnsmp, ptr(out), N.value, C.byref(N), C.byref(D))
+        if rc:
+            raise GMMError(rc, f"gmm_read_param: cannot read {path}")
+    return out

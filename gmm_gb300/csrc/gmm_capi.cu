@@ -7,8 +7,14 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <cstring>
 #include <new>
 #include <string>
+
+#include <atomic>
+#include <condition_variable>
+#include <mutex>
+#include <thread>
 
 #include "gmm_internal.cuh"
 
@@ -590,6 +596,174 @@ int gmm_mllr_batch(gmm_handle h, int S, const long long* offs, int ubm_init, dou
   dfree(c, doffs, boffs);
   dfree(c, dmu, bmu);
   return rc;
+}
+
+// File-by-file accumulation (accumulateStatsMT(CFileList&, ...), OL_GMMStatsEstimator.cpp:641-698):
+// a loader thread fills two page-locked batch buffers in turn while the device accumulates the
+// other one.
+int gmm_accumulate_files(gmm_handle h, int flags, int n_files, const char* const* paths, int prm_type,
+                         unsigned int dwnsmp, double buffer_gb, int* files_used) {
+  if (!h) return GMM_ERR_ARG;
+  Ctx* c = h;
+  if (n_files < 0 || (n_files > 0 && !paths)) return fail(c, GMM_ERR_ARG, "gmm_accumulate_files: bad file list");
+  if (prm_type < GMM_PRM_SVES || prm_type > GMM_PRM_RAW)
+    return fail(c, GMM_ERR_ARG, "accumulateStatsMT(): Unknown input data type specified");
+  if (!c->w) return fail(c, GMM_ERR_STATE, "no model uploaded");
+  cudaSetDevice(c->device);
+  free_features(c);
+  cudaMemsetAsync(c->stats, 0, sizeof(double) * ((size_t)c->M * (1 + 2 * c->D) + 2), c->stream);
+  c->stats_valid = false;
+
+  struct Slot {
+    float* h = nullptr;
+    size_t cap = 0;  // floats
+    long long n = 0;
+    int D = 0, files = 0;
+  } slot[2];
+  std::mutex mu;
+  std::condition_variable cv;
+  int produced = 0, consumed = 0;
+  bool done = false, abort_load = false;
+  int lrc = GMM_OK;
+  std::string lerr;
+  const double limit = buffer_gb * 1024.0 * 1024.0 * 1024.0;
+  const int Dm = c->D;
+
+  std::thread loader([&] {
+    cudaSetDevice(c->device);
+    Slot* b = nullptr;
+    auto acquire = [&]() -> bool {
+      std::unique_lock<std::mutex> lk(mu);
+      cv.wait(lk, [&] { return abort_load || produced - consumed < 2; });
+      if (abort_load) return false;
+      b = &slot[produced % 2];
+      b->n = 0;
+      b->D = 0;
+      b->files = 0;
+      return true;
+    };
+    auto publish = [&] {
+      std::lock_guard<std::mutex> lk(mu);
+      ++produced;
+      cv.notify_all();
+    };
+    int rc = GMM_OK;
+    std::string err;
+    if (acquire()) {
+      for (int f = 0; f < n_files && rc == GMM_OK; ++f) {
+        long long N = 0;
+        int D = 0;
+        const int hr = param_header(paths[f], prm_type, dwnsmp, &N, &D, &err);
+        if (hr < 0 || (hr == GMM_OK && N == 0)) continue;  // missing or empty: skipped
+        if (hr) { rc = hr; break; }
+        if (D != Dm) {
+          rc = GMM_ERR_ARG;
+          err = std::string("Inconsistent model & feature vector - different dimensions (") + paths[f] + ")";
+          break;
+        }
+        const size_t need = (size_t)(b->n + N) * D;
+        if (need > b->cap) {
+          float* nb = nullptr;
+          const size_t cap = need + need / 2;
+          if (cudaMallocHost((void**)&nb, cap * sizeof(float)) != cudaSuccess) {
+            rc = GMM_ERR_NOMEM;
+            err = "gmm_accumulate_files: page-locked batch buffer";
+            break;
+          }
+          if (b->n) std::memcpy(nb, b->h, (size_t)b->n * D * sizeof(float));
+          if (b->h) cudaFreeHost(b->h);
+          b->h = nb;
+          b->cap = cap;
+        }
+        const int r = param_read(paths[f], prm_type, dwnsmp, b->h + (size_t)b->n * D, &err);
+        if (r < 0) continue;
+        if (r) { rc = r; break; }
+        b->n += N;
+        b->D = D;
+        ++b->files;
+        if ((double)b->n * D * sizeof(float) >= limit) {
+          publish();
+          if (!acquire()) break;
+        }
+      }
+      if (rc == GMM_OK && b && b->n > 0) publish();
+    }
+    std::lock_guard<std::mutex> lk(mu);
+    if (rc) {
+      lrc = rc;
+      lerr = err;
+    }
+    done = true;
+    cv.notify_all();
+  });
+
+  float* dX[2] = {nullptr, nullptr};
+  size_t dcap[2] = {0, 0};
+  int rc = GMM_OK, used = 0;
+  long long total = 0;
+  for (int k = 0; rc == GMM_OK; ++k) {
+    Slot* b;
+    {
+      std::unique_lock<std::mutex> lk(mu);
+      cv.wait(lk, [&] { return produced > consumed || done; });
+      if (produced == consumed) break;
+      b = &slot[consumed % 2];
+    }
+    const int d = k % 2;
+    const size_t bytes = (size_t)b->n * b->D * sizeof(float);
+    if (bytes > dcap[d]) {
+      dfree(c, dX[d], dcap[d]);
+      dX[d] = nullptr;
+      dcap[d] = 0;
+      rc = dalloc(c, (void**)&dX[d], bytes, "feature batch");
+      if (rc) break;
+      dcap[d] = bytes;
+    }
+    if ((size_t)(b->n + 256) * sizeof(float) > c->ll_cap) {
+      dfree(c, c->ll, c->ll_cap);
+      c->ll = nullptr;
+      c->ll_cap = 0;
+      dfree(c, c->llpart, c->llpart_cap * sizeof(double));
+      c->llpart = nullptr;
+      c->llpart_cap = 0;
+      rc = alloc_frame_buffers(c, b->n);
+      if (rc) break;
+    }
+    cudaMemcpyAsync(dX[d], b->h, bytes, cudaMemcpyHostToDevice, c->stream);
+    c->X = dX[d];
+    c->N = b->n;
+    c->Dx = b->D;
+    c->tcx_valid = false;
+    rc = estep(c, flags, true, nullptr);  // adds into the statistics
+    if (!rc) rc = sync(c, "gmm_accumulate_files");
+    total += b->n;
+    used += b->files;
+    std::lock_guard<std::mutex> lk(mu);
+    ++consumed;
+    cv.notify_all();
+  }
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    abort_load = true;
+    cv.notify_all();
+  }
+  loader.join();
+  cudaStreamSynchronize(c->stream);
+  for (int d = 0; d < 2; ++d) {
+    dfree(c, dX[d], dcap[d]);
+    if (slot[d].h) cudaFreeHost(slot[d].h);
+  }
+  // the batches were transient: no resident features remain
+  c->X = nullptr;
+  c->N = 0;
+  c->tcx_valid = false;
+  if (rc == GMM_OK && lrc) rc = fail(c, lrc, lerr);
+  if (rc) return rc;
+  c->tot_frames = total;
+  c->acc_flags = flags;
+  c->stats_valid = true;
+  if (files_used) *files_used = used;
+  return GMM_OK;
 }
 
 int gmm_em_iterate(gmm_handle h, int iters, int upW, int upM, int upV, double* ll, int* alive) {

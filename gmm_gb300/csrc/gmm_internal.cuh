@@ -180,6 +180,11 @@ int plain_speaker_stats(Ctx* c, int S, const long long* offs, int flags, double*
 int mstep_mllr_batch(Ctx* c, int S, const double* plain, const SpeakerStats* ss, int ubm_init, double* dW,
                      int* dstatus, float* dmu_out, double* dll);
 
+// Feature files (SVES / HTK / RAW): header (frames after down-sampling, dimension) and frames.
+// Both return -1 for a file that cannot be opened, GMM_ERR_ARG with *err for a bad file.
+int param_header(const char* path, int type, unsigned dwnsmp, long long* N, int* D, std::string* err);
+int param_read(const char* path, int type, unsigned dwnsmp, float* out, std::string* err);
+
 // One tensor-core E-step over a batch of requests that may use different resident models (all
 // with the same D and chunk count): feature planes for the batch's padded row layout, the
 // logits / log-sum-exp kernel over every row (W chunks from the tile's model), and the

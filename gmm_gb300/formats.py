@@ -133,13 +133,22 @@ def write_gmm_bin(path: str, g: GMModel) -> None:
             f.write(np.asarray(g.var[m], "<f4").tobytes())
 
 
-def read_raw(path: str) -> np.ndarray:
+def _downsample(X: np.ndarray, dwnsmp: int) -> np.ndarray:
+    """Param's down-sampling: frames 0, d, 2d, ... (N / d + (N % d > 0) frames)."""
+    return X[::dwnsmp].copy() if dwnsmp > 1 else X
+
+
+def read_raw(path: str, dwnsmp: int = 1) -> np.ndarray:
+    """RAW_PRM_IN (Param::LoadRaw, param/OL_Param.cpp:345-450): int32 frames, int32 dim, floats;
+    frames < 1 means the rest of the file."""
     with open(path, "rb") as f:
         buf = f.read()
     N, D = struct.unpack_from("<ii", buf, 0)
+    if D > 0 and N < 1:
+        N = (len(buf) - 8) // D // 4
     if N < 0 or D <= 0 or 8 + 4 * N * D > len(buf):
         raise ValueError(f"truncated or malformed RAW feature file (N={N}, D={D})")
-    return np.frombuffer(buf, "<f4", N * D, 8).reshape(N, D).copy()
+    return _downsample(np.frombuffer(buf, "<f4", N * D, 8).reshape(N, D).copy(), dwnsmp)
 
 
 def write_raw(path: str, X: np.ndarray) -> None:
@@ -147,6 +156,51 @@ def write_raw(path: str, X: np.ndarray) -> None:
     with open(path, "wb") as f:
         f.write(struct.pack("<ii", X.shape[0], X.shape[1]))
         f.write(X.tobytes())
+
+
+def write_sves(path: str, X: np.ndarray, cf: np.ndarray | None = None) -> None:
+    """SVES_PRM_IN (Param::Save / Param::Load, param/OL_Param.cpp:245-340): "SV-ES-PARAM",
+    int32 dim, int32 frames, float CF[frames], float frames[frames][dim]."""
+    X = np.ascontiguousarray(X, "<f4")
+    N, D = X.shape
+    cf = np.ones(N, "<f4") if cf is None else np.ascontiguousarray(cf, "<f4")
+    with open(path, "wb") as f:
+        f.write(b"SV-ES-PARAM")
+        f.write(struct.pack("<ii", D, N))
+        f.write(cf.tobytes())
+        f.write(X.tobytes())
+
+
+def read_sves(path: str, dwnsmp: int = 1) -> np.ndarray:
+    with open(path, "rb") as f:
+        buf = f.read()
+    if buf[:11] != b"SV-ES-PARAM":
+        raise ValueError(f"{path}: format different from SV-ES-PARAM")
+    D, N = struct.unpack_from("<ii", buf, 11)
+    if N <= 0 or D <= 0:
+        return np.zeros((0, 0), np.float32)
+    off = 19 + 4 * N
+    return _downsample(np.frombuffer(buf, "<f4", N * D, off).reshape(N, D).copy(), dwnsmp)
+
+
+def write_htk(path: str, X: np.ndarray, sample_period: int = 100000, parm_kind: int = 9) -> None:
+    """HTK_PRM_IN (Param::LoadHTK, param/OL_Param.cpp:474-560): big-endian int32 frames, int32
+    sample period, int16 bytes per frame, int16 parameter kind, big-endian float frames."""
+    X = np.ascontiguousarray(X, ">f4")
+    N, D = X.shape
+    with open(path, "wb") as f:
+        f.write(struct.pack(">iihh", N, sample_period, 4 * D, parm_kind))
+        f.write(X.tobytes())
+
+
+def read_htk(path: str, dwnsmp: int = 1) -> np.ndarray:
+    with open(path, "rb") as f:
+        buf = f.read()
+    N, _, nb, _ = struct.unpack_from(">iihh", buf, 0)
+    D = nb // 4
+    if N <= 0 or D <= 0:
+        return np.zeros((0, 0), np.float32)
+    return _downsample(np.frombuffer(buf, ">f4", N * D, 12).reshape(N, D).astype(np.float32), dwnsmp)
 
 
 def write_loglikes_txt(path: str, ll: np.ndarray) -> None:

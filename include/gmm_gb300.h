@@ -173,6 +173,27 @@ int gmm_profile_read(gmm_handle h, int cap, const char** names, double* ms, long
 /* Number of kernel launches this handle issued since creation (all kernels). */
 long long gmm_launch_count(gmm_handle h);
 
+/* ------------------------------------------------------------------ feature files
+ * The reference's parameter-file formats (Param::Load / LoadHTK / LoadRaw, param/OL_Param.cpp:224-580):
+ * GMM_PRM_SVES "SV-ES-PARAM" files, GMM_PRM_HTK big-endian HTK files, GMM_PRM_RAW
+ * (int32 frames, int32 dim, floats). dwnsmp > 1 keeps every dwnsmp-th frame. */
+#define GMM_PRM_SVES 0
+#define GMM_PRM_HTK 1
+#define GMM_PRM_RAW 2
+/* Reads one file: with out = NULL only *N (frames after down-sampling) and *D are returned;
+ * otherwise up to cap_frames frames [N][D] go to out. GMM_ERR_ARG for a missing or bad file. */
+int gmm_read_param(const char* path, int prm_type, unsigned int dwnsmp, float* out, long long cap_frames,
+                   long long* N, int* D);
+/* File-by-file accumulation: accumulateStatsMT(CFileList&, ...) (OL_GMMStatsEstimator.cpp:641-698).
+ * Files are read on a loader thread into page-locked buffers and appended until the buffered
+ * frames reach buffer_gb GiB (the reference's _memoryBuffDataGB), then each batch is copied to the
+ * device and accumulated while the loader reads the next one. Statistics are zeroed first and
+ * summed over all batches on the device (read them with gmm_read_stats; the M-step entry points
+ * use them). Missing or empty files are skipped, as the reference does; *files_used counts the
+ * files that contributed frames. The batches are transient: afterwards no features are resident. */
+int gmm_accumulate_files(gmm_handle h, int flags, int n_files, const char* const* paths, int prm_type,
+                         unsigned int dwnsmp, double buffer_gb, int* files_used);
+
 /* ------------------------------------------------------------------ request server
  * Continuous-batching server for scoring and MAP-adaptation requests against resident GMMs. It
  * replaces the reference's one-request-at-a-time tools: getLogLike's per-file scoring

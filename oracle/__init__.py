@@ -264,3 +264,21 @@ def ref_mllr(X, w, mu, var, iters=1, ubm_init=False, threads=1, sse=False):
     if rc:
         raise RuntimeError(ref().ref_last_error().decode())
     return W, omu
+
+
+def ref_param_load(path, prm_type, dwnsmp=1):
+    """The reference's Param::Load on one feature file (None when the file is missing)."""
+    N, D = C.c_longlong(), C.c_int()
+    f = ref().ref_param_load
+    f.argtypes = [C.c_char_p, C.c_int, C.c_uint, C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong),
+                  C.POINTER(C.c_int)]
+    rc = f(path.encode(), prm_type, dwnsmp, None, 0, C.byref(N), C.byref(D))
+    if rc == -1:
+        return None
+    if rc:
+        raise RuntimeError(f"reference Param::Load failed ({rc})")
+    out = np.zeros((N.value, D.value), np.float32)
+    rc = f(path.encode(), prm_type, dwnsmp, _p(out) if out.size else None, N.value, C.byref(N), C.byref(D))
+    if rc:
+        raise RuntimeError(f"reference Param::Load failed ({rc})")
+    return out

@@ -259,4 +259,29 @@ int ref_mllr(const float* X, long N, int D, int M, const float* w, const float* 
   catch (Exception* ex) { g_err = ex->m_strDescription; delete ex; return 2; }
 }
 
+// Param::Load (param/OL_Param.cpp:224-243 -> Load / LoadHTK / LoadRaw): one feature file.
+// out = NULL: only *N and *D. Returns the loader's status (-1: file not found), -2 on exception.
+int ref_param_load(const char* path, int type, unsigned int dwnsmp, float* out, long long cap,
+                   long long* N, int* D) {
+  try {
+    Param p;
+    int rc = p.Load(path, type, dwnsmp);
+    if (rc) return rc;
+    *N = p.GetNumberOfVectors();
+    *D = (int)p.GetVectorDim();
+    if (out && *N > 0) {
+      if (*N > cap) return -3;
+      float** v = *p.GetVectors();
+      for (long long i = 0; i < *N; ++i) memcpy(out + (size_t)i * *D, v[i], sizeof(float) * *D);
+    }
+    return 0;
+  } catch (std::exception& e) {
+    g_err = e.what();
+    return -2;
+  } catch (Exception* e) {
+    g_err = "reference exception";
+    return -2;
+  }
+}
+
 }  // extern "C"
