@@ -228,6 +228,7 @@ class Handle:
     def em_update(self, upW=True, upM=True, upV=True):
         a = C.c_int()
         self.check(self.lib.gmm_em_update(self.h, int(upW), int(upM), int(upV), C.byref(a)))
+        self.last_alive = a.value
         return a.value
 
     def map_update(self, tau, upW=False, upM=True, upV=False):

@@ -32,8 +32,53 @@ class Options:
     mllrUBMInit: bool = False
     applyTransforms: bool = False
     min_var: float = 1e-6
+    splitXpercAtOnce: float = 0.0   # --split-X
+    splitTh: float = 0.0            # --split-th
+    llTh: float = 0.0               # --ll-Th
     verbosity: int = 0
     precision: int = _lib.PREC_FP32
+
+
+_RESET_VAR = np.frombuffer(np.array([0x01010101], np.uint32).tobytes(), np.float32)[0]
+
+
+def _empty_model(M: int, D: int) -> GMModel:
+    """``GMModel(dim, nummix)``: zero weights, components in GMMMixture::Reset state (mean 0,
+    variance bytes 0x01 from memset; OL_GMModel.cpp:45-83, 120-165)."""
+    return GMModel(np.zeros(M, np.float32), np.zeros((M, D), np.float32), np.full((M, D), _RESET_VAR, np.float32))
+
+
+def _gauss_stats(model: GMModel, get_list: bool):
+    """``CModelAdapt::GetGaussStats`` (OL_ModelAdapt.cpp:951-990): index of the largest weight
+    (the highest index among equal maxima), zero-weight indices from the top down, and the
+    non-zero indices sorted by decreasing weight in the reference's insertion order."""
+    i_max, wm = 0, np.float32(0.0)
+    zero, srt = [], []
+    for m in range(model.M - 1, -1, -1):
+        w = model.w[m]
+        if wm < w:
+            wm, i_max = w, m
+        if w == 0:
+            zero.append(m)
+            continue
+        if get_list:
+            k = 0
+            while k < len(srt) and model.w[srt[k]] > w:
+                k += 1
+            srt.insert(k, m)
+    return i_max, zero, srt
+
+
+def _split_gaussian(model: GMModel, m2: int, mnew: int) -> None:
+    """``CModelAdapt::splitGaussian`` (OL_ModelAdapt.cpp:612-665), diagonal covariances: the new
+    component takes the variance, both take half the weight, means move by +-sqrt(var)/2."""
+    model.var[mnew] = model.var[m2]
+    w = np.float32(model.w[m2] / np.float32(2.0))
+    model.w[mnew] = w
+    model.w[m2] = w
+    shift = (np.sqrt(model.var[m2].astype(np.float64)) * 0.5).astype(np.float32)
+    model.mu[mnew] = model.mu[m2] + shift
+    model.mu[m2] = model.mu[m2] - shift
 
 
 def _compose(W_sum: np.ndarray, W_new: np.ndarray) -> np.ndarray:
@@ -141,6 +186,94 @@ class ModelAdapt:
             Wt = self.ComputeW_MLLR(sp, ubm)
             W = _compose(W, Wt)
         return W
+
+    def _em_step(self, model: GMModel, update: bool):
+        """One AccumulateStats + UpdateModelEM of TrainFromScratch: insertModel rearranges the
+        model in place, then the device accumulates and (if asked) updates it."""
+        self._upload(model)
+        self.dev.accumulate_device(_lib.ACC_MEAN | _lib.ACC_VAR)
+        st = self.dev.read_stats()
+        alive = None
+        if update:
+            alive = self.dev.em_update(True, True, True)
+            model.w, model.mu, model.var = self.dev.read_model()
+        return st, alive
+
+    def splitMultipleGaussians(self, model: GMModel) -> None:
+        """``CModelAdapt::splitMultipleGaussians`` (OL_ModelAdapt.cpp:590-610)."""
+        o = self.opt
+        i_max, zero, srt = _gauss_stats(model, o.splitXpercAtOnce > 0.0)
+        n_split = int(np.ceil(np.float32(o.splitXpercAtOnce) * np.float32(model.M - len(zero))))
+        if n_split < 2:
+            _split_gaussian(model, i_max, zero[0])
+            return
+        th = np.float32(o.splitTh) * model.w[i_max]
+        for n, (m, z) in enumerate(zip(srt, zero + [None] * max(0, len(srt) - len(zero)))):
+            if model.w[m] < th or z is None or n >= n_split:
+                break
+            _split_gaussian(model, m, z)
+
+    def TrainFromScratch(self, nummix: int, init: GMModel | None = None) -> GMModel:
+        """``CModelAdapt::TrainFromScratch`` (OL_ModelAdapt.cpp:667-821), diagonal covariances:
+        a global Gaussian, then EM iterations on the device alternating with splits of the
+        heaviest Gaussians into free slots until nummix components (or a stop rule)."""
+        o = self.opt
+        self._ensure_features()
+        if self._X.shape[0] <= 3:
+            raise RuntimeError("TrainFromScratch(): Not enough data to model training.")
+        D = self._X.shape[1]
+        if init is None:
+            # global statistics: one component, every posterior 1
+            g = GMModel(np.ones(1, np.float32), np.zeros((1, D), np.float32), np.ones((1, D), np.float32))
+            _, alive = self._em_step(g, True)
+            if alive == 0:
+                raise RuntimeError("trainFromScratch(): amount of data too low to estimate a model, or data are "
+                                   "constant!")
+            init = g
+            max_iter = nummix
+        else:
+            if nummix <= init.M:
+                raise RuntimeError("trainFromScratch(): init model already contains specified number of Gaussians!")
+            max_iter = nummix - init.M
+        model = _empty_model(nummix, D)
+        model.w[:init.M], model.mu[:init.M], model.var[:init.M] = init.w, init.mu, init.var
+        if nummix < 2:
+            max_iter = 0
+        iters_em = 2 if (o.iterCountEM < 2 and o.llTh > 0.0) else o.iterCountEM
+        lowest = -np.finfo(np.float32).max
+        ll = [lowest, lowest, lowest]
+        m2 = m3 = None
+        non_zero = init.M
+        for it in range(max_iter):
+            for _ in range(iters_em):
+                st, _ = self._em_step(model, False)
+                if o.verbosity:  # the reference only computes the average LL when verbose
+                    ll[0] = np.float32(st["totLL"] / st["totN"])
+                if non_zero > 1:
+                    self.dev.em_update(True, True, True)
+                    model.w, model.mu, model.var = self.dev.read_model()
+                    non_zero = self.dev.last_alive
+                if non_zero < 2:
+                    if non_zero < 1:
+                        model = init.copy()
+                    break
+            if non_zero == 0 or non_zero == nummix:
+                break
+            if o.llTh > 0.0:
+                mx = max(ll[1], ll[2])
+                if it > 2 and ll[0] - mx < o.llTh:
+                    if mx > ll[0]:
+                        model = (m2 if mx == ll[1] else m3).copy()
+                    break
+                m3 = m2.copy() if m2 is not None else _empty_model(0, D)
+                m2 = model.copy()
+                ll[2], ll[1] = ll[1], ll[0]
+            if it < max_iter - 1:
+                self.splitMultipleGaussians(model)
+                non_zero += 1
+        model.rearrange()
+        self._model = model
+        return model
 
     def AdaptModelMLLR(self, model: GMModel, W: np.ndarray) -> GMModel:
         """``CModelAdapt::AdaptModelMLLR`` (OL_ModelAdapt.cpp:1583-1612)."""

@@ -282,3 +282,17 @@ def ref_param_load(path, prm_type, dwnsmp=1):
     if rc:
         raise RuntimeError(f"reference Param::Load failed ({rc})")
     return out
+
+
+def ref_train(X, nummix, iters_em=5, split_x=0.0, split_th=0.0, ll_th=0.0, verbosity=0, threads=1):
+    """The reference's TrainFromScratch on X (diagonal covariances); returns (w, mu, var)."""
+    X = _f32(X)
+    N, D = X.shape
+    w, mu, var = np.zeros(nummix, np.float32), np.zeros((nummix, D), np.float32), np.zeros((nummix, D), np.float32)
+    f = ref().ref_train
+    f.argtypes = [C.c_void_p, C.c_long, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_int,
+                  C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+    rc = f(_p(X), N, D, nummix, iters_em, split_x, split_th, ll_th, verbosity, threads, _p(w), _p(mu), _p(var))
+    if rc:
+        raise RuntimeError(f"reference TrainFromScratch failed: {ref().ref_last_error().decode()}")
+    return w, mu, var

@@ -259,6 +259,40 @@ int ref_mllr(const float* X, long N, int D, int M, const float* w, const float* 
   catch (Exception* ex) { g_err = ex->m_strDescription; delete ex; return 2; }
 }
 
+// Train from scratch: CModelAdapt::TrainFromScratch (OL_ModelAdapt.cpp:667-821) with the
+// splitting of splitMultipleGaussians / splitGaussian (:590-665). Outputs the final model in
+// its final (rearranged) component order.
+int ref_train(const float* X, long N, int D, int nummix, int iters_em, float split_x, float split_th,
+              float ll_th, int verbosity, int threads, float* w, float* mu, float* var) {
+  try {
+    CModelAdapt cm;
+    CModelAdapt::OPTIONS opt = base_options(threads, 0);
+    opt._adaptType = FROM_SCRATCH;
+    opt._iterCountEM = iters_em;
+    opt._splitXpercAtOnce = split_x;
+    opt._splitTh = split_th;
+    opt._llTh = ll_th;
+    opt._verbosity = verbosity;
+    cm.SetOptions(opt);
+    Param p;
+    fill_param(p, X, N, D);
+    cm.InsertData(p, false);
+    std::streambuf* old = std::cout.rdbuf();
+    std::ostringstream sink;
+    std::cout.rdbuf(sink.rdbuf());  // the reference reports progress on stdout when verbose
+    try {
+      cm.TrainFromScratch((unsigned)nummix, false, NULL, "ref_train", false);
+    } catch (...) {
+      std::cout.rdbuf(old);
+      throw;
+    }
+    std::cout.rdbuf(old);
+    read_model(cm._modelSP, nummix, D, w, mu, var);
+    return 0;
+  } catch (std::exception& ex) { g_err = ex.what(); return 1; }
+  catch (Exception* ex) { g_err = ex->m_strDescription; delete ex; return 2; }
+}
+
 // Param::Load (param/OL_Param.cpp:224-243 -> Load / LoadHTK / LoadRaw): one feature file.
 // out = NULL: only *N and *D. Returns the loader's status (-1: file not found), -2 on exception.
 int ref_param_load(const char* path, int type, unsigned int dwnsmp, float* out, long long cap,

@@ -106,6 +106,23 @@ def main():
         if fn.endswith(".npz"):
             print(fn, os.path.getsize(os.path.join(HERE, fn)))
 
+    train_fixture()
+
+
+def train_fixture():
+    """TrainFromScratch (OL_ModelAdapt.cpp:667-821) by the reference build on seeded data."""
+    gw, gmu, gvar = synth.generator_gmm(31, 6, 5)
+    X = synth.sample_gmm(32, gw, gmu, gvar, 3000)
+    out = {"X": X}
+    cases = {"one": dict(nummix=6, iters_em=3),
+             "multi": dict(nummix=8, iters_em=3, split_x=0.5, split_th=0.2),
+             "llth_quiet": dict(nummix=8, iters_em=2, ll_th=0.01, verbosity=0),
+             "llth_verbose": dict(nummix=8, iters_em=2, ll_th=0.01, verbosity=1)}
+    for name, kw in cases.items():
+        w, mu, var = O.ref_train(X, **kw)
+        out.update({f"{name}_w": w, f"{name}_mu": mu, f"{name}_var": var})
+    np.savez_compressed(os.path.join(HERE, "train.npz"), **out)
+
 
 if __name__ == "__main__":
     main()
