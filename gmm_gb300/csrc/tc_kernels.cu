@@ -15,10 +15,12 @@
 // (K x 256 bytes). A tile reaches shared memory in one cp.async.bulk.tensor.2d copy per plane over a
 // [rows][128 elements] view (256-byte rows); 64-row half tiles take one 1 KB copy per column chunk.
 //
-// Two kernels per E-step. Each has one TMA-producer warp, one MMA-issuer thread and eight
-// epilogue warps (two per TMEM lane quadrant); the MMAs take their A operand from TMEM
-// (tcgen05.mma ... [a_tmem], b_desc), so only B is read from shared memory and the TMA ring keeps
-// shared-memory bandwidth to itself.
+// Two kernels per E-step. Each has one TMA-producer warp, two MMA-issuing threads in warps on
+// different SM sub-partitions and eight epilogue warps (two per TMEM lane quadrant); the MMAs
+// take their A operand from TMEM (tcgen05.mma ... [a_tmem], b_desc), so only B is read from
+// shared memory and the TMA ring keeps shared-memory bandwidth to itself. The tensor pipe accepts
+// only a few MMAs ahead, and an issuing warp shares its sub-partition with busy epilogue warps:
+// two issuers and fully unrolled issue loops (descriptor = per-stage base + constant) keep it fed.
 //   ll_kernel  (frame-tile major, persistent): four loader warps copy the 128-frame Z tile into
 //              TMEM (double-buffered where it fits); 128-component W chunks stream through a
 //              3-stage TMA ring; S[128 frames x 128 comps] accumulates in one of two TMEM
@@ -59,7 +61,7 @@ namespace {
 constexpr double kLog2e = 1.4426950408889634;
 constexpr float kLn2 = 0.69314718055994531f;
 constexpr long long kWaitLimit = 4000000000LL;  // clock cycles (~2 s)
-constexpr int kThreads = 320;                    // warp 0 TMA, warp 1 MMA, warps 2-9 epilogue
+constexpr int kThreads = 352;  // warp 0 TMA, warp 1 logits MMA, warps 2-9 epilogue, warp 10 statistics MMA
 
 // ------------------------------------------------------------------ operand preparation
 
@@ -201,8 +203,18 @@ __device__ __forceinline__ void named_sync(int id, int nthreads) {
 }
 
 // Plane products (Z plane, W plane) with i + j <= 4 (1-based), small terms first.
-__device__ __constant__ int kProdZ[6] = {2, 1, 0, 1, 0, 0};
-__device__ __constant__ int kProdW[6] = {0, 1, 2, 0, 1, 0};
+// (Z plane, W plane) of product pr: (2,0) (1,1) (0,2) (1,0) (0,1) (0,0).
+__host__ __device__ constexpr int prod_z(int pr) { return pr == 0 ? 2 : (pr == 1 || pr == 3) ? 1 : 0; }
+__host__ __device__ constexpr int prod_w(int pr) { return pr == 2 ? 2 : (pr == 1 || pr == 4) ? 1 : 0; }
+
+// The MMA issuer shares its SM sub-partition with busy epilogue warps and the tensor pipe
+// accepts only a few MMAs ahead, so every cycle between two tcgen05.mma instructions can leave
+// the pipe idle. The issue loops below are fully unrolled: each descriptor is a per-stage base
+// plus a compile-time offset (the 14-bit address field of a shared-memory descriptor counts
+// 16-byte units, and no operand crosses 256 KB), and the accumulate flags are constants.
+__device__ __forceinline__ uint64_t desc_add(uint64_t base, uint32_t byte_offset) {
+  return base + (uint64_t)(byte_offset >> 4);
+}
 
 // Copies row `r` of one 128-row tile image (all three planes) from HBM into TMEM, laid out as
 // a tcgen05 A operand: lane = row, each 32-bit column holds two consecutive bf16 of K. Plane p
@@ -249,7 +261,7 @@ struct LlCfg {
   static constexpr int SMEM = cmax(OFF_MISC + 64 + 1024, 120 * 1024);
   static_assert(Z_COL + ZB * ZCOLS <= 512, "TMEM budget");
 };
-constexpr int kLlThreads = 448;  // warp 0 TMA, 1 MMA, 2-9 epilogue, 10-13 Z loaders
+constexpr int kLlThreads = 480;  // warp 0 TMA, 1 and 14 MMA, 2-9 epilogue, 10-13 Z loaders
 
 template <int K>
 __global__ void __launch_bounds__(kLlThreads, 1)
@@ -269,7 +281,7 @@ __global__ void __launch_bounds__(kLlThreads, 1)
   uint64_t* w_empty = bars + 7;  // [NW]
   uint64_t* s_full = bars + 10;  // [2]
   uint64_t* s_empty = bars + 12; // [2]
-  uint64_t* mma_done = bars + 14;
+  uint64_t* mma_done = bars + 14;  // [2]: one per MMA-issuing thread
   uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(smem + C::OFF_MISC);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + C::OFF_MISC + 8);
   float* red_m = reinterpret_cast<float*>(smem + C::OFF_RED);
@@ -277,10 +289,14 @@ __global__ void __launch_bounds__(kLlThreads, 1)
   volatile int* stop_s = reinterpret_cast<volatile int*>(red_m + 256);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // with an even chunk count two threads issue the MMAs, even chunks (buffer 0) and odd chunks
+  // (buffer 1), from different SM sub-partitions: each competes with busy epilogue warps for
+  // issue slots, and the tensor pipe accepts only a few MMAs ahead
+  const bool two_issuers = (n_chunks % 2) == 0;
   if (threadIdx.x == 0) {
     for (int i = 0; i < ZB; ++i) {
       mbar_init(&z_full[i], 4);
-      mbar_init(&z_empty[i], 1);
+      mbar_init(&z_empty[i], two_issuers ? 2 : 1);
     }
     for (int i = 0; i < NW; ++i) {
       mbar_init(&w_full[i], 1);
@@ -290,7 +306,8 @@ __global__ void __launch_bounds__(kLlThreads, 1)
       mbar_init(&s_full[i], 1);
       mbar_init(&s_empty[i], 8);
     }
-    mbar_init(mma_done, 1);
+    mbar_init(&mma_done[0], 1);
+    mbar_init(&mma_done[1], 1);
     *abort_flag = 0;
     fence_mbar_init();
   }
@@ -326,8 +343,9 @@ __global__ void __launch_bounds__(kLlThreads, 1)
         for (int k = max(0, last - NW); k < last; ++k) mbar_drain(&w_full[k % NW], (k / NW) & 1);
       }
     }
-  } else if (warp == 1) {
-    if (lane == 0 && my_tiles > 0) {
+  } else if (warp == 1 || warp == 14) {
+    const int role = warp == 14;  // parity of the chunks this thread issues
+    if (lane == 0 && my_tiles > 0 && (two_issuers || role == 0)) {
       const uint32_t idesc = idesc_bf16(128, 128, false, false);
       const uint32_t wb0 = smem_u32(smem + C::OFF_W);
       int j = 0;
@@ -337,31 +355,30 @@ __global__ void __launch_bounds__(kLlThreads, 1)
         if (!mbar_wait(&z_full[zb], (it / ZB) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
         const uint32_t za = tmem + C::Z_COL + zb * C::ZCOLS;
         for (int ch = 0; ch < n_chunks; ++ch, ++j) {
+          if (two_issuers && (ch & 1) != role) continue;
           const int ws = j % NW, b = j & 1;
           if (!mbar_wait(&w_full[ws], (j / NW) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
           if (!mbar_wait(&s_empty[b], ((j >> 1) & 1) ^ 1, abort_flag, kWaitLimit)) { ok = false; break; }
           tc_fence_after();
-          const uint32_t wb = wb0 + ws * C::W_STAGE;
+          const uint64_t wd = smem_desc(wb0 + ws * C::W_STAGE, 128 * 16, 128);
           const uint32_t d = tmem + C::S_COL + b * 128;
-          int acc = 0;
-#pragma unroll 1
+#pragma unroll
           for (int pr = 0; pr < 6; ++pr) {
-            const uint32_t a_pl = za + kProdZ[pr] * (K / 2);
-            const uint32_t w_pl = wb + kProdW[pr] * C::W_PLANE;
 #pragma unroll
             for (int q = 0; q < K / 16; ++q) {
-              const uint64_t bd = smem_desc(w_pl + q * 2 * 128 * 16, 128 * 16, 128);
-              mma_ts(d, a_pl + q * 8, bd, idesc, acc);
-              acc = 1;
+              const uint64_t bd = desc_add(wd, prod_w(pr) * C::W_PLANE + q * 2 * 128 * 16);
+              const uint32_t a = za + prod_z(pr) * (K / 2) + q * 8;
+              if (pr == 0 && q == 0) mma_ts_c<false>(d, a, bd, idesc);
+              else mma_ts_c<true>(d, a, bd, idesc);
             }
           }
           mma_commit(&s_full[b]);
           mma_commit(&w_empty[ws]);
-          if (ch == n_chunks - 1) mma_commit(&z_empty[zb]);
+          if (ch >= n_chunks - (two_issuers ? 2 : 1)) mma_commit(&z_empty[zb]);  // each issuer's last chunk
         }
       }
-      mma_commit(mma_done);
-      mbar_drain(mma_done, 0);
+      mma_commit(&mma_done[role]);
+      mbar_drain(&mma_done[role], 0);
     }
   } else if (warp >= 10) {
     // Z loaders: thread = frame row of the tile; fill the next TMEM Z buffer from HBM
@@ -502,7 +519,7 @@ struct AccCfg {
   static constexpr int OFF_Z = 0;
   static constexpr int OFF_LL = OFF_Z + NZ * Z_STAGE;
   static constexpr int OFF_BAR = OFF_LL + NZ * LL_STAGE;
-  static constexpr int OFF_MISC = OFF_BAR + 16 * 8;
+  static constexpr int OFF_MISC = OFF_BAR + 24 * 8;
   static constexpr int SMEM = cmax(OFF_MISC + 64 + 1024, 120 * 1024);
   static constexpr int FLUSH = 64 * 128 / FT;   // tiles per FP64 flush (8192 frames)
   static_assert(D_COL + K <= 512, "TMEM budget");
@@ -524,10 +541,11 @@ __global__ void __launch_bounds__(kThreads, 1)
   uint64_t* z_full = bars + 1;   // [NZ <= 4]
   uint64_t* z_empty = bars + 5;  // [NZ]
   uint64_t* s_full = bars + 9;   // [2]
-  uint64_t* g_full = bars + 11;  // [2]
-  uint64_t* d_full = bars + 13;
-  uint64_t* d_empty = bars + 14;
-  uint64_t* mma_done = bars + 15;
+  uint64_t* g_full = bars + 11;  // [2 buffers][2 frame halves]
+  uint64_t* d_full = bars + 15;
+  uint64_t* d_empty = bars + 16;
+  uint64_t* mma_done = bars + 17;   // [2]: one per MMA-issuing thread
+  uint64_t* s_free = bars + 19;     // [2]: the statistics MMAs are done with a posterior buffer
   uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(smem + C::OFF_MISC);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + C::OFF_MISC + 8);
   float* ll_s = reinterpret_cast<float*>(smem + C::OFF_LL);
@@ -561,11 +579,15 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     for (int i = 0; i < 2; ++i) {
       mbar_init(&s_full[i], 1);
-      mbar_init(&g_full[i], 8);
+      mbar_init(&g_full[2 * i], 8);
+      mbar_init(&g_full[2 * i + 1], 8);
     }
     mbar_init(d_full, 1);
     mbar_init(d_empty, 8);
-    mbar_init(mma_done, 1);
+    mbar_init(&mma_done[0], 1);
+    mbar_init(&mma_done[1], 1);
+    mbar_init(&s_free[0], 1);
+    mbar_init(&s_free[1], 1);
     *abort_flag = 0;
     fence_mbar_init();
   }
@@ -598,72 +620,84 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (*abort_flag)  // drain the copies still in flight
         for (int i = max(0, issued - NZ); i < issued; ++i) mbar_drain(&z_full[i % NZ], (i / NZ) & 1);
     }
-  } else if (warp == 1) {
+  } else if (warp == 1 || warp == 10) {
+    // Two MMA-issuing threads on different SM sub-partitions: the logits (warp 1) and the
+    // statistics (warp 10). Each shares its sub-partition with two busy epilogue warps; split
+    // this way each needs half the issue slots. A posterior buffer is reused by the logits of
+    // tile i + 2 only after the statistics of tile i released it (s_free).
     if (lane == 0 && nt > 0) {
-      const uint32_t idesc_l = idesc_bf16(128, FT, false, false);
-      const uint32_t idesc_s = idesc_bf16(128, K, false, true);
       const uint32_t zb0 = smem_u32(smem + C::OFF_Z);
-      const uint32_t wa = tmem + C::W_COL;
-      bool ok = mbar_wait(w_full, 0, abort_flag, kWaitLimit);
-      auto logits = [&](int i) {
-        const uint32_t zb = zb0 + (i % NZ) * C::Z_STAGE;
-        const uint32_t d = tmem + C::S_COL + (i & 1) * FT;
-        int acc = 0;
-#pragma unroll 1
-        for (int pr = 0; pr < 6; ++pr) {
-          const uint32_t a_pl = wa + kProdW[pr] * (K / 2);
-          const uint32_t z_pl = zb + kProdZ[pr] * C::Z_PLANE;
+      bool ok = true;
+      if (warp == 1) {
+        const uint32_t idesc_l = idesc_bf16(128, FT, false, false);
+        const uint32_t wa = tmem + C::W_COL;
+        ok = mbar_wait(w_full, 0, abort_flag, kWaitLimit);
+        for (int i = 0; i < nt && ok; ++i) {
+          if (!mbar_wait(&z_full[i % NZ], (i / NZ) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
+          if (i >= 2 && !mbar_wait(&s_free[i & 1], ((i - 2) >> 1) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
+          tc_fence_after();
+          const uint64_t zd = smem_desc(zb0 + (i % NZ) * C::Z_STAGE, FT * 16, 128);
+          const uint32_t d = tmem + C::S_COL + (i & 1) * FT;
 #pragma unroll
-          for (int q = 0; q < K / 16; ++q) {
-            const uint64_t bd = smem_desc(z_pl + q * 2 * FT * 16, FT * 16, 128);
-            mma_ts(d, a_pl + q * 8, bd, idesc_l, acc);
-            acc = 1;
+          for (int pr = 0; pr < 6; ++pr) {
+#pragma unroll
+            for (int q = 0; q < K / 16; ++q) {
+              const uint64_t bd = desc_add(zd, prod_z(pr) * C::Z_PLANE + q * 2 * FT * 16);
+              const uint32_t a = wa + prod_w(pr) * (K / 2) + q * 8;
+              if (pr == 0 && q == 0) mma_ts_c<false>(d, a, bd, idesc_l);
+              else mma_ts_c<true>(d, a, bd, idesc_l);
+            }
           }
+          mma_commit(&s_full[i & 1]);
         }
-        mma_commit(&s_full[i & 1]);
-      };
-      auto stats = [&](int j) -> bool {
-        const int b = j & 1;
-        if (!mbar_wait(&g_full[b], (j >> 1) & 1, abort_flag, kWaitLimit)) return false;
-        tc_fence_after();
-        // D2 holds one tile: wait until the epilogue has read out tile j - 1
-        if (j > 0 && !mbar_wait(d_empty, (j - 1) & 1, abort_flag, kWaitLimit)) return false;
-        tc_fence_after();
+        mma_commit(&mma_done[0]);
+        mbar_drain(&mma_done[0], 0);
+      } else {
+        const uint32_t idesc_s = idesc_bf16(128, K, false, true);
         const uint32_t dcol = tmem + C::D_COL;
-        const uint32_t gb = tmem + C::S_COL + b * FT;
-        const uint32_t zb = zb0 + (j % NZ) * C::Z_STAGE;
-        int acc = 0;
-#pragma unroll
-        for (int q = 0; q < FT / 16; ++q) {
-          const uint32_t hi = gb + 32 * (q >> 1) + 8 * (q & 1);
-          const uint32_t lo = hi + 16;
+        for (int j = 0; j < nt && ok; ++j) {
+          const int b = j & 1;
+          // the tile's operands are in its stage; D2 holds one tile: wait until the epilogue
+          // has read out tile j - 1
+          if (!mbar_wait(&z_full[j % NZ], (j / NZ) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
+          if (j > 0 && !mbar_wait(d_empty, (j - 1) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
+          const uint32_t gb = tmem + C::S_COL + b * FT;
           // B = Z as [N = K columns] x [K' = frames], MN-major: LBO along frames, SBO along columns
-          const uint64_t z1 = smem_desc(zb + 0 * C::Z_PLANE + q * 2 * 128, 128, FT * 16);
-          const uint64_t z2 = smem_desc(zb + 1 * C::Z_PLANE + q * 2 * 128, 128, FT * 16);
-          const uint64_t z3 = smem_desc(zb + 2 * C::Z_PLANE + q * 2 * 128, 128, FT * 16);
-          // gamma (hi + lo) x Z (z1 + z2 + z3): the five products above 2^-18, smallest first
-          mma_ts(dcol, lo, z2, idesc_s, acc);
-          acc = 1;
-          mma_ts(dcol, hi, z3, idesc_s, 1);
-          mma_ts(dcol, lo, z1, idesc_s, 1);
-          mma_ts(dcol, hi, z2, idesc_s, 1);
-          mma_ts(dcol, hi, z1, idesc_s, 1);
+          const uint64_t zd = smem_desc(zb0 + (j % NZ) * C::Z_STAGE, 128, FT * 16);
+#pragma unroll
+          for (int q = 0; q < FT / 16; ++q) {
+            // the posteriors of each half of the tile's frames are signalled separately, so the
+            // statistics of the first half run while the epilogue converts the second
+            if (q % (FT / 32) == 0) {
+              if (!mbar_wait(&g_full[2 * b + q / (FT / 32)], (j >> 1) & 1, abort_flag, kWaitLimit)) {
+                ok = false;
+                break;
+              }
+              tc_fence_after();
+            }
+            const uint32_t hi = gb + 32 * (q >> 1) + 8 * (q & 1);
+            const uint32_t lo = hi + 16;
+            const uint64_t z1 = desc_add(zd, 0 * C::Z_PLANE + q * 2 * 128);
+            const uint64_t z2 = desc_add(zd, 1 * C::Z_PLANE + q * 2 * 128);
+            const uint64_t z3 = desc_add(zd, 2 * C::Z_PLANE + q * 2 * 128);
+            // gamma (hi + lo) x Z (z1 + z2 + z3): the five products above 2^-18, smallest first
+            if (q == 0) mma_ts_c<false>(dcol, lo, z2, idesc_s);
+            else mma_ts_c<true>(dcol, lo, z2, idesc_s);
+            mma_ts_c<true>(dcol, hi, z3, idesc_s);
+            mma_ts_c<true>(dcol, lo, z1, idesc_s);
+            mma_ts_c<true>(dcol, hi, z2, idesc_s);
+            mma_ts_c<true>(dcol, hi, z1, idesc_s);
+          }
+          if (!ok) break;
+          mma_commit(&z_empty[j % NZ]);
+          mma_commit(d_full);
+          mma_commit(&s_free[b]);
         }
-        mma_commit(&z_empty[j % NZ]);
-        mma_commit(d_full);
-        return true;
-      };
-      for (int i = 0; i < nt && ok; ++i) {
-        if (!mbar_wait(&z_full[i % NZ], (i / NZ) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
-        tc_fence_after();
-        logits(i);
-        if (i > 0 && !stats(i - 1)) { ok = false; break; }
+        mma_commit(&mma_done[1]);
+        mbar_drain(&mma_done[1], 0);
       }
-      if (ok) stats(nt - 1);
-      mma_commit(mma_done);
-      mbar_drain(mma_done, 0);
     }
-  } else if (nt > 0) {
+  } else if (warp < 10 && nt > 0) {
     // epilogue: thread = component row; the two warps of a lane quadrant split the work
     const int q4 = warp & 3;
     const int hf = (warp - 2) >> 2;
@@ -744,9 +778,11 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (!mbar_wait(&s_full[b], (i >> 1) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
       tc_fence_after();
       const float* lls = ll_s + (i % NZ) * FT;
+      // pass cc converts 32-frame chunk 2 cc + hf: the two warps of a quadrant finish the first
+      // half of the tile's frames together and signal it before the second half
 #pragma unroll 1
       for (int cc = 0; cc < NCH; ++cc) {
-        const int c = hf * NCH + cc;
+        const int c = 2 * cc + hf;
         const uint32_t col = tmem + lane_off + C::S_COL + b * FT + 32 * c;
         uint32_t v[32];
         tmem_ld32(col, v);
@@ -782,11 +818,22 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         tmem_st16(col, hi);
         tmem_st16(col + 16, lo);
+        if (NCH == 2) {
+          tmem_st_wait();
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&g_full[2 * b + cc]);
+        }
       }
-      tmem_st_wait();
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&g_full[b]);
+      if (NCH == 1) {  // 64-frame tiles: one pass covers both halves
+        tmem_st_wait();
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) {
+          mbar_arrive(&g_full[2 * b]);
+          mbar_arrive(&g_full[2 * b + 1]);
+        }
+      }
       if (i > 0 && !readout(i - 1, end_prev, slot_prev)) { ok = false; break; }
     }
     if (ok && !*abort_flag) readout(nt - 1, true, per.slot_of(nt - 1));

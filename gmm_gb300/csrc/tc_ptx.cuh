@@ -132,6 +132,17 @@ __device__ __forceinline__ void mma_ts(uint32_t d, uint32_t a, uint64_t b, uint3
       : "memory");
 }
 
+// The same with a compile-time accumulate flag (no predicate arithmetic in the issue stream).
+template <bool ACC>
+__device__ __forceinline__ void mma_ts_c(uint32_t d, uint32_t a, uint64_t b, uint32_t idesc) {
+  if (ACC)
+    asm volatile("tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, 1;" ::"r"(d), "r"(a), "l"(b), "r"(idesc)
+                 : "memory");
+  else
+    asm volatile("tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, 0;" ::"r"(d), "r"(a), "l"(b), "r"(idesc)
+                 : "memory");
+}
+
 // mbarrier arrives once all tcgen05 operations issued so far by this thread completed
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
