@@ -679,8 +679,13 @@ def main():
     flop_fc = wl.flop_per_fc(name)
     achieved = flop_fc * (wl.fc / launches_per_step) / (per_launch_ms / 1e3) / 1e12 if kcnt else 0.0
     peak = bf16s if bf16s else bf16
+    # DRAM bytes per launch of the dominant kernel from an ncu capture of a smaller case of the
+    # same workload, scaled by the frames a launch processes (the operand planes are read once)
+    traffic = None
+    if args.workload == "ubm-em" and name == "tc_acc_kernel" and args.dim == 39 and args.mix == 2048:
+        traffic = 503.2 * wl.N  # 503.2 MB per 1M frames: profiles/acc_kernel_ubm_em_1Mx2048x39.md
     roofline = {"bound": "tensor", "kernel": name, "achieved": achieved, "peak": peak,
-                "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
                 "algorithmic_flop_per_fc": flop_fc,
                 "peak_source": f"{peak_kind} (bf16 sustained, MEASURED_PEAKS.json)",
                 "kernel_ms_per_launch": per_launch_ms,
