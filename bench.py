@@ -414,8 +414,10 @@ def run_serve(args):
     ids = [srv.add_model(*m) for m in models]
     rates = [float(x) for x in args.rates.split(",")]
     sweep = []
-    clk_all = []
-    launches = 0
+    # one clock sampler for the whole sweep, started ahead: starting nvidia-smi stalls the
+    # process for a while, which would show up as latency of the first requests
+    clk = ClockSampler(gpu).__enter__()
+    time.sleep(1.0)
     for ri, rate in enumerate(rates):
         t_arr, kinds, mods, utt = serve_trace(args, rate, args.duration, pinned, len(ids), args.seed + 100 + ri)
         tickets = [None] * len(t_arr)
@@ -437,27 +439,26 @@ def run_serve(args):
 
         th = threading.Thread(target=collect)
         th.start()
-        with ClockSampler(gpu) as clk:
-            t0 = time.perf_counter()
-            for i in range(len(t_arr)):
-                now = time.perf_counter() - t0
-                if t_arr[i] > now:
-                    time.sleep(t_arr[i] - now)
-                k = int(kinds[i])
-                X = pinned[k][utt[i]]
-                tickets[i] = srv.submit(k, ids[int(mods[i])], X, upM=1, no_copy=True)
-                lag[i] = (time.perf_counter() - t0) - t_arr[i]
-                q.put((i, tickets[i]))
-            q.put(None)
-            th.join()
-            t_end = time.perf_counter() - t0
-        clk_all.append(clk.summary())
+        t0 = time.perf_counter()
+        for i in range(len(t_arr)):
+            now = time.perf_counter() - t0
+            if t_arr[i] > now:
+                time.sleep(t_arr[i] - now)
+            k = int(kinds[i])
+            X = pinned[k][utt[i]]
+            tickets[i] = srv.submit(k, ids[int(mods[i])], X, upM=1, no_copy=True)
+            lag[i] = (time.perf_counter() - t0) - t_arr[i]
+            q.put((i, tickets[i]))
+        q.put(None)
+        th.join()
+        t_end = time.perf_counter() - t0
         lat = np.array([x["latency_ms"] for x in res]) + 1e3 * lag
         frames = sum(len(pinned[int(k)][u]) for k, u in zip(kinds, utt))
         sweep.append({"rate": rate, "requests": len(t_arr), "achieved_rps": len(t_arr) / t_end,
                       "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
                       "max_ms": float(lat.max()), "batches": srv.stats()["batches"] - b0,
                       "fc_per_s": frames * args.mix / t_end})
+    clk.__exit__(None, None, None)
     st = srv.stats()
     srv.close()
     # one request at a time through the one-model entry points, plain FP32 kernels (and the
@@ -506,7 +507,7 @@ def run_serve(args):
         "sweep": sweep, "p50_ms": best["p50_ms"] if best else None, "p99_ms": best["p99_ms"] if best else None,
         "serial_plain_rps": serial_plain, "serial_tc_rps": serial_tc,
         "speedup_vs_serial_plain": value / serial_plain if serial_plain else None,
-        "clocks": clk_all[-1] if clk_all else None,
+        "clocks": clk.summary(),
         "e2e": {"value": value, "unit": "req/s", "h2d_bytes_per_step": None, "d2h_bytes_per_step": None,
                 "note": "the served path is end to end: host frames in, results on the host"},
         "server": st, "gpu_launches": None,

@@ -267,6 +267,8 @@ int gmm_destroy(gmm_handle h) {
   dfree(c, c->tcpart, c->tcpart_cap);
   dfree(c, c->tcm.planes, 0);
   dfree(c, c->tcm.comp_of_row, 0);
+  if (c->em_graph) cudaGraphExecDestroy(c->em_graph);
+  dfree(c, c->ll_hist, 0);
   dfree(c, c->tcm.ll2, 0);
   dfree(c, c->tcx.planes, 0);
   dfree(c, c->tc_err, 0);
@@ -766,11 +768,121 @@ int gmm_accumulate_files(gmm_handle h, int flags, int n_files, const char* const
   return GMM_OK;
 }
 
+// One EM iteration of gmm_em_iterate as device work only (no host readback), in the order of
+// the eager loop below: rearrange, precompute, statistics, LL record, backup, update, restore.
+static int em_iteration_device(Ctx* c, int flags, int upW, int upM, int upV) {
+  int rc = mstep_rearrange(c);
+  if (!rc) rc = plain_precompute_async(c);
+  if (!rc) {
+    cudaError_t e = cudaMemsetAsync(c->stats, 0, sizeof(double) * ((size_t)c->M * (1 + 2 * c->D) + 2), c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaMemsetAsync(stats)");
+    rc = tc_estep(c, flags, true, nullptr);
+  }
+  if (rc) return rc;
+  c->tot_frames = c->N;
+  c->acc_flags = flags;
+  c->stats_valid = true;
+  rc = record_iteration_ll(c);
+  const size_t md = sizeof(float) * (size_t)c->M * c->D, m1 = sizeof(float) * (size_t)c->M;
+  cudaMemcpyAsync(c->bw, c->w, m1, cudaMemcpyDeviceToDevice, c->stream);
+  cudaMemcpyAsync(c->bmu, c->mu, md, cudaMemcpyDeviceToDevice, c->stream);
+  cudaMemcpyAsync(c->bvar, c->var, md, cudaMemcpyDeviceToDevice, c->stream);
+  if (!rc) rc = mstep_em(c, upW, upM, upV, nullptr);
+  if (!rc) rc = mstep_em_restore(c);
+  return rc;
+}
+
+// gmm_em_iterate on the tensor-core path: the first iteration runs eagerly (it allocates what
+// the kernels need), the others replay a CUDA graph of one iteration captured from the stream.
+// Shapes are fixed at all M components, so components that die stay as padding rows.
+static int em_iterate_graph(Ctx* c, int iters, int upW, int upM, int upV, double* ll, int* alive) {
+  const int flags = (upM ? GMM_ACC_MEAN : 0) | (upV ? GMM_ACC_VAR : 0) |
+                    ((upW && !upM && !upV) ? GMM_ACC_PROBS_ONLY : 0);
+  // the model as given is checked once, as insertModel does (later models come from the update,
+  // which floors variances at min_var)
+  int rc = plain_precompute(c);
+  if (rc) return rc;
+  if (!c->tcx_valid || c->tcx.planes == nullptr) {
+    c->static_shapes = false;
+    rc = tc_estep(c, flags, false, nullptr);  // builds the feature planes
+    if (rc) return rc;
+  }
+  if (iters > c->ll_hist_cap) {
+    dfree(c, c->ll_hist, sizeof(double) * (c->ll_hist_cap + 1));
+    c->ll_hist = nullptr;
+    c->ll_hist_cap = 0;
+    rc = dalloc(c, (void**)&c->ll_hist, sizeof(double) * (iters + 1), "EM log-likelihood history");
+    if (rc) return rc;
+    c->ll_hist_cap = iters;
+  }
+  cudaMemsetAsync(c->ll_hist, 0, sizeof(double) * (c->ll_hist_cap + 1), c->stream);
+  const bool prof = c->profile;
+  c->static_shapes = true;
+  rc = em_iteration_device(c, flags, upW, upM, upV);
+  if (!rc) rc = sync(c, "EM iteration");
+  // the graph holds these buffers by address: any change means a new capture
+  const long long key[] = {c->M, c->D, c->N, flags | upW << 4 | upM << 5 | upV << 6,
+                           (long long)(size_t)c->X, (long long)(size_t)c->w, (long long)(size_t)c->mu,
+                           (long long)(size_t)c->var, (long long)(size_t)c->stats, (long long)(size_t)c->act,
+                           (long long)(size_t)c->flag, (long long)(size_t)c->icov, (long long)(size_t)c->logG,
+                           (long long)(size_t)c->logW, (long long)(size_t)c->bw, (long long)(size_t)c->bmu,
+                           (long long)(size_t)c->bvar, (long long)(size_t)c->tcm.planes,
+                           (long long)(size_t)c->tcm.comp_of_row, (long long)(size_t)c->tcm.ll2,
+                           (long long)(size_t)c->tcx.planes, (long long)(size_t)c->tcpart,
+                           (long long)(size_t)c->tc_llpart, (long long)(size_t)c->tc_err,
+                           (long long)(size_t)c->ll_hist, (long long)c->ll_hist_cap,
+                           (long long)c->tcpart_cap, (long long)c->tc_llpart_cap};
+  static_assert(sizeof(key) == sizeof(c->em_graph_key), "graph key size");
+  if (!rc && iters > 1 && (c->em_graph == nullptr || std::memcmp(key, c->em_graph_key, sizeof(key)) != 0)) {
+    if (c->em_graph) cudaGraphExecDestroy(c->em_graph);
+    c->em_graph = nullptr;
+    c->profile = false;  // no timing events inside the graph
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed);
+    if (e == cudaSuccess) {
+      rc = em_iteration_device(c, flags, upW, upM, upV);
+      e = cudaStreamEndCapture(c->stream, &g);
+      if (!rc && e == cudaSuccess) e = cudaGraphInstantiate(&c->em_graph, g, 0);
+      if (g) cudaGraphDestroy(g);
+    }
+    c->profile = prof;
+    if (!rc && e != cudaSuccess) rc = cuda_fail(c, e, "EM iteration graph");
+    if (!rc) std::memcpy(c->em_graph_key, key, sizeof(key));
+  }
+  for (int it = 1; it < iters && !rc; ++it) {
+    cudaError_t e = cudaGraphLaunch(c->em_graph, c->stream);
+    if (e != cudaSuccess) rc = cuda_fail(c, e, "cudaGraphLaunch");
+    c->launches += 1;
+  }
+  c->static_shapes = false;
+  c->model_dirty = true;
+  int herr = 0;
+  if (!rc) {
+    if (ll) cudaMemcpyAsync(ll, c->ll_hist, sizeof(double) * iters, cudaMemcpyDeviceToHost, c->stream);
+    cudaMemcpyAsync(c->hflag, c->flag, 8 * sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+    cudaMemcpyAsync(&herr, c->tc_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+    rc = sync(c, "gmm_em_iterate");
+  }
+  if (!rc && herr) {
+    cudaMemsetAsync(c->tc_err, 0, sizeof(int), c->stream);
+    rc = fail(c, GMM_ERR_TIMEOUT, "tensor-core E-step: a bounded device wait expired");
+  }
+  if (!rc && alive) *alive = c->hflag[2];
+  return rc;
+}
+
 int gmm_em_iterate(gmm_handle h, int iters, int upW, int upM, int upV, double* ll, int* alive) {
   if (!h) return GMM_ERR_ARG;
   Ctx* c = h;
   if (iters < 0) return fail(c, GMM_ERR_ARG, "iters must be >= 0");
   cudaSetDevice(c->device);
+  if (c->precision == GMM_PREC_TC && iters > 0) {
+    if (!c->w) return fail(c, GMM_ERR_STATE, "no model uploaded");
+    if (!c->X || c->N == 0) return fail(c, GMM_ERR_STATE, "no features uploaded");
+    if (c->Dx != c->D) return fail(c, GMM_ERR_ARG, "Inconsistent model & feature vector - different dimensions");
+    if (!tc_supported(c->D)) return fail(c, GMM_ERR_UNSUPPORTED, "tensor-core path supports 1 <= D <= 63");
+    return em_iterate_graph(c, iters, upW, upM, upV, ll, alive);
+  }
   const int flags = (upM ? GMM_ACC_MEAN : 0) | (upV ? GMM_ACC_VAR : 0) |
                     ((upW && !upM && !upV) ? GMM_ACC_PROBS_ONLY : 0);
   const size_t md = sizeof(float) * (size_t)c->M * c->D, m1 = sizeof(float) * (size_t)c->M;

@@ -103,6 +103,13 @@ struct Ctx {
   double* tc_llpart = nullptr;                    // per-thread log-likelihood partials
   size_t tc_llpart_cap = 0;
   int sms = 0;
+  // EM iterations replayed from a CUDA graph: shapes fixed at all M components (padded rows for
+  // the dead ones), the active count read on the device, no host readbacks inside an iteration
+  bool static_shapes = false;
+  cudaGraphExec_t em_graph = nullptr;
+  long long em_graph_key[28] = {};
+  double* ll_hist = nullptr;  // [ll_hist_cap + 1]: per-iteration total LL, then a counter
+  int ll_hist_cap = 0;
 
   // timing
   bool profile = false;
@@ -128,11 +135,15 @@ struct LaunchScope {
 
 // ------------------------------------------------------------------ plain FP32 path
 int plain_precompute(Ctx* c);
+int plain_precompute_async(Ctx* c);  // the same launches without the host readback
 int plain_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev);
 
 // ------------------------------------------------------------------ M-step
 int mstep_em(Ctx* c, int upW, int upM, int upV, int* alive);
 int mstep_map(Ctx* c, int tau, int upW, int upM, int upV);
+// device-side steps of a captured EM iteration
+int mstep_em_restore(Ctx* c);           // restore the backup model if no component survived
+int record_iteration_ll(Ctx* c);        // append the statistics' total LL to c->ll_hist
 int mstep_rearrange(Ctx* c);
 int mstep_mllr(Ctx* c, int ubm_init, double* W_host);
 int mstep_mllr_apply(Ctx* c, const double* W_host);

@@ -649,6 +649,28 @@ __global__ void mllr_batch_apply_kernel(int S, int M, int D, const float* __rest
   }
 }
 
+// IterEM keeps a copy of the model and UpdateModelMAP restores it when no component survives
+// (OL_ModelAdapt.cpp:1276-1296): the device-side form for a captured iteration.
+__global__ void em_restore_kernel(int M, int D, const int* __restrict__ flag, float* __restrict__ w,
+                                  float* __restrict__ mu, float* __restrict__ var,
+                                  const float* __restrict__ bw, const float* __restrict__ bmu,
+                                  const float* __restrict__ bvar) {
+  if (flag[2] != 0) return;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < M) w[t] = bw[t];
+  if (t < (long long)M * D) {
+    mu[t] = bmu[t];
+    var[t] = bvar[t];
+  }
+}
+
+// hist[counter] = total LL of the statistics; ++counter (the counter is the last element).
+__global__ void ll_record_kernel(const double* __restrict__ tot, double* __restrict__ hist, int cap) {
+  const int k = (int)hist[cap];
+  if (k < cap) hist[k] = *tot;
+  hist[cap] = (double)(k + 1);
+}
+
 }  // namespace
 
 int mstep_em(Ctx* c, int upW, int upM, int upV, int* alive) {
@@ -862,6 +884,20 @@ int mstep_mllr_batch(Ctx* c, int S, const double* plain, const SpeakerStats* ss,
   dfree(c, Gp, bGp);
   dfree(c, kp, bkp);
   return rc;
+}
+
+int mstep_em_restore(Ctx* c) {
+  GMM_LAUNCH(c, "em_restore_kernel");
+  const long long tot = (long long)c->M * c->D;
+  em_restore_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(c->M, c->D, c->flag, c->w, c->mu,
+                                                                          c->var, c->bw, c->bmu, c->bvar);
+  return GMM_OK;
+}
+
+int record_iteration_ll(Ctx* c) {
+  GMM_LAUNCH(c, "ll_record_kernel");
+  ll_record_kernel<<<1, 1, 0, c->stream>>>(c->stats + (size_t)c->M * (1 + 2 * c->D), c->ll_hist, c->ll_hist_cap);
+  return GMM_OK;
 }
 
 }  // namespace gmm

@@ -314,6 +314,19 @@ void launch_stats(Ctx* c, long long f0, long long nf, long long ldg, int flags, 
 
 }  // namespace
 
+int plain_precompute_async(Ctx* c) {
+  {
+    GMM_LAUNCH(c, "active_list_kernel");
+    active_list_kernel<<<1, 32, 0, c->stream>>>(c->M, c->w, c->act, c->flag + 4);
+  }
+  {
+    GMM_LAUNCH(c, "precompute_kernel");
+    precompute_kernel<<<(c->M + 127) / 128, 128, 0, c->stream>>>(
+        c->M, c->D, c->w, c->var, c->min_var, c->minLL, c->icov, c->logG, c->logW, c->flag);
+  }
+  return GMM_OK;
+}
+
 int plain_precompute(Ctx* c) {
   {
     GMM_LAUNCH(c, "active_list_kernel");

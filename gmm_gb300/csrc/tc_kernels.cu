@@ -134,7 +134,9 @@ __global__ void features_kernel(const float* __restrict__ X, long long N, long l
 __global__ void model_kernel(int D, int K, int Mact, int Mpad, long long plane_rows, long long row0,
                              const int* __restrict__ act, const float* __restrict__ w,
                              const float* __restrict__ mu, const float* __restrict__ var,
-                             uint16_t* __restrict__ planes, int* __restrict__ comp_of_row) {
+                             uint16_t* __restrict__ planes, int* __restrict__ comp_of_row,
+                             const int* __restrict__ mact_dev) {
+  if (mact_dev) Mact = *mact_dev;  // active count produced on the device (captured iterations)
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int KC = K / 8;
   if (t >= (long long)Mpad * K) return;
@@ -530,8 +532,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     acc_kernel(const __grid_constant__ CUtensorMap zmap, const uint16_t* __restrict__ wplanes,
                int nTz, int nTw, const float* __restrict__ ll2, int n_tiles, int n_chunks, int slices,
                const int* __restrict__ tile_slot, const int4* __restrict__ work, float minGamma,
-               int single_comp,
+               int single_comp, const int* __restrict__ mact_dev,
                double* __restrict__ part, int* __restrict__ err) {
+  if (mact_dev) single_comp = *mact_dev == 1;
   using C = AccCfg<K>;
   constexpr int FT = C::FT, NZ = C::NZ, FLUSH = C::FLUSH;
   extern __shared__ uint8_t smem_raw[];
@@ -856,6 +859,7 @@ __global__ void reduce_kernel(int M, int D, int K, int Mact, int n_chunks, int s
   const int rr = (int)(t & 127), e = (int)((t >> 7) % K), ch = (int)(t / (128LL * K));
   const int r = ch * 128 + rr;
   if (r >= Mact || e > 2 * D) return;
+  if (comp_of_row[r] < 0) return;  // padding row
   const int per = (n_tiles + slices - 1) / slices;
   double s = 0.0;
   for (int sl = 0; sl < slices; ++sl) {
@@ -1001,13 +1005,14 @@ int launch_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
     const CUtensorMap& zm = AC::FT == 128 ? c->tm_zfull : c->tm_zhalf;
     acc_kernel<K><<<grid, kThreads, AC::SMEM, c->stream>>>(
         zm, c->tcm.planes, nTz, nTw, c->tcm.ll2, n_tiles, n_chunks, slices, nullptr, nullptr,
-        c->minGamma, c->Mact == 1, c->tcpart, c->tc_err);
+        c->minGamma, c->Mact == 1, c->static_shapes ? c->flag + 4 : nullptr, c->tcpart, c->tc_err);
   }
   {
     GMM_LAUNCH(c, "tc_reduce_kernel");
     long long tot = (long long)n_chunks * K * 128;
     reduce_kernel<<<(int)((tot + 255) / 256), 256, 0, c->stream>>>(
-        c->M, c->D, K, c->Mact, n_chunks, slices, n_tiles, c->tcm.comp_of_row, c->tcpart, flags, c->stats);
+        c->M, c->D, K, c->static_shapes ? c->tcm.Mpad : c->Mact, n_chunks, slices, n_tiles, c->tcm.comp_of_row,
+        c->tcpart, flags, c->stats);
   }
   return GMM_OK;
 }
@@ -1049,7 +1054,8 @@ int tc_prepare_features(Ctx* c) {
 
 int tc_prepare_model(Ctx* c) {
   const int K = tc_K(c->D);
-  const int Mpad = (c->Mact + 127) / 128 * 128;
+  // fixed shapes: every component gets a row (dead ones are padding rows)
+  const int Mpad = ((c->static_shapes ? c->M : c->Mact) + 127) / 128 * 128;
   if (c->tcm.planes == nullptr || c->tcm.Mpad != Mpad || c->tcm.K != K) {
     dfree(c, c->tcm.planes, (size_t)3 * c->tcm.Mpad * c->tcm.K * sizeof(uint16_t));
     dfree(c, c->tcm.comp_of_row, sizeof(int) * (size_t)c->tcm.Mpad);
@@ -1065,7 +1071,8 @@ int tc_prepare_model(Ctx* c) {
     GMM_LAUNCH(c, "tc_model_kernel");
     const long long tot = (long long)Mpad * K;
     model_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(
-        c->D, K, c->Mact, Mpad, Mpad, 0, c->act, c->w, c->mu, c->var, c->tcm.planes, c->tcm.comp_of_row);
+        c->D, K, c->Mact, Mpad, Mpad, 0, c->act, c->w, c->mu, c->var, c->tcm.planes, c->tcm.comp_of_row,
+        c->static_shapes ? c->flag + 4 : nullptr);
   }
   int rc = make_map(c, &c->tm_wfull, c->tcm.planes, 3LL * Mpad * K, K);
   if (!rc) rc = make_map(c, &c->tm_whalf, c->tcm.planes, 3LL * Mpad * K, 4);
@@ -1102,6 +1109,7 @@ int tc_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
     default: return fail(c, GMM_ERR_UNSUPPORTED, "tensor-core path: unsupported K");
   }
   if (rc) return rc;
+  if (c->static_shapes) return GMM_OK;  // checked by the caller after the captured iterations
   // surface a bounded-wait expiry as an error status (the context stays usable)
   int herr = 0;
   cudaMemcpyAsync(&herr, c->tc_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
@@ -1308,7 +1316,7 @@ int tc_build_model(Ctx* c, int D, int K, int Mact, int Mpad, long long plane_row
   GMM_LAUNCH(c, "tc_model_kernel");
   const long long tot = (long long)Mpad * K;
   model_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(D, K, Mact, Mpad, plane_rows, row0, act,
-                                                                     w, mu, var, planes, comp_of_row);
+                                                                     w, mu, var, planes, comp_of_row, nullptr);
   return GMM_OK;
 }
 
@@ -1332,7 +1340,7 @@ void run_batch_k(Ctx* c, const TcBatch& b, const CUtensorMap& zfull, const CUten
     const CUtensorMap& zm = AC::FT == 128 ? zfull : zhalf;
     acc_kernel<K><<<b.n_work, kThreads, AC::SMEM, c->stream>>>(
         zm, b.wplanes, nTz, b.w_chunks_total, b.ll2, (int)(b.Rpad / AC::FT), b.n_chunks, 1, b.tile_slot,
-        b.work, c->minGamma, b.single_comp, b.part, c->tc_err);
+        b.work, c->minGamma, b.single_comp, nullptr, b.part, c->tc_err);
   }
 }
 }  // namespace

@@ -109,3 +109,30 @@ def test_tc_c1_full_size(glib, oracle):
     # the kept posterior mass per frame never exceeds one
     assert s["n"].sum() <= len(X) * (1 + 1e-6)
     h.close()
+
+
+def test_tc_em_iterate_graph_replays_eager_iterations(glib, golden):
+    """gmm_em_iterate on the tensor-core path replays a captured CUDA graph of one iteration
+    after an eager first one: five iterations in one call equal five one-iteration calls
+    bit for bit (same kernels, same fixed shapes), including a component that dies."""
+    from gmm_gb300 import synth
+    X, w, mu, var = synth.config_em(17, 6000, 13, 8, 24)
+    w = w.copy()
+    w[3] = 1e-9  # a component with almost no support, killed by the first update
+    w /= w.sum()
+    h = tc_handle(glib)
+    h.upload_model(w, mu, var)
+    h.upload_features(X)
+    ll5, a5 = h.em_iterate(5)
+    m5 = h.read_model()
+    h.upload_model(w, mu, var)
+    lls = []
+    for _ in range(5):
+        l1, a1 = h.em_iterate(1)
+        lls.append(l1[0])
+    m1 = h.read_model()
+    h.close()
+    assert np.array_equal(ll5, np.array(lls)) and a5 == a1
+    for x, y in zip(m5, m1):
+        assert np.array_equal(x, y)
+    assert a5 < 24  # the weak component died
