@@ -49,6 +49,8 @@ SIGNATURES = {
     "gmm_profile_read": (_i, [_vp, _i, C.POINTER(C.c_char_p), _vp, _vp]),
     "gmm_launch_count": (_ll, [_vp]),
     "gmm_accumulate_noalloc": (_i, [_vp, _ll, _i, _i, _vp, _vp, _vp, _f, _f, _f, _i, _vp, _vp]),
+    "gmm_set_autotune": (_i, [_vp, _i]),
+    "gmm_autotune_choice": (_i, [_vp, C.POINTER(_i), _vp, _vp, _i]),
     "gmm_read_param": (_i, [C.c_char_p, _i, C.c_uint, _vp, _ll, C.POINTER(_ll), C.POINTER(_i)]),
     "gmm_accumulate_files": (_i, [_vp, _i, _i, C.POINTER(C.c_char_p), _i, C.c_uint, _d, C.POINTER(_i)]),
     "gmm_server_create": (_i, [_i, _i, _i, _i, _sz, C.POINTER(_vp)]),
@@ -148,6 +150,17 @@ class Handle:
 
     def set_memory_budget(self, nbytes):
         self.check(self.lib.gmm_set_memory_budget(self.h, nbytes))
+
+    def set_autotune(self, on: bool):
+        self.check(self.lib.gmm_set_autotune(self.h, int(on)))
+
+    def autotune_choices(self) -> dict:
+        n = C.c_int()
+        self.check(self.lib.gmm_autotune_choice(self.h, C.byref(n), None, None, 0))
+        keys = np.zeros(max(1, n.value), np.int64)
+        waves = np.zeros(max(1, n.value), np.int32)
+        self.check(self.lib.gmm_autotune_choice(self.h, C.byref(n), ptr(keys), ptr(waves), n.value))
+        return {int(k): int(w) for k, w in zip(keys[:n.value], waves[:n.value])}
 
     def stream(self) -> int:
         s = C.c_void_p()

@@ -301,6 +301,25 @@ int gmm_set_precision(gmm_handle h, int mode) {
   return GMM_OK;
 }
 
+int gmm_set_autotune(gmm_handle h, int on) {
+  if (!h) return GMM_ERR_ARG;
+  h->autotune = on != 0;
+  if (!on) h->tuned_waves.clear();
+  return GMM_OK;
+}
+
+int gmm_autotune_choice(gmm_handle h, int* n, long long* keys, int* waves, int cap) {
+  if (!h || !n) return GMM_ERR_ARG;
+  int k = 0;
+  for (const auto& kv : h->tuned_waves) {
+    if (k < cap && keys) keys[k] = kv.first;
+    if (k < cap && waves) waves[k] = kv.second;
+    ++k;
+  }
+  *n = k;
+  return GMM_OK;
+}
+
 int gmm_set_memory_budget(gmm_handle h, size_t bytes) {
   if (!h) return GMM_ERR_ARG;
   h->budget = bytes;

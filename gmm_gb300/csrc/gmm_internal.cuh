@@ -6,6 +6,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <map>
 #include <vector>
 
 #include "gmm_gb300.h"
@@ -106,6 +107,9 @@ struct Ctx {
   // EM iterations replayed from a CUDA graph: shapes fixed at all M components (padded rows for
   // the dead ones), the active count read on the device, no host readbacks inside an iteration
   bool static_shapes = false;
+  // autotuner: statistics-kernel decomposition (CTA waves) measured once per shape
+  bool autotune = true;
+  std::map<long long, int> tuned_waves;  // key: K, component chunks, frame tiles (bucket)
   cudaGraphExec_t em_graph = nullptr;
   long long em_graph_key[28] = {};
   double* ll_hist = nullptr;  // [ll_hist_cap + 1]: per-iteration total LL, then a counter

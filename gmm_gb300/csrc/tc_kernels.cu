@@ -983,11 +983,11 @@ int launch_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
                                                 c->stats + (size_t)c->M * (1 + 2 * c->D));
   }
   const int n_tiles = (int)(Npad / AC::FT);
-  int slices = c->sms / n_chunks;
-  if (slices < 1) slices = 1;
-  if (slices > n_tiles) slices = n_tiles;
-  const int grid = n_chunks * slices;
-  size_t pneed = (size_t)grid * 128 * K * sizeof(double);
+  // CTAs = component chunks x frame slices, one CTA per SM at a time: `waves` full waves of the
+  // SMs (more waves = finer slices, which fill the SMs that a single wave leaves idle, at the
+  // cost of more CTA start-ups). The autotuner measures 1-3 waves once per shape.
+  auto slices_for = [&](int waves) { return std::max(1, std::min(n_tiles, waves * c->sms / n_chunks)); };
+  const size_t pneed = (size_t)n_chunks * slices_for(3) * 128 * K * sizeof(double);
   if (pneed > c->tcpart_cap) {
     dfree(c, c->tcpart, c->tcpart_cap);
     c->tcpart = nullptr;
@@ -1000,12 +1000,45 @@ int launch_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
     cudaFuncSetAttribute(acc_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, AC::SMEM);
     attr_set_acc = true;
   }
+  const CUtensorMap& zm = AC::FT == 128 ? c->tm_zfull : c->tm_zhalf;
+  auto launch_acc = [&](int sl) {
+    acc_kernel<K><<<n_chunks * sl, kThreads, AC::SMEM, c->stream>>>(
+        zm, c->tcm.planes, nTz, nTw, c->tcm.ll2, n_tiles, n_chunks, sl, nullptr, nullptr,
+        c->minGamma, c->Mact == 1, c->static_shapes ? c->flag + 4 : nullptr, c->tcpart, c->tc_err);
+  };
+  int waves = 1;
+  {
+    int tb = 0;
+    while ((1LL << (tb + 1)) <= n_tiles) ++tb;  // frame-tile bucket: power of two
+    const long long key = ((long long)K << 40) | ((long long)n_chunks << 20) | tb;
+    auto it = c->tuned_waves.find(key);
+    if (it != c->tuned_waves.end()) {
+      waves = it->second;
+    } else if (c->autotune && !c->profile) {
+      // each candidate launch rewrites the partials it uses, so the timed runs are harmless
+      cudaEvent_t e0, e1;
+      cudaEventCreate(&e0);
+      cudaEventCreate(&e1);
+      float best = 1e30f;
+      for (int w = 1; w <= 3; ++w) {
+        if (w > 1 && slices_for(w) == slices_for(w - 1)) break;
+        cudaEventRecord(e0, c->stream);
+        launch_acc(slices_for(w));
+        cudaEventRecord(e1, c->stream);
+        cudaEventSynchronize(e1);
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) { best = ms; waves = w; }
+      }
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      c->tuned_waves[key] = waves;
+    }
+  }
+  const int slices = slices_for(waves);
   {
     GMM_LAUNCH(c, "tc_acc_kernel");
-    const CUtensorMap& zm = AC::FT == 128 ? c->tm_zfull : c->tm_zhalf;
-    acc_kernel<K><<<grid, kThreads, AC::SMEM, c->stream>>>(
-        zm, c->tcm.planes, nTz, nTw, c->tcm.ll2, n_tiles, n_chunks, slices, nullptr, nullptr,
-        c->minGamma, c->Mact == 1, c->static_shapes ? c->flag + 4 : nullptr, c->tcpart, c->tc_err);
+    launch_acc(slices);
   }
   {
     GMM_LAUNCH(c, "tc_reduce_kernel");

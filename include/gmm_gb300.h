@@ -97,6 +97,15 @@ int gmm_read_stats(gmm_handle h, double* n, double* F, double* S, double* tot_lo
  * compLogLikes + getLogLikes (CU_GMMStatsEstimator_CUDA.cu:606-643). out: N floats (host). */
 int gmm_loglikes(gmm_handle h, float* out);
 
+/* Autotuner of the tensor-core statistics kernel (no counterpart in the reference): on the first
+ * E-step of a shape (K, component chunks, frame-tile bucket) it times 1, 2 and 3 waves of CTAs
+ * and keeps the fastest for the handle's later E-steps. On by default; off = one wave, the fixed
+ * decomposition. The decomposition groups the FP64 partial sums, so results with different
+ * choices differ only by FP64 rounding. gmm_autotune_choice lists the choices made so far
+ * (*n entries; keys and waves up to cap). */
+int gmm_set_autotune(gmm_handle h, int on);
+int gmm_autotune_choice(gmm_handle h, int* n, long long* keys, int* waves, int cap);
+
 /* M-step on the device statistics (FP64 math, float model), in place on the resident model:
  * CModelAdapt::UpdateModelEM (OL_ModelAdapt.cpp:823-949). *alive = components left with
  * non-zero weight. */

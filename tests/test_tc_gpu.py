@@ -136,3 +136,23 @@ def test_tc_em_iterate_graph_replays_eager_iterations(glib, golden):
     for x, y in zip(m5, m1):
         assert np.array_equal(x, y)
     assert a5 < 24  # the weak component died
+
+
+def test_tc_autotune_choice_and_results(glib):
+    """The autotuner picks a decomposition once per shape and keeps it; statistics with and
+    without tuning agree to FP64 rounding."""
+    from gmm_gb300 import synth
+    X, w, mu, var = synth.config_em(23, 200_000, 20, 16, 300)
+    h = tc_handle(glib)
+    h.upload_model(w, mu, var)
+    h.upload_features(X)
+    a = h.accumulate()
+    ch = h.autotune_choices()
+    assert len(ch) == 1 and list(ch.values())[0] in (1, 2, 3)
+    h.accumulate()
+    assert h.autotune_choices() == ch
+    h.set_autotune(False)
+    b = h.accumulate()
+    h.close()
+    for k in ("n", "F", "S"):
+        assert np.allclose(a[k], b[k], rtol=1e-12, atol=1e-9), k
