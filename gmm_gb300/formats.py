@@ -204,9 +204,35 @@ def read_htk(path: str, dwnsmp: int = 1) -> np.ndarray:
 
 
 def write_loglikes_txt(path: str, ll: np.ndarray) -> None:
-    """Per-frame log-likelihoods in the text layout of ``saveMat`` (IOMats.h:204-220):
-    header "1 N", then the values on one line."""
+    """Per-frame log-likelihoods in the text layout of ``saveMat`` (IOMats.h:169-215): header
+    "1 N", then every value followed by a space, a newline, and a final empty line."""
     with open(path, "w") as f:
         f.write(f"1 {len(ll)}\n")
-        f.write(" ".join("%g" % v for v in ll))
-        f.write("\n")
+        f.write("".join("%g " % v for v in ll))
+        f.write("\n\n")
+
+
+def read_mat(path: str, txt: bool) -> np.ndarray:
+    """``loadMat`` of a ``saveMat`` file: text "x y" then x*y values, or binary int32 x, int32 y
+    and x*y float32 values. Returns an (x, y) float32 array."""
+    if txt:
+        with open(path) as f:
+            tok = f.read().split()
+        x, y = int(tok[0]), int(tok[1])
+        return np.array(tok[2:2 + x * y], np.float32).reshape(x, y)
+    with open(path, "rb") as f:
+        buf = f.read()
+    x, y = struct.unpack_from("<ii", buf, 0)
+    return np.frombuffer(buf, "<f4", x * y, 8).reshape(x, y).copy()
+
+
+def read_trn(path: str) -> np.ndarray:
+    """An MLLR transform file of ``CModelAdapt::SaveTRNMatrices`` (OL_ModelAdapt.cpp:1900-1928):
+    " MLLR", " 1<TAB>x y", then x rows of y values."""
+    with open(path) as f:
+        lines = f.read().split("\n")
+    if lines[0].strip() not in ("MLLR", "fMLLR"):
+        raise ValueError(f"{path}: not a transform file")
+    _, x, y = (int(v) for v in lines[1].split())
+    vals = " ".join(lines[2:]).split()
+    return np.array(vals[:x * y], np.float64).reshape(x, y)

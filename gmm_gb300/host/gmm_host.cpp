@@ -1,0 +1,576 @@
+// Implementation of gmm_host.hpp: model files, the estimator over the C ABI, and the
+// re-estimation driver (EM / MAP / MLLR / training from scratch).
+#include "gmm_host.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <limits>
+#include <sstream>
+
+namespace gmmgb {
+
+namespace {
+
+float reset_var() {
+  // GMMMixture::Reset fills the variances with memset(.., 1, ..) (OL_GMModel.cpp:73-83)
+  uint32_t bits = 0x01010101u;
+  float f;
+  std::memcpy(&f, &bits, sizeof f);
+  return f;
+}
+
+void fail(const std::string& m) { throw std::runtime_error(m); }
+
+}  // namespace
+
+// ------------------------------------------------------------------ GMModel
+
+GMModel::GMModel(int dim, int nummix)
+    : dim_(dim), norm_((size_t)dim, 1.0f), w_((size_t)nummix, 0.0f), mu_((size_t)nummix * dim, 0.0f),
+      var_((size_t)nummix * dim, reset_var()) {}
+
+int GMModel::RearrangeMixtures() {
+  const int M = GetNumberOfMixtures();
+  std::vector<int> order((size_t)M);
+  int nz = 0, z = 1;
+  for (int m = 0; m < M; ++m) {
+    if (w_[(size_t)m] > 0.0f) order[(size_t)nz++] = m;
+    else order[(size_t)(M - z++)] = m;
+  }
+  std::vector<float> w((size_t)M), mu(mu_.size()), var(var_.size());
+  for (int k = 0; k < M; ++k) {
+    const int m = order[(size_t)k];
+    w[(size_t)k] = w_[(size_t)m];
+    std::memcpy(&mu[(size_t)k * dim_], &mu_[(size_t)m * dim_], sizeof(float) * dim_);
+    std::memcpy(&var[(size_t)k * dim_], &var_[(size_t)m * dim_], sizeof(float) * dim_);
+  }
+  w_.swap(w);
+  mu_.swap(mu);
+  var_.swap(var);
+  return z - 1;
+}
+
+void GMModel::Load(const std::string& path, bool txt) {
+  if (txt) {
+    std::ifstream f(path);
+    if (!f) fail("GMModel::Load(): cannot open " + path);
+    std::vector<std::string> lines;
+    std::string ln;
+    while (std::getline(f, ln)) {
+      const size_t a = ln.find_first_not_of(" \t\r"), b = ln.find_last_not_of(" \t\r");
+      lines.push_back(a == std::string::npos ? std::string() : ln.substr(a, b - a + 1));
+    }
+    size_t i = 0;
+    auto num = [&](size_t k) -> double {
+      if (k >= lines.size()) fail("GMModel::Load(): truncated file " + path);
+      return std::stod(lines[k]);
+    };
+    dim_ = (int)num(i++);
+    norm_.assign((size_t)dim_, 0.0f);
+    for (int d = 0; d < dim_; ++d) norm_[(size_t)d] = (float)num(i++);
+    const int M = (int)num(i++);
+    w_.assign((size_t)M, 0.0f);
+    mu_.assign((size_t)M * dim_, 0.0f);
+    var_.assign((size_t)M * dim_, 0.0f);
+    for (int m = 0; m < M; ++m) {
+      std::istringstream head(lines.at(i));
+      std::string tok, kind;
+      head >> tok >> kind;
+      if (kind == "F") fail("GMModel::Load(): full-covariance models are outside the diagonal hot path");
+      w_[(size_t)m] = (float)std::stod(tok);
+      i += 2;
+      for (int d = 0; d < dim_; ++d) mu_[(size_t)m * dim_ + d] = (float)num(i + d);
+      i += dim_ + 1;
+      for (int d = 0; d < dim_; ++d) var_[(size_t)m * dim_ + d] = (float)num(i + d);
+      i += dim_ + 1;
+    }
+  } else {
+    std::ifstream f(path, std::ios::binary);
+    if (!f) fail("GMModel::Load(): cannot open " + path);
+    char tag[9];
+    int16_t D = 0, M = 0;
+    f.read(tag, 9);
+    if (!f || std::memcmp(tag, "GMM-DB-VN", 9) != 0) fail("GMModel::Load(): not a GMM-DB-VN file: " + path);
+    f.read(reinterpret_cast<char*>(&D), 2);
+    if (D < 0) fail("GMModel::Load(): full-covariance models are outside the diagonal hot path");
+    dim_ = D;
+    norm_.assign((size_t)D, 0.0f);
+    f.read(reinterpret_cast<char*>(norm_.data()), sizeof(float) * D);
+    f.read(reinterpret_cast<char*>(&M), 2);
+    w_.assign((size_t)M, 0.0f);
+    mu_.assign((size_t)M * D, 0.0f);
+    var_.assign((size_t)M * D, 0.0f);
+    f.read(reinterpret_cast<char*>(w_.data()), sizeof(float) * M);
+    for (int m = 0; m < M; ++m) {
+      f.read(reinterpret_cast<char*>(&mu_[(size_t)m * D]), sizeof(float) * D);
+      f.read(reinterpret_cast<char*>(&var_[(size_t)m * D]), sizeof(float) * D);
+    }
+    if (!f) fail("GMModel::Load(): truncated file " + path);
+  }
+}
+
+void GMModel::Save(const std::string& path, bool txt) const {
+  std::vector<int> keep;
+  for (int m = 0; m < GetNumberOfMixtures(); ++m)
+    if (w_[(size_t)m] != 0.0f) keep.push_back(m);
+  if (txt) {
+    FILE* f = std::fopen(path.c_str(), "w");
+    if (!f) fail("GMModel::Save(): cannot open " + path);
+    std::fprintf(f, "%d\n", dim_);
+    for (float v : norm_) std::fprintf(f, "%15e\n", v);
+    std::fprintf(f, "%d\n", (int)keep.size());
+    for (int m : keep) {
+      std::fprintf(f, "%15e\n\n", w_[(size_t)m]);
+      for (int d = 0; d < dim_; ++d) std::fprintf(f, "%15e\n", mu_[(size_t)m * dim_ + d]);
+      std::fprintf(f, "\n");
+      for (int d = 0; d < dim_; ++d) std::fprintf(f, "%15e\n", var_[(size_t)m * dim_ + d]);
+      std::fprintf(f, "\n");
+    }
+    std::fclose(f);
+  } else {
+    std::ofstream f(path, std::ios::binary);
+    if (!f) fail("GMModel::Save(): cannot open " + path);
+    const int16_t D = (int16_t)dim_, M = (int16_t)keep.size();
+    f.write("GMM-DB-VN", 9);
+    f.write(reinterpret_cast<const char*>(&D), 2);
+    f.write(reinterpret_cast<const char*>(norm_.data()), sizeof(float) * dim_);
+    f.write(reinterpret_cast<const char*>(&M), 2);
+    for (int m : keep) f.write(reinterpret_cast<const char*>(&w_[(size_t)m]), sizeof(float));
+    for (int m : keep) {
+      f.write(reinterpret_cast<const char*>(&mu_[(size_t)m * dim_]), sizeof(float) * dim_);
+      f.write(reinterpret_cast<const char*>(&var_[(size_t)m * dim_]), sizeof(float) * dim_);
+    }
+  }
+}
+
+// ------------------------------------------------------------------ GMMStats
+
+void GMMStats::alloc(int M_, int D_) {
+  M = M_;
+  D = D_;
+  n.assign((size_t)M, 0.0);
+  F.assign((size_t)M * D, 0.0);
+  S.assign((size_t)M * D, 0.0);
+  totLogLike = 0.0;
+  totalAccSamples = 0;
+}
+
+void GMMStats::reset() { alloc(M, D); }
+
+// ------------------------------------------------------------------ estimator
+
+GMMStatsEstimatorGB300::GMMStatsEstimatorGB300(int gpu_id, int precision) {
+  if (gmm_create(gpu_id < 0 ? 0 : gpu_id, &h_)) throw std::runtime_error(gmm_last_error(nullptr));
+  check(gmm_set_precision(h_, precision));
+}
+
+GMMStatsEstimatorGB300::~GMMStatsEstimatorGB300() { gmm_destroy(h_); }
+
+void GMMStatsEstimatorGB300::check(int rc) const {
+  if (rc) throw std::runtime_error(gmm_last_error(h_));
+}
+
+void GMMStatsEstimatorGB300::insertModel(GMModel& model, bool) {
+  model.RearrangeMixtures();
+  check(gmm_set_options(h_, _minLogLike, _minGamma, _min_var));
+  check(gmm_upload_model(h_, model.GetNumberOfMixtures(), model.GetDimension(), model.weights().data(),
+                         model.means().data(), model.vars().data()));
+  M_ = model.GetNumberOfMixtures();
+}
+
+void GMMStatsEstimatorGB300::setAccFlags(bool mixProbsOnly, bool mean, bool var) {
+  flags_ = (mean ? GMM_ACC_MEAN : 0) | (var ? GMM_ACC_VAR : 0) | (mixProbsOnly ? GMM_ACC_PROBS_ONLY : 0);
+}
+
+void GMMStatsEstimatorGB300::upload(const float* vecs, unsigned N, unsigned dim) {
+  // the frames stay resident while the caller says they did not change (setSameDataFlag)
+  if (!(same_data_ && vecs == last_ && N == last_n_)) check(gmm_upload_features(h_, vecs, N, (int)dim));
+  last_ = vecs;
+  last_n_ = N;
+  same_data_ = false;
+}
+
+void GMMStatsEstimatorGB300::accumulateStatsMT(const float* vecs, unsigned N, unsigned dim, GMMStats& gmms) {
+  if (M_ == 0) fail("accumulateStatsMT(): None model inserted!");
+  upload(vecs, N, dim);
+  // the estimator allocates the statistics when the caller did not (OL_GMMStatsEstimator.cpp:1108-1112)
+  if (gmms.M == 0) gmms.alloc(M_, (int)dim);
+  if (gmms.M != M_ || gmms.D != (int)dim) fail("accumulateStatsMT(): statistics and model sizes differ");
+  const int M = M_;
+  std::vector<double> n, F, S;
+  double tl = 0.0;
+  long long tn = 0;
+  n.assign((size_t)M, 0.0);
+  F.assign((size_t)M * dim, 0.0);
+  S.assign((size_t)M * dim, 0.0);
+  check(gmm_accumulate(h_, flags_, n.data(), F.data(), S.data(), &tl, &tn));
+  for (size_t k = 0; k < n.size(); ++k) gmms.n[k] += n[k];
+  for (size_t k = 0; k < F.size(); ++k) {
+    gmms.F[k] += F[k];
+    gmms.S[k] += S[k];
+  }
+  gmms.totLogLike += tl;
+  gmms.totalAccSamples += tn;
+}
+
+void GMMStatsEstimatorGB300::compVecsLogLikeMT(const float* vecs, unsigned N, unsigned dim, float* out) {
+  upload(vecs, N, dim);
+  check(gmm_loglikes(h_, out));
+}
+
+// ------------------------------------------------------------------ ModelAdapt
+
+ModelAdapt::ModelAdapt(const AdaptOptions& opt) : o_(opt) {
+  if (gmm_create(o_.gpu, &h_)) throw std::runtime_error(gmm_last_error(nullptr));
+  check(gmm_set_precision(h_, o_.precision));
+}
+
+ModelAdapt::~ModelAdapt() { gmm_destroy(h_); }
+
+void ModelAdapt::check(int rc) const {
+  if (rc) throw std::runtime_error(gmm_last_error(h_));
+}
+
+void ModelAdapt::InsertData(const float* X, long long N, int D) {
+  X_.assign(X, X + (size_t)N * D);
+  N_ = N;
+  D_ = D;
+  uploaded_ = false;
+  files_.clear();
+}
+
+void ModelAdapt::InsertFiles(const std::vector<std::string>& paths, int prm_type, unsigned dwnsmp, double buffer_gb) {
+  files_.clear();
+  N_ = 0;
+  D_ = 0;
+  for (const auto& p : paths) {  // headers only: frame counts and the dimension
+    long long n = 0;
+    int d = 0;
+    if (gmm_read_param(p.c_str(), prm_type, dwnsmp, nullptr, 0, &n, &d) || n == 0) continue;
+    if (D_ && d != D_) fail("InsertData(): feature files of different dimensions");
+    D_ = d;
+    N_ += n;
+    files_.push_back(p);
+  }
+  prm_type_ = prm_type;
+  dwnsmp_ = dwnsmp;
+  buffer_gb_ = buffer_gb;
+  X_.clear();
+  uploaded_ = false;
+}
+
+void ModelAdapt::upload_model(GMModel& m) {
+  if (N_ == 0) fail("AdaptModel(): Insert adaptation data first!");
+  if (!uploaded_ && files_.empty()) {
+    check(gmm_upload_features(h_, X_.data(), N_, D_));
+    uploaded_ = true;
+  }
+  check(gmm_set_options(h_, -1e20f, 1e-4f, o_.min_var));
+  check(gmm_upload_model(h_, m.GetNumberOfMixtures(), m.GetDimension(), m.weights().data(), m.means().data(),
+                         m.vars().data()));
+}
+
+void ModelAdapt::estep(int flags) {
+  if (files_.empty()) {
+    check(gmm_accumulate_device(h_, flags));
+    return;
+  }
+  std::vector<const char*> p;
+  for (const auto& f : files_) p.push_back(f.c_str());
+  int used = 0;
+  check(gmm_accumulate_files(h_, flags, (int)p.size(), p.data(), prm_type_, dwnsmp_, buffer_gb_, &used));
+}
+
+void ModelAdapt::IterEM(GMModel& model, int iters) {
+  if (files_.empty()) {
+    upload_model(model);  // gmm_em_iterate rearranges on the device each iteration, as insertModel
+    std::vector<double> ll((size_t)std::max(iters, 1));
+    int alive = 0;
+    check(gmm_em_iterate(h_, iters, o_.AdaptWeightBool, o_.AdaptMeanBool, o_.AdaptVarBool, ll.data(), &alive));
+    ll_history.insert(ll_history.end(), ll.begin(), ll.begin() + iters);
+    check(gmm_read_model(h_, model.weights().data(), model.means().data(), model.vars().data()));
+    return;
+  }
+  // file by file: one pass over the files per iteration (IterEM, OL_ModelAdapt.cpp:1276-1296)
+  const int flags = GMM_ACC_MEAN | GMM_ACC_VAR;
+  for (int it = 0; it < iters; ++it) {
+    model.RearrangeMixtures();
+    upload_model(model);
+    estep(flags);
+    double tl = 0.0;
+    long long tn = 0;
+    check(gmm_read_stats(h_, nullptr, nullptr, nullptr, &tl, &tn));
+    ll_history.push_back(tl);
+    int alive = 0;
+    check(gmm_em_update(h_, o_.AdaptWeightBool, o_.AdaptMeanBool, o_.AdaptVarBool, &alive));
+    check(gmm_read_model(h_, model.weights().data(), model.means().data(), model.vars().data()));
+  }
+}
+
+void ModelAdapt::IterMAP(GMModel& model, const GMModel& ubm, int iters) {
+  const int flags = (o_.AdaptMeanBool ? GMM_ACC_MEAN : 0) | (o_.AdaptVarBool ? GMM_ACC_VAR : 0) |
+                    ((o_.AdaptWeightBool && !o_.AdaptMeanBool && !o_.AdaptVarBool) ? GMM_ACC_PROBS_ONLY : 0);
+  for (int it = 0; it < iters; ++it) {
+    model.RearrangeMixtures();
+    upload_model(model);
+    check(gmm_set_prior(h_, ubm.weights().data(), ubm.means().data(), ubm.vars().data()));
+    estep(flags);
+    double tl = 0.0;
+    long long tn = 0;
+    check(gmm_read_stats(h_, nullptr, nullptr, nullptr, &tl, &tn));
+    ll_history.push_back(tl);
+    if (o_.tau == 0) {
+      int alive = 0;
+      check(gmm_em_update(h_, o_.AdaptWeightBool, o_.AdaptMeanBool, o_.AdaptVarBool, &alive));
+      if (alive == 0) {
+        model = ubm;
+        continue;
+      }
+    } else {
+      check(gmm_map_update(h_, o_.tau, o_.AdaptWeightBool, o_.AdaptMeanBool, o_.AdaptVarBool));
+    }
+    check(gmm_read_model(h_, model.weights().data(), model.means().data(), model.vars().data()));
+  }
+}
+
+std::vector<double> ModelAdapt::ComputeW_MLLR(GMModel& model, const GMModel& ubm) {
+  model.RearrangeMixtures();
+  upload_model(model);
+  check(gmm_set_prior(h_, ubm.weights().data(), ubm.means().data(), ubm.vars().data()));
+  estep(GMM_ACC_MEAN);
+  std::vector<double> W((size_t)D_ * (D_ + 1));
+  check(gmm_mllr_estimate(h_, o_.mllrUBMInit, W.data()));
+  return W;
+}
+
+GMModel ModelAdapt::AdaptModelMLLR(const GMModel& model, const std::vector<double>& W) {
+  GMModel out = model;
+  upload_model(out);
+  check(gmm_mllr_apply(h_, W.data()));
+  check(gmm_read_model(h_, out.weights().data(), out.means().data(), out.vars().data()));
+  return out;
+}
+
+namespace {
+// CModelAdapt::UpdateMLLRMatrix (OL_ModelAdapt.cpp:1319-1340): [A|b] <- [A_new A | A_new b + b_new].
+std::vector<double> compose(const std::vector<double>& Ws, const std::vector<double>& Wn, int D) {
+  const int E = D + 1;
+  std::vector<double> out((size_t)D * E, 0.0);
+  for (int k = 0; k < D; ++k) {
+    for (int x = 0; x < D; ++x) {
+      double s = 0.0;
+      for (int y = 0; y < D; ++y) s += Wn[(size_t)k * E + y] * Ws[(size_t)y * E + x];
+      out[(size_t)k * E + x] += s;
+      out[(size_t)k * E + D] += Wn[(size_t)k * E + x] * Ws[(size_t)x * E + D];
+    }
+    out[(size_t)k * E + D] += Wn[(size_t)k * E + D];
+  }
+  return out;
+}
+}  // namespace
+
+void ModelAdapt::AdaptModel(const GMModel& ubm) {
+  if (o_.adaptType == MAP) {
+    GMModel model = ubm;
+    if (o_.iterCountEM) IterEM(model, o_.iterCountEM);
+    if (o_.iterCountMAP) IterMAP(model, ubm, o_.iterCountMAP);
+    model_ = model;
+    trained_ = true;
+  } else if (o_.adaptType == MLLR) {
+    // IterW_MLLR (OL_ModelAdapt.cpp:1365-1415)
+    GMModel u = ubm;
+    std::vector<double> W = ComputeW_MLLR(u, ubm);
+    if (o_.iterMLLR > 1) {
+      GMModel sp = AdaptModelMLLR(ubm, W);
+      for (int it = 1; it < o_.iterMLLR - 1; ++it) {
+        std::vector<double> Wt = ComputeW_MLLR(sp, ubm);
+        sp = AdaptModelMLLR(sp, Wt);
+        W = compose(W, Wt, D_);
+      }
+      std::vector<double> Wt = ComputeW_MLLR(sp, ubm);
+      W = compose(W, Wt, D_);
+    }
+    W_ = W;
+    if (o_.applyTransforms) {
+      model_ = AdaptModelMLLR(ubm, W_);
+      trained_ = true;
+    }
+  } else {
+    fail("AdaptModel(): use TrainFromScratch for --type 0");
+  }
+}
+
+namespace {
+// GetGaussStats (OL_ModelAdapt.cpp:951-990)
+void gauss_stats(const GMModel& m, bool get_list, int* i_max, std::vector<int>* zero, std::vector<int>* srt) {
+  *i_max = 0;
+  float wm = 0.0f;
+  zero->clear();
+  srt->clear();
+  for (int k = m.GetNumberOfMixtures() - 1; k >= 0; --k) {
+    const float w = m.GetMixtureWeight(k);
+    if (wm < w) {
+      wm = w;
+      *i_max = k;
+    }
+    if (w == 0.0f) {
+      zero->push_back(k);
+      continue;
+    }
+    if (get_list) {
+      size_t p = 0;
+      while (p < srt->size() && m.GetMixtureWeight((*srt)[p]) > w) ++p;
+      srt->insert(srt->begin() + (long)p, k);
+    }
+  }
+}
+
+// splitGaussian (OL_ModelAdapt.cpp:612-665), diagonal covariances
+void split_gaussian(GMModel& model, int m2, int mnew) {
+  const int D = model.GetDimension();
+  std::memcpy(model.GetMixtureVar(mnew), model.GetMixtureVar(m2), sizeof(float) * D);
+  const float w = model.GetMixtureWeight(m2) / 2.0f;
+  model.SetMixWeight(mnew, w);
+  model.SetMixWeight(m2, w);
+  float* m = model.GetMixtureMean(m2);
+  float* mn = model.GetMixtureMean(mnew);
+  for (int d = 0; d < D; ++d) {
+    const float shift = (float)(std::sqrt((double)model.GetMixtureVar(m2)[d]) * 0.5);
+    mn[d] = m[d] + shift;
+    m[d] -= shift;
+  }
+}
+}  // namespace
+
+void ModelAdapt::splitMultipleGaussians(GMModel& model) {
+  int i_max = 0;
+  std::vector<int> zero, srt;
+  gauss_stats(model, o_.splitXpercAtOnce > 0.0f, &i_max, &zero, &srt);
+  const unsigned n_split =
+      (unsigned)std::ceil(o_.splitXpercAtOnce * (float)(model.GetNumberOfMixtures() - (int)zero.size()));
+  if (n_split < 2) {
+    split_gaussian(model, i_max, zero.front());
+    return;
+  }
+  const float th = o_.splitTh * model.GetMixtureWeight(i_max);
+  for (size_t n = 0; n < srt.size(); ++n) {
+    if (model.GetMixtureWeight(srt[n]) < th || n >= zero.size() || n >= n_split) break;
+    split_gaussian(model, srt[n], zero[n]);
+  }
+}
+
+void ModelAdapt::TrainFromScratch(int nummix, const GMModel* init_model) {
+  if (N_ <= 3) fail("TrainFromScratch(): Not enough data to model training.");
+  const int D = D_;
+  GMModel init;
+  int max_iter = nummix;
+  if (!init_model) {
+    // global Gaussian: one component, every posterior 1
+    init = GMModel(D, 1);
+    init.SetMixWeight(0, 1.0f);
+    for (int d = 0; d < D; ++d) init.GetMixtureVar(0)[d] = 1.0f;
+    upload_model(init);
+    estep(GMM_ACC_MEAN | GMM_ACC_VAR);
+    int alive = 0;
+    check(gmm_em_update(h_, 1, 1, 1, &alive));
+    if (alive == 0) fail("trainFromScratch(): amount of data too low to estimate a model, or data are constant!");
+    check(gmm_read_model(h_, init.weights().data(), init.means().data(), init.vars().data()));
+  } else {
+    init = *init_model;
+    if (init.GetDimension() != D) fail("trainFromScratch(): init model and data dimensions differ!");
+    if (nummix <= init.GetNumberOfMixtures())
+      fail("trainFromScratch(): init model already contains specified number of Gaussians!");
+    max_iter = nummix - init.GetNumberOfMixtures();
+  }
+  if (nummix < 2) max_iter = 0;
+  GMModel model(D, nummix);
+  for (int m = 0; m < init.GetNumberOfMixtures(); ++m) {
+    model.SetMixWeight(m, init.GetMixtureWeight(m));
+    std::memcpy(model.GetMixtureMean(m), init.GetMixtureMean(m), sizeof(float) * D);
+    std::memcpy(model.GetMixtureVar(m), init.GetMixtureVar(m), sizeof(float) * D);
+  }
+  const int iters_em = (o_.iterCountEM < 2 && o_.llTh > 0.0f) ? 2 : o_.iterCountEM;
+  const float lowest = -std::numeric_limits<float>::max();
+  float ll[3] = {lowest, lowest, lowest};
+  GMModel m2, m3;
+  int non_zero = init.GetNumberOfMixtures();
+  for (int it = 0; it < max_iter; ++it) {
+    for (int e = 0; e < iters_em; ++e) {
+      model.RearrangeMixtures();
+      upload_model(model);
+      estep(GMM_ACC_MEAN | GMM_ACC_VAR);
+      if (o_.verbosity) {  // the reference only tracks the average LL when verbose
+        double tl = 0.0;
+        long long tn = 0;
+        check(gmm_read_stats(h_, nullptr, nullptr, nullptr, &tl, &tn));
+        ll[0] = (float)(tl / (double)tn);
+      }
+      if (non_zero > 1) {
+        check(gmm_em_update(h_, 1, 1, 1, &non_zero));
+        check(gmm_read_model(h_, model.weights().data(), model.means().data(), model.vars().data()));
+      }
+      if (non_zero < 2) {
+        if (non_zero < 1) model = init;
+        break;
+      }
+    }
+    if (non_zero == 0 || non_zero == nummix) break;
+    if (o_.llTh > 0.0f) {
+      const float mx = std::max(ll[1], ll[2]);
+      if (it > 2 && ll[0] - mx < o_.llTh) {
+        if (mx > ll[0]) model = (mx == ll[1]) ? m2 : m3;
+        break;
+      }
+      m3 = m2;
+      m2 = model;
+      ll[2] = ll[1];
+      ll[1] = ll[0];
+    }
+    if (it < max_iter - 1) {
+      splitMultipleGaussians(model);
+      non_zero += 1;
+    }
+  }
+  model.RearrangeMixtures();
+  model_ = model;
+  trained_ = true;
+}
+
+void ModelAdapt::SaveTRNMatrices(const std::string& FileName) const {
+  std::string out = FileName;
+  const size_t dot = out.rfind('.');
+  if (dot != std::string::npos) out.erase(dot);
+  out += o_.transformFileExt;
+  FILE* f = std::fopen(out.c_str(), "w");
+  if (!f) fail("Save(): Unable to open output file " + out + "!");
+  const int E = D_ + 1;
+  std::fprintf(f, " MLLR\n 1\t%d %d\n", D_, E);
+  for (int i = 0; i < D_; ++i) {  // the reference streams a float matrix with ostream defaults (%g)
+    for (int j = 0; j < E; ++j) std::fprintf(f, " %g", (double)(float)W_[(size_t)i * E + j]);
+    std::fprintf(f, "\n");
+  }
+  std::fclose(f);
+}
+
+void ModelAdapt::Save(const std::string& FileName, bool save_txt) const {
+  const bool trn = !W_.empty();
+  if (!trained_ && !trn) fail("Save(): Missing client model or transformation matrix!");
+  if (trn && (!trained_ || o_.saveTransforms)) SaveTRNMatrices(FileName);
+  if (trained_) model_.Save(FileName, save_txt);
+}
+
+// ------------------------------------------------------------------ feature files
+
+std::vector<float> read_features(const std::string& path, int prm_type, unsigned dwnsmp, long long* N, int* D) {
+  if (gmm_read_param(path.c_str(), prm_type, dwnsmp, nullptr, 0, N, D))
+    fail("Param::Load(): cannot read " + path);
+  std::vector<float> X((size_t)(*N) * (*D));
+  if (*N > 0 && gmm_read_param(path.c_str(), prm_type, dwnsmp, X.data(), *N, N, D))
+    fail("Param::Load(): cannot read " + path);
+  return X;
+}
+
+}  // namespace gmmgb
