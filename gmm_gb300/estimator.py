@@ -74,6 +74,24 @@ class GMMStats:
     def getVar(self, m):
         return self.S[m]
 
+    def save(self, filename: str, saveTxt: bool) -> None:
+        """``GMMStats<double>::save`` file layout (formats.write_gmm_stats)."""
+        from . import formats
+        formats.write_gmm_stats(filename, saveTxt, self.n, self.F if self._allM else None,
+                                self.S if self._allV else None)
+
+    def load(self, filename: str, loadTxt: bool) -> None:
+        """``GMMStats<double>::load``: (re)allocates to the file's sizes and fills it."""
+        from . import formats
+        n, F, S = formats.read_gmm_stats(filename, loadTxt)
+        D = F.shape[1] if F is not None else (S.shape[1] if S is not None else 0)
+        self.alloc(D, len(n), F is not None, S is not None)
+        self.n[:] = n
+        if F is not None:
+            self.F[:] = F
+        if S is not None:
+            self.S[:] = S
+
     def __iadd__(self, o: "GMMStats"):
         if self._M != o._M:
             raise ValueError("operator+= : Inconsistent statistics differing in number of mixtures!")

@@ -203,6 +203,59 @@ def read_htk(path: str, dwnsmp: int = 1) -> np.ndarray:
     return _downsample(np.frombuffer(buf, ">f4", N * D, 12).reshape(N, D).astype(np.float32), dwnsmp)
 
 
+def write_gmm_stats(path: str, txt: bool, n, F=None, S=None, dtype=np.float64) -> None:
+    """``GMMStats<T>::save`` (model/OL_GMMStats.cpp:657-778), diagonal statistics: seven int32
+    (mixProb saved, means saved, vars saved, full vars saved, dim, varsize, nummix), then per
+    component n, F[dim], S[dim] as ``dtype``; the text layout has the same header line, a blank
+    line, then per component "n", " F ...", " S ...", blank, in ostream's default format (%g)."""
+    n = np.asarray(n, dtype)
+    M = len(n)
+    D = np.asarray(F).shape[1] if F is not None else (np.asarray(S).shape[1] if S is not None else 0)
+    hdr = [1, int(F is not None), int(S is not None), 0, D, D if S is not None else 0, M]
+    if txt:
+        with open(path, "w") as f:
+            f.write(" ".join(map(str, hdr)) + "\n\n")
+            for m in range(M):
+                f.write("%g\n" % n[m])
+                if F is not None:
+                    f.write("".join(" %g" % v for v in np.asarray(F, dtype)[m]) + "\n")
+                if S is not None:
+                    f.write("".join(" %g" % v for v in np.asarray(S, dtype)[m]) + "\n")
+                f.write("\n")
+        return
+    with open(path, "wb") as f:
+        f.write(np.asarray(hdr, "<i4").tobytes())
+        for m in range(M):
+            f.write(np.asarray(n[m], dtype).tobytes())
+            if F is not None:
+                f.write(np.asarray(F, dtype)[m].tobytes())
+            if S is not None:
+                f.write(np.asarray(S, dtype)[m].tobytes())
+
+
+def read_gmm_stats(path: str, txt: bool, dtype=np.float64):
+    """``GMMStats<T>::load`` (OL_GMMStats.cpp:493-655): returns (n, F or None, S or None)."""
+    if txt:
+        with open(path) as f:
+            tok = f.read().split()
+        hdr = [int(v) for v in tok[:7]]
+        vals = np.array(tok[7:], np.float64)
+    else:
+        with open(path, "rb") as f:
+            buf = f.read()
+        hdr = list(np.frombuffer(buf, "<i4", 7))
+        vals = np.frombuffer(buf, dtype, offset=28).astype(np.float64)
+    mp, mean, var, full, D, varsize, M = hdr
+    if full:
+        raise ValueError("full-covariance statistics are outside the diagonal hot path")
+    rec = int(mp) + int(mean) * D + int(var) * varsize
+    body = vals[:M * rec].reshape(M, rec)
+    n = body[:, 0] if mp else None
+    F = body[:, int(mp):int(mp) + D] if mean else None
+    S = body[:, int(mp) + int(mean) * D:] if var else None
+    return n, F, S
+
+
 def write_loglikes_txt(path: str, ll: np.ndarray) -> None:
     """Per-frame log-likelihoods in the text layout of ``saveMat`` (IOMats.h:169-215): header
     "1 N", then every value followed by a space, a newline, and a final empty line."""

@@ -38,6 +38,7 @@ std::vector<gmmgb::cli::Opt> options() {
       {"data-T", 0, STR, "0", "feature files in sves(0) / htk(1) / raw(2) format"},
       {"load-txt", 'L', FLAG, "0", "load models from text files"},
       {"save-txt", 'T', FLAG, "0", "save the model as a text file"},
+      {"save-in-stat-form", 0, FLAG, "0", "save the model (or MLLR transform) in the GMMStats file layout"},
       {"dwnsmp", 0, STR, "1", "down-sample factor of the feature vectors"},
       {"verbosity", 'v', STR, "0", "verbose mode"},
       {"type", 't', STR, "2", "FROM_SCRATCH=0, MLLR=1, MAP=2"},
@@ -232,7 +233,7 @@ int main(int argc, char** argv) {
       }
       if (from_scratch) ma.TrainFromScratch(nummix, no_model ? nullptr : &ubm);
       else ma.AdaptModel(ubm);
-      ma.Save(j.out, save_txt);
+      ma.Save(j.out, save_txt, P.get_bool("save-in-stat-form"));
       if (o.verbosity)
         for (size_t i = 0; i < ma.ll_history.size(); ++i)
           std::printf(" [%s] E-step %zu: total log-likelihood %.17g\n", j.name.c_str(), i, ma.ll_history[i]);

@@ -160,6 +160,83 @@ void GMMStats::alloc(int M_, int D_) {
 
 void GMMStats::reset() { alloc(M, D); }
 
+namespace {
+
+// The header and records of the GMMStats file layout, for T = double or float.
+template <typename T>
+void write_stats(const std::string& path, bool txt, int dim, int nummix, const T* mp, const T* mean,
+                 const T* var) {
+  FILE* f = std::fopen(path.c_str(), txt ? "w" : "wb");
+  if (!f) fail("save(): Unable to open file " + path);
+  const int32_t hdr[7] = {1, mean != nullptr, var != nullptr, 0, dim, var ? dim : 0, nummix};
+  bool ok = true;
+  if (txt) {
+    ok = std::fprintf(f, "%d %d %d %d %d %d %d\n\n", hdr[0], hdr[1], hdr[2], hdr[3], hdr[4], hdr[5], hdr[6]) > 0;
+    for (int m = 0; ok && m < nummix; ++m) {
+      ok = std::fprintf(f, "%g\n", (double)mp[m]) > 0;
+      if (mean) {
+        for (int d = 0; ok && d < dim; ++d) ok = std::fprintf(f, " %g", (double)mean[(size_t)m * dim + d]) > 0;
+        ok = ok && std::fputc('\n', f) != EOF;
+      }
+      if (var) {
+        for (int d = 0; ok && d < dim; ++d) ok = std::fprintf(f, " %g", (double)var[(size_t)m * dim + d]) > 0;
+        ok = ok && std::fputc('\n', f) != EOF;
+      }
+      ok = ok && std::fputc('\n', f) != EOF;
+    }
+  } else {
+    ok = std::fwrite(hdr, sizeof hdr, 1, f) == 1;
+    for (int m = 0; ok && m < nummix; ++m) {
+      ok = std::fwrite(&mp[m], sizeof(T), 1, f) == 1;
+      if (ok && mean) ok = std::fwrite(&mean[(size_t)m * dim], sizeof(T), (size_t)dim, f) == (size_t)dim;
+      if (ok && var) ok = std::fwrite(&var[(size_t)m * dim], sizeof(T), (size_t)dim, f) == (size_t)dim;
+    }
+  }
+  if (std::fclose(f) != 0 || !ok) fail("save(): Exception writing file " + path);
+}
+
+}  // namespace
+
+void GMMStats::save(const std::string& path, bool txt) const {
+  write_stats<double>(path, txt, D, M, n.data(), F.data(), S.data());
+}
+
+void GMMStats::load(const std::string& path, bool txt) {
+  std::ifstream f(path, txt ? std::ios::in : std::ios::binary);
+  if (!f) fail("load(): Unable to open file " + path);
+  int32_t h[7] = {0, 0, 0, 0, 0, 0, 0};
+  if (txt) {
+    for (int k = 0; k < 7; ++k) f >> h[k];
+  } else {
+    f.read(reinterpret_cast<char*>(h), sizeof h);
+  }
+  if (!f) fail("load(): Exception reading file " + path);
+  if (h[3]) fail("load(): full-covariance statistics are outside the diagonal hot path");
+  alloc(h[6], h[4]);
+  const int varsize = h[5];
+  for (int m = 0; m < M; ++m) {
+    double* Fm = &F[(size_t)m * D];
+    double* Sm = &S[(size_t)m * D];
+    if (txt) {
+      if (h[0]) f >> n[(size_t)m];
+      if (h[1])
+        for (int d = 0; d < D; ++d) f >> Fm[d];
+      if (h[2])
+        for (int d = 0; d < varsize; ++d) f >> Sm[d];
+    } else {
+      if (h[0]) f.read(reinterpret_cast<char*>(&n[(size_t)m]), sizeof(double));
+      if (h[1]) f.read(reinterpret_cast<char*>(Fm), sizeof(double) * D);
+      if (h[2]) f.read(reinterpret_cast<char*>(Sm), sizeof(double) * varsize);
+    }
+    if (!f) fail("load(): Exception reading file " + path);
+  }
+}
+
+void save_stats_float(const std::string& path, bool txt, int dim, int nummix, const float* mixprob,
+                      const float* mean, const float* var) {
+  write_stats<float>(path, txt, dim, nummix, mixprob, mean, var);
+}
+
 // ------------------------------------------------------------------ estimator
 
 GMMStatsEstimatorGB300::GMMStatsEstimatorGB300(int gpu_id, int precision) {
@@ -555,11 +632,25 @@ void ModelAdapt::SaveTRNMatrices(const std::string& FileName) const {
   std::fclose(f);
 }
 
-void ModelAdapt::Save(const std::string& FileName, bool save_txt) const {
+void ModelAdapt::Save(const std::string& FileName, bool save_txt, bool save_in_stat_form) const {
   const bool trn = !W_.empty();
   if (!trained_ && !trn) fail("Save(): Missing client model or transformation matrix!");
-  if (trn && (!trained_ || o_.saveTransforms)) SaveTRNMatrices(FileName);
-  if (trained_) model_.Save(FileName, save_txt);
+  if (trn && (!trained_ || o_.saveTransforms)) {
+    if (!save_in_stat_form) {
+      SaveTRNMatrices(FileName);
+    } else {  // D records of dimension D+1: occupancy 1, "mean" = the row of W
+      std::vector<float> one((size_t)D_, 1.0f), rows(W_.size());
+      for (size_t k = 0; k < W_.size(); ++k) rows[k] = (float)W_[k];
+      save_stats_float(FileName, save_txt, D_ + 1, D_, one.data(), rows.data(), nullptr);
+    }
+  }
+  if (trained_) {
+    if (!save_in_stat_form)
+      model_.Save(FileName, save_txt);
+    else  // every component slot, zero weights included
+      save_stats_float(FileName, save_txt, model_.GetDimension(), model_.GetNumberOfMixtures(),
+                       model_.weights().data(), model_.means().data(), model_.vars().data());
+  }
 }
 
 // ------------------------------------------------------------------ feature files

@@ -57,7 +57,19 @@ struct GMMStats {
   long long totalAccSamples = 0;
   void alloc(int M_, int D_);
   void reset();
+  // GMMStats<double>::save / load (OL_GMMStats.cpp:493-778): binary = seven int32 (mixProb,
+  // mean, var and full-var flags, dim, varsize, nummix) then per component n, F[D], S[D] as
+  // doubles; text = the same header line, a blank line, then per component "n", " F..", " S..",
+  // blank, in ostream's default 6-digit format. Diagonal statistics only.
+  void save(const std::string& path, bool txt) const;
+  void load(const std::string& path, bool txt);
 };
+
+// The same layout for single-precision records (GMMStats<float>), as CModelAdapt::Save writes a
+// model or an MLLR transform with --save-in-stat-form (OL_ModelAdapt.cpp:1946-1987); `mean` or
+// `var` may be null (not saved).
+void save_stats_float(const std::string& path, bool txt, int dim, int nummix, const float* mixprob,
+                      const float* mean, const float* var);
 
 // GMMStatsEstimator implemented on one GB300: the virtuals the reference's estimators override
 // (insertModel, accumulateStatsMT, compVecsLogLikeMT) and its public knobs.
@@ -131,7 +143,7 @@ class ModelAdapt {
   // CModelAdapt::Save (OL_ModelAdapt.cpp:1930-1989): the MLLR transform (when it is the result,
   // or saveTransforms is set) to FileName with its extension replaced by transformFileExt, and
   // the adapted / trained model to FileName.
-  void Save(const std::string& FileName, bool save_txt) const;
+  void Save(const std::string& FileName, bool save_txt, bool save_in_stat_form = false) const;
   // SaveTRNMatrices (OL_ModelAdapt.cpp:1900-1928): " MLLR", " 1\tD D+1", rows of " value".
   void SaveTRNMatrices(const std::string& FileName) const;
   std::vector<double> ll_history;

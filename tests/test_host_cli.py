@@ -27,6 +27,11 @@ int main(int argc, char** argv) {
     const int z = g.RearrangeMixtures();
     g.Save(argv[4], std::atoi(argv[5]));
     std::printf("%d %d %d\n", g.GetDimension(), g.GetNumberOfMixtures(), z);
+  } else if (cmd == "stats") {     // stats IN TXT_IN OUT TXT_OUT
+    gmmgb::GMMStats st;
+    st.load(argv[2], std::atoi(argv[3]));
+    st.save(argv[4], std::atoi(argv[5]));
+    std::printf("%d %d\n", st.M, st.D);
   } else if (cmd == "newpath") {   // newpath FILE DIR EXT
     std::printf("%s\n", gmmgb::cli::new_path(argv[2], argv[3], argv[4]).c_str());
   } else if (cmd == "list") {      // list PATH EXT
@@ -120,6 +125,31 @@ def test_rearrange_matches_reference_rule(driver, tmp_path):
     r = formats.read_gmm_bin(str(out))
     keep = order[:7]
     assert np.array_equal(r.w, g.w[:7]) and np.array_equal(r.mu, formats.read_gmm_txt(str(p)).mu[keep])
+
+
+@pytest.mark.parametrize("txt_in", [0, 1])
+@pytest.mark.parametrize("txt_out", [0, 1])
+def test_stats_files_match_python_writer(driver, tmp_path, txt_in, txt_out):
+    from gmm_gb300 import estimator, formats
+    rng = np.random.default_rng(4)
+    n = rng.uniform(0, 500, 6)
+    F = rng.standard_normal((6, 4)) * 100
+    S = rng.uniform(1, 1e4, (6, 4))
+    if txt_in:  # the text file holds 6 digits: start from values it represents exactly
+        n, F, S = (np.array(["%g" % v for v in a.ravel()], float).reshape(a.shape) for a in (n, F, S))
+    src = tmp_path / "in.st"
+    formats.write_gmm_stats(str(src), txt_in, n, F, S)
+    out = tmp_path / "out.st"
+    assert driver("stats", src, txt_in, out, txt_out).split() == ["6", "4"]
+    want = tmp_path / "want.st"
+    formats.write_gmm_stats(str(want), txt_out, n, F, S)
+    assert out.read_bytes() == want.read_bytes()
+    st = estimator.GMMStats()
+    st.load(str(out), txt_out)
+    tol = 1e-5 if txt_out else 0
+    assert np.allclose(st.n, n, rtol=tol, atol=0) and np.allclose(st.F, F, rtol=tol) and np.allclose(st.S, S, rtol=tol)
+    st.save(str(tmp_path / "again.st"), txt_out)
+    assert (tmp_path / "again.st").read_bytes() == out.read_bytes()
 
 
 def test_output_naming_and_lists(driver, tmp_path):

@@ -119,6 +119,17 @@ def test_map_and_mllr_match_reference(exe, golden, tmp_path):
         assert np.allclose(W, g[f"mllr_W{key}"], rtol=2e-5, atol=2e-6)
         a = read_model(out)
         assert np.allclose(a.mu, g[f"mllr_mu{key}"], rtol=1e-5, atol=1e-5)
+    # --save-in-stat-form: the model and the transform in the GMMStats<float> layout
+    run(exe("gmm_adapt"), "-i", feat, "-u", ubm, "-o", tmp_path / "map.st", "-t", "2", "--it-MAP", "1",
+        "-r", "16", "-M", "--precision", "fp32", "--save-in-stat-form")
+    n, F, S = formats.read_gmm_stats(str(tmp_path / "map.st"), False, np.float32)
+    assert np.array_equal(n, m.w) and np.array_equal(F, m.mu) and np.array_equal(S, m.var)
+    run(exe("gmm_adapt"), "-i", feat, "-u", ubm, "-o", tmp_path / "w.st", "-t", "1", "--precision", "fp32",
+        "--save-in-stat-form", "-T")
+    n, F, S = formats.read_gmm_stats(str(tmp_path / "w.st"), True)
+    D = g["X"].shape[1]
+    assert S is None and np.all(n == 1) and F.shape == (D, D + 1)
+    assert np.allclose(F, g["mllr_W0"], rtol=2e-5, atol=2e-6)
     # without --apply-trn only the transform is written
     out = tmp_path / "only.gmm"
     run(exe("gmm_adapt"), "-i", feat, "-u", ubm, "-o", out, "-t", "1", "-X", ".trn")
