@@ -28,6 +28,15 @@ SIGNATURES = {
     "gmm_set_memory_budget": (_i, [_vp, _sz]),
     "gmm_get_stream": (_i, [_vp, C.POINTER(_vp)]),
     "gmm_upload_model": (_i, [_vp, _i, _i, _vp, _vp, _vp]),
+    "gmm_upload_model_full": (_i, [_vp, _i, _i, _vp, _vp, _vp]),
+    "gmm_set_prior_full": (_i, [_vp, _vp, _vp, _vp]),
+    "gmm_read_model_full": (_i, [_vp, _vp, _vp, _vp]),
+    "gmm_accumulate_full": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _vp]),
+    "gmm_accumulate_full_device": (_i, [_vp, _i]),
+    "gmm_read_stats_full": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "gmm_loglikes_full": (_i, [_vp, _vp]),
+    "gmm_em_update_full": (_i, [_vp, _i, _i, _i, _vp]),
+    "gmm_map_update_full": (_i, [_vp, _i, _i, _i, _i]),
     "gmm_set_prior": (_i, [_vp, _vp, _vp, _vp]),
     "gmm_read_model": (_i, [_vp, _vp, _vp, _vp]),
     "gmm_upload_features": (_i, [_vp, _vp, _ll, _i]),
@@ -246,6 +255,61 @@ class Handle:
 
     def map_update(self, tau, upW=False, upM=True, upV=False):
         self.check(self.lib.gmm_map_update(self.h, int(tau), int(upW), int(upM), int(upV)))
+
+    # -- full covariances (cov [M, D, D]; second-order statistics packed [M, D(D+1)/2])
+    def upload_model_full(self, w, mu, cov):
+        w = np.ascontiguousarray(w, np.float32)
+        mu = np.ascontiguousarray(mu, np.float32)
+        cov = np.ascontiguousarray(cov, np.float32)
+        M, D = mu.shape
+        if cov.shape != (M, D, D):
+            raise ValueError("cov must be [M, D, D]")
+        self.check(self.lib.gmm_upload_model_full(self.h, M, D, ptr(w), ptr(mu), ptr(cov)))
+        self.Mf, self.Df = M, D
+
+    def set_prior_full(self, w=None, mu=None, cov=None):
+        if w is None:
+            self.check(self.lib.gmm_set_prior_full(self.h, None, None, None))
+            return
+        w, mu, cov = (np.ascontiguousarray(a, np.float32) for a in (w, mu, cov))
+        self.check(self.lib.gmm_set_prior_full(self.h, ptr(w), ptr(mu), ptr(cov)))
+
+    def read_model_full(self):
+        w = np.zeros(self.Mf, np.float32)
+        mu = np.zeros((self.Mf, self.Df), np.float32)
+        cov = np.zeros((self.Mf, self.Df, self.Df), np.float32)
+        self.check(self.lib.gmm_read_model_full(self.h, ptr(w), ptr(mu), ptr(cov)))
+        return w, mu, cov
+
+    def _full_stats(self, fn, *args):
+        P = self.Df * (self.Df + 1) // 2
+        n, F, Sp = np.zeros(self.Mf), np.zeros((self.Mf, self.Df)), np.zeros((self.Mf, P))
+        tl, tn = C.c_double(), C.c_longlong()
+        self.check(fn(self.h, *args, ptr(n), ptr(F), ptr(Sp), C.byref(tl), C.byref(tn)))
+        return dict(n=n, F=F, Sp=Sp, totLL=tl.value, totN=tn.value)
+
+    def accumulate_full(self, flags=ACC_MEAN | ACC_VAR):
+        return self._full_stats(self.lib.gmm_accumulate_full, flags)
+
+    def accumulate_full_device(self, flags=ACC_MEAN | ACC_VAR):
+        self.check(self.lib.gmm_accumulate_full_device(self.h, flags))
+
+    def read_stats_full(self):
+        return self._full_stats(self.lib.gmm_read_stats_full)
+
+    def loglikes_full(self):
+        out = np.zeros(self.N, np.float32)
+        self.check(self.lib.gmm_loglikes_full(self.h, ptr(out)))
+        return out
+
+    def em_update_full(self, upW=True, upM=True, upV=True):
+        a = C.c_int()
+        self.check(self.lib.gmm_em_update_full(self.h, int(upW), int(upM), int(upV), C.byref(a)))
+        self.last_alive = a.value
+        return a.value
+
+    def map_update_full(self, tau, upW=False, upM=True, upV=False):
+        self.check(self.lib.gmm_map_update_full(self.h, int(tau), int(upW), int(upM), int(upV)))
 
     def map_batch(self, offs, tau, upW=False, upM=True, upV=False):
         """One MAP iteration per speaker against the resident model (the UBM); speaker s owns the

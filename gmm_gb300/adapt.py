@@ -134,11 +134,41 @@ class ModelAdapt:
     def _upload(self, model: GMModel):
         self.dev.set_options(-1e20, 1e-4, self.opt.min_var)
         model.rearrange()
-        self.dev.upload_model(model.w, model.mu, model.var)
+        if model.full:
+            self.dev.upload_model_full(model.w, model.mu, model.var)
+        else:
+            self.dev.upload_model(model.w, model.mu, model.var)
+
+    def _read(self, model: GMModel):
+        model.w, model.mu, model.var = self.dev.read_model_full() if model.full else self.dev.read_model()
+
+    def _iter_full(self, model: GMModel, ubm: GMModel | None, iters: int) -> GMModel:
+        """IterEM (ubm None) / IterMAP on a full-covariance model: insertModel (rearrange +
+        upload), the E-step with full second-order statistics, UpdateModelEM / UpdateModelMAP."""
+        o = self.opt
+        self._ensure_features()
+        for _ in range(iters):
+            self._upload(model)
+            if ubm is not None:
+                self.dev.set_prior_full(ubm.w, ubm.mu, ubm.var)
+            self.dev.accumulate_full_device(self._acc_flags())
+            self.ll_history.append(self.dev.read_stats_full()["totLL"])
+            if ubm is None or o.tau == 0:
+                before = model.copy()
+                alive = self.dev.em_update_full(o.AdaptWeightBool, o.AdaptMeanBool, o.AdaptVarBool)
+                if alive == 0:  # all Gaussians discarded: keep the initial model
+                    model = (ubm if ubm is not None else before).copy()
+                    continue
+            else:
+                self.dev.map_update_full(o.tau, o.AdaptWeightBool, o.AdaptMeanBool, o.AdaptVarBool)
+            self._read(model)
+        return model
 
     def IterEM(self, model: GMModel, iters: int) -> GMModel:
         """``CModelAdapt::IterEM`` (OL_ModelAdapt.cpp:1276-1296) on the device."""
         o = self.opt
+        if model.full:
+            return self._iter_full(model, None, iters)
         self._ensure_features()
         self.dev.set_options(-1e20, 1e-4, o.min_var)
         self.dev.upload_model(model.w, model.mu, model.var)
@@ -150,6 +180,8 @@ class ModelAdapt:
     def IterMAP(self, model: GMModel, ubm: GMModel, iters: int) -> GMModel:
         """``CModelAdapt::IterMAP`` (OL_ModelAdapt.cpp:1298-1317) on the device."""
         o = self.opt
+        if model.full:
+            return self._iter_full(model, ubm, iters)
         self._ensure_features()
         for _ in range(iters):
             self._upload(model)
@@ -295,6 +327,8 @@ class ModelAdapt:
                 model = self.IterMAP(model, ubm, o.iterCountMAP)
             self._model = model
         elif o.adaptType == MLLR:
+            if ubm.full:
+                raise NotImplementedError("MLLR of full-covariance models is not built")
             self._W = self.IterW_MLLR(ubm, o.iterMLLR)
             if o.applyTransforms:
                 self._model = self.AdaptModelMLLR(ubm, self._W)

@@ -260,6 +260,7 @@ int gmm_destroy(gmm_handle h) {
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   drain_timers(c);
+  full_destroy(c);
   free_model(c);
   free_features(c);
   dfree(c, c->logits, c->logits_cap);

@@ -31,6 +31,8 @@ struct KernelTimer {
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;
 };
 
+struct FullModel;  // full-covariance model and statistics (full_kernels.cu)
+
 // ------------------------------------------------------------------ tensor-core model planes
 struct TcModel {
   int K = 0;            // padded contraction length (multiple of 16) of [x, x^2, 1, ...]
@@ -114,6 +116,9 @@ struct Ctx {
   long long em_graph_key[28] = {};
   double* ll_hist = nullptr;  // [ll_hist_cap + 1]: per-iteration total LL, then a counter
   int ll_hist_cap = 0;
+
+  // full-covariance model (own parameters and statistics; shares the features and scratch)
+  FullModel* full = nullptr;
 
   // timing
   bool profile = false;
@@ -234,6 +239,9 @@ int tc_build_model(Ctx* c, int D, int K, int Mact, int Mpad, long long plane_row
                    uint16_t* planes, int* comp_of_row);
 
 int sync(Ctx* c, const char* what);
+
+// Full-covariance model state (allocated on the first gmm_upload_model_full).
+void full_destroy(Ctx* c);
 
 }  // namespace gmm
 

@@ -28,17 +28,21 @@ class GMMStats:
     sums, the accumulated total log-likelihood and frame count."""
 
     def __init__(self, dim: int = 0, nummix: int = 0, allocMeans: bool = True,
-                 allocVars: bool = False):
+                 allocVars: bool = False, allocFullVars: bool = False):
         self._allocated = False
+        self._allM = self._allV = self._allFV = False
         if nummix:
-            self.alloc(dim, nummix, allocMeans, allocVars)
+            self.alloc(dim, nummix, allocMeans, allocVars, allocFullVars)
 
-    def alloc(self, dim, nummix, allocMeans=True, allocVars=False):
+    def alloc(self, dim, nummix, allocMeans=True, allocVars=False, allocFullVars=False):
+        """allocFullVars: second-order statistics of a full-covariance model, the packed upper
+        triangle [nummix, dim(dim+1)/2] (GMMStats' _varsize, OL_GMMStats.cpp:233-239)."""
         self._dim, self._M = dim, nummix
-        self._allM, self._allV = bool(allocMeans), bool(allocVars)
+        self._allM, self._allV = bool(allocMeans), bool(allocVars or allocFullVars)
+        self._allFV = bool(allocFullVars)
         self.n = np.zeros(nummix)
         self.F = np.zeros((nummix, dim))
-        self.S = np.zeros((nummix, dim))
+        self.S = np.zeros((nummix, dim * (dim + 1) // 2 if self._allFV else dim))
         self._totLogLike = 0.0
         self._totalAccSamples = 0
         self._allocated = True
@@ -85,12 +89,16 @@ class GMMStats:
         from . import formats
         n, F, S = formats.read_gmm_stats(filename, loadTxt)
         D = F.shape[1] if F is not None else (S.shape[1] if S is not None else 0)
-        self.alloc(D, len(n), F is not None, S is not None)
+        full = S is not None and F is not None and S.shape[1] != D
+        self.alloc(D, len(n), F is not None, S is not None and not full, full)
         self.n[:] = n
         if F is not None:
             self.F[:] = F
         if S is not None:
             self.S[:] = S
+
+    def hasFullCov(self):
+        return getattr(self, "_allFV", False)
 
     def __iadd__(self, o: "GMMStats"):
         if self._M != o._M:
@@ -133,14 +141,12 @@ class GMMStatsEstimatorGB300:
         return self._estimType
 
     def insertModel(self, model: GMModel, first: bool = True):
-        if model.var.ndim != 2:
-            raise ValueError("only diagonal-covariance models are supported")
         if first:
             self._models = []
         elif self._models and model.D != self._models[0].D:
             raise RuntimeError("Models (GMMs) have to have same dimensions")
         model.rearrange()
-        bad = (model.var[model.w > 0] < self._min_var)
+        bad = np.zeros(1, bool) if model.full else (model.var[model.w > 0] < self._min_var)
         if bad.any():
             raise RuntimeError("insertModel(): model contains very low variances "
                                f"[{float(model.var[model.w > 0][bad].min())}]!")
@@ -150,14 +156,18 @@ class GMMStatsEstimatorGB300:
     def setModelToBeUsed(self, n: int):
         self._model = self._models[n]
         self._dev.set_options(self._minLogLike, self._minGamma, self._min_var)
-        self._dev.upload_model(self._model.w, self._model.mu, self._model.var)
+        if self._model.full:  # GMM_ERR_MODEL (RuntimeError) if a covariance is not positive definite
+            self._dev.upload_model_full(self._model.w, self._model.mu, self._model.var)
+        else:
+            self._dev.upload_model(self._model.w, self._model.mu, self._model.var)
 
     def setAccFlags(self, mixProbsOnly, meanStats, varStats, varFull=False, auxStats=False):
-        if varFull or auxStats:
-            raise NotImplementedError("full-covariance and robust auxiliary statistics are "
-                                      "outside the diagonal hot path")
+        if auxStats:
+            raise NotImplementedError("robust auxiliary statistics are not built")
         self._flagsSet = True
-        self._fMixProbOnly, self._fMean, self._fVar = bool(mixProbsOnly), bool(meanStats), bool(varStats)
+        # full second-order statistics imply variance statistics (OL_GMMStatsEstimator.cpp:410-412)
+        self._fMixProbOnly, self._fMean = bool(mixProbsOnly), bool(meanStats)
+        self._fVar = bool(varStats) or bool(varFull)
 
     def resetAccFlags(self):
         self._flagsSet = False
@@ -195,14 +205,16 @@ class GMMStatsEstimatorGB300:
         if dim != self._model.D:
             raise RuntimeError("accumulateStats(): Inconsistent model & feature dimensions!")
         flags = self._flags(gmms)
+        full = self._model.full
         if not gmms.isAllocated():
-            gmms.alloc(dim, self._model.M, self._fMean or self._fVar, self._fVar)
+            gmms.alloc(dim, self._model.M, self._fMean or self._fVar, self._fVar and not full,
+                       self._fVar and full)
         self._features(vectors, NSamples, dim)
-        st = self._dev.accumulate(flags)
-        part = GMMStats(dim, self._model.M, gmms._allM, gmms._allV)
+        st = self._dev.accumulate_full(flags) if full else self._dev.accumulate(flags)
+        part = GMMStats(dim, self._model.M, gmms._allM, gmms._allV and not full, gmms._allV and full)
         part.n[:] = st["n"]
         part.F[:] = st["F"]
-        part.S[:] = st["S"]
+        part.S[:] = st["Sp"] if full else st["S"]
         part._totLogLike = st["totLL"]
         part._totalAccSamples = st["totN"]
         gmms += part
@@ -213,7 +225,7 @@ class GMMStatsEstimatorGB300:
         if dim != self._model.D:
             raise RuntimeError("compVecsLogLike(): Inconsistent model & feature dimensions!")
         self._features(vecs, NSamples, dim)
-        ll = self._dev.loglikes()
+        ll = self._dev.loglikes_full() if self._model.full else self._dev.loglikes()
         self._fNumStabilityTroubles = bool((ll == np.float32(self._minLogLike)).any())
         if outLogLikes is not None:
             outLogLikes[:NSamples] = ll

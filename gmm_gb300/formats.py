@@ -11,7 +11,9 @@
 * RAW features (``Param::LoadRaw``, lib_bmssr/param/OL_Param.cpp:358-463):
   int32 nsamples, int32 dimension, float32 data.
 
-Only diagonal covariances are in scope; a full-covariance file raises ``ValueError``.
+Full-covariance models (``GMModel(dim, nummix, true)``: Var holds D x D per component) carry
+``var`` as [M, D, D]: text weight lines end in " F" and each covariance row is written as its
+diagonal element followed by the D row values; the binary dimension is stored negated.
 """
 from __future__ import annotations
 
@@ -45,6 +47,11 @@ class GMModel:
     def D(self) -> int:
         return int(self.mu.shape[1])
 
+    @property
+    def full(self) -> bool:
+        """Full covariances (var is [M, D, D])."""
+        return self.var.ndim == 3
+
     def copy(self) -> "GMModel":
         return GMModel(self.w.copy(), self.mu.copy(), self.var.copy(), self.norm.copy())
 
@@ -77,13 +84,17 @@ def read_gmm_txt(path: str) -> GMModel:
     norm = np.array([float(lines[i + k]) for k in range(D)], np.float32); i += D
     M = int(lines[i]); i += 1
     w, mu, var = [], [], []
+    full = False
     for _ in range(M):
         head = lines[i].split()
-        if len(head) > 1 and head[1] == "F":
-            raise ValueError("full-covariance models are outside the diagonal hot path")
+        full = len(head) > 1 and head[1] == "F"
         w.append(float(head[0])); i += 2
         mu.append([float(lines[i + k]) for k in range(D)]); i += D + 1
-        var.append([float(lines[i + k]) for k in range(D)]); i += D + 1
+        if full:  # each row: the diagonal element, then the D values of the row
+            var.append([[float(v) for v in lines[i + k].split()[1:D + 1]] for k in range(D)])
+        else:
+            var.append([float(lines[i + k]) for k in range(D)])
+        i += D + 1
     return GMModel(np.array(w), np.array(mu), np.array(var), norm)
 
 
@@ -95,12 +106,16 @@ def write_gmm_txt(path: str, g: GMModel) -> None:
         keep = [m for m in range(g.M) if g.w[m] != 0]
         f.write(f"{len(keep)}\n")
         for m in keep:
-            f.write("%15e\n\n" % g.w[m])
+            f.write(("%15e F\n\n" if g.full else "%15e\n\n") % g.w[m])
             for v in g.mu[m]:
                 f.write("%15e\n" % v)
             f.write("\n")
-            for v in g.var[m]:
-                f.write("%15e\n" % v)
+            if g.full:
+                for k in range(g.D):
+                    f.write("%15e" % g.var[m, k, k] + "".join(" %15e" % v for v in g.var[m, k]) + "\n")
+            else:
+                for v in g.var[m]:
+                    f.write("%15e\n" % v)
             f.write("\n")
 
 
@@ -110,21 +125,23 @@ def read_gmm_bin(path: str) -> GMModel:
     if buf[:9] != b"GMM-DB-VN":
         raise ValueError("not a GMM-DB-VN file")
     (D,) = struct.unpack_from("<h", buf, 9)
-    if D < 0:
-        raise ValueError("full-covariance models are outside the diagonal hot path")
+    full = D < 0
+    D = abs(D)
+    V = D * D if full else D
     off = 11
     norm = np.frombuffer(buf, "<f4", D, off); off += 4 * D
     (M,) = struct.unpack_from("<h", buf, off); off += 2
     w = np.frombuffer(buf, "<f4", M, off); off += 4 * M
-    body = np.frombuffer(buf, "<f4", 2 * M * D, off).reshape(M, 2, D)
-    return GMModel(w.copy(), body[:, 0].copy(), body[:, 1].copy(), norm.copy())
+    body = np.frombuffer(buf, "<f4", M * (D + V), off).reshape(M, D + V)
+    var = body[:, D:].reshape(M, D, D) if full else body[:, D:]
+    return GMModel(w.copy(), body[:, :D].copy(), var.copy(), norm.copy())
 
 
 def write_gmm_bin(path: str, g: GMModel) -> None:
     keep = [m for m in range(g.M) if g.w[m] > 0]
     with open(path, "wb") as f:
         f.write(b"GMM-DB-VN")
-        f.write(struct.pack("<h", g.D))
+        f.write(struct.pack("<h", -g.D if g.full else g.D))
         f.write(np.asarray(g.norm, "<f4").tobytes())
         f.write(struct.pack("<h", len(keep)))
         f.write(np.asarray(g.w[keep], "<f4").tobytes())
@@ -211,7 +228,9 @@ def write_gmm_stats(path: str, txt: bool, n, F=None, S=None, dtype=np.float64) -
     n = np.asarray(n, dtype)
     M = len(n)
     D = np.asarray(F).shape[1] if F is not None else (np.asarray(S).shape[1] if S is not None else 0)
-    hdr = [1, int(F is not None), int(S is not None), 0, D, D if S is not None else 0, M]
+    varsize = np.asarray(S).shape[1] if S is not None else 0
+    full = int(S is not None and varsize != D)  # packed full second-order statistics
+    hdr = [1, int(F is not None), int(S is not None), full, D, varsize, M]
     if txt:
         with open(path, "w") as f:
             f.write(" ".join(map(str, hdr)) + "\n\n")
@@ -234,7 +253,8 @@ def write_gmm_stats(path: str, txt: bool, n, F=None, S=None, dtype=np.float64) -
 
 
 def read_gmm_stats(path: str, txt: bool, dtype=np.float64):
-    """``GMMStats<T>::load`` (OL_GMMStats.cpp:493-655): returns (n, F or None, S or None)."""
+    """``GMMStats<T>::load`` (OL_GMMStats.cpp:493-655): returns (n, F or None, S or None); S is
+    [M, varsize] (the packed upper triangle for full-covariance statistics)."""
     if txt:
         with open(path) as f:
             tok = f.read().split()
@@ -246,8 +266,6 @@ def read_gmm_stats(path: str, txt: bool, dtype=np.float64):
         hdr = list(np.frombuffer(buf, "<i4", 7))
         vals = np.frombuffer(buf, dtype, offset=28).astype(np.float64)
     mp, mean, var, full, D, varsize, M = hdr
-    if full:
-        raise ValueError("full-covariance statistics are outside the diagonal hot path")
     rec = int(mp) + int(mean) * D + int(var) * varsize
     body = vals[:M * rec].reshape(M, rec)
     n = body[:, 0] if mp else None

@@ -28,12 +28,17 @@ void fail(const std::string& m) { throw std::runtime_error(m); }
 
 // ------------------------------------------------------------------ GMModel
 
-GMModel::GMModel(int dim, int nummix)
-    : dim_(dim), norm_((size_t)dim, 1.0f), w_((size_t)nummix, 0.0f), mu_((size_t)nummix * dim, 0.0f),
-      var_((size_t)nummix * dim, reset_var()) {}
+GMModel::GMModel(int dim, int nummix, bool full_cov)
+    : dim_(dim), full_(full_cov), norm_((size_t)dim, 1.0f), w_((size_t)nummix, 0.0f),
+      mu_((size_t)nummix * dim, 0.0f),
+      var_((size_t)nummix * (full_cov ? dim * dim : dim), full_cov ? 0.0f : reset_var()) {
+  if (full_cov)
+    for (int m = 0; m < nummix; ++m)
+      for (int d = 0; d < dim; ++d) var_[((size_t)m * dim + d) * dim + d] = 1.0f;
+}
 
 int GMModel::RearrangeMixtures() {
-  const int M = GetNumberOfMixtures();
+  const int M = GetNumberOfMixtures(), V = DimVar();
   std::vector<int> order((size_t)M);
   int nz = 0, z = 1;
   for (int m = 0; m < M; ++m) {
@@ -45,7 +50,7 @@ int GMModel::RearrangeMixtures() {
     const int m = order[(size_t)k];
     w[(size_t)k] = w_[(size_t)m];
     std::memcpy(&mu[(size_t)k * dim_], &mu_[(size_t)m * dim_], sizeof(float) * dim_);
-    std::memcpy(&var[(size_t)k * dim_], &var_[(size_t)m * dim_], sizeof(float) * dim_);
+    std::memcpy(&var[(size_t)k * V], &var_[(size_t)m * V], sizeof(float) * V);
   }
   w_.swap(w);
   mu_.swap(mu);
@@ -73,18 +78,31 @@ void GMModel::Load(const std::string& path, bool txt) {
     for (int d = 0; d < dim_; ++d) norm_[(size_t)d] = (float)num(i++);
     const int M = (int)num(i++);
     w_.assign((size_t)M, 0.0f);
-    mu_.assign((size_t)M * dim_, 0.0f);
-    var_.assign((size_t)M * dim_, 0.0f);
+    mu_.clear();
+    var_.clear();
     for (int m = 0; m < M; ++m) {
       std::istringstream head(lines.at(i));
       std::string tok, kind;
       head >> tok >> kind;
-      if (kind == "F") fail("GMModel::Load(): full-covariance models are outside the diagonal hot path");
+      full_ = kind == "F";
       w_[(size_t)m] = (float)std::stod(tok);
       i += 2;
-      for (int d = 0; d < dim_; ++d) mu_[(size_t)m * dim_ + d] = (float)num(i + d);
+      for (int d = 0; d < dim_; ++d) mu_.push_back((float)num(i + d));
       i += dim_ + 1;
-      for (int d = 0; d < dim_; ++d) var_[(size_t)m * dim_ + d] = (float)num(i + d);
+      if (full_) {  // each row: the diagonal element, then the D values of the row
+        for (int r = 0; r < dim_; ++r) {
+          if (i + r >= lines.size()) fail("GMModel::Load(): truncated file " + path);
+          std::istringstream row(lines[i + r]);
+          double v = 0.0;
+          row >> v;
+          for (int c = 0; c < dim_; ++c) {
+            if (!(row >> v)) fail("GMModel::Load(): short covariance row in " + path);
+            var_.push_back((float)v);
+          }
+        }
+      } else {
+        for (int d = 0; d < dim_; ++d) var_.push_back((float)num(i + d));
+      }
       i += dim_ + 1;
     }
   } else {
@@ -95,18 +113,19 @@ void GMModel::Load(const std::string& path, bool txt) {
     f.read(tag, 9);
     if (!f || std::memcmp(tag, "GMM-DB-VN", 9) != 0) fail("GMModel::Load(): not a GMM-DB-VN file: " + path);
     f.read(reinterpret_cast<char*>(&D), 2);
-    if (D < 0) fail("GMModel::Load(): full-covariance models are outside the diagonal hot path");
-    dim_ = D;
-    norm_.assign((size_t)D, 0.0f);
-    f.read(reinterpret_cast<char*>(norm_.data()), sizeof(float) * D);
+    full_ = D < 0;
+    dim_ = full_ ? -D : D;
+    const int V = DimVar();
+    norm_.assign((size_t)dim_, 0.0f);
+    f.read(reinterpret_cast<char*>(norm_.data()), sizeof(float) * dim_);
     f.read(reinterpret_cast<char*>(&M), 2);
     w_.assign((size_t)M, 0.0f);
-    mu_.assign((size_t)M * D, 0.0f);
-    var_.assign((size_t)M * D, 0.0f);
+    mu_.assign((size_t)M * dim_, 0.0f);
+    var_.assign((size_t)M * V, 0.0f);
     f.read(reinterpret_cast<char*>(w_.data()), sizeof(float) * M);
     for (int m = 0; m < M; ++m) {
-      f.read(reinterpret_cast<char*>(&mu_[(size_t)m * D]), sizeof(float) * D);
-      f.read(reinterpret_cast<char*>(&var_[(size_t)m * D]), sizeof(float) * D);
+      f.read(reinterpret_cast<char*>(&mu_[(size_t)m * dim_]), sizeof(float) * dim_);
+      f.read(reinterpret_cast<char*>(&var_[(size_t)m * V]), sizeof(float) * V);
     }
     if (!f) fail("GMModel::Load(): truncated file " + path);
   }
@@ -116,6 +135,7 @@ void GMModel::Save(const std::string& path, bool txt) const {
   std::vector<int> keep;
   for (int m = 0; m < GetNumberOfMixtures(); ++m)
     if (w_[(size_t)m] != 0.0f) keep.push_back(m);
+  const int V = DimVar();
   if (txt) {
     FILE* f = std::fopen(path.c_str(), "w");
     if (!f) fail("GMModel::Save(): cannot open " + path);
@@ -123,17 +143,26 @@ void GMModel::Save(const std::string& path, bool txt) const {
     for (float v : norm_) std::fprintf(f, "%15e\n", v);
     std::fprintf(f, "%d\n", (int)keep.size());
     for (int m : keep) {
-      std::fprintf(f, "%15e\n\n", w_[(size_t)m]);
+      std::fprintf(f, full_ ? "%15e F\n\n" : "%15e\n\n", w_[(size_t)m]);
       for (int d = 0; d < dim_; ++d) std::fprintf(f, "%15e\n", mu_[(size_t)m * dim_ + d]);
       std::fprintf(f, "\n");
-      for (int d = 0; d < dim_; ++d) std::fprintf(f, "%15e\n", var_[(size_t)m * dim_ + d]);
+      const float* C = &var_[(size_t)m * V];
+      if (full_) {
+        for (int r = 0; r < dim_; ++r) {
+          std::fprintf(f, "%15e", C[(size_t)r * dim_ + r]);
+          for (int c = 0; c < dim_; ++c) std::fprintf(f, " %15e", C[(size_t)r * dim_ + c]);
+          std::fprintf(f, "\n");
+        }
+      } else {
+        for (int d = 0; d < dim_; ++d) std::fprintf(f, "%15e\n", C[d]);
+      }
       std::fprintf(f, "\n");
     }
     std::fclose(f);
   } else {
     std::ofstream f(path, std::ios::binary);
     if (!f) fail("GMModel::Save(): cannot open " + path);
-    const int16_t D = (int16_t)dim_, M = (int16_t)keep.size();
+    const int16_t D = (int16_t)(full_ ? -dim_ : dim_), M = (int16_t)keep.size();
     f.write("GMM-DB-VN", 9);
     f.write(reinterpret_cast<const char*>(&D), 2);
     f.write(reinterpret_cast<const char*>(norm_.data()), sizeof(float) * dim_);
@@ -141,34 +170,36 @@ void GMModel::Save(const std::string& path, bool txt) const {
     for (int m : keep) f.write(reinterpret_cast<const char*>(&w_[(size_t)m]), sizeof(float));
     for (int m : keep) {
       f.write(reinterpret_cast<const char*>(&mu_[(size_t)m * dim_]), sizeof(float) * dim_);
-      f.write(reinterpret_cast<const char*>(&var_[(size_t)m * dim_]), sizeof(float) * dim_);
+      f.write(reinterpret_cast<const char*>(&var_[(size_t)m * V]), sizeof(float) * V);
     }
   }
 }
 
 // ------------------------------------------------------------------ GMMStats
 
-void GMMStats::alloc(int M_, int D_) {
+void GMMStats::alloc(int M_, int D_, bool full_) {
   M = M_;
   D = D_;
+  full = full_;
   n.assign((size_t)M, 0.0);
   F.assign((size_t)M * D, 0.0);
-  S.assign((size_t)M * D, 0.0);
+  S.assign((size_t)M * varsize(), 0.0);
   totLogLike = 0.0;
   totalAccSamples = 0;
 }
 
-void GMMStats::reset() { alloc(M, D); }
+void GMMStats::reset() { alloc(M, D, full); }
 
 namespace {
 
 // The header and records of the GMMStats file layout, for T = double or float.
 template <typename T>
 void write_stats(const std::string& path, bool txt, int dim, int nummix, const T* mp, const T* mean,
-                 const T* var) {
+                 const T* var, int varsize) {
   FILE* f = std::fopen(path.c_str(), txt ? "w" : "wb");
   if (!f) fail("save(): Unable to open file " + path);
-  const int32_t hdr[7] = {1, mean != nullptr, var != nullptr, 0, dim, var ? dim : 0, nummix};
+  const int32_t hdr[7] = {1, mean != nullptr, var != nullptr, var != nullptr && varsize != dim, dim,
+                          var ? varsize : 0, nummix};
   bool ok = true;
   if (txt) {
     ok = std::fprintf(f, "%d %d %d %d %d %d %d\n\n", hdr[0], hdr[1], hdr[2], hdr[3], hdr[4], hdr[5], hdr[6]) > 0;
@@ -179,7 +210,7 @@ void write_stats(const std::string& path, bool txt, int dim, int nummix, const T
         ok = ok && std::fputc('\n', f) != EOF;
       }
       if (var) {
-        for (int d = 0; ok && d < dim; ++d) ok = std::fprintf(f, " %g", (double)var[(size_t)m * dim + d]) > 0;
+        for (int d = 0; ok && d < varsize; ++d) ok = std::fprintf(f, " %g", (double)var[(size_t)m * varsize + d]) > 0;
         ok = ok && std::fputc('\n', f) != EOF;
       }
       ok = ok && std::fputc('\n', f) != EOF;
@@ -189,7 +220,7 @@ void write_stats(const std::string& path, bool txt, int dim, int nummix, const T
     for (int m = 0; ok && m < nummix; ++m) {
       ok = std::fwrite(&mp[m], sizeof(T), 1, f) == 1;
       if (ok && mean) ok = std::fwrite(&mean[(size_t)m * dim], sizeof(T), (size_t)dim, f) == (size_t)dim;
-      if (ok && var) ok = std::fwrite(&var[(size_t)m * dim], sizeof(T), (size_t)dim, f) == (size_t)dim;
+      if (ok && var) ok = std::fwrite(&var[(size_t)m * varsize], sizeof(T), (size_t)varsize, f) == (size_t)varsize;
     }
   }
   if (std::fclose(f) != 0 || !ok) fail("save(): Exception writing file " + path);
@@ -198,7 +229,7 @@ void write_stats(const std::string& path, bool txt, int dim, int nummix, const T
 }  // namespace
 
 void GMMStats::save(const std::string& path, bool txt) const {
-  write_stats<double>(path, txt, D, M, n.data(), F.data(), S.data());
+  write_stats<double>(path, txt, D, M, n.data(), F.data(), S.data(), varsize());
 }
 
 void GMMStats::load(const std::string& path, bool txt) {
@@ -211,12 +242,12 @@ void GMMStats::load(const std::string& path, bool txt) {
     f.read(reinterpret_cast<char*>(h), sizeof h);
   }
   if (!f) fail("load(): Exception reading file " + path);
-  if (h[3]) fail("load(): full-covariance statistics are outside the diagonal hot path");
-  alloc(h[6], h[4]);
+  alloc(h[6], h[4], h[3] != 0);
   const int varsize = h[5];
+  if (h[2] && varsize != this->varsize()) fail("load(): inconsistent statistics sizes in " + path);
   for (int m = 0; m < M; ++m) {
     double* Fm = &F[(size_t)m * D];
-    double* Sm = &S[(size_t)m * D];
+    double* Sm = &S[(size_t)m * varsize];
     if (txt) {
       if (h[0]) f >> n[(size_t)m];
       if (h[1])
@@ -234,7 +265,7 @@ void GMMStats::load(const std::string& path, bool txt) {
 
 void save_stats_float(const std::string& path, bool txt, int dim, int nummix, const float* mixprob,
                       const float* mean, const float* var) {
-  write_stats<float>(path, txt, dim, nummix, mixprob, mean, var);
+  write_stats<float>(path, txt, dim, nummix, mixprob, mean, var, dim);
 }
 
 // ------------------------------------------------------------------ estimator
@@ -253,8 +284,13 @@ void GMMStatsEstimatorGB300::check(int rc) const {
 void GMMStatsEstimatorGB300::insertModel(GMModel& model, bool) {
   model.RearrangeMixtures();
   check(gmm_set_options(h_, _minLogLike, _minGamma, _min_var));
-  check(gmm_upload_model(h_, model.GetNumberOfMixtures(), model.GetDimension(), model.weights().data(),
-                         model.means().data(), model.vars().data()));
+  full_ = model.GetFullCovStatus();
+  if (full_)
+    check(gmm_upload_model_full(h_, model.GetNumberOfMixtures(), model.GetDimension(), model.weights().data(),
+                                model.means().data(), model.vars().data()));
+  else
+    check(gmm_upload_model(h_, model.GetNumberOfMixtures(), model.GetDimension(), model.weights().data(),
+                           model.means().data(), model.vars().data()));
   M_ = model.GetNumberOfMixtures();
 }
 
@@ -274,28 +310,30 @@ void GMMStatsEstimatorGB300::accumulateStatsMT(const float* vecs, unsigned N, un
   if (M_ == 0) fail("accumulateStatsMT(): None model inserted!");
   upload(vecs, N, dim);
   // the estimator allocates the statistics when the caller did not (OL_GMMStatsEstimator.cpp:1108-1112)
-  if (gmms.M == 0) gmms.alloc(M_, (int)dim);
-  if (gmms.M != M_ || gmms.D != (int)dim) fail("accumulateStatsMT(): statistics and model sizes differ");
+  if (gmms.M == 0) gmms.alloc(M_, (int)dim, full_);
+  if (gmms.M != M_ || gmms.D != (int)dim || gmms.full != full_)
+    fail("accumulateStatsMT(): statistics and model sizes differ");
   const int M = M_;
   std::vector<double> n, F, S;
   double tl = 0.0;
   long long tn = 0;
   n.assign((size_t)M, 0.0);
   F.assign((size_t)M * dim, 0.0);
-  S.assign((size_t)M * dim, 0.0);
-  check(gmm_accumulate(h_, flags_, n.data(), F.data(), S.data(), &tl, &tn));
+  S.assign((size_t)M * gmms.varsize(), 0.0);
+  if (full_)  // full second-order statistics imply variance statistics (OL_GMMStatsEstimator.cpp:410-412)
+    check(gmm_accumulate_full(h_, flags_ | GMM_ACC_VAR, n.data(), F.data(), S.data(), &tl, &tn));
+  else
+    check(gmm_accumulate(h_, flags_, n.data(), F.data(), S.data(), &tl, &tn));
   for (size_t k = 0; k < n.size(); ++k) gmms.n[k] += n[k];
-  for (size_t k = 0; k < F.size(); ++k) {
-    gmms.F[k] += F[k];
-    gmms.S[k] += S[k];
-  }
+  for (size_t k = 0; k < F.size(); ++k) gmms.F[k] += F[k];
+  for (size_t k = 0; k < S.size(); ++k) gmms.S[k] += S[k];
   gmms.totLogLike += tl;
   gmms.totalAccSamples += tn;
 }
 
 void GMMStatsEstimatorGB300::compVecsLogLikeMT(const float* vecs, unsigned N, unsigned dim, float* out) {
   upload(vecs, N, dim);
-  check(gmm_loglikes(h_, out));
+  check(full_ ? gmm_loglikes_full(h_, out) : gmm_loglikes(h_, out));
 }
 
 // ------------------------------------------------------------------ ModelAdapt
@@ -346,11 +384,47 @@ void ModelAdapt::upload_model(GMModel& m) {
     uploaded_ = true;
   }
   check(gmm_set_options(h_, -1e20f, 1e-4f, o_.min_var));
-  check(gmm_upload_model(h_, m.GetNumberOfMixtures(), m.GetDimension(), m.weights().data(), m.means().data(),
-                         m.vars().data()));
+  full_ = m.GetFullCovStatus();
+  if (full_ && !files_.empty()) fail("AdaptModel(): file-by-file accumulation supports diagonal models only");
+  if (full_)
+    check(gmm_upload_model_full(h_, m.GetNumberOfMixtures(), m.GetDimension(), m.weights().data(),
+                                m.means().data(), m.vars().data()));
+  else
+    check(gmm_upload_model(h_, m.GetNumberOfMixtures(), m.GetDimension(), m.weights().data(), m.means().data(),
+                           m.vars().data()));
+}
+
+// The device-side M-step / readback entry points of the current model's family.
+void ModelAdapt::set_prior(const GMModel& u) {
+  check(full_ ? gmm_set_prior_full(h_, u.weights().data(), u.means().data(), u.vars().data())
+              : gmm_set_prior(h_, u.weights().data(), u.means().data(), u.vars().data()));
+}
+
+double ModelAdapt::total_ll() {
+  double tl = 0.0;
+  long long tn = 0;
+  check(full_ ? gmm_read_stats_full(h_, nullptr, nullptr, nullptr, &tl, &tn)
+              : gmm_read_stats(h_, nullptr, nullptr, nullptr, &tl, &tn));
+  return tl;
+}
+
+int ModelAdapt::em_update() {
+  int alive = 0;
+  check(full_ ? gmm_em_update_full(h_, o_.AdaptWeightBool, o_.AdaptMeanBool, o_.AdaptVarBool, &alive)
+              : gmm_em_update(h_, o_.AdaptWeightBool, o_.AdaptMeanBool, o_.AdaptVarBool, &alive));
+  return alive;
+}
+
+void ModelAdapt::read_model(GMModel& m) {
+  check(full_ ? gmm_read_model_full(h_, m.weights().data(), m.means().data(), m.vars().data())
+              : gmm_read_model(h_, m.weights().data(), m.means().data(), m.vars().data()));
 }
 
 void ModelAdapt::estep(int flags) {
+  if (full_) {  // a full model always gathers full second-order statistics
+    check(gmm_accumulate_full_device(h_, flags | GMM_ACC_VAR));
+    return;
+  }
   if (files_.empty()) {
     check(gmm_accumulate_device(h_, flags));
     return;
@@ -362,7 +436,7 @@ void ModelAdapt::estep(int flags) {
 }
 
 void ModelAdapt::IterEM(GMModel& model, int iters) {
-  if (files_.empty()) {
+  if (files_.empty() && !model.GetFullCovStatus()) {
     upload_model(model);  // gmm_em_iterate rearranges on the device each iteration, as insertModel
     std::vector<double> ll((size_t)std::max(iters, 1));
     int alive = 0;
@@ -371,19 +445,16 @@ void ModelAdapt::IterEM(GMModel& model, int iters) {
     check(gmm_read_model(h_, model.weights().data(), model.means().data(), model.vars().data()));
     return;
   }
-  // file by file: one pass over the files per iteration (IterEM, OL_ModelAdapt.cpp:1276-1296)
+  // file by file, or a full-covariance model: insertModel + E-step + UpdateModelEM per iteration
+  // (IterEM, OL_ModelAdapt.cpp:1276-1296); all components killed -> the model before the update
   const int flags = GMM_ACC_MEAN | GMM_ACC_VAR;
   for (int it = 0; it < iters; ++it) {
     model.RearrangeMixtures();
     upload_model(model);
     estep(flags);
-    double tl = 0.0;
-    long long tn = 0;
-    check(gmm_read_stats(h_, nullptr, nullptr, nullptr, &tl, &tn));
-    ll_history.push_back(tl);
-    int alive = 0;
-    check(gmm_em_update(h_, o_.AdaptWeightBool, o_.AdaptMeanBool, o_.AdaptVarBool, &alive));
-    check(gmm_read_model(h_, model.weights().data(), model.means().data(), model.vars().data()));
+    ll_history.push_back(total_ll());
+    if (em_update() == 0) continue;
+    read_model(model);
   }
 }
 
@@ -393,27 +464,24 @@ void ModelAdapt::IterMAP(GMModel& model, const GMModel& ubm, int iters) {
   for (int it = 0; it < iters; ++it) {
     model.RearrangeMixtures();
     upload_model(model);
-    check(gmm_set_prior(h_, ubm.weights().data(), ubm.means().data(), ubm.vars().data()));
+    set_prior(ubm);
     estep(flags);
-    double tl = 0.0;
-    long long tn = 0;
-    check(gmm_read_stats(h_, nullptr, nullptr, nullptr, &tl, &tn));
-    ll_history.push_back(tl);
+    ll_history.push_back(total_ll());
     if (o_.tau == 0) {
-      int alive = 0;
-      check(gmm_em_update(h_, o_.AdaptWeightBool, o_.AdaptMeanBool, o_.AdaptVarBool, &alive));
-      if (alive == 0) {
+      if (em_update() == 0) {
         model = ubm;
         continue;
       }
     } else {
-      check(gmm_map_update(h_, o_.tau, o_.AdaptWeightBool, o_.AdaptMeanBool, o_.AdaptVarBool));
+      check(full_ ? gmm_map_update_full(h_, o_.tau, o_.AdaptWeightBool, o_.AdaptMeanBool, o_.AdaptVarBool)
+                  : gmm_map_update(h_, o_.tau, o_.AdaptWeightBool, o_.AdaptMeanBool, o_.AdaptVarBool));
     }
-    check(gmm_read_model(h_, model.weights().data(), model.means().data(), model.vars().data()));
+    read_model(model);
   }
 }
 
 std::vector<double> ModelAdapt::ComputeW_MLLR(GMModel& model, const GMModel& ubm) {
+  if (model.GetFullCovStatus()) fail("ComputeW_MLLR(): MLLR of full-covariance models is not built");
   model.RearrangeMixtures();
   upload_model(model);
   check(gmm_set_prior(h_, ubm.weights().data(), ubm.means().data(), ubm.vars().data()));
@@ -541,6 +609,8 @@ void ModelAdapt::splitMultipleGaussians(GMModel& model) {
 
 void ModelAdapt::TrainFromScratch(int nummix, const GMModel* init_model) {
   if (N_ <= 3) fail("TrainFromScratch(): Not enough data to model training.");
+  if (init_model && init_model->GetFullCovStatus())
+    fail("TrainFromScratch(): the full-covariance split is not built");
   const int D = D_;
   GMModel init;
   int max_iter = nummix;
@@ -647,9 +717,15 @@ void ModelAdapt::Save(const std::string& FileName, bool save_txt, bool save_in_s
   if (trained_) {
     if (!save_in_stat_form)
       model_.Save(FileName, save_txt);
-    else  // every component slot, zero weights included
-      save_stats_float(FileName, save_txt, model_.GetDimension(), model_.GetNumberOfMixtures(),
-                       model_.weights().data(), model_.means().data(), model_.vars().data());
+    else {  // every component slot, zero weights included; variances = the diagonal (GetMixtureVarDiag)
+      const int D = model_.GetDimension(), M = model_.GetNumberOfMixtures();
+      std::vector<float> diag((size_t)M * D);
+      for (int m = 0; m < M; ++m)
+        for (int d = 0; d < D; ++d)
+          diag[(size_t)m * D + d] = model_.GetFullCovStatus() ? model_.GetMixtureVar(m)[(size_t)d * D + d]
+                                                              : model_.GetMixtureVar(m)[d];
+      save_stats_float(FileName, save_txt, D, M, model_.weights().data(), model_.means().data(), diag.data());
+    }
   }
 }
 

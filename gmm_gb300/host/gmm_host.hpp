@@ -15,20 +15,24 @@
 
 namespace gmmgb {
 
-// Diagonal-covariance GMM (weights [M], means [M][D], variances [M][D]) with the file's
-// normalisation coefficients.
+// GMM with diagonal (var [M][D]) or full (var [M][D][D], row-major) covariances, with the
+// file's normalisation coefficients.
 class GMModel {
  public:
   GMModel() = default;
-  GMModel(int dim, int nummix);  // zero weights, components in GMMMixture::Reset state
+  // zero weights, components in GMMMixture::Reset state (mean 0; variances of bytes 0x01 for a
+  // diagonal model, the identity for a full one; OL_GMModel.cpp:73-83)
+  GMModel(int dim, int nummix, bool full_cov = false);
   int GetDimension() const { return dim_; }
   int GetNumberOfMixtures() const { return (int)w_.size(); }
+  bool GetFullCovStatus() const { return full_; }
+  int DimVar() const { return full_ ? dim_ * dim_ : dim_; }
   float GetMixtureWeight(int m) const { return w_[(size_t)m]; }
   void SetMixWeight(int m, float w) { w_[(size_t)m] = w; }
   float* GetMixtureMean(int m) { return &mu_[(size_t)m * dim_]; }
-  float* GetMixtureVar(int m) { return &var_[(size_t)m * dim_]; }
+  float* GetMixtureVar(int m) { return &var_[(size_t)m * DimVar()]; }
   const float* GetMixtureMean(int m) const { return &mu_[(size_t)m * dim_]; }
-  const float* GetMixtureVar(int m) const { return &var_[(size_t)m * dim_]; }
+  const float* GetMixtureVar(int m) const { return &var_[(size_t)m * DimVar()]; }
   std::vector<float>& weights() { return w_; }
   std::vector<float>& means() { return mu_; }
   std::vector<float>& vars() { return var_; }
@@ -39,28 +43,33 @@ class GMModel {
   // k-th zero-weight component goes to slot M-1-k. Returns the number of zero-weight components.
   int RearrangeMixtures();
   // GMModel::Load / Save (text: WriteTXT / ReadTXT, OL_GMModel.cpp:475-547, 627-753; binary
-  // "GMM-DB-VN": WriteBIN / ReadBIN, :551-624, 757-853). Zero-weight components are not saved.
+  // "GMM-DB-VN": WriteBIN / ReadBIN, :551-624, 757-853; a full model's text weight line ends in
+  // " F" and its binary dimension is negated). Zero-weight components are not saved.
   void Load(const std::string& path, bool txt);
   void Save(const std::string& path, bool txt) const;
 
  private:
   int dim_ = 0;
+  bool full_ = false;
   std::vector<float> norm_, w_, mu_, var_;
 };
 
-// GMMStats<double>: occupation n [M], first order F [M][D], second order S [M][D], totals.
+// GMMStats<double>: occupation n [M], first order F [M][D], second order S [M][varsize] with
+// varsize = D, or D(D+1)/2 (the packed upper triangle in row order) for a full-covariance model.
 // The estimator only ever adds into it (OL_GMMStats.cpp:99-145).
 struct GMMStats {
   int M = 0, D = 0;
+  bool full = false;
   std::vector<double> n, F, S;
   double totLogLike = 0.0;
   long long totalAccSamples = 0;
-  void alloc(int M_, int D_);
+  int varsize() const { return full ? D * (D + 1) / 2 : D; }
+  void alloc(int M_, int D_, bool full_ = false);
   void reset();
   // GMMStats<double>::save / load (OL_GMMStats.cpp:493-778): binary = seven int32 (mixProb,
-  // mean, var and full-var flags, dim, varsize, nummix) then per component n, F[D], S[D] as
-  // doubles; text = the same header line, a blank line, then per component "n", " F..", " S..",
-  // blank, in ostream's default 6-digit format. Diagonal statistics only.
+  // mean, var and full-var flags, dim, varsize, nummix) then per component n, F[D], S[varsize]
+  // as doubles; text = the same header line, a blank line, then per component "n", " F..",
+  // " S..", blank, in ostream's default 6-digit format.
   void save(const std::string& path, bool txt) const;
   void load(const std::string& path, bool txt);
 };
@@ -83,7 +92,7 @@ class GMMStatsEstimatorGB300 {
   float _minLogLike = -1e20f, _minGamma = 1e-4f, _min_var = 1e-6f;
 
   // insertModel (OL_GMMStatsEstimator.cpp:234-313): rearranges `model` in place, checks the
-  // variances and makes the model resident.
+  // variances (a full model: factors its covariances) and makes the model resident.
   void insertModel(GMModel& model, bool first = true);
   void setAccFlags(bool mixProbsOnly, bool mean, bool var);
   void setSameDataFlag() { same_data_ = true; }
@@ -98,6 +107,7 @@ class GMMStatsEstimatorGB300 {
   void upload(const float* vecs, unsigned N, unsigned dim);
   gmm_handle h_ = nullptr;
   int M_ = 0;
+  bool full_ = false;
   int flags_ = GMM_ACC_MEAN | GMM_ACC_VAR;
   bool same_data_ = false;
   const float* last_ = nullptr;
@@ -134,7 +144,8 @@ class ModelAdapt {
   // AdaptModel (OL_ModelAdapt.cpp:1163-1226): MAP (IterEM then IterMAP) or MLLR.
   void AdaptModel(const GMModel& ubm);
   // TrainFromScratch (OL_ModelAdapt.cpp:667-821), diagonal covariances; `init` (optional) is the
-  // model the splitting starts from instead of the global Gaussian.
+  // model the splitting starts from instead of the global Gaussian. (The full-covariance split
+  // along the leading eigenvector is not built.)
   void TrainFromScratch(int nummix, const GMModel* init = nullptr);
   const GMModel& GetModel() const { return model_; }
   const std::vector<double>& GetW() const { return W_; }  // MLLR transform D x (D+1)
@@ -150,6 +161,10 @@ class ModelAdapt {
 
  private:
   void upload_model(GMModel& m);
+  void set_prior(const GMModel& ubm);
+  double total_ll();
+  int em_update();
+  void read_model(GMModel& m);
   void estep(int flags);
   void check(int rc) const;
   void IterEM(GMModel& model, int iters);
@@ -162,7 +177,7 @@ class ModelAdapt {
   std::vector<float> X_;
   long long N_ = 0;
   int D_ = 0;
-  bool uploaded_ = false, trained_ = false;
+  bool uploaded_ = false, trained_ = false, full_ = false;
   std::vector<std::string> files_;
   int prm_type_ = 0;
   unsigned dwnsmp_ = 1;

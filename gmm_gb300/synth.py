@@ -52,6 +52,38 @@ def sample_gmm(seed: int, w, mu, var, N: int, chunk: int = 1 << 20) -> np.ndarra
     return X
 
 
+def generator_gmm_full(seed: int, M: int, D: int, mean_sd: float = 2.0, corr: float = 0.6):
+    """Random full-covariance GMM: w ~ Dirichlet(1), mu ~ N(0, mean_sd^2), cov = S C S with a
+    random correlation structure C = (B B^T + D I) normalised to unit diagonal (B ~ N(0, corr^2))
+    and scales S ~ LogNormal(0, 0.4). Returns float32 w [M], mu [M, D], cov [M, D, D]."""
+    r = rng(seed)
+    w = r.dirichlet(np.ones(M)).astype(np.float32)
+    mu = (r.standard_normal((M, D)) * mean_sd).astype(np.float32)
+    cov = np.empty((M, D, D), np.float32)
+    for m in range(M):
+        B = r.standard_normal((D, D)) * corr
+        A = B @ B.T + D * np.eye(D)
+        d = 1.0 / np.sqrt(np.diag(A))
+        C = A * d[:, None] * d[None, :]
+        s = np.exp(r.standard_normal(D) * 0.4)
+        Cm = (C * s[:, None] * s[None, :]).astype(np.float32)
+        cov[m] = 0.5 * (Cm + Cm.T)
+    return w, mu, cov
+
+
+def sample_gmm_full(seed: int, w, mu, cov, N: int) -> np.ndarray:
+    """N frames from the full-covariance GMM, float32 [N, D]."""
+    r = rng(seed)
+    M, D = mu.shape
+    p = np.asarray(w, np.float64)
+    p = p / p.sum()
+    comp = r.choice(M, size=N, p=p)
+    L = np.linalg.cholesky(np.asarray(cov, np.float64))
+    z = r.standard_normal((N, D))
+    X = np.einsum("nij,nj->ni", L[comp], z) + mu[comp]
+    return X.astype(np.float32)
+
+
 def random_frame_init(seed: int, X: np.ndarray, M: int):
     """Random-init model: M random frames as means, global variance, uniform weights
     (the initialisation the reference README recommends)."""

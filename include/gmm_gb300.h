@@ -97,6 +97,32 @@ int gmm_read_stats(gmm_handle h, double* n, double* F, double* S, double* tot_lo
  * compLogLikes + getLogLikes (CU_GMMStatsEstimator_CUDA.cu:606-643). out: N floats (host). */
 int gmm_loglikes(gmm_handle h, float* out);
 
+/* ------------------------------------------------------------------ full covariances
+ * The full-covariance model family (GMModel with Var[D*D], the reference's --full-cov models):
+ * insertModel's full branch (OL_GMMStatsEstimator.cpp:298-305, getCovInverse / getLogDet
+ * :155-229), computeMixLogLikeFullCov (:593-620), accumulateStats with full second-order
+ * statistics (:1334-1378) and the full branches of UpdateModelEM / UpdateModelMAP
+ * (OL_ModelAdapt.cpp:905-917, 1074-1083). The full model lives beside the diagonal one on the
+ * handle and shares its resident features. cov: [M][D][D] row-major, symmetric; 1 <= D <= 64.
+ * A covariance that is not positive definite fails with GMM_ERR_MODEL (the reference throws
+ * "cholesky factorization failed"). Second-order statistics are the packed upper triangle per
+ * component in row order: Sp[m][k*D + kk - k(k+1)/2] = sum g x_k x_kk for kk >= k
+ * (GMMStats' full layout). Arithmetic: FP64 Cholesky factor, |L^-1 (x - mu)|^2 in FP32 with
+ * fused multiply-adds, float products of the statistics summed in double-float; the precision
+ * mode of the handle does not apply. */
+int gmm_upload_model_full(gmm_handle h, int M, int D, const float* w, const float* mu, const float* cov);
+int gmm_set_prior_full(gmm_handle h, const float* w, const float* mu, const float* cov);
+int gmm_read_model_full(gmm_handle h, float* w, float* mu, float* cov);
+int gmm_accumulate_full(gmm_handle h, int flags, double* n, double* F, double* Sp, double* tot_loglike,
+                        long long* tot_frames);
+int gmm_accumulate_full_device(gmm_handle h, int flags);
+int gmm_read_stats_full(gmm_handle h, double* n, double* F, double* Sp, double* tot_loglike,
+                        long long* tot_frames);
+int gmm_loglikes_full(gmm_handle h, float* out);
+/* UpdateModelEM / UpdateModelMAP (tau > 0, against gmm_set_prior_full) on the full model. */
+int gmm_em_update_full(gmm_handle h, int up_weight, int up_mean, int up_var, int* alive);
+int gmm_map_update_full(gmm_handle h, int tau, int up_weight, int up_mean, int up_var);
+
 /* Autotuner of the tensor-core statistics kernel (no counterpart in the reference): on the first
  * E-step of a shape (K, component chunks, frame-tile bucket) it times 1, 2 and 3 waves of CTAs
  * and keeps the fastest for the handle's later E-steps. On by default; off = one wave, the fixed

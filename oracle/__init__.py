@@ -296,3 +296,89 @@ def ref_train(X, nummix, iters_em=5, split_x=0.0, split_th=0.0, ll_th=0.0, verbo
     if rc:
         raise RuntimeError(f"reference TrainFromScratch failed: {ref().ref_last_error().decode()}")
     return w, mu, var
+
+# ------------------------------------------------------------------ full covariances
+
+def full64_loglikes(X, w, mu, cov):
+    """FP64 per-frame log-likelihoods under a full-covariance model (cov: [M, D, D])."""
+    X, w, mu, cov = map(_f32, (X, w, mu, cov))
+    N, D = X.shape
+    out = np.zeros(N)
+    rc = lib().orc64_full_loglikes(_p(X), C.c_longlong(N), D, len(w), _p(w), _p(mu), _p(cov), _p(out))
+    if rc:
+        raise RuntimeError(f"orc64_full_loglikes failed ({rc})")
+    return out
+
+
+def full64_accumulate(X, w, mu, cov, flags=ACC_MEAN | ACC_VAR, **kw):
+    """FP64 statistics: n [M], F [M, D], Sp [M, D(D+1)/2] (packed upper triangle, row order)."""
+    X, w, mu, cov = map(_f32, (X, w, mu, cov))
+    N, D = X.shape
+    M = len(w)
+    P = D * (D + 1) // 2
+    n, F, Sp = np.zeros(M), np.zeros((M, D)), np.zeros((M, P))
+    tl, tn = C.c_double(0.0), C.c_longlong(0)
+    o = _opts(1, **kw)
+    rc = lib().orc64_full_accumulate(_p(X), C.c_longlong(N), D, M, _p(w), _p(mu), _p(cov), C.byref(o),
+                                     flags, _p(n), _p(F), _p(Sp), C.byref(tl), C.byref(tn))
+    if rc:
+        raise RuntimeError(f"orc64_full_accumulate failed ({rc})")
+    return dict(n=n, F=F, Sp=Sp, totLL=tl.value, totN=tn.value)
+
+
+def full_em_update(w, mu, cov, st, upW=True, upM=True, upV=True):
+    w, mu, cov = _f32(w).copy(), _f32(mu).copy(), _f32(cov).copy()
+    M, D = mu.shape
+    n, F, Sp = (np.ascontiguousarray(st[k], np.float64) for k in ("n", "F", "Sp"))
+    alive = lib().orc_full_em_update(M, D, _p(w), _p(mu), _p(cov), _p(n), _p(F), _p(Sp),
+                                     C.c_longlong(int(st["totN"])), int(upW), int(upM), int(upV))
+    return w, mu, cov, alive
+
+
+def full_map_update(ubm_w, ubm_mu, ubm_cov, st, tau, upW=False, upM=True, upV=False):
+    ubm_w, ubm_mu, ubm_cov = map(_f32, (ubm_w, ubm_mu, ubm_cov))
+    w, mu, cov = ubm_w.copy(), ubm_mu.copy(), ubm_cov.copy()
+    M, D = mu.shape
+    n, F, Sp = (np.ascontiguousarray(st[k], np.float64) for k in ("n", "F", "Sp"))
+    lib().orc_full_map_update(M, D, _p(w), _p(mu), _p(cov), _p(ubm_w), _p(ubm_mu), _p(ubm_cov), _p(n),
+                              _p(F), _p(Sp), C.c_longlong(int(st["totN"])), int(tau), int(upW), int(upM),
+                              int(upV))
+    return w, mu, cov
+
+
+def ref_full_loglikes(X, w, mu, cov, threads=1):
+    X, w, mu, cov = map(_f32, (X, w, mu, cov))
+    N, D = X.shape
+    out = np.zeros(N, np.float32)
+    rc = ref().ref_full_loglikes(_p(X), C.c_long(N), D, len(w), _p(w), _p(mu), _p(cov), threads, _p(out))
+    if rc:
+        raise RuntimeError(ref().ref_last_error().decode())
+    return out
+
+
+def ref_full_accumulate(X, w, mu, cov, flags=ACC_MEAN | ACC_VAR, threads=1):
+    X, w, mu, cov = map(_f32, (X, w, mu, cov))
+    N, D = X.shape
+    M = len(w)
+    P = D * (D + 1) // 2
+    n, F, Sp = np.zeros(M), np.zeros((M, D)), np.zeros((M, P))
+    tl, tn = C.c_double(0.0), C.c_uint(0)
+    order = np.zeros(M, np.int32)
+    rc = ref().ref_full_accumulate(_p(X), C.c_long(N), D, M, _p(w), _p(mu), _p(cov), threads, flags,
+                                   _p(n), _p(F), _p(Sp), C.byref(tl), C.byref(tn), _p(order))
+    if rc:
+        raise RuntimeError(ref().ref_last_error().decode())
+    return dict(n=n, F=F, Sp=Sp, totLL=tl.value, totN=tn.value, order=order)
+
+
+def ref_full_adapt(X, w, mu, cov, tau, iters, upW=True, upM=True, upV=True, threads=1):
+    """IterEM (tau = 0) or IterMAP (tau > 0) on a full-covariance model."""
+    X = _f32(X)
+    w, mu, cov = _f32(w).copy(), _f32(mu).copy(), _f32(cov).copy()
+    N, D = X.shape
+    ll = np.zeros(iters)
+    rc = ref().ref_full_adapt(_p(X), C.c_long(N), D, len(w), _p(w), _p(mu), _p(cov), int(tau), iters,
+                              int(upW), int(upM), int(upV), threads, _p(ll))
+    if rc:
+        raise RuntimeError(ref().ref_last_error().decode())
+    return w, mu, cov, ll

@@ -677,3 +677,217 @@ void orc_mllr_apply(int M, int D, const float* mu, const double* W, float* omu) 
     }
   }
 }
+
+/* ---------------------------------------------------------------- full covariance ------ */
+/* The full-covariance branch of the reference (OL_GMMStatsEstimator.cpp:155-229 getCovInverse /
+ * getLogDet, :593-620 computeMixLogLikeFullCov, :1334-1378 accumulateStats with _fFullVar;
+ * OL_ModelAdapt.cpp:905-917 UpdateModelEM, :1074-1086 UpdateModelMAP). The reference inverts
+ * and factors with single-precision LAPACK (ACML spotrf/spotri, not vendored); this restatement
+ * works in double: Cholesky factor L (cov = L L^T), log det = 2 sum log L_ii, and
+ * (x-mu)^T cov^-1 (x-mu) = |L^-1 (x-mu)|^2 by forward substitution. Second-order statistics
+ * are the packed upper triangle in row order: S[k][kk] for kk >= k at k*D + kk - k(k+1)/2. */
+
+/* Cholesky of each active component's covariance, in double. chol: M*D*D (lower, row-major),
+ * logdet: M. Returns 4 if a covariance is not positive definite. */
+int orc64_full_prepare(int M, int D, const float* w, const float* cov, double* chol, double* logdet) {
+  for (int c = 0; c < M; ++c) {
+    double* L = chol + (size_t)c * D * D;
+    memset(L, 0, sizeof(double) * (size_t)D * D);
+    logdet[c] = 0.0;
+    if (!(w[c] > 0)) continue;
+    const float* A = cov + (size_t)c * D * D;
+    for (int j = 0; j < D; ++j) {
+      double s = A[(size_t)j * D + j];
+      for (int k = 0; k < j; ++k) s -= L[(size_t)j * D + k] * L[(size_t)j * D + k];
+      if (!(s > 0.0)) return 4;
+      const double ljj = sqrt(s);
+      L[(size_t)j * D + j] = ljj;
+      for (int i = j + 1; i < D; ++i) {
+        double t = A[(size_t)i * D + j];
+        for (int k = 0; k < j; ++k) t -= L[(size_t)i * D + k] * L[(size_t)j * D + k];
+        L[(size_t)i * D + j] = t / ljj;
+      }
+      logdet[c] += 2.0 * log(ljj);
+    }
+  }
+  return 0;
+}
+
+static double full_frame64(int M, int D, const float* w, const float* mu, const double* chol,
+                           const double* logc, const float* x, double* g, double* y) {
+  double mx = -INFINITY;
+  for (int c = 0; c < M; ++c) {
+    if (!(w[c] > 0)) { g[c] = -INFINITY; continue; }
+    const float* mean = mu + (size_t)c * D;
+    const double* L = chol + (size_t)c * D * D;
+    double e = 0.0;
+    for (int i = 0; i < D; ++i) {  /* y = L^-1 (x - mu) */
+      double t = (double)x[i] - (double)mean[i];
+      for (int k = 0; k < i; ++k) t -= L[(size_t)i * D + k] * y[k];
+      y[i] = t / L[(size_t)i * D + i];
+      e += y[i] * y[i];
+    }
+    g[c] = logc[c] - 0.5 * e;
+    if (g[c] > mx) mx = g[c];
+  }
+  if (mx == -INFINITY) return mx;
+  double s = 0;
+  for (int c = 0; c < M; ++c)
+    if (g[c] > -INFINITY) s += exp(g[c] - mx);
+  return mx + log(s);
+}
+
+static int full_model64(int M, int D, const float* w, const float* cov, double** chol, double** logc) {
+  *chol = (double*)malloc(sizeof(double) * (size_t)M * D * D);
+  *logc = (double*)malloc(sizeof(double) * (size_t)M);
+  double* logdet = (double*)malloc(sizeof(double) * (size_t)M);
+  int rc = orc64_full_prepare(M, D, w, cov, *chol, logdet);
+  for (int c = 0; c < M; ++c)
+    (*logc)[c] = (w[c] > 0) ? log((double)w[c]) + MINUS_LOG_2PI * D / 2.0 - 0.5 * logdet[c] : 0.0;
+  free(logdet);
+  return rc;
+}
+
+int orc64_full_loglikes(const float* X, long long N, int D, int M, const float* w, const float* mu,
+                        const float* cov, double* out) {
+  double *chol, *logc;
+  int rc = full_model64(M, D, w, cov, &chol, &logc);
+  if (!rc) {
+    double* g = (double*)malloc(sizeof(double) * (size_t)M);
+    double* y = (double*)malloc(sizeof(double) * (size_t)D);
+    for (long long i = 0; i < N; ++i) out[i] = full_frame64(M, D, w, mu, chol, logc, X + (size_t)i * D, g, y);
+    free(g);
+    free(y);
+  }
+  free(chol);
+  free(logc);
+  return rc;
+}
+
+/* FP64 statistics for a full-covariance model into zeroed n[M], F[M*D], Sp[M*D(D+1)/2]. */
+int orc64_full_accumulate(const float* X, long long N, int D, int M, const float* w, const float* mu,
+                          const float* cov, const orc_opts* o, int flags, double* n, double* F,
+                          double* Sp, double* totLL, long long* totN) {
+  double *chol, *logc;
+  int rc = full_model64(M, D, w, cov, &chol, &logc);
+  if (rc) { free(chol); free(logc); return rc; }
+  const int fm = (flags & ORC_ACC_MEAN) != 0, fv = (flags & ORC_ACC_VAR) != 0;
+  const int probsOnly = (flags & ORC_ACC_PROBS_ONLY) != 0;
+  const int nactive = count_active(M, w);
+  const size_t P = (size_t)D * (D + 1) / 2;
+  double* g = (double*)malloc(sizeof(double) * (size_t)M);
+  double* y = (double*)malloc(sizeof(double) * (size_t)D);
+  for (long long i = 0; i < N; ++i) {
+    const float* x = X + (size_t)i * D;
+    double ll = full_frame64(M, D, w, mu, chol, logc, x, g, y);
+    if (ll == -INFINITY) { *totLL += (double)o->minLogLike; continue; }
+    *totLL += ll;
+    for (int c = 0; c < M; ++c) {
+      if (!(w[c] > 0)) continue;
+      double gc = (nactive == 1) ? 1.0 : exp(g[c] - ll);
+      if (gc <= (double)o->minGamma) continue;
+      n[c] += gc;
+      if (probsOnly) continue;
+      size_t e = 0;
+      for (int k = 0; k < D; ++k) {
+        if (fm) F[(size_t)c * D + k] += gc * x[k];
+        if (fv)
+          for (int kk = k; kk < D; ++kk) Sp[(size_t)c * P + e++] += gc * (double)x[k] * (double)x[kk];
+      }
+    }
+  }
+  *totN += N;
+  free(g);
+  free(y);
+  free(chol);
+  free(logc);
+  return 0;
+}
+
+/* UpdateModelEM for full covariances (OL_ModelAdapt.cpp:858-931): as the diagonal update, the
+ * covariance (float)(S/n - mean_k*mean_kk) with a float product of the float means, symmetric,
+ * no floor; a killed component gets mean 0 and the identity (GMMMixture::Reset). */
+int orc_full_em_update(int M, int D, float* w, float* mu, float* cov, const double* n,
+                       const double* F, const double* Sp, long long totN, int upW, int upM, int upV) {
+  int changed = 0, nzero = 0;
+  double corr = 0.0;
+  const size_t P = (size_t)D * (D + 1) / 2;
+  float* mean = (float*)malloc(sizeof(float) * (size_t)D);
+  for (int j = 0; j < M; ++j) {
+    if (w[j] == 0.0f) { ++nzero; continue; }
+    const double mp = n[j];
+    float* C = cov + (size_t)j * D * D;
+    if (mp < 2.0) {
+      for (int k = 0; k < D; ++k) mu[(size_t)j * D + k] = 0.0f;
+      for (int e = 0; e < D * D; ++e) C[e] = 0.0f;
+      for (int k = 0; k < D; ++k) C[(size_t)k * D + k] = 1.0f;
+      w[j] = 0.0f;
+      changed = 1;
+      continue;
+    }
+    if (upW) {
+      w[j] = (float)(mp / (double)(unsigned int)totN);
+      changed = 1;
+    }
+    corr += w[j];
+    if (upM || upV) {
+      for (int k = 0; k < D; ++k) mean[k] = (float)(F[(size_t)j * D + k] / mp);
+      if (upV) {
+        size_t e = 0;
+        for (int k = 0; k < D; ++k)
+          for (int kk = k; kk < D; ++kk) {
+            const float mm = mean[k] * mean[kk];
+            const float v = (float)(Sp[(size_t)j * P + e++] / mp - (double)mm);
+            C[(size_t)k * D + kk] = v;
+            C[(size_t)kk * D + k] = v;
+          }
+      }
+      if (upM) memcpy(mu + (size_t)j * D, mean, sizeof(float) * (size_t)D);
+    }
+  }
+  if (changed && corr > 0.0)
+    for (int j = 0; j < M; ++j) w[j] = (float)((double)w[j] / corr);
+  free(mean);
+  return M - nzero;
+}
+
+/* UpdateModelMAP, tau > 0, full covariances (OL_ModelAdapt.cpp:1024-1099). */
+void orc_full_map_update(int M, int D, float* w, float* mu, float* cov, const float* ubm_w,
+                         const float* ubm_mu, const float* ubm_cov, const double* n, const double* F,
+                         const double* Sp, long long totN, int tau, int upW, int upM, int upV) {
+  double corr = 0.0;
+  const size_t P = (size_t)D * (D + 1) / 2;
+  float* am = (float*)malloc(sizeof(float) * (size_t)D);
+  for (int j = 0; j < M; ++j) {
+    if (ubm_w[j] == 0.0f) continue;
+    const double mp = n[j];
+    if (!(mp > 0.0)) continue;
+    const float* um = ubm_mu + (size_t)j * D;
+    const float* uc = ubm_cov + (size_t)j * D * D;
+    const double alfa = mp / (mp + tau);
+    if (upW && totN > 0) {
+      const float aw = (float)(alfa * (mp / (double)(unsigned int)totN) + (1 - alfa) * ubm_w[j]);
+      w[j] = aw;
+      corr += aw;
+    }
+    if (upM || upV) {
+      for (int k = 0; k < D; ++k) am[k] = (float)(alfa * F[(size_t)j * D + k] / mp + (1 - alfa) * um[k]);
+      if (upV) {
+        float* C = cov + (size_t)j * D * D;
+        size_t e = 0;
+        for (int k = 0; k < D; ++k)
+          for (int kk = k; kk < D; ++kk) {
+            const float second = uc[(size_t)k * D + kk] + um[k] * um[kk];
+            const float msq = am[k] * am[kk];
+            const float v = (float)(alfa * Sp[(size_t)j * P + e++] / mp + (1 - alfa) * second - msq);
+            C[(size_t)k * D + kk] = v;
+            C[(size_t)kk * D + k] = v;
+          }
+      }
+      memcpy(mu + (size_t)j * D, am, sizeof(float) * (size_t)D);
+    }
+  }
+  if (upW && corr != 0.0)
+    for (int j = 0; j < M; ++j) w[j] = w[j] / (float)corr;
+  free(am);
+}

@@ -88,6 +88,22 @@ void orc_mllr_apply(int M, int D, const float* mu, const double* W, float* omu);
 /* Pivot-free Gauss-Jordan inverse in place (MATRIX::_Invert_Gen semantics). */
 void orc_gj_invert(int n, double* a);
 
+/* Full covariances (cov: M*D*D row-major, symmetric). FP64: Cholesky, |L^-1 (x-mu)|^2, exact
+ * LSE; Sp = packed upper triangle [M][D(D+1)/2]. Return 4 if a covariance is not positive
+ * definite (the reference's getCovInverse throws). */
+int orc64_full_prepare(int M, int D, const float* w, const float* cov, double* chol, double* logdet);
+int orc64_full_loglikes(const float* X, long long N, int D, int M, const float* w, const float* mu,
+                        const float* cov, double* out);
+int orc64_full_accumulate(const float* X, long long N, int D, int M, const float* w, const float* mu,
+                          const float* cov, const orc_opts* o, int flags, double* n, double* F,
+                          double* Sp, double* totLL, long long* totN);
+/* The reference's full-covariance EM and MAP updates (float model, double arithmetic). */
+int orc_full_em_update(int M, int D, float* w, float* mu, float* cov, const double* n,
+                       const double* F, const double* Sp, long long totN, int upW, int upM, int upV);
+void orc_full_map_update(int M, int D, float* w, float* mu, float* cov, const float* ubm_w,
+                         const float* ubm_mu, const float* ubm_cov, const double* n, const double* F,
+                         const double* Sp, long long totN, int tau, int upW, int upM, int upV);
+
 #ifdef __cplusplus
 }
 #endif

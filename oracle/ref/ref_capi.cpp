@@ -319,3 +319,112 @@ int ref_param_load(const char* path, int type, unsigned int dwnsmp, float* out, 
 }
 
 }  // extern "C"
+
+
+
+// ---- full covariances (cov: M*D*D row-major). The factor and inverse go through the shim's
+// restatement of spotrf / spotri (oracle/ref/shim/acml.h).
+
+namespace {
+GMModel* make_model_full(int M, int D, const float* w, const float* mu, const float* cov) {
+  GMModel* g = new GMModel(D, M, true);
+  for (int m = 0; m < M; ++m)
+    g->SetMixParam(m, const_cast<float*>(mu + (size_t)m * D), const_cast<float*>(cov + (size_t)m * D * D), w[m]);
+  return g;
+}
+void read_model_full(GMModel* g, int M, int D, float* w, float* mu, float* cov) {
+  for (int m = 0; m < M; ++m) {
+    w[m] = g->GetMixtureWeight(m);
+    memcpy(mu + (size_t)m * D, g->GetMixtureMean(m), sizeof(float) * D);
+    memcpy(cov + (size_t)m * D * D, g->GetMixtureVar(m), sizeof(float) * D * D);
+  }
+}
+}  // namespace
+
+extern "C" {
+
+int ref_full_loglikes(const float* X, long N, int D, int M, const float* w, const float* mu,
+                      const float* cov, int threads, float* out) {
+  try {
+    GMModel* g = make_model_full(M, D, w, mu, cov);
+    GMMStatsEstimator<double>* e = make_estimator(0, threads);
+    e->insertModel(*g);
+    std::vector<float*> r = rows(X, N, D);
+    e->compVecsLogLikeMT(r.data(), (unsigned)N, (unsigned)D, out);
+    delete e;
+    delete g;
+    return 0;
+  } catch (std::exception& ex) { g_err = ex.what(); return 1; }
+}
+
+// E-step with full second-order statistics: Sp[M][D(D+1)/2] packed upper triangle, in the
+// rearranged order (order[k] = original index at slot k).
+int ref_full_accumulate(const float* X, long N, int D, int M, const float* w, const float* mu,
+                        const float* cov, int threads, int flags, double* n, double* F, double* Sp,
+                        double* totLL, unsigned* totSamples, int* order) {
+  try {
+    GMModel* g = make_model_full(M, D, w, mu, cov);
+    std::vector<float*> before((size_t)M);
+    for (int m = 0; m < M; ++m) before[(size_t)m] = g->GetMixtureMean(m);
+    GMMStatsEstimator<double>* e = make_estimator(0, threads);
+    e->insertModel(*g);
+    for (int k = 0; k < M; ++k) {
+      order[k] = -1;
+      for (int m = 0; m < M; ++m)
+        if (g->GetMixtureMean(k) == before[(size_t)m]) order[k] = m;
+    }
+    const bool probsOnly = (flags & 4) != 0, fm = (flags & 1) != 0, fv = (flags & 2) != 0;
+    GMMStats<double> st(D, M, fm || fv, fv, fv, false);
+    st.reset();
+    e->setAccFlags(probsOnly, fm, fv, fv, false);
+    std::vector<float*> r = rows(X, N, D);
+    e->accumulateStatsMT(r.data(), (unsigned)N, (unsigned)D, st);
+    const size_t P = (size_t)D * (D + 1) / 2;
+    for (int m = 0; m < M; ++m) {
+      n[m] = st.getProb(m);
+      for (int d = 0; d < D; ++d) F[(size_t)m * D + d] = (fm || fv) ? st.getMean(m)[d] : 0.0;
+      for (size_t q = 0; q < P; ++q) Sp[(size_t)m * P + q] = fv ? st.getVar(m)[q] : 0.0;
+    }
+    *totLL = st.getTotLogLike();
+    *totSamples = st.getTotAccSamples();
+    delete e;
+    delete g;
+    return 0;
+  } catch (std::exception& ex) { g_err = ex.what(); return 1; }
+}
+
+// EM iterations (IterEM, tau = 0) or MAP iterations (IterMAP, tau > 0) on a full-covariance
+// model; the model arrays receive the result (rearranged order). ll[i]: total LL of iteration i.
+int ref_full_adapt(const float* X, long N, int D, int M, float* w, float* mu, float* cov, int tau,
+                   int iters, int upW, int upM, int upV, int threads, double* ll) {
+  try {
+    GMModel* ubm = make_model_full(M, D, w, mu, cov);
+    CModelAdapt cm;
+    CModelAdapt::OPTIONS opt = base_options(threads, 0);
+    opt._adaptType = MAP;
+    opt._tau = tau;
+    opt._iterCountEM = tau == 0 ? iters : 0;
+    opt._iterCountMAP = tau == 0 ? 0 : iters;
+    opt._AdaptWeightBool = upW != 0;
+    opt._AdaptMeanBool = upM != 0;
+    opt._AdaptVarBool = upV != 0;
+    cm.SetOptions(opt);
+    Param p;
+    fill_param(p, X, N, D);
+    cm.InsertData(p, false);
+    cm.Initialize(ubm);
+    GMModel* model = new GMModel(ubm);
+    for (int it = 0; it < iters; ++it) {
+      if (tau == 0) cm.IterEM(model, 1);
+      else cm.IterMAP(model, 1);
+      ll[it] = cm._stats.getTotLogLike();
+    }
+    read_model_full(model, M, D, w, mu, cov);
+    delete model;
+    delete ubm;
+    return 0;
+  } catch (std::exception& ex) { g_err = ex.what(); return 1; }
+  catch (Exception* ex) { g_err = ex->m_strDescription; delete ex; return 2; }
+}
+
+}  // extern "C"

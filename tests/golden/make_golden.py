@@ -18,6 +18,12 @@ from their own sources, see oracle/Makefile) and records its outputs on small in
   that kills an under-occupied component.
 * ``map_mllr.npz`` -- mean-only MAP (tau = 16) and one global MLLR transform, with and without
   the UBM-based initialisation.
+* ``train.npz``    -- TrainFromScratch with four option sets.
+* ``full.npz``     -- full covariances: per-frame log-likelihoods of the first 1000 frames of
+  example/data.bin under example/myModelFC.gmm (4 threads) and their E-step statistics; three EM
+  iterations (weights, means, covariances) and one MAP iteration (tau = 16, all parameters) of
+  a seeded full-covariance model. The reference's single-precision LAPACK calls go through the
+  restatement in oracle/ref/shim/acml.h.
 """
 from __future__ import annotations
 
@@ -107,6 +113,26 @@ def main():
             print(fn, os.path.getsize(os.path.join(HERE, fn)))
 
     train_fixture()
+    full_fixture(a.ref_root)
+
+
+def full_fixture(ref_root):
+    """Full-covariance outputs of the reference build (see the module docstring)."""
+    ex = os.path.join(ref_root, "example")
+    X = formats.read_raw(os.path.join(ex, "data.bin"))[:1000]
+    g = formats.read_gmm_txt(os.path.join(ex, "myModelFC.gmm"))
+    out = {"ex_X": X, "ex_w": g.w, "ex_mu": g.mu, "ex_cov": g.var}
+    out["ex_ll"] = O.ref_full_loglikes(X, g.w, g.mu, g.var, threads=4)
+    st = O.ref_full_accumulate(X, g.w, g.mu, g.var, threads=1)
+    out.update(ex_n=st["n"], ex_F=st["F"], ex_Sp=st["Sp"], ex_totLL=st["totLL"])
+    w, mu, cov = synth.generator_gmm_full(41, 6, 10)
+    Xs = synth.sample_gmm_full(42, w, mu + 0.3, cov, 3000)
+    out.update(X=Xs, w=w, mu=mu, cov=cov)
+    ew, emu, ecov, ell = O.ref_full_adapt(Xs, w, mu, cov, 0, 3, threads=2)
+    out.update(em_w=ew, em_mu=emu, em_cov=ecov, em_ll=ell)
+    mw, mmu, mcov, mll = O.ref_full_adapt(Xs, w, mu, cov, 16, 1, threads=2)
+    out.update(map_w=mw, map_mu=mmu, map_cov=mcov, map_ll=mll)
+    np.savez_compressed(os.path.join(HERE, "full.npz"), **out)
 
 
 def train_fixture():
@@ -125,4 +151,8 @@ def train_fixture():
 
 
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) > 1 and sys.argv[1] == "--full-only":
+        O.build(ref=True)
+        full_fixture("/root/reference/GMM")
+    else:
+        main()

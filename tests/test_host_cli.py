@@ -106,6 +106,39 @@ def test_model_files_match_python_writers(driver, tmp_path, txt_in, txt_out):
     assert out.read_bytes() == want.read_bytes()
 
 
+@pytest.mark.parametrize("txt_in", [0, 1])
+@pytest.mark.parametrize("txt_out", [0, 1])
+def test_full_model_files_match_python_writers(driver, tmp_path, txt_in, txt_out):
+    from gmm_gb300 import formats, synth
+    w, mu, cov = synth.generator_gmm_full(8, 5, 6)
+    w[1] = 0.0
+    g = formats.GMModel(w, mu, cov)
+    src = tmp_path / ("in.txt" if txt_in else "in.bin")
+    (formats.write_gmm_txt if txt_in else formats.write_gmm_bin)(str(src), g)
+    out = tmp_path / "out"
+    assert driver("model", src, txt_in, out, txt_out).split() == ["6", "4", "0"]
+    ref = (formats.read_gmm_txt if txt_in else formats.read_gmm_bin)(str(src))
+    assert ref.full
+    want = tmp_path / "want"
+    (formats.write_gmm_txt if txt_out else formats.write_gmm_bin)(str(want), ref)
+    assert out.read_bytes() == want.read_bytes()
+
+
+def test_full_stats_files(driver, tmp_path):
+    from gmm_gb300 import estimator, formats
+    rng = np.random.default_rng(9)
+    D, M = 5, 3
+    n, F, Sp = rng.uniform(1, 9, M), rng.standard_normal((M, D)), rng.standard_normal((M, D * (D + 1) // 2))
+    src = tmp_path / "full.st"
+    formats.write_gmm_stats(str(src), False, n, F, Sp)
+    out = tmp_path / "o.st"
+    assert driver("stats", src, 0, out, 0).split() == ["3", "5"]
+    assert out.read_bytes() == src.read_bytes()
+    st = estimator.GMMStats()
+    st.load(str(out), False)
+    assert st.hasFullCov() and np.array_equal(st.S, Sp)
+
+
 def test_rearrange_matches_reference_rule(driver, tmp_path):
     """A text model that keeps zero-weight components (hand-written file) is rearranged as
     GMModel::RearrangeMixtures does, and Save drops the zero-weight ones."""

@@ -76,6 +76,37 @@ def test_loglike_for_each_matches_reference(exe, golden, tmp_path, prec):
     assert name == str(feat) and abs(float(mean) - ref.mean()) < 1e-3
 
 
+def test_full_covariance_models(exe, golden, tmp_path):
+    """gmm_loglike on the reference's example/myModelFC.gmm (text, full covariances) and gmm_adapt
+    EM / MAP of a full-covariance model, against the reference build (tests/golden/full.npz);
+    tolerances as tests/test_full_gpu.py (LL 1e-4 abs, models rel 1e-4 / abs 1e-5)."""
+    from gmm_gb300 import formats
+    g = golden("full.npz")
+    feat = tmp_path / "data.raw"
+    formats.write_raw(str(feat), g["ex_X"])
+    mdl = tmp_path / "fc.gmm"
+    formats.write_gmm_txt(str(mdl), formats.GMModel(g["ex_w"], g["ex_mu"], g["ex_cov"]))
+    out = tmp_path / "out"
+    out.mkdir()
+    run(exe("gmm_loglike"), "-i", feat, "-g", mdl, "-L", "--data-T", "2", "-f", "-o", out)
+    ll = formats.read_mat(str(out / "data.logL"), False)[0]
+    assert np.abs(ll - g["ex_ll"]).max() < 1e-4
+    xs = tmp_path / "x.prm"
+    formats.write_sves(str(xs), g["X"])
+    ubm = tmp_path / "ubm.gmm"
+    formats.write_gmm_bin(str(ubm), formats.GMModel(g["w"], g["mu"], g["cov"]))
+    run(exe("gmm_adapt"), "-i", xs, "-u", ubm, "-o", tmp_path / "em.gmm", "--it-EM", "3", "-W", "-M", "-V")
+    m = formats.read_gmm_bin(str(tmp_path / "em.gmm"))
+    assert m.full
+    assert np.allclose(m.w, g["em_w"], rtol=1e-4, atol=1e-5) and np.allclose(m.mu, g["em_mu"], rtol=1e-4, atol=1e-5)
+    assert np.allclose(m.var, g["em_cov"], rtol=1e-4, atol=1e-5)
+    run(exe("gmm_adapt"), "-i", xs, "-u", ubm, "-o", tmp_path / "map.gmm", "--it-MAP", "1", "-r", "16",
+        "-W", "-M", "-V")
+    m = formats.read_gmm_bin(str(tmp_path / "map.gmm"))
+    assert np.allclose(m.w, g["map_w"], rtol=1e-4, atol=1e-5) and np.allclose(m.mu, g["map_mu"], rtol=1e-4, atol=1e-5)
+    assert np.allclose(m.var, g["map_cov"], rtol=1e-4, atol=1e-5)
+
+
 def test_em_matches_reference(exe, golden, tmp_path):
     from gmm_gb300 import formats
     g = golden("em_small.npz")

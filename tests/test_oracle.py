@@ -119,3 +119,44 @@ def test_rearrange_order(oracle):
     assert nz == 3 and list(order) == [0, 2, 4, 3, 1]
     g = GMModel(w, np.arange(10, dtype=np.float32).reshape(5, 2), np.ones((5, 2)))
     assert list(g.rearrange()) == [0, 2, 4, 3, 1]
+
+
+def test_full_oracle_against_reference(oracle, golden):
+    """Full covariances: the FP64 restatement against the reference build (single-precision
+    Cholesky / inverse through the restated LAPACK routines): per-frame LL within 5e-5 abs,
+    statistics within 2e-6 of each statistic's scale; three EM iterations and one MAP iteration
+    of the oracle (FP64 E-step, the reference's update expressions) within 1e-4 rel."""
+    g = golden("full.npz")
+    ll = oracle.full64_loglikes(g["ex_X"], g["ex_w"], g["ex_mu"], g["ex_cov"])
+    assert np.abs(ll - g["ex_ll"]).max() < 5e-5
+    st = oracle.full64_accumulate(g["ex_X"], g["ex_w"], g["ex_mu"], g["ex_cov"])
+    for k, ref in (("n", g["ex_n"]), ("F", g["ex_F"]), ("Sp", g["ex_Sp"])):
+        assert np.abs(st[k] - ref).max() <= 2e-6 * np.abs(ref).max(), k
+    assert abs(st["totLL"] - g["ex_totLL"]) <= 1e-6 * abs(g["ex_totLL"])
+    w, mu, cov = g["w"].copy(), g["mu"].copy(), g["cov"].copy()
+    for it in range(3):
+        st = oracle.full64_accumulate(g["X"], w, mu, cov)
+        assert abs(st["totLL"] - g["em_ll"][it]) <= 1e-6 * abs(g["em_ll"][it])
+        w, mu, cov, alive = oracle.full_em_update(w, mu, cov, st)
+    assert np.allclose(w, g["em_w"], rtol=1e-4) and np.allclose(mu, g["em_mu"], rtol=1e-4, atol=1e-5)
+    assert np.allclose(cov, g["em_cov"], rtol=1e-4, atol=1e-5)
+    st = oracle.full64_accumulate(g["X"], g["w"], g["mu"], g["cov"])
+    mw, mmu, mcov = oracle.full_map_update(g["w"], g["mu"], g["cov"], st, 16, True, True, True)
+    assert np.allclose(mw, g["map_w"], rtol=1e-5) and np.allclose(mmu, g["map_mu"], rtol=1e-5, atol=1e-6)
+    assert np.allclose(mcov, g["map_cov"], rtol=1e-5, atol=1e-6)
+
+
+def test_full_model_files(tmp_path):
+    from gmm_gb300 import formats, synth
+    w, mu, cov = synth.generator_gmm_full(3, 5, 7)
+    w[2] = 0
+    g = formats.GMModel(w, mu, cov)
+    for ext, wr, rd in (("txt", formats.write_gmm_txt, formats.read_gmm_txt),
+                        ("bin", formats.write_gmm_bin, formats.read_gmm_bin)):
+        p = str(tmp_path / f"m.{ext}")
+        wr(p, g)
+        r = rd(p)
+        keep = w > 0
+        assert r.full and r.var.shape == (4, 7, 7)
+        tol = 1e-6 if ext == "txt" else 0
+        assert np.allclose(r.var, cov[keep], rtol=tol) and np.allclose(r.mu, mu[keep], rtol=tol, atol=1e-7)
