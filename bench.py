@@ -16,6 +16,10 @@ Workloads (--workload):
              step = one transform estimation for every speaker (mean statistics, G and k, FP64
              solves), in one call.
   serve      the request server under Poisson arrivals (see run_serve).
+  full-em    EM of a full-covariance GMM -- N = 1,000,000 frames, D = 39, M = 256 components with
+             full covariance matrices (frames drawn from a seeded full-covariance GMM; the fit
+             starts from it with shifted means). One step = one EM iteration: FP64 Cholesky
+             precompute, E-step with full second-order statistics, UpdateModelEM.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--precision tc|fp32] [--workload ...]
     python bench.py --impl reference ...   # the reference CPU algorithm on the host cores
@@ -49,7 +53,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="ubm-em", choices=["ubm-em", "map-batch", "mllr-batch", "serve"])
+    ap.add_argument("--workload", default="ubm-em", choices=["ubm-em", "map-batch", "mllr-batch", "serve", "full-em"])
     ap.add_argument("--models", type=int, default=200, help="serve: resident models")
     ap.add_argument("--pool", type=int, default=256, help="serve: utterances per request kind")
     ap.add_argument("--rates", default="500,1000,2000,5000,10000,15000,20000", help="serve: arrival rates (req/s)")
@@ -69,12 +73,13 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     a = ap.parse_args()
     big = a.workload in ("ubm-em", "mllr-batch")  # M = 2048, D = 39 workloads
-    a.frames = a.frames or 10_000_000
-    a.mix = a.mix or (2048 if big else 1024)
-    a.dim = a.dim or (39 if big else 60)
+    full = a.workload == "full-em"
+    a.frames = a.frames or (1_000_000 if full else 10_000_000)
+    a.mix = a.mix or (2048 if big else 256 if full else 1024)
+    a.dim = a.dim or (39 if big or full else 60)
     if a.workload == "mllr-batch" and a.speakers == 1000:
         a.speakers = 500
-    a.seed = a.seed if a.seed is not None else {"ubm-em": 2, "map-batch": 3, "mllr-batch": 4, "serve": 5}[a.workload]
+    a.seed = a.seed if a.seed is not None else {"ubm-em": 2, "map-batch": 3, "mllr-batch": 4, "serve": 5, "full-em": 6}[a.workload]
     return a
 
 
@@ -361,7 +366,85 @@ class MllrBatch:
                                       f"(MLLR: E-step + G/k + solves), {dt:.1f} s")
 
 
-WORKLOADS = {"ubm-em": UbmEm, "map-batch": MapBatch, "mllr-batch": MllrBatch}
+class FullEm:
+    """One EM iteration of a full-covariance GMM over N resident frames."""
+    metric = "frames·components/s per EM iter (full covariances)"
+    bound = "fp32"
+
+    def __init__(self, args, rank, gen_frames=None):
+        from gmm_gb300 import synth
+        self.a = args
+        self.N, self.M, self.D = args.frames, args.mix, args.dim
+        n = self.N if gen_frames is None else min(self.N, gen_frames)
+        seed = args.seed + rank
+        w, mu, cov = synth.generator_gmm_full(seed, self.M, self.D)
+        self.X = synth.sample_gmm_full(seed + 1, w, mu, cov, n)
+        shift = synth.rng(seed + 2).standard_normal(mu.shape).astype(np.float32) * 0.3
+        self.w, self.mu, self.cov = np.full(self.M, 1.0 / self.M, np.float32), mu + shift, cov
+        self.fc = self.N * self.M
+
+    def describe(self):
+        return {"workload": f"full-covariance EM iteration, N={self.N} frames, M={self.M}, D={self.D} "
+                            "(seeded full-covariance generator, fit started at shifted means)",
+                "frames": self.N, "components": self.M, "dim": self.D,
+                "l2": f"inputs larger than L2 (features {self.N * self.D * 4 / 1e9:.2f} GB, "
+                      f"posteriors {self.N * self.M * 4 / 1e9:.2f} GB)"}
+
+    def setup(self, dev, lib, torch, device):
+        self.dev, self.lib = dev, lib
+        self.Xpin = torch.from_numpy(self.X).pin_memory()
+        self.dX = self.Xpin.to(device)
+        dev.upload_model_full(self.w, self.mu, self.cov)
+        dev.upload_features_device(self.dX.data_ptr(), self.N, self.D)
+
+    def step(self):
+        self.dev.accumulate_full_device(self.lib.ACC_MEAN | self.lib.ACC_VAR)
+        self.dev.em_update_full(True, True, True)
+
+    def flop_per_fc(self, kernel):
+        D = self.D
+        P = D * (D + 1) // 2
+        if kernel == "full_ll_kernel":
+            return 2 * (P + D) + D + 4       # |U (x - mu)|^2 by FMAs, x - mu, the log-joint
+        if kernel == "full_stats_kernel":
+            return 2 * (P + D) + 1           # gamma x_k x_kk products + sums, gamma x_k, n
+        return 2 * (P + D)
+
+    def e2e_prepare(self, torch):
+        M, D = self.M, self.D
+        self.Xhost = self.Xpin.numpy()
+        self.out = [torch.empty(s, dtype=torch.float32).pin_memory().numpy() for s in (M, (M, D), (M, D, D))]
+        self.dev.upload_model_full(self.w, self.mu, self.cov)
+        return int(self.X.nbytes), int(sum(o.nbytes for o in self.out))
+
+    def e2e_step(self):
+        dev = self.dev
+        dev.upload_features(self.Xhost)
+        self.step()
+        wb, mub, cb = self.out
+        dev.check(dev.lib.gmm_read_model_full(dev.h, wb.ctypes.data, mub.ctypes.data, cb.ctypes.data))
+
+    def cpu_rate(self, seconds, threads):
+        """The full-covariance E-step + EM update restated on the CPU (the FP64 oracle, one
+        thread) on a bounded prefix of the frames."""
+        import oracle
+        oracle.build(ref=False)
+        X, w, mu, cov = self.X, self.w, self.mu, self.cov
+        n0 = min(len(X), 500)
+        t = time.perf_counter()
+        st = oracle.full64_accumulate(X[:n0], w, mu, cov)
+        oracle.full_em_update(w, mu, cov, st)
+        dt = time.perf_counter() - t
+        n = int(min(len(X), 200_000, max(n0, n0 * seconds / max(dt, 1e-3))))
+        t = time.perf_counter()
+        st = oracle.full64_accumulate(X[:n], w, mu, cov)
+        oracle.full_em_update(w, mu, cov, st)
+        dt = time.perf_counter() - t
+        return n * self.M / dt, (f"{n} frames x {self.M} components (full-covariance E-step + EM update) "
+                                 f"of the same workload, {dt:.1f} s, one thread")
+
+
+WORKLOADS = {"ubm-em": UbmEm, "map-batch": MapBatch, "mllr-batch": MllrBatch, "full-em": FullEm}
 
 
 # ------------------------------------------------------------------ served request loop
@@ -526,7 +609,8 @@ def run_reference(args):
     threads = os.cpu_count() or 1
     if args.workload == "serve":
         return run_serve_reference(args, threads)
-    wl = UbmEm(args, 0, gen_frames=400_000) if args.workload == "ubm-em" else WORKLOADS[args.workload](args, 0)
+    wl = (UbmEm(args, 0, gen_frames=400_000) if args.workload == "ubm-em" else
+          FullEm(args, 0, gen_frames=200_000) if args.workload == "full-em" else WORKLOADS[args.workload](args, 0))
     per_step = max(1.0, 60.0 / max(1, args.steps + args.warmup))
     rates = []
     for i in range(args.warmup + args.steps):
@@ -541,9 +625,10 @@ def run_reference(args):
         "ms_per_step": 1e3 * wl.fc / value, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": cfg,
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": rates[-1][1] + " per step; reference CPU algorithm (oracle port), "
-                                                  "all host threads"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1 if args.workload == "full-em" else threads,
+                         "kind": "port",
+                         "sample": rates[-1][1] + " per step; reference CPU algorithm (oracle port)" +
+                                   ("" if args.workload == "full-em" else ", all host threads")},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out), flush=True)
@@ -685,16 +770,21 @@ def main():
     traffic = None
     if args.workload == "ubm-em" and name == "tc_acc_kernel" and args.dim == 39 and args.mix == 2048:
         traffic = 503.2 * wl.N  # 503.2 MB per 1M frames: profiles/acc_kernel_ubm_em_1Mx2048x39.md
-    roofline = {"bound": "tensor", "kernel": name, "achieved": achieved, "peak": peak,
+    peak_source = f"{peak_kind} (bf16 sustained, MEASURED_PEAKS.json)"
+    bound = getattr(wl, "bound", "tensor")
+    if bound == "fp32":  # SIMT FP32 kernels: nominal FMA rate (no measured FP32 peak in the file)
+        peak = 152 * 128 * 2 * 2.07e9 / 1e12
+        peak_source = "nominal FP32 SIMT: 152 SMs x 128 lanes x 2 flop x 2.07 GHz"
+    roofline = {"bound": bound, "kernel": name, "achieved": achieved, "peak": peak,
                 "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
                 "algorithmic_flop_per_fc": flop_fc,
-                "peak_source": f"{peak_kind} (bf16 sustained, MEASURED_PEAKS.json)",
+                "peak_source": peak_source,
                 "kernel_ms_per_launch": per_launch_ms,
                 "kernel_share": kms / max(1e-9, sum(v[0] for v in prof.values()))}
 
     threads = os.cpu_count() or 1
     r, sample = wl.cpu_rate(args.cpu_seconds, threads)
-    cpu = {"value": r, "unit": UNIT, "cores": threads, "kind": "port",
+    cpu = {"value": r, "unit": UNIT, "cores": 1 if args.workload == "full-em" else threads, "kind": "port",
            "sample": sample + "; reference CPU algorithm (oracle port)"}
 
     cfg = wl.describe()
@@ -703,7 +793,8 @@ def main():
         "metric": wl.metric, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32" if prec == _lib.PREC_FP32 else "bf16x3 split (tcgen05), f32 accumulate, f64 reduce",
+        "dtype": ("f32 FMA, f64 Cholesky, double-float sums" if args.workload == "full-em" else
+                  "f32" if prec == _lib.PREC_FP32 else "bf16x3 split (tcgen05), f32 accumulate, f64 reduce"),
         "data": "synthetic", "config": cfg, "clocks": clk.summary(), "e2e": e2e,
         "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
         "kernels": {k: {"ms": v[0], "launches": v[1]} for k, v in prof.items()},

@@ -197,9 +197,11 @@ struct FullTile {
   static constexpr int TC = DP <= 40 ? 8 : 4;  // components per shared-memory tile
 };
 
-// One thread per frame: log joint g = logGconst - 0.5 |U (x - mu)|^2 + logW per active
-// component, raw values written component-major [Mact][chunk], frame LL by sequential addLog.
-template <int DP>
+// FPT frames per thread (each U row loaded from shared memory serves all of them): log joint
+// g = logGconst - 0.5 |U (x - mu)|^2 + logW per active component, raw values written
+// component-major [Mact][chunk], frame LL by sequential addLog. Block = 128 threads covering
+// 128 * FPT frames; frame i of the block's range is thread i % 128, slot i / 128.
+template <int DP, int FPT>
 __global__ void __launch_bounds__(128) full_ll_kernel(
     const float* __restrict__ X, long long f0, long long nf, int D, int Mact,
     const int* __restrict__ act, const float* __restrict__ mu, const float* __restrict__ U,
@@ -211,13 +213,19 @@ __global__ void __launch_bounds__(128) full_ll_kernel(
   __shared__ __align__(16) float s_mu[TC][DP];
   __shared__ float s_c[TC], s_lw[TC];
   __shared__ double s_red[4];
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const bool valid = i < nf;
-  float x[DP];
+  long long fi[FPT];
+  bool valid[FPT];
+  float x[FPT][DP];
 #pragma unroll
-  for (int d = 0; d < DP; ++d) x[d] = (valid && d < D) ? X[(size_t)(f0 + i) * D + d] : 0.0f;
-
-  float maxLL = minLL, sumLL = minLL;
+  for (int p = 0; p < FPT; ++p) {
+    fi[p] = (long long)blockIdx.x * (128 * FPT) + p * 128 + threadIdx.x;
+    valid[p] = fi[p] < nf;
+#pragma unroll
+    for (int d = 0; d < DP; ++d) x[p][d] = (valid[p] && d < D) ? X[(size_t)(f0 + fi[p]) * D + d] : 0.0f;
+  }
+  float maxLL[FPT], sumLL[FPT];
+#pragma unroll
+  for (int p = 0; p < FPT; ++p) maxLL[p] = sumLL[p] = minLL;
   for (int t0 = 0; t0 < Mact; t0 += TC) {
     const int nt = min(TC, Mact - t0);
     __syncthreads();
@@ -237,38 +245,58 @@ __global__ void __launch_bounds__(128) full_ll_kernel(
     }
     __syncthreads();
     for (int j = 0; j < nt; ++j) {
-      float a[DP];
+      float a[FPT][DP];
 #pragma unroll
-      for (int d = 0; d < DP; ++d) a[d] = __fsub_rn(x[d], s_mu[j][d]);
+      for (int d = 0; d < DP; ++d) {
+        const float m = s_mu[j][d];
+#pragma unroll
+        for (int p = 0; p < FPT; ++p) a[p][d] = __fsub_rn(x[p][d], m);
+      }
       const float4* u4 = reinterpret_cast<const float4*>(&s_u[j][0]);
-      float e = 0.0f;
+      float e[FPT];
+#pragma unroll
+      for (int p = 0; p < FPT; ++p) e[p] = 0.0f;
 #pragma unroll
       for (int r = 0; r < DP; ++r) {
-        float acc = 0.0f;
+        float acc[FPT];
+#pragma unroll
+        for (int p = 0; p < FPT; ++p) acc[p] = 0.0f;
 #pragma unroll
         for (int q = 0; q < row_len4(r) / 4; ++q) {
           const float4 u = u4[rowoff(r) / 4 + q];
-          acc = __fmaf_rn(u.x, a[4 * q + 0], acc);
-          acc = __fmaf_rn(u.y, a[4 * q + 1], acc);
-          acc = __fmaf_rn(u.z, a[4 * q + 2], acc);
-          acc = __fmaf_rn(u.w, a[4 * q + 3], acc);
+#pragma unroll
+          for (int p = 0; p < FPT; ++p) {
+            acc[p] = __fmaf_rn(u.x, a[p][4 * q + 0], acc[p]);
+            acc[p] = __fmaf_rn(u.y, a[p][4 * q + 1], acc[p]);
+            acc[p] = __fmaf_rn(u.z, a[p][4 * q + 2], acc[p]);
+            acc[p] = __fmaf_rn(u.w, a[p][4 * q + 3], acc[p]);
+          }
         }
-        e = __fmaf_rn(acc, acc, e);
+#pragma unroll
+        for (int p = 0; p < FPT; ++p) e[p] = __fmaf_rn(acc[p], acc[p], e[p]);
       }
-      float s = __fsub_rn(s_c[j], __fmul_rn(0.5f, e));
-      if (!isfinite(s)) s = minLL;
-      const float g = __fadd_rn(s, s_lw[j]);
-      if (G != nullptr && valid) G[(size_t)(t0 + j) * ldg + i] = g;
-      if (maxLL < g) maxLL = g;
-      add_log(sumLL, g);
+#pragma unroll
+      for (int p = 0; p < FPT; ++p) {
+        float s = __fsub_rn(s_c[j], __fmul_rn(0.5f, e[p]));
+        if (!isfinite(s)) s = minLL;
+        const float g = __fadd_rn(s, s_lw[j]);
+        if (G != nullptr && valid[p]) G[(size_t)(t0 + j) * ldg + fi[p]] = g;
+        if (maxLL[p] < g) maxLL[p] = g;
+        add_log(sumLL[p], g);
+      }
     }
   }
-  const float l = (maxLL == minLL) ? minLL : sumLL;
-  if (valid) {
-    if (maxLL == minLL) flag[1] = 1;
-    ll[f0 + i] = l;
+  double v = 0.0;
+#pragma unroll
+  for (int p = 0; p < FPT; ++p) {
+    const float l = (maxLL[p] == minLL) ? minLL : sumLL[p];
+    if (valid[p]) {
+      if (maxLL[p] == minLL) flag[1] = 1;
+      ll[f0 + fi[p]] = l;
+      v += (double)l;
+    }
   }
-  const double v = warp_sum(valid ? (double)l : 0.0);
+  v = warp_sum(v);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (lane == 0) s_red[warp] = v;
   __syncthreads();
@@ -279,8 +307,6 @@ __global__ void __launch_bounds__(128) full_ll_kernel(
   }
 }
 
-// One warp per (active component j, frame slice s): posteriors of 32 frames per ballot, kept
-// frames' statistics in double-float accumulators; lanes split the packed second-order entries.
 // Lanes hold at most kMaxEntries packed entries each; wider triangles are split over
 // gridDim.z entry groups, each re-deriving the posteriors (group 0 also sums n and F).
 constexpr int kMaxEntries = 34;
@@ -612,13 +638,18 @@ int full_precompute(Ctx* c) {
   return GMM_OK;
 }
 
+// frames per thread of the log-likelihood kernel (register budget: FPT x 2 x DP floats)
+constexpr int ll_fpt(int DP) { return DP <= 40 ? 2 : 1; }
+
 template <int DP>
-void launch_full_ll(Ctx* c, long long f0, long long nf, float* G, long long ldg, float* llout, int blocks) {
+void launch_full_ll(Ctx* c, long long f0, long long nf, float* G, long long ldg, float* llout) {
   FullModel* f = c->full;
+  constexpr int FPT = ll_fpt(DP);
+  const int blocks = (int)((nf + 128 * FPT - 1) / (128 * FPT));
   GMM_LAUNCH(c, "full_ll_kernel");
-  full_ll_kernel<DP><<<blocks, 128, 0, c->stream>>>(c->X, f0, nf, f->D, f->Mact, f->act, f->mu, f->U,
-                                                    f->logG, f->logW, c->minLL, G, ldg, llout,
-                                                    c->llpart, c->flag);
+  full_ll_kernel<DP, FPT><<<blocks, 128, 0, c->stream>>>(c->X, f0, nf, f->D, f->Mact, f->act, f->mu, f->U,
+                                                         f->logG, f->logW, c->minLL, G, ldg, llout,
+                                                         c->llpart, c->flag);
 }
 
 template <int DP>
@@ -634,16 +665,20 @@ void launch_full_stats(Ctx* c, long long f0, long long nf, long long ldg, int fl
                                                      slice_len, c->part);
 }
 
-void dispatch_ll(Ctx* c, long long f0, long long nf, float* G, long long ldg, float* llout, int blocks) {
-  switch (c->full->DP) {
-    case 8: launch_full_ll<8>(c, f0, nf, G, ldg, llout, blocks); break;
-    case 16: launch_full_ll<16>(c, f0, nf, G, ldg, llout, blocks); break;
-    case 24: launch_full_ll<24>(c, f0, nf, G, ldg, llout, blocks); break;
-    case 32: launch_full_ll<32>(c, f0, nf, G, ldg, llout, blocks); break;
-    case 40: launch_full_ll<40>(c, f0, nf, G, ldg, llout, blocks); break;
-    case 48: launch_full_ll<48>(c, f0, nf, G, ldg, llout, blocks); break;
-    default: launch_full_ll<64>(c, f0, nf, G, ldg, llout, blocks); break;
+// Launches the log-likelihood kernel for D's width; returns its block count.
+int dispatch_ll(Ctx* c, long long f0, long long nf, float* G, long long ldg, float* llout) {
+  const int DP = c->full->DP;
+  switch (DP) {
+    case 8: launch_full_ll<8>(c, f0, nf, G, ldg, llout); break;
+    case 16: launch_full_ll<16>(c, f0, nf, G, ldg, llout); break;
+    case 24: launch_full_ll<24>(c, f0, nf, G, ldg, llout); break;
+    case 32: launch_full_ll<32>(c, f0, nf, G, ldg, llout); break;
+    case 40: launch_full_ll<40>(c, f0, nf, G, ldg, llout); break;
+    case 48: launch_full_ll<48>(c, f0, nf, G, ldg, llout); break;
+    default: launch_full_ll<64>(c, f0, nf, G, ldg, llout); break;
   }
+  const int fpt = DP <= 40 ? 2 : 1;
+  return (int)((nf + 128 * fpt - 1) / (128 * fpt));
 }
 
 void dispatch_stats(Ctx* c, long long f0, long long nf, long long ldg, int flags, int slices, long long slice_len) {
@@ -688,11 +723,22 @@ int full_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
     }
   }
   float* llbuf = ll_out_dev ? ll_out_dev : c->ll;
+  // per-block LL partials: this kernel runs 128-frame blocks (the buffer is sized for 256)
+  const size_t need_part = (size_t)((chunk + 127) / 128) + 1;
+  if (need_part > c->llpart_cap) {
+    const int rc0 = sync(c, "full-covariance E-step");
+    if (rc0) return rc0;
+    dfree(c, c->llpart, c->llpart_cap * sizeof(double));
+    c->llpart = nullptr;
+    c->llpart_cap = 0;
+    const int rc = dalloc(c, (void**)&c->llpart, need_part * sizeof(double), "log-likelihood partial sums");
+    if (rc) return rc;
+    c->llpart_cap = need_part;
+  }
   for (long long f0 = 0; f0 < N; f0 += chunk) {
     const long long nf = (N - f0 < chunk) ? N - f0 : chunk;
-    const int blocks = (int)((nf + 127) / 128);
-    if ((size_t)blocks > c->llpart_cap) return fail(c, GMM_ERR_STATE, "llpart too small");
-    dispatch_ll(c, f0, nf, want_stats ? c->logits : nullptr, chunk, llbuf, blocks);
+    if ((size_t)((nf + 127) / 128) > c->llpart_cap) return fail(c, GMM_ERR_STATE, "llpart too small");
+    const int blocks = dispatch_ll(c, f0, nf, want_stats ? c->logits : nullptr, chunk, llbuf);
     if (!want_stats) continue;
     {
       GMM_LAUNCH(c, "full_ll_total_kernel");

@@ -80,8 +80,11 @@ def sample_gmm_full(seed: int, w, mu, cov, N: int) -> np.ndarray:
     comp = r.choice(M, size=N, p=p)
     L = np.linalg.cholesky(np.asarray(cov, np.float64))
     z = r.standard_normal((N, D))
-    X = np.einsum("nij,nj->ni", L[comp], z) + mu[comp]
-    return X.astype(np.float32)
+    X = np.empty((N, D), np.float32)
+    for m in range(M):  # per component: x = L_m z + mu_m
+        idx = np.nonzero(comp == m)[0]
+        X[idx] = (z[idx] @ L[m].T + mu[m]).astype(np.float32)
+    return X
 
 
 def random_frame_init(seed: int, X: np.ndarray, M: int):

@@ -106,7 +106,7 @@ def test_update_kernels_given_statistics(dev, golden, oracle):
     assert np.allclose(cov, ocov, rtol=2e-7, atol=1e-7)
 
 
-@pytest.mark.parametrize("M,D,N", [(1, 5, 700), (5, 1, 900), (8, 60, 2000), (33, 24, 3000)])
+@pytest.mark.parametrize("M,D,N", [(1, 5, 700), (5, 1, 900), (8, 60, 2000), (33, 24, 3000), (6, 8, 300_000)])
 def test_shapes_against_oracle(dev, oracle, M, D, N):
     from gmm_gb300 import synth
     w, mu, cov = synth.generator_gmm_full(100 + D, M, D)
