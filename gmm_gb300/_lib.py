@@ -29,6 +29,8 @@ SIGNATURES = {
     "gmm_get_stream": (_i, [_vp, C.POINTER(_vp)]),
     "gmm_upload_model": (_i, [_vp, _i, _i, _vp, _vp, _vp]),
     "gmm_upload_model_full": (_i, [_vp, _i, _i, _vp, _vp, _vp]),
+    "gmm_fmllr_estimate": (_i, [_vp, _i, _vp]),
+    "gmm_fmllr_apply": (_i, [_vp, _vp]),
     "gmm_set_prior_full": (_i, [_vp, _vp, _vp, _vp]),
     "gmm_read_model_full": (_i, [_vp, _vp, _vp, _vp]),
     "gmm_accumulate_full": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _vp]),
@@ -255,6 +257,17 @@ class Handle:
 
     def map_update(self, tau, upW=False, upM=True, upV=False):
         self.check(self.lib.gmm_map_update(self.h, int(tau), int(upW), int(upM), int(upV)))
+
+    # -- fMLLR
+    def fmllr_estimate(self, iters=20):
+        """W [D, D+1] = [A | b] of the resident features against the resident diagonal model."""
+        W = np.zeros((self.D, self.D + 1))
+        self.check(self.lib.gmm_fmllr_estimate(self.h, int(iters), ptr(W)))
+        return W
+
+    def fmllr_apply(self, W):
+        W = np.ascontiguousarray(W, np.float64)
+        self.check(self.lib.gmm_fmllr_apply(self.h, ptr(W)))
 
     # -- full covariances (cov [M, D, D]; second-order statistics packed [M, D(D+1)/2])
     def upload_model_full(self, w, mu, cov):

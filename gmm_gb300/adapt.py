@@ -29,6 +29,7 @@ class Options:
     AdaptVarBool: bool = False
     AdaptWeightBool: bool = False
     iterMLLR: int = 1
+    iterfMLLR: int = 20             # _iter_fMLLR (fixed to 20 in the reference)
     mllrUBMInit: bool = False
     applyTransforms: bool = False
     min_var: float = 1e-6
@@ -326,6 +327,12 @@ class ModelAdapt:
             if o.iterCountMAP:
                 model = self.IterMAP(model, ubm, o.iterCountMAP)
             self._model = model
+        elif o.adaptType == FMLLR:
+            if ubm.full:
+                raise NotImplementedError("fMLLR of full-covariance models is not built")
+            self._ensure_features()
+            self._upload(ubm.copy())
+            self._W = self.dev.fmllr_estimate(o.iterfMLLR)
         elif o.adaptType == MLLR:
             if ubm.full:
                 raise NotImplementedError("MLLR of full-covariance models is not built")

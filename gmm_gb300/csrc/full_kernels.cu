@@ -652,17 +652,18 @@ void launch_full_ll(Ctx* c, long long f0, long long nf, float* G, long long ldg,
                                                          c->llpart, c->flag);
 }
 
+// Statistics of frames [f0, f0 + nf) from the log joints in c->logits and the LLs in c->ll, for a
+// model with D dimensions and Mact active components (full or diagonal).
 template <int DP>
-void launch_full_stats(Ctx* c, long long f0, long long nf, long long ldg, int flags, int slices,
-                       long long slice_len) {
-  FullModel* f = c->full;
+void launch_full_stats(Ctx* c, int D, int Mact, long long f0, long long nf, long long ldg, int flags,
+                       int slices, long long slice_len) {
   GMM_LAUNCH(c, "full_stats_kernel");
   constexpr int R = entries_per_lane(DP);
-  const int groups = (f->P + 32 * R - 1) / (32 * R);
-  dim3 grid(f->Mact, (slices + 3) / 4, groups);
-  full_stats_kernel<DP><<<grid, 128, 0, c->stream>>>(c->X, f0, nf, f->D, f->Mact, c->logits, ldg, c->ll,
-                                                     c->minLL, c->minGamma, f->Mact == 1, flags, slices,
-                                                     slice_len, c->part);
+  const int P = D * (D + 1) / 2;
+  const int groups = (P + 32 * R - 1) / (32 * R);
+  dim3 grid(Mact, (slices + 3) / 4, groups);
+  full_stats_kernel<DP><<<grid, 128, 0, c->stream>>>(c->X, f0, nf, D, Mact, c->logits, ldg, c->ll, c->minLL,
+                                                     c->minGamma, Mact == 1, flags, slices, slice_len, c->part);
 }
 
 // Launches the log-likelihood kernel for D's width; returns its block count.
@@ -681,16 +682,54 @@ int dispatch_ll(Ctx* c, long long f0, long long nf, float* G, long long ldg, flo
   return (int)((nf + 128 * fpt - 1) / (128 * fpt));
 }
 
-void dispatch_stats(Ctx* c, long long f0, long long nf, long long ldg, int flags, int slices, long long slice_len) {
-  switch (c->full->DP) {
-    case 8: launch_full_stats<8>(c, f0, nf, ldg, flags, slices, slice_len); break;
-    case 16: launch_full_stats<16>(c, f0, nf, ldg, flags, slices, slice_len); break;
-    case 24: launch_full_stats<24>(c, f0, nf, ldg, flags, slices, slice_len); break;
-    case 32: launch_full_stats<32>(c, f0, nf, ldg, flags, slices, slice_len); break;
-    case 40: launch_full_stats<40>(c, f0, nf, ldg, flags, slices, slice_len); break;
-    case 48: launch_full_stats<48>(c, f0, nf, ldg, flags, slices, slice_len); break;
-    default: launch_full_stats<64>(c, f0, nf, ldg, flags, slices, slice_len); break;
+void dispatch_stats(Ctx* c, int DP, int D, int Mact, long long f0, long long nf, long long ldg, int flags,
+                    int slices, long long slice_len) {
+  switch (DP) {
+    case 8: launch_full_stats<8>(c, D, Mact, f0, nf, ldg, flags, slices, slice_len); break;
+    case 16: launch_full_stats<16>(c, D, Mact, f0, nf, ldg, flags, slices, slice_len); break;
+    case 24: launch_full_stats<24>(c, D, Mact, f0, nf, ldg, flags, slices, slice_len); break;
+    case 32: launch_full_stats<32>(c, D, Mact, f0, nf, ldg, flags, slices, slice_len); break;
+    case 40: launch_full_stats<40>(c, D, Mact, f0, nf, ldg, flags, slices, slice_len); break;
+    case 48: launch_full_stats<48>(c, D, Mact, f0, nf, ldg, flags, slices, slice_len); break;
+    default: launch_full_stats<64>(c, D, Mact, f0, nf, ldg, flags, slices, slice_len); break;
   }
+}
+
+// Frame slices of a statistics launch (about 64 warps per SM in total) and the FP64 partials
+// buffer they need.
+int plan_slices(Ctx* c, int Mact, int E, long long nf, long long* slices_out, long long* slice_len_out) {
+  long long slices = 152LL * 64 / Mact;
+  if (slices < 1) slices = 1;
+  if (slices > nf / 128) slices = nf / 128;
+  if (slices < 1) slices = 1;
+  slices = (slices + 3) / 4 * 4;
+  long long slice_len = (nf + slices - 1) / slices;
+  slice_len = (slice_len + 31) / 32 * 32;
+  const size_t need = (size_t)slices * Mact * E * sizeof(double);
+  if (need > c->part_cap) {
+    dfree(c, c->part, c->part_cap);
+    c->part = nullptr;
+    c->part_cap = 0;
+    const int rc = dalloc(c, (void**)&c->part, need, "partial statistics");
+    if (rc) return rc;
+    c->part_cap = need;
+  }
+  *slices_out = slices;
+  *slice_len_out = slice_len;
+  return GMM_OK;
+}
+
+// The log-posterior buffer for `chunk` frames of Mact components.
+int ensure_logits(Ctx* c, int Mact, long long chunk) {
+  const size_t need = (size_t)Mact * (size_t)chunk * sizeof(float);
+  if (need <= c->logits_cap) return GMM_OK;
+  dfree(c, c->logits, c->logits_cap);
+  c->logits = nullptr;
+  c->logits_cap = 0;
+  const int rc = dalloc(c, (void**)&c->logits, need, "log-posterior buffer");
+  if (rc) return rc;
+  c->logits_cap = need;
+  return GMM_OK;
 }
 
 // One E-step over the resident features with the full-covariance model.
@@ -712,15 +751,8 @@ int full_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
   if (chunk < 256) chunk = 256;
   if (chunk > N) chunk = N;
   if (want_stats) {
-    const size_t need = (size_t)f->Mact * (size_t)chunk * sizeof(float);
-    if (need > c->logits_cap) {
-      dfree(c, c->logits, c->logits_cap);
-      c->logits = nullptr;
-      c->logits_cap = 0;
-      const int rc = dalloc(c, (void**)&c->logits, need, "log-posterior buffer");
-      if (rc) return rc;
-      c->logits_cap = need;
-    }
+    const int rc = ensure_logits(c, f->Mact, chunk);
+    if (rc) return rc;
   }
   float* llbuf = ll_out_dev ? ll_out_dev : c->ll;
   // per-block LL partials: this kernel runs 128-frame blocks (the buffer is sized for 256)
@@ -744,23 +776,10 @@ int full_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
       GMM_LAUNCH(c, "full_ll_total_kernel");
       full_ll_total_kernel<<<1, 1024, 0, c->stream>>>(blocks, c->llpart, f->stats + (size_t)f->M * E);
     }
-    long long slices = 152LL * 64 / f->Mact;
-    if (slices < 1) slices = 1;
-    if (slices > nf / 128) slices = nf / 128;
-    if (slices < 1) slices = 1;
-    slices = (slices + 3) / 4 * 4;
-    long long slice_len = (nf + slices - 1) / slices;
-    slice_len = (slice_len + 31) / 32 * 32;
-    const size_t need = (size_t)slices * f->Mact * E * sizeof(double);
-    if (need > c->part_cap) {
-      dfree(c, c->part, c->part_cap);
-      c->part = nullptr;
-      c->part_cap = 0;
-      const int rc = dalloc(c, (void**)&c->part, need, "partial statistics");
-      if (rc) return rc;
-      c->part_cap = need;
-    }
-    dispatch_stats(c, f0, nf, chunk, flags, (int)slices, slice_len);
+    long long slices = 0, slice_len = 0;
+    const int rc = plan_slices(c, f->Mact, E, nf, &slices, &slice_len);
+    if (rc) return rc;
+    dispatch_stats(c, f->DP, D, f->Mact, f0, nf, chunk, flags, (int)slices, slice_len);
     {
       GMM_LAUNCH(c, "full_reduce_kernel");
       const long long tot = (long long)f->Mact * E;
@@ -803,6 +822,48 @@ int full_read_stats(Ctx* c, double* n, double* F, double* Sp, double* tl, long l
 }
 
 }  // namespace
+
+int diag_fullstats_estep(Ctx* c, double* stats) {
+  if (!c->w) return fail(c, GMM_ERR_STATE, "no model uploaded");
+  if (!c->X) return fail(c, GMM_ERR_STATE, "no features uploaded");
+  if (c->Dx != c->D) return fail(c, GMM_ERR_ARG, "Inconsistent model & feature vector - different dimensions");
+  if (c->D > kFullMaxDim) return fail(c, GMM_ERR_UNSUPPORTED, "full second-order statistics support D <= 64");
+  if (c->model_dirty) {
+    const int rc = plain_precompute(c);
+    if (rc) return rc;
+  }
+  if (c->Mact <= 0) return fail(c, GMM_ERR_STATE, "no component with non-zero weight");
+  const int M = c->M, D = c->D, P = D * (D + 1) / 2, E = 1 + D + P;
+  cudaError_t e = cudaMemsetAsync(stats, 0, sizeof(double) * ((size_t)M * E + 2), c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "cudaMemsetAsync(statistics)");
+  const long long N = c->N;
+  long long chunk = (long long)(((size_t)4 << 30) / ((size_t)c->Mact * sizeof(float)));
+  chunk = chunk / 256 * 256;
+  if (chunk < 256) chunk = 256;
+  if (chunk > N) chunk = N;
+  int rc = ensure_logits(c, c->Mact, chunk);
+  if (rc) return rc;
+  for (long long f0 = 0; f0 < N; f0 += chunk) {
+    const long long nf = (N - f0 < chunk) ? N - f0 : chunk;
+    if ((size_t)((nf + 255) / 256) > c->llpart_cap) return fail(c, GMM_ERR_STATE, "llpart too small");
+    const int blocks = plain_ll_chunk(c, f0, nf, c->logits, chunk, c->ll);
+    {
+      GMM_LAUNCH(c, "full_ll_total_kernel");
+      full_ll_total_kernel<<<1, 1024, 0, c->stream>>>(blocks, c->llpart, stats + (size_t)M * E);
+    }
+    long long slices = 0, slice_len = 0;
+    rc = plan_slices(c, c->Mact, E, nf, &slices, &slice_len);
+    if (rc) return rc;
+    dispatch_stats(c, dp_for(D), D, c->Mact, f0, nf, chunk, GMM_ACC_MEAN | GMM_ACC_VAR, (int)slices, slice_len);
+    {
+      GMM_LAUNCH(c, "full_reduce_kernel");
+      const long long tot = (long long)c->Mact * E;
+      full_reduce_kernel<<<(int)((tot + 255) / 256), 256, 0, c->stream>>>(M, D, P, c->Mact, c->act, (int)slices,
+                                                                          c->part, stats);
+    }
+  }
+  return GMM_OK;
+}
 
 void full_destroy(Ctx* c) {
   if (!c->full) return;

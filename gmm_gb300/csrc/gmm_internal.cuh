@@ -146,6 +146,10 @@ struct LaunchScope {
 int plain_precompute(Ctx* c);
 int plain_precompute_async(Ctx* c);  // the same launches without the host readback
 int plain_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev);
+int plain_ll_chunk(Ctx* c, long long f0, long long nf, float* G, long long ldg, float* llout);
+// E-step of the resident diagonal model with packed full second-order statistics (fMLLR):
+// stats [n (M) | F (M x D) | S (M x D(D+1)/2) | totLL | pad] on the device, zeroed by the callee.
+int diag_fullstats_estep(Ctx* c, double* stats);
 
 // ------------------------------------------------------------------ M-step
 int mstep_em(Ctx* c, int upW, int upM, int upV, int* alive);

@@ -352,6 +352,26 @@ int plain_precompute(Ctx* c) {
   return GMM_OK;
 }
 
+// The diagonal model's log joints of frames [f0, f0 + nf): raw values into G [Mact][ldg] (when
+// G is not null), frame LLs into llout[f0 + i], per-256-frame-block LL partials into c->llpart.
+// Returns the number of blocks.
+int plain_ll_chunk(Ctx* c, long long f0, long long nf, float* G, long long ldg, float* llout) {
+  const int D = c->D;
+  const int blocks = (int)((nf + 255) / 256);
+  if (D <= 16) launch_ll<16>(c, f0, nf, G, ldg, llout, blocks);
+  else if (D <= 32) launch_ll<32>(c, f0, nf, G, ldg, llout, blocks);
+  else if (D <= 40) launch_ll<40>(c, f0, nf, G, ldg, llout, blocks);
+  else if (D <= 64) launch_ll<64>(c, f0, nf, G, ldg, llout, blocks);
+  else if (D <= 128) launch_ll<128>(c, f0, nf, G, ldg, llout, blocks);
+  else {
+    GMM_LAUNCH(c, "plain_ll_kernel_large");
+    ll_kernel_large<<<blocks, 256, 0, c->stream>>>(c->X, f0, nf, D, c->Mact, c->act, c->mu, c->icov,
+                                                   c->logG, c->logW, c->minLL, G, ldg, llout, c->llpart,
+                                                   c->flag);
+  }
+  return blocks;
+}
+
 // One E-step over the resident features. want_stats: accumulate statistics into c->stats
 // (zeroed by the caller); ll_out_dev: optional per-frame LL destination (device, N floats).
 int plain_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
@@ -381,18 +401,7 @@ int plain_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
     const long long nf = (N - f0 < chunk) ? N - f0 : chunk;
     const int blocks = (int)((nf + 255) / 256);
     if ((size_t)blocks > c->llpart_cap) return fail(c, GMM_ERR_STATE, "llpart too small");
-    float* G = want_stats ? c->logits : nullptr;
-    if (D <= 16) launch_ll<16>(c, f0, nf, G, chunk, llbuf, blocks);
-    else if (D <= 32) launch_ll<32>(c, f0, nf, G, chunk, llbuf, blocks);
-    else if (D <= 40) launch_ll<40>(c, f0, nf, G, chunk, llbuf, blocks);
-    else if (D <= 64) launch_ll<64>(c, f0, nf, G, chunk, llbuf, blocks);
-    else if (D <= 128) launch_ll<128>(c, f0, nf, G, chunk, llbuf, blocks);
-    else {
-      GMM_LAUNCH(c, "plain_ll_kernel_large");
-      ll_kernel_large<<<blocks, 256, 0, c->stream>>>(c->X, f0, nf, D, c->Mact, c->act, c->mu,
-                                                     c->icov, c->logG, c->logW, c->minLL, G,
-                                                     chunk, llbuf, c->llpart, c->flag);
-    }
+    plain_ll_chunk(c, f0, nf, want_stats ? c->logits : nullptr, chunk, llbuf);
     if (want_stats) {
       GMM_LAUNCH(c, "ll_total_kernel");
       ll_total_kernel<<<1, 1024, 0, c->stream>>>(blocks, c->llpart,

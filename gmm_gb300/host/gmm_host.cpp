@@ -543,6 +543,13 @@ void ModelAdapt::AdaptModel(const GMModel& ubm) {
       model_ = AdaptModelMLLR(ubm, W_);
       trained_ = true;
     }
+  } else if (o_.adaptType == FMLLR) {  // ComputeW_fMLLR(_UBM): the transform is the result
+    if (ubm.GetFullCovStatus()) fail("ComputeW_fMLLR(): fMLLR of full-covariance models is not built");
+    GMModel u = ubm;
+    u.RearrangeMixtures();
+    upload_model(u);
+    W_.assign((size_t)D_ * (D_ + 1), 0.0);
+    check(gmm_fmllr_estimate(h_, o_.iterfMLLR, W_.data()));
   } else {
     fail("AdaptModel(): use TrainFromScratch for --type 0");
   }
@@ -694,7 +701,7 @@ void ModelAdapt::SaveTRNMatrices(const std::string& FileName) const {
   FILE* f = std::fopen(out.c_str(), "w");
   if (!f) fail("Save(): Unable to open output file " + out + "!");
   const int E = D_ + 1;
-  std::fprintf(f, " MLLR\n 1\t%d %d\n", D_, E);
+  std::fprintf(f, o_.adaptType == FMLLR ? " fMLLR\n 1\t%d %d\n" : " MLLR\n 1\t%d %d\n", D_, E);
   for (int i = 0; i < D_; ++i) {  // the reference streams a float matrix with ostream defaults (%g)
     for (int j = 0; j < E; ++j) std::fprintf(f, " %g", (double)(float)W_[(size_t)i * E + j]);
     std::fprintf(f, "\n");
@@ -705,7 +712,7 @@ void ModelAdapt::SaveTRNMatrices(const std::string& FileName) const {
 void ModelAdapt::Save(const std::string& FileName, bool save_txt, bool save_in_stat_form) const {
   const bool trn = !W_.empty();
   if (!trained_ && !trn) fail("Save(): Missing client model or transformation matrix!");
-  if (trn && (!trained_ || o_.saveTransforms)) {
+  if (trn && (!trained_ || o_.saveTransforms || o_.adaptType == FMLLR)) {
     if (!save_in_stat_form) {
       SaveTRNMatrices(FileName);
     } else {  // D records of dimension D+1: occupancy 1, "mean" = the row of W

@@ -116,13 +116,14 @@ class GMMStatsEstimatorGB300 {
 
 // The options of CModelAdapt::OPTIONS on the diagonal hot path (defaults of GetOptions,
 // OL_ModelAdapt.cpp:2032-2132).
-enum AdaptType { FROM_SCRATCH = 0, MLLR = 1, MAP = 2 };
+enum AdaptType { FROM_SCRATCH = 0, MLLR = 1, MAP = 2, FMLLR = 3 };
 struct AdaptOptions {
   int adaptType = MAP;
   int tau = 0;
   int iterCountEM = 0, iterCountMAP = 0;
   bool AdaptWeightBool = false, AdaptMeanBool = true, AdaptVarBool = false;
   int iterMLLR = 1;
+  int iterfMLLR = 20;  // _iter_fMLLR (OL_ModelAdapt.cpp:190)
   bool mllrUBMInit = false, applyTransforms = false, saveTransforms = false;
   std::string transformFileExt = ".mat";
   float min_var = 1e-6f;
@@ -141,21 +142,21 @@ class ModelAdapt {
   // InsertData(CFileList*) (file-by-file mode): every E-step streams the files through
   // gmm_accumulate_files in batches of at most buffer_gb instead of keeping the frames resident.
   void InsertFiles(const std::vector<std::string>& paths, int prm_type, unsigned dwnsmp, double buffer_gb);
-  // AdaptModel (OL_ModelAdapt.cpp:1163-1226): MAP (IterEM then IterMAP) or MLLR.
+  // AdaptModel (OL_ModelAdapt.cpp:1163-1226): MAP (IterEM then IterMAP), MLLR or fMLLR.
   void AdaptModel(const GMModel& ubm);
   // TrainFromScratch (OL_ModelAdapt.cpp:667-821), diagonal covariances; `init` (optional) is the
   // model the splitting starts from instead of the global Gaussian. (The full-covariance split
   // along the leading eigenvector is not built.)
   void TrainFromScratch(int nummix, const GMModel* init = nullptr);
   const GMModel& GetModel() const { return model_; }
-  const std::vector<double>& GetW() const { return W_; }  // MLLR transform D x (D+1)
+  const std::vector<double>& GetW() const { return W_; }  // (f)MLLR transform D x (D+1)
   bool ModelTrained() const { return trained_; }
   long long NumFrames() const { return N_; }
   // CModelAdapt::Save (OL_ModelAdapt.cpp:1930-1989): the MLLR transform (when it is the result,
   // or saveTransforms is set) to FileName with its extension replaced by transformFileExt, and
   // the adapted / trained model to FileName.
   void Save(const std::string& FileName, bool save_txt, bool save_in_stat_form = false) const;
-  // SaveTRNMatrices (OL_ModelAdapt.cpp:1900-1928): " MLLR", " 1\tD D+1", rows of " value".
+  // SaveTRNMatrices (OL_ModelAdapt.cpp:1900-1928): " MLLR" / " fMLLR", " 1\tD D+1", rows of " value".
   void SaveTRNMatrices(const std::string& FileName) const;
   std::vector<double> ll_history;
 

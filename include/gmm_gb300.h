@@ -123,6 +123,17 @@ int gmm_loglikes_full(gmm_handle h, float* out);
 int gmm_em_update_full(gmm_handle h, int up_weight, int up_mean, int up_var, int* alive);
 int gmm_map_update_full(gmm_handle h, int tau, int up_weight, int up_mean, int up_var);
 
+/* fMLLR (feature-space MLLR, one regression class) against the resident diagonal model:
+ * CModelAdapt::ComputeW_fMLLR (OL_ModelAdapt.cpp:1614-1719) with ComputeKiGi_fMLLR (:1794-1848)
+ * and EstimateAb_fmllr (:1721-1792). Runs the E-step over the resident features with full
+ * second-order statistics (the plain FP32 log-likelihood kernel whatever the precision mode),
+ * then the row passes (`iters`; the reference uses 20) on the device in FP64. W: D x (D+1)
+ * row-major [A | b]; features are adapted as x' = A x + b. GMM_ERR_MLLR when CheckInvertibility
+ * fails or a row's quadratic has no usable root. D <= 64. */
+int gmm_fmllr_estimate(gmm_handle h, int iters, double* W);
+/* Applies W to the features uploaded with gmm_upload_features, in place on the device. */
+int gmm_fmllr_apply(gmm_handle h, const double* W);
+
 /* Autotuner of the tensor-core statistics kernel (no counterpart in the reference): on the first
  * E-step of a shape (K, component chunks, frame-tile bucket) it times 1, 2 and 3 waves of CTAs
  * and keeps the fastest for the handle's later E-steps. On by default; off = one wave, the fixed

@@ -382,3 +382,49 @@ def ref_full_adapt(X, w, mu, cov, tau, iters, upW=True, upM=True, upV=True, thre
     if rc:
         raise RuntimeError(ref().ref_last_error().decode())
     return w, mu, cov, ll
+
+
+# ------------------------------------------------------------------ fMLLR
+
+def accumulate64_fullstats(X, w, mu, var, **kw):
+    """FP64 E-step of a diagonal model with packed full second-order statistics."""
+    X, w, mu, var = map(_f32, (X, w, mu, var))
+    N, D = X.shape
+    M = len(w)
+    P = D * (D + 1) // 2
+    n, F, Sp = np.zeros(M), np.zeros((M, D)), np.zeros((M, P))
+    tl, tn = C.c_double(0.0), C.c_longlong(0)
+    o = _opts(1, **kw)
+    rc = lib().orc64_accumulate_fullstats(_p(X), C.c_longlong(N), D, M, _p(w), _p(mu), _p(var), C.byref(o),
+                                          _p(n), _p(F), _p(Sp), C.byref(tl), C.byref(tn))
+    if rc:
+        raise RuntimeError(f"orc64_accumulate_fullstats failed ({rc})")
+    return dict(n=n, F=F, Sp=Sp, totLL=tl.value, totN=tn.value)
+
+
+def fmllr_w(mu, var, st, iters=20):
+    """ComputeW_fMLLR from statistics (n, F, Sp, totN): W [D, D+1]."""
+    mu, var = _f32(mu), _f32(var)
+    M, D = mu.shape
+    n, F, Sp = (np.ascontiguousarray(st[k], np.float64) for k in ("n", "F", "Sp"))
+    W = np.zeros((D, D + 1))
+    rc = lib().orc_fmllr_w(M, D, _p(mu), _p(var), _p(n), _p(F), _p(Sp), C.c_longlong(int(st["totN"])),
+                           int(iters), _p(W))
+    if rc:
+        raise RuntimeError(f"orc_fmllr_w failed ({rc})")
+    return W
+
+
+def ref_fmllr(X, w, mu, var, threads=1):
+    X, w, mu, var = map(_f32, (X, w, mu, var))
+    N, D = X.shape
+    M = len(w)
+    P = D * (D + 1) // 2
+    W = np.zeros((D, D + 1))
+    n, F, Sp = np.zeros(M), np.zeros((M, D)), np.zeros((M, P))
+    tl = C.c_double(0.0)
+    rc = ref().ref_fmllr(_p(X), C.c_long(N), D, M, _p(w), _p(mu), _p(var), threads, _p(W), _p(n), _p(F),
+                         _p(Sp), C.byref(tl))
+    if rc:
+        raise RuntimeError(ref().ref_last_error().decode())
+    return W, dict(n=n, F=F, Sp=Sp, totLL=tl.value, totN=N)

@@ -891,3 +891,180 @@ void orc_full_map_update(int M, int D, float* w, float* mu, float* cov, const fl
     for (int j = 0; j < M; ++j) w[j] = w[j] / (float)corr;
   free(am);
 }
+
+/* ---------------------------------------------------------------- fMLLR -------------- */
+
+/* FP64 E-step of a diagonal model with full (packed upper-triangle) second-order statistics,
+ * as ComputeW_fMLLR gathers them (AccumulateStats with varFull, OL_ModelAdapt.cpp:1626-1628). */
+int orc64_accumulate_fullstats(const float* X, long long N, int D, int M, const float* w,
+                               const float* mu, const float* var, const orc_opts* o, double* n,
+                               double* F, double* Sp, double* totLL, long long* totN) {
+  model64 m;
+  int rc = prep64(&m, M, D, w, mu, var, o);
+  if (rc) { free(m.logc); return rc; }
+  const int nactive = count_active(M, w);
+  const size_t P = (size_t)D * (D + 1) / 2;
+  double* g = (double*)malloc(sizeof(double) * (size_t)M);
+  for (long long i = 0; i < N; ++i) {
+    const float* x = X + (size_t)i * D;
+    double ll = frame64(&m, x, g);
+    if (ll == -INFINITY) { *totLL += (double)o->minLogLike; continue; }
+    *totLL += ll;
+    for (int c = 0; c < M; ++c) {
+      if (!(w[c] > 0)) continue;
+      double gc = (nactive == 1) ? 1.0 : exp(g[c] - ll);
+      if (gc <= (double)o->minGamma) continue;
+      n[c] += gc;
+      size_t e = 0;
+      for (int k = 0; k < D; ++k) {
+        F[(size_t)c * D + k] += gc * x[k];
+        for (int kk = k; kk < D; ++kk) Sp[(size_t)c * P + e++] += gc * (double)x[k] * (double)x[kk];
+      }
+    }
+  }
+  *totN += N;
+  free(g);
+  free(m.logc);
+  return 0;
+}
+
+/* Determinant by elimination with partial pivoting (MATRIX::_Det_Gen + pivot,
+ * Matrix4_LMa.cpp:1925-1962, 2091-2120). a is overwritten. */
+static double det_gen(int n, double* a) {
+  double det = 1.0;
+  for (int k = 0; k < n; ++k) {
+    int p = k;
+    double amax = -1.0;
+    for (int i = k; i < n; ++i) {
+      const double t = fabs(a[i * n + k]);
+      if (t > amax && t != 0.0) { amax = t; p = i; }
+    }
+    if (a[p * n + k] == 0.0) return 0.0;
+    if (p != k) {
+      for (int j = 0; j < n; ++j) { double t = a[p * n + j]; a[p * n + j] = a[k * n + j]; a[k * n + j] = t; }
+      det = -det;
+    }
+    det = det * a[k * n + k];
+    for (int i = k + 1; i < n; ++i) {
+      const double piv = a[i * n + k] / a[k * n + k];
+      for (int j = k + 1; j < n; ++j) a[i * n + j] -= piv * a[k * n + j];
+    }
+  }
+  return det;
+}
+
+/* ComputeW_fMLLR (OL_ModelAdapt.cpp:1614-1719) with ComputeKiGi_fMLLR (:1794-1848) and
+ * EstimateAb_fmllr (:1721-1792): per row i, G_i = sum_m (1/var_mi) [S_m F_m; F_m^T n_m] and
+ * k_i = sum_m (mu_mi/var_mi) [F_m; n_m] (the coefficients as float quotients), G_i inverted by
+ * pivot-free Gauss-Jordan; then `iters` passes over the rows starting from A = I, b = 0: the
+ * cofactors of A at the start of the pass (inv(A) det(A)), the quadratic in the row's scale
+ * factor and the root that maximises the row's auxiliary function. W = [A | b], D x (D+1).
+ * Returns 0, 3 (CheckInvertibility), or 5 (a negative discriminant or a zero root). */
+int orc_fmllr_w(int M, int D, const float* mu, const float* var, const double* n, const double* F,
+                const double* Sp, long long totN, int iters, double* W) {
+  const int E = D + 1;
+  const size_t P = (size_t)D * (D + 1) / 2;
+  if (M < E) return 3;
+  int active = 0;
+  double occ = 0.0;
+  for (int m = 0; m < M; ++m)
+    if (n[m] > 0) { ++active; occ += n[m]; }
+  if (active < E) return 3;
+  if (occ * D < (double)D * E) return 3;
+  double* G = (double*)calloc((size_t)D * E * E, sizeof(double));
+  double* Gi = (double*)malloc(sizeof(double) * (size_t)D * E * E);
+  double* K = (double*)calloc((size_t)D * E, sizeof(double));
+  for (int i = 0; i < D; ++i) {
+    double* g = G + (size_t)i * E * E;
+    double* k = K + (size_t)i * E;
+    for (int m = 0; m < M; ++m) {
+      const double mp = n[m];
+      if (!(mp > 0)) continue;
+      const float fv = 1.0f / var[(size_t)m * D + i];
+      const float fm = mu[(size_t)m * D + i] / var[(size_t)m * D + i];
+      const double cv = fv, cm = fm;
+      const double* Fm = F + (size_t)m * D;
+      const double* Sm = Sp + (size_t)m * P;
+      size_t e = 0;
+      for (int a = 0; a < D; ++a) {
+        k[a] += cm * Fm[a];
+        for (int b = a; b < D; ++b) {
+          g[a * E + b] += cv * Sm[e++];
+          g[b * E + a] = g[a * E + b];
+        }
+        g[a * E + D] += cv * Fm[a];
+        g[D * E + a] = g[a * E + D];
+      }
+      k[D] += cm * mp;
+      g[D * E + D] += cv * mp;
+    }
+    memcpy(Gi + (size_t)i * E * E, g, sizeof(double) * (size_t)E * E);
+    orc_gj_invert(E, Gi + (size_t)i * E * E);
+  }
+  double* A = (double*)calloc((size_t)D * D, sizeof(double));
+  double* b = (double*)calloc((size_t)D, sizeof(double));
+  double* cofm = (double*)malloc(sizeof(double) * (size_t)D * D);
+  double* tmp = (double*)malloc(sizeof(double) * (size_t)D * D);
+  double* c = (double*)calloc((size_t)E, sizeof(double));
+  double* foo = (double*)malloc(sizeof(double) * (size_t)E);
+  double* wv = (double*)malloc(sizeof(double) * (size_t)E);
+  double* w2 = (double*)malloc(sizeof(double) * 2 * (size_t)E);
+  int rc = 0;
+  for (int d = 0; d < D; ++d) A[d * D + d] = 1.0;
+  const double aa = (double)(float)totN;
+  for (int it = 0; it < iters && !rc; ++it) {
+    memcpy(cofm, A, sizeof(double) * (size_t)D * D);
+    orc_gj_invert(D, cofm);
+    memcpy(tmp, A, sizeof(double) * (size_t)D * D);
+    const double det = det_gen(D, tmp);
+    for (int e = 0; e < D * D; ++e) cofm[e] *= det;
+    for (int i = 0; i < D && !rc; ++i) {
+      const double* g = G + (size_t)i * E * E;
+      const double* gi = Gi + (size_t)i * E * E;
+      const double* k = K + (size_t)i * E;
+      for (int a = 0; a < D; ++a) c[a] = cofm[a * D + i];
+      c[D] = 0.0;
+      for (int q = 0; q < E; ++q) {
+        double s = 0.0;
+        for (int p = 0; p < E; ++p) s += c[p] * gi[p * E + q];
+        foo[q] = s;
+      }
+      double bb = 0.0, cc = 0.0;
+      for (int q = 0; q < E; ++q) bb += foo[q] * k[q];
+      for (int q = 0; q < E; ++q) cc += foo[q] * c[q];
+      bb *= -1.0;
+      cc *= -1.0;
+      const double sqrtD = sqrt(bb * bb - 4 * aa * cc);
+      if (sqrtD < 0 || isnan(sqrtD)) { rc = 5; break; }
+      const double f[2] = {(-bb + sqrtD) / (2 * aa), (-bb - sqrtD) / (2 * aa)};
+      double Q[2];
+      for (int j = 0; j < 2; ++j) {
+        if (f[j] == 0) { rc = 5; break; }
+        for (int a = 0; a <= D; ++a) wv[a] = c[a] / f[j] + k[a];
+        double* wj = w2 + (size_t)j * E;
+        for (int q = 0; q < E; ++q) {
+          double s = 0.0;
+          for (int p = 0; p < E; ++p) s += wv[p] * gi[p * E + q];
+          wj[q] = s;
+        }
+        Q[j] = 0.0;
+        for (int a = 0; a <= D; ++a) {
+          double s = 0.0;
+          for (int q = 0; q < E; ++q) s += g[a * E + q] * wj[q];
+          Q[j] += wj[a] * (k[a] - 0.5 * s);
+        }
+      }
+      if (rc) break;
+      const double* best = w2 + (size_t)(Q[0] > Q[1] ? 0 : 1) * E;
+      for (int a = 0; a < D; ++a) A[i * D + a] = best[a];
+      b[i] = best[D];
+    }
+  }
+  if (!rc)
+    for (int i = 0; i < D; ++i) {
+      for (int j = 0; j < D; ++j) W[(size_t)i * E + j] = A[i * D + j];
+      W[(size_t)i * E + D] = b[i];
+    }
+  free(G); free(Gi); free(K); free(A); free(b); free(cofm); free(tmp); free(c); free(foo); free(wv); free(w2);
+  return rc;
+}

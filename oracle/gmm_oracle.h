@@ -104,6 +104,15 @@ void orc_full_map_update(int M, int D, float* w, float* mu, float* cov, const fl
                          const float* ubm_mu, const float* ubm_cov, const double* n, const double* F,
                          const double* Sp, long long totN, int tau, int upW, int upM, int upV);
 
+/* fMLLR: the E-step of a diagonal model with packed full second-order statistics (FP64), and
+ * ComputeW_fMLLR from such statistics (W: D x (D+1) row-major). Return 0, 3 (CheckInvertibility)
+ * or 5 (EstimateAb_fmllr: negative discriminant or zero root). */
+int orc64_accumulate_fullstats(const float* X, long long N, int D, int M, const float* w,
+                               const float* mu, const float* var, const orc_opts* o, double* n,
+                               double* F, double* Sp, double* totLL, long long* totN);
+int orc_fmllr_w(int M, int D, const float* mu, const float* var, const double* n, const double* F,
+                const double* Sp, long long totN, int iters, double* W);
+
 #ifdef __cplusplus
 }
 #endif

@@ -428,3 +428,40 @@ int ref_full_adapt(const float* X, long N, int D, int M, float* w, float* mu, fl
 }
 
 }  // extern "C"
+
+extern "C" {
+
+// fMLLR (CModelAdapt::ComputeW_fMLLR, OL_ModelAdapt.cpp:1614-1719) of a diagonal UBM: W is
+// D x (D+1) row-major; n, F, Sp receive the E-step statistics it used (packed full second order).
+int ref_fmllr(const float* X, long N, int D, int M, const float* w, const float* mu, const float* var,
+              int threads, double* W, double* n, double* F, double* Sp, double* totLL) {
+  try {
+    GMModel* ubm = make_model(M, D, w, mu, var);
+    CModelAdapt cm;
+    CModelAdapt::OPTIONS opt = base_options(threads, 0);
+    opt._adaptType = fMLLR;
+    cm.SetOptions(opt);
+    Param p;
+    fill_param(p, X, N, D);
+    cm.InsertData(p, false);
+    cm.Initialize(ubm);
+    cm._UBM = ubm;
+    MATRIX* Wm = cm.ComputeW_fMLLR(ubm);
+    for (int i = 0; i < D; ++i)
+      for (int j = 0; j <= D; ++j) W[(size_t)i * (D + 1) + j] = Wm->GetXY(i, j);
+    const size_t P = (size_t)D * (D + 1) / 2;
+    for (int m = 0; m < M; ++m) {
+      n[m] = cm._stats.getProb(m);
+      for (int d = 0; d < D; ++d) F[(size_t)m * D + d] = cm._stats.getMean(m)[d];
+      for (size_t q = 0; q < P; ++q) Sp[(size_t)m * P + q] = cm._stats.getVar(m)[q];
+    }
+    *totLL = cm._stats.getTotLogLike();
+    Wm->Delete();
+    delete Wm;
+    delete ubm;
+    return 0;
+  } catch (std::exception& ex) { g_err = ex.what(); return 1; }
+  catch (Exception* ex) { g_err = ex->m_strDescription; delete ex; return 2; }
+}
+
+}  // extern "C"

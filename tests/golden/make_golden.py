@@ -24,6 +24,9 @@ from their own sources, see oracle/Makefile) and records its outputs on small in
   iterations (weights, means, covariances) and one MAP iteration (tau = 16, all parameters) of
   a seeded full-covariance model. The reference's single-precision LAPACK calls go through the
   restatement in oracle/ref/shim/acml.h.
+* ``fmllr.npz``    -- fMLLR (ComputeW_fMLLR, 20 passes) of a diagonal UBM (M = 32, D = 12) from
+  one speaker of seeded affinely transformed UBM samples: the transform and the E-step
+  statistics (packed full second order) it was computed from.
 """
 from __future__ import annotations
 
@@ -114,6 +117,7 @@ def main():
 
     train_fixture()
     full_fixture(a.ref_root)
+    fmllr_fixture()
 
 
 def full_fixture(ref_root):
@@ -135,6 +139,14 @@ def full_fixture(ref_root):
     np.savez_compressed(os.path.join(HERE, "full.npz"), **out)
 
 
+def fmllr_fixture():
+    X, offs, (uw, umu, uvar), _ = synth.c4(5, 2, 32, 12, 3000, 4000)
+    X = X[offs[0]:offs[1]]
+    W, st = O.ref_fmllr(X, uw, umu, uvar, threads=1)
+    np.savez_compressed(os.path.join(HERE, "fmllr.npz"), X=X, w=uw, mu=umu, var=uvar, W=W, n=st["n"], F=st["F"],
+                        Sp=st["Sp"], totLL=st["totLL"])
+
+
 def train_fixture():
     """TrainFromScratch (OL_ModelAdapt.cpp:667-821) by the reference build on seeded data."""
     gw, gmu, gvar = synth.generator_gmm(31, 6, 5)
@@ -154,5 +166,8 @@ if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "--full-only":
         O.build(ref=True)
         full_fixture("/root/reference/GMM")
+    elif len(sys.argv) > 1 and sys.argv[1] == "--fmllr-only":
+        O.build(ref=True)
+        fmllr_fixture()
     else:
         main()

@@ -160,3 +160,16 @@ def test_full_model_files(tmp_path):
         assert r.full and r.var.shape == (4, 7, 7)
         tol = 1e-6 if ext == "txt" else 0
         assert np.allclose(r.var, cov[keep], rtol=tol) and np.allclose(r.mu, mu[keep], rtol=tol, atol=1e-7)
+
+
+def test_fmllr_oracle_against_reference(oracle, golden):
+    """fMLLR: the restatement is bit-identical to the reference given the reference's own
+    statistics; from the FP64 oracle's statistics W agrees within 1e-6 (abs) of the
+    reference's W."""
+    g = golden("fmllr.npz")
+    st = dict(n=g["n"], F=g["F"], Sp=g["Sp"], totN=len(g["X"]))
+    assert np.array_equal(oracle.fmllr_w(g["mu"], g["var"], st), g["W"])
+    s64 = oracle.accumulate64_fullstats(g["X"], g["w"], g["mu"], g["var"])
+    for k in ("n", "F", "Sp"):
+        assert np.abs(s64[k] - g[k]).max() <= 1e-6 * np.abs(g[k]).max(), k
+    assert np.abs(oracle.fmllr_w(g["mu"], g["var"], s64) - g["W"]).max() < 1e-6
