@@ -318,7 +318,7 @@ class ModelAdapt:
         return out
 
     def AdaptModel(self, ubm: GMModel):
-        """``CModelAdapt::AdaptModel`` (OL_ModelAdapt.cpp:1163-1226) for MAP and MLLR."""
+        """``CModelAdapt::AdaptModel`` (OL_ModelAdapt.cpp:1163-1226): MAP, MLLR, fMLLR, MLLR+MAP."""
         o = self.opt
         if o.adaptType == MAP:
             model = ubm.copy()
@@ -339,9 +339,25 @@ class ModelAdapt:
             self._W = self.IterW_MLLR(ubm, o.iterMLLR)
             if o.applyTransforms:
                 self._model = self.AdaptModelMLLR(ubm, self._W)
+        elif o.adaptType == MLLR_MAP:
+            # MLLR of the UBM, then AdaptModelMAP of the transformed model with the original
+            # UBM as the MAP prior (OL_ModelAdapt.cpp:1190-1205)
+            if ubm.full:
+                raise NotImplementedError("MLLR of full-covariance models is not built")
+            try:
+                W = self.IterW_MLLR(ubm, o.iterMLLR)
+                model = self.AdaptModelMLLR(ubm, W)
+            except _lib.GMMError as e:
+                if e.code != _lib.ERR_MLLR:
+                    raise
+                model = ubm.copy()  # not enough data for MLLR: MAP only, as the reference warns
+            if o.iterCountEM:
+                model = self.IterEM(model, o.iterCountEM)
+            if o.iterCountMAP:
+                model = self.IterMAP(model, ubm, o.iterCountMAP)
+            self._model = model
         else:
-            raise NotImplementedError("only MAP (incl. EM with tau = 0) and MLLR are on the "
-                                      "diagonal hot path")
+            raise NotImplementedError("adaptation type not built")
 
     def PickUpClientModel(self) -> GMModel | None:
         m, self._model = self._model, None

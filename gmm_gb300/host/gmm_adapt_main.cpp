@@ -2,7 +2,8 @@
 // (Model_ADAPT.cpp:106-263) on one GB300, with the reference's option names
 // (loadConfiguration / checkOptions, Model_ADAPT.cpp:276-475, and CModelAdapt::GetOptions,
 // OL_ModelAdapt.cpp:2032-2132): train from scratch (no input model, --nummix), MAP / EM
-// (--type 2), MLLR (--type 1) or fMLLR (--type 3) from SVES / HTK / RAW feature files; one model for all inputs
+// (--type 2), MLLR (--type 1), fMLLR (--type 3) or MLLR+MAP (--type 4) from SVES / HTK / RAW
+// feature files; one model for all inputs
 // (-o), one per input file (--model-file-mode) or one per class (-S, CLASS mode).
 #include <cstdio>
 #include <iostream>
@@ -42,7 +43,7 @@ std::vector<gmmgb::cli::Opt> options() {
       {"save-in-stat-form", 0, FLAG, "0", "save the model (or MLLR transform) in the GMMStats file layout"},
       {"dwnsmp", 0, STR, "1", "down-sample factor of the feature vectors"},
       {"verbosity", 'v', STR, "0", "verbose mode"},
-      {"type", 't', STR, "2", "FROM_SCRATCH=0, MLLR=1, MAP=2, fMLLR=3"},
+      {"type", 't', STR, "2", "FROM_SCRATCH=0, MLLR=1, MAP=2, fMLLR=3, MLLR+MAP=4"},
       {"split-X", 0, STR, "0", "(FROM_SCRATCH) fraction of Gaussians split at once per round"},
       {"split-th", 0, STR, "0", "(FROM_SCRATCH) split only weights above split-th * max weight"},
       {"ll-Th", 0, STR, "0", "(FROM_SCRATCH) stop when the log-likelihood gain is below this"},
@@ -112,9 +113,8 @@ int main(int argc, char** argv) {
 
     gmmgb::AdaptOptions o;
     o.adaptType = from_scratch ? gmmgb::FROM_SCRATCH : P.get_int("type");
-    if (o.adaptType != gmmgb::MLLR && o.adaptType != gmmgb::MAP && o.adaptType != gmmgb::FROM_SCRATCH &&
-        o.adaptType != gmmgb::FMLLR)
-      throw std::runtime_error("--type must be 0, 1, 2 or 3 (MLLR+MAP is not supported)");
+    if (o.adaptType < gmmgb::FROM_SCRATCH || o.adaptType > gmmgb::MLLR_MAP)
+      throw std::runtime_error("--type must be 0 (from scratch), 1 (MLLR), 2 (MAP), 3 (fMLLR) or 4 (MLLR+MAP)");
     o.tau = P.get_int("tau");
     o.iterCountEM = P.get_int("it-EM");
     o.iterCountMAP = P.get_int("it-MAP");

@@ -517,6 +517,24 @@ std::vector<double> compose(const std::vector<double>& Ws, const std::vector<dou
 }
 }  // namespace
 
+// IterW_MLLR (OL_ModelAdapt.cpp:1365-1415): iterMLLR transforms, each estimated on the model the
+// previous ones produced, composed into one.
+std::vector<double> ModelAdapt::IterW_MLLR(const GMModel& ubm) {
+  GMModel u = ubm;
+  std::vector<double> W = ComputeW_MLLR(u, ubm);
+  if (o_.iterMLLR > 1) {
+    GMModel sp = AdaptModelMLLR(ubm, W);
+    for (int it = 1; it < o_.iterMLLR - 1; ++it) {
+      std::vector<double> Wt = ComputeW_MLLR(sp, ubm);
+      sp = AdaptModelMLLR(sp, Wt);
+      W = compose(W, Wt, D_);
+    }
+    std::vector<double> Wt = ComputeW_MLLR(sp, ubm);
+    W = compose(W, Wt, D_);
+  }
+  return W;
+}
+
 void ModelAdapt::AdaptModel(const GMModel& ubm) {
   if (o_.adaptType == MAP) {
     GMModel model = ubm;
@@ -525,24 +543,26 @@ void ModelAdapt::AdaptModel(const GMModel& ubm) {
     model_ = model;
     trained_ = true;
   } else if (o_.adaptType == MLLR) {
-    // IterW_MLLR (OL_ModelAdapt.cpp:1365-1415)
-    GMModel u = ubm;
-    std::vector<double> W = ComputeW_MLLR(u, ubm);
-    if (o_.iterMLLR > 1) {
-      GMModel sp = AdaptModelMLLR(ubm, W);
-      for (int it = 1; it < o_.iterMLLR - 1; ++it) {
-        std::vector<double> Wt = ComputeW_MLLR(sp, ubm);
-        sp = AdaptModelMLLR(sp, Wt);
-        W = compose(W, Wt, D_);
-      }
-      std::vector<double> Wt = ComputeW_MLLR(sp, ubm);
-      W = compose(W, Wt, D_);
-    }
-    W_ = W;
+    W_ = IterW_MLLR(ubm);
     if (o_.applyTransforms) {
       model_ = AdaptModelMLLR(ubm, W_);
       trained_ = true;
     }
+  } else if (o_.adaptType == MLLR_MAP) {
+    // MLLR of the UBM, then AdaptModelMAP of the transformed model against the original UBM
+    // (OL_ModelAdapt.cpp:1190-1205); without enough data for MLLR, MAP alone
+    GMModel model = ubm;
+    try {
+      model = AdaptModelMLLR(ubm, IterW_MLLR(ubm));
+    } catch (const std::runtime_error& e) {
+      if (std::string(e.what()).find("CheckInvertibility") == std::string::npos) throw;
+      std::fprintf(stderr, "[WARNING: not enough data to perform MLLR adaptation -> only MAP performed]\n");
+      model = ubm;
+    }
+    if (o_.iterCountEM) IterEM(model, o_.iterCountEM);
+    if (o_.iterCountMAP) IterMAP(model, ubm, o_.iterCountMAP);
+    model_ = model;
+    trained_ = true;
   } else if (o_.adaptType == FMLLR) {  // ComputeW_fMLLR(_UBM): the transform is the result
     if (ubm.GetFullCovStatus()) fail("ComputeW_fMLLR(): fMLLR of full-covariance models is not built");
     GMModel u = ubm;

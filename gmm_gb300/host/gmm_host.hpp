@@ -116,7 +116,7 @@ class GMMStatsEstimatorGB300 {
 
 // The options of CModelAdapt::OPTIONS on the diagonal hot path (defaults of GetOptions,
 // OL_ModelAdapt.cpp:2032-2132).
-enum AdaptType { FROM_SCRATCH = 0, MLLR = 1, MAP = 2, FMLLR = 3 };
+enum AdaptType { FROM_SCRATCH = 0, MLLR = 1, MAP = 2, FMLLR = 3, MLLR_MAP = 4 };
 struct AdaptOptions {
   int adaptType = MAP;
   int tau = 0;
@@ -142,7 +142,7 @@ class ModelAdapt {
   // InsertData(CFileList*) (file-by-file mode): every E-step streams the files through
   // gmm_accumulate_files in batches of at most buffer_gb instead of keeping the frames resident.
   void InsertFiles(const std::vector<std::string>& paths, int prm_type, unsigned dwnsmp, double buffer_gb);
-  // AdaptModel (OL_ModelAdapt.cpp:1163-1226): MAP (IterEM then IterMAP), MLLR or fMLLR.
+  // AdaptModel (OL_ModelAdapt.cpp:1163-1226): MAP (IterEM then IterMAP), MLLR, fMLLR or MLLR+MAP.
   void AdaptModel(const GMModel& ubm);
   // TrainFromScratch (OL_ModelAdapt.cpp:667-821), diagonal covariances; `init` (optional) is the
   // model the splitting starts from instead of the global Gaussian. (The full-covariance split
@@ -171,6 +171,7 @@ class ModelAdapt {
   void IterEM(GMModel& model, int iters);
   void IterMAP(GMModel& model, const GMModel& ubm, int iters);
   std::vector<double> ComputeW_MLLR(GMModel& model, const GMModel& ubm);
+  std::vector<double> IterW_MLLR(const GMModel& ubm);
   GMModel AdaptModelMLLR(const GMModel& model, const std::vector<double>& W);
   void splitMultipleGaussians(GMModel& model);
   AdaptOptions o_;

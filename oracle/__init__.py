@@ -428,3 +428,19 @@ def ref_fmllr(X, w, mu, var, threads=1):
     if rc:
         raise RuntimeError(ref().ref_last_error().decode())
     return W, dict(n=n, F=F, Sp=Sp, totLL=tl.value, totN=N)
+
+
+def ref_adapt_model(X, w, mu, var, adapt_type, tau=16, it_em=0, it_map=1, it_mllr=1, mllr_init=False,
+                    upW=False, upM=True, upV=False, threads=1):
+    """CModelAdapt::AdaptModel of the reference build (2 = MAP, 4 = MLLR+MAP)."""
+    X, w, mu, var = map(_f32, (X, w, mu, var))
+    N, D = X.shape
+    M = len(w)
+    ow, omu, ovar = np.zeros_like(w), np.zeros_like(mu), np.zeros_like(var)
+    rc = ref().ref_adapt_model(_p(X), C.c_long(N), D, M, _p(w), _p(mu), _p(var), int(adapt_type), int(tau),
+                               int(it_em), int(it_map), int(it_mllr), int(mllr_init), int(upW), int(upM),
+                               int(upV), threads,
+                               _p(ow), _p(omu), _p(ovar))
+    if rc:
+        raise RuntimeError(ref().ref_last_error().decode())
+    return ow, omu, ovar

@@ -465,3 +465,40 @@ int ref_fmllr(const float* X, long N, int D, int M, const float* w, const float*
 }
 
 }  // extern "C"
+
+extern "C" {
+
+// CModelAdapt::AdaptModel (OL_ModelAdapt.cpp:1163-1226) of a diagonal UBM with the given
+// adaptation type (2 MAP, 4 MLLR+MAP), iterations and flags; the adapted model out.
+int ref_adapt_model(const float* X, long N, int D, int M, const float* w, const float* mu, const float* var,
+                    int type, int tau, int it_em, int it_map, int it_mllr, int mllr_init, int upW, int upM,
+                    int upV, int threads, float* ow, float* omu, float* ovar) {
+  try {
+    GMModel* ubm = make_model(M, D, w, mu, var);
+    CModelAdapt cm;
+    CModelAdapt::OPTIONS opt = base_options(threads, 0);
+    opt._adaptType = type;
+    opt._tau = tau;
+    opt._iterCountEM = it_em;
+    opt._iterCountMAP = it_map;
+    opt._iterMLLR = it_mllr;
+    opt._mllrUBMInit = mllr_init != 0;  // the OPTIONS default is true, the command line's false
+    opt._AdaptWeightBool = upW != 0;
+    opt._AdaptMeanBool = upM != 0;
+    opt._AdaptVarBool = upV != 0;
+    cm.SetOptions(opt);
+    Param p;
+    fill_param(p, X, N, D);
+    cm.InsertData(p, false);
+    cm.AdaptModel(ubm);
+    GMModel* model = cm.PickUpClientModel();
+    if (!model) throw std::runtime_error("no adapted model");
+    read_model(model, M, D, ow, omu, ovar);
+    delete model;
+    delete ubm;
+    return 0;
+  } catch (std::exception& ex) { g_err = ex.what(); return 1; }
+  catch (Exception* ex) { g_err = ex->m_strDescription; delete ex; return 2; }
+}
+
+}  // extern "C"

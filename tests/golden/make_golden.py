@@ -24,6 +24,8 @@ from their own sources, see oracle/Makefile) and records its outputs on small in
   iterations (weights, means, covariances) and one MAP iteration (tau = 16, all parameters) of
   a seeded full-covariance model. The reference's single-precision LAPACK calls go through the
   restatement in oracle/ref/shim/acml.h.
+* ``mllr_map.npz`` -- MLLR+MAP (adaptation type 4): one global MLLR transform, then one MAP
+  iteration (tau = 16, means and variances) of the transformed UBM against the original UBM.
 * ``fmllr.npz``    -- fMLLR (ComputeW_fMLLR, 20 passes) of a diagonal UBM (M = 32, D = 12) from
   one speaker of seeded affinely transformed UBM samples: the transform and the E-step
   statistics (packed full second order) it was computed from.
@@ -118,6 +120,7 @@ def main():
     train_fixture()
     full_fixture(a.ref_root)
     fmllr_fixture()
+    mllr_map_fixture()
 
 
 def full_fixture(ref_root):
@@ -137,6 +140,13 @@ def full_fixture(ref_root):
     mw, mmu, mcov, mll = O.ref_full_adapt(Xs, w, mu, cov, 16, 1, threads=2)
     out.update(map_w=mw, map_mu=mmu, map_cov=mcov, map_ll=mll)
     np.savez_compressed(os.path.join(HERE, "full.npz"), **out)
+
+
+def mllr_map_fixture():
+    g = dict(np.load(os.path.join(HERE, "map_mllr.npz")))
+    w, mu, var = O.ref_adapt_model(g["X"], g["w"], g["mu"], g["var"], 4, tau=16, it_map=1, upM=True, upV=True,
+                                   threads=2)
+    np.savez_compressed(os.path.join(HERE, "mllr_map.npz"), w=w, mu=mu, var=var)
 
 
 def fmllr_fixture():
@@ -166,6 +176,9 @@ if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "--full-only":
         O.build(ref=True)
         full_fixture("/root/reference/GMM")
+    elif len(sys.argv) > 1 and sys.argv[1] == "--mllr-map-only":
+        O.build(ref=True)
+        mllr_map_fixture()
     elif len(sys.argv) > 1 and sys.argv[1] == "--fmllr-only":
         O.build(ref=True)
         fmllr_fixture()

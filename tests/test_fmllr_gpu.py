@@ -76,3 +76,30 @@ def test_invertibility_check(dev, glib, golden):
     with pytest.raises(glib.GMMError) as e:
         dev.fmllr_estimate(20)
     assert e.value.code == glib.ERR_MLLR
+
+
+def test_mllr_map_matches_reference(glib, golden, tmp_path):
+    """MLLR+MAP (--type 4): the MLLR-transformed UBM, then one MAP iteration against the original
+    UBM; against the reference's AdaptModel (tests/golden/mllr_map.npz): means rel 1e-5 / abs
+    1e-5, variances rel 1e-4 / abs 1e-5, through the Python driver and the command line."""
+    from gmm_gb300 import adapt, build, formats
+    g = golden("map_mllr.npz")
+    want = golden("mllr_map.npz")
+    ma = adapt.ModelAdapt(adapt.Options(adaptType=adapt.MLLR_MAP, tau=16, iterCountMAP=1, AdaptMeanBool=True,
+                                        AdaptVarBool=True))
+    ma.InsertData(g["X"])
+    ma.AdaptModel(formats.GMModel(g["w"], g["mu"], g["var"]))
+    m = ma.PickUpClientModel()
+    assert np.allclose(m.mu, want["mu"], rtol=1e-5, atol=1e-5)
+    assert np.allclose(m.var, want["var"], rtol=1e-4, atol=1e-5)
+    feat = tmp_path / "s.prm"
+    formats.write_sves(str(feat), g["X"])
+    ubm = tmp_path / "ubm.gmm"
+    formats.write_gmm_bin(str(ubm), formats.GMModel(g["w"], g["mu"], g["var"]))
+    r = subprocess.run([os.path.join(build.OUT_DIR, "gmm_adapt"), "-i", str(feat), "-u", str(ubm), "-o",
+                        str(tmp_path / "s.gmm"), "-t", "4", "--it-MAP", "1", "-r", "16", "-M", "-V",
+                        "--precision", "fp32"], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    c = formats.read_gmm_bin(str(tmp_path / "s.gmm"))
+    assert np.allclose(c.mu, want["mu"], rtol=1e-5, atol=1e-5)
+    assert np.allclose(c.var, want["var"], rtol=1e-4, atol=1e-5)

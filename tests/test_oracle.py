@@ -173,3 +173,18 @@ def test_fmllr_oracle_against_reference(oracle, golden):
     for k in ("n", "F", "Sp"):
         assert np.abs(s64[k] - g[k]).max() <= 1e-6 * np.abs(g[k]).max(), k
     assert np.abs(oracle.fmllr_w(g["mu"], g["var"], s64) - g["W"]).max() < 1e-6
+
+
+def test_mllr_map_oracle_against_reference(oracle, golden):
+    """MLLR+MAP: MLLR of the UBM (no UBM initialisation, the command-line default), then MAP of
+    the transformed model against the original UBM -- the port reproduces the reference's
+    AdaptModel bit for bit."""
+    g = golden("map_mllr.npz")
+    want = golden("mllr_map.npz")
+    X, w, mu, var = g["X"], g["w"], g["mu"], g["var"]
+    st = oracle.accumulate32(X, w, mu, var, flags=oracle.ACC_MEAN, threads=2)
+    mu2 = oracle.mllr_apply(mu, oracle.mllr_w(mu, var, st))
+    st2 = oracle.accumulate32(X, w, mu2, var, flags=oracle.ACC_MEAN | oracle.ACC_VAR, threads=2)
+    _, omu, ovar = oracle.map_update(w, mu, var, st2, 16, w=w.copy(), mu=mu2.copy(), var=var.copy(),
+                                     upM=True, upV=True)
+    assert np.array_equal(omu, want["mu"]) and np.array_equal(ovar, want["var"])
