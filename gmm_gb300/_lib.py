@@ -30,6 +30,8 @@ SIGNATURES = {
     "gmm_upload_model": (_i, [_vp, _i, _i, _vp, _vp, _vp]),
     "gmm_upload_model_full": (_i, [_vp, _i, _i, _vp, _vp, _vp]),
     "gmm_fmllr_estimate": (_i, [_vp, _i, _vp]),
+    "gmm_set_robust": (_i, [_vp, _i]),
+    "gmm_read_aux": (_i, [_vp, _i, _vp, _vp, _vp]),
     "gmm_fmllr_apply": (_i, [_vp, _vp]),
     "gmm_set_prior_full": (_i, [_vp, _vp, _vp, _vp]),
     "gmm_read_model_full": (_i, [_vp, _vp, _vp, _vp]),
@@ -257,6 +259,16 @@ class Handle:
 
     def map_update(self, tau, upW=False, upM=True, upV=False):
         self.check(self.lib.gmm_map_update(self.h, int(tau), int(upW), int(upM), int(upV)))
+
+    # -- --robust
+    def set_robust(self, on=True):
+        self.check(self.lib.gmm_set_robust(self.h, int(on)))
+
+    def read_aux(self, full=False):
+        M, D = (self.Mf, self.Df) if full else (self.M, self.D)
+        aux, aux2, aux3 = np.zeros((M, D)), np.zeros(M), np.zeros(M)
+        self.check(self.lib.gmm_read_aux(self.h, int(full), ptr(aux), ptr(aux2), ptr(aux3)))
+        return dict(aux=aux, aux2=aux2, aux3=aux3)
 
     # -- fMLLR
     def fmllr_estimate(self, iters=20):

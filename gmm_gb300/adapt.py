@@ -37,6 +37,7 @@ class Options:
     splitTh: float = 0.0            # --split-th
     llTh: float = 0.0               # --ll-Th
     verbosity: int = 0
+    robustCov: bool = False         # --robust
     precision: int = _lib.PREC_FP32
 
 
@@ -105,6 +106,7 @@ class ModelAdapt:
         self.opt = options or Options()
         self.dev = _lib.Handle(device)
         self.dev.set_precision(self.opt.precision)
+        self.dev.set_robust(self.opt.robustCov)
         self._X = None
         self._model: GMModel | None = None
         self._W = None
@@ -113,6 +115,7 @@ class ModelAdapt:
     def SetOptions(self, opt: Options):
         self.opt = opt
         self.dev.set_precision(opt.precision)
+        self.dev.set_robust(opt.robustCov)
 
     def InsertData(self, X: np.ndarray):
         self._X = np.ascontiguousarray(X, np.float32)

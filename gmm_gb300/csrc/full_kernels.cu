@@ -46,6 +46,9 @@ struct FullModel {
   int acc_flags = 0;
   long long tot_frames = 0;
   bool dirty = true;
+  double* aux = nullptr;  // --robust auxiliary statistics [M x D | M | M]
+  size_t aux_cap = 0;
+  bool aux_valid = false;
   size_t stats_count() const { return (size_t)M * (1 + D + P) + 2; }
 };
 
@@ -443,7 +446,8 @@ __global__ void full_ll_total_kernel(int nblocks, const double* __restrict__ llp
 // flag[6] <- components that had zero weight before the update.
 __global__ void full_em_kernel(int M, int D, int P, float* __restrict__ w, float* __restrict__ mu,
                                float* __restrict__ cov, const double* __restrict__ stats,
-                               unsigned int tot, int upW, int upM, int upV, int* __restrict__ flag) {
+                               unsigned int tot, int upW, int upM, int upV, const double* __restrict__ nind,
+                               int* __restrict__ flag) {
   __shared__ float s_mean[kFullMaxDim];
   const int j = blockIdx.x, t = threadIdx.x;
   const double* n = stats;
@@ -456,7 +460,7 @@ __global__ void full_em_kernel(int M, int D, int P, float* __restrict__ w, float
   const double mp = n[j];
   float* mj = mu + (size_t)j * D;
   float* C = cov + (size_t)j * D * D;
-  if (mp < 2.0) {  // _MIN_IND_SAMPLES_: GMMMixture::Reset -> mean 0, identity covariance
+  if ((nind ? nind[j] : mp) < 2.0) {  // _MIN_IND_SAMPLES_ (robust: on nind): Reset -> mean 0, identity
     for (int e = t; e < D * D; e += blockDim.x) C[e] = (e / D == e % D) ? 1.0f : 0.0f;
     for (int k = t; k < D; k += blockDim.x) mj[k] = 0.0f;
     if (t == 0) {
@@ -578,6 +582,7 @@ void free_full(Ctx* c) {
   dfree(c, f->act, sizeof(int) * (size_t)f->M);
   dfree(c, f->pw, m1); dfree(c, f->pmu, md); dfree(c, f->pcov, mdd);
   dfree(c, f->stats, sizeof(double) * f->stats_count());
+  dfree(c, f->aux, f->aux_cap);
   *f = FullModel();
 }
 
@@ -786,6 +791,10 @@ int full_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
       full_reduce_kernel<<<(int)((tot + 255) / 256), 256, 0, c->stream>>>(f->M, D, f->P, f->Mact, f->act,
                                                                           (int)slices, c->part, f->stats);
     }
+    if (c->robust && f->aux) {
+      const int rc2 = robust_chunk(c, f->M, D, f->Mact, f->act, f0, nf, chunk, f->aux);
+      if (rc2) return rc2;
+    }
   }
   return GMM_OK;
 }
@@ -796,11 +805,17 @@ int full_accumulate_device(Ctx* c, int flags) {
   cudaError_t e = cudaMemsetAsync(f->stats, 0, sizeof(double) * f->stats_count(), c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "cudaMemsetAsync(full statistics)");
   f->stats_valid = false;
+  f->aux_valid = false;
+  if (c->robust) {
+    const int rc0 = ensure_aux(c, &f->aux, &f->aux_cap, f->M, f->D);
+    if (rc0) return rc0;
+  }
   int rc = full_estep(c, flags, true, nullptr);
   if (rc) return rc;
   f->tot_frames = c->N;
   f->acc_flags = flags;
   f->stats_valid = true;
+  f->aux_valid = c->robust;
   return sync(c, "full-covariance E-step");
 }
 
@@ -863,6 +878,15 @@ int diag_fullstats_estep(Ctx* c, double* stats) {
     }
   }
   return GMM_OK;
+}
+
+bool full_aux(Ctx* c, const double** aux, int* M, int* D) {
+  FullModel* f = c->full;
+  if (!f || !f->aux_valid) return false;
+  *aux = f->aux;
+  *M = f->M;
+  *D = f->D;
+  return true;
 }
 
 void full_destroy(Ctx* c) {
@@ -970,12 +994,18 @@ int gmm_em_update_full(gmm_handle h, int upW, int upM, int upV, int* alive) {
   FullModel* f = c->full;
   if (!f || !f->stats_valid) return fail(c, GMM_ERR_STATE, "no statistics accumulated");
   cudaSetDevice(c->device);
+  double* nind = nullptr;
+  if (c->robust && f->aux_valid) {  // UpdateModelEM with _robustCov: MakeRobustStats first
+    const int rc0 = robust_make(c, f->M, f->D, 1, f->stats, f->aux, &nind);
+    if (rc0) return rc0;
+    f->aux_valid = false;
+  }
   cudaMemsetAsync(c->flag + 5, 0, 2 * sizeof(int), c->stream);
   const unsigned int tot = (unsigned int)f->tot_frames;
   {
     GMM_LAUNCH(c, "full_em_kernel");
     full_em_kernel<<<f->M, 128, 0, c->stream>>>(f->M, f->D, f->P, f->w, f->mu, f->cov, f->stats, tot, upW,
-                                                upM, upV, c->flag);
+                                                upM, upV, nind, c->flag);
   }
   {
     GMM_LAUNCH(c, "full_em_norm_kernel");
@@ -999,6 +1029,12 @@ int gmm_map_update_full(gmm_handle h, int tau, int upW, int upM, int upV) {
   if (!f || !f->stats_valid) return fail(c, GMM_ERR_STATE, "no statistics accumulated");
   if (!f->have_prior) return fail(c, GMM_ERR_STATE, "MAP needs a prior model (gmm_set_prior_full)");
   cudaSetDevice(c->device);
+  if (c->robust && f->aux_valid) {  // UpdateModelMAP with _robustCov: MakeRobustStats first
+    double* nind = nullptr;
+    const int rc0 = robust_make(c, f->M, f->D, 1, f->stats, f->aux, &nind);
+    if (rc0) return rc0;
+    f->aux_valid = false;
+  }
   const unsigned int tot = (unsigned int)f->tot_frames;
   {
     GMM_LAUNCH(c, "full_map_kernel");

@@ -173,7 +173,8 @@ static int estep(Ctx* c, int flags, bool want_stats, float* ll_dev) {
     rc = plain_precompute(c);
     if (rc) return rc;
   }
-  if (c->precision == GMM_PREC_TC) return tc_estep(c, flags, want_stats, ll_dev);
+  // robust statistics need the per-frame posteriors, which only the plain E-step writes out
+  if (c->precision == GMM_PREC_TC && !(c->robust && want_stats)) return tc_estep(c, flags, want_stats, ll_dev);
   return plain_estep(c, flags, want_stats, ll_dev);
 }
 
@@ -184,11 +185,17 @@ static int accumulate_device(Ctx* c, int flags) {
                                   c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "cudaMemsetAsync(stats)");
   c->stats_valid = false;
+  c->aux_valid = false;
+  if (c->robust) {
+    const int rc = ensure_aux(c, &c->aux, &c->aux_cap, c->M, c->D);
+    if (rc) return rc;
+  }
   int rc = estep(c, flags, true, nullptr);
   if (rc) return rc;
   c->tot_frames = c->N;
   c->acc_flags = flags;
   c->stats_valid = true;
+  c->aux_valid = c->robust;
   return GMM_OK;
 }
 
@@ -261,6 +268,10 @@ int gmm_destroy(gmm_handle h) {
   cudaStreamSynchronize(c->stream);
   drain_timers(c);
   full_destroy(c);
+  dfree(c, c->aux, c->aux_cap);
+  dfree(c, c->gs, c->gs_cap * sizeof(float));
+  dfree(c, c->gprev, c->gprev_cap * sizeof(float));
+  dfree(c, c->nind, c->nind_cap * sizeof(double));
   free_model(c);
   free_features(c);
   dfree(c, c->logits, c->logits_cap);
@@ -467,6 +478,26 @@ int gmm_loglikes(gmm_handle h, float* out) {
     if (e != cudaSuccess) return cuda_fail(c, e, "cudaMemcpyAsync(loglikes)");
   }
   return sync(c, "gmm_loglikes");
+}
+
+int gmm_read_aux(gmm_handle h, int full, double* aux, double* aux2, double* aux3) {
+  if (!h) return GMM_ERR_ARG;
+  Ctx* c = h;
+  const double* src = nullptr;
+  int M = 0, D = 0;
+  if (full) {
+    if (!c->full || !full_aux(c, &src, &M, &D)) return fail(c, GMM_ERR_STATE, "no auxiliary statistics accumulated");
+  } else {
+    if (!c->aux_valid) return fail(c, GMM_ERR_STATE, "no auxiliary statistics accumulated");
+    src = c->aux;
+    M = c->M;
+    D = c->D;
+  }
+  cudaSetDevice(c->device);
+  if (aux) cudaMemcpyAsync(aux, src, sizeof(double) * (size_t)M * D, cudaMemcpyDeviceToHost, c->stream);
+  if (aux2) cudaMemcpyAsync(aux2, src + (size_t)M * D, sizeof(double) * M, cudaMemcpyDeviceToHost, c->stream);
+  if (aux3) cudaMemcpyAsync(aux3, src + (size_t)M * D + M, sizeof(double) * M, cudaMemcpyDeviceToHost, c->stream);
+  return sync(c, "gmm_read_aux");
 }
 
 int gmm_em_update(gmm_handle h, int upW, int upM, int upV, int* alive) {
@@ -896,7 +927,7 @@ int gmm_em_iterate(gmm_handle h, int iters, int upW, int upM, int upV, double* l
   Ctx* c = h;
   if (iters < 0) return fail(c, GMM_ERR_ARG, "iters must be >= 0");
   cudaSetDevice(c->device);
-  if (c->precision == GMM_PREC_TC && iters > 0) {
+  if (c->precision == GMM_PREC_TC && iters > 0 && !c->robust) {
     if (!c->w) return fail(c, GMM_ERR_STATE, "no model uploaded");
     if (!c->X || c->N == 0) return fail(c, GMM_ERR_STATE, "no features uploaded");
     if (c->Dx != c->D) return fail(c, GMM_ERR_ARG, "Inconsistent model & feature vector - different dimensions");

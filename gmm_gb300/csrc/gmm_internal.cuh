@@ -120,6 +120,19 @@ struct Ctx {
   // full-covariance model (own parameters and statistics; shares the features and scratch)
   FullModel* full = nullptr;
 
+  // --robust: auxiliary statistics of the diagonal model [aux (M x D) | aux2 (M) | aux3 (M)],
+  // per-frame gs of a chunk, the previous chunk's last posteriors, independent-frame counts
+  bool robust = false;
+  double* aux = nullptr;
+  size_t aux_cap = 0;
+  bool aux_valid = false;
+  float* gs = nullptr;
+  size_t gs_cap = 0;
+  float* gprev = nullptr;
+  size_t gprev_cap = 0;
+  double* nind = nullptr;
+  size_t nind_cap = 0;
+
   // timing
   bool profile = false;
   std::vector<KernelTimer> timers;
@@ -246,6 +259,15 @@ int sync(Ctx* c, const char* what);
 
 // Full-covariance model state (allocated on the first gmm_upload_model_full).
 void full_destroy(Ctx* c);
+
+// --robust: auxiliary statistics of frames [f0, f0 + nf) from the chunk's log joints (c->logits,
+// ldg) and LLs into aux (caller order, M components); GetNIndFrames + MakeRobustStats on the
+// device statistics (second-order part modified in place), *nind -> the device counts.
+int robust_chunk(Ctx* c, int M, int D, int Mact, const int* act, long long f0, long long nf, long long ldg,
+                 double* aux);
+int robust_make(Ctx* c, int M, int D, int full, double* stats, const double* aux, double** nind);
+int ensure_aux(Ctx* c, double** aux, size_t* cap, int M, int D);
+bool full_aux(Ctx* c, const double** aux, int* M, int* D);  // the full model's valid auxiliary statistics
 
 }  // namespace gmm
 

@@ -24,7 +24,7 @@ __device__ __forceinline__ float reset_var_value() {
 __global__ void em_comp_kernel(int M, int D, float* __restrict__ w, float* __restrict__ mu,
                                float* __restrict__ var, const double* __restrict__ stats,
                                unsigned int tot, int upW, int upM, int upV, float min_var,
-                               int* __restrict__ flag) {
+                               const double* __restrict__ nind, int* __restrict__ flag) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= M) return;
   const double* n = stats;
@@ -34,7 +34,7 @@ __global__ void em_comp_kernel(int M, int D, float* __restrict__ w, float* __res
   double mp = n[j];
   float* mj = mu + (size_t)j * D;
   float* vj = var + (size_t)j * D;
-  if (mp < 2.0) {  // _MIN_IND_SAMPLES_ (OL_ModelAdapt.h:54)
+  if ((nind ? nind[j] : mp) < 2.0) {  // _MIN_IND_SAMPLES_ (OL_ModelAdapt.h:54); robust: on nind
     for (int k = 0; k < D; ++k) { mj[k] = 0.0f; vj[k] = reset_var_value(); }
     w[j] = 0.0f;
     atomicExch(&flag[5], 1);
@@ -675,12 +675,18 @@ __global__ void ll_record_kernel(const double* __restrict__ tot, double* __restr
 
 int mstep_em(Ctx* c, int upW, int upM, int upV, int* alive) {
   if (!c->stats_valid) return fail(c, GMM_ERR_STATE, "no statistics accumulated");
+  double* nind = nullptr;
+  if (c->robust && c->aux_valid) {  // UpdateModelEM with _robustCov: MakeRobustStats first
+    const int rc = robust_make(c, c->M, c->D, 0, c->stats, c->aux, &nind);
+    if (rc) return rc;
+    c->aux_valid = false;
+  }
   cudaMemsetAsync(c->flag + 5, 0, 2 * sizeof(int), c->stream);
   unsigned int tot = (unsigned int)c->tot_frames;
   {
     GMM_LAUNCH(c, "em_comp_kernel");
     em_comp_kernel<<<(c->M + 127) / 128, 128, 0, c->stream>>>(
-        c->M, c->D, c->w, c->mu, c->var, c->stats, tot, upW, upM, upV, c->min_var, c->flag);
+        c->M, c->D, c->w, c->mu, c->var, c->stats, tot, upW, upM, upV, c->min_var, nind, c->flag);
   }
   {
     GMM_LAUNCH(c, "em_norm_kernel");
@@ -702,6 +708,12 @@ int mstep_em(Ctx* c, int upW, int upM, int upV, int* alive) {
 int mstep_map(Ctx* c, int tau, int upW, int upM, int upV) {
   if (!c->stats_valid) return fail(c, GMM_ERR_STATE, "no statistics accumulated");
   if (!c->have_prior) return fail(c, GMM_ERR_STATE, "MAP needs a prior model (gmm_set_prior)");
+  if (c->robust && c->aux_valid) {  // UpdateModelMAP with _robustCov: MakeRobustStats first
+    double* nind = nullptr;
+    const int rc = robust_make(c, c->M, c->D, 0, c->stats, c->aux, &nind);
+    if (rc) return rc;
+    c->aux_valid = false;
+  }
   unsigned int tot = (unsigned int)c->tot_frames;
   // adapted weights scratch: reuse the logW buffer (recomputed by the next precompute)
   {

@@ -442,6 +442,10 @@ int plain_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
       reduce_kernel<<<(int)((tot + 255) / 256), 256, 0, c->stream>>>(
           c->M, D, c->Mact, c->act, (int)slices, c->part, c->stats);
     }
+    if (c->robust && c->aux) {
+      const int rc = robust_chunk(c, c->M, D, c->Mact, c->act, f0, nf, chunk, c->aux);
+      if (rc) return rc;
+    }
   }
   return GMM_OK;
 }

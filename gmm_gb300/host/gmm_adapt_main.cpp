@@ -47,6 +47,7 @@ std::vector<gmmgb::cli::Opt> options() {
       {"split-X", 0, STR, "0", "(FROM_SCRATCH) fraction of Gaussians split at once per round"},
       {"split-th", 0, STR, "0", "(FROM_SCRATCH) split only weights above split-th * max weight"},
       {"ll-Th", 0, STR, "0", "(FROM_SCRATCH) stop when the log-likelihood gain is below this"},
+      {"robust", 'R', FLAG, "0", "(FROM_SCRATCH|MAP) robust statistics (independent-frame counts)"},
       {"it-EM", 0, STR, "0", "(MAP|FROM_SCRATCH) EM iterations"},
       {"it-MAP", 0, STR, "0", "(MAP) MAP iterations against the UBM"},
       {"mean", 'M', FLAG, "0", "(MAP) adapt means"},
@@ -130,6 +131,7 @@ int main(int argc, char** argv) {
     o.splitXpercAtOnce = P.get_float("split-X");
     o.splitTh = P.get_float("split-th");
     o.llTh = P.get_float("ll-Th");
+    o.robustCov = P.get_bool("robust");
     o.verbosity = P.get_int("verbosity");
     o.precision = P.get("precision") == "fp32" ? GMM_PREC_FP32 : GMM_PREC_TC;
     o.gpu = P.get_int("GPU-id") < 0 ? 0 : P.get_int("GPU-id");

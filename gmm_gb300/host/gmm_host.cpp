@@ -341,6 +341,7 @@ void GMMStatsEstimatorGB300::compVecsLogLikeMT(const float* vecs, unsigned N, un
 ModelAdapt::ModelAdapt(const AdaptOptions& opt) : o_(opt) {
   if (gmm_create(o_.gpu, &h_)) throw std::runtime_error(gmm_last_error(nullptr));
   check(gmm_set_precision(h_, o_.precision));
+  check(gmm_set_robust(h_, o_.robustCov));
 }
 
 ModelAdapt::~ModelAdapt() { gmm_destroy(h_); }

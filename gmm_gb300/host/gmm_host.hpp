@@ -128,6 +128,7 @@ struct AdaptOptions {
   std::string transformFileExt = ".mat";
   float min_var = 1e-6f;
   float splitXpercAtOnce = 0.0f, splitTh = 0.0f, llTh = 0.0f;
+  bool robustCov = false;  // --robust
   int verbosity = 0;
   int precision = GMM_PREC_TC;
   int gpu = 0;

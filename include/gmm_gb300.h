@@ -134,6 +134,19 @@ int gmm_fmllr_estimate(gmm_handle h, int iters, double* W);
 /* Applies W to the features uploaded with gmm_upload_features, in place on the device. */
 int gmm_fmllr_apply(gmm_handle h, const double* W);
 
+/* --robust (CModelAdapt::OPTIONS::_robustCov): E-steps also gather the auxiliary statistics of
+ * consecutive frames (GMMStatsEstimator::accumulateAuxStats, OL_GMMStatsEstimator.cpp:1253-1286;
+ * pairs inside the resident block, the reference's one-thread behaviour), and the EM / MAP
+ * updates first apply GetNIndFrames + MakeRobustStats (OL_ModelAdapt.cpp:468-588) to the device
+ * statistics (the second-order part is modified in place; UpdateModelEM kills components with
+ * fewer than 2 independent frames). Diagonal and full-covariance models. Robust E-steps run on
+ * the plain kernels whatever the precision mode (they need every frame's posteriors). */
+int gmm_set_robust(gmm_handle h, int on);
+/* The auxiliary statistics of the last robust E-step of the diagonal (full = 0) or
+ * full-covariance (full = 1) model: aux [M][D] (sum g |x_t - x_t-1|), aux2 [M] (sum sqrt(post)),
+ * aux3 [M] (sum g); any pointer may be NULL. */
+int gmm_read_aux(gmm_handle h, int full, double* aux, double* aux2, double* aux3);
+
 /* Autotuner of the tensor-core statistics kernel (no counterpart in the reference): on the first
  * E-step of a shape (K, component chunks, frame-tile bucket) it times 1, 2 and 3 waves of CTAs
  * and keeps the fastest for the handle's later E-steps. On by default; off = one wave, the fixed

@@ -444,3 +444,74 @@ def ref_adapt_model(X, w, mu, var, adapt_type, tau=16, it_em=0, it_map=1, it_mll
     if rc:
         raise RuntimeError(ref().ref_last_error().decode())
     return ow, omu, ovar
+
+
+# ------------------------------------------------------------------ --robust
+
+def aux64(X, w, mu, var, full=False, **kw):
+    """FP64 auxiliary statistics of --robust: aux [M, D], aux2 [M], aux3 [M]."""
+    X, w, mu, var = map(_f32, (X, w, mu, var))
+    N, D = X.shape
+    M = len(w)
+    aux, aux2, aux3 = np.zeros((M, D)), np.zeros(M), np.zeros(M)
+    o = _opts(1, **kw)
+    rc = lib().orc64_aux_stats(_p(X), C.c_longlong(N), D, M, _p(w), _p(mu), _p(var), int(full), C.byref(o),
+                               _p(aux), _p(aux2), _p(aux3))
+    if rc:
+        raise RuntimeError(f"orc64_aux_stats failed ({rc})")
+    return dict(aux=aux, aux2=aux2, aux3=aux3)
+
+
+def make_robust(st, aux, full=False):
+    """GetNIndFrames + MakeRobustStats: returns (modified second-order statistics, nind)."""
+    n, F = (np.ascontiguousarray(st[k], np.float64) for k in ("n", "F"))
+    S = np.ascontiguousarray(st["Sp" if full else "S"], np.float64).copy()
+    M, D = F.shape
+    a, a2, a3 = (np.ascontiguousarray(aux[k], np.float64) for k in ("aux", "aux2", "aux3"))
+    nind = np.zeros(M)
+    rc = lib().orc_make_robust(M, D, int(full), _p(n), _p(F), _p(S), _p(a), _p(a2), _p(a3), _p(nind))
+    if rc:
+        raise RuntimeError(f"orc_make_robust failed ({rc})")
+    return S, nind
+
+
+def em_update_robust(w, mu, var, st, S, nind, upW=True, upM=True, upV=True, min_var=1e-6, full=False):
+    """UpdateModelEM with robust statistics S and the kill rule on nind."""
+    w, mu, var = _f32(w).copy(), _f32(mu).copy(), _f32(var).copy()
+    M, D = mu.shape
+    n, F = (np.ascontiguousarray(st[k], np.float64) for k in ("n", "F"))
+    S = np.ascontiguousarray(S, np.float64)
+    nind = np.ascontiguousarray(nind, np.float64)
+    if full:
+        alive = lib().orc_full_em_update_nind(M, D, _p(w), _p(mu), _p(var), _p(n), _p(F), _p(S),
+                                              C.c_longlong(int(st["totN"])), int(upW), int(upM), int(upV), _p(nind))
+    else:
+        alive = lib().orc_em_update_nind(M, D, _p(w), _p(mu), _p(var), _p(n), _p(F), _p(S),
+                                         C.c_longlong(int(st["totN"])), int(upW), int(upM), int(upV),
+                                         C.c_float(min_var), _p(nind))
+    return w, mu, var, alive
+
+
+def ref_aux_accumulate(X, w, mu, var, full=False):
+    X, w, mu, var = map(_f32, (X, w, mu, var))
+    N, D = X.shape
+    M = len(w)
+    aux, aux2, aux3 = np.zeros((M, D)), np.zeros(M), np.zeros(M)
+    order = np.zeros(M, np.int32)
+    rc = ref().ref_aux_accumulate(_p(X), C.c_long(N), D, M, _p(w), _p(mu), _p(var), int(full), _p(aux), _p(aux2),
+                                  _p(aux3), _p(order))
+    if rc:
+        raise RuntimeError(ref().ref_last_error().decode())
+    return dict(aux=aux, aux2=aux2, aux3=aux3, order=order)
+
+
+def ref_robust_adapt(X, w, mu, var, tau, iters, full=False, upW=True, upM=True, upV=True):
+    X = _f32(X)
+    w, mu, var = _f32(w).copy(), _f32(mu).copy(), _f32(var).copy()
+    N, D = X.shape
+    ll = np.zeros(iters)
+    rc = ref().ref_robust_adapt(_p(X), C.c_long(N), D, len(w), _p(w), _p(mu), _p(var), int(full), int(tau),
+                                iters, int(upW), int(upM), int(upV), _p(ll))
+    if rc:
+        raise RuntimeError(ref().ref_last_error().decode())
+    return w, mu, var, ll

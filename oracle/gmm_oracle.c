@@ -26,6 +26,13 @@
 #define MIN_FRAMES_FOR_THREAD 100
 #define MIN_IND_SAMPLES 2.0
 
+int orc_em_update_nind(int M, int D, float* w, float* mu, float* var, const double* n,
+                       const double* F, const double* S, long long totN, int upW, int upM, int upV,
+                       float min_var, const double* nind);
+int orc_full_em_update_nind(int M, int D, float* w, float* mu, float* cov, const double* n,
+                            const double* F, const double* Sp, long long totN, int upW, int upM, int upV,
+                            const double* nind);
+
 int orc_rearrange_order(int M, const float* w, int* order) {
   int nz = 0, z = 1;
   for (int m = 0; m < M; ++m) {
@@ -467,6 +474,14 @@ static float reset_var_value(void) {
 int orc_em_update(int M, int D, float* w, float* mu, float* var, const double* n,
                   const double* F, const double* S, long long totN, int upW, int upM, int upV,
                   float min_var) {
+  return orc_em_update_nind(M, D, w, mu, var, n, F, S, totN, upW, upM, upV, min_var, NULL);
+}
+
+/* UpdateModelEM with the kill rule on `nind` (the robust independent-frame counts of
+ * MakeRobustStats) instead of the occupancies when nind is not NULL. */
+int orc_em_update_nind(int M, int D, float* w, float* mu, float* var, const double* n,
+                       const double* F, const double* S, long long totN, int upW, int upM, int upV,
+                       float min_var, const double* nind) {
   int changed = 0, nzero = 0;
   double corr = 0.0;
   float* mean = (float*)malloc(sizeof(float) * (size_t)D);
@@ -475,7 +490,7 @@ int orc_em_update(int M, int D, float* w, float* mu, float* var, const double* n
   for (int j = 0; j < M; ++j) {
     if (w[j] == 0.0f) { ++nzero; continue; }
     double mp = n[j];
-    if (mp < MIN_IND_SAMPLES) {
+    if ((nind ? nind[j] : mp) < MIN_IND_SAMPLES) {
       for (int k = 0; k < D; ++k) { mu[(size_t)j * D + k] = 0.0f; var[(size_t)j * D + k] = rv; }
       w[j] = 0.0f;
       changed = 1;
@@ -809,6 +824,12 @@ int orc64_full_accumulate(const float* X, long long N, int D, int M, const float
  * no floor; a killed component gets mean 0 and the identity (GMMMixture::Reset). */
 int orc_full_em_update(int M, int D, float* w, float* mu, float* cov, const double* n,
                        const double* F, const double* Sp, long long totN, int upW, int upM, int upV) {
+  return orc_full_em_update_nind(M, D, w, mu, cov, n, F, Sp, totN, upW, upM, upV, NULL);
+}
+
+int orc_full_em_update_nind(int M, int D, float* w, float* mu, float* cov, const double* n,
+                            const double* F, const double* Sp, long long totN, int upW, int upM, int upV,
+                            const double* nind) {
   int changed = 0, nzero = 0;
   double corr = 0.0;
   const size_t P = (size_t)D * (D + 1) / 2;
@@ -817,7 +838,7 @@ int orc_full_em_update(int M, int D, float* w, float* mu, float* cov, const doub
     if (w[j] == 0.0f) { ++nzero; continue; }
     const double mp = n[j];
     float* C = cov + (size_t)j * D * D;
-    if (mp < 2.0) {
+    if ((nind ? nind[j] : mp) < 2.0) {
       for (int k = 0; k < D; ++k) mu[(size_t)j * D + k] = 0.0f;
       for (int e = 0; e < D * D; ++e) C[e] = 0.0f;
       for (int k = 0; k < D; ++k) C[(size_t)k * D + k] = 1.0f;
@@ -1066,5 +1087,138 @@ int orc_fmllr_w(int M, int D, const float* mu, const float* var, const double* n
       W[(size_t)i * E + D] = b[i];
     }
   free(G); free(Gi); free(K); free(A); free(b); free(cofm); free(tmp); free(c); free(foo); free(wv); free(w2);
+  return rc;
+}
+
+/* ---------------------------------------------------------------- robust statistics ---- */
+
+/* Auxiliary statistics of --robust (GMMStatsEstimator::accumulateAuxStats, no-pruning branch,
+ * OL_GMMStatsEstimator.cpp:1253-1286, driven per consecutive frame pair by accumulateStats
+ * :1175-1188, one thread): for frames i >= 1, with the posteriors of frames i and i-1,
+ * gs = 1 / sum_m [g_m > minGamma] g_m over g_m = post_i,m post_i-1,m; aux2_m += sqrt(post_i,m)
+ * when post_i,m > minGamma; for g = gs post_i,m post_i-1,m > minGamma: aux_m[k] += g |x_i,k -
+ * x_i-1,k| and aux3_m += g. Posteriors in FP64 here (the diagonal or the full model). */
+int orc64_aux_stats(const float* X, long long N, int D, int M, const float* w, const float* mu,
+                    const float* var, int full, const orc_opts* o, double* aux, double* aux2, double* aux3) {
+  model64 m;
+  double *chol = NULL, *logc = NULL;
+  int rc = 0;
+  if (full) rc = full_model64(M, D, w, var, &chol, &logc);
+  else rc = prep64(&m, M, D, w, mu, var, o);
+  if (rc) { if (full) { free(chol); free(logc); } else free(m.logc); return rc; }
+  const int nactive = count_active(M, w);
+  double* g = (double*)malloc(sizeof(double) * (size_t)M);
+  double* y = (double*)malloc(sizeof(double) * (size_t)D);
+  double* p0 = (double*)calloc((size_t)M, sizeof(double));
+  double* p1 = (double*)calloc((size_t)M, sizeof(double));
+  for (long long i = 0; i < N; ++i) {
+    const float* x = X + (size_t)i * D;
+    const double ll = full ? full_frame64(M, D, w, mu, chol, logc, x, g, y) : frame64(&m, x, g);
+    for (int c = 0; c < M; ++c) {
+      if (!(w[c] > 0)) { p1[c] = 0.0; continue; }
+      if (nactive == 1) p1[c] = 1.0;
+      else if (ll == -INFINITY) p1[c] = (double)o->minGamma;
+      else p1[c] = exp(g[c] - ll);
+    }
+    if (i > 0) {
+      double gs = 0.0;
+      for (int c = 0; c < M; ++c) {
+        if (!(w[c] > 0)) continue;
+        const double gg = p1[c] * p0[c];
+        if (gg > o->minGamma) gs += gg;
+      }
+      if (gs > 0) gs = 1.0 / gs;
+      const float* xp = x - D;
+      for (int c = 0; c < M; ++c) {
+        if (!(w[c] > 0)) continue;
+        const double gg = gs * p1[c] * p0[c];
+        if (p1[c] > o->minGamma) aux2[c] += sqrt(p1[c]);
+        if (gg <= o->minGamma) continue;
+        for (int k = 0; k < D; ++k) aux[(size_t)c * D + k] += gg * fabs((double)x[k] - (double)xp[k]);
+        aux3[c] += gg;
+      }
+    }
+    double* t = p0; p0 = p1; p1 = t;
+  }
+  free(g); free(y); free(p0); free(p1);
+  if (full) { free(chol); free(logc); } else free(m.logc);
+  return 0;
+}
+
+static float diag_cov_multiplier(double nind) {
+  if (nind < 2) return (float)pow(pow((1.0 + (1.0 / (2.0 - 1.25))), 3.5), (3 - nind));
+  return (float)pow((1.0 + (1.0 / (nind - 1.25))), 3.5);
+}
+
+static float offdiag_cov_multiplier(double nind, int D) {
+  if (nind < 2) return 0.0f;
+  return (float)(1 - pow(((double)D / (D - 1 + nind)), 1.4));
+}
+
+/* GetNIndFrames + MakeRobustStats (OL_ModelAdapt.cpp:468-588): the per-component count of
+ * independent frames from the auxiliary statistics, and the second-order statistics pulled
+ * toward the squared means with the diagonal / off-diagonal multipliers. S is [M][D] (diagonal)
+ * or [M][D(D+1)/2] (full, packed) and is modified in place; nind receives the counts.
+ * Returns 6 if a global variance is zero (the reference throws). */
+int orc_make_robust(int M, int D, int full, const double* n, const double* F, double* S,
+                    const double* aux, const double* aux2, const double* aux3, double* nind) {
+  const size_t P = full ? (size_t)D * (D + 1) / 2 : (size_t)D;
+  double* gstd = (double*)calloc((size_t)D, sizeof(double));
+  double* gmean = (double*)calloc((size_t)D, sizeof(double));
+  double gmp = 0.0, sumNg = 0.0;
+  for (int m = 0; m < M; ++m) {
+    gmp += n[m];
+    size_t shift = 0;
+    for (int d = 0; d < D; ++d) {
+      gmean[d] += F[(size_t)m * D + d];
+      if (full) {
+        shift += (size_t)d;
+        gstd[d] += S[(size_t)m * P + (size_t)d * D + d - shift];
+      } else {
+        gstd[d] += S[(size_t)m * P + d];
+      }
+    }
+    nind[m] = 0;
+    sumNg += aux2[m];
+  }
+  int rc = 0;
+  for (int d = 0; d < D; ++d) {
+    gmean[d] /= gmp;
+    gstd[d] = sqrt(gstd[d] / gmp - gmean[d] * gmean[d]);
+    if (gstd[d] == 0) rc = 6;
+  }
+  if (!rc) {
+    for (int m = 0; m < M; ++m) {
+      if (n[m] == 0 || aux3[m] == 0) {
+        nind[m] = 0;
+      } else {
+        for (int d = 0; d < D; ++d) nind[m] += aux[(size_t)m * D + d] / aux3[m] / gstd[d];
+        nind[m] /= D;
+        nind[m] = pow(nind[m] / 1.12, 3);
+        nind[m] = 1 + (aux2[m] * gmp / sumNg - 1) * nind[m];
+      }
+    }
+    for (int j = 0; j < M; ++j) {
+      float dc = diag_cov_multiplier(nind[j]);
+      dc *= nind[j] / (nind[j] - 1);
+      double* Sj = S + (size_t)j * P;
+      const double* Fj = F + (size_t)j * D;
+      if (full) {
+        const float odc = offdiag_cov_multiplier(nind[j], D);
+        size_t shift = 0;
+        for (int k = 0; k < D - 1; ++k) {
+          shift += (size_t)k;
+          Sj[(size_t)k * D + k - shift] = dc * Sj[(size_t)k * D + k - shift] + (1 - dc) * pow(Fj[k], 2.0) / n[j];
+          for (int kk = k + 1; kk < D; ++kk)
+            Sj[(size_t)k * D + kk - shift] = odc * Sj[(size_t)k * D + kk - shift] + (1 - odc) * Fj[k] * Fj[kk] / n[j];
+        }
+        Sj[P - 1] = dc * Sj[P - 1] + (1 - dc) * pow(Fj[D - 1], 2.0) / n[j];
+      } else {
+        for (int k = 0; k < D; ++k) Sj[k] = dc * Sj[k] + (1 - dc) * pow(Fj[k], 2.0) / n[j];
+      }
+    }
+  }
+  free(gstd);
+  free(gmean);
   return rc;
 }

@@ -113,6 +113,20 @@ int orc64_accumulate_fullstats(const float* X, long long N, int D, int M, const 
 int orc_fmllr_w(int M, int D, const float* mu, const float* var, const double* n, const double* F,
                 const double* Sp, long long totN, int iters, double* W);
 
+/* --robust: auxiliary statistics (FP64 posteriors; full = 1 for a full-covariance model, var
+ * then [M][D][D]), GetNIndFrames + MakeRobustStats (S modified in place, nind out; returns 6
+ * for a zero global variance) and the EM updates with the kill rule on nind. */
+int orc64_aux_stats(const float* X, long long N, int D, int M, const float* w, const float* mu,
+                    const float* var, int full, const orc_opts* o, double* aux, double* aux2, double* aux3);
+int orc_make_robust(int M, int D, int full, const double* n, const double* F, double* S,
+                    const double* aux, const double* aux2, const double* aux3, double* nind);
+int orc_em_update_nind(int M, int D, float* w, float* mu, float* var, const double* n,
+                       const double* F, const double* S, long long totN, int upW, int upM, int upV,
+                       float min_var, const double* nind);
+int orc_full_em_update_nind(int M, int D, float* w, float* mu, float* cov, const double* n,
+                            const double* F, const double* Sp, long long totN, int upW, int upM, int upV,
+                            const double* nind);
+
 #ifdef __cplusplus
 }
 #endif

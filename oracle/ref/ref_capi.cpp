@@ -502,3 +502,75 @@ int ref_adapt_model(const float* X, long N, int D, int M, const float* w, const 
 }
 
 }  // extern "C"
+
+extern "C" {
+
+// E-step with the --robust auxiliary statistics (accumulateAuxStats) of a diagonal (full = 0,
+// var [M][D]) or full-covariance (full = 1, var [M][D][D]) model, one thread; order as
+// ref_accumulate.
+int ref_aux_accumulate(const float* X, long N, int D, int M, const float* w, const float* mu,
+                       const float* var, int full, double* aux, double* aux2, double* aux3, int* order) {
+  try {
+    GMModel* g = full ? make_model_full(M, D, w, mu, var) : make_model(M, D, w, mu, var);
+    std::vector<float*> before((size_t)M);
+    for (int m = 0; m < M; ++m) before[(size_t)m] = g->GetMixtureMean(m);
+    GMMStatsEstimator<double>* e = make_estimator(0, 1);
+    e->insertModel(*g);
+    for (int k = 0; k < M; ++k) {
+      order[k] = -1;
+      for (int m = 0; m < M; ++m)
+        if (g->GetMixtureMean(k) == before[(size_t)m]) order[k] = m;
+    }
+    GMMStats<double> st(D, M, true, true, full != 0, true);
+    st.reset();
+    e->setAccFlags(false, true, true, full != 0, true);
+    std::vector<float*> r = rows(X, N, D);
+    e->accumulateStatsMT(r.data(), (unsigned)N, (unsigned)D, st);
+    for (int m = 0; m < M; ++m) {
+      for (int d = 0; d < D; ++d) aux[(size_t)m * D + d] = st[m].aux[d];
+      aux2[m] = st[m].aux2;
+      aux3[m] = st[m].aux3;
+    }
+    delete e;
+    delete g;
+    return 0;
+  } catch (std::exception& ex) { g_err = ex.what(); return 1; }
+}
+
+// EM (tau = 0) or MAP iterations with --robust on a diagonal or full-covariance model, one
+// thread; the model arrays receive the result (rearranged order).
+int ref_robust_adapt(const float* X, long N, int D, int M, float* w, float* mu, float* var, int full, int tau,
+                     int iters, int upW, int upM, int upV, double* ll) {
+  try {
+    GMModel* ubm = full ? make_model_full(M, D, w, mu, var) : make_model(M, D, w, mu, var);
+    CModelAdapt cm;
+    CModelAdapt::OPTIONS opt = base_options(1, 0);
+    opt._adaptType = MAP;
+    opt._tau = tau;
+    opt._iterCountEM = tau == 0 ? iters : 0;
+    opt._iterCountMAP = tau == 0 ? 0 : iters;
+    opt._AdaptWeightBool = upW != 0;
+    opt._AdaptMeanBool = upM != 0;
+    opt._AdaptVarBool = upV != 0;
+    opt._robustCov = true;
+    cm.SetOptions(opt);
+    Param p;
+    fill_param(p, X, N, D);
+    cm.InsertData(p, false);
+    cm.Initialize(ubm);
+    GMModel* model = new GMModel(ubm);
+    for (int it = 0; it < iters; ++it) {
+      if (tau == 0) cm.IterEM(model, 1);
+      else cm.IterMAP(model, 1);
+      ll[it] = cm._stats.getTotLogLike();
+    }
+    if (full) read_model_full(model, M, D, w, mu, var);
+    else read_model(model, M, D, w, mu, var);
+    delete model;
+    delete ubm;
+    return 0;
+  } catch (std::exception& ex) { g_err = ex.what(); return 1; }
+  catch (Exception* ex) { g_err = ex->m_strDescription; delete ex; return 2; }
+}
+
+}  // extern "C"

@@ -26,6 +26,9 @@ from their own sources, see oracle/Makefile) and records its outputs on small in
   restatement in oracle/ref/shim/acml.h.
 * ``mllr_map.npz`` -- MLLR+MAP (adaptation type 4): one global MLLR transform, then one MAP
   iteration (tau = 16, means and variances) of the transformed UBM against the original UBM.
+* ``robust.npz``   -- --robust: the auxiliary statistics (one thread) of a diagonal and a
+  full-covariance model, two robust EM iterations of each, and one robust MAP iteration
+  (tau = 16, means and variances) of a diagonal UBM.
 * ``fmllr.npz``    -- fMLLR (ComputeW_fMLLR, 20 passes) of a diagonal UBM (M = 32, D = 12) from
   one speaker of seeded affinely transformed UBM samples: the transform and the E-step
   statistics (packed full second order) it was computed from.
@@ -121,6 +124,7 @@ def main():
     full_fixture(a.ref_root)
     fmllr_fixture()
     mllr_map_fixture()
+    robust_fixture()
 
 
 def full_fixture(ref_root):
@@ -140,6 +144,24 @@ def full_fixture(ref_root):
     mw, mmu, mcov, mll = O.ref_full_adapt(Xs, w, mu, cov, 16, 1, threads=2)
     out.update(map_w=mw, map_mu=mmu, map_cov=mcov, map_ll=mll)
     np.savez_compressed(os.path.join(HERE, "full.npz"), **out)
+
+
+def robust_fixture():
+    e = dict(np.load(os.path.join(HERE, "em_small.npz")))
+    f = dict(np.load(os.path.join(HERE, "full.npz")))
+    mm = dict(np.load(os.path.join(HERE, "map_mllr.npz")))
+    out = {}
+    a = O.ref_aux_accumulate(e["X"], e["w"], e["mu"], e["var"])
+    out.update(diag_aux=a["aux"], diag_aux2=a["aux2"], diag_aux3=a["aux3"])
+    a = O.ref_aux_accumulate(f["X"], f["w"], f["mu"], f["cov"], full=True)
+    out.update(full_aux=a["aux"], full_aux2=a["aux2"], full_aux3=a["aux3"])
+    w, mu, var, ll = O.ref_robust_adapt(e["X"], e["w"], e["mu"], e["var"], 0, 2)
+    out.update(diag_em_w=w, diag_em_mu=mu, diag_em_var=var, diag_em_ll=ll)
+    w, mu, cov, ll = O.ref_robust_adapt(f["X"], f["w"], f["mu"], f["cov"], 0, 2, full=True)
+    out.update(full_em_w=w, full_em_mu=mu, full_em_cov=cov, full_em_ll=ll)
+    w, mu, var, ll = O.ref_robust_adapt(mm["X"], mm["w"], mm["mu"], mm["var"], 16, 1, upW=False)
+    out.update(map_w=w, map_mu=mu, map_var=var)
+    np.savez_compressed(os.path.join(HERE, "robust.npz"), **out)
 
 
 def mllr_map_fixture():
@@ -176,6 +198,9 @@ if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "--full-only":
         O.build(ref=True)
         full_fixture("/root/reference/GMM")
+    elif len(sys.argv) > 1 and sys.argv[1] == "--robust-only":
+        O.build(ref=True)
+        robust_fixture()
     elif len(sys.argv) > 1 and sys.argv[1] == "--mllr-map-only":
         O.build(ref=True)
         mllr_map_fixture()

@@ -188,3 +188,30 @@ def test_mllr_map_oracle_against_reference(oracle, golden):
     _, omu, ovar = oracle.map_update(w, mu, var, st2, 16, w=w.copy(), mu=mu2.copy(), var=var.copy(),
                                      upM=True, upV=True)
     assert np.array_equal(omu, want["mu"]) and np.array_equal(ovar, want["var"])
+
+
+def test_robust_oracle_against_reference(oracle, golden):
+    """--robust: FP64 auxiliary statistics within 1e-6 of the reference's scale, and two robust
+    EM iterations (FP64 E-step, the reference's MakeRobustStats / UpdateModelEM expressions)
+    within 1e-4 rel / 1e-4 abs of the reference's models (diagonal and full covariances)."""
+    r = golden("robust.npz")
+    e = golden("em_small.npz")
+    f = golden("full.npz")
+    for key, X, w, mu, var, full in (("diag", e["X"], e["w"], e["mu"], e["var"], False),
+                                      ("full", f["X"], f["w"], f["mu"], f["cov"], True)):
+        a = oracle.aux64(X, w, mu, var, full=full)
+        for k in ("aux", "aux2", "aux3"):
+            ref = r[f"{key}_{k}"]
+            assert np.abs(a[k] - ref).max() <= 1e-6 * np.abs(ref).max(), (key, k)
+        ww, mm, vv = w.copy(), mu.copy(), var.copy()
+        for _ in range(2):
+            order, _ = oracle.rearrange_order(ww)  # insertModel moves killed components to the end
+            ww, mm, vv = ww[order], mm[order], vv[order]
+            st = oracle.full64_accumulate(X, ww, mm, vv) if full else oracle.accumulate64(X, ww, mm, vv)
+            ax = oracle.aux64(X, ww, mm, vv, full=full)
+            S, nind = oracle.make_robust(st, ax, full=full)
+            ww, mm, vv, _ = oracle.em_update_robust(ww, mm, vv, st, S, nind, full=full)
+        vkey = "cov" if full else "var"
+        assert np.allclose(ww, r[f"{key}_em_w"], rtol=1e-4, atol=1e-6), key
+        assert np.allclose(mm, r[f"{key}_em_mu"], rtol=1e-4, atol=1e-4), key
+        assert np.allclose(vv, r[f"{key}_em_{vkey}"], rtol=1e-4, atol=1e-4), key
