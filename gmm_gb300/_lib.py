@@ -31,6 +31,8 @@ SIGNATURES = {
     "gmm_upload_model_full": (_i, [_vp, _i, _i, _vp, _vp, _vp]),
     "gmm_fmllr_estimate": (_i, [_vp, _i, _vp]),
     "gmm_set_robust": (_i, [_vp, _i]),
+    "gmm_mllr_estimate_full": (_i, [_vp, _i, _vp]),
+    "gmm_mllr_apply_full": (_i, [_vp, _vp]),
     "gmm_read_aux": (_i, [_vp, _i, _vp, _vp, _vp]),
     "gmm_fmllr_apply": (_i, [_vp, _vp]),
     "gmm_set_prior_full": (_i, [_vp, _vp, _vp, _vp]),
@@ -332,6 +334,15 @@ class Handle:
         self.check(self.lib.gmm_em_update_full(self.h, int(upW), int(upM), int(upV), C.byref(a)))
         self.last_alive = a.value
         return a.value
+
+    def mllr_estimate_full(self, ubm_init=False):
+        W = np.zeros((self.Df, self.Df + 1))
+        self.check(self.lib.gmm_mllr_estimate_full(self.h, int(ubm_init), ptr(W)))
+        return W
+
+    def mllr_apply_full(self, W):
+        W = np.ascontiguousarray(W, np.float64)
+        self.check(self.lib.gmm_mllr_apply_full(self.h, ptr(W)))
 
     def map_update_full(self, tau, upW=False, upM=True, upV=False):
         self.check(self.lib.gmm_map_update_full(self.h, int(tau), int(upW), int(upM), int(upV)))

@@ -44,10 +44,25 @@ class Options:
 _RESET_VAR = np.frombuffer(np.array([0x01010101], np.uint32).tobytes(), np.float32)[0]
 
 
-def _empty_model(M: int, D: int) -> GMModel:
-    """``GMModel(dim, nummix)``: zero weights, components in GMMMixture::Reset state (mean 0,
-    variance bytes 0x01 from memset; OL_GMModel.cpp:45-83, 120-165)."""
-    return GMModel(np.zeros(M, np.float32), np.zeros((M, D), np.float32), np.full((M, D), _RESET_VAR, np.float32))
+def _empty_model(M: int, D: int, full: bool = False) -> GMModel:
+    """``GMModel(dim, nummix, full)``: zero weights, components in GMMMixture::Reset state (mean
+    0; diagonal variances of bytes 0x01 from memset, full covariances the identity;
+    OL_GMModel.cpp:45-83, 120-165)."""
+    var = (np.tile(np.eye(D, dtype=np.float32), (M, 1, 1)) if full
+           else np.full((M, D), _RESET_VAR, np.float32))
+    return GMModel(np.zeros(M, np.float32), np.zeros((M, D), np.float32), var)
+
+
+def leading_eigenpair(cov: np.ndarray):
+    """Largest eigenvalue (float32) and its unit eigenvector (float32) of a symmetric matrix, in
+    FP64; the sign makes the largest-magnitude component positive (the eigenvector's sign is not
+    fixed by the problem; getEigValVecs, OL_ModelAdapt.cpp:73-160, takes LAPACK's)."""
+    lam, vec = np.linalg.eigh(np.asarray(cov, np.float64))
+    v = vec[:, -1]
+    big = int(np.argmax(np.abs(v)))
+    if v[big] < 0:
+        v = -v
+    return np.float32(lam[-1]), v.astype(np.float32)
 
 
 def _gauss_stats(model: GMModel, get_list: bool):
@@ -72,13 +87,20 @@ def _gauss_stats(model: GMModel, get_list: bool):
 
 
 def _split_gaussian(model: GMModel, m2: int, mnew: int) -> None:
-    """``CModelAdapt::splitGaussian`` (OL_ModelAdapt.cpp:612-665), diagonal covariances: the new
-    component takes the variance, both take half the weight, means move by +-sqrt(var)/2."""
+    """``CModelAdapt::splitGaussian`` (OL_ModelAdapt.cpp:612-665): the new component takes the
+    covariance, both take half the weight; the means move by +-sqrt(var)/2 (diagonal) or by
+    +-sqrt(lambda) v along the leading eigenvector of the covariance (full)."""
     model.var[mnew] = model.var[m2]
     w = np.float32(model.w[m2] / np.float32(2.0))
     model.w[mnew] = w
     model.w[m2] = w
-    shift = (np.sqrt(model.var[m2].astype(np.float64)) * 0.5).astype(np.float32)
+    if model.full:
+        lam, v = leading_eigenpair(model.var[m2])
+        if lam < 0:
+            raise RuntimeError("splitGaussian(): covariance matrix not positive definite!")
+        shift = (np.sqrt(lam) * v).astype(np.float32)
+    else:
+        shift = (np.sqrt(model.var[m2].astype(np.float64)) * 0.5).astype(np.float32)
     model.mu[mnew] = model.mu[m2] + shift
     model.mu[m2] = model.mu[m2] - shift
 
@@ -203,9 +225,14 @@ class ModelAdapt:
         return model
 
     def ComputeW_MLLR(self, model: GMModel, ubm: GMModel) -> np.ndarray:
-        """``CModelAdapt::ComputeW_MLLR`` (OL_ModelAdapt.cpp:1417-1482)."""
+        """``CModelAdapt::ComputeW_MLLR`` (OL_ModelAdapt.cpp:1417-1482); a full-covariance model
+        uses its covariance diagonals (GetMixtureVarDiag)."""
         self._ensure_features()
         self._upload(model)
+        if model.full:
+            self.dev.set_prior_full(ubm.w, ubm.mu, ubm.var)
+            self.dev.accumulate_full_device(_lib.ACC_MEAN)
+            return self.dev.mllr_estimate_full(self.opt.mllrUBMInit)
         self.dev.set_prior(ubm.w, ubm.mu, ubm.var)
         self.dev.accumulate_device(_lib.ACC_MEAN)
         return self.dev.mllr_estimate(self.opt.mllrUBMInit)
@@ -227,12 +254,16 @@ class ModelAdapt:
         """One AccumulateStats + UpdateModelEM of TrainFromScratch: insertModel rearranges the
         model in place, then the device accumulates and (if asked) updates it."""
         self._upload(model)
-        self.dev.accumulate_device(_lib.ACC_MEAN | _lib.ACC_VAR)
-        st = self.dev.read_stats()
+        if model.full:
+            self.dev.accumulate_full_device(_lib.ACC_MEAN | _lib.ACC_VAR)
+            st = self.dev.read_stats_full()
+        else:
+            self.dev.accumulate_device(_lib.ACC_MEAN | _lib.ACC_VAR)
+            st = self.dev.read_stats()
         alive = None
         if update:
-            alive = self.dev.em_update(True, True, True)
-            model.w, model.mu, model.var = self.dev.read_model()
+            alive = self.dev.em_update_full(True, True, True) if model.full else self.dev.em_update(True, True, True)
+            self._read(model)
         return st, alive
 
     def splitMultipleGaussians(self, model: GMModel) -> None:
@@ -249,18 +280,23 @@ class ModelAdapt:
                 break
             _split_gaussian(model, m, z)
 
-    def TrainFromScratch(self, nummix: int, init: GMModel | None = None) -> GMModel:
-        """``CModelAdapt::TrainFromScratch`` (OL_ModelAdapt.cpp:667-821), diagonal covariances:
-        a global Gaussian, then EM iterations on the device alternating with splits of the
-        heaviest Gaussians into free slots until nummix components (or a stop rule)."""
+    def TrainFromScratch(self, nummix: int, init: GMModel | None = None, fullcov: bool = False) -> GMModel:
+        """``CModelAdapt::TrainFromScratch`` (OL_ModelAdapt.cpp:667-821): a global Gaussian, then
+        EM iterations on the device alternating with splits of the heaviest Gaussians into free
+        slots until nummix components (or a stop rule). fullcov: full covariance matrices (an
+        init model, if given, decides: a diagonal one switches the training to diagonal, as the
+        reference warns)."""
         o = self.opt
         self._ensure_features()
         if self._X.shape[0] <= 3:
             raise RuntimeError("TrainFromScratch(): Not enough data to model training.")
         D = self._X.shape[1]
+        if init is not None:
+            fullcov = init.full
         if init is None:
             # global statistics: one component, every posterior 1
-            g = GMModel(np.ones(1, np.float32), np.zeros((1, D), np.float32), np.ones((1, D), np.float32))
+            g = GMModel(np.ones(1, np.float32), np.zeros((1, D), np.float32),
+                        np.eye(D, dtype=np.float32)[None] if fullcov else np.ones((1, D), np.float32))
             _, alive = self._em_step(g, True)
             if alive == 0:
                 raise RuntimeError("trainFromScratch(): amount of data too low to estimate a model, or data are "
@@ -271,7 +307,7 @@ class ModelAdapt:
             if nummix <= init.M:
                 raise RuntimeError("trainFromScratch(): init model already contains specified number of Gaussians!")
             max_iter = nummix - init.M
-        model = _empty_model(nummix, D)
+        model = _empty_model(nummix, D, fullcov)
         model.w[:init.M], model.mu[:init.M], model.var[:init.M] = init.w, init.mu, init.var
         if nummix < 2:
             max_iter = 0
@@ -286,9 +322,9 @@ class ModelAdapt:
                 if o.verbosity:  # the reference only computes the average LL when verbose
                     ll[0] = np.float32(st["totLL"] / st["totN"])
                 if non_zero > 1:
-                    self.dev.em_update(True, True, True)
-                    model.w, model.mu, model.var = self.dev.read_model()
-                    non_zero = self.dev.last_alive
+                    non_zero = (self.dev.em_update_full(True, True, True) if model.full
+                                else self.dev.em_update(True, True, True))
+                    self._read(model)
                 if non_zero < 2:
                     if non_zero < 1:
                         model = init.copy()
@@ -301,7 +337,7 @@ class ModelAdapt:
                     if mx > ll[0]:
                         model = (m2 if mx == ll[1] else m3).copy()
                     break
-                m3 = m2.copy() if m2 is not None else _empty_model(0, D)
+                m3 = m2.copy() if m2 is not None else _empty_model(0, D, fullcov)
                 m2 = model.copy()
                 ll[2], ll[1] = ll[1], ll[0]
             if it < max_iter - 1:
@@ -315,6 +351,11 @@ class ModelAdapt:
         """``CModelAdapt::AdaptModelMLLR`` (OL_ModelAdapt.cpp:1583-1612)."""
         out = model.copy()
         self.dev.set_options(-1e20, 1e-4, self.opt.min_var)
+        if out.full:
+            self.dev.upload_model_full(out.w, out.mu, out.var)
+            self.dev.mllr_apply_full(W)
+            out.w, out.mu, out.var = self.dev.read_model_full()
+            return out
         self.dev.upload_model(out.w, out.mu, out.var)
         self.dev.mllr_apply(W)
         out.w, out.mu, out.var = self.dev.read_model()
@@ -337,16 +378,12 @@ class ModelAdapt:
             self._upload(ubm.copy())
             self._W = self.dev.fmllr_estimate(o.iterfMLLR)
         elif o.adaptType == MLLR:
-            if ubm.full:
-                raise NotImplementedError("MLLR of full-covariance models is not built")
             self._W = self.IterW_MLLR(ubm, o.iterMLLR)
             if o.applyTransforms:
                 self._model = self.AdaptModelMLLR(ubm, self._W)
         elif o.adaptType == MLLR_MAP:
             # MLLR of the UBM, then AdaptModelMAP of the transformed model with the original
             # UBM as the MAP prior (OL_ModelAdapt.cpp:1190-1205)
-            if ubm.full:
-                raise NotImplementedError("MLLR of full-covariance models is not built")
             try:
                 W = self.IterW_MLLR(ubm, o.iterMLLR)
                 model = self.AdaptModelMLLR(ubm, W)

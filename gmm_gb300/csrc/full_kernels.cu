@@ -570,6 +570,14 @@ __global__ void full_map_norm_kernel(int M, float* __restrict__ w, const float* 
   }
 }
 
+// Diagonal of each covariance (GMModel::GetMixtureVarDiag): out [M][D].
+__global__ void full_diag_kernel(int M, int D, const float* __restrict__ cov, float* __restrict__ out) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)M * D) return;
+  const int m = (int)(t / D), d = (int)(t - (long long)m * D);
+  out[t] = cov[((size_t)m * D + d) * D + d];
+}
+
 // ------------------------------------------------------------------ host side
 
 void free_full(Ctx* c) {
@@ -1018,6 +1026,74 @@ int gmm_em_update_full(gmm_handle h, int upW, int upM, int upV, int* alive) {
   if (rc) return rc;
   if (alive) *alive = c->hflag[2];
   return GMM_OK;
+}
+
+// MLLR of a full-covariance model: the reference's ComputeKiGi_MLLR / prepareKiGiInitMatrices
+// read GetMixtureVarDiag, so the diagonal model's MLLR routines run on the full model's
+// occupancies, first-order statistics, means and covariance diagonals (the statistics layout
+// [n | F | ...] is the same).
+namespace {
+struct DiagView {  // the diagonal-model fields of the context, saved while they point at the full model
+  int M, D;
+  float *mu, *var, *pmu, *pvar;
+  bool have_prior, stats_valid, model_dirty;
+  double* stats;
+  int acc_flags;
+  long long tot_frames;
+};
+DiagView save_view(Ctx* c) {
+  return {c->M, c->D, c->mu, c->var, c->pmu, c->pvar, c->have_prior, c->stats_valid, c->model_dirty,
+          c->stats, c->acc_flags, c->tot_frames};
+}
+void restore_view(Ctx* c, const DiagView& v) {
+  c->M = v.M; c->D = v.D; c->mu = v.mu; c->var = v.var; c->pmu = v.pmu; c->pvar = v.pvar;
+  c->have_prior = v.have_prior; c->stats_valid = v.stats_valid; c->model_dirty = v.model_dirty;
+  c->stats = v.stats; c->acc_flags = v.acc_flags; c->tot_frames = v.tot_frames;
+}
+}  // namespace
+
+int gmm_mllr_estimate_full(gmm_handle h, int ubm_init, double* W) {
+  if (!h || !W) return GMM_ERR_ARG;
+  Ctx* c = h;
+  FullModel* f = c->full;
+  if (!f || !f->stats_valid) return fail(c, GMM_ERR_STATE, "no statistics accumulated");
+  cudaSetDevice(c->device);
+  const size_t md = sizeof(float) * (size_t)f->M * f->D;
+  float* dv = nullptr;
+  float* dpv = nullptr;
+  int rc = dalloc(c, (void**)&dv, md, "covariance diagonals");
+  if (!rc && f->have_prior) rc = dalloc(c, (void**)&dpv, md, "prior covariance diagonals");
+  if (rc) {
+    dfree(c, dv, md);
+    return rc;
+  }
+  const long long tot = (long long)f->M * f->D;
+  full_diag_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(f->M, f->D, f->cov, dv);
+  if (dpv) full_diag_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(f->M, f->D, f->pcov, dpv);
+  const DiagView saved = save_view(c);
+  c->M = f->M; c->D = f->D; c->mu = f->mu; c->var = dv; c->pmu = f->pmu; c->pvar = dpv;
+  c->have_prior = f->have_prior; c->stats = f->stats; c->stats_valid = true; c->acc_flags = f->acc_flags;
+  c->tot_frames = f->tot_frames;
+  rc = mstep_mllr(c, ubm_init, W);
+  restore_view(c, saved);
+  cudaStreamSynchronize(c->stream);
+  dfree(c, dv, md);
+  dfree(c, dpv, md);
+  return rc;
+}
+
+int gmm_mllr_apply_full(gmm_handle h, const double* W) {
+  if (!h || !W) return GMM_ERR_ARG;
+  Ctx* c = h;
+  FullModel* f = c->full;
+  if (!f || !f->w) return fail(c, GMM_ERR_STATE, "no full-covariance model uploaded");
+  cudaSetDevice(c->device);
+  const DiagView saved = save_view(c);
+  c->M = f->M; c->D = f->D; c->mu = f->mu;
+  const int rc = mstep_mllr_apply(c, W);
+  restore_view(c, saved);
+  f->dirty = true;
+  return rc;
 }
 
 int gmm_map_update_full(gmm_handle h, int tau, int upW, int upM, int upV) {

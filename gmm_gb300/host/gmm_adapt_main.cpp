@@ -32,7 +32,7 @@ std::vector<gmmgb::cli::Opt> options() {
       {"in-UBM", 'u', STR, "", "UBM / initial model (none: train from scratch)"},
       {"in-dir-UBM", 'U', STR, "", "directory with one initial model per output model"},
       {"nummix", 'g', STR, "0", "number of Gaussians when training from scratch"},
-      {"full-cov", 0, FLAG, "0", "(FROM_SCRATCH) full covariances: refused (the eigenvector split is not built)"},
+      {"full-cov", 0, FLAG, "0", "(FROM_SCRATCH) train full covariance matrices"},
       {"inExt-gmm", 'E', STR, ".gmm", "extension of models in --in-dir-UBM"},
       {"outFile", 'o', STR, "", "output model"},
       {"file-by-file", 'f', FLAG, "0", "stream the feature files each iteration instead of keeping them resident"},
@@ -104,9 +104,6 @@ int main(int argc, char** argv) {
     const bool no_model = !P.count("in-UBM") && !P.count("in-dir-UBM");
     const int nummix = P.get_int("nummix");
     const bool from_scratch = nummix > 0;  // Model_ADAPT.cpp:392: --nummix selects training
-    if (from_scratch && P.get_bool("full-cov"))
-      throw std::runtime_error("training full-covariance models from scratch is not built (use a diagonal "
-                               "model, or adapt a full-covariance UBM with --type 2)");
     if (no_model && !from_scratch)
       throw std::runtime_error("LoadConfiguration(): None input model specified (\"in-UBM\" or \"in-dir-UBM\") and \"nummix\" < 1!");
     std::string in_ext = P.get("inExt");
@@ -238,7 +235,7 @@ int main(int argc, char** argv) {
         }
         ma.InsertData(X.data(), N, D);
       }
-      if (from_scratch) ma.TrainFromScratch(nummix, no_model ? nullptr : &ubm);
+      if (from_scratch) ma.TrainFromScratch(nummix, no_model ? nullptr : &ubm, P.get_bool("full-cov"));
       else ma.AdaptModel(ubm);
       ma.Save(j.out, save_txt, P.get_bool("save-in-stat-form"));
       if (o.verbosity)

@@ -482,21 +482,21 @@ void ModelAdapt::IterMAP(GMModel& model, const GMModel& ubm, int iters) {
 }
 
 std::vector<double> ModelAdapt::ComputeW_MLLR(GMModel& model, const GMModel& ubm) {
-  if (model.GetFullCovStatus()) fail("ComputeW_MLLR(): MLLR of full-covariance models is not built");
+  // a full-covariance model uses its covariance diagonals (GetMixtureVarDiag)
   model.RearrangeMixtures();
   upload_model(model);
-  check(gmm_set_prior(h_, ubm.weights().data(), ubm.means().data(), ubm.vars().data()));
+  set_prior(ubm);
   estep(GMM_ACC_MEAN);
   std::vector<double> W((size_t)D_ * (D_ + 1));
-  check(gmm_mllr_estimate(h_, o_.mllrUBMInit, W.data()));
+  check(full_ ? gmm_mllr_estimate_full(h_, o_.mllrUBMInit, W.data()) : gmm_mllr_estimate(h_, o_.mllrUBMInit, W.data()));
   return W;
 }
 
 GMModel ModelAdapt::AdaptModelMLLR(const GMModel& model, const std::vector<double>& W) {
   GMModel out = model;
   upload_model(out);
-  check(gmm_mllr_apply(h_, W.data()));
-  check(gmm_read_model(h_, out.weights().data(), out.means().data(), out.vars().data()));
+  check(full_ ? gmm_mllr_apply_full(h_, W.data()) : gmm_mllr_apply(h_, W.data()));
+  read_model(out);
   return out;
 }
 
@@ -601,19 +601,77 @@ void gauss_stats(const GMModel& m, bool get_list, int* i_max, std::vector<int>* 
   }
 }
 
-// splitGaussian (OL_ModelAdapt.cpp:612-665), diagonal covariances
+// Largest eigenvalue and its unit eigenvector of a symmetric n x n matrix by cyclic Jacobi
+// rotations in double (getEigValVecs, OL_ModelAdapt.cpp:73-160, asks LAPACK for this pair). The
+// eigenvector's sign is not fixed by the problem: its largest-magnitude component is made positive.
+void leading_eigenpair(const float* a, int n, float* lam, float* v) {
+  std::vector<double> A((size_t)n * n), V((size_t)n * n, 0.0);
+  for (size_t e = 0; e < A.size(); ++e) A[e] = a[e];
+  for (int i = 0; i < n; ++i) V[(size_t)i * n + i] = 1.0;
+  for (int sweep = 0; sweep < 100; ++sweep) {
+    double off = 0.0;
+    for (int p = 0; p < n; ++p)
+      for (int q = p + 1; q < n; ++q) off += A[(size_t)p * n + q] * A[(size_t)p * n + q];
+    if (off < 1e-30) break;
+    for (int p = 0; p < n; ++p)
+      for (int q = p + 1; q < n; ++q) {
+        const double apq = A[(size_t)p * n + q];
+        if (apq == 0.0) continue;
+        const double theta = (A[(size_t)q * n + q] - A[(size_t)p * n + p]) / (2.0 * apq);
+        const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+        const double c = 1.0 / std::sqrt(t * t + 1.0), sn = t * c;
+        for (int k = 0; k < n; ++k) {
+          const double akp = A[(size_t)k * n + p], akq = A[(size_t)k * n + q];
+          A[(size_t)k * n + p] = c * akp - sn * akq;
+          A[(size_t)k * n + q] = sn * akp + c * akq;
+        }
+        for (int k = 0; k < n; ++k) {
+          const double apk = A[(size_t)p * n + k], aqk = A[(size_t)q * n + k];
+          A[(size_t)p * n + k] = c * apk - sn * aqk;
+          A[(size_t)q * n + k] = sn * apk + c * aqk;
+        }
+        for (int k = 0; k < n; ++k) {
+          const double vkp = V[(size_t)k * n + p], vkq = V[(size_t)k * n + q];
+          V[(size_t)k * n + p] = c * vkp - sn * vkq;
+          V[(size_t)k * n + q] = sn * vkp + c * vkq;
+        }
+      }
+  }
+  int best = 0;
+  for (int i = 1; i < n; ++i)
+    if (A[(size_t)i * n + i] > A[(size_t)best * n + best]) best = i;
+  int big = 0;
+  for (int i = 1; i < n; ++i)
+    if (std::fabs(V[(size_t)i * n + best]) > std::fabs(V[(size_t)big * n + best])) big = i;
+  const double sg = V[(size_t)big * n + best] < 0 ? -1.0 : 1.0;
+  for (int i = 0; i < n; ++i) v[i] = (float)(sg * V[(size_t)i * n + best]);
+  *lam = (float)A[(size_t)best * n + best];
+}
+
+// splitGaussian (OL_ModelAdapt.cpp:612-665): the new component takes the covariance, both take
+// half the weight; the means move by +-sqrt(var)/2 (diagonal) or by +-sqrt(lambda) v along the
+// leading eigenvector (full).
 void split_gaussian(GMModel& model, int m2, int mnew) {
   const int D = model.GetDimension();
-  std::memcpy(model.GetMixtureVar(mnew), model.GetMixtureVar(m2), sizeof(float) * D);
+  std::memcpy(model.GetMixtureVar(mnew), model.GetMixtureVar(m2), sizeof(float) * model.DimVar());
   const float w = model.GetMixtureWeight(m2) / 2.0f;
   model.SetMixWeight(mnew, w);
   model.SetMixWeight(m2, w);
   float* m = model.GetMixtureMean(m2);
   float* mn = model.GetMixtureMean(mnew);
+  std::vector<float> shift((size_t)D);
+  if (model.GetFullCovStatus()) {
+    float lam = 0.0f;
+    std::vector<float> v((size_t)D);
+    leading_eigenpair(model.GetMixtureVar(m2), D, &lam, v.data());
+    if (lam < 0) fail("splitGaussian(): covariance matrix not positive definite!");
+    for (int d = 0; d < D; ++d) shift[(size_t)d] = std::sqrt(lam) * v[(size_t)d];
+  } else {
+    for (int d = 0; d < D; ++d) shift[(size_t)d] = (float)(std::sqrt((double)model.GetMixtureVar(m2)[d]) * 0.5);
+  }
   for (int d = 0; d < D; ++d) {
-    const float shift = (float)(std::sqrt((double)model.GetMixtureVar(m2)[d]) * 0.5);
-    mn[d] = m[d] + shift;
-    m[d] -= shift;
+    mn[d] = m[d] + shift[(size_t)d];
+    m[d] -= shift[(size_t)d];
   }
 }
 }  // namespace
@@ -635,24 +693,27 @@ void ModelAdapt::splitMultipleGaussians(GMModel& model) {
   }
 }
 
-void ModelAdapt::TrainFromScratch(int nummix, const GMModel* init_model) {
+void ModelAdapt::TrainFromScratch(int nummix, const GMModel* init_model, bool fullcov) {
   if (N_ <= 3) fail("TrainFromScratch(): Not enough data to model training.");
-  if (init_model && init_model->GetFullCovStatus())
-    fail("TrainFromScratch(): the full-covariance split is not built");
+  if (init_model) fullcov = init_model->GetFullCovStatus();  // the init model decides
   const int D = D_;
   GMModel init;
   int max_iter = nummix;
+  auto em_all = [&](int* alive) {  // UpdateModelEM with every parameter updated
+    check(full_ ? gmm_em_update_full(h_, 1, 1, 1, alive) : gmm_em_update(h_, 1, 1, 1, alive));
+  };
   if (!init_model) {
-    // global Gaussian: one component, every posterior 1
-    init = GMModel(D, 1);
+    // global Gaussian: one component, every posterior 1 (identity covariance for a full model)
+    init = GMModel(D, 1, fullcov);
     init.SetMixWeight(0, 1.0f);
-    for (int d = 0; d < D; ++d) init.GetMixtureVar(0)[d] = 1.0f;
+    if (!fullcov)
+      for (int d = 0; d < D; ++d) init.GetMixtureVar(0)[d] = 1.0f;
     upload_model(init);
     estep(GMM_ACC_MEAN | GMM_ACC_VAR);
     int alive = 0;
-    check(gmm_em_update(h_, 1, 1, 1, &alive));
+    em_all(&alive);
     if (alive == 0) fail("trainFromScratch(): amount of data too low to estimate a model, or data are constant!");
-    check(gmm_read_model(h_, init.weights().data(), init.means().data(), init.vars().data()));
+    read_model(init);
   } else {
     init = *init_model;
     if (init.GetDimension() != D) fail("trainFromScratch(): init model and data dimensions differ!");
@@ -661,11 +722,11 @@ void ModelAdapt::TrainFromScratch(int nummix, const GMModel* init_model) {
     max_iter = nummix - init.GetNumberOfMixtures();
   }
   if (nummix < 2) max_iter = 0;
-  GMModel model(D, nummix);
+  GMModel model(D, nummix, fullcov);
   for (int m = 0; m < init.GetNumberOfMixtures(); ++m) {
     model.SetMixWeight(m, init.GetMixtureWeight(m));
     std::memcpy(model.GetMixtureMean(m), init.GetMixtureMean(m), sizeof(float) * D);
-    std::memcpy(model.GetMixtureVar(m), init.GetMixtureVar(m), sizeof(float) * D);
+    std::memcpy(model.GetMixtureVar(m), init.GetMixtureVar(m), sizeof(float) * model.DimVar());
   }
   const int iters_em = (o_.iterCountEM < 2 && o_.llTh > 0.0f) ? 2 : o_.iterCountEM;
   const float lowest = -std::numeric_limits<float>::max();
@@ -677,15 +738,11 @@ void ModelAdapt::TrainFromScratch(int nummix, const GMModel* init_model) {
       model.RearrangeMixtures();
       upload_model(model);
       estep(GMM_ACC_MEAN | GMM_ACC_VAR);
-      if (o_.verbosity) {  // the reference only tracks the average LL when verbose
-        double tl = 0.0;
-        long long tn = 0;
-        check(gmm_read_stats(h_, nullptr, nullptr, nullptr, &tl, &tn));
-        ll[0] = (float)(tl / (double)tn);
-      }
+      if (o_.verbosity)  // the reference only tracks the average LL when verbose
+        ll[0] = (float)(total_ll() / (double)N_);
       if (non_zero > 1) {
-        check(gmm_em_update(h_, 1, 1, 1, &non_zero));
-        check(gmm_read_model(h_, model.weights().data(), model.means().data(), model.vars().data()));
+        em_all(&non_zero);
+        read_model(model);
       }
       if (non_zero < 2) {
         if (non_zero < 1) model = init;

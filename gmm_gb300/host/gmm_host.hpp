@@ -145,10 +145,10 @@ class ModelAdapt {
   void InsertFiles(const std::vector<std::string>& paths, int prm_type, unsigned dwnsmp, double buffer_gb);
   // AdaptModel (OL_ModelAdapt.cpp:1163-1226): MAP (IterEM then IterMAP), MLLR, fMLLR or MLLR+MAP.
   void AdaptModel(const GMModel& ubm);
-  // TrainFromScratch (OL_ModelAdapt.cpp:667-821), diagonal covariances; `init` (optional) is the
-  // model the splitting starts from instead of the global Gaussian. (The full-covariance split
-  // along the leading eigenvector is not built.)
-  void TrainFromScratch(int nummix, const GMModel* init = nullptr);
+  // TrainFromScratch (OL_ModelAdapt.cpp:667-821); `init` (optional) is the model the splitting
+  // starts from instead of the global Gaussian and decides diagonal vs full; fullcov trains full
+  // covariance matrices (splits along the leading eigenvector, sign: largest component positive).
+  void TrainFromScratch(int nummix, const GMModel* init = nullptr, bool fullcov = false);
   const GMModel& GetModel() const { return model_; }
   const std::vector<double>& GetW() const { return W_; }  // (f)MLLR transform D x (D+1)
   bool ModelTrained() const { return trained_; }

@@ -119,6 +119,11 @@ int gmm_accumulate_full_device(gmm_handle h, int flags);
 int gmm_read_stats_full(gmm_handle h, double* n, double* F, double* Sp, double* tot_loglike,
                         long long* tot_frames);
 int gmm_loglikes_full(gmm_handle h, float* out);
+/* MLLR of the full model (ComputeW_MLLR reads the covariance diagonals, GetMixtureVarDiag):
+ * W from the occupancies and first-order statistics of the last gmm_accumulate_full*, and
+ * AdaptModelMLLR on the full model's means. */
+int gmm_mllr_estimate_full(gmm_handle h, int ubm_init, double* W);
+int gmm_mllr_apply_full(gmm_handle h, const double* W);
 /* UpdateModelEM / UpdateModelMAP (tau > 0, against gmm_set_prior_full) on the full model. */
 int gmm_em_update_full(gmm_handle h, int up_weight, int up_mean, int up_var, int* alive);
 int gmm_map_update_full(gmm_handle h, int tau, int up_weight, int up_mean, int up_var);

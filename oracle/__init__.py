@@ -515,3 +515,28 @@ def ref_robust_adapt(X, w, mu, var, tau, iters, full=False, upW=True, upM=True, 
     if rc:
         raise RuntimeError(ref().ref_last_error().decode())
     return w, mu, var, ll
+
+
+def ref_full_mllr(X, w, mu, cov, iters=1, ubm_init=False, threads=1):
+    X, w, mu, cov = map(_f32, (X, w, mu, cov))
+    N, D = X.shape
+    M = len(w)
+    W = np.zeros((D, D + 1))
+    omu = np.zeros_like(mu)
+    rc = ref().ref_full_mllr(_p(X), C.c_long(N), D, M, _p(w), _p(mu), _p(cov), iters, int(ubm_init), threads,
+                             _p(W), _p(omu))
+    if rc:
+        raise RuntimeError(ref().ref_last_error().decode())
+    return W, omu
+
+
+def ref_train_full(X, nummix, iters_em=5, split_x=0.0, split_th=0.0, ll_th=0.0, verbosity=0, threads=1):
+    """TrainFromScratch with full covariances (the split along the leading eigenvector)."""
+    X = _f32(X)
+    N, D = X.shape
+    w, mu, cov = np.zeros(nummix, np.float32), np.zeros((nummix, D), np.float32), np.zeros((nummix, D, D), np.float32)
+    rc = ref().ref_train_full(_p(X), C.c_long(N), D, nummix, iters_em, C.c_float(split_x), C.c_float(split_th),
+                              C.c_float(ll_th), verbosity, threads, 1, _p(w), _p(mu), _p(cov))
+    if rc:
+        raise RuntimeError(ref().ref_last_error().decode())
+    return w, mu, cov

@@ -44,6 +44,12 @@
 #undef private
 #undef protected
 
+GMModel* make_model_full(int M, int D, const float* w, const float* mu, const float* cov);
+void read_model_full(GMModel* g, int M, int D, float* w, float* mu, float* cov);
+extern "C" int ref_train_full(const float* X, long N, int D, int nummix, int iters_em, float split_x,
+                              float split_th, float ll_th, int verbosity, int threads, int fullcov, float* w,
+                              float* mu, float* var);
+
 namespace {
 
 // Builds a diagonal GMModel from flat arrays (w[M], mu[M*D], var[M*D]).
@@ -264,6 +270,12 @@ int ref_mllr(const float* X, long N, int D, int M, const float* w, const float* 
 // its final (rearranged) component order.
 int ref_train(const float* X, long N, int D, int nummix, int iters_em, float split_x, float split_th,
               float ll_th, int verbosity, int threads, float* w, float* mu, float* var) {
+  return ref_train_full(X, N, D, nummix, iters_em, split_x, split_th, ll_th, verbosity, threads, 0, w, mu, var);
+}
+
+// ref_train with full covariances (fullcov = 1: var receives [nummix][D][D]).
+int ref_train_full(const float* X, long N, int D, int nummix, int iters_em, float split_x, float split_th,
+                   float ll_th, int verbosity, int threads, int fullcov, float* w, float* mu, float* var) {
   try {
     CModelAdapt cm;
     CModelAdapt::OPTIONS opt = base_options(threads, 0);
@@ -281,13 +293,14 @@ int ref_train(const float* X, long N, int D, int nummix, int iters_em, float spl
     std::ostringstream sink;
     std::cout.rdbuf(sink.rdbuf());  // the reference reports progress on stdout when verbose
     try {
-      cm.TrainFromScratch((unsigned)nummix, false, NULL, "ref_train", false);
+      cm.TrainFromScratch((unsigned)nummix, fullcov != 0, NULL, "ref_train", false);
     } catch (...) {
       std::cout.rdbuf(old);
       throw;
     }
     std::cout.rdbuf(old);
-    read_model(cm._modelSP, nummix, D, w, mu, var);
+    if (fullcov) read_model_full(cm._modelSP, nummix, D, w, mu, var);
+    else read_model(cm._modelSP, nummix, D, w, mu, var);
     return 0;
   } catch (std::exception& ex) { g_err = ex.what(); return 1; }
   catch (Exception* ex) { g_err = ex->m_strDescription; delete ex; return 2; }
@@ -326,6 +339,8 @@ int ref_param_load(const char* path, int type, unsigned int dwnsmp, float* out, 
 // restatement of spotrf / spotri (oracle/ref/shim/acml.h).
 
 namespace {
+}  // namespace
+
 GMModel* make_model_full(int M, int D, const float* w, const float* mu, const float* cov) {
   GMModel* g = new GMModel(D, M, true);
   for (int m = 0; m < M; ++m)
@@ -339,7 +354,6 @@ void read_model_full(GMModel* g, int M, int D, float* w, float* mu, float* cov) 
     memcpy(cov + (size_t)m * D * D, g->GetMixtureVar(m), sizeof(float) * D * D);
   }
 }
-}  // namespace
 
 extern "C" {
 
@@ -567,6 +581,41 @@ int ref_robust_adapt(const float* X, long N, int D, int M, float* w, float* mu, 
     if (full) read_model_full(model, M, D, w, mu, var);
     else read_model(model, M, D, w, mu, var);
     delete model;
+    delete ubm;
+    return 0;
+  } catch (std::exception& ex) { g_err = ex.what(); return 1; }
+  catch (Exception* ex) { g_err = ex->m_strDescription; delete ex; return 2; }
+}
+
+}  // extern "C"
+
+extern "C" {
+
+// Global MLLR of a full-covariance UBM (IterW_MLLR + AdaptModelMLLR): W D x (D+1), omu = A mu + b.
+int ref_full_mllr(const float* X, long N, int D, int M, const float* w, const float* mu, const float* cov,
+                  int iters, int ubm_init, int threads, double* W, float* omu) {
+  try {
+    GMModel* ubm = make_model_full(M, D, w, mu, cov);
+    CModelAdapt cm;
+    CModelAdapt::OPTIONS opt = base_options(threads, 0);
+    opt._adaptType = MLLR;
+    opt._iterMLLR = iters;
+    opt._mllrUBMInit = ubm_init != 0;
+    opt._applyTransforms = true;
+    cm.SetOptions(opt);
+    Param p;
+    fill_param(p, X, N, D);
+    cm.InsertData(p, false);
+    cm.Initialize(ubm);
+    cm._UBM = ubm;
+    MATRIX* Wm = cm.IterW_MLLR(ubm, iters, NULL);
+    for (int i = 0; i < D; ++i)
+      for (int j = 0; j <= D; ++j) W[(size_t)i * (D + 1) + j] = Wm->GetXY(i, j);
+    GMModel* ad = cm.AdaptModelMLLR(ubm, Wm);
+    for (int m = 0; m < M; ++m) memcpy(omu + (size_t)m * D, ad->GetMixtureMean(m), sizeof(float) * D);
+    delete ad;
+    Wm->Delete();
+    delete Wm;
     delete ubm;
     return 0;
   } catch (std::exception& ex) { g_err = ex.what(); return 1; }

@@ -4,12 +4,13 @@
 // the inverse from it), in single precision, column-major, lower triangle -- the reference calls
 // them with uplo 'L' on its row-major symmetric matrices. A vendor library may order the float
 // operations differently, so full-covariance outputs of this build pin the reference's logic,
-// not the last bits of ACML's arithmetic. ssyevr (eigenvectors for the full-covariance split of
-// training from scratch) is not restated; calling it throws.
+// not the last bits of ACML's arithmetic. ssyevr (the eigenvector of the full-covariance split of
+// training from scratch) is restated for the largest eigenpair only, below.
 #ifndef ORACLE_SHIM_ACML_H
 #define ORACLE_SHIM_ACML_H
 #include <cmath>
 #include <stdexcept>
+#include <vector>
 
 namespace acml_shim {
 inline float& at(float* a, int lda, int i, int j) { return a[i + (long)j * lda]; }
@@ -87,7 +88,58 @@ inline void spotri(char uplo, int n, float* a, int lda, int* info) {
   }
 }
 
-inline void ssyevr(char, char, char, int, float*, int, float, float, int, int, float, int*, float*, float*, int, int*, int*) {
-  throw std::runtime_error("ssyevr: the full-covariance split of training from scratch is not restated");
+// ssyevr for the one call the reference makes (getEigValVecs: jobz 'V', range 'I', il = iu = n):
+// the largest eigenvalue of the symmetric matrix and its unit eigenvector, by cyclic Jacobi
+// rotations in double. The eigenvector's sign is not fixed by the problem; this stand-in makes
+// its largest-magnitude component positive (the convention the GB300 drivers use for the
+// full-covariance split), where ACML's choice is unknown.
+inline void ssyevr(char jobz, char range, char, int n, float* a, int lda, float, float, int il, int iu, float, int* m,
+                   float* w, float* z, int, int*, int* info) {
+  if (jobz != 'V' || range != 'I' || il != n || iu != n)
+    throw std::runtime_error("ssyevr: only the largest eigenpair is restated");
+  std::vector<double> A((size_t)n * n), V((size_t)n * n, 0.0);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) A[(size_t)i * n + j] = a[i + (long)j * lda];
+  for (int i = 0; i < n; ++i) V[(size_t)i * n + i] = 1.0;
+  for (int sweep = 0; sweep < 100; ++sweep) {
+    double off = 0.0;
+    for (int p = 0; p < n; ++p)
+      for (int q = p + 1; q < n; ++q) off += A[(size_t)p * n + q] * A[(size_t)p * n + q];
+    if (off < 1e-30) break;
+    for (int p = 0; p < n; ++p)
+      for (int q = p + 1; q < n; ++q) {
+        const double apq = A[(size_t)p * n + q];
+        if (apq == 0.0) continue;
+        const double theta = (A[(size_t)q * n + q] - A[(size_t)p * n + p]) / (2.0 * apq);
+        const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+        const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+        for (int k = 0; k < n; ++k) {  // A <- J^T A J, V <- V J
+          const double akp = A[(size_t)k * n + p], akq = A[(size_t)k * n + q];
+          A[(size_t)k * n + p] = c * akp - s * akq;
+          A[(size_t)k * n + q] = s * akp + c * akq;
+        }
+        for (int k = 0; k < n; ++k) {
+          const double apk = A[(size_t)p * n + k], aqk = A[(size_t)q * n + k];
+          A[(size_t)p * n + k] = c * apk - s * aqk;
+          A[(size_t)q * n + k] = s * apk + c * aqk;
+        }
+        for (int k = 0; k < n; ++k) {
+          const double vkp = V[(size_t)k * n + p], vkq = V[(size_t)k * n + q];
+          V[(size_t)k * n + p] = c * vkp - s * vkq;
+          V[(size_t)k * n + q] = s * vkp + c * vkq;
+        }
+      }
+  }
+  int best = 0;
+  for (int i = 1; i < n; ++i)
+    if (A[(size_t)i * n + i] > A[(size_t)best * n + best]) best = i;
+  int big = 0;
+  for (int i = 1; i < n; ++i)
+    if (std::fabs(V[(size_t)i * n + best]) > std::fabs(V[(size_t)big * n + best])) big = i;
+  const double sg = V[(size_t)big * n + best] < 0 ? -1.0 : 1.0;
+  for (int i = 0; i < n; ++i) z[i] = (float)(sg * V[(size_t)i * n + best]);
+  w[0] = (float)A[(size_t)best * n + best];
+  *m = 1;
+  *info = 0;
 }
 #endif

@@ -19,6 +19,7 @@ from their own sources, see oracle/Makefile) and records its outputs on small in
 * ``map_mllr.npz`` -- mean-only MAP (tau = 16) and one global MLLR transform, with and without
   the UBM-based initialisation.
 * ``train.npz``    -- TrainFromScratch with four option sets.
+* ``train_full.npz`` -- TrainFromScratch with full covariances (one split per round, and several).
 * ``full.npz``     -- full covariances: per-frame log-likelihoods of the first 1000 frames of
   example/data.bin under example/myModelFC.gmm (4 threads) and their E-step statistics; three EM
   iterations (weights, means, covariances) and one MAP iteration (tau = 16, all parameters) of
@@ -29,6 +30,8 @@ from their own sources, see oracle/Makefile) and records its outputs on small in
 * ``robust.npz``   -- --robust: the auxiliary statistics (one thread) of a diagonal and a
   full-covariance model, two robust EM iterations of each, and one robust MAP iteration
   (tau = 16, means and variances) of a diagonal UBM.
+* ``full_mllr.npz`` -- global MLLR of a seeded full-covariance UBM (M = 16, D = 8), with and
+  without the UBM-based initialisation: W and the transformed means.
 * ``fmllr.npz``    -- fMLLR (ComputeW_fMLLR, 20 passes) of a diagonal UBM (M = 32, D = 12) from
   one speaker of seeded affinely transformed UBM samples: the transform and the E-step
   statistics (packed full second order) it was computed from.
@@ -121,10 +124,12 @@ def main():
             print(fn, os.path.getsize(os.path.join(HERE, fn)))
 
     train_fixture()
+    train_full_fixture()
     full_fixture(a.ref_root)
     fmllr_fixture()
     mllr_map_fixture()
     robust_fixture()
+    full_mllr_fixture()
 
 
 def full_fixture(ref_root):
@@ -144,6 +149,15 @@ def full_fixture(ref_root):
     mw, mmu, mcov, mll = O.ref_full_adapt(Xs, w, mu, cov, 16, 1, threads=2)
     out.update(map_w=mw, map_mu=mmu, map_cov=mcov, map_ll=mll)
     np.savez_compressed(os.path.join(HERE, "full.npz"), **out)
+
+
+def full_mllr_fixture():
+    w, mu, cov = synth.generator_gmm_full(51, 16, 8)
+    X = synth.sample_gmm_full(52, w, mu + 0.4, cov, 3000)
+    W0, mu0 = O.ref_full_mllr(X, w, mu, cov)
+    W1, mu1 = O.ref_full_mllr(X, w, mu, cov, ubm_init=True)
+    np.savez_compressed(os.path.join(HERE, "full_mllr.npz"), X=X, w=w, mu=mu, cov=cov, W0=W0, mu0=mu0, W1=W1,
+                        mu1=mu1)
 
 
 def robust_fixture():
@@ -179,6 +193,19 @@ def fmllr_fixture():
                         Sp=st["Sp"], totLL=st["totLL"])
 
 
+def train_full_fixture():
+    """TrainFromScratch with full covariances (the split along the leading eigenvector; the
+    reference build's ssyevr is the restated stand-in of oracle/ref/shim/acml.h)."""
+    w, mu, cov = synth.generator_gmm_full(61, 4, 6)
+    X = synth.sample_gmm_full(62, w, mu, cov, 3000)
+    out = {"X": X}
+    for name, kw in {"one": dict(nummix=4, iters_em=3),
+                     "multi": dict(nummix=6, iters_em=3, split_x=0.5, split_th=0.2)}.items():
+        rw, rmu, rcov = O.ref_train_full(X, **kw)
+        out.update({f"{name}_w": rw, f"{name}_mu": rmu, f"{name}_cov": rcov})
+    np.savez_compressed(os.path.join(HERE, "train_full.npz"), **out)
+
+
 def train_fixture():
     """TrainFromScratch (OL_ModelAdapt.cpp:667-821) by the reference build on seeded data."""
     gw, gmu, gvar = synth.generator_gmm(31, 6, 5)
@@ -198,6 +225,9 @@ if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "--full-only":
         O.build(ref=True)
         full_fixture("/root/reference/GMM")
+    elif len(sys.argv) > 1 and sys.argv[1] == "--train-full-only":
+        O.build(ref=True)
+        train_full_fixture()
     elif len(sys.argv) > 1 and sys.argv[1] == "--robust-only":
         O.build(ref=True)
         robust_fixture()

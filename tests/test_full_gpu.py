@@ -154,3 +154,21 @@ def test_estimator_interface(glib, golden, oracle):
     assert np.abs(st.S - 2 * g["ex_Sp"]).max() <= 2e-5 * np.abs(2 * g["ex_Sp"]).max()
     ll = est.compVecsLogLikeMT(g["ex_X"], 1000, 20)
     assert np.abs(ll - g["ex_ll"]).max() < 1e-4
+
+
+@pytest.mark.parametrize("init", [False, True])
+def test_mllr_of_full_model(glib, golden, init):
+    """MLLR of a full-covariance UBM (the covariance diagonals in G and k) against the reference
+    build (tests/golden/full_mllr.npz): W within 1e-4 abs (the E-step's LL arithmetic differs at
+    ~1e-6), transformed means within 1e-4."""
+    from gmm_gb300 import adapt, formats
+    g = golden("full_mllr.npz")
+    ma = adapt.ModelAdapt(adapt.Options(adaptType=adapt.MLLR, mllrUBMInit=init, applyTransforms=True))
+    ma.InsertData(g["X"])
+    ma.AdaptModel(formats.GMModel(g["w"], g["mu"], g["cov"]))
+    key = "1" if init else "0"
+    W = ma.PickUpTRNMatrix()
+    assert np.abs(W - g[f"W{key}"]).max() < 1e-4, np.abs(W - g[f"W{key}"]).max()
+    m = ma.PickUpClientModel()
+    assert m.full and np.abs(m.mu - g[f"mu{key}"]).max() < 1e-4
+    assert np.array_equal(m.var, g["cov"])

@@ -217,3 +217,22 @@ def test_model_file_and_class_modes(exe, glib, tmp_path):
         want = python_map(x)
         assert np.allclose(got.mu, want.mu, rtol=1e-6, atol=1e-7), name
         assert np.allclose(got.var, want.var, rtol=1e-6), name
+
+
+def test_train_full_covariance_command_line(exe, golden, tmp_path):
+    """gmm_adapt --full-cov -g 6 --split-X 0.5 --split-th 0.2 against the reference build's
+    full-covariance TrainFromScratch (tests/golden/train_full.npz); 1e-4 abs + rel."""
+    from gmm_gb300 import formats
+    g = golden("train_full.npz")
+    feat = tmp_path / "t.raw"
+    formats.write_raw(str(feat), g["X"])
+    out = tmp_path / "t.gmm"
+    run(exe("gmm_adapt"), "-i", feat, "--data-T", "2", "-g", "6", "--it-EM", "3", "--split-X", "0.5",
+        "--split-th", "0.2", "--full-cov", "-o", out)
+    m = formats.read_gmm_bin(str(out))
+    w, mu, cov = g["multi_w"], g["multi_mu"], g["multi_cov"]
+    alive = w > 0
+    assert m.full and m.M == alive.sum()
+    assert np.allclose(m.w, w[alive], rtol=1e-4, atol=1e-4)
+    assert np.allclose(m.mu, mu[alive], rtol=1e-4, atol=1e-4)
+    assert np.allclose(m.var, cov[alive], rtol=1e-4, atol=1e-4)

@@ -36,3 +36,25 @@ def test_train_from_scratch_matches_reference(glib, golden, name):
     assert np.allclose(model.w, w, rtol=1e-4, atol=1e-4), np.abs(model.w - w).max()
     assert np.allclose(model.mu[alive], mu[alive], rtol=1e-4, atol=1e-4), np.abs(model.mu - mu)[alive].max()
     assert np.allclose(model.var[alive], var[alive], rtol=1e-4), (np.abs(model.var - var)[alive] / var[alive]).max()
+
+
+@pytest.mark.parametrize("name", ["one", "multi"])
+def test_train_full_covariance_matches_reference(glib, golden, name):
+    """Full covariances: splits along the leading eigenvector (sign: largest component positive,
+    the convention of the reference build's restated ssyevr). Weights / means 1e-4 abs + rel,
+    covariances 1e-4 abs + rel."""
+    from gmm_gb300 import adapt
+    g = golden("train_full.npz")
+    kw = {"one": dict(nummix=4, iters_em=3), "multi": dict(nummix=6, iters_em=3, split_x=0.5, split_th=0.2)}[name]
+    opt = adapt.Options(adaptType=adapt.FROM_SCRATCH, iterCountEM=kw["iters_em"],
+                        splitXpercAtOnce=kw.get("split_x", 0.0), splitTh=kw.get("split_th", 0.0))
+    ma = adapt.ModelAdapt(opt)
+    ma.InsertData(g["X"])
+    model = ma.TrainFromScratch(kw["nummix"], fullcov=True)
+    assert model.full
+    w, mu, cov = g[f"{name}_w"], g[f"{name}_mu"], g[f"{name}_cov"]
+    assert np.array_equal(model.w > 0, w > 0)
+    alive = w > 0
+    assert np.allclose(model.w, w, rtol=1e-4, atol=1e-4)
+    assert np.allclose(model.mu[alive], mu[alive], rtol=1e-4, atol=1e-4)
+    assert np.allclose(model.var[alive], cov[alive], rtol=1e-4, atol=1e-4)
