@@ -35,6 +35,7 @@ SIGNATURES = {
     "gmm_mllr_apply_full": (_i, [_vp, _vp]),
     "gmm_read_aux": (_i, [_vp, _i, _vp, _vp, _vp]),
     "gmm_fmllr_apply": (_i, [_vp, _vp]),
+    "gmm_fmllr_estimate_full": (_i, [_vp, _i, _vp]),
     "gmm_set_prior_full": (_i, [_vp, _vp, _vp, _vp]),
     "gmm_read_model_full": (_i, [_vp, _vp, _vp, _vp]),
     "gmm_accumulate_full": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _vp]),
@@ -277,6 +278,11 @@ class Handle:
         """W [D, D+1] = [A | b] of the resident features against the resident diagonal model."""
         W = np.zeros((self.D, self.D + 1))
         self.check(self.lib.gmm_fmllr_estimate(self.h, int(iters), ptr(W)))
+        return W
+
+    def fmllr_estimate_full(self, iters=20):
+        W = np.zeros((self.Df, self.Df + 1))
+        self.check(self.lib.gmm_fmllr_estimate_full(self.h, int(iters), ptr(W)))
         return W
 
     def fmllr_apply(self, W):

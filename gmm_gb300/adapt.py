@@ -372,11 +372,10 @@ class ModelAdapt:
                 model = self.IterMAP(model, ubm, o.iterCountMAP)
             self._model = model
         elif o.adaptType == FMLLR:
-            if ubm.full:
-                raise NotImplementedError("fMLLR of full-covariance models is not built")
             self._ensure_features()
             self._upload(ubm.copy())
-            self._W = self.dev.fmllr_estimate(o.iterfMLLR)
+            self._W = (self.dev.fmllr_estimate_full(o.iterfMLLR) if ubm.full
+                       else self.dev.fmllr_estimate(o.iterfMLLR))
         elif o.adaptType == MLLR:
             self._W = self.IterW_MLLR(ubm, o.iterMLLR)
             if o.applyTransforms:

@@ -272,36 +272,20 @@ __global__ void fmllr_apply_kernel(long long N, int D, const double* __restrict_
 
 using namespace gmm;
 
-extern "C" {
-
-int gmm_fmllr_estimate(gmm_handle h, int iters, double* W) {
-  if (!h) return GMM_ERR_ARG;
-  Ctx* c = h;
-  if (!W) return fail(c, GMM_ERR_ARG, "gmm_fmllr_estimate: null output");
-  if (iters < 1) return fail(c, GMM_ERR_ARG, "gmm_fmllr_estimate: iters must be >= 1");
-  if (!c->w) return fail(c, GMM_ERR_STATE, "no model uploaded");
-  cudaSetDevice(c->device);
-  const int M = c->M, D = c->D, E = D + 1, P = D * (D + 1) / 2;
-  if (D > 64) return fail(c, GMM_ERR_UNSUPPORTED, "fMLLR supports D <= 64");
-  const size_t nst = (size_t)M * (1 + D + P) + 2;
-  double *d_stats = nullptr, *dG = nullptr, *dGi = nullptr, *dK = nullptr, *dW = nullptr;
+namespace gmm {
+// From the E-step statistics on the device ([n | F | S packed | ...], M components of dimension
+// D) and the model's means and variances (diagonals for a full model): CheckInvertibility, G and
+// k, the inverses and the row passes; W to the host. beta = the frame count.
+static int fmllr_from_stats(Ctx* c, int M, int D, const float* mu, const float* var, const double* d_stats,
+                            long long frames, int iters, double* W) {
+  const int E = D + 1;
+  double *dG = nullptr, *dGi = nullptr, *dK = nullptr, *dW = nullptr;
   int* dstatus = nullptr;
-  int rc = dalloc(c, (void**)&d_stats, nst * sizeof(double), "fMLLR statistics");
-  if (!rc) rc = dalloc(c, (void**)&dG, sizeof(double) * (size_t)D * E * E, "fMLLR G");
+  int rc = dalloc(c, (void**)&dG, sizeof(double) * (size_t)D * E * E, "fMLLR G");
   if (!rc) rc = dalloc(c, (void**)&dGi, sizeof(double) * (size_t)D * E * E, "fMLLR G inverse");
   if (!rc) rc = dalloc(c, (void**)&dK, sizeof(double) * (size_t)D * E, "fMLLR k");
   if (!rc) rc = dalloc(c, (void**)&dW, sizeof(double) * (size_t)D * E, "fMLLR transform");
   if (!rc) rc = dalloc(c, (void**)&dstatus, sizeof(int), "fMLLR status");
-  auto release = [&]() {
-    cudaStreamSynchronize(c->stream);
-    dfree(c, d_stats, nst * sizeof(double));
-    dfree(c, dG, sizeof(double) * (size_t)D * E * E);
-    dfree(c, dGi, sizeof(double) * (size_t)D * E * E);
-    dfree(c, dK, sizeof(double) * (size_t)D * E);
-    dfree(c, dW, sizeof(double) * (size_t)D * E);
-    dfree(c, dstatus, sizeof(int));
-  };
-  if (!rc) rc = diag_fullstats_estep(c, d_stats);
   // CheckInvertibility (OL_ModelAdapt.cpp:1851-1878) on the occupancies
   std::vector<double> n((size_t)M);
   if (!rc) {
@@ -323,7 +307,7 @@ int gmm_fmllr_estimate(gmm_handle h, int iters, double* W) {
     GMM_LAUNCH(c, "fmllr_gk_kernel");
     const int entries = E * (E + 1) / 2 + E;
     dim3 grid((entries + 127) / 128, D);
-    fmllr_gk_kernel<<<grid, 128, 0, c->stream>>>(M, D, c->mu, c->var, d_stats, dG, dK);
+    fmllr_gk_kernel<<<grid, 128, 0, c->stream>>>(M, D, mu, var, d_stats, dG, dK);
   }
   if (!rc) {
     GMM_LAUNCH(c, "fmllr_ginv_kernel");
@@ -334,7 +318,7 @@ int gmm_fmllr_estimate(gmm_handle h, int iters, double* W) {
     cudaFuncSetAttribute(fmllr_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     GMM_LAUNCH(c, "fmllr_rows_kernel");
     // beta: the frame count as the reference passes it, (float) getTotAccSamples()
-    const double beta = (double)(float)c->N;
+    const double beta = (double)(float)frames;
     fmllr_rows_kernel<<<1, 256, smem, c->stream>>>(D, iters, beta, dG, dGi, dK, dW, dstatus);
   }
   int status = 0;
@@ -344,7 +328,58 @@ int gmm_fmllr_estimate(gmm_handle h, int iters, double* W) {
     rc = sync(c, "fMLLR transform");
   }
   if (!rc && status) rc = fail(c, GMM_ERR_MLLR, "EstimateAb_fmllr(): Discriminant < 0 or a zero root!");
-  release();
+  cudaStreamSynchronize(c->stream);
+  dfree(c, dG, sizeof(double) * (size_t)D * E * E);
+  dfree(c, dGi, sizeof(double) * (size_t)D * E * E);
+  dfree(c, dK, sizeof(double) * (size_t)D * E);
+  dfree(c, dW, sizeof(double) * (size_t)D * E);
+  dfree(c, dstatus, sizeof(int));
+  return rc;
+}
+}  // namespace gmm
+
+extern "C" {
+
+int gmm_fmllr_estimate(gmm_handle h, int iters, double* W) {
+  if (!h) return GMM_ERR_ARG;
+  Ctx* c = h;
+  if (!W) return fail(c, GMM_ERR_ARG, "gmm_fmllr_estimate: null output");
+  if (iters < 1) return fail(c, GMM_ERR_ARG, "gmm_fmllr_estimate: iters must be >= 1");
+  if (!c->w) return fail(c, GMM_ERR_STATE, "no model uploaded");
+  cudaSetDevice(c->device);
+  const int M = c->M, D = c->D, P = D * (D + 1) / 2;
+  if (D > 64) return fail(c, GMM_ERR_UNSUPPORTED, "fMLLR supports D <= 64");
+  const size_t nst = (size_t)M * (1 + D + P) + 2;
+  double* d_stats = nullptr;
+  int rc = dalloc(c, (void**)&d_stats, nst * sizeof(double), "fMLLR statistics");
+  if (!rc) rc = diag_fullstats_estep(c, d_stats);
+  if (!rc) rc = fmllr_from_stats(c, M, D, c->mu, c->var, d_stats, c->N, iters, W);
+  cudaStreamSynchronize(c->stream);
+  dfree(c, d_stats, nst * sizeof(double));
+  return rc;
+}
+
+int gmm_fmllr_estimate_full(gmm_handle h, int iters, double* W) {
+  if (!h) return GMM_ERR_ARG;
+  Ctx* c = h;
+  if (!W) return fail(c, GMM_ERR_ARG, "gmm_fmllr_estimate_full: null output");
+  if (iters < 1) return fail(c, GMM_ERR_ARG, "gmm_fmllr_estimate_full: iters must be >= 1");
+  cudaSetDevice(c->device);
+  // the full model's E-step with full second-order statistics, then its covariance diagonals
+  int rc = gmm_accumulate_full_device(h, GMM_ACC_MEAN | GMM_ACC_VAR);
+  if (rc) return rc;
+  const double* stats = nullptr;
+  const float *mu = nullptr, *dvar = nullptr;
+  int M = 0, D = 0;
+  long long frames = 0;
+  float* diag = nullptr;
+  rc = full_fmllr_inputs(c, &stats, &mu, &diag, &M, &D, &frames);
+  if (!rc) {
+    dvar = diag;
+    rc = fmllr_from_stats(c, M, D, mu, dvar, stats, frames, iters, W);
+  }
+  cudaStreamSynchronize(c->stream);
+  dfree(c, diag, sizeof(float) * (size_t)M * D);
   return rc;
 }
 

@@ -888,6 +888,23 @@ int diag_fullstats_estep(Ctx* c, double* stats) {
   return GMM_OK;
 }
 
+int full_fmllr_inputs(Ctx* c, const double** stats, const float** mu, float** diag, int* M, int* D,
+                      long long* frames) {
+  FullModel* f = c->full;
+  if (!f || !f->stats_valid) return fail(c, GMM_ERR_STATE, "no statistics accumulated");
+  if (f->M < 1) return fail(c, GMM_ERR_STATE, "no full-covariance model uploaded");
+  const int rc = dalloc(c, (void**)diag, sizeof(float) * (size_t)f->M * f->D, "covariance diagonals");
+  if (rc) return rc;
+  const long long tot = (long long)f->M * f->D;
+  full_diag_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(f->M, f->D, f->cov, *diag);
+  *stats = f->stats;
+  *mu = f->mu;
+  *M = f->M;
+  *D = f->D;
+  *frames = f->tot_frames;
+  return GMM_OK;
+}
+
 bool full_aux(Ctx* c, const double** aux, int* M, int* D) {
   FullModel* f = c->full;
   if (!f || !f->aux_valid) return false;

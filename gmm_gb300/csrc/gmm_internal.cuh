@@ -268,6 +268,10 @@ int robust_chunk(Ctx* c, int M, int D, int Mact, const int* act, long long f0, l
 int robust_make(Ctx* c, int M, int D, int full, double* stats, const double* aux, double** nind);
 int ensure_aux(Ctx* c, double** aux, size_t* cap, int M, int D);
 bool full_aux(Ctx* c, const double** aux, int* M, int* D);  // the full model's valid auxiliary statistics
+// fMLLR of the full model: its device statistics, means, and a new device array of covariance
+// diagonals (the caller frees it with dfree(c, *diag, M * D * sizeof(float))).
+int full_fmllr_inputs(Ctx* c, const double** stats, const float** mu, float** diag, int* M, int* D,
+                      long long* frames);
 
 }  // namespace gmm
 

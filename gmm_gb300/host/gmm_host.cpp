@@ -565,12 +565,12 @@ void ModelAdapt::AdaptModel(const GMModel& ubm) {
     model_ = model;
     trained_ = true;
   } else if (o_.adaptType == FMLLR) {  // ComputeW_fMLLR(_UBM): the transform is the result
-    if (ubm.GetFullCovStatus()) fail("ComputeW_fMLLR(): fMLLR of full-covariance models is not built");
     GMModel u = ubm;
     u.RearrangeMixtures();
     upload_model(u);
     W_.assign((size_t)D_ * (D_ + 1), 0.0);
-    check(gmm_fmllr_estimate(h_, o_.iterfMLLR, W_.data()));
+    check(full_ ? gmm_fmllr_estimate_full(h_, o_.iterfMLLR, W_.data())
+                : gmm_fmllr_estimate(h_, o_.iterfMLLR, W_.data()));
   } else {
     fail("AdaptModel(): use TrainFromScratch for --type 0");
   }

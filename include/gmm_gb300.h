@@ -136,6 +136,9 @@ int gmm_map_update_full(gmm_handle h, int tau, int up_weight, int up_mean, int u
  * row-major [A | b]; features are adapted as x' = A x + b. GMM_ERR_MLLR when CheckInvertibility
  * fails or a row's quadratic has no usable root. D <= 64. */
 int gmm_fmllr_estimate(gmm_handle h, int iters, double* W);
+/* fMLLR of the full-covariance model: its E-step with full statistics, and the covariance
+ * diagonals in G and k (ComputeKiGi_fMLLR reads GetMixtureVarDiag). */
+int gmm_fmllr_estimate_full(gmm_handle h, int iters, double* W);
 /* Applies W to the features uploaded with gmm_upload_features, in place on the device. */
 int gmm_fmllr_apply(gmm_handle h, const double* W);
 

@@ -540,3 +540,13 @@ def ref_train_full(X, nummix, iters_em=5, split_x=0.0, split_th=0.0, ll_th=0.0, 
     if rc:
         raise RuntimeError(ref().ref_last_error().decode())
     return w, mu, cov
+
+
+def ref_fmllr_full(X, w, mu, cov):
+    X, w, mu, cov = map(_f32, (X, w, mu, cov))
+    N, D = X.shape
+    W = np.zeros((D, D + 1))
+    rc = ref().ref_fmllr_full(_p(X), C.c_long(N), D, len(w), _p(w), _p(mu), _p(cov), _p(W))
+    if rc:
+        raise RuntimeError(ref().ref_last_error().decode())
+    return W

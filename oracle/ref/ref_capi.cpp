@@ -623,3 +623,32 @@ int ref_full_mllr(const float* X, long N, int D, int M, const float* w, const fl
 }
 
 }  // extern "C"
+
+extern "C" {
+
+// fMLLR of a full-covariance UBM (ComputeW_fMLLR with GetMixtureVarDiag): W D x (D+1).
+int ref_fmllr_full(const float* X, long N, int D, int M, const float* w, const float* mu, const float* cov,
+                   double* W) {
+  try {
+    GMModel* ubm = make_model_full(M, D, w, mu, cov);
+    CModelAdapt cm;
+    CModelAdapt::OPTIONS opt = base_options(1, 0);
+    opt._adaptType = fMLLR;
+    cm.SetOptions(opt);
+    Param p;
+    fill_param(p, X, N, D);
+    cm.InsertData(p, false);
+    cm.Initialize(ubm);
+    cm._UBM = ubm;
+    MATRIX* Wm = cm.ComputeW_fMLLR(ubm);
+    for (int i = 0; i < D; ++i)
+      for (int j = 0; j <= D; ++j) W[(size_t)i * (D + 1) + j] = Wm->GetXY(i, j);
+    Wm->Delete();
+    delete Wm;
+    delete ubm;
+    return 0;
+  } catch (std::exception& ex) { g_err = ex.what(); return 1; }
+  catch (Exception* ex) { g_err = ex->m_strDescription; delete ex; return 2; }
+}
+
+}  // extern "C"

@@ -31,7 +31,7 @@ from their own sources, see oracle/Makefile) and records its outputs on small in
   full-covariance model, two robust EM iterations of each, and one robust MAP iteration
   (tau = 16, means and variances) of a diagonal UBM.
 * ``full_mllr.npz`` -- global MLLR of a seeded full-covariance UBM (M = 16, D = 8), with and
-  without the UBM-based initialisation: W and the transformed means.
+  without the UBM-based initialisation: W and the transformed means; and its fMLLR transform.
 * ``fmllr.npz``    -- fMLLR (ComputeW_fMLLR, 20 passes) of a diagonal UBM (M = 32, D = 12) from
   one speaker of seeded affinely transformed UBM samples: the transform and the E-step
   statistics (packed full second order) it was computed from.
@@ -156,8 +156,9 @@ def full_mllr_fixture():
     X = synth.sample_gmm_full(52, w, mu + 0.4, cov, 3000)
     W0, mu0 = O.ref_full_mllr(X, w, mu, cov)
     W1, mu1 = O.ref_full_mllr(X, w, mu, cov, ubm_init=True)
+    fW = O.ref_fmllr_full(X, w, mu, cov)
     np.savez_compressed(os.path.join(HERE, "full_mllr.npz"), X=X, w=w, mu=mu, cov=cov, W0=W0, mu0=mu0, W1=W1,
-                        mu1=mu1)
+                        mu1=mu1, fW=fW)
 
 
 def robust_fixture():

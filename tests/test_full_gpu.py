@@ -172,3 +172,15 @@ def test_mllr_of_full_model(glib, golden, init):
     m = ma.PickUpClientModel()
     assert m.full and np.abs(m.mu - g[f"mu{key}"]).max() < 1e-4
     assert np.array_equal(m.var, g["cov"])
+
+
+def test_fmllr_of_full_model(glib, golden):
+    """fMLLR of a full-covariance UBM (full E-step statistics, covariance diagonals in G and k)
+    against the reference build: W within 1e-4 abs."""
+    from gmm_gb300 import adapt, formats
+    g = golden("full_mllr.npz")
+    ma = adapt.ModelAdapt(adapt.Options(adaptType=adapt.FMLLR))
+    ma.InsertData(g["X"])
+    ma.AdaptModel(formats.GMModel(g["w"], g["mu"], g["cov"]))
+    W = ma.PickUpTRNMatrix()
+    assert np.abs(W - g["fW"]).max() < 1e-4, np.abs(W - g["fW"]).max()
