@@ -198,9 +198,10 @@ class UbmEm:
         return int(self.X.nbytes), int(sum(o.nbytes for o in self.out))
 
     def e2e_step(self):
+        # E-step over the pinned host features (chunked copies overlapping the logits kernels),
+        # M-step on the device, the updated model back to the host
         dev = self.dev
-        dev.upload_features(self.Xhost)
-        dev.accumulate_device(self.lib.ACC_MEAN | self.lib.ACC_VAR)
+        dev.accumulate_host(self.Xhost, self.lib.ACC_MEAN | self.lib.ACC_VAR)
         dev.em_update(True, True, True)
         wb, mub, varb = self.out
         dev.check(dev.lib.gmm_read_model(dev.h, wb.ctypes.data, mub.ctypes.data, varb.ctypes.data))

@@ -31,6 +31,7 @@ SIGNATURES = {
     "gmm_upload_model_full": (_i, [_vp, _i, _i, _vp, _vp, _vp]),
     "gmm_fmllr_estimate": (_i, [_vp, _i, _vp]),
     "gmm_set_robust": (_i, [_vp, _i]),
+    "gmm_accumulate_host": (_i, [_vp, _i, _vp, _ll, _i]),
     "gmm_mllr_estimate_full": (_i, [_vp, _i, _vp]),
     "gmm_mllr_apply_full": (_i, [_vp, _vp]),
     "gmm_read_aux": (_i, [_vp, _i, _vp, _vp, _vp]),
@@ -236,6 +237,14 @@ class Handle:
         self.check(self.lib.gmm_accumulate(self.h, flags, ptr(n), ptr(F), ptr(S),
                                            C.byref(tl), C.byref(tn)))
         return dict(n=n, F=F, S=S, totLL=tl.value, totN=tn.value)
+
+    def accumulate_host(self, X, flags=ACC_MEAN | ACC_VAR):
+        """E-step over host features (uploaded in chunks that overlap the E-step); statistics
+        stay on the device."""
+        X = np.ascontiguousarray(X, np.float32)
+        N, D = X.shape
+        self.check(self.lib.gmm_accumulate_host(self.h, flags, ptr(X), N, D))
+        self.N = N
 
     def accumulate_device(self, flags=ACC_MEAN | ACC_VAR):
         self.check(self.lib.gmm_accumulate_device(self.h, flags))

@@ -288,6 +288,8 @@ int gmm_destroy(gmm_handle h) {
   dfree(c, c->flag, 0);
   if (c->hflag) cudaFreeHost(c->hflag);
   if (c->hstage) cudaFreeHost(c->hstage);
+  for (cudaEvent_t ev : c->copy_events) cudaEventDestroy(ev);
+  if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   cudaStreamDestroy(c->stream);
   delete c;
   return GMM_OK;
@@ -449,6 +451,49 @@ int gmm_accumulate_device(gmm_handle h, int flags) {
   int rc = accumulate_device(h, flags);
   if (rc) return rc;
   return sync(h, "gmm_accumulate");
+}
+
+int gmm_accumulate_host(gmm_handle h, int flags, const float* X, long long N, int D) {
+  if (!h) return GMM_ERR_ARG;
+  Ctx* c = h;
+  if (!X && N > 0) return fail(c, GMM_ERR_ARG, "gmm_accumulate_host: null array");
+  if (N < 0 || D < 1 || D > kMaxDim) return fail(c, GMM_ERR_ARG, "gmm_accumulate_host: bad N or D");
+  cudaSetDevice(c->device);
+  const bool streamed = c->precision == GMM_PREC_TC && !c->robust && c->w && D == c->D && tc_supported(D) && N > 0;
+  if (!streamed) {  // the plain path (or a robust E-step): upload, then the E-step
+    int rc = gmm_upload_features(h, X, N, D);
+    if (!rc) rc = gmm_accumulate_device(h, flags);
+    return rc;
+  }
+  // the handle's own feature buffer, filled by the E-step's chunked copies
+  const bool reuse = c->Xown && c->N == N && c->Dx == D && c->ll;
+  if (!reuse) {
+    free_features(c);
+    int rc = dalloc(c, (void**)&c->Xown, sizeof(float) * (size_t)N * D, "features");
+    if (!rc) {
+      c->N = N;
+      c->Dx = D;
+      rc = alloc_frame_buffers(c, N);
+    }
+    if (rc) return rc;
+  }
+  c->X = c->Xown;
+  c->N = N;
+  c->Dx = D;
+  c->tcx_valid = false;
+  cudaError_t e = cudaMemsetAsync(c->stats, 0, sizeof(double) * ((size_t)c->M * (1 + 2 * c->D) + 2), c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "cudaMemsetAsync(stats)");
+  c->stats_valid = false;
+  if (c->model_dirty) {
+    const int rc = plain_precompute(c);
+    if (rc) return rc;
+  }
+  const int rc = tc_estep_streamed(c, X, flags, 8);
+  if (rc) return rc;
+  c->tot_frames = c->N;
+  c->acc_flags = flags;
+  c->stats_valid = true;
+  return GMM_OK;
 }
 
 int gmm_read_stats(gmm_handle h, double* n, double* F, double* S, double* tl, long long* tn) {

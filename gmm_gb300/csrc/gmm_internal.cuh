@@ -120,6 +120,10 @@ struct Ctx {
   // full-covariance model (own parameters and statistics; shares the features and scratch)
   FullModel* full = nullptr;
 
+  // host-to-device copies that overlap the E-step (gmm_accumulate_host)
+  cudaStream_t copy_stream = nullptr;
+  std::vector<cudaEvent_t> copy_events;
+
   // --robust: auxiliary statistics of the diagonal model [aux (M x D) | aux2 (M) | aux3 (M)],
   // per-frame gs of a chunk, the previous chunk's last posteriors, independent-frame counts
   bool robust = false;
@@ -179,6 +183,7 @@ int tc_supported(int D);
 int tc_prepare_features(Ctx* c);
 int tc_prepare_model(Ctx* c);
 int tc_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev);
+int tc_estep_streamed(Ctx* c, const float* Xh, int flags, int nchunks);
 
 // One MAP iteration for S speakers against the resident model (the UBM); speaker s owns the
 // resident frames [offs[s], offs[s+1]).

@@ -94,10 +94,11 @@ __device__ __forceinline__ void split3d(double v, uint16_t& a, uint16_t& b, uint
 // plane, and a warp covers 32 consecutive rows of a group (512 contiguous bytes per plane).
 __global__ void features_kernel(const float* __restrict__ X, long long N, long long nT, int D,
                                 int K, const long long* __restrict__ row_frame,
-                                uint16_t* __restrict__ planes) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+                                uint16_t* __restrict__ planes, long long t_begin, long long t_end) {
+  // threads [t_begin, t_end) of the image: whole tiles [t_begin, t_end) / (128 K/8)
+  const long long t = t_begin + (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int KC = K / 8;
-  if (t >= nT * 128 * KC) return;
+  if (t >= t_end) return;
   const int r = (int)(t & 127);
   const long long blk = t >> 7;  // (tile, column group) in image order
   const int c = (int)(blk % KC);
@@ -269,9 +270,10 @@ template <int K>
 __global__ void __launch_bounds__(kLlThreads, 1)
     ll_kernel(const __grid_constant__ CUtensorMap wfull, const uint16_t* __restrict__ zplanes,
               long long N, const long long* __restrict__ row_frame, const int* __restrict__ tile_wbase,
-              int nTz, int nTw, int n_tiles, int n_chunks, float trouble2, float minLL,
+              int nTz, int nTw, int tile0, int n_tiles, int n_chunks, float trouble2, float minLL,
               float* __restrict__ ll2_out, float* __restrict__ ll_out, double* __restrict__ llpart,
               int* __restrict__ err) {
+  // frame tiles tile0 .. tile0 + n_tiles - 1, strided over the CTAs
   using C = LlCfg<K>;
   constexpr int ZB = C::ZB, NW = C::NW;
   extern __shared__ uint8_t smem_raw[];
@@ -330,7 +332,7 @@ __global__ void __launch_bounds__(kLlThreads, 1)
       bool ok = true;
       for (int it = 0; it < my_tiles && ok; ++it) {
         // first W chunk of the tile's model (one model unless a per-tile base is given)
-        const int wbase = tile_wbase ? tile_wbase[(int)blockIdx.x + it * (int)gridDim.x] : 0;
+        const int wbase = tile_wbase ? tile_wbase[tile0 + (int)blockIdx.x + it * (int)gridDim.x] : 0;
         for (int ch = 0; ch < n_chunks; ++ch, ++j) {
           const int ws = j % NW;
           if (!mbar_wait(&w_empty[ws], ((j / NW) & 1) ^ 1, abort_flag, kWaitLimit)) { ok = false; break; }
@@ -389,7 +391,7 @@ __global__ void __launch_bounds__(kLlThreads, 1)
     const uint32_t lane_off = (uint32_t)(q4 * 32) << 16;
     for (int it = 0; it < my_tiles; ++it) {
       const int zb = it % ZB;
-      const int tile = (int)blockIdx.x + it * (int)gridDim.x;
+      const int tile = tile0 + (int)blockIdx.x + it * (int)gridDim.x;
       if (!mbar_wait(&z_empty[zb], ((it / ZB) & 1) ^ 1, abort_flag, kWaitLimit)) break;
       tc_fence_after();
       image_row_to_tmem(zplanes, nTz, K, tile, row, tmem + lane_off + C::Z_COL + zb * C::ZCOLS, tile < nTz);
@@ -409,7 +411,7 @@ __global__ void __launch_bounds__(kLlThreads, 1)
     int j = 0;
     bool ok = true;
     for (int it = 0; it < my_tiles; ++it) {
-      const int tile = (int)blockIdx.x + it * (int)gridDim.x;
+      const int tile = tile0 + (int)blockIdx.x + it * (int)gridDim.x;
       float m = -INFINITY, sum = 0.0f;
       for (int ch = 0; ch < n_chunks && ok; ++ch, ++j) {
         const int b = j & 1;
@@ -947,12 +949,10 @@ int make_map(Ctx* c, CUtensorMap* map, const uint16_t* base, long long total_ele
 }
 
 template <int K>
-int launch_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
+int launch_ll_part(Ctx* c, int tile0, int n_tiles_ll, float* ll_out_dev, bool want_total) {
   using LC = LlCfg<K>;
-  using AC = AccCfg<K>;
   const long long Npad = c->tcx.Npad;
   const int nTz = (int)(Npad / 128), nTw = c->tcm.Mpad / 128;
-  const int n_tiles_ll = nTz;
   const int n_chunks = nTw;
   int grid_ll = std::min(n_tiles_ll, c->sms);
   if (grid_ll < 1) grid_ll = 1;
@@ -964,7 +964,7 @@ int launch_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
     if (rc) return rc;
     c->tc_llpart_cap = need;
   }
-  static bool attr_set_ll = false, attr_set_acc = false;
+  static bool attr_set_ll = false;
   if (!attr_set_ll) {
     cudaFuncSetAttribute(ll_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, LC::SMEM);
     attr_set_ll = true;
@@ -973,15 +973,35 @@ int launch_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
   {
     GMM_LAUNCH(c, "tc_ll_kernel");
     ll_kernel<K><<<grid_ll, kLlThreads, LC::SMEM, c->stream>>>(
-        c->tm_wfull, c->tcx.planes, c->N, nullptr, nullptr, nTz, nTw, n_tiles_ll, n_chunks, trouble2, c->minLL,
-        c->tcm.ll2, ll_out_dev, c->tc_llpart, c->tc_err);
+        c->tm_wfull, c->tcx.planes, c->N, nullptr, nullptr, nTz, nTw, tile0, n_tiles_ll, n_chunks, trouble2,
+        c->minLL, c->tcm.ll2, ll_out_dev, c->tc_llpart, c->tc_err);
   }
-  if (!want_stats) return GMM_OK;
+  if (!want_total) return GMM_OK;
   {
     GMM_LAUNCH(c, "tc_ll_total_kernel");
     ll_total_kernel<<<1, 1024, 0, c->stream>>>(grid_ll * 128, c->tc_llpart,
                                                 c->stats + (size_t)c->M * (1 + 2 * c->D));
   }
+  return GMM_OK;
+}
+
+template <int K>
+int launch_acc_part(Ctx* c, int flags);
+
+template <int K>
+int launch_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
+  const int rc = launch_ll_part<K>(c, 0, (int)(c->tcx.Npad / 128), ll_out_dev, want_stats);
+  if (rc || !want_stats) return rc;
+  return launch_acc_part<K>(c, flags);
+}
+
+template <int K>
+int launch_acc_part(Ctx* c, int flags) {
+  using AC = AccCfg<K>;
+  const long long Npad = c->tcx.Npad;
+  const int nTz = (int)(Npad / 128), nTw = c->tcm.Mpad / 128;
+  const int n_chunks = nTw;
+  static bool attr_set_acc = false;
   const int n_tiles = (int)(Npad / AC::FT);
   // CTAs = component chunks x frame slices, one CTA per SM at a time: `waves` full waves of the
   // SMs (more waves = finer slices, which fill the SMs that a single wave leaves idle, at the
@@ -1076,7 +1096,7 @@ int tc_prepare_features(Ctx* c) {
     GMM_LAUNCH(c, "tc_features_kernel");
     const long long tot = Npad * (K / 8);
     features_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(c->X, c->N, Npad / 128, c->D, K,
-                                                                         nullptr, c->tcx.planes);
+                                                                         nullptr, c->tcx.planes, 0, tot);
   }
   int rc = make_map(c, &c->tm_zfull, c->tcx.planes, 3 * Npad * K, K);
   if (!rc) rc = make_map(c, &c->tm_zhalf, c->tcx.planes, 3 * Npad * K, 4);
@@ -1110,6 +1130,108 @@ int tc_prepare_model(Ctx* c) {
   int rc = make_map(c, &c->tm_wfull, c->tcm.planes, 3LL * Mpad * K, K);
   if (!rc) rc = make_map(c, &c->tm_whalf, c->tcm.planes, 3LL * Mpad * K, 4);
   return rc;
+}
+
+// E-step whose features arrive from the host while it runs: the frames go up in chunks of
+// whole 128-frame tiles on a copy stream, and each chunk's feature planes and log-likelihood
+// tiles start as soon as its copy lands, so the transfer hides behind the logits kernels; the
+// statistics kernel then runs over all tiles. c->X must be the handle's own device buffer of
+// c->N x c->D floats; Xh is the host block (page-locked for the copies to overlap).
+int tc_estep_streamed(Ctx* c, const float* Xh, int flags, int nchunks) {
+  if (!tc_supported(c->D)) return fail(c, GMM_ERR_UNSUPPORTED, "tensor-core path supports 1 <= D <= 63");
+  if (c->N == 0) return GMM_OK;
+  if (!c->tc_err) {
+    int rc = dalloc(c, (void**)&c->tc_err, sizeof(int), "tc error flag");
+    if (rc) return rc;
+    cudaMemsetAsync(c->tc_err, 0, sizeof(int), c->stream);
+    int dev;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, dev);
+  }
+  const int K = tc_K(c->D), KC = K / 8;
+  const long long Npad = (c->N + 127) / 128 * 128;
+  if (c->tcx.planes == nullptr || c->tcx.Npad != Npad || c->tcx.K != K) {
+    dfree(c, c->tcx.planes, (size_t)3 * c->tcx.Npad * c->tcx.K * sizeof(uint16_t));
+    dfree(c, c->tcm.ll2, sizeof(float) * (size_t)c->tcx.Npad);
+    c->tcx.planes = nullptr;
+    c->tcm.ll2 = nullptr;
+    c->tcx.Npad = 0;
+    int rc = dalloc(c, (void**)&c->tcx.planes, (size_t)3 * Npad * K * sizeof(uint16_t), "tensor-core feature planes");
+    if (!rc) rc = dalloc(c, (void**)&c->tcm.ll2, sizeof(float) * (size_t)Npad, "tensor-core frame LSE");
+    if (rc) return rc;
+    c->tcx.Npad = Npad;
+    c->tcx.K = K;
+  }
+  int rc = make_map(c, &c->tm_zfull, c->tcx.planes, 3 * Npad * K, K);
+  if (!rc) rc = make_map(c, &c->tm_zhalf, c->tcx.planes, 3 * Npad * K, 4);
+  if (!rc) rc = tc_prepare_model(c);
+  if (rc) return rc;
+  if (!c->copy_stream) {
+    cudaError_t e = cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamCreate(copy)");
+  }
+  while ((int)c->copy_events.size() < nchunks) {
+    cudaEvent_t ev;
+    cudaError_t e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaEventCreate");
+    c->copy_events.push_back(ev);
+  }
+  // the copies must not overwrite frames a previous E-step on the compute stream still reads
+  cudaEventRecord(c->copy_events[0], c->stream);
+  cudaStreamWaitEvent(c->copy_stream, c->copy_events[0], 0);
+  const int nT = (int)(Npad / 128);
+  const int per = (nT + nchunks - 1) / nchunks;
+  float* X = const_cast<float*>(c->X);
+  for (int k = 0; k < nchunks; ++k) {
+    const int ta = k * per, tb = std::min(nT, ta + per);
+    if (ta >= tb) break;
+    const long long fa = (long long)ta * 128, fb = std::min(c->N, (long long)tb * 128);
+    if (fb > fa) {
+      cudaError_t e = cudaMemcpyAsync(X + fa * c->D, Xh + fa * c->D, sizeof(float) * (size_t)(fb - fa) * c->D,
+                                      cudaMemcpyHostToDevice, c->copy_stream);
+      if (e != cudaSuccess) return cuda_fail(c, e, "cudaMemcpyAsync(feature chunk)");
+    }
+    cudaEventRecord(c->copy_events[k], c->copy_stream);
+    cudaStreamWaitEvent(c->stream, c->copy_events[k], 0);
+    {
+      GMM_LAUNCH(c, "tc_features_kernel");
+      const long long t0 = (long long)ta * 128 * KC, t1 = (long long)tb * 128 * KC;
+      features_kernel<<<(unsigned)((t1 - t0 + 255) / 256), 256, 0, c->stream>>>(c->X, c->N, nT, c->D, K, nullptr,
+                                                                               c->tcx.planes, t0, t1);
+    }
+    switch (K) {
+      case 16: rc = launch_ll_part<16>(c, ta, tb - ta, nullptr, true); break;
+      case 32: rc = launch_ll_part<32>(c, ta, tb - ta, nullptr, true); break;
+      case 48: rc = launch_ll_part<48>(c, ta, tb - ta, nullptr, true); break;
+      case 64: rc = launch_ll_part<64>(c, ta, tb - ta, nullptr, true); break;
+      case 80: rc = launch_ll_part<80>(c, ta, tb - ta, nullptr, true); break;
+      case 96: rc = launch_ll_part<96>(c, ta, tb - ta, nullptr, true); break;
+      case 112: rc = launch_ll_part<112>(c, ta, tb - ta, nullptr, true); break;
+      default: rc = launch_ll_part<128>(c, ta, tb - ta, nullptr, true); break;
+    }
+    if (rc) return rc;
+  }
+  c->tcx_valid = true;
+  switch (K) {
+    case 16: rc = launch_acc_part<16>(c, flags); break;
+    case 32: rc = launch_acc_part<32>(c, flags); break;
+    case 48: rc = launch_acc_part<48>(c, flags); break;
+    case 64: rc = launch_acc_part<64>(c, flags); break;
+    case 80: rc = launch_acc_part<80>(c, flags); break;
+    case 96: rc = launch_acc_part<96>(c, flags); break;
+    case 112: rc = launch_acc_part<112>(c, flags); break;
+    default: rc = launch_acc_part<128>(c, flags); break;
+  }
+  if (rc) return rc;
+  int herr = 0;
+  cudaMemcpyAsync(&herr, c->tc_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  rc = sync(c, "tensor-core E-step");
+  if (rc) return rc;
+  if (herr) {
+    cudaMemsetAsync(c->tc_err, 0, sizeof(int), c->stream);
+    return fail(c, GMM_ERR_TIMEOUT, "tensor-core E-step: a bounded device wait expired");
+  }
+  return GMM_OK;
 }
 
 int tc_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
@@ -1365,7 +1487,7 @@ void run_batch_k(Ctx* c, const TcBatch& b, const CUtensorMap& zfull, const CUten
   {
     GMM_LAUNCH(c, "tc_ll_kernel");
     ll_kernel<K><<<grid_ll, kLlThreads, LC::SMEM, c->stream>>>(
-        *b.wmap, b.zplanes, b.N, b.row_frame, b.tile_wbase, nTz, b.w_chunks_total, nTz, b.n_chunks,
+        *b.wmap, b.zplanes, b.N, b.row_frame, b.tile_wbase, nTz, b.w_chunks_total, 0, nTz, b.n_chunks,
         (float)(c->minLL * kLog2e), c->minLL, b.ll2, b.ll, b.llpart, c->tc_err);
   }
   if (b.n_work > 0) {
@@ -1383,7 +1505,7 @@ int tc_run_batch(Ctx* c, const TcBatch& b) {
   {
     GMM_LAUNCH(c, "tc_features_kernel");
     features_kernel<<<(unsigned)((b.Rpad * (b.K / 8) + 255) / 256), 256, 0, c->stream>>>(
-        b.X, b.N, b.Rpad / 128, b.D, b.K, b.row_frame, b.zplanes);
+        b.X, b.N, b.Rpad / 128, b.D, b.K, b.row_frame, b.zplanes, 0, b.Rpad * (b.K / 8));
   }
   CUtensorMap zfull, zhalf;
   int rc = make_map(c, &zfull, b.zplanes, 3 * b.Rpad * b.K, b.K);

@@ -93,6 +93,13 @@ int gmm_accumulate_device(gmm_handle h, int flags);
 int gmm_read_stats(gmm_handle h, double* n, double* F, double* S, double* tot_loglike,
                    long long* tot_frames);
 
+/* E-step over host features (gmm_upload_features + gmm_accumulate_device in one call): on the
+ * tensor-core path the frames go up in chunks on a copy stream while the logits kernels already
+ * run on the chunks that landed, so the transfer hides behind compute (X should be page-locked
+ * for that); afterwards the features are resident as after gmm_upload_features. Statistics stay
+ * on the device (gmm_read_stats, the M-step entry points). */
+int gmm_accumulate_host(gmm_handle h, int flags, const float* X, long long N, int D);
+
 /* Per-frame log-likelihoods: compVecsLogLikeMT (OL_GMMStatsEstimator.cpp:811-879) /
  * compLogLikes + getLogLikes (CU_GMMStatsEstimator_CUDA.cu:606-643). out: N floats (host). */
 int gmm_loglikes(gmm_handle h, float* out);

@@ -156,3 +156,31 @@ def test_tc_autotune_choice_and_results(glib):
     h.close()
     for k in ("n", "F", "S"):
         assert np.allclose(a[k], b[k], rtol=1e-12, atol=1e-9), k
+
+
+@pytest.mark.parametrize("N", [1000, 300_000])
+def test_accumulate_host_streams_features(glib, N):
+    """gmm_accumulate_host (chunked host-to-device copies overlapping the E-step) gives the same
+    statistics as gmm_upload_features + gmm_accumulate: n, F, S bit-identical (the same
+    statistics kernel over the same planes), total LL within 1e-12 rel (the LL partials are
+    grouped per chunk); the features stay resident for the next E-step."""
+    from gmm_gb300 import synth
+    X, w, mu, var = synth.config_em(5, N, 39, 32, 64)
+    a = glib.Handle(0)
+    a.set_precision(glib.PREC_TC)
+    a.upload_model(w, mu, var)
+    a.upload_features(X)
+    ref = a.accumulate()
+    a.close()
+    b = glib.Handle(0)
+    b.set_precision(glib.PREC_TC)
+    b.upload_model(w, mu, var)
+    b.accumulate_host(X)
+    st = b.read_stats()
+    again = b.accumulate()  # resident features
+    b.close()
+    for k in ("n", "F", "S"):
+        assert np.array_equal(st[k], ref[k]), k
+        assert np.array_equal(again[k], ref[k]), k
+    assert abs(st["totLL"] - ref["totLL"]) <= 1e-12 * abs(ref["totLL"])
+    assert st["totN"] == N
