@@ -246,6 +246,7 @@ __device__ __forceinline__ void image_row_to_tmem(const uint16_t* __restrict__ p
 // W chunks (128 components) stream through an NW-stage shared-memory ring. The MMAs read only W
 // from shared memory (A from TMEM), which leaves shared-memory bandwidth for the TMA ring.
 __host__ __device__ constexpr int cmax(int a, int b) { return a > b ? a : b; }
+__host__ __device__ constexpr int cmin(int a, int b) { return a < b ? a : b; }
 __host__ __device__ constexpr int ll_zb(int K) { return K <= 80 ? 2 : 1; }
 __host__ __device__ constexpr int ll_nw(int K) { return K <= 96 ? 3 : 2; }
 
@@ -517,16 +518,32 @@ struct AccCfg {
   static constexpr int Z_PLANE = FT * K * 2;
   static constexpr int Z_STAGE = 3 * Z_PLANE;
   static constexpr int LL_STAGE = FT * 4;
-  static constexpr int S_COL = 0;               // 2 posterior buffers of FT columns
-  static constexpr int W_COL = 2 * FT;          // W planes, 3 K/2 columns
-  static constexpr int D_COL = (W_COL + 3 * K / 2 + 15) / 16 * 16;  // statistics accumulator
+  // TMEM holds the posterior buffers (NS x FT columns), the W planes (K/2 columns each) and the
+  // statistics accumulators (ND x K columns). Two accumulators let the statistics MMAs of tile
+  // j + 1 queue behind those of tile j before the epilogue has read tile j out, so the tensor
+  // pipe never drains while it waits for a buffer. Where two accumulators do not fit beside
+  // three W planes, W plane 2 (one of the six logits products) moves to shared memory and that
+  // product reads both operands from there. Otherwise one accumulator and as many FT-column
+  // posterior buffers (at most 4) as fit.
+  static constexpr int WC3 = (3 * K / 2 + 15) / 16 * 16;
+  static constexpr bool FIT3 = 2 * FT + WC3 + 2 * K <= 512;
+  static constexpr bool FIT2 = !FIT3 && FT == 128 && 2 * FT + (K + 15) / 16 * 16 + 2 * K <= 512;
+  static constexpr int WT = FIT2 ? 2 : 3;                  // W planes in TMEM
+  static constexpr int ND = (FIT3 || FIT2) ? 2 : 1;         // statistics accumulators
+  static constexpr int NS = ND == 2 ? 2 : cmin(4, (512 - WC3 - K) / FT);  // posterior buffers
+  static constexpr int S_COL = 0;
+  static constexpr int W_COL = NS * FT;
+  static constexpr int D_COL = (W_COL + WT * K / 2 + 15) / 16 * 16;
+  static constexpr int W2_BYTES = WT == 2 ? K * 256 : 0;  // W plane 2 image in shared memory
   static constexpr int OFF_Z = 0;
-  static constexpr int OFF_LL = OFF_Z + NZ * Z_STAGE;
+  static constexpr int OFF_W2 = OFF_Z + NZ * Z_STAGE;
+  static constexpr int OFF_LL = OFF_W2 + W2_BYTES;
   static constexpr int OFF_BAR = OFF_LL + NZ * LL_STAGE;
-  static constexpr int OFF_MISC = OFF_BAR + 24 * 8;
+  static constexpr int OFF_MISC = OFF_BAR + 32 * 8;
   static constexpr int SMEM = cmax(OFF_MISC + 64 + 1024, 120 * 1024);
   static constexpr int FLUSH = 64 * 128 / FT;   // tiles per FP64 flush (8192 frames)
-  static_assert(D_COL + K <= 512, "TMEM budget");
+  static_assert(NS >= 2 && D_COL + ND * K <= 512, "TMEM budget");
+  static_assert(SMEM <= 227 * 1024, "shared memory budget");
 };
 
 template <int K>
@@ -538,19 +555,20 @@ __global__ void __launch_bounds__(kThreads, 1)
                double* __restrict__ part, int* __restrict__ err) {
   if (mact_dev) single_comp = *mact_dev == 1;
   using C = AccCfg<K>;
-  constexpr int FT = C::FT, NZ = C::NZ, FLUSH = C::FLUSH;
+  constexpr int FT = C::FT, NZ = C::NZ, NS = C::NS, ND = C::ND, FLUSH = C::FLUSH;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + C::OFF_BAR);
   uint64_t* w_full = bars + 0;
   uint64_t* z_full = bars + 1;   // [NZ <= 4]
   uint64_t* z_empty = bars + 5;  // [NZ]
-  uint64_t* s_full = bars + 9;   // [2]
-  uint64_t* g_full = bars + 11;  // [2 buffers][2 frame halves]
-  uint64_t* d_full = bars + 15;
-  uint64_t* d_empty = bars + 16;
-  uint64_t* mma_done = bars + 17;   // [2]: one per MMA-issuing thread
-  uint64_t* s_free = bars + 19;     // [2]: the statistics MMAs are done with a posterior buffer
+  uint64_t* s_full = bars + 9;   // [NS <= 4]
+  uint64_t* g_full = bars + 13;  // [NS buffers][2 frame halves]
+  uint64_t* d_full = bars + 21;     // [ND]
+  uint64_t* d_empty = bars + 23;    // [ND]
+  uint64_t* mma_done = bars + 25;   // [2]: one per MMA-issuing thread
+  uint64_t* s_free = bars + 27;     // [NS]: the statistics MMAs are done with a posterior buffer
+  uint64_t* w2_full = bars + 31;    // W plane 2 in shared memory (WT == 2)
   uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(smem + C::OFF_MISC);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + C::OFF_MISC + 8);
   float* ll_s = reinterpret_cast<float*>(smem + C::OFF_LL);
@@ -582,17 +600,19 @@ __global__ void __launch_bounds__(kThreads, 1)
       mbar_init(&z_full[i], 1);
       mbar_init(&z_empty[i], 1);
     }
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < NS; ++i) {
       mbar_init(&s_full[i], 1);
       mbar_init(&g_full[2 * i], 8);
       mbar_init(&g_full[2 * i + 1], 8);
+      mbar_init(&s_free[i], 1);
     }
-    mbar_init(d_full, 1);
-    mbar_init(d_empty, 8);
+    for (int i = 0; i < ND; ++i) {
+      mbar_init(&d_full[i], 1);
+      mbar_init(&d_empty[i], 8);
+    }
+    mbar_init(w2_full, 1);
     mbar_init(&mma_done[0], 1);
     mbar_init(&mma_done[1], 1);
-    mbar_init(&s_free[0], 1);
-    mbar_init(&s_free[1], 1);
     *abort_flag = 0;
     fence_mbar_init();
   }
@@ -608,6 +628,10 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (warp == 0) {
     if (lane == 0 && nt > 0) {
       prefetch_tmap(&zmap);
+      if (C::WT == 2) {  // W plane 2: its image is already the operand layout, one bulk copy
+        mbar_arrive_expect_tx(w2_full, C::W2_BYTES);
+        bulk_load(smem + C::OFF_W2, wplanes + (size_t)(2 * nTw + wchunk) * (K / 8) * 1024, C::W2_BYTES, w2_full);
+      }
       int issued = 0;
       for (int i = 0; i < nt; ++i) {
         const int s = i % NZ;
@@ -622,14 +646,16 @@ __global__ void __launch_bounds__(kThreads, 1)
         bulk_load(ll_s + s * FT, ll2 + (size_t)t * FT, FT * 4, &z_full[s]);
         issued = i + 1;
       }
-      if (*abort_flag)  // drain the copies still in flight
+      if (*abort_flag) {  // drain the copies still in flight
         for (int i = max(0, issued - NZ); i < issued; ++i) mbar_drain(&z_full[i % NZ], (i / NZ) & 1);
+        if (C::WT == 2) mbar_drain(w2_full, 0);
+      }
     }
   } else if (warp == 1 || warp == 10) {
     // Two MMA-issuing threads on different SM sub-partitions: the logits (warp 1) and the
     // statistics (warp 10). Each shares its sub-partition with two busy epilogue warps; split
     // this way each needs half the issue slots. A posterior buffer is reused by the logits of
-    // tile i + 2 only after the statistics of tile i released it (s_free).
+    // tile i + NS only after the statistics of tile i released it (s_free).
     if (lane == 0 && nt > 0) {
       const uint32_t zb0 = smem_u32(smem + C::OFF_Z);
       bool ok = true;
@@ -637,35 +663,38 @@ __global__ void __launch_bounds__(kThreads, 1)
         const uint32_t idesc_l = idesc_bf16(128, FT, false, false);
         const uint32_t wa = tmem + C::W_COL;
         ok = mbar_wait(w_full, 0, abort_flag, kWaitLimit);
+        if (ok && C::WT == 2) ok = mbar_wait(w2_full, 0, abort_flag, kWaitLimit);
+        const uint64_t w2d = smem_desc(smem_u32(smem + C::OFF_W2), 128 * 16, 128);
         for (int i = 0; i < nt && ok; ++i) {
           if (!mbar_wait(&z_full[i % NZ], (i / NZ) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
-          if (i >= 2 && !mbar_wait(&s_free[i & 1], ((i - 2) >> 1) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
+          if (i >= NS && !mbar_wait(&s_free[i % NS], ((i - NS) / NS) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
           tc_fence_after();
           const uint64_t zd = smem_desc(zb0 + (i % NZ) * C::Z_STAGE, FT * 16, 128);
-          const uint32_t d = tmem + C::S_COL + (i & 1) * FT;
+          const uint32_t d = tmem + C::S_COL + (i % NS) * FT;
 #pragma unroll
           for (int pr = 0; pr < 6; ++pr) {
 #pragma unroll
             for (int q = 0; q < K / 16; ++q) {
               const uint64_t bd = desc_add(zd, prod_z(pr) * C::Z_PLANE + q * 2 * FT * 16);
               const uint32_t a = wa + prod_w(pr) * (K / 2) + q * 8;
-              if (pr == 0 && q == 0) mma_ts_c<false>(d, a, bd, idesc_l);
+              if (prod_w(pr) >= C::WT) mma_ss_c<true>(d, desc_add(w2d, q * 2 * 128 * 16), bd, idesc_l);
+              else if (pr == 0 && q == 0) mma_ts_c<false>(d, a, bd, idesc_l);
               else mma_ts_c<true>(d, a, bd, idesc_l);
             }
           }
-          mma_commit(&s_full[i & 1]);
+          mma_commit(&s_full[i % NS]);
         }
         mma_commit(&mma_done[0]);
         mbar_drain(&mma_done[0], 0);
       } else {
         const uint32_t idesc_s = idesc_bf16(128, K, false, true);
-        const uint32_t dcol = tmem + C::D_COL;
         for (int j = 0; j < nt && ok; ++j) {
-          const int b = j & 1;
-          // the tile's operands are in its stage; D2 holds one tile: wait until the epilogue
-          // has read out tile j - 1
+          const int b = j % NS;
+          const uint32_t dcol = tmem + C::D_COL + (j % ND) * K;
+          // the tile's operands are in its stage; an accumulator holds one tile: wait until the
+          // epilogue has read out tile j - ND
           if (!mbar_wait(&z_full[j % NZ], (j / NZ) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
-          if (j > 0 && !mbar_wait(d_empty, (j - 1) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
+          if (j >= ND && !mbar_wait(&d_empty[j % ND], ((j - ND) / ND) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
           const uint32_t gb = tmem + C::S_COL + b * FT;
           // B = Z as [N = K columns] x [K' = frames], MN-major: LBO along frames, SBO along columns
           const uint64_t zd = smem_desc(zb0 + (j % NZ) * C::Z_STAGE, 128, FT * 16);
@@ -674,7 +703,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             // the posteriors of each half of the tile's frames are signalled separately, so the
             // statistics of the first half run while the epilogue converts the second
             if (q % (FT / 32) == 0) {
-              if (!mbar_wait(&g_full[2 * b + q / (FT / 32)], (j >> 1) & 1, abort_flag, kWaitLimit)) {
+              if (!mbar_wait(&g_full[2 * b + q / (FT / 32)], (j / NS) & 1, abort_flag, kWaitLimit)) {
                 ok = false;
                 break;
               }
@@ -695,7 +724,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
           if (!ok) break;
           mma_commit(&z_empty[j % NZ]);
-          mma_commit(d_full);
+          mma_commit(&d_full[j % ND]);
           mma_commit(&s_free[b]);
         }
         mma_commit(&mma_done[1]);
@@ -709,10 +738,11 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int row = q4 * 32 + lane;
     const uint32_t lane_off = (uint32_t)(q4 * 32) << 16;
     // the chunk's W planes into TMEM (A operand of the logits MMA): planes 0-1 by one warp of
-    // the pair, plane 2 by the other
+    // the pair, plane 2 by the other; with two planes in TMEM one each
     {
       const int KC = K / 8;
-      for (int p = (hf ? 2 : 0); p < (hf ? 3 : 2); ++p) {
+      const int p0 = C::WT == 2 ? hf : (hf ? 2 : 0), p1 = C::WT == 2 ? hf + 1 : (hf ? 3 : 2);
+      for (int p = p0; p < p1; ++p) {
         const uint4* src = reinterpret_cast<const uint4*>(wplanes + ((size_t)(p * nTw + wchunk) * KC) * 1024 + (size_t)row * 8);
         for (int c = 0; c < KC; c += 2) {
           const uint4 u0 = __ldg(src + (size_t)c * 128), u1 = __ldg(src + (size_t)(c + 1) * 128);
@@ -738,21 +768,28 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int k = 0; k < KH * 16; ++k) dacc[k] = 0.0f;
     int last_slot = -1;
     auto readout = [&](int t, bool flush, int slot) -> bool {
-      if (!mbar_wait(d_full, t & 1, abort_flag, kWaitLimit)) return false;
+      if (!mbar_wait(&d_full[t % ND], (t / ND) & 1, abort_flag, kWaitLimit)) return false;
       tc_fence_after();
+      const uint32_t dbase = tmem + lane_off + C::D_COL + (t % ND) * K;
+      constexpr int RB = KH <= 3 ? KH : 2;  // loads in flight before each wait
 #pragma unroll
-      for (int cc = 0; cc < KH; ++cc) {
-        if (kc0 + cc < kc1) {
-          uint32_t r[16];
-          tmem_ld16(tmem + lane_off + C::D_COL + 16 * (kc0 + cc), r);
-          tmem_ld_wait();
+      for (int g = 0; g < KH; g += RB) {
+        uint32_t r[RB][16];
 #pragma unroll
-          for (int k = 0; k < 16; ++k) dacc[cc * 16 + k] += __uint_as_float(r[k]);
+        for (int u = 0; u < RB; ++u)
+          if (g + u < KH && kc0 + g + u < kc1) tmem_ld16(dbase + 16 * (kc0 + g + u), r[u]);
+        tmem_ld_wait();
+#pragma unroll
+        for (int u = 0; u < RB; ++u) {
+          if (g + u < KH && kc0 + g + u < kc1) {
+#pragma unroll
+            for (int k = 0; k < 16; ++k) dacc[(g + u) * 16 + k] += __uint_as_float(r[u][k]);
+          }
         }
       }
       tc_fence_before();
       __syncwarp();
-      if (lane == 0) mbar_arrive(d_empty);
+      if (lane == 0) mbar_arrive(&d_empty[t % ND]);
       if (flush) {
         double* mypart = part + ((size_t)slot * n_chunks + chunk) * K * 128 + row;  // [col][row]
         const bool first_flush = slot != last_slot;
@@ -774,13 +811,13 @@ __global__ void __launch_bounds__(kThreads, 1)
     };
     bool ok = true;
     for (int i = 0; i < nt; ++i) {
-      const int b = i & 1;
+      const int b = i % NS;
       // period bookkeeping of the previous tile, before begin(i) moves the run start
       const bool end_prev = i > 0 && per.end(i - 1, FLUSH);
       const int slot_prev = i > 0 ? per.slot_of(i - 1) : 0;
       per.begin(i, FLUSH);
       if (!mbar_wait(&z_full[i % NZ], (i / NZ) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
-      if (!mbar_wait(&s_full[b], (i >> 1) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
+      if (!mbar_wait(&s_full[b], (i / NS) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
       tc_fence_after();
       const float* lls = ll_s + (i % NZ) * FT;
       // pass cc converts 32-frame chunk 2 cc + hf: the two warps of a quadrant finish the first

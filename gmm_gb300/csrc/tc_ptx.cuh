@@ -122,6 +122,17 @@ __device__ __forceinline__ void mma_ss(uint32_t d, uint64_t a, uint64_t b, uint3
       : "memory");
 }
 
+// The same with a compile-time accumulate flag.
+template <bool ACC>
+__device__ __forceinline__ void mma_ss_c(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc) {
+  if (ACC)
+    asm volatile("tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, 1;" ::"r"(d), "l"(a), "l"(b), "r"(idesc)
+                 : "memory");
+  else
+    asm volatile("tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, 0;" ::"r"(d), "l"(a), "l"(b), "r"(idesc)
+                 : "memory");
+}
+
 // D[tmem] (+)= A[tmem] * B[smem desc]
 __device__ __forceinline__ void mma_ts(uint32_t d, uint32_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
   asm volatile(
