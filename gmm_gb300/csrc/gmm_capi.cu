@@ -54,6 +54,21 @@ void dfree(Ctx* c, void* p, size_t bytes) {
   c->allocated = c->allocated >= bytes ? c->allocated - bytes : 0;
 }
 
+int scratch(Ctx* c, int slot, size_t bytes, const char* what, void** out) {
+  Ctx::Scratch& b = c->scratch[slot];
+  if (bytes > b.cap) {
+    cudaStreamSynchronize(c->stream);  // the old buffer may still be read by queued work
+    dfree(c, b.p, b.cap);
+    b.p = nullptr;
+    b.cap = 0;
+    int rc = dalloc(c, &b.p, bytes, what);
+    if (rc) return rc;
+    b.cap = bytes;
+  }
+  *out = bytes ? b.p : nullptr;
+  return GMM_OK;
+}
+
 int sync(Ctx* c, const char* what) {
   cudaError_t e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, what);
@@ -272,6 +287,7 @@ int gmm_destroy(gmm_handle h) {
   dfree(c, c->gs, c->gs_cap * sizeof(float));
   dfree(c, c->gprev, c->gprev_cap * sizeof(float));
   dfree(c, c->nind, c->nind_cap * sizeof(double));
+  for (auto& b : c->scratch) dfree(c, b.p, b.cap);
   free_model(c);
   free_features(c);
   dfree(c, c->logits, c->logits_cap);
@@ -601,13 +617,13 @@ static int map_batch(Ctx* c, int S, const long long* offs, int tau, int upW, int
   long long* d_offs = nullptr;
   float *ow = nullptr, *omu = nullptr, *ovar = nullptr;
   double* oll = nullptr;
-  rc = dalloc(c, (void**)&d_offs, boffs, "speaker offsets");
-  if (!rc) rc = dalloc(c, (void**)&b.aw, bw, "adapted weight scratch");
+  rc = scratch(c, SC_OFFS, boffs, "speaker offsets", (void**)&d_offs);
+  if (!rc) rc = scratch(c, SC_AW, bw, "adapted weight scratch", (void**)&b.aw);
   // device staging for host outputs; weights and log-likelihoods are always computed
-  if (!rc && !(dev_out && w)) rc = dalloc(c, (void**)&ow, bw, "adapted weights");
-  if (!rc && !dev_out && mu) rc = dalloc(c, (void**)&omu, bmu, "adapted means");
-  if (!rc && !dev_out && var) rc = dalloc(c, (void**)&ovar, bmu, "adapted variances");
-  if (!rc && !(dev_out && ll)) rc = dalloc(c, (void**)&oll, bll, "speaker log-likelihoods");
+  if (!rc && !(dev_out && w)) rc = scratch(c, SC_W, bw, "adapted weights", (void**)&ow);
+  if (!rc && !dev_out && mu) rc = scratch(c, SC_MU, bmu, "adapted means", (void**)&omu);
+  if (!rc && !dev_out && var) rc = scratch(c, SC_VAR, bmu, "adapted variances", (void**)&ovar);
+  if (!rc && !(dev_out && ll)) rc = scratch(c, SC_LL, bll, "speaker log-likelihoods", (void**)&oll);
   if (!rc) {
     b.d_offs = d_offs;
     b.w = ow ? ow : w;
@@ -625,12 +641,6 @@ static int map_batch(Ctx* c, int S, const long long* offs, int tau, int upW, int
   }
   if (!rc) rc = sync(c, "gmm_map_batch");
   cudaStreamSynchronize(c->stream);
-  dfree(c, d_offs, boffs);
-  dfree(c, b.aw, bw);
-  dfree(c, ow, bw);
-  dfree(c, omu, bmu);
-  dfree(c, ovar, bmu);
-  dfree(c, oll, bll);
   return rc;
 }
 
@@ -659,11 +669,11 @@ int gmm_mllr_batch(gmm_handle h, int S, const long long* offs, int ubm_init, dou
   int* dst = nullptr;
   float* dmu = nullptr;
   long long* doffs = nullptr;
-  rc = dalloc(c, (void**)&dW, bW, "MLLR transforms");
-  if (!rc) rc = dalloc(c, (void**)&dst, bst, "MLLR status");
-  if (!rc) rc = dalloc(c, (void**)&dll, bll, "speaker log-likelihoods");
-  if (!rc) rc = dalloc(c, (void**)&doffs, boffs, "speaker offsets");
-  if (!rc && mu_out) rc = dalloc(c, (void**)&dmu, bmu, "MLLR adapted means");
+  rc = scratch(c, SC_MLLR_W, bW, "MLLR transforms", (void**)&dW);
+  if (!rc) rc = scratch(c, SC_MLLR_ST, bst, "MLLR status", (void**)&dst);
+  if (!rc) rc = scratch(c, SC_LL, bll, "speaker log-likelihoods", (void**)&dll);
+  if (!rc) rc = scratch(c, SC_OFFS, boffs, "speaker offsets", (void**)&doffs);
+  if (!rc && mu_out) rc = scratch(c, SC_MU, bmu, "MLLR adapted means", (void**)&dmu);
   if (!rc) {
     cudaMemcpyAsync(doffs, offs, boffs, cudaMemcpyHostToDevice, c->stream);
     if (c->precision == GMM_PREC_TC) {
@@ -688,11 +698,6 @@ int gmm_mllr_batch(gmm_handle h, int S, const long long* offs, int ubm_init, dou
     rc = sync(c, "gmm_mllr_batch");
   }
   cudaStreamSynchronize(c->stream);
-  dfree(c, dW, bW);
-  dfree(c, dst, bst);
-  dfree(c, dll, bll);
-  dfree(c, doffs, boffs);
-  dfree(c, dmu, bmu);
   return rc;
 }
 

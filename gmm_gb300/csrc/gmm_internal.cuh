@@ -137,6 +137,15 @@ struct Ctx {
   double* nind = nullptr;
   size_t nind_cap = 0;
 
+  // grow-only device scratch of the batched speaker calls (gmm_map_batch, gmm_mllr_batch):
+  // kept between calls so that a call allocates nothing once the largest batch has been seen;
+  // released by gmm_destroy
+  struct Scratch {
+    void* p = nullptr;
+    size_t cap = 0;
+  };
+  Scratch scratch[24];
+
   // timing
   bool profile = false;
   std::vector<KernelTimer> timers;
@@ -200,6 +209,16 @@ struct MapBatch {
 // Per-speaker statistics from the tensor-core path: FP64 partials of pieces of at most 8192
 // frames, [piece][chunk][K cols][128 rows] (columns x | x^2 | 1, rows = padded active list);
 // speaker s owns pieces [piece0[s], piece0[s] + npieces[s]), summed in piece order.
+// Slots of Ctx::scratch
+enum ScratchSlot {
+  SC_OFFS, SC_AW, SC_W, SC_MU, SC_VAR, SC_LL, SC_ROWMAP, SC_TILESLOT, SC_WORK, SC_PAD, SC_PART,
+  SC_PIECE0, SC_NPIECES, SC_ROWCOMP, SC_MLLR_W, SC_MLLR_ST, SC_MLLR_N, SC_MLLR_F, SC_MLLR_G,
+  SC_MLLR_K, SC_MLLR_B, SC_MLLR_XI, SC_MLLR_GP, SC_MLLR_KP, SC_COUNT
+};
+static_assert(SC_COUNT <= 24, "Ctx::scratch slots");
+// Pointer to at least `bytes` of the slot's buffer (grown, contents not kept, when smaller).
+int scratch(Ctx* c, int slot, size_t bytes, const char* what, void** out);
+
 struct SpeakerStats {
   int S = 0, n_chunks = 0, K = 0, pieces = 0;
   double* part = nullptr;

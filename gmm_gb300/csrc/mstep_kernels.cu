@@ -828,14 +828,14 @@ int mstep_mllr_batch(Ctx* c, int S, const double* plain, const SpeakerStats* ss,
   const size_t bk = sizeof(double) * (size_t)S * D * E, bB = sizeof(float) * (size_t)M * T;
   const size_t bXi = sizeof(float) * (size_t)M * E;
   const size_t bGp = sizeof(double) * (size_t)D * T, bkp = sizeof(double) * (size_t)D * E;
-  int rc = dalloc(c, (void**)&n, bn, "MLLR n");
-  if (!rc) rc = dalloc(c, (void**)&F, bF, "MLLR F");
-  if (!rc) rc = dalloc(c, (void**)&Gd, bG, "MLLR G");
-  if (!rc) rc = dalloc(c, (void**)&kd, bk, "MLLR k");
-  if (!rc) rc = dalloc(c, (void**)&B, bB, "MLLR outer products");
-  if (!rc) rc = dalloc(c, (void**)&Xi, bXi, "MLLR extended means");
-  if (!rc && ubm_init) rc = dalloc(c, (void**)&Gp, bGp, "MLLR prior G");
-  if (!rc && ubm_init) rc = dalloc(c, (void**)&kp, bkp, "MLLR prior k");
+  int rc = scratch(c, SC_MLLR_N, bn, "MLLR n", (void**)&n);
+  if (!rc) rc = scratch(c, SC_MLLR_F, bF, "MLLR F", (void**)&F);
+  if (!rc) rc = scratch(c, SC_MLLR_G, bG, "MLLR G", (void**)&Gd);
+  if (!rc) rc = scratch(c, SC_MLLR_K, bk, "MLLR k", (void**)&kd);
+  if (!rc) rc = scratch(c, SC_MLLR_B, bB, "MLLR outer products", (void**)&B);
+  if (!rc) rc = scratch(c, SC_MLLR_XI, bXi, "MLLR extended means", (void**)&Xi);
+  if (!rc && ubm_init) rc = scratch(c, SC_MLLR_GP, bGp, "MLLR prior G", (void**)&Gp);
+  if (!rc && ubm_init) rc = scratch(c, SC_MLLR_KP, bkp, "MLLR prior k", (void**)&kp);
   const size_t smem = sizeof(double) * (size_t)kSolveWarps * E * (E + 2);
   if (!rc && smem > 200 * 1024) rc = fail(c, GMM_ERR_UNSUPPORTED, "MLLR: D too large for the shared-memory solve");
   if (!rc) {
@@ -887,14 +887,6 @@ int mstep_mllr_batch(Ctx* c, int S, const double* plain, const SpeakerStats* ss,
     }
     rc = sync(c, "batched MLLR");
   }
-  dfree(c, n, bn);
-  dfree(c, F, bF);
-  dfree(c, Gd, bG);
-  dfree(c, kd, bk);
-  dfree(c, B, bB);
-  dfree(c, Xi, bXi);
-  dfree(c, Gp, bGp);
-  dfree(c, kp, bkp);
   return rc;
 }
 

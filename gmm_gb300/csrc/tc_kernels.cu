@@ -938,6 +938,22 @@ __global__ void row_of_comp_kernel(int M, int Mpad, const int* __restrict__ comp
 
 // Per-speaker total log-likelihood: FP64 sum of the speaker's frame log-likelihoods (strided
 // per thread, then a fixed warp and block tree).
+// Padded row r of a speaker batch -> its frame (-1 for the padding rows at a speaker's end):
+// speaker s owns rows [pad[s], pad[s+1]) and frames [offs[s], offs[s+1]).
+__global__ void row_frame_kernel(int S, const long long* __restrict__ pad, const long long* __restrict__ offs,
+                                 long long Rpad, long long* __restrict__ rf) {
+  const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= Rpad) return;
+  int lo = 0, hi = S;  // the last s with pad[s] <= r
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (pad[mid] <= r) lo = mid;
+    else hi = mid;
+  }
+  const long long f = S > 0 ? offs[lo] + (r - pad[lo]) : -1;
+  rf[r] = (S > 0 && f < offs[lo + 1]) ? f : -1;
+}
+
 __global__ void seg_sum_kernel(const long long* __restrict__ offs, const float* __restrict__ ll,
                                double* __restrict__ out) {
   __shared__ double red[32];
@@ -1324,6 +1340,7 @@ int tc_speaker_stats(Ctx* c, int S, const long long* offs, const long long* d_of
                      SpeakerStats* ss) {
   *ss = SpeakerStats();
   if (!tc_supported(c->D)) return fail(c, GMM_ERR_UNSUPPORTED, "tensor-core path supports 1 <= D <= 63");
+  if (!d_offs) return fail(c, GMM_ERR_ARG, "per-speaker statistics: device speaker offsets missing");
   if (!c->tc_err) {
     int rc = dalloc(c, (void**)&c->tc_err, sizeof(int), "tc error flag");
     if (rc) return rc;
@@ -1337,13 +1354,10 @@ int tc_speaker_stats(Ctx* c, int S, const long long* offs, const long long* d_of
   if (rc) return rc;
   const int FT = acc_ft(K), FLUSH = 64 * 128 / FT;
   const int n_chunks = c->tcm.Mpad / 128;
-  // padded row layout and pieces
+  // padded row layout (the row map itself is built on the device) and pieces
   std::vector<long long> pad((size_t)S + 1, 0);
   for (int s = 0; s < S; ++s) pad[s + 1] = pad[s] + (offs[s + 1] - offs[s] + 127) / 128 * 128;
   const long long Rpad = pad[S] > 0 ? pad[S] : 128;
-  std::vector<long long> row_frame((size_t)Rpad, -1);
-  for (int s = 0; s < S; ++s)
-    for (long long f = offs[s]; f < offs[s + 1]; ++f) row_frame[(size_t)(pad[s] + f - offs[s])] = f;
   const long long ntiles = Rpad / FT;
   std::vector<int> tile_slot((size_t)ntiles, 0), piece0((size_t)S, 0), npieces((size_t)S, 0);
   int pieces = 0;
@@ -1377,7 +1391,9 @@ int tc_speaker_stats(Ctx* c, int S, const long long* offs, const long long* d_of
   }
   const size_t rf_bytes = sizeof(long long) * (size_t)Rpad, ts_bytes = sizeof(int) * (size_t)ntiles;
   const size_t wk_bytes = sizeof(int4) * std::max<size_t>(1, work.size());
+  const size_t pad_bytes = sizeof(long long) * ((size_t)S + 1);
   long long* d_rf = nullptr;
+  long long* d_pad = nullptr;
   int* d_ts = nullptr;
   int4* d_wk = nullptr;
   ss->S = S;
@@ -1385,13 +1401,15 @@ int tc_speaker_stats(Ctx* c, int S, const long long* offs, const long long* d_of
   ss->K = K;
   ss->pieces = pieces;
   ss->part_bytes = (size_t)std::max(pieces, 1) * n_chunks * K * 128 * sizeof(double);
-  rc = dalloc(c, (void**)&d_rf, rf_bytes, "row map");
-  if (!rc) rc = dalloc(c, (void**)&d_ts, ts_bytes, "tile slots");
-  if (!rc) rc = dalloc(c, (void**)&d_wk, wk_bytes, "work items");
-  if (!rc) rc = dalloc(c, (void**)&ss->part, ss->part_bytes, "per-speaker statistics");
-  if (!rc) rc = dalloc(c, (void**)&ss->piece0, sizeof(int) * std::max(S, 1), "speaker pieces");
-  if (!rc) rc = dalloc(c, (void**)&ss->npieces, sizeof(int) * std::max(S, 1), "speaker pieces");
-  if (!rc) rc = dalloc(c, (void**)&ss->row_of_comp, sizeof(int) * M, "component rows");
+  // all from the handle's grow-only scratch: nothing is allocated once the largest batch was seen
+  rc = scratch(c, SC_ROWMAP, rf_bytes, "row map", (void**)&d_rf);
+  if (!rc) rc = scratch(c, SC_PAD, pad_bytes, "padded speaker offsets", (void**)&d_pad);
+  if (!rc) rc = scratch(c, SC_TILESLOT, ts_bytes, "tile slots", (void**)&d_ts);
+  if (!rc) rc = scratch(c, SC_WORK, wk_bytes, "work items", (void**)&d_wk);
+  if (!rc) rc = scratch(c, SC_PART, ss->part_bytes, "per-speaker statistics", (void**)&ss->part);
+  if (!rc) rc = scratch(c, SC_PIECE0, sizeof(int) * std::max(S, 1), "speaker pieces", (void**)&ss->piece0);
+  if (!rc) rc = scratch(c, SC_NPIECES, sizeof(int) * std::max(S, 1), "speaker pieces", (void**)&ss->npieces);
+  if (!rc) rc = scratch(c, SC_ROWCOMP, sizeof(int) * M, "component rows", (void**)&ss->row_of_comp);
   if (!rc) {
     // operand planes in the padded layout; the next regular E-step rebuilds its own
     const size_t pbytes = (size_t)3 * Rpad * K * sizeof(uint16_t);
@@ -1419,7 +1437,11 @@ int tc_speaker_stats(Ctx* c, int S, const long long* offs, const long long* d_of
     if (!rc) c->tc_llpart_cap = need;
   }
   if (!rc) {
-    cudaMemcpyAsync(d_rf, row_frame.data(), rf_bytes, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(d_pad, pad.data(), pad_bytes, cudaMemcpyHostToDevice, c->stream);
+    {
+      GMM_LAUNCH(c, "row_frame_kernel");
+      row_frame_kernel<<<(unsigned)((Rpad + 255) / 256), 256, 0, c->stream>>>(S, d_pad, d_offs, Rpad, d_rf);
+    }
     cudaMemcpyAsync(d_ts, tile_slot.data(), ts_bytes, cudaMemcpyHostToDevice, c->stream);
     if (!work.empty()) cudaMemcpyAsync(d_wk, work.data(), work.size() * sizeof(int4), cudaMemcpyHostToDevice, c->stream);
     if (S > 0) {
@@ -1467,20 +1489,12 @@ int tc_speaker_stats(Ctx* c, int S, const long long* offs, const long long* d_of
     }
   }
   cudaStreamSynchronize(c->stream);
-  dfree(c, d_rf, rf_bytes);
-  dfree(c, d_ts, ts_bytes);
-  dfree(c, d_wk, wk_bytes);
   if (rc) tc_free_speaker_stats(c, ss);
   return rc;
 }
 
-void tc_free_speaker_stats(Ctx* c, SpeakerStats* ss) {
-  dfree(c, ss->part, ss->part_bytes);
-  dfree(c, ss->piece0, sizeof(int) * std::max(ss->S, 1));
-  dfree(c, ss->npieces, sizeof(int) * std::max(ss->S, 1));
-  dfree(c, ss->row_of_comp, sizeof(int) * c->M);
-  *ss = SpeakerStats();
-}
+// The buffers belong to the handle's scratch (reused by the next batch).
+void tc_free_speaker_stats(Ctx*, SpeakerStats* ss) { *ss = SpeakerStats(); }
 
 int tc_map_batch(Ctx* c, const MapBatch& b) {
   SpeakerStats ss;
