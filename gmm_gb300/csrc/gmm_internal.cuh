@@ -144,7 +144,7 @@ struct Ctx {
     void* p = nullptr;
     size_t cap = 0;
   };
-  Scratch scratch[24];
+  Scratch scratch[32];
 
   // timing
   bool profile = false;
@@ -213,9 +213,12 @@ struct MapBatch {
 enum ScratchSlot {
   SC_OFFS, SC_AW, SC_W, SC_MU, SC_VAR, SC_LL, SC_ROWMAP, SC_TILESLOT, SC_WORK, SC_PAD, SC_PART,
   SC_PIECE0, SC_NPIECES, SC_ROWCOMP, SC_MLLR_W, SC_MLLR_ST, SC_MLLR_N, SC_MLLR_F, SC_MLLR_G,
-  SC_MLLR_K, SC_MLLR_B, SC_MLLR_XI, SC_MLLR_GP, SC_MLLR_KP, SC_COUNT
+  SC_MLLR_K, SC_MLLR_B, SC_MLLR_XI, SC_MLLR_GP, SC_MLLR_KP, SC_MLLR_AIMG, SC_MLLR_BIMG, SC_MLLR_RVAR,
+  SC_COUNT
 };
-static_assert(SC_COUNT <= 24, "Ctx::scratch slots");
+static_assert(SC_COUNT <= 32, "Ctx::scratch slots");
+// Tensor-core G data term of batched MLLR: d_G [S][D][T] (FP64) from the dense counts d_n [S][M].
+int tc_mllr_g(Ctx* c, int S, const double* d_n, double* d_G);
 // Pointer to at least `bytes` of the slot's buffer (grown, contents not kept, when smaller).
 int scratch(Ctx* c, int slot, size_t bytes, const char* what, void** out);
 

@@ -9,6 +9,7 @@
 #include <math.h>
 
 #include "gmm_internal.cuh"
+#include "dfloat.cuh"
 
 namespace gmm {
 
@@ -573,22 +574,26 @@ __global__ void mllr_prior_kernel(int M, int D, const float* __restrict__ umu, c
   }
 }
 
-// w_i = G_i^-1 k_i per (speaker, row), in FP64: Gaussian elimination without pivoting on the
-// augmented system [G_i | k_i] and back substitution -- the same elimination order as the
-// reference's pivot-free Gauss-Jordan inverse (MATRIX::_Invert_Gen, Matrix4_LMa.cpp:2232-2300)
-// followed by the product with k, without forming the inverse (a third of the work). One warp per
-// (row i, speaker s), lanes over the rows below the pivot; four systems per block.
+// w_i = G_i^-1 k_i per (speaker, row): Gaussian elimination without pivoting on the augmented
+// system [G_i | k_i] and back substitution -- the elimination order of the reference's pivot-free
+// Gauss-Jordan inverse (MATRIX::_Invert_Gen, Matrix4_LMa.cpp:2232-2300) followed by the product
+// with k, without forming the inverse (a third of the work). The arithmetic is double-float
+// (about 2^-48 relative per operation) on the FP32 pipes: the FP64 inputs are split once, the
+// result is returned in FP64. One warp per (row i, speaker s), lanes over the rows below the
+// pivot, then over the rows above it in the column-oriented back substitution; four systems per
+// block. Row stride LD is odd so that the lanes' 8-byte accesses to one column hit distinct banks.
 constexpr int kSolveWarps = 4;
+__host__ __device__ inline int solve_ld(int E) { return (E + 1) | 1; }
 __global__ void mllr_solve_kernel(int S, int D, const double* __restrict__ Gd, const double* __restrict__ kd,
                                   const double* __restrict__ Gp, const double* __restrict__ kp,
                                   const int* __restrict__ status, double* __restrict__ W) {
-  extern __shared__ double sm[];
-  const int E = D + 1, T = E * (E + 1) / 2, LD = E + 2;  // row stride: E columns + k + pad
+  extern __shared__ dfloat smdf[];
+  const int E = D + 1, T = E * (E + 1) / 2, LD = solve_ld(E);  // E columns + k
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const long long sys = (long long)blockIdx.x * kSolveWarps + warp;
   if (sys >= (long long)S * D) return;
   const int s = (int)(sys / D), i = (int)(sys - (long long)s * D);
-  double* A = sm + (size_t)warp * E * LD;
+  dfloat* A = smdf + (size_t)warp * E * LD;
   double* Wr = W + ((size_t)s * D + i) * E;
   if (status[s] != GMM_OK) {
     for (int a = lane; a < E; a += 32) Wr[a] = 0.0;
@@ -599,31 +604,30 @@ __global__ void mllr_solve_kernel(int S, int D, const double* __restrict__ Gd, c
     const int ti = a <= b ? tri_index(a, b, E) : tri_index(b, a, E);
     double g = Gd[((size_t)s * D + i) * T + ti];
     if (Gp) g = __dadd_rn(Gp[(size_t)i * T + ti], g);
-    A[a * LD + b] = g;
+    A[a * LD + b] = df_from_double(g);
   }
   for (int a = lane; a < E; a += 32) {
     double k = kd[((size_t)s * D + i) * E + a];
     if (kp) k = __dadd_rn(kp[(size_t)i * E + a], k);
-    A[a * LD + E] = k;
+    A[a * LD + E] = df_from_double(k);
   }
   __syncwarp();
   for (int k = 0; k < E; ++k) {
-    const double ipiv = __ddiv_rn(1.0, A[k * LD + k]);
+    const dfloat ipiv = df_div(df_make(1.0f), A[k * LD + k]);
     for (int r = k + 1 + lane; r < E; r += 32) {
-      const double f = __dmul_rn(A[r * LD + k], ipiv);
-      for (int c = k + 1; c <= E; ++c) A[r * LD + c] = __dsub_rn(A[r * LD + c], __dmul_rn(f, A[k * LD + c]));
+      const dfloat f = df_mul(A[r * LD + k], ipiv);
+      for (int c = k + 1; c <= E; ++c) A[r * LD + c] = df_sub_mul(A[r * LD + c], f, A[k * LD + c]);
     }
     __syncwarp();
   }
-  if (lane == 0) {
-    for (int r = E - 1; r >= 0; --r) {
-      double v = A[r * LD + E];
-      for (int c = r + 1; c < E; ++c) v = __dsub_rn(v, __dmul_rn(A[r * LD + c], A[c * LD + E]));
-      A[r * LD + E] = __ddiv_rn(v, A[r * LD + r]);
-    }
+  for (int r = E - 1; r >= 0; --r) {
+    if (lane == 0) A[r * LD + E] = df_div(A[r * LD + E], A[r * LD + r]);
+    __syncwarp();
+    const dfloat x = A[r * LD + E];
+    for (int q = lane; q < r; q += 32) A[q * LD + E] = df_sub_mul(A[q * LD + E], A[q * LD + r], x);
+    __syncwarp();
   }
-  __syncwarp();
-  for (int a = lane; a < E; a += 32) Wr[a] = A[a * LD + E];
+  for (int a = lane; a < E; a += 32) Wr[a] = df_to_double(A[a * LD + E]);
 }
 
 // AdaptModelMLLR (OL_ModelAdapt.cpp:1597-1608) for every (speaker, component): mu' = A mu + b.
@@ -836,10 +840,10 @@ int mstep_mllr_batch(Ctx* c, int S, const double* plain, const SpeakerStats* ss,
   if (!rc) rc = scratch(c, SC_MLLR_XI, bXi, "MLLR extended means", (void**)&Xi);
   if (!rc && ubm_init) rc = scratch(c, SC_MLLR_GP, bGp, "MLLR prior G", (void**)&Gp);
   if (!rc && ubm_init) rc = scratch(c, SC_MLLR_KP, bkp, "MLLR prior k", (void**)&kp);
-  const size_t smem = sizeof(double) * (size_t)kSolveWarps * E * (E + 2);
+  const size_t smem = sizeof(dfloat) * (size_t)kSolveWarps * E * solve_ld(E);
   if (!rc && smem > 200 * 1024) rc = fail(c, GMM_ERR_UNSUPPORTED, "MLLR: D too large for the shared-memory solve");
+  const long long tot = (long long)S * M;
   if (!rc) {
-    const long long tot = (long long)S * M;
     {
       GMM_LAUNCH(c, "mllr_gather_kernel");
       mllr_gather_kernel<<<(unsigned)((tot + 7) / 8), 256, 0, c->stream>>>(
@@ -850,7 +854,7 @@ int mstep_mllr_batch(Ctx* c, int S, const double* plain, const SpeakerStats* ss,
       GMM_LAUNCH(c, "mllr_batch_check_kernel");
       mllr_batch_check_kernel<<<(S + 7) / 8, 256, 0, c->stream>>>(S, M, D, n, dstatus);
     }
-    {
+    if (c->precision != GMM_PREC_TC) {
       GMM_LAUNCH(c, "mllr_outer_kernel");
       mllr_outer_kernel<<<(unsigned)(((long long)M * T + 255) / 256), 256, 0, c->stream>>>(M, D, umu, B);
     }
@@ -858,12 +862,17 @@ int mstep_mllr_batch(Ctx* c, int S, const double* plain, const SpeakerStats* ss,
       GMM_LAUNCH(c, "mllr_xi_kernel");
       mllr_xi_kernel<<<(unsigned)(((long long)M * E + 255) / 256), 256, 0, c->stream>>>(M, D, umu, Xi);
     }
-    {
+    if (c->precision == GMM_PREC_TC) {
+      // G data term on the tensor cores (split-bf16 operands, FP32 products)
+      rc = tc_mllr_g(c, S, n, Gd);
+    } else {
       // G data term: coef = n[s][m]
       GMM_LAUNCH(c, "mllr_gemm_kernel");
       dim3 grid((T + 63) / 64, (S + 127) / 128, D);
       mllr_gemm_kernel<<<grid, 256, 0, c->stream>>>(S, M, D, T, n, (long long)M, 1, 0, uvar, B, T, Gd);
     }
+  }
+  if (!rc) {
     {
       // k data term: coef = F[s][m][i]
       GMM_LAUNCH(c, "mllr_gemm_kernel");
@@ -886,6 +895,14 @@ int mstep_mllr_batch(Ctx* c, int S, const double* plain, const SpeakerStats* ss,
       mllr_batch_apply_kernel<<<(unsigned)((tot + 7) / 8), 256, 0, c->stream>>>(S, M, D, umu, dW, dstatus, dmu_out);
     }
     rc = sync(c, "batched MLLR");
+    if (!rc && c->precision == GMM_PREC_TC && c->tc_err) {
+      int herr = 0;
+      cudaMemcpy(&herr, c->tc_err, sizeof(int), cudaMemcpyDeviceToHost);
+      if (herr) {
+        cudaMemset(c->tc_err, 0, sizeof(int));
+        rc = fail(c, GMM_ERR_TIMEOUT, "batched MLLR: a bounded device wait expired");
+      }
+    }
   }
   return rc;
 }

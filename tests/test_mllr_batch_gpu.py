@@ -67,3 +67,33 @@ def test_mllr_batch_single_speaker_close_to_exact_path(glib):
     h.close()
     assert st[0] == glib.OK
     assert np.all(np.abs(W[0] - We) <= 2e-4 * (1 + np.abs(We)))
+
+
+def test_mllr_batch_tc_tiles_match_fp32_path(glib, oracle):
+    """The tensor-core G term over several speaker tiles (140 speakers), component chunks
+    (M = 300: three 128-component accumulator readouts, the last one partial) and column tiles
+    (D = 24: 325 upper-triangle pairs in two tiles of 176) agrees with the FP32 GEMM path and,
+    for a few speakers, with the oracle's FP64 MLLR."""
+    D, M, S = 24, 300, 140
+    lens = [250 + 7 * (s % 11) for s in range(S)]
+    X, offs, ubm = c4_small(D=D, M=M, lens=lens, seed=11)
+    res = {}
+    for prec in ("PREC_FP32", "PREC_TC"):
+        h = glib.Handle(0)
+        h.set_precision(getattr(glib, prec))
+        h.upload_model(*ubm)
+        h.upload_features(X)
+        res[prec] = h.mllr_batch(offs, means=False)
+        h.close()
+    Wf, stf = res["PREC_FP32"][0], res["PREC_FP32"][1]
+    Wt, stt = res["PREC_TC"][0], res["PREC_TC"][1]
+    assert np.array_equal(stf, stt)
+    ok = stf == glib.OK
+    assert ok.sum() > S // 2
+    assert np.all(np.abs(Wt[ok] - Wf[ok]) <= 1e-3 * (1 + np.abs(Wf[ok]))), np.abs(Wt[ok] - Wf[ok]).max()
+    for s in (0, 77, S - 1):
+        if not ok[s]:
+            continue
+        o = oracle.accumulate64(X[offs[s]:offs[s + 1]], *ubm, flags=oracle.ACC_MEAN)
+        oW = oracle.mllr_w(ubm[1], ubm[2], o, ubm_init=False)
+        assert np.all(np.abs(Wt[s] - oW) <= 1e-3 * (1 + np.abs(oW))), (s, np.abs(Wt[s] - oW).max())
