@@ -678,7 +678,7 @@ int gmm_mllr_batch(gmm_handle h, int S, const long long* offs, int ubm_init, dou
     cudaMemcpyAsync(doffs, offs, boffs, cudaMemcpyHostToDevice, c->stream);
     if (c->precision == GMM_PREC_TC) {
       SpeakerStats ss;
-      rc = tc_speaker_stats(c, S, offs, doffs, dll, &ss);
+      rc = tc_speaker_stats(c, S, offs, doffs, dll, false, &ss);  // n and F only
       if (!rc) rc = mstep_mllr_batch(c, S, nullptr, &ss, ubm_init, dW, dst, dmu, nullptr);
       tc_free_speaker_stats(c, &ss);
     } else {

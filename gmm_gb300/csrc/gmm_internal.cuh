@@ -209,6 +209,16 @@ struct MapBatch {
 // Per-speaker statistics from the tensor-core path: FP64 partials of pieces of at most 8192
 // frames, [piece][chunk][K cols][128 rows] (columns x | x^2 | 1, rows = padded active list);
 // speaker s owns pieces [piece0[s], piece0[s] + npieces[s]), summed in piece order.
+// Columns of the tensor-core operand layout [x (D) | 1 | x^2 (D) | 0 ...] (features Z, model W,
+// statistics partials): the first-order statistics and the count lead, so an E-step without
+// second-order statistics multiplies only the first tc_mean_cols(D) columns.
+__host__ __device__ inline int tc_col_one(int D) { return D; }
+__host__ __device__ inline int tc_col_sq(int D, int d) { return D + 1 + d; }
+__host__ __device__ inline int tc_mean_cols(int D) { return (D + 1 + 15) / 16 * 16; }
+// Physical column of statistic e in the order n / F / S used by the plain layout's readers
+// (e < D: F_e, D <= e < 2D: S_(e-D), e = 2D: n).
+__host__ __device__ inline int tc_stat_col(int D, int e) { return e < D ? e : e == 2 * D ? D : e + 1; }
+
 // Slots of Ctx::scratch
 enum ScratchSlot {
   SC_OFFS, SC_AW, SC_W, SC_MU, SC_VAR, SC_LL, SC_ROWMAP, SC_TILESLOT, SC_WORK, SC_PAD, SC_PART,
@@ -231,7 +241,7 @@ struct SpeakerStats {
   size_t part_bytes = 0;
 };
 int tc_speaker_stats(Ctx* c, int S, const long long* offs, const long long* d_offs, double* d_ll,
-                     SpeakerStats* ss);
+                     bool second_order, SpeakerStats* ss);
 void tc_free_speaker_stats(Ctx* c, SpeakerStats* ss);
 // Per-speaker statistics from the plain path: [speaker][n (M) | F (M x D) | S (M x D) | totLL | pad]
 // MAP update for all speakers from either form (exactly one of plain / ss is non-null).
@@ -272,6 +282,7 @@ struct TcBatch {
   const int* tile_slot = nullptr;     // [Rpad / FT] statistics slot of each FT tile
   double* part = nullptr;             // [slots][n_chunks][K][128]
   int single_comp = 0;
+  bool second_order = true;           // S statistics wanted (else only the [x | 1] columns)
 };
 int tc_stats_ft(int K);  // frames per statistics tile for K
 int tc_flush_tiles(int K);  // statistics tiles per FP64 flush

@@ -315,8 +315,8 @@ __global__ void map_batch_kernel(int S, int M, int D, const double* __restrict__
   const float* uv = uvar + (size_t)m * D;
   float* om = omu ? omu + (size_t)t * D : nullptr;
   float* ov = ovar ? ovar + (size_t)t * D : nullptr;
-  // statistic e (columns x | x^2 | 1 of the tensor-core partials, or n / F / S of the plain
-  // layout) of component m for speaker s
+  // statistic e (n / F / S order; columns x | 1 | x^2 of the tensor-core partials) of component
+  // m for speaker s
   const int row = plain ? 0 : row_of_comp[m];
   const double* pst = plain ? plain + (size_t)s * ((size_t)M * (1 + 2 * D) + 2) : nullptr;
   if (plain && m == 0 && lane == 0) ll[s] = pst[(size_t)M * (1 + 2 * D)];
@@ -328,8 +328,9 @@ __global__ void map_batch_kernel(int S, int M, int D, const double* __restrict__
     }
     if (row < 0) return 0.0;  // inactive components were never accumulated
     double v = 0.0;
+    const int col = tc_stat_col(D, e);
     for (int p = 0; p < npieces[s]; ++p) {
-      const double x = part[((size_t)(piece0[s] + p) * n_chunks + row / 128) * K * 128 + (size_t)e * 128 + (row % 128)];
+      const double x = part[((size_t)(piece0[s] + p) * n_chunks + row / 128) * K * 128 + (size_t)col * 128 + (row % 128)];
       v = p == 0 ? x : __dadd_rn(v, x);
     }
     return v;
@@ -407,8 +408,9 @@ __global__ void mllr_gather_kernel(int S, int M, int D, const double* __restrict
     if (plain) return e == 2 * D ? pst[m] : pst[M + (size_t)m * D + e];
     if (row < 0) return 0.0;
     double v = 0.0;
+    const int col = tc_stat_col(D, e);
     for (int p = 0; p < npieces[s]; ++p) {
-      const double x = part[((size_t)(piece0[s] + p) * n_chunks + row / 128) * K * 128 + (size_t)e * 128 + (row % 128)];
+      const double x = part[((size_t)(piece0[s] + p) * n_chunks + row / 128) * K * 128 + (size_t)col * 128 + (row % 128)];
       v = p == 0 ? x : __dadd_rn(v, x);
     }
     return v;

@@ -96,7 +96,7 @@ __global__ void srv_map_kernel(int R, int M, int D, int K, int n_chunks, const i
     }
     return v;
   };
-  const double mp = row >= 0 ? col(2 * D) : 0.0;
+  const double mp = row >= 0 ? col(tc_col_one(D)) : 0.0;
   const bool adapt = uwm != 0.0f && mp > 0.0;
   const unsigned int tot = (unsigned int)req_frames[r];
   const double alfa = adapt ? __ddiv_rn(mp, __dadd_rn(mp, (double)tau)) : 0.0;
@@ -119,7 +119,7 @@ __global__ void srv_map_kernel(int R, int M, int D, int K, int n_chunks, const i
       if (upV) {
         const float second = __fadd_rn(uv[k], __fmul_rn(um[k], um[k]));
         const float msq = __fmul_rn(am, am);
-        const double b1 = __ddiv_rn(__dmul_rn(alfa, col(D + k)), mp);
+        const double b1 = __ddiv_rn(__dmul_rn(alfa, col(tc_col_sq(D, k))), mp);
         const double b2 = __dadd_rn(b1, __dmul_rn(one_m, (double)second));
         av = (float)__dsub_rn(b2, (double)msq);
         if (av < min_var) av = min_var;
@@ -241,6 +241,7 @@ struct Batch {
   double* part = nullptr;
   int4* work = nullptr;
   int n_work = 0;
+  bool second_order = false;  // a MAP request of the batch updates variances
   long long* rx0 = nullptr;
   long long* rn = nullptr;
   double* rll = nullptr;
@@ -397,6 +398,7 @@ bool plan(Server* s, Batch& b) {
       hpar[4 * im + 2] = r->upM;
       hpar[4 * im + 3] = r->upV;
       hmf[im] = r->N;
+      if (r->upV) b.second_order = true;
       ++im;
     }
   }
@@ -458,6 +460,7 @@ int launch(Server* s, Batch& b) {
   t.tile_slot = b.tile_slot;
   t.part = b.part;
   t.single_comp = s->M == 1;
+  t.second_order = b.second_order;
   int rc = tc_run_batch(c, t);
   if (rc) return rc;
   const int R = (int)b.reqs.size();

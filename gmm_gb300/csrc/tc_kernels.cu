@@ -112,8 +112,8 @@ __global__ void features_kernel(const float* __restrict__ X, long long N, long l
     float v = 0.0f;
     if (f >= 0) {
       if (k < D) v = X[f * D + k];
-      else if (k < 2 * D) { const float x = X[f * D + k - D]; v = x * x; }
-      else if (k == 2 * D) v = 1.0f;
+      else if (k == D) v = 1.0f;
+      else if (k <= 2 * D) { const float x = X[f * D + k - D - 1]; v = x * x; }
     }
     split3f(v, a[e], b[e], cc[e]);
   }
@@ -152,8 +152,8 @@ __global__ void model_kernel(int D, int K, int Mact, int Mpad, long long plane_r
     const float* mm = mu + (size_t)m * D;
     const float* vv = var + (size_t)m * D;
     if (k < D) v = kLog2e * (double)mm[k] / (double)vv[k];
-    else if (k < 2 * D) v = -0.5 * kLog2e / (double)vv[k - D];
-    else if (k == 2 * D) {
+    else if (k > D && k <= 2 * D) v = -0.5 * kLog2e / (double)vv[k - D - 1];
+    else if (k == D) {
       // constant of the expanded quadratic: log w - D/2 log 2pi - 1/2 sum log var - 1/2 sum mu^2/var
       double sl = 0.0, q = 0.0;
       for (int d = 0; d < D; ++d) {
@@ -162,7 +162,7 @@ __global__ void model_kernel(int D, int K, int Mact, int Mpad, long long plane_r
       }
       v = kLog2e * (log((double)w[m]) + kMinusLog2Pi * D / 2.0 - 0.5 * sl - 0.5 * q);
     }
-  } else if (k == 2 * D) {
+  } else if (k == D) {
     v = -1e30;
   }
   uint16_t a, b, c;
@@ -546,13 +546,20 @@ struct AccCfg {
   static_assert(SMEM <= 227 * 1024, "shared memory budget");
 };
 
-template <int K>
+// Statistics columns without second-order statistics: the [x | 1] columns rounded up to the MMA
+// granularity. For every D with this K (K = 2D + 1 rounded up to 16) that is the same number.
+__host__ __device__ constexpr int acc_mean_cols(int K) { return ((K - 1) / 2 + 1 + 15) / 16 * 16; }
+
+// SO: second-order statistics wanted. The statistics MMA multiplies and the epilogue reads N2
+// columns: all K, or the leading [x | 1] ones.
+template <int K, bool SO>
 __global__ void __launch_bounds__(kThreads, 1)
     acc_kernel(const __grid_constant__ CUtensorMap zmap, const uint16_t* __restrict__ wplanes,
                int nTz, int nTw, const float* __restrict__ ll2, int n_tiles, int n_chunks, int slices,
                const int* __restrict__ tile_slot, const int4* __restrict__ work, float minGamma,
                int single_comp, const int* __restrict__ mact_dev,
                double* __restrict__ part, int* __restrict__ err) {
+  constexpr int N2 = SO ? K : acc_mean_cols(K);
   if (mact_dev) single_comp = *mact_dev == 1;
   using C = AccCfg<K>;
   constexpr int FT = C::FT, NZ = C::NZ, NS = C::NS, ND = C::ND, FLUSH = C::FLUSH;
@@ -687,7 +694,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         mma_commit(&mma_done[0]);
         mbar_drain(&mma_done[0], 0);
       } else {
-        const uint32_t idesc_s = idesc_bf16(128, K, false, true);
+        const uint32_t idesc_s = idesc_bf16(128, N2, false, true);
         for (int j = 0; j < nt && ok; ++j) {
           const int b = j % NS;
           const uint32_t dcol = tmem + C::D_COL + (j % ND) * K;
@@ -756,7 +763,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (lane == 0) mbar_arrive(w_full);
     }
     constexpr int NCH = FT / 64;         // 32-frame chunks per warp
-    constexpr int KCH = K / 16;          // 16-column chunks of the statistics
+    constexpr int KCH = N2 / 16;         // 16-column chunks of the statistics
     constexpr int KH = (KCH + 1) / 2;    // chunks per warp of a pair
     const int kc0 = hf ? KH : 0, kc1 = hf ? KCH : KH;
     // The statistics MMA leaves one tile's sums in D2. The epilogue reads them one tile late
@@ -906,9 +913,9 @@ __global__ void reduce_kernel(int M, int D, int K, int Mact, int n_chunks, int s
     s += part[(((size_t)sl * n_chunks + ch) * K + e) * 128 + rr];
   }
   const int m = comp_of_row[r];
-  if (e == 2 * D) stats[m] += s;
+  if (e == D) stats[m] += s;
   else if (e < D) { if (flags & GMM_ACC_MEAN) stats[(size_t)M + (size_t)m * D + e] += s; }
-  else if (flags & GMM_ACC_VAR) stats[(size_t)M + (size_t)M * D + (size_t)m * D + (e - D)] += s;
+  else if (flags & GMM_ACC_VAR) stats[(size_t)M + (size_t)M * D + (size_t)m * D + (e - D - 1)] += s;
 }
 
 __global__ void ll_total_kernel(int n, const double* __restrict__ llpart, double* __restrict__ tot) {
@@ -1070,12 +1077,15 @@ int launch_acc_part(Ctx* c, int flags) {
     c->tcpart_cap = pneed;
   }
   if (!attr_set_acc) {
-    cudaFuncSetAttribute(acc_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, AC::SMEM);
+    cudaFuncSetAttribute(acc_kernel<K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, AC::SMEM);
+    cudaFuncSetAttribute(acc_kernel<K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, AC::SMEM);
     attr_set_acc = true;
   }
   const CUtensorMap& zm = AC::FT == 128 ? c->tm_zfull : c->tm_zhalf;
+  const bool so = (flags & GMM_ACC_VAR) != 0;  // second-order statistics
   auto launch_acc = [&](int sl) {
-    acc_kernel<K><<<n_chunks * sl, kThreads, AC::SMEM, c->stream>>>(
+    auto kern = so ? acc_kernel<K, true> : acc_kernel<K, false>;
+    kern<<<n_chunks * sl, kThreads, AC::SMEM, c->stream>>>(
         zm, c->tcm.planes, nTz, nTw, c->tcm.ll2, n_tiles, n_chunks, sl, nullptr, nullptr,
         c->minGamma, c->Mact == 1, c->static_shapes ? c->flag + 4 : nullptr, c->tcpart, c->tc_err);
   };
@@ -1083,7 +1093,7 @@ int launch_acc_part(Ctx* c, int flags) {
   {
     int tb = 0;
     while ((1LL << (tb + 1)) <= n_tiles) ++tb;  // frame-tile bucket: power of two
-    const long long key = ((long long)K << 40) | ((long long)n_chunks << 20) | tb;
+    const long long key = ((long long)so << 62) | ((long long)K << 40) | ((long long)n_chunks << 20) | tb;
     auto it = c->tuned_waves.find(key);
     if (it != c->tuned_waves.end()) {
       waves = it->second;
@@ -1337,7 +1347,7 @@ int tc_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
 // its own FP64 slot, and the statistics kernel runs over work items (component chunk x range of
 // whole pieces) of about equal size. A speaker's sums are the piece slots added in piece order.
 int tc_speaker_stats(Ctx* c, int S, const long long* offs, const long long* d_offs, double* d_ll,
-                     SpeakerStats* ss) {
+                     bool second_order, SpeakerStats* ss) {
   *ss = SpeakerStats();
   if (!tc_supported(c->D)) return fail(c, GMM_ERR_UNSUPPORTED, "tensor-core path supports 1 <= D <= 63");
   if (!d_offs) return fail(c, GMM_ERR_ARG, "per-speaker statistics: device speaker offsets missing");
@@ -1469,6 +1479,7 @@ int tc_speaker_stats(Ctx* c, int S, const long long* offs, const long long* d_of
     t.tile_slot = d_ts;
     t.part = ss->part;
     t.single_comp = c->Mact == 1;
+    t.second_order = second_order;
     rc = tc_run_batch(c, t);
   }
   if (!rc) {
@@ -1498,7 +1509,7 @@ void tc_free_speaker_stats(Ctx*, SpeakerStats* ss) { *ss = SpeakerStats(); }
 
 int tc_map_batch(Ctx* c, const MapBatch& b) {
   SpeakerStats ss;
-  int rc = tc_speaker_stats(c, b.S, b.offs, b.d_offs, b.ll, &ss);
+  int rc = tc_speaker_stats(c, b.S, b.offs, b.d_offs, b.ll, b.upV != 0, &ss);
   if (rc) return rc;
   rc = mstep_map_batch(c, b, nullptr, &ss);
   if (!rc) rc = sync(c, "batched MAP update");
@@ -1534,7 +1545,8 @@ void run_batch_k(Ctx* c, const TcBatch& b, const CUtensorMap& zfull, const CUten
   const int nTz = (int)(b.Rpad / 128);
   const int grid_ll = std::max(1, std::min(nTz, c->sms));
   cudaFuncSetAttribute(ll_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, LC::SMEM);
-  cudaFuncSetAttribute(acc_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, AC::SMEM);
+  cudaFuncSetAttribute(acc_kernel<K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, AC::SMEM);
+  cudaFuncSetAttribute(acc_kernel<K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, AC::SMEM);
   {
     GMM_LAUNCH(c, "tc_ll_kernel");
     ll_kernel<K><<<grid_ll, kLlThreads, LC::SMEM, c->stream>>>(
@@ -1544,7 +1556,8 @@ void run_batch_k(Ctx* c, const TcBatch& b, const CUtensorMap& zfull, const CUten
   if (b.n_work > 0) {
     GMM_LAUNCH(c, "tc_acc_kernel");
     const CUtensorMap& zm = AC::FT == 128 ? zfull : zhalf;
-    acc_kernel<K><<<b.n_work, kThreads, AC::SMEM, c->stream>>>(
+    auto kern = b.second_order ? acc_kernel<K, true> : acc_kernel<K, false>;
+    kern<<<b.n_work, kThreads, AC::SMEM, c->stream>>>(
         zm, b.wplanes, nTz, b.w_chunks_total, b.ll2, (int)(b.Rpad / AC::FT), b.n_chunks, 1, b.tile_slot,
         b.work, c->minGamma, b.single_comp, nullptr, b.part, c->tc_err);
   }
