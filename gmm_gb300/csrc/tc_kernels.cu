@@ -509,32 +509,42 @@ struct Periods {
 // stream through an NZ-stage shared-memory ring; posteriors go from the logits accumulator into
 // TMEM in place and feed the statistics MMA; one statistics accumulator, flushed to FP64
 // partials every FLUSH tiles.
-__host__ __device__ constexpr int acc_ft(int K) { return K <= 96 ? 128 : 64; }
-__host__ __device__ constexpr int acc_nz(int K) { return K <= 96 ? 3 : 4; }
+__host__ __device__ constexpr int acc_ft(int) { return 128; }
 
-template <int K>
+// Statistics columns without second-order statistics: the [x | 1] columns rounded up to the MMA
+// granularity. For every D with this K (K = 2D + 1 rounded up to 16) that is the same number.
+__host__ __device__ constexpr int acc_mean_cols(int K) { return ((K - 1) / 2 + 1 + 15) / 16 * 16; }
+
+// Resources of the statistics kernel for K and SO (second-order statistics wanted). Tiles are
+// FT = 128 frames: a tcgen05.mma with M = 128 and K = 16 costs max(45.5, N / 2) cycles on GB300
+// (measured), so the logits MMA (N = frames) reaches the full rate only from N = 96 on; 64-frame
+// tiles would cost the logits 42% more. TMEM holds two 128-column posterior buffers, the W planes
+// (K/2 columns each) and ND statistics accumulators of N2 columns. Two accumulators let the
+// statistics MMAs of tile j + 1 queue behind those of tile j before the epilogue has read tile j
+// out; W plane 2 (one of the six logits products) moves to shared memory, where that product
+// reads both operands, when that makes room. Plans in order of preference: (3 W planes in TMEM,
+// 2 accumulators), (2, 2), (3, 1), (2, 1). The Z ring takes as many stages (2 or 3) as the
+// shared memory left holds.
+template <int K, bool SO>
 struct AccCfg {
-  static constexpr int FT = acc_ft(K), NZ = acc_nz(K);
+  static constexpr int FT = 128;
+  static constexpr int N2 = SO ? K : acc_mean_cols(K);
   static constexpr int Z_PLANE = FT * K * 2;
   static constexpr int Z_STAGE = 3 * Z_PLANE;
   static constexpr int LL_STAGE = FT * 4;
-  // TMEM holds the posterior buffers (NS x FT columns), the W planes (K/2 columns each) and the
-  // statistics accumulators (ND x K columns). Two accumulators let the statistics MMAs of tile
-  // j + 1 queue behind those of tile j before the epilogue has read tile j out, so the tensor
-  // pipe never drains while it waits for a buffer. Where two accumulators do not fit beside
-  // three W planes, W plane 2 (one of the six logits products) moves to shared memory and that
-  // product reads both operands from there. Otherwise one accumulator and as many FT-column
-  // posterior buffers (at most 4) as fit.
-  static constexpr int WC3 = (3 * K / 2 + 15) / 16 * 16;
-  static constexpr bool FIT3 = 2 * FT + WC3 + 2 * K <= 512;
-  static constexpr bool FIT2 = !FIT3 && FT == 128 && 2 * FT + (K + 15) / 16 * 16 + 2 * K <= 512;
-  static constexpr int WT = FIT2 ? 2 : 3;                  // W planes in TMEM
-  static constexpr int ND = (FIT3 || FIT2) ? 2 : 1;         // statistics accumulators
-  static constexpr int NS = ND == 2 ? 2 : cmin(4, (512 - WC3 - K) / FT);  // posterior buffers
+  static constexpr int WC3 = (3 * K / 2 + 15) / 16 * 16, WC2 = (K + 15) / 16 * 16;
+  static constexpr bool P1 = 2 * FT + WC3 + 2 * N2 <= 512;
+  static constexpr bool P2 = !P1 && 2 * FT + WC2 + 2 * N2 <= 512;
+  static constexpr bool P3 = !P1 && !P2 && 2 * FT + WC3 + N2 <= 512;
+  static constexpr int WT = (P1 || P3) ? 3 : 2;   // W planes in TMEM
+  static constexpr int ND = (P1 || P2) ? 2 : 1;   // statistics accumulators
+  static constexpr int NS = 2;                    // posterior buffers
   static constexpr int S_COL = 0;
   static constexpr int W_COL = NS * FT;
   static constexpr int D_COL = (W_COL + WT * K / 2 + 15) / 16 * 16;
   static constexpr int W2_BYTES = WT == 2 ? K * 256 : 0;  // W plane 2 image in shared memory
+  static constexpr int FIXED = W2_BYTES + 32 * 8 + 64 + 1024;
+  static constexpr int NZ = cmin(3, (227 * 1024 - FIXED) / (Z_STAGE + LL_STAGE));
   static constexpr int OFF_Z = 0;
   static constexpr int OFF_W2 = OFF_Z + NZ * Z_STAGE;
   static constexpr int OFF_LL = OFF_W2 + W2_BYTES;
@@ -542,13 +552,10 @@ struct AccCfg {
   static constexpr int OFF_MISC = OFF_BAR + 32 * 8;
   static constexpr int SMEM = cmax(OFF_MISC + 64 + 1024, 120 * 1024);
   static constexpr int FLUSH = 64 * 128 / FT;   // tiles per FP64 flush (8192 frames)
-  static_assert(NS >= 2 && D_COL + ND * K <= 512, "TMEM budget");
+  static_assert(NZ >= 2 && NZ <= 4, "Z ring");
+  static_assert(D_COL + ND * N2 <= 512, "TMEM budget");
   static_assert(SMEM <= 227 * 1024, "shared memory budget");
 };
-
-// Statistics columns without second-order statistics: the [x | 1] columns rounded up to the MMA
-// granularity. For every D with this K (K = 2D + 1 rounded up to 16) that is the same number.
-__host__ __device__ constexpr int acc_mean_cols(int K) { return ((K - 1) / 2 + 1 + 15) / 16 * 16; }
 
 // SO: second-order statistics wanted. The statistics MMA multiplies and the epilogue reads N2
 // columns: all K, or the leading [x | 1] ones.
@@ -559,10 +566,9 @@ __global__ void __launch_bounds__(kThreads, 1)
                const int* __restrict__ tile_slot, const int4* __restrict__ work, float minGamma,
                int single_comp, const int* __restrict__ mact_dev,
                double* __restrict__ part, int* __restrict__ err) {
-  constexpr int N2 = SO ? K : acc_mean_cols(K);
   if (mact_dev) single_comp = *mact_dev == 1;
-  using C = AccCfg<K>;
-  constexpr int FT = C::FT, NZ = C::NZ, NS = C::NS, ND = C::ND, FLUSH = C::FLUSH;
+  using C = AccCfg<K, SO>;
+  constexpr int FT = C::FT, NZ = C::NZ, NS = C::NS, ND = C::ND, N2 = C::N2, FLUSH = C::FLUSH;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + C::OFF_BAR);
@@ -697,7 +703,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         const uint32_t idesc_s = idesc_bf16(128, N2, false, true);
         for (int j = 0; j < nt && ok; ++j) {
           const int b = j % NS;
-          const uint32_t dcol = tmem + C::D_COL + (j % ND) * K;
+          const uint32_t dcol = tmem + C::D_COL + (j % ND) * N2;
           // the tile's operands are in its stage; an accumulator holds one tile: wait until the
           // epilogue has read out tile j - ND
           if (!mbar_wait(&z_full[j % NZ], (j / NZ) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
@@ -777,7 +783,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     auto readout = [&](int t, bool flush, int slot) -> bool {
       if (!mbar_wait(&d_full[t % ND], (t / ND) & 1, abort_flag, kWaitLimit)) return false;
       tc_fence_after();
-      const uint32_t dbase = tmem + lane_off + C::D_COL + (t % ND) * K;
+      const uint32_t dbase = tmem + lane_off + C::D_COL + (t % ND) * N2;
       constexpr int RB = KH <= 3 ? KH : 2;  // loads in flight before each wait
 #pragma unroll
       for (int g = 0; g < KH; g += RB) {
@@ -1057,7 +1063,8 @@ int launch_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
 
 template <int K>
 int launch_acc_part(Ctx* c, int flags) {
-  using AC = AccCfg<K>;
+  using AC = AccCfg<K, true>;   // FT is the same for both statistics widths
+  using ACm = AccCfg<K, false>;
   const long long Npad = c->tcx.Npad;
   const int nTz = (int)(Npad / 128), nTw = c->tcm.Mpad / 128;
   const int n_chunks = nTw;
@@ -1078,14 +1085,14 @@ int launch_acc_part(Ctx* c, int flags) {
   }
   if (!attr_set_acc) {
     cudaFuncSetAttribute(acc_kernel<K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, AC::SMEM);
-    cudaFuncSetAttribute(acc_kernel<K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, AC::SMEM);
+    cudaFuncSetAttribute(acc_kernel<K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, ACm::SMEM);
     attr_set_acc = true;
   }
   const CUtensorMap& zm = AC::FT == 128 ? c->tm_zfull : c->tm_zhalf;
   const bool so = (flags & GMM_ACC_VAR) != 0;  // second-order statistics
   auto launch_acc = [&](int sl) {
     auto kern = so ? acc_kernel<K, true> : acc_kernel<K, false>;
-    kern<<<n_chunks * sl, kThreads, AC::SMEM, c->stream>>>(
+    kern<<<n_chunks * sl, kThreads, so ? AC::SMEM : ACm::SMEM, c->stream>>>(
         zm, c->tcm.planes, nTz, nTw, c->tcm.ll2, n_tiles, n_chunks, sl, nullptr, nullptr,
         c->minGamma, c->Mact == 1, c->static_shapes ? c->flag + 4 : nullptr, c->tcpart, c->tc_err);
   };
@@ -1541,12 +1548,13 @@ namespace {
 template <int K>
 void run_batch_k(Ctx* c, const TcBatch& b, const CUtensorMap& zfull, const CUtensorMap& zhalf) {
   using LC = LlCfg<K>;
-  using AC = AccCfg<K>;
+  using AC = AccCfg<K, true>;
+  using ACm = AccCfg<K, false>;
   const int nTz = (int)(b.Rpad / 128);
   const int grid_ll = std::max(1, std::min(nTz, c->sms));
   cudaFuncSetAttribute(ll_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, LC::SMEM);
   cudaFuncSetAttribute(acc_kernel<K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, AC::SMEM);
-  cudaFuncSetAttribute(acc_kernel<K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, AC::SMEM);
+  cudaFuncSetAttribute(acc_kernel<K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, ACm::SMEM);
   {
     GMM_LAUNCH(c, "tc_ll_kernel");
     ll_kernel<K><<<grid_ll, kLlThreads, LC::SMEM, c->stream>>>(
@@ -1557,7 +1565,7 @@ void run_batch_k(Ctx* c, const TcBatch& b, const CUtensorMap& zfull, const CUten
     GMM_LAUNCH(c, "tc_acc_kernel");
     const CUtensorMap& zm = AC::FT == 128 ? zfull : zhalf;
     auto kern = b.second_order ? acc_kernel<K, true> : acc_kernel<K, false>;
-    kern<<<b.n_work, kThreads, AC::SMEM, c->stream>>>(
+    kern<<<b.n_work, kThreads, b.second_order ? AC::SMEM : ACm::SMEM, c->stream>>>(
         zm, b.wplanes, nTz, b.w_chunks_total, b.ll2, (int)(b.Rpad / AC::FT), b.n_chunks, 1, b.tile_slot,
         b.work, c->minGamma, b.single_comp, nullptr, b.part, c->tc_err);
   }
