@@ -770,7 +770,10 @@ def main():
     # same workload, scaled by the frames a launch processes (the operand planes are read once)
     traffic = None
     if args.workload == "ubm-em" and name == "tc_acc_kernel" and args.dim == 39 and args.mix == 2048:
-        traffic = 503.2 * wl.N  # 503.2 MB per 1M frames: profiles/acc_kernel_ubm_em_1Mx2048x39.md
+        # reads 509.5 MB per 1M frames (operand planes + frame LSE, scaled by N) and the FP64
+        # partial write-back, 39.1 MB at 1M frames (it does not grow with N):
+        # profiles/acc_kernel_ubm_em_1Mx2048x39.md
+        traffic = 509.5 * wl.N + 39.1e6
     peak_source = f"{peak_kind} (bf16 sustained, MEASURED_PEAKS.json)"
     bound = getattr(wl, "bound", "tensor")
     if bound == "fp32":  # SIMT FP32 kernels: nominal FMA rate (no measured FP32 peak in the file)
