@@ -209,15 +209,17 @@ struct MapBatch {
 // Per-speaker statistics from the tensor-core path: FP64 partials of pieces of at most 8192
 // frames, [piece][chunk][K cols][128 rows] (columns x | x^2 | 1, rows = padded active list);
 // speaker s owns pieces [piece0[s], piece0[s] + npieces[s]), summed in piece order.
-// Columns of the tensor-core operand layout [x (D) | 1 | x^2 (D) | 0 ...] (features Z, model W,
-// statistics partials): the first-order statistics and the count lead, so an E-step without
-// second-order statistics multiplies only the first tc_mean_cols(D) columns.
+// Columns of the tensor-core operand layout (features Z, model W, statistics partials) of width
+// K = 2D + 1 rounded up to 16 (so K >= 2D + 2): x_d at d, the constant at D, x_d^2 at K/2 + d,
+// zeros elsewhere. The first-order statistics and the count lead, so an E-step without
+// second-order statistics multiplies only the first tc_mean_cols(D) columns; the squares start at
+// a column fixed by K, so code specialised on K addresses them with constant offsets.
 __host__ __device__ inline int tc_col_one(int D) { return D; }
-__host__ __device__ inline int tc_col_sq(int D, int d) { return D + 1 + d; }
+__host__ __device__ inline int tc_col_sq(int K, int d) { return K / 2 + d; }
 __host__ __device__ inline int tc_mean_cols(int D) { return (D + 1 + 15) / 16 * 16; }
 // Physical column of statistic e in the order n / F / S used by the plain layout's readers
 // (e < D: F_e, D <= e < 2D: S_(e-D), e = 2D: n).
-__host__ __device__ inline int tc_stat_col(int D, int e) { return e < D ? e : e == 2 * D ? D : e + 1; }
+__host__ __device__ inline int tc_stat_col(int D, int K, int e) { return e < D ? e : e == 2 * D ? D : K / 2 + (e - D); }
 
 // Slots of Ctx::scratch
 enum ScratchSlot {

@@ -328,7 +328,7 @@ __global__ void map_batch_kernel(int S, int M, int D, const double* __restrict__
     }
     if (row < 0) return 0.0;  // inactive components were never accumulated
     double v = 0.0;
-    const int col = tc_stat_col(D, e);
+    const int col = tc_stat_col(D, K, e);
     for (int p = 0; p < npieces[s]; ++p) {
       const double x = part[((size_t)(piece0[s] + p) * n_chunks + row / 128) * K * 128 + (size_t)col * 128 + (row % 128)];
       v = p == 0 ? x : __dadd_rn(v, x);
@@ -408,7 +408,7 @@ __global__ void mllr_gather_kernel(int S, int M, int D, const double* __restrict
     if (plain) return e == 2 * D ? pst[m] : pst[M + (size_t)m * D + e];
     if (row < 0) return 0.0;
     double v = 0.0;
-    const int col = tc_stat_col(D, e);
+    const int col = tc_stat_col(D, K, e);
     for (int p = 0; p < npieces[s]; ++p) {
       const double x = part[((size_t)(piece0[s] + p) * n_chunks + row / 128) * K * 128 + (size_t)col * 128 + (row % 128)];
       v = p == 0 ? x : __dadd_rn(v, x);

@@ -119,7 +119,7 @@ __global__ void srv_map_kernel(int R, int M, int D, int K, int n_chunks, const i
       if (upV) {
         const float second = __fadd_rn(uv[k], __fmul_rn(um[k], um[k]));
         const float msq = __fmul_rn(am, am);
-        const double b1 = __ddiv_rn(__dmul_rn(alfa, col(tc_col_sq(D, k))), mp);
+        const double b1 = __ddiv_rn(__dmul_rn(alfa, col(tc_col_sq(K, k))), mp);
         const double b2 = __dadd_rn(b1, __dmul_rn(one_m, (double)second));
         av = (float)__dsub_rn(b2, (double)msq);
         if (av < min_var) av = min_var;

@@ -88,14 +88,26 @@ __device__ __forceinline__ void split3d(double v, uint16_t& a, uint16_t& b, uint
 }
 
 // Z planes as tile images: element (row f, column k) of plane p sits at
-// ((p * nT + f / 128) * K/8 + k / 8) * 1024 + (f % 128) * 8 + k % 8; row f = [x, x^2, 1, 0...]
-// of frame row_frame[f] (identity when row_frame is null), zero for padding rows (past N, or
-// row_frame < 0). One thread per 8-column group of a row: it writes one 16-byte chunk per
-// plane, and a warp covers 32 consecutive rows of a group (512 contiguous bytes per plane).
+// ((p * nT + f / 128) * K/8 + k / 8) * 1024 + (f % 128) * 8 + k % 8; row f holds the operand
+// columns (x at d, 1 at D, x^2 at K/2 + d) of frame row_frame[f] (identity when row_frame is
+// null), zero for padding rows (past N, or row_frame < 0). For K <= 80 the logits kernel's loader
+// warps build them on their first pass over the frames (features_row_to_tmem, hidden behind the
+// MMAs of the previous tile); for larger K, where TMEM holds one Z tile only, features_kernel
+// does it beforehand: one thread per 8-column group of a row, one 16-byte chunk per plane, a warp
+// covering 32 consecutive rows of a group (512 contiguous bytes per plane).
+__device__ __forceinline__ float zcol(const float* __restrict__ xr, int D, int K, int k) {
+  if (k < D) return xr[k];
+  if (k == D) return 1.0f;
+  if (k >= K / 2 && k < K / 2 + D) {
+    const float x = xr[k - K / 2];
+    return __fmul_rn(x, x);
+  }
+  return 0.0f;
+}
+
 __global__ void features_kernel(const float* __restrict__ X, long long N, long long nT, int D,
                                 int K, const long long* __restrict__ row_frame,
                                 uint16_t* __restrict__ planes, long long t_begin, long long t_end) {
-  // threads [t_begin, t_end) of the image: whole tiles [t_begin, t_end) / (128 K/8)
   const long long t = t_begin + (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int KC = K / 8;
   if (t >= t_end) return;
@@ -107,16 +119,7 @@ __global__ void features_kernel(const float* __restrict__ X, long long N, long l
   const long long f = row_frame ? row_frame[row] : (row < N ? row : -1);
   uint16_t a[8], b[8], cc[8];
 #pragma unroll
-  for (int e = 0; e < 8; ++e) {
-    const int k = c * 8 + e;
-    float v = 0.0f;
-    if (f >= 0) {
-      if (k < D) v = X[f * D + k];
-      else if (k == D) v = 1.0f;
-      else if (k <= 2 * D) { const float x = X[f * D + k - D - 1]; v = x * x; }
-    }
-    split3f(v, a[e], b[e], cc[e]);
-  }
+  for (int e = 0; e < 8; ++e) split3f(f >= 0 ? zcol(X + f * D, D, K, c * 8 + e) : 0.0f, a[e], b[e], cc[e]);
   const size_t plane = (size_t)nT * 128 * K;
   const size_t off = (size_t)t * 8;  // == (T * KC + c) * 1024 + r * 8
   auto pack = [](const uint16_t* h) {
@@ -152,7 +155,7 @@ __global__ void model_kernel(int D, int K, int Mact, int Mpad, long long plane_r
     const float* mm = mu + (size_t)m * D;
     const float* vv = var + (size_t)m * D;
     if (k < D) v = kLog2e * (double)mm[k] / (double)vv[k];
-    else if (k > D && k <= 2 * D) v = -0.5 * kLog2e / (double)vv[k - D - 1];
+    else if (k >= K / 2 && k < K / 2 + D) v = -0.5 * kLog2e / (double)vv[k - K / 2];
     else if (k == D) {
       // constant of the expanded quadratic: log w - D/2 log 2pi - 1/2 sum log var - 1/2 sum mu^2/var
       double sl = 0.0, q = 0.0;
@@ -240,6 +243,56 @@ __device__ __forceinline__ void image_row_to_tmem(const uint16_t* __restrict__ p
   }
 }
 
+// Row `r` of tile `tile` built from the raw features instead (K <= 80): the operand columns of
+// frame f (zeros when f < 0 or !valid), split into three bf16 planes, stored into TMEM (laid out
+// as image_row_to_tmem does) and into the plane images, which the statistics kernel reads next.
+// The row's D <= K/2 - 1 features are loaded into registers first (independent loads, one
+// latency); the squares sit at the constant column K/2 + d, so every register index is static.
+template <int K>
+__device__ __forceinline__ void features_row_to_tmem(const float* __restrict__ X, int D, long long f,
+                                                     uint16_t* __restrict__ planes, int nT, int tile, int r,
+                                                     uint32_t taddr, bool valid) {
+  constexpr int KC = K / 8, DMAX = K / 2 - 1;
+  const bool live = valid && f >= 0;
+  const float* xr = X + (live ? f : 0) * (long long)D;
+  float xv[DMAX];
+#pragma unroll
+  for (int d = 0; d < DMAX; ++d) xv[d] = (live && d < D) ? __ldg(xr + d) : 0.0f;
+#pragma unroll
+  for (int c = 0; c < KC; c += 2) {
+    uint32_t w[3][8];
+#pragma unroll
+    for (int e = 0; e < 16; e += 2) {
+      uint16_t a[2], b[2], cc[2];
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int k = c * 8 + e + u;  // compile-time
+        float v = 0.0f;
+        if (k < K / 2) {
+          if (k < DMAX && k < D) v = xv[k < DMAX ? k : 0];
+          else if (k == D && live) v = 1.0f;
+        } else if (k - K / 2 < DMAX) {
+          const float x = xv[k - K / 2 < DMAX ? k - K / 2 : 0];
+          v = __fmul_rn(x, x);  // zero for d >= D (xv is zero there)
+        }
+        split3f(v, a[u], b[u], cc[u]);
+      }
+      w[0][e >> 1] = a[0] | ((uint32_t)a[1] << 16);
+      w[1][e >> 1] = b[0] | ((uint32_t)b[1] << 16);
+      w[2][e >> 1] = cc[0] | ((uint32_t)cc[1] << 16);
+    }
+#pragma unroll
+    for (int p = 0; p < 3; ++p) {
+      tmem_st8(taddr + p * (K / 2) + c * 4, w[p]);
+      if (valid) {
+        uint4* dst = reinterpret_cast<uint4*>(planes + ((size_t)(p * nT + tile) * KC + c) * 1024 + (size_t)r * 8);
+        dst[0] = make_uint4(w[p][0], w[p][1], w[p][2], w[p][3]);
+        dst[128] = make_uint4(w[p][4], w[p][5], w[p][6], w[p][7]);  // chunk c + 1: 1024 elements on
+      }
+    }
+  }
+}
+
 // ------------------------------------------------------------------ log-likelihood kernel
 
 // Z tiles (the A operand: 128 frames x K, 3 planes) live in TMEM, double-buffered when it fits;
@@ -248,6 +301,9 @@ __device__ __forceinline__ void image_row_to_tmem(const uint16_t* __restrict__ p
 __host__ __device__ constexpr int cmax(int a, int b) { return a > b ? a : b; }
 __host__ __device__ constexpr int cmin(int a, int b) { return a < b ? a : b; }
 __host__ __device__ constexpr int ll_zb(int K) { return K <= 80 ? 2 : 1; }
+// With two Z buffers the loader warps build a tile from the raw features while the MMAs run on
+// the previous one; with one, features_kernel builds the planes beforehand.
+__host__ __device__ constexpr bool ll_builds_planes(int K) { return ll_zb(K) == 2; }
 __host__ __device__ constexpr int ll_nw(int K) { return K <= 96 ? 3 : 2; }
 
 template <int K>
@@ -269,12 +325,14 @@ constexpr int kLlThreads = 480;  // warp 0 TMA, 1 and 14 MMA, 2-9 epilogue, 10-1
 
 template <int K>
 __global__ void __launch_bounds__(kLlThreads, 1)
-    ll_kernel(const __grid_constant__ CUtensorMap wfull, const uint16_t* __restrict__ zplanes,
+    ll_kernel(const __grid_constant__ CUtensorMap wfull, uint16_t* __restrict__ zplanes,
               long long N, const long long* __restrict__ row_frame, const int* __restrict__ tile_wbase,
               int nTz, int nTw, int tile0, int n_tiles, int n_chunks, float trouble2, float minLL,
               float* __restrict__ ll2_out, float* __restrict__ ll_out, double* __restrict__ llpart,
-              int* __restrict__ err) {
-  // frame tiles tile0 .. tile0 + n_tiles - 1, strided over the CTAs
+              int* __restrict__ err, const float* __restrict__ X, int D) {
+  // frame tiles tile0 .. tile0 + n_tiles - 1, strided over the CTAs. With X the loaders build
+  // the Z tiles from the raw features (and write the plane images for the statistics kernel);
+  // without, they copy them from the plane images.
   using C = LlCfg<K>;
   constexpr int ZB = C::ZB, NW = C::NW;
   extern __shared__ uint8_t smem_raw[];
@@ -395,7 +453,17 @@ __global__ void __launch_bounds__(kLlThreads, 1)
       const int tile = tile0 + (int)blockIdx.x + it * (int)gridDim.x;
       if (!mbar_wait(&z_empty[zb], ((it / ZB) & 1) ^ 1, abort_flag, kWaitLimit)) break;
       tc_fence_after();
-      image_row_to_tmem(zplanes, nTz, K, tile, row, tmem + lane_off + C::Z_COL + zb * C::ZCOLS, tile < nTz);
+      const uint32_t zaddr = tmem + lane_off + C::Z_COL + zb * C::ZCOLS;
+      bool built = false;
+      if constexpr (ll_builds_planes(K)) {
+        if (X) {
+          const long long rr = (long long)tile * 128 + row;
+          const long long f = tile < nTz ? (row_frame ? row_frame[rr] : (rr < N ? rr : -1)) : -1;
+          features_row_to_tmem<K>(X, D, f, zplanes, nTz, tile, row, zaddr, tile < nTz);
+          built = true;
+        }
+      }
+      if (!built) image_row_to_tmem(zplanes, nTz, K, tile, row, zaddr, tile < nTz);
       tmem_st_wait();
       tc_fence_before();
       __syncwarp();
@@ -910,7 +978,7 @@ __global__ void reduce_kernel(int M, int D, int K, int Mact, int n_chunks, int s
   if (t >= (long long)n_chunks * K * 128) return;
   const int rr = (int)(t & 127), e = (int)((t >> 7) % K), ch = (int)(t / (128LL * K));
   const int r = ch * 128 + rr;
-  if (r >= Mact || e > 2 * D) return;
+  if (r >= Mact || e >= K) return;
   if (comp_of_row[r] < 0) return;  // padding row
   const int per = (n_tiles + slices - 1) / slices;
   double s = 0.0;
@@ -921,7 +989,9 @@ __global__ void reduce_kernel(int M, int D, int K, int Mact, int n_chunks, int s
   const int m = comp_of_row[r];
   if (e == D) stats[m] += s;
   else if (e < D) { if (flags & GMM_ACC_MEAN) stats[(size_t)M + (size_t)m * D + e] += s; }
-  else if (flags & GMM_ACC_VAR) stats[(size_t)M + (size_t)M * D + (size_t)m * D + (e - D - 1)] += s;
+  else if (e >= K / 2 && e < K / 2 + D) {
+    if (flags & GMM_ACC_VAR) stats[(size_t)M + (size_t)M * D + (size_t)m * D + (e - K / 2)] += s;
+  }
 }
 
 __global__ void ll_total_kernel(int n, const double* __restrict__ llpart, double* __restrict__ tot) {
@@ -1014,8 +1084,9 @@ int make_map(Ctx* c, CUtensorMap* map, const uint16_t* base, long long total_ele
   return GMM_OK;
 }
 
+// build_planes: the logits kernel builds the feature planes of its tiles from c->X on the way
 template <int K>
-int launch_ll_part(Ctx* c, int tile0, int n_tiles_ll, float* ll_out_dev, bool want_total) {
+int launch_ll_part(Ctx* c, int tile0, int n_tiles_ll, float* ll_out_dev, bool want_total, bool build_planes) {
   using LC = LlCfg<K>;
   const long long Npad = c->tcx.Npad;
   const int nTz = (int)(Npad / 128), nTw = c->tcm.Mpad / 128;
@@ -1036,11 +1107,18 @@ int launch_ll_part(Ctx* c, int tile0, int n_tiles_ll, float* ll_out_dev, bool wa
     attr_set_ll = true;
   }
   const float trouble2 = (float)(c->minLL * kLog2e);
+  if (build_planes && !ll_builds_planes(K)) {
+    GMM_LAUNCH(c, "tc_features_kernel");
+    const long long t0 = (long long)tile0 * 128 * (K / 8), t1 = (long long)(tile0 + n_tiles_ll) * 128 * (K / 8);
+    features_kernel<<<(unsigned)((t1 - t0 + 255) / 256), 256, 0, c->stream>>>(c->X, c->N, nTz, c->D, K, nullptr,
+                                                                             c->tcx.planes, t0, t1);
+  }
   {
     GMM_LAUNCH(c, "tc_ll_kernel");
     ll_kernel<K><<<grid_ll, kLlThreads, LC::SMEM, c->stream>>>(
         c->tm_wfull, c->tcx.planes, c->N, nullptr, nullptr, nTz, nTw, tile0, n_tiles_ll, n_chunks, trouble2,
-        c->minLL, c->tcm.ll2, ll_out_dev, c->tc_llpart, c->tc_err);
+        c->minLL, c->tcm.ll2, ll_out_dev, c->tc_llpart, c->tc_err,
+        build_planes && ll_builds_planes(K) ? c->X : nullptr, c->D);
   }
   if (!want_total) return GMM_OK;
   {
@@ -1055,8 +1133,8 @@ template <int K>
 int launch_acc_part(Ctx* c, int flags);
 
 template <int K>
-int launch_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
-  const int rc = launch_ll_part<K>(c, 0, (int)(c->tcx.Npad / 128), ll_out_dev, want_stats);
+int launch_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev, bool build_planes) {
+  const int rc = launch_ll_part<K>(c, 0, (int)(c->tcx.Npad / 128), ll_out_dev, want_stats, build_planes);
   if (rc || !want_stats) return rc;
   return launch_acc_part<K>(c, flags);
 }
@@ -1162,17 +1240,10 @@ int tc_prepare_features(Ctx* c) {
     c->tcx.Npad = Npad;
     c->tcx.K = K;
   }
-  {
-    GMM_LAUNCH(c, "tc_features_kernel");
-    const long long tot = Npad * (K / 8);
-    features_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(c->X, c->N, Npad / 128, c->D, K,
-                                                                         nullptr, c->tcx.planes, 0, tot);
-  }
+  // the logits kernel fills the planes from the features on its first pass over them
   int rc = make_map(c, &c->tm_zfull, c->tcx.planes, 3 * Npad * K, K);
   if (!rc) rc = make_map(c, &c->tm_zhalf, c->tcx.planes, 3 * Npad * K, 4);
-  if (rc) return rc;
-  c->tcx_valid = true;
-  return GMM_OK;
+  return rc;
 }
 
 int tc_prepare_model(Ctx* c) {
@@ -1218,7 +1289,7 @@ int tc_estep_streamed(Ctx* c, const float* Xh, int flags, int nchunks) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, dev);
   }
-  const int K = tc_K(c->D), KC = K / 8;
+  const int K = tc_K(c->D);
   const long long Npad = (c->N + 127) / 128 * 128;
   if (c->tcx.planes == nullptr || c->tcx.Npad != Npad || c->tcx.K != K) {
     dfree(c, c->tcx.planes, (size_t)3 * c->tcx.Npad * c->tcx.K * sizeof(uint16_t));
@@ -1240,7 +1311,16 @@ int tc_estep_streamed(Ctx* c, const float* Xh, int flags, int nchunks) {
     cudaError_t e = cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamCreate(copy)");
   }
-  while ((int)c->copy_events.size() < nchunks) {
+  // Chunks of whole 128-frame tiles: the first ones grow geometrically from 1/8 of the steady
+  // chunk (nT / nchunks) so that little of the transfer is exposed before the first kernels run;
+  // the copies outpace the logits kernels from then on.
+  const int nT = (int)(Npad / 128);
+  const int per = (nT + nchunks - 1) / nchunks;
+  std::vector<int> bounds{0};
+  for (int sz = std::max(1, per / 8); bounds.back() < nT; sz = std::min(per, 2 * sz))
+    bounds.push_back(std::min(nT, bounds.back() + sz));
+  const int nck = (int)bounds.size() - 1;
+  while ((int)c->copy_events.size() < nck) {
     cudaEvent_t ev;
     cudaError_t e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
     if (e != cudaSuccess) return cuda_fail(c, e, "cudaEventCreate");
@@ -1249,11 +1329,9 @@ int tc_estep_streamed(Ctx* c, const float* Xh, int flags, int nchunks) {
   // the copies must not overwrite frames a previous E-step on the compute stream still reads
   cudaEventRecord(c->copy_events[0], c->stream);
   cudaStreamWaitEvent(c->copy_stream, c->copy_events[0], 0);
-  const int nT = (int)(Npad / 128);
-  const int per = (nT + nchunks - 1) / nchunks;
   float* X = const_cast<float*>(c->X);
-  for (int k = 0; k < nchunks; ++k) {
-    const int ta = k * per, tb = std::min(nT, ta + per);
+  for (int k = 0; k < nck; ++k) {
+    const int ta = bounds[k], tb = bounds[k + 1];
     if (ta >= tb) break;
     const long long fa = (long long)ta * 128, fb = std::min(c->N, (long long)tb * 128);
     if (fb > fa) {
@@ -1263,21 +1341,16 @@ int tc_estep_streamed(Ctx* c, const float* Xh, int flags, int nchunks) {
     }
     cudaEventRecord(c->copy_events[k], c->copy_stream);
     cudaStreamWaitEvent(c->stream, c->copy_events[k], 0);
-    {
-      GMM_LAUNCH(c, "tc_features_kernel");
-      const long long t0 = (long long)ta * 128 * KC, t1 = (long long)tb * 128 * KC;
-      features_kernel<<<(unsigned)((t1 - t0 + 255) / 256), 256, 0, c->stream>>>(c->X, c->N, nT, c->D, K, nullptr,
-                                                                               c->tcx.planes, t0, t1);
-    }
+    // the logits kernel builds the chunk's feature planes as it reads the frames
     switch (K) {
-      case 16: rc = launch_ll_part<16>(c, ta, tb - ta, nullptr, true); break;
-      case 32: rc = launch_ll_part<32>(c, ta, tb - ta, nullptr, true); break;
-      case 48: rc = launch_ll_part<48>(c, ta, tb - ta, nullptr, true); break;
-      case 64: rc = launch_ll_part<64>(c, ta, tb - ta, nullptr, true); break;
-      case 80: rc = launch_ll_part<80>(c, ta, tb - ta, nullptr, true); break;
-      case 96: rc = launch_ll_part<96>(c, ta, tb - ta, nullptr, true); break;
-      case 112: rc = launch_ll_part<112>(c, ta, tb - ta, nullptr, true); break;
-      default: rc = launch_ll_part<128>(c, ta, tb - ta, nullptr, true); break;
+      case 16: rc = launch_ll_part<16>(c, ta, tb - ta, nullptr, true, true); break;
+      case 32: rc = launch_ll_part<32>(c, ta, tb - ta, nullptr, true, true); break;
+      case 48: rc = launch_ll_part<48>(c, ta, tb - ta, nullptr, true, true); break;
+      case 64: rc = launch_ll_part<64>(c, ta, tb - ta, nullptr, true, true); break;
+      case 80: rc = launch_ll_part<80>(c, ta, tb - ta, nullptr, true, true); break;
+      case 96: rc = launch_ll_part<96>(c, ta, tb - ta, nullptr, true, true); break;
+      case 112: rc = launch_ll_part<112>(c, ta, tb - ta, nullptr, true, true); break;
+      default: rc = launch_ll_part<128>(c, ta, tb - ta, nullptr, true, true); break;
     }
     if (rc) return rc;
   }
@@ -1316,24 +1389,26 @@ int tc_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
     cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, dev);
   }
   int rc;
-  if (!c->tcx_valid || c->tcx.planes == nullptr) {
+  const bool build = !c->tcx_valid || c->tcx.planes == nullptr;
+  if (build) {
     rc = tc_prepare_features(c);
     if (rc) return rc;
   }
   rc = tc_prepare_model(c);  // model may change every iteration
   if (rc) return rc;
   switch (c->tcm.K) {
-    case 16: rc = launch_estep<16>(c, flags, want_stats, ll_out_dev); break;
-    case 32: rc = launch_estep<32>(c, flags, want_stats, ll_out_dev); break;
-    case 48: rc = launch_estep<48>(c, flags, want_stats, ll_out_dev); break;
-    case 64: rc = launch_estep<64>(c, flags, want_stats, ll_out_dev); break;
-    case 80: rc = launch_estep<80>(c, flags, want_stats, ll_out_dev); break;
-    case 96: rc = launch_estep<96>(c, flags, want_stats, ll_out_dev); break;
-    case 112: rc = launch_estep<112>(c, flags, want_stats, ll_out_dev); break;
-    case 128: rc = launch_estep<128>(c, flags, want_stats, ll_out_dev); break;
+    case 16: rc = launch_estep<16>(c, flags, want_stats, ll_out_dev, build); break;
+    case 32: rc = launch_estep<32>(c, flags, want_stats, ll_out_dev, build); break;
+    case 48: rc = launch_estep<48>(c, flags, want_stats, ll_out_dev, build); break;
+    case 64: rc = launch_estep<64>(c, flags, want_stats, ll_out_dev, build); break;
+    case 80: rc = launch_estep<80>(c, flags, want_stats, ll_out_dev, build); break;
+    case 96: rc = launch_estep<96>(c, flags, want_stats, ll_out_dev, build); break;
+    case 112: rc = launch_estep<112>(c, flags, want_stats, ll_out_dev, build); break;
+    case 128: rc = launch_estep<128>(c, flags, want_stats, ll_out_dev, build); break;
     default: return fail(c, GMM_ERR_UNSUPPORTED, "tensor-core path: unsupported K");
   }
   if (rc) return rc;
+  c->tcx_valid = true;
   if (c->static_shapes) return GMM_OK;  // checked by the caller after the captured iterations
   // surface a bounded-wait expiry as an error status (the context stays usable)
   int herr = 0;
@@ -1555,11 +1630,17 @@ void run_batch_k(Ctx* c, const TcBatch& b, const CUtensorMap& zfull, const CUten
   cudaFuncSetAttribute(ll_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, LC::SMEM);
   cudaFuncSetAttribute(acc_kernel<K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, AC::SMEM);
   cudaFuncSetAttribute(acc_kernel<K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, ACm::SMEM);
+  if (!ll_builds_planes(K)) {
+    GMM_LAUNCH(c, "tc_features_kernel");
+    features_kernel<<<(unsigned)((b.Rpad * (K / 8) + 255) / 256), 256, 0, c->stream>>>(
+        b.X, b.N, b.Rpad / 128, b.D, K, b.row_frame, b.zplanes, 0, b.Rpad * (K / 8));
+  }
   {
     GMM_LAUNCH(c, "tc_ll_kernel");
     ll_kernel<K><<<grid_ll, kLlThreads, LC::SMEM, c->stream>>>(
         *b.wmap, b.zplanes, b.N, b.row_frame, b.tile_wbase, nTz, b.w_chunks_total, 0, nTz, b.n_chunks,
-        (float)(c->minLL * kLog2e), c->minLL, b.ll2, b.ll, b.llpart, c->tc_err);
+        (float)(c->minLL * kLog2e), c->minLL, b.ll2, b.ll, b.llpart, c->tc_err,
+        ll_builds_planes(K) ? b.X : nullptr, b.D);
   }
   if (b.n_work > 0) {
     GMM_LAUNCH(c, "tc_acc_kernel");
@@ -1574,11 +1655,7 @@ void run_batch_k(Ctx* c, const TcBatch& b, const CUtensorMap& zfull, const CUten
 
 int tc_run_batch(Ctx* c, const TcBatch& b) {
   if (b.Rpad <= 0) return GMM_OK;
-  {
-    GMM_LAUNCH(c, "tc_features_kernel");
-    features_kernel<<<(unsigned)((b.Rpad * (b.K / 8) + 255) / 256), 256, 0, c->stream>>>(
-        b.X, b.N, b.Rpad / 128, b.D, b.K, b.row_frame, b.zplanes, 0, b.Rpad * (b.K / 8));
-  }
+  // the logits kernel builds the feature planes (row map applied) from b.X as it goes
   CUtensorMap zfull, zhalf;
   int rc = make_map(c, &zfull, b.zplanes, 3 * b.Rpad * b.K, b.K);
   if (!rc) rc = make_map(c, &zhalf, b.zplanes, 3 * b.Rpad * b.K, 4);
