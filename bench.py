@@ -370,7 +370,11 @@ class MllrBatch:
 class FullEm:
     """One EM iteration of a full-covariance GMM over N resident frames."""
     metric = "frames·components/s per EM iter (full covariances)"
-    bound = "fp32"
+
+    @staticmethod
+    def bound_for(kernel):
+        # the log-likelihood runs on the tensor cores for D <= 63, the statistics on FP32 lanes
+        return "tensor" if kernel == "full_tc_ll_kernel" else "fp32"
 
     def __init__(self, args, rank, gen_frames=None):
         from gmm_gb300 import synth
@@ -405,8 +409,8 @@ class FullEm:
     def flop_per_fc(self, kernel):
         D = self.D
         P = D * (D + 1) // 2
-        if kernel == "full_ll_kernel":
-            return 2 * (P + D) + D + 4       # |U (x - mu)|^2 by FMAs, x - mu, the log-joint
+        if kernel in ("full_ll_kernel", "full_tc_ll_kernel"):
+            return 2 * (P + D) + D + 4       # |U (x - mu)|^2 (triangular U), x - mu, the log-joint
         if kernel == "full_stats_kernel":
             return 2 * (P + D) + 1           # gamma x_k x_kk products + sums, gamma x_k, n
         return 2 * (P + D)
@@ -775,7 +779,7 @@ def main():
         # profiles/acc_kernel_ubm_em_1Mx2048x39.md
         traffic = 509.5 * wl.N + 39.1e6
     peak_source = f"{peak_kind} (bf16 sustained, MEASURED_PEAKS.json)"
-    bound = getattr(wl, "bound", "tensor")
+    bound = wl.bound_for(name) if hasattr(wl, "bound_for") else getattr(wl, "bound", "tensor")
     if bound == "fp32":  # SIMT FP32 kernels: nominal FMA rate (no measured FP32 peak in the file)
         peak = 152 * 128 * 2 * 2.07e9 / 1e12
         peak_source = "nominal FP32 SIMT: 152 SMs x 128 lanes x 2 flop x 2.07 GHz"

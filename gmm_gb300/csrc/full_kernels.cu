@@ -25,12 +25,15 @@
 // of U stored at rowoff(i) padded with zeros to a multiple of 4 floats (UP = rowoff(DP), DP = D
 // rounded up to a kernel width), statistics [n (M) | F (M x D) | S (M x P) | totLL | pad] with
 // P = D(D+1)/2.
+#include <cuda_bf16.h>
 #include <math.h>
 
+#include <algorithm>
 #include <cstring>
 #include <new>
 
 #include "gmm_internal.cuh"
+#include "tc_ptx.cuh"
 
 namespace gmm {
 
@@ -49,6 +52,9 @@ struct FullModel {
   double* aux = nullptr;  // --robust auxiliary statistics [M x D | M | M]
   size_t aux_cap = 0;
   bool aux_valid = false;
+  uint16_t* tcB = nullptr;  // tensor-core operand images of [U | -U mu], per component group
+  size_t tcB_cap = 0;
+  int tc_ng = 0;            // component groups (0: the FP32 kernel is used)
   size_t stats_count() const { return (size_t)M * (1 + D + P) + 2; }
 };
 
@@ -89,6 +95,273 @@ __device__ __forceinline__ void add_log(float& p1, float p2) {
   if (__fsub_rn(p1, 15.0f) > p2) return;
   if (p1 > p2) p1 = __fadd_rn(p1, logf(__fadd_rn(1.0f, expf(__fsub_rn(p2, p1)))));
   else p1 = __fadd_rn(p2, logf(__fadd_rn(1.0f, expf(__fsub_rn(p1, p2)))));
+}
+
+// ------------------------------------------------------------------ tensor-core log-likelihood
+//
+// y = U (x - mu) for every frame and component as one tcgen05 GEMM per group of GC components:
+// A = the 128-frame tile [x | 1 | 0...] (KX = D + 1 rounded up to 16 columns), B = the group's
+// rows [U_m | -U_m mu_m | 0...] (KX rows per component, N = GC KX), D[128 frames x N] in TMEM.
+// Both operands are split into three bf16 planes and the six plane products with i + j <= 2 are
+// summed (FP32-level products); -U mu is formed in FP64 and rounded to float. The epilogue
+// (thread = frame) sums y_i^2 over the D rows of each component in order with fused
+// multiply-adds, then applies the FP32 kernel's rules (non-finite -> minLogLike, log weight,
+// sequential addLog over the active components in order).
+constexpr int kFtThreads = 192;  // warp 0 copies, warp 1 MMA, warps 2-5 epilogue (one per lane quadrant)
+constexpr long long kFtWait = 4000000000LL;
+__host__ __device__ constexpr int ft_gc(int KX) { return KX == 16 ? 15 : KX == 32 ? 7 : KX == 48 ? 4 : 3; }
+__host__ __device__ constexpr int ft_min(int a, int b) { return a < b ? a : b; }
+
+template <int KX>
+struct FtCfg {
+  static constexpr int GC = ft_gc(KX), N = GC * KX;
+  static constexpr int A_COL = 2 * N;            // two accumulators at 0 and N, then the X tile
+  static constexpr int B_PLANE = N * KX * 2;     // bytes of one plane of a group image
+  static constexpr int B_STAGE = 3 * B_PLANE;
+  static constexpr int NB = ft_min(3, (227 * 1024 - 2048) / B_STAGE);
+  static constexpr int OFF_BAR = NB * B_STAGE;
+  static constexpr int SMEM = OFF_BAR + 256 + 1024;
+  static_assert(N <= 256 && A_COL + 3 * KX / 2 <= 512 && NB >= 2, "tensor-core full LL budget");
+};
+
+__device__ __forceinline__ void ft_split3(float v, uint16_t& a, uint16_t& b, uint16_t& c) {
+  const __nv_bfloat16 h1 = __float2bfloat16_rn(v);
+  float r = v - __bfloat162float(h1);
+  const __nv_bfloat16 h2 = __float2bfloat16_rn(r);
+  r = r - __bfloat162float(h2);
+  const __nv_bfloat16 h3 = __float2bfloat16_rn(r);
+  a = __bfloat16_as_ushort(h1);
+  b = __bfloat16_as_ushort(h2);
+  c = __bfloat16_as_ushort(h3);
+}
+
+// Group images: element (row, k) of plane p of group g at
+// ((g * 3 + p) * KX/8 + k / 8) * N * 8 + row * 8 + k % 8, row = j * KX + i for component slot j
+// and row i of U. One thread per element of a plane, in image order.
+__global__ void full_tc_b_kernel(int Mact, int D, int UP, int KX, int GC, int ng, const int* __restrict__ act,
+                                 const float* __restrict__ mu, const float* __restrict__ U,
+                                 uint16_t* __restrict__ B) {
+  const int N = GC * KX;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)ng * N * KX) return;
+  const int g = (int)(t / ((long long)N * KX));
+  const int e = (int)(t - (long long)g * N * KX);
+  const int kc = e / (N * 8), row = (e / 8) % N, k = kc * 8 + (e & 7);
+  const int j = row / KX, i = row - j * KX, a = g * GC + j;
+  float v = 0.0f;
+  if (a < Mact && i < D) {
+    const int m = act[a];
+    const float* Ur = U + (size_t)m * UP + rowoff(i);
+    if (k <= i) {
+      v = Ur[k];
+    } else if (k == D) {
+      double sum = 0.0;
+      for (int kk = 0; kk <= i; ++kk) sum += (double)Ur[kk] * (double)mu[(size_t)m * D + kk];
+      v = (float)(-sum);
+    }
+  }
+  uint16_t p1, p2, p3;
+  ft_split3(v, p1, p2, p3);
+  uint16_t* base = B + (size_t)g * 3 * N * KX + e;
+  base[0] = p1;
+  base[(size_t)N * KX] = p2;
+  base[2 * (size_t)N * KX] = p3;
+}
+
+__device__ __forceinline__ int ft_pa(int pr) { return pr == 0 ? 2 : (pr == 1 || pr == 3) ? 1 : 0; }
+__device__ __forceinline__ int ft_pb(int pr) { return pr == 2 ? 2 : (pr == 1 || pr == 4) ? 1 : 0; }
+
+// One component's KX accumulator columns of this thread's row (all loads in flight at once).
+template <int KX>
+__device__ __forceinline__ void ft_ld(uint32_t taddr, uint32_t (&y)[KX / 16][16]) {
+#pragma unroll
+  for (int q = 0; q < KX / 16; ++q) ptx::tmem_ld16(taddr + 16 * q, y[q]);
+  ptx::tmem_ld_wait();
+}
+
+template <int KX>
+__global__ void __launch_bounds__(kFtThreads, 1)
+    full_tc_ll_kernel(const float* __restrict__ X, long long f0, long long nf, int D, int Mact,
+                      const int* __restrict__ act, const float* __restrict__ logG,
+                      const float* __restrict__ logW, const uint16_t* __restrict__ Bimg, int ng, float minLL,
+                      float* __restrict__ G, long long ldg, float* __restrict__ ll, double* __restrict__ llpart,
+                      int* __restrict__ flag, int* __restrict__ err) {
+  using namespace ptx;
+  using C = FtCfg<KX>;
+  constexpr int GC = C::GC, N = C::N, NB = C::NB;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + C::OFF_BAR);
+  uint64_t* b_full = bars;           // [NB <= 3]
+  uint64_t* b_empty = bars + 3;      // [NB]
+  uint64_t* d_full = bars + 6;       // [2]
+  uint64_t* d_empty = bars + 8;      // [2]
+  uint64_t* a_full = bars + 10;
+  uint64_t* mma_done = bars + 11;
+  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(bars + 12);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(bars + 13);
+  double* s_red = reinterpret_cast<double*>(bars + 14);  // [4]
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long n_tiles = (nf + 127) / 128;
+  const int my_tiles = blockIdx.x < n_tiles ? (int)((n_tiles - 1 - blockIdx.x) / gridDim.x) + 1 : 0;
+  const int steps = my_tiles * ng;
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < NB; ++i) {
+      mbar_init(&b_full[i], 1);
+      mbar_init(&b_empty[i], 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&d_full[i], 1);
+      mbar_init(&d_empty[i], 4);
+    }
+    mbar_init(a_full, 4);
+    mbar_init(mma_done, 1);
+    *abort_flag = 0;
+    fence_mbar_init();
+  }
+  if (warp == 1) {
+    tmem_alloc(tmem_holder, 512);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_holder;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int issued = 0;
+      for (int sidx = 0; sidx < steps; ++sidx) {
+        const int st = sidx % NB, g = sidx % ng;
+        if (!mbar_wait(&b_empty[st], ((sidx / NB) & 1) ^ 1, abort_flag, kFtWait)) break;
+        mbar_arrive_expect_tx(&b_full[st], C::B_STAGE);
+        bulk_load(smem + st * C::B_STAGE, Bimg + (size_t)g * 3 * N * KX, C::B_STAGE, &b_full[st]);
+        issued = sidx + 1;
+      }
+      if (*abort_flag)
+        for (int sidx = max(0, issued - NB); sidx < issued; ++sidx) {
+          const long long t0 = clock64();
+          while (!mbar_try_wait(&b_full[sidx % NB], (sidx / NB) & 1))
+            if (clock64() - t0 > kFtWait) break;
+        }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = idesc_bf16(128, N, false, false);
+      const uint32_t sb = smem_u32(smem);
+      bool ok = true;
+      for (int it = 0; it < my_tiles && ok; ++it) {
+        if (!mbar_wait(a_full, it & 1, abort_flag, kFtWait)) break;
+        tc_fence_after();
+        for (int g = 0; g < ng; ++g) {
+          const int sidx = it * ng + g, st = sidx % NB, b = sidx & 1;
+          if (!mbar_wait(&b_full[st], (sidx / NB) & 1, abort_flag, kFtWait)) { ok = false; break; }
+          if (sidx >= 2 && !mbar_wait(&d_empty[b], ((sidx - 2) >> 1) & 1, abort_flag, kFtWait)) { ok = false; break; }
+          tc_fence_after();
+          const uint32_t d = tmem + (uint32_t)(b * N);
+#pragma unroll
+          for (int q = 0; q < KX / 16; ++q) {
+#pragma unroll
+            for (int pr = 0; pr < 6; ++pr) {
+              const uint32_t a = tmem + C::A_COL + ft_pa(pr) * (KX / 2) + q * 8;
+              const uint64_t bd = smem_desc(sb + st * C::B_STAGE + ft_pb(pr) * C::B_PLANE + q * 2 * N * 16, N * 16, 128);
+              mma_ts(d, a, bd, idesc, (q > 0 || pr > 0) ? 1u : 0u);
+            }
+          }
+          mma_commit(&b_empty[st]);
+          mma_commit(&d_full[b]);
+        }
+      }
+      mma_commit(mma_done);
+      const long long t0 = clock64();
+      while (!mbar_try_wait(mma_done, 0))
+        if (clock64() - t0 > kFtWait) break;
+    }
+  } else {
+    // epilogue: thread = frame row of the tile
+    const int q4 = warp & 3, row = q4 * 32 + lane;
+    const uint32_t lane_off = (uint32_t)(q4 * 32) << 16;
+    double v = 0.0;
+    bool ok = true;
+    for (int it = 0; it < my_tiles && ok; ++it) {
+      const long long fi = ((long long)blockIdx.x + (long long)it * gridDim.x) * 128 + row;
+      const bool valid = fi < nf;
+      // the X tile into TMEM (the previous tile's MMAs are complete: their last accumulator
+      // was read below)
+      {
+        const float* xr = X + (size_t)(f0 + (valid ? fi : 0)) * D;
+        for (int c = 0; c < KX / 8; c += 2) {
+          uint32_t w[3][8];
+#pragma unroll
+          for (int e = 0; e < 16; e += 2) {
+            uint16_t a[2], b[2], cc[2];
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+              const int k = c * 8 + e + u;
+              const float val = !valid ? 0.0f : k < D ? __ldg(xr + k) : (k == D ? 1.0f : 0.0f);
+              ft_split3(val, a[u], b[u], cc[u]);
+            }
+            w[0][e >> 1] = a[0] | ((uint32_t)a[1] << 16);
+            w[1][e >> 1] = b[0] | ((uint32_t)b[1] << 16);
+            w[2][e >> 1] = cc[0] | ((uint32_t)cc[1] << 16);
+          }
+#pragma unroll
+          for (int p = 0; p < 3; ++p) tmem_st8(tmem + lane_off + C::A_COL + p * (KX / 2) + c * 4, w[p]);
+        }
+        tmem_st_wait();
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(a_full);
+      }
+      float maxLL = minLL, sumLL = minLL;
+      for (int g = 0; g < ng && ok; ++g) {
+        const int sidx = it * ng + g, b = sidx & 1;
+        if (!mbar_wait(&d_full[b], (sidx >> 1) & 1, abort_flag, kFtWait)) { ok = false; break; }
+        tc_fence_after();
+        const int nt = min(GC, Mact - g * GC);
+        for (int j = 0; j < nt; ++j) {
+          uint32_t y[KX / 16][16];
+          ft_ld<KX>(tmem + lane_off + (uint32_t)(b * N + j * KX), y);
+          float e = 0.0f;
+#pragma unroll
+          for (int i = 0; i < KX; ++i)
+            if (i < D) {
+              const float yi = __uint_as_float(y[i / 16][i % 16]);
+              e = __fmaf_rn(yi, yi, e);
+            }
+          const int a = g * GC + j, m = act[a];
+          float s = __fsub_rn(logG[m], __fmul_rn(0.5f, e));
+          if (!isfinite(s)) s = minLL;
+          const float gv = __fadd_rn(s, logW[m]);
+          if (G != nullptr && valid) G[(size_t)a * ldg + fi] = gv;
+          if (maxLL < gv) maxLL = gv;
+          add_log(sumLL, gv);
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&d_empty[b]);
+      }
+      if (ok && valid) {
+        const float l = (maxLL == minLL) ? minLL : sumLL;
+        if (maxLL == minLL) flag[1] = 1;
+        ll[f0 + fi] = l;
+        v += (double)l;
+      }
+    }
+    v = warp_sum(v);
+    if (lane == 0) s_red[q4] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (*abort_flag) atomicExch(err, 1);
+    llpart[blockIdx.x] = s_red[0] + s_red[1] + s_red[2] + s_red[3];
+  }
+  if (warp == 1) {
+    tc_fence_after();
+    tmem_dealloc(tmem, 512);
+  }
 }
 
 // (k, kk) of packed entry e of the upper triangle in row order, kk >= k.
@@ -591,6 +864,7 @@ void free_full(Ctx* c) {
   dfree(c, f->pw, m1); dfree(c, f->pmu, md); dfree(c, f->pcov, mdd);
   dfree(c, f->stats, sizeof(double) * f->stats_count());
   dfree(c, f->aux, f->aux_cap);
+  dfree(c, f->tcB, f->tcB_cap);
   *f = FullModel();
 }
 
@@ -647,6 +921,36 @@ int full_precompute(Ctx* c) {
     cudaMemsetAsync(c->flag + 7, 0, sizeof(int), c->stream);
     return fail(c, GMM_ERR_MODEL, "getCovInverse(): cholesky factorization failed!");
   }
+  // operand images of the tensor-core log-likelihood kernel (D <= 63)
+  f->tc_ng = 0;
+  if (f->D <= 63 && f->Mact > 0) {
+    const int KX = (f->D + 1 + 15) / 16 * 16, GC = ft_gc(KX), N = GC * KX;
+    const int ng = (f->Mact + GC - 1) / GC;
+    const size_t need = sizeof(uint16_t) * (size_t)ng * 3 * N * KX;
+    if (need > f->tcB_cap) {
+      dfree(c, f->tcB, f->tcB_cap);
+      f->tcB = nullptr;
+      f->tcB_cap = 0;
+      const int rc2 = dalloc(c, (void**)&f->tcB, need, "full-covariance operand images");
+      if (rc2) return rc2;
+      f->tcB_cap = need;
+    }
+    if (!c->tc_err) {
+      const int rc2 = dalloc(c, (void**)&c->tc_err, sizeof(int), "tc error flag");
+      if (rc2) return rc2;
+      cudaMemsetAsync(c->tc_err, 0, sizeof(int), c->stream);
+    }
+    if (c->sms == 0) {
+      int dev;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, dev);
+    }
+    GMM_LAUNCH(c, "full_tc_b_kernel");
+    const long long tot = (long long)ng * N * KX;
+    full_tc_b_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(f->Mact, f->D, f->UP, KX, GC, ng, f->act,
+                                                                          f->mu, f->U, f->tcB);
+    f->tc_ng = ng;
+  }
   f->dirty = false;
   return GMM_OK;
 }
@@ -679,8 +983,35 @@ void launch_full_stats(Ctx* c, int D, int Mact, long long f0, long long nf, long
                                                      c->minGamma, Mact == 1, flags, slices, slice_len, c->part);
 }
 
-// Launches the log-likelihood kernel for D's width; returns its block count.
+template <int KX>
+int launch_full_tc_ll(Ctx* c, long long f0, long long nf, float* G, long long ldg, float* llout) {
+  FullModel* f = c->full;
+  using C = FtCfg<KX>;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(full_tc_ll_kernel<KX>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
+    attr = true;
+  }
+  const long long n_tiles = (nf + 127) / 128;
+  const int grid = (int)std::max(1LL, std::min<long long>(n_tiles, c->sms));
+  GMM_LAUNCH(c, "full_tc_ll_kernel");
+  full_tc_ll_kernel<KX><<<grid, kFtThreads, C::SMEM, c->stream>>>(
+      c->X, f0, nf, f->D, f->Mact, f->act, f->logG, f->logW, f->tcB, f->tc_ng, c->minLL, G, ldg, llout,
+      c->llpart, c->flag, c->tc_err);
+  return grid;
+}
+
+// Launches the log-likelihood kernel for D's width (the tensor-core one for D <= 63); returns its
+// block count.
 int dispatch_ll(Ctx* c, long long f0, long long nf, float* G, long long ldg, float* llout) {
+  if (c->full->tc_ng > 0) {
+    switch ((c->full->D + 1 + 15) / 16 * 16) {
+      case 16: return launch_full_tc_ll<16>(c, f0, nf, G, ldg, llout);
+      case 32: return launch_full_tc_ll<32>(c, f0, nf, G, ldg, llout);
+      case 48: return launch_full_tc_ll<48>(c, f0, nf, G, ldg, llout);
+      default: return launch_full_tc_ll<64>(c, f0, nf, G, ldg, llout);
+    }
+  }
   const int DP = c->full->DP;
   switch (DP) {
     case 8: launch_full_ll<8>(c, f0, nf, G, ldg, llout); break;
@@ -802,6 +1133,16 @@ int full_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
     if (c->robust && f->aux) {
       const int rc2 = robust_chunk(c, f->M, D, f->Mact, f->act, f0, nf, chunk, f->aux);
       if (rc2) return rc2;
+    }
+  }
+  if (f->tc_ng > 0) {  // surface a bounded-wait expiry of the tensor-core kernel
+    int herr = 0;
+    cudaMemcpyAsync(&herr, c->tc_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+    const int rc = sync(c, "full-covariance E-step");
+    if (rc) return rc;
+    if (herr) {
+      cudaMemsetAsync(c->tc_err, 0, sizeof(int), c->stream);
+      return fail(c, GMM_ERR_TIMEOUT, "full-covariance E-step: a bounded device wait expired");
     }
   }
   return GMM_OK;

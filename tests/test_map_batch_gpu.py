@@ -138,3 +138,35 @@ def test_batch_bad_offsets_are_errors(glib):
         h.map_batch(offs, 0)
     assert e.value.code == glib.ERR_ARG
     h.close()
+
+
+def test_batch_scratch_reuse_across_sizes(glib):
+    """The batched calls keep their device buffers between calls (grow-only scratch): a small
+    batch after a large one, a large one after a small one and a MAP call after an MLLR call on
+    the same handle give what a fresh handle gives for each batch."""
+    X, offs, ubm = workload(seed=57)
+    small = offs[3:7] - 0  # a few speakers, a sub-range of the frames
+    calls = [("map", offs, (16, 1, 1, 1)), ("map", small, (8, 0, 1, 0)), ("mllr", offs, ()),
+             ("map", offs, (16, 0, 1, 1)), ("map", small, (8, 1, 1, 0))]
+
+    def run(h, kind, o, args):
+        if kind == "map":
+            return h.map_batch(o, *args)
+        W, st, _, ll = h.mllr_batch(o, means=False)
+        return W, st, ll
+
+    h = glib.Handle(0)
+    h.set_precision(glib.PREC_TC)
+    h.upload_model(*ubm)
+    h.upload_features(X)
+    shared = [run(h, *c) for c in calls]
+    h.close()
+    for c, got in zip(calls, shared):
+        f = glib.Handle(0)
+        f.set_precision(glib.PREC_TC)
+        f.upload_model(*ubm)
+        f.upload_features(X)
+        want = run(f, *c)
+        f.close()
+        for x, y in zip(got, want):
+            assert np.array_equal(x, y), c[0]
