@@ -54,6 +54,7 @@ struct FullModel {
   bool aux_valid = false;
   uint16_t* tcB = nullptr;  // tensor-core operand images of [U | -U mu], per component group
   size_t tcB_cap = 0;
+  float2* tcC = nullptr;    // (log Gconst, log w) of the active components in order [M]
   int tc_ng = 0;            // component groups (0: the FP32 kernel is used)
   size_t stats_count() const { return (size_t)M * (1 + D + P) + 2; }
 };
@@ -104,9 +105,9 @@ __device__ __forceinline__ void add_log(float& p1, float p2) {
 // rows [U_m | -U_m mu_m | 0...] (KX rows per component, N = GC KX), D[128 frames x N] in TMEM.
 // Both operands are split into three bf16 planes and the six plane products with i + j <= 2 are
 // summed (FP32-level products); -U mu is formed in FP64 and rounded to float. The epilogue
-// (thread = frame) sums y_i^2 over the D rows of each component in order with fused
-// multiply-adds, then applies the FP32 kernel's rules (non-finite -> minLogLike, log weight,
-// sequential addLog over the active components in order).
+// (thread = frame) sums y_i^2 over the D rows of each component in four interleaved FMA chains,
+// then applies the FP32 kernel's rules (non-finite -> minLogLike, log weight, sequential addLog
+// over the active components in order).
 constexpr int kFtThreads = 192;  // warp 0 copies, warp 1 MMA, warps 2-5 epilogue (one per lane quadrant)
 constexpr long long kFtWait = 4000000000LL;
 __host__ __device__ constexpr int ft_gc(int KX) { return KX == 16 ? 15 : KX == 32 ? 7 : KX == 48 ? 4 : 3; }
@@ -140,9 +141,11 @@ __device__ __forceinline__ void ft_split3(float v, uint16_t& a, uint16_t& b, uin
 // and row i of U. One thread per element of a plane, in image order.
 __global__ void full_tc_b_kernel(int Mact, int D, int UP, int KX, int GC, int ng, const int* __restrict__ act,
                                  const float* __restrict__ mu, const float* __restrict__ U,
-                                 uint16_t* __restrict__ B) {
+                                 const float* __restrict__ logG, const float* __restrict__ logW,
+                                 uint16_t* __restrict__ B, float2* __restrict__ cpair) {
   const int N = GC * KX;
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < Mact) cpair[t] = make_float2(logG[act[t]], logW[act[t]]);
   if (t >= (long long)ng * N * KX) return;
   const int g = (int)(t / ((long long)N * KX));
   const int e = (int)(t - (long long)g * N * KX);
@@ -182,8 +185,7 @@ __device__ __forceinline__ void ft_ld(uint32_t taddr, uint32_t (&y)[KX / 16][16]
 template <int KX>
 __global__ void __launch_bounds__(kFtThreads, 1)
     full_tc_ll_kernel(const float* __restrict__ X, long long f0, long long nf, int D, int Mact,
-                      const int* __restrict__ act, const float* __restrict__ logG,
-                      const float* __restrict__ logW, const uint16_t* __restrict__ Bimg, int ng, float minLL,
+                      const float2* __restrict__ cpair, const uint16_t* __restrict__ Bimg, int ng, float minLL,
                       float* __restrict__ G, long long ldg, float* __restrict__ ll, double* __restrict__ llpart,
                       int* __restrict__ flag, int* __restrict__ err) {
   using namespace ptx;
@@ -321,24 +323,43 @@ __global__ void __launch_bounds__(kFtThreads, 1)
         if (!mbar_wait(&d_full[b], (sidx >> 1) & 1, abort_flag, kFtWait)) { ok = false; break; }
         tc_fence_after();
         const int nt = min(GC, Mact - g * GC);
-        for (int j = 0; j < nt; ++j) {
-          uint32_t y[KX / 16][16];
-          ft_ld<KX>(tmem + lane_off + (uint32_t)(b * N + j * KX), y);
-          float e = 0.0f;
+        float2 cp[GC];  // the group's constants, loaded before the accumulator
 #pragma unroll
-          for (int i = 0; i < KX; ++i)
-            if (i < D) {
-              const float yi = __uint_as_float(y[i / 16][i % 16]);
-              e = __fmaf_rn(yi, yi, e);
+        for (int j = 0; j < GC; ++j) cp[j] = j < nt ? __ldg(cpair + g * GC + j) : make_float2(0.0f, 0.0f);
+        // one component's columns in flight while the previous one is summed
+        uint32_t ya[KX / 16][16], yb[KX / 16][16];
+#pragma unroll
+        for (int q = 0; q < KX / 16; ++q) tmem_ld16(tmem + lane_off + (uint32_t)(b * N + 16 * q), ya[q]);
+#pragma unroll
+        for (int j = 0; j < GC; ++j) {
+          if (j < nt) {
+            tmem_ld_wait();
+            uint32_t (&y)[KX / 16][16] = (j & 1) ? yb : ya;
+            uint32_t (&yn)[KX / 16][16] = (j & 1) ? ya : yb;
+            if (j + 1 < nt) {
+#pragma unroll
+              for (int q = 0; q < KX / 16; ++q)
+                tmem_ld16(tmem + lane_off + (uint32_t)(b * N + (j + 1) * KX + 16 * q), yn[q]);
             }
-          const int a = g * GC + j, m = act[a];
-          float s = __fsub_rn(logG[m], __fmul_rn(0.5f, e));
-          if (!isfinite(s)) s = minLL;
-          const float gv = __fadd_rn(s, logW[m]);
-          if (G != nullptr && valid) G[(size_t)a * ldg + fi] = gv;
-          if (maxLL < gv) maxLL = gv;
-          add_log(sumLL, gv);
+            // four interleaved FMA chains (rows i mod 4), then their sum
+            float e4[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+            for (int i = 0; i < KX; ++i)
+              if (i < D) {
+                const float yi = __uint_as_float(y[i / 16][i % 16]);
+                e4[i & 3] = __fmaf_rn(yi, yi, e4[i & 3]);
+              }
+            const float e = __fadd_rn(__fadd_rn(e4[0], e4[1]), __fadd_rn(e4[2], e4[3]));
+            const int a = g * GC + j;
+            float s = __fsub_rn(cp[j].x, __fmul_rn(0.5f, e));
+            if (!isfinite(s)) s = minLL;
+            const float gv = __fadd_rn(s, cp[j].y);
+            if (G != nullptr && valid) G[(size_t)a * ldg + fi] = gv;
+            if (maxLL < gv) maxLL = gv;
+            add_log(sumLL, gv);
+          }
         }
+        tmem_ld_wait();  // nothing left in flight before the buffer is released
         tc_fence_before();
         __syncwarp();
         if (lane == 0) mbar_arrive(&d_empty[b]);
@@ -865,6 +886,7 @@ void free_full(Ctx* c) {
   dfree(c, f->stats, sizeof(double) * f->stats_count());
   dfree(c, f->aux, f->aux_cap);
   dfree(c, f->tcB, f->tcB_cap);
+  dfree(c, f->tcC, sizeof(float2) * (size_t)f->M);
   *f = FullModel();
 }
 
@@ -940,6 +962,10 @@ int full_precompute(Ctx* c) {
       if (rc2) return rc2;
       cudaMemsetAsync(c->tc_err, 0, sizeof(int), c->stream);
     }
+    if (!f->tcC) {
+      const int rc2 = dalloc(c, (void**)&f->tcC, sizeof(float2) * (size_t)f->M, "full-covariance log constants");
+      if (rc2) return rc2;
+    }
     if (c->sms == 0) {
       int dev;
       cudaGetDevice(&dev);
@@ -947,8 +973,8 @@ int full_precompute(Ctx* c) {
     }
     GMM_LAUNCH(c, "full_tc_b_kernel");
     const long long tot = (long long)ng * N * KX;
-    full_tc_b_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(f->Mact, f->D, f->UP, KX, GC, ng, f->act,
-                                                                          f->mu, f->U, f->tcB);
+    full_tc_b_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(
+        f->Mact, f->D, f->UP, KX, GC, ng, f->act, f->mu, f->U, f->logG, f->logW, f->tcB, f->tcC);
     f->tc_ng = ng;
   }
   f->dirty = false;
@@ -996,7 +1022,7 @@ int launch_full_tc_ll(Ctx* c, long long f0, long long nf, float* G, long long ld
   const int grid = (int)std::max(1LL, std::min<long long>(n_tiles, c->sms));
   GMM_LAUNCH(c, "full_tc_ll_kernel");
   full_tc_ll_kernel<KX><<<grid, kFtThreads, C::SMEM, c->stream>>>(
-      c->X, f0, nf, f->D, f->Mact, f->act, f->logG, f->logW, f->tcB, f->tc_ng, c->minLL, G, ldg, llout,
+      c->X, f0, nf, f->D, f->Mact, f->tcC, f->tcB, f->tc_ng, c->minLL, G, ldg, llout,
       c->llpart, c->flag, c->tc_err);
   return grid;
 }
