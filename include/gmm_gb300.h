@@ -185,7 +185,10 @@ int gmm_map_update(gmm_handle h, int tau, int up_weight, int up_mean, int up_var
  * [offs[s], offs[s+1]) (offs: S + 1 non-decreasing entries, offs[S] <= N). With GMM_PREC_TC one
  * fused E-step covers all speakers; with GMM_PREC_FP32 the speakers run one after the other.
  * Outputs (host, any may be NULL): w [S][M], mu [S][M][D], var [S][M][D], ll [S] (each speaker's
- * total log-likelihood under the UBM). tau >= 1. The resident model is not changed. */
+ * total log-likelihood under the UBM). tau >= 1. The resident model is not changed. The batched
+ * calls (gmm_map_batch[_device], gmm_mllr_batch) keep their device working buffers on the handle
+ * between calls, grown to the largest batch seen and released by gmm_destroy; they count against
+ * the handle's memory budget. */
 int gmm_map_batch(gmm_handle h, int S, const long long* offs, int tau, int up_weight, int up_mean,
                   int up_var, float* w, float* mu, float* var, double* ll);
 /* Global MLLR mean transforms for S speakers in one call (one regression class, one iteration):
@@ -193,9 +196,12 @@ int gmm_map_batch(gmm_handle h, int S, const long long* offs, int tau, int up_we
  * (OL_ModelAdapt.cpp:1175-1184: IterW_MLLR -> ComputeW_MLLR :1417-1482, ComputeKiGi_MLLR
  * :1525-1581, prepareKiGiInitMatrices :1484-1523 when ubm_init, CheckInvertibility :1851-1878,
  * AdaptModelMLLR :1583-1612). Speakers own resident frame ranges as in gmm_map_batch; the
- * resident model is the UBM. The G and k sums over components run as FP32-product GEMMs with FP64
- * accumulation (the single-speaker gmm_mllr_estimate keeps the reference's FP64 sequence); each
- * row is solved in FP64 with the reference's pivot-free Gauss-Jordan inverse. Outputs (host, any
+ * resident model is the UBM. The G and k sums over components run as GEMMs with FP32 products
+ * (G on the tensor cores under GMM_PREC_TC, split-bf16 operands) and sums in FP32 per 128
+ * components, added in FP64 (GMM_PREC_FP32) or in FP32 with round-to-nearest (GMM_PREC_TC); the
+ * single-speaker gmm_mllr_estimate keeps the reference's FP64 sequence. Each row is solved by
+ * the elimination order of the reference's pivot-free Gauss-Jordan inverse in double-float
+ * arithmetic (about 2^-48 relative per operation; GB300's FP64 rate is 1/64 of FP32). Outputs (host, any
  * may be NULL): W [S][D][D+1] row-major, status [S] (GMM_OK or GMM_ERR_MLLR when the speaker has
  * too few components or frames; its W is zero and its means stay the UBM's), mu_out [S][M][D]
  * adapted means, ll [S]. */
