@@ -367,6 +367,23 @@ class MllrBatch:
                                       f"(MLLR: E-step + G/k + solves), {dt:.1f} s")
 
 
+def tc_mma_flop_per_fc(kernel, D, second_order=True):
+    """Tensor-core flops the kernel issues per frame x component (dense, padding included): the
+    six split-bf16 plane products of the K-column logits, the five of the statistics (all K
+    columns, or the leading [x | 1] ones without second-order statistics), or the six of the
+    full-covariance y = [U | -U mu][x; 1]. None for SIMT kernels."""
+    K = (2 * D + 1 + 15) // 16 * 16
+    if kernel == "tc_ll_kernel":
+        return 6 * 2 * K
+    if kernel == "tc_acc_kernel":
+        n2 = K if second_order else ((K - 1) // 2 + 1 + 15) // 16 * 16
+        return 6 * 2 * K + 5 * 2 * n2
+    if kernel == "full_tc_ll_kernel":
+        kx = (D + 1 + 15) // 16 * 16
+        return 6 * 2 * kx * kx
+    return None
+
+
 class FullEm:
     """One EM iteration of a full-covariance GMM over N resident frames."""
     metric = "frames·components/s per EM iter (full covariances)"
@@ -783,9 +800,16 @@ def main():
     if bound == "fp32":  # SIMT FP32 kernels: nominal FMA rate (no measured FP32 peak in the file)
         peak = 152 * 128 * 2 * 2.07e9 / 1e12
         peak_source = "nominal FP32 SIMT: 152 SMs x 128 lanes x 2 flop x 2.07 GHz"
+    # the tensor-core flops the kernel actually issues (split-precision products, padding), beside
+    # the algorithmic ones: how busy the tensor pipe is, where `frac` is how much useful work
+    mma_fc = tc_mma_flop_per_fc(name, args.dim, args.workload in ("ubm-em", "full-em")) if kcnt else None
+    executed = mma_fc * (wl.fc / launches_per_step) / (per_launch_ms / 1e3) / 1e12 if mma_fc else None
     roofline = {"bound": bound, "kernel": name, "achieved": achieved, "peak": peak,
                 "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
                 "algorithmic_flop_per_fc": flop_fc,
+                "mma_flop_per_fc": mma_fc,
+                "executed_tflops": executed,
+                "executed_frac": executed / peak if executed else None,
                 "peak_source": peak_source,
                 "kernel_ms_per_launch": per_launch_ms,
                 "kernel_share": kms / max(1e-9, sum(v[0] for v in prof.values()))}
