@@ -165,9 +165,10 @@ int gmm_read_aux(gmm_handle h, int full, double* aux, double* aux2, double* aux3
 /* Autotuner of the tensor-core statistics kernel (no counterpart in the reference): on the first
  * E-step of a shape (K, component chunks, frame-tile bucket) it times 1, 2 and 3 waves of CTAs
  * and keeps the fastest for the handle's later E-steps. On by default; off = one wave, the fixed
- * decomposition. The decomposition groups the FP64 partial sums, so results with different
- * choices differ only by FP64 rounding. gmm_autotune_choice lists the choices made so far
- * (*n entries; keys and waves up to cap). */
+ * decomposition. The decomposition only groups the partial sums (which frame tiles share an FP32
+ * period, which periods share an FP64 partial), so results with different choices differ only in
+ * the rounding of those sums. gmm_autotune_choice lists the choices made so far (*n entries; keys
+ * and waves up to cap). */
 int gmm_set_autotune(gmm_handle h, int on);
 int gmm_autotune_choice(gmm_handle h, int* n, long long* keys, int* waves, int cap);
 

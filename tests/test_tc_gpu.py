@@ -140,7 +140,8 @@ def test_tc_em_iterate_graph_replays_eager_iterations(glib, golden):
 
 def test_tc_autotune_choice_and_results(glib):
     """The autotuner picks a decomposition once per shape and keeps it; statistics with and
-    without tuning agree to FP64 rounding."""
+    without tuning agree to FP32 rounding: the decomposition decides which frame tiles share an
+    FP32 period (64 tiles from each slice start) before the FP64 partial sums."""
     from gmm_gb300 import synth
     X, w, mu, var = synth.config_em(23, 200_000, 20, 16, 300)
     h = tc_handle(glib)
@@ -155,7 +156,7 @@ def test_tc_autotune_choice_and_results(glib):
     b = h.accumulate()
     h.close()
     for k in ("n", "F", "S"):
-        assert np.allclose(a[k], b[k], rtol=1e-12, atol=1e-9), k
+        assert np.allclose(a[k], b[k], rtol=1e-6, atol=1e-6 * np.abs(b[k]).max()), k
 
 
 @pytest.mark.parametrize("N", [1000, 300_000])
