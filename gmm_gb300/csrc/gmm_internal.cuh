@@ -101,7 +101,7 @@ struct Ctx {
   bool tcx_valid = false;
   double* tcpart = nullptr;  // per-CTA FP64 partial statistics
   size_t tcpart_cap = 0;
-  CUtensorMap tm_zfull, tm_zhalf, tm_wfull, tm_whalf;  // TMA maps over the operand images
+  CUtensorMap tm_zfull, tm_wfull;  // TMA maps over the operand images (box = one 128-row tile)
   int* tc_err = nullptr;                          // bounded-wait expiry flag
   double* tc_llpart = nullptr;                    // per-thread log-likelihood partials
   size_t tc_llpart_cap = 0;

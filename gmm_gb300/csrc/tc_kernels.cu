@@ -1,44 +1,50 @@
 // Tensor-core (tcgen05) E-step for sm_103a.
 //
 // The diagonal-covariance log-likelihood is a contraction:
-//   s_fm = sum_k Z_fk W_km,  Z_f = [x_f, x_f^2, 1, 0...],
-//   W_m  = log2(e) * [mu_m / var_m, -1 / (2 var_m), c_m, 0...],
+//   s_fm = sum_k Z_fk W_km,  Z_f = [x_f | 1 | 0... | x_f^2 | 0...] (x_d at column d, the
+//   constant at D, x_d^2 at K/2 + d), W_m = log2(e) * [mu_m / var_m | c_m | -1 / (2 var_m)],
 //   c_m  = log w_m - D/2 log 2pi - 1/2 sum log var_m - 1/2 sum mu_m^2 / var_m
 // (log2 units), K = 2D+1 padded to a multiple of 16. Z and W are each held as three bf16 planes
 // (v = p1 + p2 + p3, each plane the bf16 rounding of what the previous ones left), and the
-// contraction sums the six plane products p_i q_j with i + j <= 4 into an FP32 TMEM
+// contraction sums the six plane products p_i q_j with i + j <= 2 (0-based) into an FP32 TMEM
 // accumulator: every operand is represented to ~2^-24 relative, so the logits carry FP32-level
 // error from the accumulation alone.
 //
 // Operand planes live in HBM as core-matrix tile images: for each plane and each 128-row tile,
 // [K/8 column chunks][128 rows][8 bf16], i.e. exactly the no-swizzle UMMA layout, contiguous
 // (K x 256 bytes). A tile reaches shared memory in one cp.async.bulk.tensor.2d copy per plane over a
-// [rows][128 elements] view (256-byte rows); 64-row half tiles take one 1 KB copy per column chunk.
+// [rows][128 elements] view (256-byte rows).
 //
-// Two kernels per E-step. Each has one TMA-producer warp, two MMA-issuing threads in warps on
-// different SM sub-partitions and eight epilogue warps (two per TMEM lane quadrant); the MMAs
-// take their A operand from TMEM (tcgen05.mma ... [a_tmem], b_desc), so only B is read from
-// shared memory and the TMA ring keeps shared-memory bandwidth to itself. The tensor pipe accepts
-// only a few MMAs ahead, and an issuing warp shares its sub-partition with busy epilogue warps:
-// two issuers and fully unrolled issue loops (descriptor = per-stage base + constant) keep it fed.
-//   ll_kernel  (frame-tile major, persistent): four loader warps copy the 128-frame Z tile into
-//              TMEM (double-buffered where it fits); 128-component W chunks stream through a
-//              3-stage TMA ring; S[128 frames x 128 comps] accumulates in one of two TMEM
-//              buffers; the epilogue releases each buffer as soon as it has read it and runs an
-//              online log2-sum-exp over all chunks -> per-frame log-likelihood.
-//   acc_kernel (component-chunk major): the chunk's W planes are stored into TMEM once; Z tiles
-//              stream through a 3-deep TMA ring. The MMA computes S^T[128 comps x FT frames];
-//              the epilogue turns it in place into posteriors gamma = 2^(s - ll) (pruned at
-//              minGamma, split into bf16 hi + lo) and the statistics MMA uses those TMEM
-//              columns as its A operand: D2[comps x K] += Gamma^T Z with the five products
-//              hi*Z1 + hi*Z2 + hi*Z3 + lo*Z1 + lo*Z2 (x and x^2 need all three planes: two
-//              leave a 2^-17 relative error that the variance update S/n - mu^2 magnifies), i.e.
-//              the n, F, S statistics in one [x, x^2, 1] product. Posteriors never leave TMEM.
-//              D2 holds one tile's sums: the tensor core's FP32 accumulation over many tiles
-//              loses low bits steadily, so the epilogue reads D2 every tile (one tile late, off
-//              the MMA's critical path), sums tiles in FP32 registers with round-to-nearest and
-//              moves them into FP64 partials every 8192 frames; a final kernel reduces the
-//              partials over CTAs in a fixed order.
+// A tcgen05.mma with M = 128 and K = 16 costs max(45.5, N / 2) cycles on GB300 (measured), so
+// both kernels use N >= 128 for the logits. Two kernels per E-step. Each has one TMA-producer
+// warp, two MMA-issuing threads in warps on different SM sub-partitions and eight epilogue warps
+// (two per TMEM lane quadrant); the logits MMAs take their A operand from TMEM
+// (tcgen05.mma ... [a_tmem], b_desc), so mostly B is read from shared memory. The tensor pipe
+// accepts only a few MMAs ahead, and an issuing warp shares its sub-partition with busy epilogue
+// warps: two issuers and fully unrolled issue loops (descriptor = per-stage base + constant).
+//   ll_kernel  (frame-tile major, persistent): four loader warps fill the 128-frame Z tile in
+//              TMEM -- built from the raw frames (and written to the plane images) on the first
+//              pass for K <= 80, copied from the plane images otherwise -- double-buffered where
+//              it fits; 128-component W chunks stream through a TMA ring; S[128 frames x 128
+//              comps] accumulates in one of two TMEM buffers; the epilogue releases each buffer
+//              as soon as it has read it and runs an online log2-sum-exp over all chunks ->
+//              per-frame log-likelihood.
+//   acc_kernel (component-chunk major, AccCfg: 128-frame tiles, a TMEM plan per K and
+//              statistics width): the chunk's W planes are stored into TMEM once (plane 2 in
+//              shared memory where TMEM is short); Z tiles stream through a TMA ring. The MMA
+//              computes S^T[128 comps x 128 frames]; the epilogue turns it in place into
+//              posteriors gamma = 2^(s - ll) (pruned at minGamma, split into bf16 hi + lo) and
+//              the statistics MMA uses those TMEM columns as its A operand: D2[comps x N2] +=
+//              Gamma^T Z with the five products hi*Z1 + hi*Z2 + hi*Z3 + lo*Z1 + lo*Z2 (x and x^2
+//              need all three planes: two leave a 2^-17 relative error that the variance update
+//              S/n - mu^2 magnifies), i.e. n, F and S in one product (N2 = K), or only the leading
+//              [x | 1] columns when no second-order statistics are wanted. Posteriors never
+//              leave TMEM. An accumulator holds one tile's sums: the tensor core's FP32
+//              accumulation over many tiles loses low bits steadily, so the epilogue reads it
+//              every tile (one tile late, off the MMA's critical path; two accumulators where
+//              TMEM allows, so the next tile's statistics MMAs queue meanwhile), sums tiles in
+//              FP32 registers with round-to-nearest and moves them into FP64 partials every 8192
+//              frames; a final kernel reduces the partials over CTAs in a fixed order.
 // Every mbarrier wait is bounded (~2 s); on expiry the kernel raises an error flag, drains its
 // own copies and MMAs (bounded), frees TMEM and returns.
 #include <cuda.h>
@@ -191,17 +197,10 @@ __device__ __forceinline__ void mbar_drain(uint64_t* bar, uint32_t parity) {
     if (clock64() - t0 > kWaitLimit) break;
 }
 
-// Copy one plane of one tile image into shared memory. half < 0: the whole 128-row image
-// (one copy of K x 256 bytes); half = 0/1: rows [64 half, 64 half + 64) of every column chunk
-// (K/8 copies of 1 KB) into a 64-row image.
-__device__ __forceinline__ void load_image(uint8_t* dst, const CUtensorMap* full, const CUtensorMap* halfm,
-                                           int plane, int nT, int K, int tile, int half, uint64_t* bar) {
-  const int y0 = (plane * nT + tile) * K;
-  if (half < 0) {
-    tma_load_2d(dst, full, 0, y0, bar);
-  } else {
-    for (int c = 0; c < K / 8; ++c) tma_load_2d(dst + c * 1024, halfm, 0, y0 + c * 8 + half * 4, bar);
-  }
+// Copy one plane of one 128-row tile image into shared memory: one copy of K x 256 bytes.
+__device__ __forceinline__ void load_image(uint8_t* dst, const CUtensorMap* map, int plane, int nT, int K, int tile,
+                                           uint64_t* bar) {
+  tma_load_2d(dst, map, 0, (plane * nT + tile) * K, bar);
 }
 
 __device__ __forceinline__ void named_sync(int id, int nthreads) {
@@ -398,7 +397,7 @@ __global__ void __launch_bounds__(kLlThreads, 1)
           mbar_arrive_expect_tx(&w_full[ws], C::W_STAGE);
           uint8_t* dst = smem + C::OFF_W + ws * C::W_STAGE;
           for (int p = 0; p < 3; ++p)
-            load_image(dst + p * C::W_PLANE, &wfull, &wfull, p, nTw, K, wbase + ch, -1, &w_full[ws]);
+            load_image(dst + p * C::W_PLANE, &wfull, p, nTw, K, wbase + ch, &w_full[ws]);
         }
       }
       if (!ok) {  // drain the copies still in flight
@@ -595,7 +594,8 @@ __host__ __device__ constexpr int acc_mean_cols(int K) { return ((K - 1) / 2 + 1
 // shared memory left holds.
 template <int K, bool SO>
 struct AccCfg {
-  static constexpr int FT = 128;
+  static constexpr int FT = acc_ft(K);
+  static_assert(FT == 128, "the epilogue converts two 32-frame chunks per warp");
   static constexpr int N2 = SO ? K : acc_mean_cols(K);
   static constexpr int Z_PLANE = FT * K * 2;
   static constexpr int Z_STAGE = 3 * Z_PLANE;
@@ -720,10 +720,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         mbar_arrive_expect_tx(&z_full[s], C::Z_STAGE + C::LL_STAGE);
         uint8_t* zs = smem + C::OFF_Z + s * C::Z_STAGE;
         const int t = t0 + i;
-        for (int p = 0; p < 3; ++p) {
-          if (FT == 128) load_image(zs + p * C::Z_PLANE, &zmap, &zmap, p, nTz, K, t, -1, &z_full[s]);
-          else load_image(zs + p * C::Z_PLANE, &zmap, &zmap, p, nTz, K, t >> 1, t & 1, &z_full[s]);
-        }
+        for (int p = 0; p < 3; ++p) load_image(zs + p * C::Z_PLANE, &zmap, p, nTz, K, t, &z_full[s]);
         bulk_load(ll_s + s * FT, ll2 + (size_t)t * FT, FT * 4, &z_full[s]);
         issued = i + 1;
       }
@@ -836,7 +833,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       __syncwarp();
       if (lane == 0) mbar_arrive(w_full);
     }
-    constexpr int NCH = FT / 64;         // 32-frame chunks per warp
+    constexpr int NCH = FT / 64;         // 32-frame chunks per warp (2)
     constexpr int KCH = N2 / 16;         // 16-column chunks of the statistics
     constexpr int KH = (KCH + 1) / 2;    // chunks per warp of a pair
     const int kc0 = hf ? KH : 0, kc1 = hf ? KCH : KH;
@@ -941,21 +938,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         tmem_st16(col, hi);
         tmem_st16(col + 16, lo);
-        if (NCH == 2) {
-          tmem_st_wait();
-          tc_fence_before();
-          __syncwarp();
-          if (lane == 0) mbar_arrive(&g_full[2 * b + cc]);
-        }
-      }
-      if (NCH == 1) {  // 64-frame tiles: one pass covers both halves
         tmem_st_wait();
         tc_fence_before();
         __syncwarp();
-        if (lane == 0) {
-          mbar_arrive(&g_full[2 * b]);
-          mbar_arrive(&g_full[2 * b + 1]);
-        }
+        if (lane == 0) mbar_arrive(&g_full[2 * b + cc]);
       }
       if (i > 0 && !readout(i - 1, end_prev, slot_prev)) { ok = false; break; }
     }
@@ -1166,7 +1152,7 @@ int launch_acc_part(Ctx* c, int flags) {
     cudaFuncSetAttribute(acc_kernel<K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, ACm::SMEM);
     attr_set_acc = true;
   }
-  const CUtensorMap& zm = AC::FT == 128 ? c->tm_zfull : c->tm_zhalf;
+  const CUtensorMap& zm = c->tm_zfull;
   const bool so = (flags & GMM_ACC_VAR) != 0;  // second-order statistics
   auto launch_acc = [&](int sl) {
     auto kern = so ? acc_kernel<K, true> : acc_kernel<K, false>;
@@ -1242,7 +1228,6 @@ int tc_prepare_features(Ctx* c) {
   }
   // the logits kernel fills the planes from the features on its first pass over them
   int rc = make_map(c, &c->tm_zfull, c->tcx.planes, 3 * Npad * K, K);
-  if (!rc) rc = make_map(c, &c->tm_zhalf, c->tcx.planes, 3 * Npad * K, 4);
   return rc;
 }
 
@@ -1269,7 +1254,6 @@ int tc_prepare_model(Ctx* c) {
         c->static_shapes ? c->flag + 4 : nullptr);
   }
   int rc = make_map(c, &c->tm_wfull, c->tcm.planes, 3LL * Mpad * K, K);
-  if (!rc) rc = make_map(c, &c->tm_whalf, c->tcm.planes, 3LL * Mpad * K, 4);
   return rc;
 }
 
@@ -1304,7 +1288,6 @@ int tc_estep_streamed(Ctx* c, const float* Xh, int flags, int nchunks) {
     c->tcx.K = K;
   }
   int rc = make_map(c, &c->tm_zfull, c->tcx.planes, 3 * Npad * K, K);
-  if (!rc) rc = make_map(c, &c->tm_zhalf, c->tcx.planes, 3 * Npad * K, 4);
   if (!rc) rc = tc_prepare_model(c);
   if (rc) return rc;
   if (!c->copy_stream) {
@@ -1621,7 +1604,7 @@ int tc_build_model(Ctx* c, int D, int K, int Mact, int Mpad, long long plane_row
 
 namespace {
 template <int K>
-void run_batch_k(Ctx* c, const TcBatch& b, const CUtensorMap& zfull, const CUtensorMap& zhalf) {
+void run_batch_k(Ctx* c, const TcBatch& b, const CUtensorMap& zfull) {
   using LC = LlCfg<K>;
   using AC = AccCfg<K, true>;
   using ACm = AccCfg<K, false>;
@@ -1644,7 +1627,7 @@ void run_batch_k(Ctx* c, const TcBatch& b, const CUtensorMap& zfull, const CUten
   }
   if (b.n_work > 0) {
     GMM_LAUNCH(c, "tc_acc_kernel");
-    const CUtensorMap& zm = AC::FT == 128 ? zfull : zhalf;
+    const CUtensorMap& zm = zfull;
     auto kern = b.second_order ? acc_kernel<K, true> : acc_kernel<K, false>;
     kern<<<b.n_work, kThreads, b.second_order ? AC::SMEM : ACm::SMEM, c->stream>>>(
         zm, b.wplanes, nTz, b.w_chunks_total, b.ll2, (int)(b.Rpad / AC::FT), b.n_chunks, 1, b.tile_slot,
@@ -1656,19 +1639,18 @@ void run_batch_k(Ctx* c, const TcBatch& b, const CUtensorMap& zfull, const CUten
 int tc_run_batch(Ctx* c, const TcBatch& b) {
   if (b.Rpad <= 0) return GMM_OK;
   // the logits kernel builds the feature planes (row map applied) from b.X as it goes
-  CUtensorMap zfull, zhalf;
+  CUtensorMap zfull;
   int rc = make_map(c, &zfull, b.zplanes, 3 * b.Rpad * b.K, b.K);
-  if (!rc) rc = make_map(c, &zhalf, b.zplanes, 3 * b.Rpad * b.K, 4);
   if (rc) return rc;
   switch (b.K) {
-    case 16: run_batch_k<16>(c, b, zfull, zhalf); break;
-    case 32: run_batch_k<32>(c, b, zfull, zhalf); break;
-    case 48: run_batch_k<48>(c, b, zfull, zhalf); break;
-    case 64: run_batch_k<64>(c, b, zfull, zhalf); break;
-    case 80: run_batch_k<80>(c, b, zfull, zhalf); break;
-    case 96: run_batch_k<96>(c, b, zfull, zhalf); break;
-    case 112: run_batch_k<112>(c, b, zfull, zhalf); break;
-    case 128: run_batch_k<128>(c, b, zfull, zhalf); break;
+    case 16: run_batch_k<16>(c, b, zfull); break;
+    case 32: run_batch_k<32>(c, b, zfull); break;
+    case 48: run_batch_k<48>(c, b, zfull); break;
+    case 64: run_batch_k<64>(c, b, zfull); break;
+    case 80: run_batch_k<80>(c, b, zfull); break;
+    case 96: run_batch_k<96>(c, b, zfull); break;
+    case 112: run_batch_k<112>(c, b, zfull); break;
+    case 128: run_batch_k<128>(c, b, zfull); break;
     default: return fail(c, GMM_ERR_UNSUPPORTED, "tensor-core path: unsupported K");
   }
   return GMM_OK;
