@@ -273,11 +273,13 @@ class MapBatch:
         return int(self.X.nbytes), int(self.mu_out.nbytes + self.ll_out.nbytes)
 
     def e2e_step(self):
+        # frames from pinned host memory, copied in chunks of speakers while the E-step runs;
+        # adapted means and speaker log-likelihoods back to the host
         dev = self.dev
-        dev.upload_features(self.Xhost)
         offs = np.ascontiguousarray(self.offs, np.int64)
-        dev.check(dev.lib.gmm_map_batch(dev.h, self.S, offs.ctypes.data, self.a.tau, 0, 1, 0, None,
-                                        self.mu_out.ctypes.data, None, self.ll_out.ctypes.data))
+        dev.check(dev.lib.gmm_map_batch_host(dev.h, self.Xhost.ctypes.data, self.N, self.D, self.S,
+                                             offs.ctypes.data, self.a.tau, 0, 1, 0, None,
+                                             self.mu_out.ctypes.data, None, self.ll_out.ctypes.data))
 
     def cpu_rate(self, seconds, threads):
         """The reference CPU algorithm per speaker (the oracle port: accumulateStatsMT with all
@@ -345,8 +347,11 @@ class MllrBatch:
         return int(self.X.nbytes), int(self.W.nbytes + self.st.nbytes)
 
     def e2e_step(self):
-        self.dev.upload_features(self.Xhost)
-        self.step()
+        # frames from pinned host memory, copied in chunks of speakers while the E-step runs
+        dev = self.dev
+        dev.check(dev.lib.gmm_mllr_batch_host(dev.h, self.Xhost.ctypes.data, self.N, self.D, self.S,
+                                              self.o.ctypes.data, 0, self.W.ctypes.data, self.st.ctypes.data,
+                                              None, None))
 
     def cpu_rate(self, seconds, threads):
         """The reference CPU algorithm per speaker (the oracle port: accumulateStatsMT with all

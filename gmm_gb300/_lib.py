@@ -59,6 +59,8 @@ SIGNATURES = {
     "gmm_map_batch": (_i, [_vp, _i, _vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp]),
     "gmm_map_batch_device": (_i, [_vp, _i, _vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp]),
     "gmm_mllr_batch": (_i, [_vp, _i, _vp, _i, _vp, _vp, _vp, _vp]),
+    "gmm_map_batch_host": (_i, [_vp, _vp, C.c_longlong, _i, _i, _vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp]),
+    "gmm_mllr_batch_host": (_i, [_vp, _vp, C.c_longlong, _i, _i, _vp, _i, _vp, _vp, _vp, _vp]),
     "gmm_mllr_estimate": (_i, [_vp, _i, _vp]),
     "gmm_mllr_apply": (_i, [_vp, _vp]),
     "gmm_profile_enable": (_i, [_vp, _i]),
@@ -393,6 +395,33 @@ class Handle:
         ll = np.zeros(S)
         self.check(self.lib.gmm_mllr_batch(self.h, S, ptr(offs), int(ubm_init), ptr(W), ptr(st),
                                            ptr(mu) if mu is not None else None, ptr(ll)))
+        return W, st, mu, ll
+
+    def map_batch_host(self, X, offs, tau, upW=False, upM=True, upV=False):
+        """map_batch over frames in host memory (X [N, D] becomes the handle's features; on the
+        tensor-core path the copy overlaps the E-step)."""
+        X = np.ascontiguousarray(X, np.float32)
+        offs = np.ascontiguousarray(offs, np.int64)
+        S = len(offs) - 1
+        w = np.zeros((S, self.M), np.float32)
+        mu = np.zeros((S, self.M, self.D), np.float32)
+        var = np.zeros((S, self.M, self.D), np.float32)
+        ll = np.zeros(S)
+        self.check(self.lib.gmm_map_batch_host(self.h, ptr(X), X.shape[0], X.shape[1], S, ptr(offs), int(tau),
+                                               int(upW), int(upM), int(upV), ptr(w), ptr(mu), ptr(var), ptr(ll)))
+        return w, mu, var, ll
+
+    def mllr_batch_host(self, X, offs, ubm_init=False, means=True):
+        """mllr_batch over frames in host memory (as map_batch_host)."""
+        X = np.ascontiguousarray(X, np.float32)
+        offs = np.ascontiguousarray(offs, np.int64)
+        S = len(offs) - 1
+        W = np.zeros((S, self.D, self.D + 1))
+        st = np.zeros(S, np.int32)
+        mu = np.zeros((S, self.M, self.D), np.float32) if means else None
+        ll = np.zeros(S)
+        self.check(self.lib.gmm_mllr_batch_host(self.h, ptr(X), X.shape[0], X.shape[1], S, ptr(offs), int(ubm_init),
+                                                ptr(W), ptr(st), ptr(mu) if mu is not None else None, ptr(ll)))
         return W, st, mu, ll
 
     def em_iterate(self, iters, upW=True, upM=True, upV=True):

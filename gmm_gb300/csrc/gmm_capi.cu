@@ -599,7 +599,7 @@ static int check_speakers(Ctx* c, const char* fn, int S, const long long* offs) 
 }
 
 static int map_batch(Ctx* c, int S, const long long* offs, int tau, int upW, int upM, int upV,
-                     float* w, float* mu, float* var, double* ll, bool dev_out) {
+                     float* w, float* mu, float* var, double* ll, bool dev_out, const float* Xh = nullptr) {
   if (tau < 1) return fail(c, GMM_ERR_ARG, "gmm_map_batch: tau must be >= 1");
   int rc = check_speakers(c, "gmm_map_batch", S, offs);
   if (rc || S == 0) return rc;
@@ -614,6 +614,7 @@ static int map_batch(Ctx* c, int S, const long long* offs, int tau, int upW, int
   b.upV = upV;
   b.flags = (upM ? GMM_ACC_MEAN : 0) | (upV ? GMM_ACC_VAR : 0) | ((upW && !upM && !upV) ? GMM_ACC_PROBS_ONLY : 0);
   b.offs = offs;
+  b.Xh = Xh;
   long long* d_offs = nullptr;
   float *ow = nullptr, *omu = nullptr, *ovar = nullptr;
   double* oll = nullptr;
@@ -656,10 +657,8 @@ int gmm_map_batch_device(gmm_handle h, int S, const long long* offs, int tau, in
   return map_batch(h, S, offs, tau, upW, upM, upV, d_w, d_mu, d_var, d_ll, true);
 }
 
-int gmm_mllr_batch(gmm_handle h, int S, const long long* offs, int ubm_init, double* W, int* status,
-                   float* mu_out, double* ll) {
-  if (!h) return GMM_ERR_ARG;
-  Ctx* c = h;
+static int mllr_batch(Ctx* c, int S, const long long* offs, int ubm_init, double* W, int* status,
+                      float* mu_out, double* ll, const float* Xh) {
   int rc = check_speakers(c, "gmm_mllr_batch", S, offs);
   if (rc || S == 0) return rc;
   const int M = c->M, D = c->D, E = D + 1;
@@ -678,7 +677,7 @@ int gmm_mllr_batch(gmm_handle h, int S, const long long* offs, int ubm_init, dou
     cudaMemcpyAsync(doffs, offs, boffs, cudaMemcpyHostToDevice, c->stream);
     if (c->precision == GMM_PREC_TC) {
       SpeakerStats ss;
-      rc = tc_speaker_stats(c, S, offs, doffs, dll, false, &ss);  // n and F only
+      rc = tc_speaker_stats(c, S, offs, doffs, dll, false, Xh, &ss);  // n and F only
       if (!rc) rc = mstep_mllr_batch(c, S, nullptr, &ss, ubm_init, dW, dst, dmu, nullptr);
       tc_free_speaker_stats(c, &ss);
     } else {
@@ -699,6 +698,61 @@ int gmm_mllr_batch(gmm_handle h, int S, const long long* offs, int ubm_init, dou
   }
   cudaStreamSynchronize(c->stream);
   return rc;
+}
+
+int gmm_mllr_batch(gmm_handle h, int S, const long long* offs, int ubm_init, double* W, int* status,
+                   float* mu_out, double* ll) {
+  if (!h) return GMM_ERR_ARG;
+  return mllr_batch(h, S, offs, ubm_init, W, status, mu_out, ll, nullptr);
+}
+
+// The features of a batched call from host memory. On the tensor-core path the handle's own
+// feature buffer is prepared here and filled by the call's chunked copies (*streamed = true);
+// otherwise the frames are uploaded now.
+static int batch_host_frames(gmm_handle h, const char* what, const float* X, long long N, int D, bool* streamed) {
+  Ctx* c = h;
+  if (!X && N > 0) return fail(c, GMM_ERR_ARG, std::string(what) + ": null array");
+  if (N < 0 || D < 1 || D > kMaxDim) return fail(c, GMM_ERR_ARG, std::string(what) + ": bad N or D");
+  cudaSetDevice(c->device);
+  *streamed = c->precision == GMM_PREC_TC && c->w && D == c->D && tc_supported(D) && N > 0;
+  if (!*streamed) return gmm_upload_features(h, X, N, D);
+  const bool reuse = c->Xown && c->N == N && c->Dx == D && c->ll;
+  if (!reuse) {
+    free_features(c);
+    int rc = dalloc(c, (void**)&c->Xown, sizeof(float) * (size_t)N * D, "features");
+    if (!rc) {
+      c->N = N;
+      c->Dx = D;
+      rc = alloc_frame_buffers(c, N);
+    }
+    if (rc) return rc;
+  }
+  c->X = c->Xown;
+  c->N = N;
+  c->Dx = D;
+  c->tcx_valid = false;
+  c->stats_valid = false;
+  return GMM_OK;
+}
+
+int gmm_map_batch_host(gmm_handle h, const float* X, long long N, int D, int S, const long long* offs, int tau,
+                       int up_weight, int up_mean, int up_var, float* w, float* mu, float* var, double* ll) {
+  if (!h) return GMM_ERR_ARG;
+  Ctx* c = h;
+  bool streamed = false;
+  int rc = batch_host_frames(h, "gmm_map_batch_host", X, N, D, &streamed);
+  if (rc) return rc;
+  return map_batch(c, S, offs, tau, up_weight, up_mean, up_var, w, mu, var, ll, false, streamed ? X : nullptr);
+}
+
+int gmm_mllr_batch_host(gmm_handle h, const float* X, long long N, int D, int S, const long long* offs,
+                        int ubm_init, double* W, int* status, float* mu_out, double* ll) {
+  if (!h) return GMM_ERR_ARG;
+  Ctx* c = h;
+  bool streamed = false;
+  int rc = batch_host_frames(h, "gmm_mllr_batch_host", X, N, D, &streamed);
+  if (rc) return rc;
+  return mllr_batch(c, S, offs, ubm_init, W, status, mu_out, ll, streamed ? X : nullptr);
 }
 
 // File-by-file accumulation (accumulateStatsMT(CFileList&, ...), OL_GMMStatsEstimator.cpp:641-698):

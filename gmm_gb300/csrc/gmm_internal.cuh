@@ -205,10 +205,8 @@ struct MapBatch {
   float* var = nullptr;
   float* aw = nullptr;                // device scratch [S][M]
   double* ll = nullptr;               // device output [S]: per-speaker total log-likelihood
+  const float* Xh = nullptr;          // frames in host memory (null: the resident features)
 };
-// Per-speaker statistics from the tensor-core path: FP64 partials of pieces of at most 8192
-// frames, [piece][chunk][K cols][128 rows] (columns x | x^2 | 1, rows = padded active list);
-// speaker s owns pieces [piece0[s], piece0[s] + npieces[s]), summed in piece order.
 // Columns of the tensor-core operand layout (features Z, model W, statistics partials) of width
 // K = 2D + 1 rounded up to 16 (so K >= 2D + 2): x_d at d, the constant at D, x_d^2 at K/2 + d,
 // zeros elsewhere. The first-order statistics and the count lead, so an E-step without
@@ -234,6 +232,9 @@ int tc_mllr_g(Ctx* c, int S, const double* d_n, double* d_G);
 // Pointer to at least `bytes` of the slot's buffer (grown, contents not kept, when smaller).
 int scratch(Ctx* c, int slot, size_t bytes, const char* what, void** out);
 
+// Per-speaker statistics from the tensor-core path: FP64 partials of pieces of at most 8192
+// frames, [piece][chunk][K cols][128 rows] (operand-layout columns, tc_stat_col; rows = padded
+// active list); speaker s owns pieces [piece0[s], piece0[s] + npieces[s]), summed in piece order.
 struct SpeakerStats {
   int S = 0, n_chunks = 0, K = 0, pieces = 0;
   double* part = nullptr;
@@ -242,8 +243,11 @@ struct SpeakerStats {
   int* row_of_comp = nullptr;  // [M], -1 for inactive components
   size_t part_bytes = 0;
 };
+// Xh: the frames in host memory (copied into the handle's feature buffer chunk by chunk, the
+// copies overlapping the logits kernels), or null for the resident features.
 int tc_speaker_stats(Ctx* c, int S, const long long* offs, const long long* d_offs, double* d_ll,
-                     bool second_order, SpeakerStats* ss);
+                     bool second_order, const float* Xh, SpeakerStats* ss);
+int ensure_copy_stream(Ctx* c, int n_events);
 void tc_free_speaker_stats(Ctx* c, SpeakerStats* ss);
 // Per-speaker statistics from the plain path: [speaker][n (M) | F (M x D) | S (M x D) | totLL | pad]
 // MAP update for all speakers from either form (exactly one of plain / ss is non-null).
@@ -290,6 +294,7 @@ int tc_stats_ft(int K);  // frames per statistics tile for K
 int tc_flush_tiles(int K);  // statistics tiles per FP64 flush
 int tc_k(int D);
 int tc_run_batch(Ctx* c, const TcBatch& b);
+int tc_run_batch_part(Ctx* c, const TcBatch& b, int tile0, int ntl, int stages);
 int tc_make_wmap(Ctx* c, CUtensorMap* map, const uint16_t* planes, long long rows, int K);
 int tc_build_model(Ctx* c, int D, int K, int Mact, int Mpad, long long plane_rows, long long row0,
                    const int* act, const float* w, const float* mu, const float* var,

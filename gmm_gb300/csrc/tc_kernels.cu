@@ -1262,6 +1262,20 @@ int tc_prepare_model(Ctx* c) {
 // tiles start as soon as its copy lands, so the transfer hides behind the logits kernels; the
 // statistics kernel then runs over all tiles. c->X must be the handle's own device buffer of
 // c->N x c->D floats; Xh is the host block (page-locked for the copies to overlap).
+int ensure_copy_stream(Ctx* c, int n_events) {
+  if (!c->copy_stream) {
+    cudaError_t e = cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamCreate(copy)");
+  }
+  while ((int)c->copy_events.size() < n_events) {
+    cudaEvent_t ev;
+    cudaError_t e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaEventCreate");
+    c->copy_events.push_back(ev);
+  }
+  return GMM_OK;
+}
+
 int tc_estep_streamed(Ctx* c, const float* Xh, int flags, int nchunks) {
   if (!tc_supported(c->D)) return fail(c, GMM_ERR_UNSUPPORTED, "tensor-core path supports 1 <= D <= 63");
   if (c->N == 0) return GMM_OK;
@@ -1412,7 +1426,7 @@ int tc_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
 // its own FP64 slot, and the statistics kernel runs over work items (component chunk x range of
 // whole pieces) of about equal size. A speaker's sums are the piece slots added in piece order.
 int tc_speaker_stats(Ctx* c, int S, const long long* offs, const long long* d_offs, double* d_ll,
-                     bool second_order, SpeakerStats* ss) {
+                     bool second_order, const float* Xh, SpeakerStats* ss) {
   *ss = SpeakerStats();
   if (!tc_supported(c->D)) return fail(c, GMM_ERR_UNSUPPORTED, "tensor-core path supports 1 <= D <= 63");
   if (!d_offs) return fail(c, GMM_ERR_ARG, "per-speaker statistics: device speaker offsets missing");
@@ -1545,7 +1559,46 @@ int tc_speaker_stats(Ctx* c, int S, const long long* offs, const long long* d_of
     t.part = ss->part;
     t.single_comp = c->Mact == 1;
     t.second_order = second_order;
-    rc = tc_run_batch(c, t);
+    if (!Xh) {
+      rc = tc_run_batch(c, t);
+    } else {
+      // Frames from host memory: copied in chunks of whole speakers on the copy stream (the first
+      // chunks growing geometrically from 1/64 of the frames, then 1/8), each chunk's rows going
+      // through the logits kernel as soon as its frames land; then the statistics.
+      const long long f_all = offs[S] - offs[0];
+      const long long steady = std::max(1LL, (f_all + 7) / 8);
+      std::vector<int> cuts{0};  // chunk boundaries (speaker indices)
+      for (long long target = std::max(1LL, steady / 8); cuts.back() < S; target = std::min(steady, 2 * target)) {
+        int sb = cuts.back() + 1;
+        while (sb < S && offs[sb] - offs[cuts.back()] < target) ++sb;
+        cuts.push_back(sb);
+      }
+      rc = ensure_copy_stream(c, (int)cuts.size());
+      int k = 0;
+      if (!rc) {
+        cudaEventRecord(c->copy_events[k], c->stream);  // frames a previous call may still read
+        cudaStreamWaitEvent(c->copy_stream, c->copy_events[k], 0);
+        ++k;
+      }
+      for (size_t ci = 0; !rc && ci + 1 < cuts.size(); ++ci) {
+        const int sa = cuts[ci], sb = cuts[ci + 1];
+        const long long fa = offs[sa], fb = offs[sb];
+        if (fb > fa) {
+          cudaError_t e = cudaMemcpyAsync(const_cast<float*>(c->X) + fa * c->D, Xh + fa * c->D,
+                                          sizeof(float) * (size_t)(fb - fa) * c->D, cudaMemcpyHostToDevice,
+                                          c->copy_stream);
+          if (e != cudaSuccess) rc = cuda_fail(c, e, "cudaMemcpyAsync(speaker frames)");
+        }
+        if (!rc) {
+          cudaEventRecord(c->copy_events[k], c->copy_stream);
+          cudaStreamWaitEvent(c->stream, c->copy_events[k], 0);
+          ++k;
+          const int ta = (int)(pad[sa] / 128), tb = (int)(pad[sb] / 128);
+          if (tb > ta) rc = tc_run_batch_part(c, t, ta, tb - ta, 1);
+        }
+      }
+      if (!rc) rc = tc_run_batch_part(c, t, 0, (int)(Rpad / 128), 2);
+    }
   }
   if (!rc) {
     {
@@ -1574,7 +1627,7 @@ void tc_free_speaker_stats(Ctx*, SpeakerStats* ss) { *ss = SpeakerStats(); }
 
 int tc_map_batch(Ctx* c, const MapBatch& b) {
   SpeakerStats ss;
-  int rc = tc_speaker_stats(c, b.S, b.offs, b.d_offs, b.ll, b.upV != 0, &ss);
+  int rc = tc_speaker_stats(c, b.S, b.offs, b.d_offs, b.ll, b.upV != 0, b.Xh, &ss);
   if (rc) return rc;
   rc = mstep_map_batch(c, b, nullptr, &ss);
   if (!rc) rc = sync(c, "batched MAP update");
@@ -1604,28 +1657,31 @@ int tc_build_model(Ctx* c, int D, int K, int Mact, int Mpad, long long plane_row
 
 namespace {
 template <int K>
-void run_batch_k(Ctx* c, const TcBatch& b, const CUtensorMap& zfull) {
+// stages: 1 = feature planes and logits of the row tiles [tile0, tile0 + ntl), 2 = statistics of
+// the whole batch
+void run_batch_k(Ctx* c, const TcBatch& b, const CUtensorMap& zfull, int tile0, int ntl, int stages) {
   using LC = LlCfg<K>;
   using AC = AccCfg<K, true>;
   using ACm = AccCfg<K, false>;
   const int nTz = (int)(b.Rpad / 128);
-  const int grid_ll = std::max(1, std::min(nTz, c->sms));
+  const int grid_ll = std::max(1, std::min(ntl, c->sms));
   cudaFuncSetAttribute(ll_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, LC::SMEM);
   cudaFuncSetAttribute(acc_kernel<K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, AC::SMEM);
   cudaFuncSetAttribute(acc_kernel<K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, ACm::SMEM);
-  if (!ll_builds_planes(K)) {
+  if ((stages & 1) && ntl > 0 && !ll_builds_planes(K)) {
     GMM_LAUNCH(c, "tc_features_kernel");
-    features_kernel<<<(unsigned)((b.Rpad * (K / 8) + 255) / 256), 256, 0, c->stream>>>(
-        b.X, b.N, b.Rpad / 128, b.D, K, b.row_frame, b.zplanes, 0, b.Rpad * (K / 8));
+    const long long t0 = (long long)tile0 * 128 * (K / 8), t1 = (long long)(tile0 + ntl) * 128 * (K / 8);
+    features_kernel<<<(unsigned)((t1 - t0 + 255) / 256), 256, 0, c->stream>>>(
+        b.X, b.N, b.Rpad / 128, b.D, K, b.row_frame, b.zplanes, t0, t1);
   }
-  {
+  if ((stages & 1) && ntl > 0) {
     GMM_LAUNCH(c, "tc_ll_kernel");
     ll_kernel<K><<<grid_ll, kLlThreads, LC::SMEM, c->stream>>>(
-        *b.wmap, b.zplanes, b.N, b.row_frame, b.tile_wbase, nTz, b.w_chunks_total, 0, nTz, b.n_chunks,
+        *b.wmap, b.zplanes, b.N, b.row_frame, b.tile_wbase, nTz, b.w_chunks_total, tile0, ntl, b.n_chunks,
         (float)(c->minLL * kLog2e), c->minLL, b.ll2, b.ll, b.llpart, c->tc_err,
         ll_builds_planes(K) ? b.X : nullptr, b.D);
   }
-  if (b.n_work > 0) {
+  if ((stages & 2) && b.n_work > 0) {
     GMM_LAUNCH(c, "tc_acc_kernel");
     const CUtensorMap& zm = zfull;
     auto kern = b.second_order ? acc_kernel<K, true> : acc_kernel<K, false>;
@@ -1636,24 +1692,26 @@ void run_batch_k(Ctx* c, const TcBatch& b, const CUtensorMap& zfull) {
 }
 }  // namespace
 
-int tc_run_batch(Ctx* c, const TcBatch& b) {
+int tc_run_batch_part(Ctx* c, const TcBatch& b, int tile0, int ntl, int stages) {
   if (b.Rpad <= 0) return GMM_OK;
   // the logits kernel builds the feature planes (row map applied) from b.X as it goes
   CUtensorMap zfull;
   int rc = make_map(c, &zfull, b.zplanes, 3 * b.Rpad * b.K, b.K);
   if (rc) return rc;
   switch (b.K) {
-    case 16: run_batch_k<16>(c, b, zfull); break;
-    case 32: run_batch_k<32>(c, b, zfull); break;
-    case 48: run_batch_k<48>(c, b, zfull); break;
-    case 64: run_batch_k<64>(c, b, zfull); break;
-    case 80: run_batch_k<80>(c, b, zfull); break;
-    case 96: run_batch_k<96>(c, b, zfull); break;
-    case 112: run_batch_k<112>(c, b, zfull); break;
-    case 128: run_batch_k<128>(c, b, zfull); break;
+    case 16: run_batch_k<16>(c, b, zfull, tile0, ntl, stages); break;
+    case 32: run_batch_k<32>(c, b, zfull, tile0, ntl, stages); break;
+    case 48: run_batch_k<48>(c, b, zfull, tile0, ntl, stages); break;
+    case 64: run_batch_k<64>(c, b, zfull, tile0, ntl, stages); break;
+    case 80: run_batch_k<80>(c, b, zfull, tile0, ntl, stages); break;
+    case 96: run_batch_k<96>(c, b, zfull, tile0, ntl, stages); break;
+    case 112: run_batch_k<112>(c, b, zfull, tile0, ntl, stages); break;
+    case 128: run_batch_k<128>(c, b, zfull, tile0, ntl, stages); break;
     default: return fail(c, GMM_ERR_UNSUPPORTED, "tensor-core path: unsupported K");
   }
   return GMM_OK;
 }
+
+int tc_run_batch(Ctx* c, const TcBatch& b) { return tc_run_batch_part(c, b, 0, (int)(b.Rpad / 128), 3); }
 
 }  // namespace gmm

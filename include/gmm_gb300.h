@@ -208,6 +208,16 @@ int gmm_map_batch(gmm_handle h, int S, const long long* offs, int tau, int up_we
  * adapted means, ll [S]. */
 int gmm_mllr_batch(gmm_handle h, int S, const long long* offs, int ubm_init, double* W, int* status,
                    float* mu_out, double* ll);
+/* gmm_map_batch / gmm_mllr_batch over frames in host memory: X [N][D] becomes the handle's
+ * features (as gmm_upload_features would make it). On the tensor-core path the frames are copied
+ * in chunks of whole speakers on a second stream and each chunk's log-likelihood kernels start
+ * as soon as its frames have landed, so the transfer overlaps the E-step (page-locked X lets the
+ * copies run asynchronously); otherwise the frames are uploaded first. Results are those of
+ * gmm_upload_features + gmm_map_batch / gmm_mllr_batch. */
+int gmm_map_batch_host(gmm_handle h, const float* X, long long N, int D, int S, const long long* offs, int tau,
+                       int up_weight, int up_mean, int up_var, float* w, float* mu, float* var, double* ll);
+int gmm_mllr_batch_host(gmm_handle h, const float* X, long long N, int D, int S, const long long* offs,
+                        int ubm_init, double* W, int* status, float* mu_out, double* ll);
 /* The same with device outputs (d_w, d_mu, d_var, d_ll on the handle's device; any may be NULL). */
 int gmm_map_batch_device(gmm_handle h, int S, const long long* offs, int tau, int up_weight,
                          int up_mean, int up_var, float* d_w, float* d_mu, float* d_var,

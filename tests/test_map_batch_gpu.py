@@ -170,3 +170,32 @@ def test_batch_scratch_reuse_across_sizes(glib):
         f.close()
         for x, y in zip(got, want):
             assert np.array_equal(x, y), c[0]
+
+
+@pytest.mark.parametrize("D", [60, 24])
+def test_batch_host_frames_match_resident(glib, D):
+    """gmm_map_batch_host / gmm_mllr_batch_host (frames copied in chunks of whole speakers, each
+    chunk's log-likelihood kernels starting when its frames land) give the results of
+    gmm_upload_features + the resident-frame calls, bit for bit. D = 60 builds the feature planes
+    in a separate pass (K = 128), D = 24 inside the logits kernel (K = 64)."""
+    X, offs, ubm = workload(D=D, seed=58)
+    h = glib.Handle(0)
+    h.set_precision(glib.PREC_TC)
+    h.upload_model(*ubm)
+    h.upload_features(X)
+    a = h.map_batch(offs, 16, 1, 1, 1)
+    m = h.mllr_batch(offs)
+    h.close()
+    g = glib.Handle(0)
+    g.set_precision(glib.PREC_TC)
+    g.upload_model(*ubm)
+    b = g.map_batch_host(X, offs, 16, 1, 1, 1)
+    n = g.mllr_batch_host(X, offs)
+    b2 = g.map_batch_host(X, offs, 16, 1, 1, 1)  # again on the same handle: buffers reused
+    g.close()
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+    for x, y in zip(a, b2):
+        assert np.array_equal(x, y)
+    for x, y in zip(m, n):
+        assert np.array_equal(x, y)
