@@ -219,6 +219,16 @@ __host__ __device__ inline int tc_mean_cols(int D) { return (D + 1 + 15) / 16 * 
 // (e < D: F_e, D <= e < 2D: S_(e-D), e = 2D: n).
 __host__ __device__ inline int tc_stat_col(int D, int K, int e) { return e < D ? e : e == 2 * D ? D : K / 2 + (e - D); }
 
+// x / d correctly rounded, given r = RN(1 / d) (__drcp_rn): q = RN(x r), the remainder x - d q
+// exactly by FMA, then RN(q + remainder r) is RN(x / d) for normal operands (Markstein's theorem).
+// Two FMAs and a product instead of a division, where many quotients share one divisor: GB300
+// runs FP64 at 1/64 of its FP32 rate and a division is an order of magnitude more FP64 work.
+__device__ __forceinline__ double div_by_rcp(double x, double d, double r) {
+  const double q = __dmul_rn(x, r);
+  const double e = __fma_rn(-d, q, x);
+  return __fma_rn(e, r, q);
+}
+
 // Slots of Ctx::scratch
 enum ScratchSlot {
   SC_OFFS, SC_AW, SC_W, SC_MU, SC_VAR, SC_LL, SC_ROWMAP, SC_TILESLOT, SC_WORK, SC_PAD, SC_PART,

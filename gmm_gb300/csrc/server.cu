@@ -111,15 +111,16 @@ __global__ void srv_map_kernel(int R, int M, int D, int K, int n_chunks, const i
     ow[t] = wset ? aw : uwm;
     adapted_w[t] = aw;
   }
+  const double rmp = adapt ? __drcp_rn(mp) : 0.0;  // the D quotients below share the divisor mp
   for (int k = lane; k < D; k += 32) {
     float am = um[k], av = uv[k];
     if (adapt && (upM || upV)) {
-      const double a1 = __ddiv_rn(__dmul_rn(alfa, col(k)), mp);
+      const double a1 = gmm::div_by_rcp(__dmul_rn(alfa, col(k)), mp, rmp);
       am = (float)__dadd_rn(a1, __dmul_rn(one_m, (double)um[k]));
       if (upV) {
         const float second = __fadd_rn(uv[k], __fmul_rn(um[k], um[k]));
         const float msq = __fmul_rn(am, am);
-        const double b1 = __ddiv_rn(__dmul_rn(alfa, col(tc_col_sq(K, k))), mp);
+        const double b1 = gmm::div_by_rcp(__dmul_rn(alfa, col(tc_col_sq(K, k))), mp, rmp);
         const double b2 = __dadd_rn(b1, __dmul_rn(one_m, (double)second));
         av = (float)__dsub_rn(b2, (double)msq);
         if (av < min_var) av = min_var;
