@@ -294,79 +294,90 @@ __global__ void mllr_apply_kernel(int M, int D, float* __restrict__ mu, const do
 // CModelAdapt::UpdateModelMAP (OL_ModelAdapt.cpp:1024-1099) for every (speaker, component),
 // with the resident model as both the starting point and the prior: AdaptModelMAP copies the UBM
 // (:1259-1260) and the first MAP iteration adapts that copy towards the statistics. Same
-// expression order as map_comp_kernel. One warp per (speaker, component), lanes over the
-// dimensions (coalesced rows). Statistics come in one of two layouts (kStatsSlots /
-// kStatsPlain); in the plain layout the speaker's total log-likelihood is copied out as well.
-__global__ void map_batch_kernel(int S, int M, int D, const double* __restrict__ plain,
-                                 const double* __restrict__ part, int K, int n_chunks,
-                                 const int* __restrict__ piece0, const int* __restrict__ npieces,
-                                 const int* __restrict__ row_of_comp,
-                                 const long long* __restrict__ offs, const float* __restrict__ uw,
-                                 const float* __restrict__ umu, const float* __restrict__ uvar,
-                                 int tau, int upW, int upM, int upV, float min_var,
-                                 float* __restrict__ ow, float* __restrict__ omu,
-                                 float* __restrict__ ovar, float* __restrict__ adapted_w,
-                                 double* __restrict__ ll) {
-  const long long t = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (t >= (long long)S * M) return;
-  const int s = (int)(t / M), m = (int)(t - (long long)s * M);
-  const float* um = umu + (size_t)m * D;
-  const float* uv = uvar + (size_t)m * D;
-  float* om = omu ? omu + (size_t)t * D : nullptr;
-  float* ov = ovar ? ovar + (size_t)t * D : nullptr;
-  // statistic e (n / F / S order; columns x | 1 | x^2 of the tensor-core partials) of component
-  // m for speaker s
-  const int row = plain ? 0 : row_of_comp[m];
-  const double* pst = plain ? plain + (size_t)s * ((size_t)M * (1 + 2 * D) + 2) : nullptr;
-  if (plain && m == 0 && lane == 0) ll[s] = pst[(size_t)M * (1 + 2 * D)];
-  auto stat = [&](int e) -> double {  // e in [0, 2D]: F_k = e < D, S_k = D + k, n = 2D
-    if (plain) {
-      if (e == 2 * D) return pst[m];
-      if (e < D) return pst[M + (size_t)m * D + e];
-      return pst[M + (size_t)M * D + (size_t)m * D + (e - D)];
-    }
-    if (row < 0) return 0.0;  // inactive components were never accumulated
-    double v = 0.0;
-    const int col = tc_stat_col(D, K, e);
-    for (int p = 0; p < npieces[s]; ++p) {
-      const double x = part[((size_t)(piece0[s] + p) * n_chunks + row / 128) * K * 128 + (size_t)col * 128 + (row % 128)];
-      v = p == 0 ? x : __dadd_rn(v, x);
-    }
-    return v;
-  };
-  const double mp = stat(2 * D);
-  const bool adapt = uw[m] != 0.0f && mp > 0.0;
-  const unsigned int tot = (unsigned int)(offs[s + 1] - offs[s]);
-  const double alfa = adapt ? __ddiv_rn(mp, __dadd_rn(mp, (double)tau)) : 0.0;
-  const double one_m = __dsub_rn(1.0, alfa);
-  if (lane == 0) {
-    float aw = 0.0f;
-    const bool wset = adapt && upW && tot > 0;
-    if (wset) {
-      const double t1 = __dmul_rn(alfa, __ddiv_rn(mp, (double)tot));
-      aw = (float)__dadd_rn(t1, __dmul_rn(one_m, (double)uw[m]));
-    }
-    ow[t] = wset ? aw : uw[m];
-    adapted_w[t] = aw;
-  }
-  const double rmp = adapt ? __drcp_rn(mp) : 0.0;  // the D quotients below share the divisor mp
-  for (int k = lane; k < D; k += 32) {
-    float am = um[k], av = uv[k];
-    if (adapt && (upM || upV)) {
-      const double a1 = div_by_rcp(__dmul_rn(alfa, stat(k)), mp, rmp);
-      am = (float)__dadd_rn(a1, __dmul_rn(one_m, (double)um[k]));
-      if (upV) {
-        const float second = __fadd_rn(uv[k], __fmul_rn(um[k], um[k]));
-        const float msq = __fmul_rn(am, am);
-        const double b1 = div_by_rcp(__dmul_rn(alfa, stat(D + k)), mp, rmp);
-        const double b2 = __dadd_rn(b1, __dmul_rn(one_m, (double)second));
-        av = (float)__dsub_rn(b2, (double)msq);
-        if (av < min_var) av = min_var;
+// expression order as map_comp_kernel. One thread per (speaker, component) (see below).
+// Statistics come in one of two layouts (kStatsSlots / kStatsPlain); in the plain layout the
+// speaker's total log-likelihood is copied out as well.
+constexpr int kMapThreads = 64;  // (speaker, component) pairs per block
+__global__ void __launch_bounds__(kMapThreads) map_batch_kernel(
+    int S, int M, int D, const double* __restrict__ plain, const double* __restrict__ part, int K, int n_chunks,
+    const int* __restrict__ piece0, const int* __restrict__ npieces, const int* __restrict__ row_of_comp,
+    const long long* __restrict__ offs, const float* __restrict__ uw, const float* __restrict__ umu,
+    const float* __restrict__ uvar, int tau, int upW, int upM, int upV, float min_var, float* __restrict__ ow,
+    float* __restrict__ omu, float* __restrict__ ovar, float* __restrict__ adapted_w, double* __restrict__ ll) {
+  // thread = (speaker, component) pair t = s M + m: the partials of consecutive components are
+  // consecutive rows (coalesced reads); the block's means and variances are staged in shared
+  // memory ([pair][D + 1], an odd stride) and written out as one contiguous range.
+  extern __shared__ float s_out[];
+  const int SD = D + 1;
+  float* s_mu = s_out;
+  float* s_var = s_out + kMapThreads * SD;
+  const long long tot_pairs = (long long)S * M;
+  const long long t0 = (long long)blockIdx.x * kMapThreads, t = t0 + threadIdx.x;
+  if (t < tot_pairs) {
+    const int s = (int)(t / M), m = (int)(t - (long long)s * M);
+    const float* um = umu + (size_t)m * D;
+    const float* uv = uvar + (size_t)m * D;
+    // statistic e (n / F / S order; operand-layout columns of the tensor-core partials) of
+    // component m for speaker s
+    const int row = plain ? 0 : row_of_comp[m];
+    const double* pst = plain ? plain + (size_t)s * ((size_t)M * (1 + 2 * D) + 2) : nullptr;
+    if (plain && m == 0) ll[s] = pst[(size_t)M * (1 + 2 * D)];
+    const int np = plain ? 0 : npieces[s], p0 = plain ? 0 : piece0[s];
+    auto stat = [&](int e) -> double {  // e in [0, 2D]: F_k = e < D, S_k = D + k, n = 2D
+      if (plain) {
+        if (e == 2 * D) return pst[m];
+        if (e < D) return pst[M + (size_t)m * D + e];
+        return pst[M + (size_t)M * D + (size_t)m * D + (e - D)];
       }
+      if (row < 0) return 0.0;  // inactive components were never accumulated
+      double v = 0.0;
+      const int col = tc_stat_col(D, K, e);
+      for (int p = 0; p < np; ++p) {
+        const double x = part[((size_t)(p0 + p) * n_chunks + row / 128) * K * 128 + (size_t)col * 128 + (row % 128)];
+        v = p == 0 ? x : __dadd_rn(v, x);
+      }
+      return v;
+    };
+    const double mp = stat(2 * D);
+    const bool adapt = uw[m] != 0.0f && mp > 0.0;
+    const unsigned int tot = (unsigned int)(offs[s + 1] - offs[s]);
+    const double alfa = adapt ? __ddiv_rn(mp, __dadd_rn(mp, (double)tau)) : 0.0;
+    const double one_m = __dsub_rn(1.0, alfa);
+    {
+      float aw = 0.0f;
+      const bool wset = adapt && upW && tot > 0;
+      if (wset) {
+        const double t1 = __dmul_rn(alfa, __ddiv_rn(mp, (double)tot));
+        aw = (float)__dadd_rn(t1, __dmul_rn(one_m, (double)uw[m]));
+      }
+      ow[t] = wset ? aw : uw[m];
+      adapted_w[t] = aw;
     }
-    if (om) om[k] = am;
-    if (ov) ov[k] = av;
+    const double rmp = adapt ? __drcp_rn(mp) : 0.0;  // the D quotients below share the divisor mp
+    for (int k = 0; k < D; ++k) {
+      float am = um[k], av = uv[k];
+      if (adapt && (upM || upV)) {
+        const double a1 = div_by_rcp(__dmul_rn(alfa, stat(k)), mp, rmp);
+        am = (float)__dadd_rn(a1, __dmul_rn(one_m, (double)um[k]));
+        if (upV) {
+          const float second = __fadd_rn(uv[k], __fmul_rn(um[k], um[k]));
+          const float msq = __fmul_rn(am, am);
+          const double b1 = div_by_rcp(__dmul_rn(alfa, stat(D + k)), mp, rmp);
+          const double b2 = __dadd_rn(b1, __dmul_rn(one_m, (double)second));
+          av = (float)__dsub_rn(b2, (double)msq);
+          if (av < min_var) av = min_var;
+        }
+      }
+      s_mu[threadIdx.x * SD + k] = am;
+      s_var[threadIdx.x * SD + k] = av;
+    }
+  }
+  __syncthreads();
+  const long long n_here = tot_pairs - t0 < kMapThreads ? tot_pairs - t0 : kMapThreads;
+  for (int i = threadIdx.x; i < n_here * D; i += kMapThreads) {
+    const int j = i / D, k = i - j * D;
+    if (omu) omu[(size_t)t0 * D + i] = s_mu[j * SD + k];
+    if (ovar) ovar[(size_t)t0 * D + i] = s_var[j * SD + k];
   }
 }
 
@@ -807,7 +818,9 @@ int mstep_map_batch(Ctx* c, const MapBatch& b, const double* plain, const Speake
   if (tot == 0) return GMM_OK;
   {
     GMM_LAUNCH(c, "map_batch_kernel");
-    map_batch_kernel<<<(unsigned)((tot + 7) / 8), 256, 0, c->stream>>>(
+    const size_t smem = sizeof(float) * 2 * kMapThreads * (size_t)(c->D + 1);
+    cudaFuncSetAttribute(map_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    map_batch_kernel<<<(unsigned)((tot + kMapThreads - 1) / kMapThreads), kMapThreads, smem, c->stream>>>(
         b.S, c->M, c->D, plain, ss ? ss->part : nullptr, ss ? ss->K : 0, ss ? ss->n_chunks : 0,
         ss ? ss->piece0 : nullptr, ss ? ss->npieces : nullptr, ss ? ss->row_of_comp : nullptr, b.d_offs,
         c->w, c->mu, c->var, b.tau, b.upW, b.upM, b.upV, c->min_var, b.w, b.mu, b.var, b.aw, b.ll);
