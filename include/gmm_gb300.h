@@ -200,9 +200,8 @@ int gmm_map_batch(gmm_handle h, int S, const long long* offs, int tau, int up_we
  * resident model is the UBM. The G and k sums over components run as GEMMs with FP32 products
  * (G on the tensor cores under GMM_PREC_TC, split-bf16 operands) and sums in FP32 per 128
  * components, added in FP64 (GMM_PREC_FP32) or in FP32 with round-to-nearest (GMM_PREC_TC); the
- * single-speaker gmm_mllr_estimate keeps the reference's FP64 sequence. Each row is solved by
- * the elimination order of the reference's pivot-free Gauss-Jordan inverse in double-float
- * arithmetic (about 2^-48 relative per operation; GB300's FP64 rate is 1/64 of FP32). Outputs (host, any
+ * single-speaker gmm_mllr_estimate keeps the reference's FP64 sequence. Each row is solved in
+ * FP64 by the elimination order of the reference's pivot-free Gauss-Jordan inverse. Outputs (host, any
  * may be NULL): W [S][D][D+1] row-major, status [S] (GMM_OK or GMM_ERR_MLLR when the speaker has
  * too few components or frames; its W is zero and its means stay the UBM's), mu_out [S][M][D]
  * adapted means, ll [S]. */
