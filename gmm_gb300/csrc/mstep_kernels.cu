@@ -546,6 +546,102 @@ __global__ void __launch_bounds__(256) mllr_gemm_kernel(int S, int M, int D, int
   }
 }
 
+// The k data term of ComputeKiGi_MLLR (OL_ModelAdapt.cpp:1525-1581) for all speakers:
+// k[s][i][a] = sum_m (F[s][m][i] / var[m][i]) xi[m][a], with the operands and sums of
+// mllr_gemm_kernel (coef * 1/var rounded to float, FP32 fused multiply-adds over 128 components
+// in order, added into FP64), so the result is bit-identical to it. One block per speaker: the
+// speaker's F rows are read once, contiguously, in chunks of 32 components, each chunk's loads
+// issued before the multiply-adds of the previous one (a block is alone on its SM at C4 sizes,
+// so nothing else hides the memory latency); a thread owns a 4 x 4 tile of (i, a).
+constexpr int kMllrKChunk = 32, kMllrKPf = 10;  // components per chunk, loads per thread per chunk
+__host__ inline int mllr_k_threads(int D) {
+  const int E = D + 1, owners = ((D + 3) / 4) * ((E + 3) / 4);
+  const int loads = (kMllrKChunk * ((E + 3) / 4) * 4 + kMllrKPf - 1) / kMllrKPf;
+  const int t = owners > loads ? owners : loads;
+  return t > 64 ? (t + 31) / 32 * 32 : 64;
+}
+__global__ void mllr_k_kernel(int S, int M, int D, const double* __restrict__ F, const float* __restrict__ var,
+                              const float* __restrict__ Xi, double* __restrict__ kd) {
+  extern __shared__ __align__(16) float sm_k[];
+  const int E = D + 1, TI = (D + 3) / 4, TA = (E + 3) / 4, D4 = TI * 4, E4 = TA * 4;
+  const int ny = kMllrKChunk * D4, nx = kMllrKChunk * E4;
+  float* Ys = sm_k;       // [32][D4]
+  float* Xs = sm_k + ny;  // [32][E4]
+  const int s = blockIdx.x;
+  const int t = threadIdx.x, ti = t / TA, ta = t - ti * TA;
+  const bool owner = t < TI * TA;
+  const double* Fs = F + (size_t)s * M * D;
+  double fy[kMllrKPf];
+  float vy[kMllrKPf], xx[kMllrKPf];
+  auto fetch = [&](int m0) {
+#pragma unroll
+    for (int j = 0; j < kMllrKPf; ++j) {
+      const int e = t + j * (int)blockDim.x;
+      fy[j] = 0.0;
+      vy[j] = 1.0f;
+      xx[j] = 0.0f;
+      if (e < ny) {
+        const int mm = e / D4, i = e - mm * D4, m = m0 + mm;
+        if (m < M && i < D) {
+          fy[j] = Fs[(size_t)m * D + i];
+          vy[j] = var[(size_t)m * D + i];
+        }
+      }
+      if (e < nx) {
+        const int mm = e / E4, a = e - mm * E4, m = m0 + mm;
+        if (m < M && a < E) xx[j] = Xi[(size_t)m * E + a];
+      }
+    }
+  };
+  float acc[4][4];
+  double dacc[4][4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) { acc[u][v] = 0.0f; dacc[u][v] = 0.0; }
+  fetch(0);
+  for (int m0 = 0; m0 < M; m0 += kMllrKChunk) {
+#pragma unroll
+    for (int j = 0; j < kMllrKPf; ++j) {
+      const int e = t + j * (int)blockDim.x;
+      if (e < ny) Ys[e] = __fmul_rn((float)fy[j], __frcp_rn(vy[j]));  // padding: 0 * 1 = 0
+      if (e < nx) Xs[e] = xx[j];
+    }
+    __syncthreads();
+    if (m0 + kMllrKChunk < M) fetch(m0 + kMllrKChunk);
+    if (owner) {
+#pragma unroll 4
+      for (int mm = 0; mm < kMllrKChunk; ++mm) {
+        const float4 y = *reinterpret_cast<const float4*>(Ys + mm * D4 + ti * 4);
+        const float4 x = *reinterpret_cast<const float4*>(Xs + mm * E4 + ta * 4);
+        const float yv[4] = {y.x, y.y, y.z, y.w}, xv[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int v = 0; v < 4; ++v) acc[u][v] = fmaf(yv[u], xv[v], acc[u][v]);
+      }
+    }
+    __syncthreads();
+    if (((m0 + kMllrKChunk) & 127) == 0 || m0 + kMllrKChunk >= M) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) { dacc[u][v] += (double)acc[u][v]; acc[u][v] = 0.0f; }
+    }
+  }
+  if (!owner) return;
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int i = ti * 4 + u;
+    if (i >= D) continue;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int a = ta * 4 + v;
+      if (a < E) kd[((size_t)s * D + i) * E + a] = dacc[u][v];
+    }
+  }
+}
+
 // The prior terms of prepareKiGiInitMatrices (OL_ModelAdapt.cpp:1484-1523), the same for every
 // speaker: Gp[i][tri(a, b)], kp[i][a], accumulated over the UBM components in order. One block
 // per row i.
@@ -588,73 +684,87 @@ __global__ void mllr_prior_kernel(int M, int D, const float* __restrict__ umu, c
 }
 
 // w_i = G_i^-1 k_i per (speaker, row): Gaussian elimination without pivoting on the augmented
-// system [G_i | k_i] and a column-oriented back substitution -- the elimination order of the
+// system [G_i | k_i] and a column-oriented back substitution -- the pivots in the order of the
 // reference's pivot-free Gauss-Jordan inverse (MATRIX::_Invert_Gen, Matrix4_LMa.cpp:2232-2300)
-// followed by the product with k, without forming the inverse (a third of the work). One warp per
-// (row i, speaker s), lanes over the rows below the pivot, then over the rows above it; four
-// systems per block. Row stride LD is odd so that the lanes' 8-byte accesses to one column hit
-// distinct banks. FP64 throughout, the updates a - f b as fused multiply-adds (one rounding).
-// GB300 runs FP64 at 1/64 of its FP32 rate: this form takes 2.1 ms for the 19,500 systems at
-// C4 against 5.3 ms for separate multiply and subtract with a one-lane back substitution; a
-// double-float version on the FP32 pipes measured 1.1 ms with W within 6.4e-14 of it.
-struct SolveF64 {
-  using V = double;
-  __device__ static V from(double x) { return x; }
-  __device__ static double to(V x) { return x; }
-  __device__ static V recip(V x) { return __drcp_rn(x); }
-  __device__ static V mul(V a, V b) { return __dmul_rn(a, b); }
-  __device__ static V div(V a, V b) { return __ddiv_rn(a, b); }
-  __device__ static V sub_mul(V a, V f, V b) { return __fma_rn(-f, b, a); }  // a - f b, one rounding
-};
-using SolveArith = SolveF64;
+// followed by the product with k, without forming the inverse. G_i is symmetric and so is every
+// trailing block of the elimination, so only the upper triangle and k are updated (a sixth of
+// E^3 multiply-adds instead of a half for Gauss-Jordan): at pivot p the multipliers
+// l_r = a_pr / a_pp go into the unused lower column p, then the lanes walk the entries (r, c),
+// r > p, c >= r, of the trailing block as one flat list. The list holds the rows from the last
+// to the first, so the entries of every trailing block are a prefix of it; it is built once per
+// block in shared memory. One warp per (row i, speaker s), four systems per block. Row stride LD
+// is odd so that the lanes' 8-byte accesses to one column hit distinct banks. FP64 throughout,
+// the updates a - l b as fused multiply-adds (one rounding). GB300 runs FP64 at 1/64 of its FP32
+// rate, so the lanes must stay busy: the full-matrix form with a lane per row took 2.1 ms for the
+// 19,500 systems at C4, and 5.3 ms with separate multiply and subtract and a one-lane back
+// substitution.
 constexpr int kSolveWarps = 4;
 __host__ __device__ inline int solve_ld(int E) { return (E + 1) | 1; }
+// entries (r, c) with 0 <= r < E, r <= c <= E (c = E is k)
+__host__ __device__ inline int solve_list_len(int E) { return E * (E + 1) / 2 + E; }
+__host__ inline size_t solve_smem(int E) {
+  return sizeof(double) * (size_t)kSolveWarps * E * solve_ld(E) + sizeof(unsigned short) * solve_list_len(E);
+}
 __global__ void mllr_solve_kernel(int S, int D, const double* __restrict__ Gd, const double* __restrict__ kd,
                                   const double* __restrict__ Gp, const double* __restrict__ kp,
                                   const int* __restrict__ status, double* __restrict__ W) {
-  using A_ = SolveArith;
-  using V = A_::V;
   extern __shared__ __align__(16) unsigned char sm_solve[];
   const int E = D + 1, T = E * (E + 1) / 2, LD = solve_ld(E);  // E columns + k
+  const int L = solve_list_len(E);
+  unsigned short* list = reinterpret_cast<unsigned short*>(sm_solve + sizeof(double) * (size_t)kSolveWarps * E * LD);
+  for (int r = threadIdx.x; r < E; r += blockDim.x) {
+    // rows E-1, E-2, ..., 0; row r holds the E + 1 - r entries c = r .. E after the n = E-1-r
+    // rows below it: n (E + 1) - (n (r + E)) / 2 entries
+    const int n = E - 1 - r;
+    unsigned short* dst = list + n * (E + 1) - n * (r + E) / 2;
+    for (int c = r; c <= E; ++c) dst[c - r] = (unsigned short)(r << 8 | c);
+  }
+  __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const long long sys = (long long)blockIdx.x * kSolveWarps + warp;
   if (sys >= (long long)S * D) return;
   const int s = (int)(sys / D), i = (int)(sys - (long long)s * D);
-  V* A = reinterpret_cast<V*>(sm_solve) + (size_t)warp * E * LD;
+  double* A = reinterpret_cast<double*>(sm_solve) + (size_t)warp * E * LD;
   double* Wr = W + ((size_t)s * D + i) * E;
   if (status[s] != GMM_OK) {
     for (int a = lane; a < E; a += 32) Wr[a] = 0.0;
     return;
   }
-  for (int e = lane; e < E * E; e += 32) {
-    const int a = e / E, b = e - a * E;
-    const int ti = a <= b ? tri_index(a, b, E) : tri_index(b, a, E);
-    double g = Gd[((size_t)s * D + i) * T + ti];
-    if (Gp) g = __dadd_rn(Gp[(size_t)i * T + ti], g);
-    A[a * LD + b] = A_::from(g);
+  for (int a = 0; a < E; ++a) {  // upper triangle, row by row
+    for (int b = a + lane; b < E; b += 32) {
+      const int ti = tri_index(a, b, E);
+      double g = Gd[((size_t)s * D + i) * T + ti];
+      if (Gp) g = __dadd_rn(Gp[(size_t)i * T + ti], g);
+      A[a * LD + b] = g;
+    }
   }
   for (int a = lane; a < E; a += 32) {
     double k = kd[((size_t)s * D + i) * E + a];
     if (kp) k = __dadd_rn(kp[(size_t)i * E + a], k);
-    A[a * LD + E] = A_::from(k);
+    A[a * LD + E] = k;
   }
   __syncwarp();
-  for (int k = 0; k < E; ++k) {
-    const V ipiv = A_::recip(A[k * LD + k]);
-    for (int r = k + 1 + lane; r < E; r += 32) {
-      const V f = A_::mul(A[r * LD + k], ipiv);
-      for (int c = k + 1; c <= E; ++c) A[r * LD + c] = A_::sub_mul(A[r * LD + c], f, A[k * LD + c]);
+  int P = L - (E + 1);  // entries of rows 1 .. E-1
+  for (int p = 0; p < E - 1; ++p) {
+    const double ipiv = __drcp_rn(A[p * LD + p]);
+    for (int r = p + 1 + lane; r < E; r += 32) A[r * LD + p] = __dmul_rn(A[p * LD + r], ipiv);
+    __syncwarp();
+    for (int e = lane; e < P; e += 32) {
+      const unsigned v = list[e];
+      const int r = (int)(v >> 8), c = (int)(v & 0xffu);
+      A[r * LD + c] = __fma_rn(-A[r * LD + p], A[p * LD + c], A[r * LD + c]);
     }
     __syncwarp();
+    P -= E - p;  // drop row p + 1
   }
   for (int r = E - 1; r >= 0; --r) {
-    if (lane == 0) A[r * LD + E] = A_::div(A[r * LD + E], A[r * LD + r]);
+    if (lane == 0) A[r * LD + E] = __ddiv_rn(A[r * LD + E], A[r * LD + r]);
     __syncwarp();
-    const V x = A[r * LD + E];
-    for (int q = lane; q < r; q += 32) A[q * LD + E] = A_::sub_mul(A[q * LD + E], A[q * LD + r], x);
+    const double x = A[r * LD + E];
+    for (int q = lane; q < r; q += 32) A[q * LD + E] = __fma_rn(-A[q * LD + r], x, A[q * LD + E]);
     __syncwarp();
   }
-  for (int a = lane; a < E; a += 32) Wr[a] = A_::to(A[a * LD + E]);
+  for (int a = lane; a < E; a += 32) Wr[a] = A[a * LD + E];
 }
 
 // AdaptModelMLLR (OL_ModelAdapt.cpp:1597-1608) for every (speaker, component): mu' = A mu + b.
@@ -869,7 +979,7 @@ int mstep_mllr_batch(Ctx* c, int S, const double* plain, const SpeakerStats* ss,
   if (!rc) rc = scratch(c, SC_MLLR_XI, bXi, "MLLR extended means", (void**)&Xi);
   if (!rc && ubm_init) rc = scratch(c, SC_MLLR_GP, bGp, "MLLR prior G", (void**)&Gp);
   if (!rc && ubm_init) rc = scratch(c, SC_MLLR_KP, bkp, "MLLR prior k", (void**)&kp);
-  const size_t smem = sizeof(SolveArith::V) * (size_t)kSolveWarps * E * solve_ld(E);
+  const size_t smem = solve_smem(E);
   if (!rc && smem > 200 * 1024) rc = fail(c, GMM_ERR_UNSUPPORTED, "MLLR: D too large for the shared-memory solve");
   const long long tot = (long long)S * M;
   if (!rc) {
@@ -904,9 +1014,10 @@ int mstep_mllr_batch(Ctx* c, int S, const double* plain, const SpeakerStats* ss,
   if (!rc) {
     {
       // k data term: coef = F[s][m][i]
-      GMM_LAUNCH(c, "mllr_gemm_kernel");
-      dim3 grid((E + 63) / 64, (S + 127) / 128, D);
-      mllr_gemm_kernel<<<grid, 256, 0, c->stream>>>(S, M, D, E, F, (long long)M * D, D, 1, uvar, Xi, E, kd);
+      GMM_LAUNCH(c, "mllr_k_kernel");
+      const int threads = mllr_k_threads(D);
+      const size_t ksmem = sizeof(float) * kMllrKChunk * (size_t)(((D + 3) / 4) * 4 + ((E + 3) / 4) * 4);
+      mllr_k_kernel<<<S, threads, ksmem, c->stream>>>(S, M, D, F, uvar, Xi, kd);
     }
     if (ubm_init) {
       GMM_LAUNCH(c, "mllr_prior_kernel");
