@@ -403,32 +403,44 @@ __global__ void map_batch_norm_kernel(int S, int M, const float* __restrict__ ad
 __host__ __device__ inline int tri_index(int a, int b, int E) { return a * E - a * (a - 1) / 2 + (b - a); }
 
 // Dense per-speaker mean statistics of MLLR (n [S][M], F [S][M][D], FP64) from either the plain
-// layout or the tensor-core pieces. One warp per (speaker, component).
-__global__ void mllr_gather_kernel(int S, int M, int D, const double* __restrict__ plain,
-                                   const double* __restrict__ part, int K, int n_chunks,
-                                   const int* __restrict__ piece0, const int* __restrict__ npieces,
-                                   const int* __restrict__ row_of_comp, double* __restrict__ n_out,
-                                   double* __restrict__ F_out, double* __restrict__ ll_out) {
-  const long long t = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (t >= (long long)S * M) return;
-  const int s = (int)(t / M), m = (int)(t - (long long)s * M);
-  const int row = plain ? 0 : row_of_comp[m];
-  const double* pst = plain ? plain + (size_t)s * ((size_t)M * (1 + 2 * D) + 2) : nullptr;
-  auto stat = [&](int e) -> double {
-    if (plain) return e == 2 * D ? pst[m] : pst[M + (size_t)m * D + e];
-    if (row < 0) return 0.0;
-    double v = 0.0;
-    const int col = tc_stat_col(D, K, e);
-    for (int p = 0; p < npieces[s]; ++p) {
-      const double x = part[((size_t)(piece0[s] + p) * n_chunks + row / 128) * K * 128 + (size_t)col * 128 + (row % 128)];
-      v = p == 0 ? x : __dadd_rn(v, x);
-    }
-    return v;
-  };
-  if (lane == 0) n_out[t] = stat(2 * D);
-  if (plain && ll_out && m == 0 && lane == 0) ll_out[s] = pst[(size_t)M * (1 + 2 * D)];
-  for (int k = lane; k < D; k += 32) F_out[(size_t)t * D + k] = stat(k);
+// layout or the tensor-core pieces. One thread per (speaker, component): the pieces of
+// consecutive components are consecutive rows (coalesced reads); a block's F rows are staged in
+// shared memory ([pair][D | 1]) and written out as one contiguous range.
+constexpr int kGatherThreads = 64;
+__global__ void __launch_bounds__(kGatherThreads) mllr_gather_kernel(
+    int S, int M, int D, const double* __restrict__ plain, const double* __restrict__ part, int K, int n_chunks,
+    const int* __restrict__ piece0, const int* __restrict__ npieces, const int* __restrict__ row_of_comp,
+    double* __restrict__ n_out, double* __restrict__ F_out, double* __restrict__ ll_out) {
+  extern __shared__ double s_F[];
+  const int SD = D | 1;  // odd stride: the lanes' rows start in distinct banks
+  const long long tot = (long long)S * M;
+  const long long t0 = (long long)blockIdx.x * kGatherThreads, t = t0 + threadIdx.x;
+  if (t < tot) {
+    const int s = (int)(t / M), m = (int)(t - (long long)s * M);
+    const int row = plain ? 0 : row_of_comp[m];
+    const double* pst = plain ? plain + (size_t)s * ((size_t)M * (1 + 2 * D) + 2) : nullptr;
+    const int np = plain ? 0 : npieces[s], p0 = plain ? 0 : piece0[s];
+    auto stat = [&](int e) -> double {
+      if (plain) return e == 2 * D ? pst[m] : pst[M + (size_t)m * D + e];
+      if (row < 0) return 0.0;
+      double v = 0.0;
+      const int col = tc_stat_col(D, K, e);
+      for (int p = 0; p < np; ++p) {
+        const double x = part[((size_t)(p0 + p) * n_chunks + row / 128) * K * 128 + (size_t)col * 128 + (row % 128)];
+        v = p == 0 ? x : __dadd_rn(v, x);
+      }
+      return v;
+    };
+    n_out[t] = stat(2 * D);
+    if (plain && ll_out && m == 0) ll_out[s] = pst[(size_t)M * (1 + 2 * D)];
+    for (int k = 0; k < D; ++k) s_F[threadIdx.x * SD + k] = stat(k);
+  }
+  __syncthreads();
+  const long long n_here = tot - t0 < kGatherThreads ? tot - t0 : kGatherThreads;
+  for (int i = threadIdx.x; i < n_here * D; i += kGatherThreads) {
+    const int j = i / D, k = i - j * D;
+    F_out[(size_t)t0 * D + i] = s_F[j * SD + k];
+  }
 }
 
 // CheckInvertibility (OL_ModelAdapt.cpp:1851-1878) per speaker: enough components and data for a
@@ -985,7 +997,8 @@ int mstep_mllr_batch(Ctx* c, int S, const double* plain, const SpeakerStats* ss,
   if (!rc) {
     {
       GMM_LAUNCH(c, "mllr_gather_kernel");
-      mllr_gather_kernel<<<(unsigned)((tot + 7) / 8), 256, 0, c->stream>>>(
+      mllr_gather_kernel<<<(unsigned)((tot + kGatherThreads - 1) / kGatherThreads), kGatherThreads,
+                           sizeof(double) * kGatherThreads * (D | 1), c->stream>>>(
           S, M, D, plain, ss ? ss->part : nullptr, ss ? ss->K : 0, ss ? ss->n_chunks : 0, ss ? ss->piece0 : nullptr,
           ss ? ss->npieces : nullptr, ss ? ss->row_of_comp : nullptr, n, F, dll);
     }

@@ -155,6 +155,8 @@ __global__ void model_kernel(int D, int K, int Mact, int Mpad, long long plane_r
   const int cchunk = (int)(blk % KC);
   const int r = (int)(blk / KC) * 128 + rr;
   const int k = cchunk * 8 + e;
+  if (k == 0) comp_of_row[r] = r < Mact ? act[r] : -1;
+  if (k == D) return;  // the constant column: model_const_kernel
   double v = 0.0;
   if (r < Mact) {
     const int m = act[r];
@@ -162,17 +164,6 @@ __global__ void model_kernel(int D, int K, int Mact, int Mpad, long long plane_r
     const float* vv = var + (size_t)m * D;
     if (k < D) v = kLog2e * (double)mm[k] / (double)vv[k];
     else if (k >= K / 2 && k < K / 2 + D) v = -0.5 * kLog2e / (double)vv[k - K / 2];
-    else if (k == D) {
-      // constant of the expanded quadratic: log w - D/2 log 2pi - 1/2 sum log var - 1/2 sum mu^2/var
-      double sl = 0.0, q = 0.0;
-      for (int d = 0; d < D; ++d) {
-        sl += log((double)vv[d]);
-        q += (double)mm[d] * (double)mm[d] / (double)vv[d];
-      }
-      v = kLog2e * (log((double)w[m]) + kMinusLog2Pi * D / 2.0 - 0.5 * sl - 0.5 * q);
-    }
-  } else if (k == D) {
-    v = -1e30;
   }
   uint16_t a, b, c;
   split3d(v, a, b, c);
@@ -181,7 +172,62 @@ __global__ void model_kernel(int D, int K, int Mact, int Mpad, long long plane_r
   planes[o] = a;
   planes[plane + o] = b;
   planes[2 * plane + o] = c;
-  if (k == 0) comp_of_row[r] = r < Mact ? act[r] : -1;
+}
+
+// The constant column (k = D) of the W planes, one warp per row: log w - D/2 log 2pi
+// - 1/2 sum log var - 1/2 sum mu^2/var in FP64, the lanes over d and a shuffle reduction (GB300's
+// FP64 rate is 1/64 of FP32, so the D logarithms of a row are spread over a warp, and the rows
+// over the SMs); padded rows get -1e30 so they never contribute.
+__global__ void model_const_kernel(int D, int K, int Mact, int Mpad, long long plane_rows, long long row0,
+                                   const int* __restrict__ act, const float* __restrict__ w,
+                                   const float* __restrict__ mu, const float* __restrict__ var,
+                                   uint16_t* __restrict__ planes, const int* __restrict__ mact_dev) {
+  if (mact_dev) Mact = *mact_dev;
+  const int r = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (r >= Mpad) return;
+  double v = -1e30;
+  if (r < Mact) {
+    const int m = act[r];
+    const float* mm = mu + (size_t)m * D;
+    const float* vv = var + (size_t)m * D;
+    double sl = 0.0, q = 0.0;
+    for (int d = lane; d < D; d += 32) {
+      sl += log((double)vv[d]);
+      q += (double)mm[d] * (double)mm[d] / (double)vv[d];
+    }
+    for (int o = 16; o; o >>= 1) {
+      sl += __shfl_xor_sync(0xffffffffu, sl, o);
+      q += __shfl_xor_sync(0xffffffffu, q, o);
+    }
+    v = kLog2e * (log((double)w[m]) + kMinusLog2Pi * D / 2.0 - 0.5 * sl - 0.5 * q);
+  }
+  if (lane != 0) return;
+  uint16_t a, b, c;
+  split3d(v, a, b, c);
+  const int KC = K / 8;
+  const size_t t = ((size_t)((r >> 7) * KC + (D >> 3)) << 10) | ((size_t)(r & 127) << 3) | (size_t)(D & 7);
+  const size_t plane = (size_t)plane_rows * K;
+  const size_t o = (size_t)row0 * K + t;
+  planes[o] = a;
+  planes[plane + o] = b;
+  planes[2 * plane + o] = c;
+}
+
+void launch_model(Ctx* c, int D, int K, int Mact, int Mpad, long long plane_rows, long long row0, const int* act,
+                  const float* w, const float* mu, const float* var, uint16_t* planes, int* comp_of_row,
+                  const int* mact_dev) {
+  {
+    GMM_LAUNCH(c, "tc_model_kernel");
+    const long long tot = (long long)Mpad * K;
+    model_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(D, K, Mact, Mpad, plane_rows, row0, act, w,
+                                                                       mu, var, planes, comp_of_row, mact_dev);
+  }
+  {
+    GMM_LAUNCH(c, "tc_model_const_kernel");
+    model_const_kernel<<<(unsigned)((Mpad + 7) / 8), 256, 0, c->stream>>>(D, K, Mact, Mpad, plane_rows, row0, act,
+                                                                          w, mu, var, planes, mact_dev);
+  }
 }
 
 // ------------------------------------------------------------------ shared helpers
@@ -1246,13 +1292,8 @@ int tc_prepare_model(Ctx* c) {
     c->tcm.Mpad = Mpad;
     c->tcm.K = K;
   }
-  {
-    GMM_LAUNCH(c, "tc_model_kernel");
-    const long long tot = (long long)Mpad * K;
-    model_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(
-        c->D, K, c->Mact, Mpad, Mpad, 0, c->act, c->w, c->mu, c->var, c->tcm.planes, c->tcm.comp_of_row,
-        c->static_shapes ? c->flag + 4 : nullptr);
-  }
+  launch_model(c, c->D, K, c->Mact, Mpad, Mpad, 0, c->act, c->w, c->mu, c->var, c->tcm.planes, c->tcm.comp_of_row,
+               c->static_shapes ? c->flag + 4 : nullptr);
   int rc = make_map(c, &c->tm_wfull, c->tcm.planes, 3LL * Mpad * K, K);
   return rc;
 }
@@ -1648,10 +1689,7 @@ int tc_make_wmap(Ctx* c, CUtensorMap* map, const uint16_t* planes, long long row
 int tc_build_model(Ctx* c, int D, int K, int Mact, int Mpad, long long plane_rows, long long row0,
                    const int* act, const float* w, const float* mu, const float* var,
                    uint16_t* planes, int* comp_of_row) {
-  GMM_LAUNCH(c, "tc_model_kernel");
-  const long long tot = (long long)Mpad * K;
-  model_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(D, K, Mact, Mpad, plane_rows, row0, act,
-                                                                     w, mu, var, planes, comp_of_row, nullptr);
+  launch_model(c, D, K, Mact, Mpad, plane_rows, row0, act, w, mu, var, planes, comp_of_row, nullptr);
   return GMM_OK;
 }
 
