@@ -61,11 +61,17 @@ __global__ void em_comp_kernel(int M, int D, float* __restrict__ w, float* __res
 // Weight renormalisation (OL_ModelAdapt.cpp:928-931): the normaliser is the sequential FP64
 // sum in component order (one thread, as the reference adds them); the divisions are
 // independent and run across the block.
+// The weights are staged in shared memory by all threads first, so the serial sum waits on
+// additions only, not on global loads.
+constexpr int kNormStage = 4096;
 __global__ void em_norm_kernel(int M, float* __restrict__ w, int* __restrict__ flag) {
   __shared__ double s_corr;
+  __shared__ float s_w[kNormStage];
+  for (int j = threadIdx.x; j < M && j < kNormStage; j += blockDim.x) s_w[j] = w[j];
+  __syncthreads();
   if (threadIdx.x == 0) {
     double corr = 0.0;
-    for (int j = 0; j < M; ++j) corr = __dadd_rn(corr, (double)w[j]);
+    for (int j = 0; j < M; ++j) corr = __dadd_rn(corr, (double)(j < kNormStage ? s_w[j] : w[j]));
     s_corr = corr;
     flag[2] = M - flag[6];
   }
@@ -433,7 +439,14 @@ __global__ void __launch_bounds__(kGatherThreads) mllr_gather_kernel(
     };
     n_out[t] = stat(2 * D);
     if (plain && ll_out && m == 0) ll_out[s] = pst[(size_t)M * (1 + 2 * D)];
-    for (int k = 0; k < D; ++k) s_F[threadIdx.x * SD + k] = stat(k);
+    if (!plain && np == 1 && row >= 0) {
+      // one piece (the common case): independent loads, eight in flight at a time
+      const double* src = part + ((size_t)p0 * n_chunks + row / 128) * K * 128 + (row % 128);
+#pragma unroll 8
+      for (int k = 0; k < D; ++k) s_F[threadIdx.x * SD + k] = src[(size_t)tc_stat_col(D, K, k) * 128];
+    } else {
+      for (int k = 0; k < D; ++k) s_F[threadIdx.x * SD + k] = stat(k);
+    }
   }
   __syncthreads();
   const long long n_here = tot - t0 < kGatherThreads ? tot - t0 : kGatherThreads;
