@@ -96,46 +96,10 @@ __device__ __forceinline__ void split3d(double v, uint16_t& a, uint16_t& b, uint
 // Z planes as tile images: element (row f, column k) of plane p sits at
 // ((p * nT + f / 128) * K/8 + k / 8) * 1024 + (f % 128) * 8 + k % 8; row f holds the operand
 // columns (x at d, 1 at D, x^2 at K/2 + d) of frame row_frame[f] (identity when row_frame is
-// null), zero for padding rows (past N, or row_frame < 0). For K <= 80 the logits kernel's loader
-// warps build them on their first pass over the frames (features_row_to_tmem, hidden behind the
-// MMAs of the previous tile); for larger K, where TMEM holds one Z tile only, features_kernel
-// does it beforehand: one thread per 8-column group of a row, one 16-byte chunk per plane, a warp
-// covering 32 consecutive rows of a group (512 contiguous bytes per plane).
-__device__ __forceinline__ float zcol(const float* __restrict__ xr, int D, int K, int k) {
-  if (k < D) return xr[k];
-  if (k == D) return 1.0f;
-  if (k >= K / 2 && k < K / 2 + D) {
-    const float x = xr[k - K / 2];
-    return __fmul_rn(x, x);
-  }
-  return 0.0f;
-}
-
-__global__ void features_kernel(const float* __restrict__ X, long long N, long long nT, int D,
-                                int K, const long long* __restrict__ row_frame,
-                                uint16_t* __restrict__ planes, long long t_begin, long long t_end) {
-  const long long t = t_begin + (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const int KC = K / 8;
-  if (t >= t_end) return;
-  const int r = (int)(t & 127);
-  const long long blk = t >> 7;  // (tile, column group) in image order
-  const int c = (int)(blk % KC);
-  const long long T = blk / KC;
-  const long long row = T * 128 + r;
-  const long long f = row_frame ? row_frame[row] : (row < N ? row : -1);
-  uint16_t a[8], b[8], cc[8];
-#pragma unroll
-  for (int e = 0; e < 8; ++e) split3f(f >= 0 ? zcol(X + f * D, D, K, c * 8 + e) : 0.0f, a[e], b[e], cc[e]);
-  const size_t plane = (size_t)nT * 128 * K;
-  const size_t off = (size_t)t * 8;  // == (T * KC + c) * 1024 + r * 8
-  auto pack = [](const uint16_t* h) {
-    return make_uint4(h[0] | ((uint32_t)h[1] << 16), h[2] | ((uint32_t)h[3] << 16),
-                      h[4] | ((uint32_t)h[5] << 16), h[6] | ((uint32_t)h[7] << 16));
-  };
-  *reinterpret_cast<uint4*>(planes + off) = pack(a);
-  *reinterpret_cast<uint4*>(planes + plane + off) = pack(b);
-  *reinterpret_cast<uint4*>(planes + 2 * plane + off) = pack(cc);
-}
+// null), zero for padding rows (past N, or row_frame < 0). The logits kernel's loader warps
+// build them on their first pass over the frames (features_row_to_tmem), hidden behind the
+// MMAs: for K <= 80 straight into the second TMEM Z buffer, for larger K (one Z buffer) one tile
+// ahead into the images, copied into TMEM when the MMAs release the buffer.
 
 // W planes as tile images (same layout as Z, rows = active components padded to 128, log2
 // units); padded rows carry a constant of -1e30 so they never contribute.
@@ -288,12 +252,42 @@ __device__ __forceinline__ void image_row_to_tmem(const uint16_t* __restrict__ p
   }
 }
 
-// Row `r` of tile `tile` built from the raw features instead (K <= 80): the operand columns of
+// image_row_to_tmem for a row that this thread wrote into the images earlier in the same kernel:
+// coherent loads (ld.global, ordered after the thread's own stores), not the read-only path.
+__device__ __forceinline__ uint4 ld_global_v4(const void* p) {
+  uint4 v;
+  asm volatile("ld.global.v4.u32 {%0, %1, %2, %3}, [%4];"
+               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+               : "l"(reinterpret_cast<uint64_t>(p))
+               : "memory");
+  return v;
+}
+template <int K>
+__device__ __forceinline__ void own_image_row_to_tmem(const uint16_t* planes, int nT, int tile, int r,
+                                                      uint32_t taddr, bool valid) {
+  constexpr int KC = K / 8;
+#pragma unroll
+  for (int p = 0; p < 3; ++p) {
+    const uint4* src = reinterpret_cast<const uint4*>(planes + ((size_t)(p * nT + tile) * KC) * 1024 + (size_t)r * 8);
+#pragma unroll
+    for (int c = 0; c < KC; c += 2) {
+      uint4 u0 = make_uint4(0, 0, 0, 0), u1 = make_uint4(0, 0, 0, 0);
+      if (valid) {
+        u0 = ld_global_v4(src + (size_t)c * 128);
+        u1 = ld_global_v4(src + (size_t)(c + 1) * 128);
+      }
+      const uint32_t w[8] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z, u1.w};
+      tmem_st8(taddr + p * (K / 2) + c * 4, w);
+    }
+  }
+}
+
+// Row `r` of tile `tile` built from the raw features instead: the operand columns of
 // frame f (zeros when f < 0 or !valid), split into three bf16 planes, stored into TMEM (laid out
 // as image_row_to_tmem does) and into the plane images, which the statistics kernel reads next.
 // The row's D <= K/2 - 1 features are loaded into registers first (independent loads, one
 // latency); the squares sit at the constant column K/2 + d, so every register index is static.
-template <int K>
+template <int K, bool TO_TMEM = true>
 __device__ __forceinline__ void features_row_to_tmem(const float* __restrict__ X, int D, long long f,
                                                      uint16_t* __restrict__ planes, int nT, int tile, int r,
                                                      uint32_t taddr, bool valid) {
@@ -328,7 +322,7 @@ __device__ __forceinline__ void features_row_to_tmem(const float* __restrict__ X
     }
 #pragma unroll
     for (int p = 0; p < 3; ++p) {
-      tmem_st8(taddr + p * (K / 2) + c * 4, w[p]);
+      if constexpr (TO_TMEM) tmem_st8(taddr + p * (K / 2) + c * 4, w[p]);
       if (valid) {
         uint4* dst = reinterpret_cast<uint4*>(planes + ((size_t)(p * nT + tile) * KC + c) * 1024 + (size_t)r * 8);
         dst[0] = make_uint4(w[p][0], w[p][1], w[p][2], w[p][3]);
@@ -346,9 +340,9 @@ __device__ __forceinline__ void features_row_to_tmem(const float* __restrict__ X
 __host__ __device__ constexpr int cmax(int a, int b) { return a > b ? a : b; }
 __host__ __device__ constexpr int cmin(int a, int b) { return a < b ? a : b; }
 __host__ __device__ constexpr int ll_zb(int K) { return K <= 80 ? 2 : 1; }
-// With two Z buffers the loader warps build a tile from the raw features while the MMAs run on
-// the previous one; with one, features_kernel builds the planes beforehand.
-__host__ __device__ constexpr bool ll_builds_planes(int K) { return ll_zb(K) == 2; }
+// With two Z buffers the loader warps build a tile from the raw features into TMEM (and the
+// plane images) while the MMAs run on the previous one. With one, they build the next tile's
+// plane images while the MMAs run on the current tile and copy them into TMEM when it is done.
 __host__ __device__ constexpr int ll_nw(int K) { return K <= 96 ? 3 : 2; }
 
 template <int K>
@@ -499,20 +493,28 @@ __global__ void __launch_bounds__(kLlThreads, 1)
       if (!mbar_wait(&z_empty[zb], ((it / ZB) & 1) ^ 1, abort_flag, kWaitLimit)) break;
       tc_fence_after();
       const uint32_t zaddr = tmem + lane_off + C::Z_COL + zb * C::ZCOLS;
-      bool built = false;
-      if constexpr (ll_builds_planes(K)) {
-        if (X) {
-          const long long rr = (long long)tile * 128 + row;
-          const long long f = tile < nTz ? (row_frame ? row_frame[rr] : (rr < N ? rr : -1)) : -1;
-          features_row_to_tmem<K>(X, D, f, zplanes, nTz, tile, row, zaddr, tile < nTz);
-          built = true;
-        }
+      auto frame_of = [&](int t) -> long long {
+        const long long rr = (long long)t * 128 + row;
+        return t < nTz ? (row_frame ? row_frame[rr] : (rr < N ? rr : -1)) : -1;
+      };
+      if (!X) {
+        image_row_to_tmem(zplanes, nTz, K, tile, row, zaddr, tile < nTz);
+      } else if constexpr (ZB == 2) {
+        features_row_to_tmem<K>(X, D, frame_of(tile), zplanes, nTz, tile, row, zaddr, tile < nTz);
+      } else {
+        if (it == 0) features_row_to_tmem<K, false>(X, D, frame_of(tile), zplanes, nTz, tile, row, 0, tile < nTz);
+        own_image_row_to_tmem<K>(zplanes, nTz, tile, row, zaddr, tile < nTz);
       }
-      if (!built) image_row_to_tmem(zplanes, nTz, K, tile, row, zaddr, tile < nTz);
       tmem_st_wait();
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&z_full[zb]);
+      if constexpr (ZB == 1) {
+        // the next tile's images, while the MMAs run on this one
+        const int next = tile + (int)gridDim.x;
+        if (X && it + 1 < my_tiles)
+          features_row_to_tmem<K, false>(X, D, frame_of(next), zplanes, nTz, next, row, 0, next < nTz);
+      }
     }
   } else {
     // epilogue: thread = frame row; the two warps of a lane quadrant take the two 64-column
@@ -1139,18 +1141,12 @@ int launch_ll_part(Ctx* c, int tile0, int n_tiles_ll, float* ll_out_dev, bool wa
     attr_set_ll = true;
   }
   const float trouble2 = (float)(c->minLL * kLog2e);
-  if (build_planes && !ll_builds_planes(K)) {
-    GMM_LAUNCH(c, "tc_features_kernel");
-    const long long t0 = (long long)tile0 * 128 * (K / 8), t1 = (long long)(tile0 + n_tiles_ll) * 128 * (K / 8);
-    features_kernel<<<(unsigned)((t1 - t0 + 255) / 256), 256, 0, c->stream>>>(c->X, c->N, nTz, c->D, K, nullptr,
-                                                                             c->tcx.planes, t0, t1);
-  }
   {
     GMM_LAUNCH(c, "tc_ll_kernel");
     ll_kernel<K><<<grid_ll, kLlThreads, LC::SMEM, c->stream>>>(
         c->tm_wfull, c->tcx.planes, c->N, nullptr, nullptr, nTz, nTw, tile0, n_tiles_ll, n_chunks, trouble2,
         c->minLL, c->tcm.ll2, ll_out_dev, c->tc_llpart, c->tc_err,
-        build_planes && ll_builds_planes(K) ? c->X : nullptr, c->D);
+        build_planes ? c->X : nullptr, c->D);
   }
   if (!want_total) return GMM_OK;
   {
@@ -1605,7 +1601,8 @@ int tc_speaker_stats(Ctx* c, int S, const long long* offs, const long long* d_of
     } else {
       // Frames from host memory: copied in chunks of whole speakers on the copy stream (the first
       // chunks growing geometrically from 1/64 of the frames, then 1/8), each chunk's rows going
-      // through the logits kernel as soon as its frames land; then the statistics.
+      // through the logits kernel as soon as its frames land; then the statistics in one launch
+      // (statistics launches per chunk measured slower: a partial wave per chunk).
       const long long f_all = offs[S] - offs[0];
       const long long steady = std::max(1LL, (f_all + 7) / 8);
       std::vector<int> cuts{0};  // chunk boundaries (speaker indices)
@@ -1706,18 +1703,12 @@ void run_batch_k(Ctx* c, const TcBatch& b, const CUtensorMap& zfull, int tile0, 
   cudaFuncSetAttribute(ll_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, LC::SMEM);
   cudaFuncSetAttribute(acc_kernel<K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, AC::SMEM);
   cudaFuncSetAttribute(acc_kernel<K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, ACm::SMEM);
-  if ((stages & 1) && ntl > 0 && !ll_builds_planes(K)) {
-    GMM_LAUNCH(c, "tc_features_kernel");
-    const long long t0 = (long long)tile0 * 128 * (K / 8), t1 = (long long)(tile0 + ntl) * 128 * (K / 8);
-    features_kernel<<<(unsigned)((t1 - t0 + 255) / 256), 256, 0, c->stream>>>(
-        b.X, b.N, b.Rpad / 128, b.D, K, b.row_frame, b.zplanes, t0, t1);
-  }
   if ((stages & 1) && ntl > 0) {
     GMM_LAUNCH(c, "tc_ll_kernel");
     ll_kernel<K><<<grid_ll, kLlThreads, LC::SMEM, c->stream>>>(
         *b.wmap, b.zplanes, b.N, b.row_frame, b.tile_wbase, nTz, b.w_chunks_total, tile0, ntl, b.n_chunks,
         (float)(c->minLL * kLog2e), c->minLL, b.ll2, b.ll, b.llpart, c->tc_err,
-        ll_builds_planes(K) ? b.X : nullptr, b.D);
+        b.X, b.D);
   }
   if ((stages & 2) && b.n_work > 0) {
     GMM_LAUNCH(c, "tc_acc_kernel");
