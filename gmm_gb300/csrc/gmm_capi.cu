@@ -295,6 +295,7 @@ int gmm_destroy(gmm_handle h) {
   dfree(c, c->tcpart, c->tcpart_cap);
   dfree(c, c->tcm.planes, 0);
   dfree(c, c->tcm.comp_of_row, 0);
+  dfree(c, c->tcm.cent, 0);
   if (c->em_graph) cudaGraphExecDestroy(c->em_graph);
   dfree(c, c->ll_hist, 0);
   dfree(c, c->tcm.ll2, 0);
@@ -983,6 +984,7 @@ static int em_iterate_graph(Ctx* c, int iters, int upW, int upM, int upV, double
                            (long long)(size_t)c->logW, (long long)(size_t)c->bw, (long long)(size_t)c->bmu,
                            (long long)(size_t)c->bvar, (long long)(size_t)c->tcm.planes,
                            (long long)(size_t)c->tcm.comp_of_row, (long long)(size_t)c->tcm.ll2,
+                           (long long)(size_t)c->tcm.cent,
                            (long long)(size_t)c->tcx.planes, (long long)(size_t)c->tcpart,
                            (long long)(size_t)c->tc_llpart, (long long)(size_t)c->tc_err,
                            (long long)(size_t)c->ll_hist, (long long)c->ll_hist_cap,

@@ -40,6 +40,9 @@ struct TcModel {
   uint16_t* planes = nullptr;  // 3 bf16 planes of W~ in the UMMA K-major tile layout
   int* comp_of_row = nullptr;  // row r of the padded active list -> caller component index
   float* ll2 = nullptr;        // per-frame log2-domain LSE of the current E-step
+  // [Mpad][D] centres of the statistics kernel's sums (the row's mean; 0 for padding rows)
+  float* cent = nullptr;
+  int D = 0;
 };
 
 struct TcFeatures {
@@ -113,7 +116,7 @@ struct Ctx {
   bool autotune = true;
   std::map<long long, int> tuned_waves;  // key: K, component chunks, frame tiles (bucket)
   cudaGraphExec_t em_graph = nullptr;
-  long long em_graph_key[28] = {};
+  long long em_graph_key[29] = {};
   double* ll_hist = nullptr;  // [ll_hist_cap + 1]: per-iteration total LL, then a counter
   int ll_hist_cap = 0;
 
@@ -218,6 +221,13 @@ __host__ __device__ inline int tc_mean_cols(int D) { return (D + 1 + 15) / 16 * 
 // Physical column of statistic e in the order n / F / S used by the plain layout's readers
 // (e < D: F_e, D <= e < 2D: S_(e-D), e = 2D: n).
 __host__ __device__ inline int tc_stat_col(int D, int K, int e) { return e < D ? e : e == 2 * D ? D : K / 2 + (e - D); }
+// The tensor-core statistics kernel accumulates around a centre c per component row (the
+// component's mean at the E-step): F' = sum g (x - c), S' = sum g (x - c)^2. Readers of its
+// partials sum the pieces and add the centre back in FP64.
+__host__ __device__ inline double tc_uncentre_F(double Fc, double n, double c) { return Fc + c * n; }
+__host__ __device__ inline double tc_uncentre_S(double Sc, double Fc, double n, double c) {
+  return Sc + c * (2.0 * Fc + c * n);
+}
 
 // x / d correctly rounded, given r = RN(1 / d) (__drcp_rn): q = RN(x r), the remainder x - d q
 // exactly by FMA, then RN(q + remainder r) is RN(x / d) for normal operands (Markstein's theorem).
@@ -244,13 +254,14 @@ int scratch(Ctx* c, int slot, size_t bytes, const char* what, void** out);
 
 // Per-speaker statistics from the tensor-core path: FP64 partials of pieces of at most 8192
 // frames, [piece][chunk][K cols][128 rows] (operand-layout columns, tc_stat_col; rows = padded
-// active list); speaker s owns pieces [piece0[s], piece0[s] + npieces[s]), summed in piece order.
+// active list; first- and second-order sums centred on cent, see tc_uncentre); speaker s owns pieces [piece0[s], piece0[s] + npieces[s]), summed in piece order.
 struct SpeakerStats {
   int S = 0, n_chunks = 0, K = 0, pieces = 0;
   double* part = nullptr;
   int* piece0 = nullptr;       // [S]
   int* npieces = nullptr;      // [S]
   int* row_of_comp = nullptr;  // [M], -1 for inactive components
+  const float* cent = nullptr; // [rows][D] centres of the partials (tc_uncentre)
   size_t part_bytes = 0;
 };
 // Xh: the frames in host memory (copied into the handle's feature buffer chunk by chunk, the
@@ -284,6 +295,7 @@ struct TcBatch {
   int n_chunks = 0;                   // W chunks per model
   int w_chunks_total = 0;             // W chunks in the shared planes
   const uint16_t* wplanes = nullptr;  // shared W planes (tile images)
+  const float* cent = nullptr;        // [W plane rows][D] centres of the statistics sums
   const CUtensorMap* wmap = nullptr;  // 2-D map over wplanes, box = K rows
   const float* X = nullptr;           // batch frames [N][D]
   long long N = 0, Rpad = 0;          // frames, padded rows (multiple of 128)
@@ -296,7 +308,8 @@ struct TcBatch {
   int n_work = 0;                     // statistics CTAs (0: log-likelihoods only)
   const int4* work = nullptr;         // {W chunk, chunk in model, first FT tile, FT tiles}
   const int* tile_slot = nullptr;     // [Rpad / FT] statistics slot of each FT tile
-  double* part = nullptr;             // [slots][n_chunks][K][128]
+  double* part = nullptr;             // [slots][n_chunks][K][128], centred (tc_uncentre)
+  size_t part_bytes = 0;              // zeroed before the statistics kernel adds into it
   int single_comp = 0;
   bool second_order = true;           // S statistics wanted (else only the [x | 1] columns)
 };
@@ -308,7 +321,7 @@ int tc_run_batch_part(Ctx* c, const TcBatch& b, int tile0, int ntl, int stages);
 int tc_make_wmap(Ctx* c, CUtensorMap* map, const uint16_t* planes, long long rows, int K);
 int tc_build_model(Ctx* c, int D, int K, int Mact, int Mpad, long long plane_rows, long long row0,
                    const int* act, const float* w, const float* mu, const float* var,
-                   uint16_t* planes, int* comp_of_row);
+                   uint16_t* planes, int* comp_of_row, float* cent);
 
 int sync(Ctx* c, const char* what);
 

@@ -21,10 +21,13 @@ __device__ __forceinline__ float reset_var_value() {
 
 // UpdateModelEM per component (OL_ModelAdapt.cpp:858-921). flag[5] <- weights changed,
 // flag[6] <- number of components that had zero weight before the update.
+// var64: the variance as S/n - (F/n)^2 in FP64 throughout (the tensor-core path's update); the
+// reference squares the float-rounded mean, which alone moves a variance by up to ~1e-5 relative
+// when mu^2 >> var. Without var64 the update is the reference's, bit for bit.
 __global__ void em_comp_kernel(int M, int D, float* __restrict__ w, float* __restrict__ mu,
                                float* __restrict__ var, const double* __restrict__ stats,
                                unsigned int tot, int upW, int upM, int upV, float min_var,
-                               const double* __restrict__ nind, int* __restrict__ flag) {
+                               const double* __restrict__ nind, int* __restrict__ flag, int var64) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= M) return;
   const double* n = stats;
@@ -46,9 +49,11 @@ __global__ void em_comp_kernel(int M, int D, float* __restrict__ w, float* __res
   }
   if (upM || upV) {
     for (int k = 0; k < D; ++k) {
-      float mean = (float)__ddiv_rn(F[(size_t)j * D + k], mp);
+      const double mean_d = __ddiv_rn(F[(size_t)j * D + k], mp);
+      float mean = (float)mean_d;
       if (upV) {
-        double m2 = __dmul_rn((double)mean, (double)mean);
+        const double mv = var64 ? mean_d : (double)mean;
+        double m2 = __dmul_rn(mv, mv);
         float v = (float)__dsub_rn(__ddiv_rn(S[(size_t)j * D + k], mp), m2);
         if (v < min_var) v = min_var;
         vj[k] = v;
@@ -81,13 +86,14 @@ __global__ void em_norm_kernel(int M, float* __restrict__ w, int* __restrict__ f
     for (int j = threadIdx.x; j < M; j += blockDim.x) w[j] = (float)__ddiv_rn((double)w[j], corr);
 }
 
-// UpdateModelMAP, tau > 0 (OL_ModelAdapt.cpp:1024-1099), one thread per component.
+// UpdateModelMAP, tau > 0 (OL_ModelAdapt.cpp:1024-1099), one thread per component. var64: the
+// variance update in FP64 throughout (see em_comp_kernel).
 __global__ void map_comp_kernel(int M, int D, float* __restrict__ w, float* __restrict__ mu,
                                 float* __restrict__ var, const float* __restrict__ uw,
                                 const float* __restrict__ umu, const float* __restrict__ uvar,
                                 const double* __restrict__ stats, unsigned int tot, int tau,
                                 int upW, int upM, int upV, float min_var,
-                                float* __restrict__ adapted_w) {
+                                float* __restrict__ adapted_w, int var64) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= M) return;
   adapted_w[j] = 0.0f;
@@ -110,13 +116,16 @@ __global__ void map_comp_kernel(int M, int D, float* __restrict__ w, float* __re
     const float* uv = uvar + (size_t)j * D;
     for (int k = 0; k < D; ++k) {
       double a1 = __ddiv_rn(__dmul_rn(alfa, F[(size_t)j * D + k]), mp);
-      float am = (float)__dadd_rn(a1, __dmul_rn(one_m, (double)um[k]));
+      const double amd = __dadd_rn(a1, __dmul_rn(one_m, (double)um[k]));
+      float am = (float)amd;
       if (upV) {
         float second = __fadd_rn(uv[k], __fmul_rn(um[k], um[k]));
         float msq = __fmul_rn(am, am);
         double b1 = __ddiv_rn(__dmul_rn(alfa, S[(size_t)j * D + k]), mp);
-        double b2 = __dadd_rn(b1, __dmul_rn(one_m, (double)second));
-        float av = (float)__dsub_rn(b2, (double)msq);
+        const double second_d =
+            var64 ? __dadd_rn((double)uv[k], __dmul_rn((double)um[k], (double)um[k])) : (double)second;
+        double b2 = __dadd_rn(b1, __dmul_rn(one_m, second_d));
+        float av = (float)__dsub_rn(b2, var64 ? __dmul_rn(amd, amd) : (double)msq);
         if (av < min_var) av = min_var;
         var[(size_t)j * D + k] = av;
       }
@@ -306,7 +315,7 @@ constexpr int kMapThreads = 64;  // (speaker, component) pairs per block
 __global__ void __launch_bounds__(kMapThreads) map_batch_kernel(
     int S, int M, int D, const double* __restrict__ plain, const double* __restrict__ part, int K, int n_chunks,
     const int* __restrict__ piece0, const int* __restrict__ npieces, const int* __restrict__ row_of_comp,
-    const long long* __restrict__ offs, const float* __restrict__ uw, const float* __restrict__ umu,
+    const float* __restrict__ cent, const long long* __restrict__ offs, const float* __restrict__ uw, const float* __restrict__ umu,
     const float* __restrict__ uvar, int tau, int upW, int upM, int upV, float min_var, float* __restrict__ ow,
     float* __restrict__ omu, float* __restrict__ ovar, float* __restrict__ adapted_w, double* __restrict__ ll) {
   // thread = (speaker, component) pair t = s M + m: the partials of consecutive components are
@@ -359,17 +368,30 @@ __global__ void __launch_bounds__(kMapThreads) map_batch_kernel(
       adapted_w[t] = aw;
     }
     const double rmp = adapt ? __drcp_rn(mp) : 0.0;  // the D quotients below share the divisor mp
+    // tensor-core partials are centred on the component's mean (cr): tc_uncentre
+    const float* cr = plain ? nullptr : cent + (size_t)(row >= 0 ? row : 0) * D;
     for (int k = 0; k < D; ++k) {
       float am = um[k], av = uv[k];
       if (adapt && (upM || upV)) {
-        const double a1 = div_by_rcp(__dmul_rn(alfa, stat(k)), mp, rmp);
-        am = (float)__dadd_rn(a1, __dmul_rn(one_m, (double)um[k]));
-        if (upV) {
+        const double Fk = stat(k);
+        const double c = plain ? 0.0 : (double)cr[k];
+        const double a1 = div_by_rcp(__dmul_rn(alfa, plain ? Fk : tc_uncentre_F(Fk, mp, c)), mp, rmp);
+        const double amd = __dadd_rn(a1, __dmul_rn(one_m, (double)um[k]));
+        am = (float)amd;
+        if (upV && plain) {
+          // the reference's expression: second moment and squared mean in float
           const float second = __fadd_rn(uv[k], __fmul_rn(um[k], um[k]));
           const float msq = __fmul_rn(am, am);
           const double b1 = div_by_rcp(__dmul_rn(alfa, stat(D + k)), mp, rmp);
           const double b2 = __dadd_rn(b1, __dmul_rn(one_m, (double)second));
           av = (float)__dsub_rn(b2, (double)msq);
+          if (av < min_var) av = min_var;
+        } else if (upV) {
+          // tensor-core path: the variance in FP64 throughout
+          const double second = __dadd_rn((double)uv[k], __dmul_rn((double)um[k], (double)um[k]));
+          const double b1 = div_by_rcp(__dmul_rn(alfa, tc_uncentre_S(stat(D + k), Fk, mp, c)), mp, rmp);
+          const double b2 = __dadd_rn(b1, __dmul_rn(one_m, second));
+          av = (float)__dsub_rn(b2, __dmul_rn(amd, amd));
           if (av < min_var) av = min_var;
         }
       }
@@ -416,7 +438,7 @@ constexpr int kGatherThreads = 64;
 __global__ void __launch_bounds__(kGatherThreads) mllr_gather_kernel(
     int S, int M, int D, const double* __restrict__ plain, const double* __restrict__ part, int K, int n_chunks,
     const int* __restrict__ piece0, const int* __restrict__ npieces, const int* __restrict__ row_of_comp,
-    double* __restrict__ n_out, double* __restrict__ F_out, double* __restrict__ ll_out) {
+    const float* __restrict__ cent, double* __restrict__ n_out, double* __restrict__ F_out, double* __restrict__ ll_out) {
   extern __shared__ double s_F[];
   const int SD = D | 1;  // odd stride: the lanes' rows start in distinct banks
   const long long tot = (long long)S * M;
@@ -437,15 +459,25 @@ __global__ void __launch_bounds__(kGatherThreads) mllr_gather_kernel(
       }
       return v;
     };
-    n_out[t] = stat(2 * D);
+    const double nn = stat(2 * D);
+    n_out[t] = nn;
     if (plain && ll_out && m == 0) ll_out[s] = pst[(size_t)M * (1 + 2 * D)];
-    if (!plain && np == 1 && row >= 0) {
-      // one piece (the common case): independent loads, eight in flight at a time
-      const double* src = part + ((size_t)p0 * n_chunks + row / 128) * K * 128 + (row % 128);
-#pragma unroll 8
-      for (int k = 0; k < D; ++k) s_F[threadIdx.x * SD + k] = src[(size_t)tc_stat_col(D, K, k) * 128];
-    } else {
+    if (plain) {
       for (int k = 0; k < D; ++k) s_F[threadIdx.x * SD + k] = stat(k);
+    } else if (row < 0) {
+      for (int k = 0; k < D; ++k) s_F[threadIdx.x * SD + k] = 0.0;
+    } else {
+      // tensor-core partials are centred on the component's mean: tc_uncentre
+      const float* cr = cent + (size_t)row * D;
+      if (np == 1) {
+        // one piece (the common case): independent loads, eight in flight at a time
+        const double* src = part + ((size_t)p0 * n_chunks + row / 128) * K * 128 + (row % 128);
+#pragma unroll 8
+        for (int k = 0; k < D; ++k)
+          s_F[threadIdx.x * SD + k] = tc_uncentre_F(src[(size_t)tc_stat_col(D, K, k) * 128], nn, (double)cr[k]);
+      } else {
+        for (int k = 0; k < D; ++k) s_F[threadIdx.x * SD + k] = tc_uncentre_F(stat(k), nn, (double)cr[k]);
+      }
     }
   }
   __syncthreads();
@@ -852,7 +884,8 @@ int mstep_em(Ctx* c, int upW, int upM, int upV, int* alive) {
   {
     GMM_LAUNCH(c, "em_comp_kernel");
     em_comp_kernel<<<(c->M + 127) / 128, 128, 0, c->stream>>>(
-        c->M, c->D, c->w, c->mu, c->var, c->stats, tot, upW, upM, upV, c->min_var, nind, c->flag);
+        c->M, c->D, c->w, c->mu, c->var, c->stats, tot, upW, upM, upV, c->min_var, nind, c->flag,
+        c->precision == GMM_PREC_TC);
   }
   {
     GMM_LAUNCH(c, "em_norm_kernel");
@@ -886,7 +919,7 @@ int mstep_map(Ctx* c, int tau, int upW, int upM, int upV) {
     GMM_LAUNCH(c, "map_comp_kernel");
     map_comp_kernel<<<(c->M + 127) / 128, 128, 0, c->stream>>>(
         c->M, c->D, c->w, c->mu, c->var, c->pw, c->pmu, c->pvar, c->stats, tot, tau, upW, upM,
-        upV, c->min_var, c->logW);
+        upV, c->min_var, c->logW, c->precision == GMM_PREC_TC);
   }
   {
     GMM_LAUNCH(c, "map_norm_kernel");
@@ -970,8 +1003,8 @@ int mstep_map_batch(Ctx* c, const MapBatch& b, const double* plain, const Speake
     cudaFuncSetAttribute(map_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     map_batch_kernel<<<(unsigned)((tot + kMapThreads - 1) / kMapThreads), kMapThreads, smem, c->stream>>>(
         b.S, c->M, c->D, plain, ss ? ss->part : nullptr, ss ? ss->K : 0, ss ? ss->n_chunks : 0,
-        ss ? ss->piece0 : nullptr, ss ? ss->npieces : nullptr, ss ? ss->row_of_comp : nullptr, b.d_offs,
-        c->w, c->mu, c->var, b.tau, b.upW, b.upM, b.upV, c->min_var, b.w, b.mu, b.var, b.aw, b.ll);
+        ss ? ss->piece0 : nullptr, ss ? ss->npieces : nullptr, ss ? ss->row_of_comp : nullptr,
+        ss ? ss->cent : nullptr, b.d_offs, c->w, c->mu, c->var, b.tau, b.upW, b.upM, b.upV, c->min_var, b.w, b.mu, b.var, b.aw, b.ll);
   }
   if (b.upW) {
     GMM_LAUNCH(c, "map_batch_norm_kernel");
@@ -1013,7 +1046,7 @@ int mstep_mllr_batch(Ctx* c, int S, const double* plain, const SpeakerStats* ss,
       mllr_gather_kernel<<<(unsigned)((tot + kGatherThreads - 1) / kGatherThreads), kGatherThreads,
                            sizeof(double) * kGatherThreads * (D | 1), c->stream>>>(
           S, M, D, plain, ss ? ss->part : nullptr, ss ? ss->K : 0, ss ? ss->n_chunks : 0, ss ? ss->piece0 : nullptr,
-          ss ? ss->npieces : nullptr, ss ? ss->row_of_comp : nullptr, n, F, dll);
+          ss ? ss->npieces : nullptr, ss ? ss->row_of_comp : nullptr, ss ? ss->cent : nullptr, n, F, dll);
     }
     {
       GMM_LAUNCH(c, "mllr_batch_check_kernel");

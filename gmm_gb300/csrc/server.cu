@@ -66,12 +66,14 @@ struct Req {
   int piece0 = 0, pieces = 0;
 };
 
-// Statistics kernel / MAP update over the pieces of each MAP request (same expression order as
-// map_comp_kernel). One warp per (request, component).
+// MAP update over the statistics pieces of each MAP request (the expression order of
+// map_comp_kernel for weights and means; the variance in FP64 throughout, as the tensor-core
+// path's M-steps compute it). One warp per (request, component).
 __global__ void srv_map_kernel(int R, int M, int D, int K, int n_chunks, const int* __restrict__ req_model,
                                const int* __restrict__ req_piece0, const int* __restrict__ req_pieces,
                                const long long* __restrict__ req_frames, const int* __restrict__ req_par,
-                               const int* __restrict__ row_of_comp, const double* __restrict__ part,
+                               const int* __restrict__ row_of_comp, const float* __restrict__ cent,
+                               const double* __restrict__ part,
                                const float* __restrict__ mw, const float* __restrict__ mmu,
                                const float* __restrict__ mvar, float min_var, float* __restrict__ ow,
                                float* __restrict__ omu, float* __restrict__ ovar,
@@ -112,17 +114,23 @@ __global__ void srv_map_kernel(int R, int M, int D, int K, int n_chunks, const i
     adapted_w[t] = aw;
   }
   const double rmp = adapt ? __drcp_rn(mp) : 0.0;  // the D quotients below share the divisor mp
+  const float* cr = cent + ((size_t)mod * n_chunks * 128 + (row >= 0 ? row : 0)) * D;
   for (int k = lane; k < D; k += 32) {
     float am = um[k], av = uv[k];
     if (adapt && (upM || upV)) {
-      const double a1 = gmm::div_by_rcp(__dmul_rn(alfa, col(k)), mp, rmp);
-      am = (float)__dadd_rn(a1, __dmul_rn(one_m, (double)um[k]));
+      // the statistics kernel's sums are centred on the component's mean (cr)
+      const double c = (double)cr[k], Fc = col(k);
+      const double a1 = gmm::div_by_rcp(__dmul_rn(alfa, gmm::tc_uncentre_F(Fc, mp, c)), mp, rmp);
+      const double amd = __dadd_rn(a1, __dmul_rn(one_m, (double)um[k]));
+      am = (float)amd;
       if (upV) {
-        const float second = __fadd_rn(uv[k], __fmul_rn(um[k], um[k]));
-        const float msq = __fmul_rn(am, am);
-        const double b1 = gmm::div_by_rcp(__dmul_rn(alfa, col(tc_col_sq(K, k))), mp, rmp);
-        const double b2 = __dadd_rn(b1, __dmul_rn(one_m, (double)second));
-        av = (float)__dsub_rn(b2, (double)msq);
+        // FP64 variance update: the second moment of the adapted model less the square of the
+        // adapted mean, both in FP64
+        const double second = __dadd_rn((double)uv[k], __dmul_rn((double)um[k], (double)um[k]));
+        const double b1 =
+            gmm::div_by_rcp(__dmul_rn(alfa, gmm::tc_uncentre_S(col(tc_col_sq(K, k)), Fc, mp, c)), mp, rmp);
+        const double b2 = __dadd_rn(b1, __dmul_rn(one_m, second));
+        av = (float)__dsub_rn(b2, __dmul_rn(amd, amd));
         if (av < min_var) av = min_var;
       }
     }
@@ -184,6 +192,7 @@ struct Server {
   CUtensorMap wmap;
   float *mw = nullptr, *mmu = nullptr, *mvar = nullptr;
   int *mact = nullptr, *comp_of_row = nullptr, *row_of_comp = nullptr;
+  float* cent = nullptr;  // [W plane rows][D] centres of the statistics sums
   std::vector<int> mact_host;
   // request arenas (device) and pinned staging, two of each
   size_t arena_bytes = 0;
@@ -438,14 +447,15 @@ int launch(Server* s, Batch& b) {
   if (e != cudaSuccess) return cuda_fail(c, e, "server: cudaMemcpyAsync(batch frames)");
   cudaEventRecord(s->copied[b.slot], s->copy_stream);
   cudaStreamWaitEvent(c->stream, s->copied[b.slot], 0);
+  // the statistics pieces (zeroed by the statistics launch, which adds into them)
   const long long pieces_bytes = (long long)((const char*)b.rll - (const char*)b.part);
-  if (b.n_work > 0) cudaMemsetAsync(b.part, 0, (size_t)pieces_bytes, c->stream);
   TcBatch t;
   t.D = s->D;
   t.K = s->K;
   t.n_chunks = s->n_chunks;
   t.w_chunks_total = s->max_models * s->n_chunks;
   t.wplanes = s->wplanes;
+  t.cent = s->cent;
   t.wmap = &s->wmap;
   t.X = b.X;
   t.N = b.N;
@@ -460,6 +470,7 @@ int launch(Server* s, Batch& b) {
   t.work = b.work;
   t.tile_slot = b.tile_slot;
   t.part = b.part;
+  t.part_bytes = (size_t)pieces_bytes;
   t.single_comp = s->M == 1;
   t.second_order = b.second_order;
   int rc = tc_run_batch(c, t);
@@ -475,7 +486,7 @@ int launch(Server* s, Batch& b) {
       const long long tot = (long long)b.R_map * s->M;
       srv_map_kernel<<<(unsigned)((tot + 7) / 8), 256, 0, c->stream>>>(
           b.R_map, s->M, s->D, s->K, s->n_chunks, b.m_model, b.m_piece0, b.m_pieces, b.m_frames, b.m_par,
-          s->row_of_comp, b.part, s->mw, s->mmu, s->mvar, c->min_var, b.ow, b.omu, b.ovar, b.oaw);
+          s->row_of_comp, s->cent, b.part, s->mw, s->mmu, s->mvar, c->min_var, b.ow, b.omu, b.ovar, b.oaw);
     }
     {
       GMM_LAUNCH(c, "srv_norm_kernel");
@@ -669,6 +680,7 @@ int gmm_server_create(int device, int D, int M, int max_models, size_t request_b
   if (!rc) rc = gmm::dalloc(c, (void**)&s->mact, sizeof(int) * max_models * M, "server active lists");
   if (!rc) rc = gmm::dalloc(c, (void**)&s->comp_of_row, sizeof(int) * wrows, "server row maps");
   if (!rc) rc = gmm::dalloc(c, (void**)&s->row_of_comp, sizeof(int) * max_models * M, "server component rows");
+  if (!rc) rc = gmm::dalloc(c, (void**)&s->cent, sizeof(float) * wrows * D, "server statistics centres");
   if (!rc) rc = gmm::dalloc(c, (void**)&s->llpart, sizeof(double) * 256 * 128, "server LL partials");
   if (!rc) rc = gmm::dalloc(c, (void**)&c->tc_err, sizeof(int), "server error flag");
   for (int i = 0; i < 2 && !rc; ++i) rc = gmm::dalloc(c, (void**)&s->arena[i], s->arena_bytes, "server request arena");
@@ -717,7 +729,8 @@ int gmm_server_destroy(gmm_server s) {
     if (s->copied[i]) cudaEventDestroy(s->copied[i]);
     if (s->finished[i]) cudaEventDestroy(s->finished[i]);
   }
-  void* bufs[] = {s->wplanes, s->mw, s->mmu, s->mvar, s->mact, s->comp_of_row, s->row_of_comp, s->llpart, s->c.tc_err};
+  void* bufs[] = {s->wplanes,     s->mw,          s->mmu,  s->mvar,   s->mact,
+                  s->comp_of_row, s->row_of_comp, s->cent, s->llpart, s->c.tc_err};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
@@ -771,7 +784,7 @@ int gmm_server_add_model(gmm_server s, const float* w, const float* mu, const fl
   gmm::tc_build_model(&tmp, D, s->K, (int)act.size(), Mpad, (long long)s->max_models * Mpad,
                       (long long)id * Mpad, s->mact + (size_t)id * M, s->mw + (size_t)id * M,
                       s->mmu + (size_t)id * md, s->mvar + (size_t)id * md, s->wplanes,
-                      s->comp_of_row + (size_t)id * Mpad);
+                      s->comp_of_row + (size_t)id * Mpad, s->cent);
   gmm::srv_row_of_comp_kernel<<<1, 1024, 0, st>>>(M, Mpad, s->comp_of_row + (size_t)id * Mpad,
                                                   s->row_of_comp + (size_t)id * M);
   cudaError_t e = cudaStreamSynchronize(st);
