@@ -314,7 +314,10 @@ struct TcBatch {
   bool second_order = true;           // S statistics wanted (else only the [x | 1] columns)
 };
 int tc_stats_ft(int K);  // frames per statistics tile for K
-int tc_flush_tiles(int K);  // statistics tiles per FP64 flush
+int tc_flush_tiles(int K);  // statistics tiles per speaker piece (one FP64 slot)
+// The statistics kernel's partials are centred (tc_uncentre) for second-order statistics with
+// K > 80 (the sparse kernel); otherwise they are plain sums.
+bool tc_stats_centred(int K, bool second_order);
 int tc_k(int D);
 int tc_run_batch(Ctx* c, const TcBatch& b);
 int tc_run_batch_part(Ctx* c, const TcBatch& b, int tile0, int ntl, int stages);

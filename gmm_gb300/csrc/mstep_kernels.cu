@@ -368,13 +368,13 @@ __global__ void __launch_bounds__(kMapThreads) map_batch_kernel(
       adapted_w[t] = aw;
     }
     const double rmp = adapt ? __drcp_rn(mp) : 0.0;  // the D quotients below share the divisor mp
-    // tensor-core partials are centred on the component's mean (cr): tc_uncentre
-    const float* cr = plain ? nullptr : cent + (size_t)(row >= 0 ? row : 0) * D;
+    // the sparse statistics kernel's partials are centred on the component's mean (cr): tc_uncentre
+    const float* cr = (plain || !cent) ? nullptr : cent + (size_t)(row >= 0 ? row : 0) * D;
     for (int k = 0; k < D; ++k) {
       float am = um[k], av = uv[k];
       if (adapt && (upM || upV)) {
         const double Fk = stat(k);
-        const double c = plain ? 0.0 : (double)cr[k];
+        const double c = cr ? (double)cr[k] : 0.0;
         const double a1 = div_by_rcp(__dmul_rn(alfa, plain ? Fk : tc_uncentre_F(Fk, mp, c)), mp, rmp);
         const double amd = __dadd_rn(a1, __dmul_rn(one_m, (double)um[k]));
         am = (float)amd;
@@ -467,16 +467,17 @@ __global__ void __launch_bounds__(kGatherThreads) mllr_gather_kernel(
     } else if (row < 0) {
       for (int k = 0; k < D; ++k) s_F[threadIdx.x * SD + k] = 0.0;
     } else {
-      // tensor-core partials are centred on the component's mean: tc_uncentre
-      const float* cr = cent + (size_t)row * D;
+      // the sparse statistics kernel's partials are centred on the component's mean: tc_uncentre
+      const float* cr = cent ? cent + (size_t)row * D : nullptr;
       if (np == 1) {
         // one piece (the common case): independent loads, eight in flight at a time
         const double* src = part + ((size_t)p0 * n_chunks + row / 128) * K * 128 + (row % 128);
 #pragma unroll 8
         for (int k = 0; k < D; ++k)
-          s_F[threadIdx.x * SD + k] = tc_uncentre_F(src[(size_t)tc_stat_col(D, K, k) * 128], nn, (double)cr[k]);
+          s_F[threadIdx.x * SD + k] =
+              tc_uncentre_F(src[(size_t)tc_stat_col(D, K, k) * 128], nn, cr ? (double)cr[k] : 0.0);
       } else {
-        for (int k = 0; k < D; ++k) s_F[threadIdx.x * SD + k] = tc_uncentre_F(stat(k), nn, (double)cr[k]);
+        for (int k = 0; k < D; ++k) s_F[threadIdx.x * SD + k] = tc_uncentre_F(stat(k), nn, cr ? (double)cr[k] : 0.0);
       }
     }
   }

@@ -114,12 +114,13 @@ __global__ void srv_map_kernel(int R, int M, int D, int K, int n_chunks, const i
     adapted_w[t] = aw;
   }
   const double rmp = adapt ? __drcp_rn(mp) : 0.0;  // the D quotients below share the divisor mp
-  const float* cr = cent + ((size_t)mod * n_chunks * 128 + (row >= 0 ? row : 0)) * D;
+  // centred statistics (the sparse kernel) or plain sums (cent null)
+  const float* cr = cent ? cent + ((size_t)mod * n_chunks * 128 + (row >= 0 ? row : 0)) * D : nullptr;
   for (int k = lane; k < D; k += 32) {
     float am = um[k], av = uv[k];
     if (adapt && (upM || upV)) {
       // the statistics kernel's sums are centred on the component's mean (cr)
-      const double c = (double)cr[k], Fc = col(k);
+      const double c = cr ? (double)cr[k] : 0.0, Fc = col(k);
       const double a1 = gmm::div_by_rcp(__dmul_rn(alfa, gmm::tc_uncentre_F(Fc, mp, c)), mp, rmp);
       const double amd = __dadd_rn(a1, __dmul_rn(one_m, (double)um[k]));
       am = (float)amd;
@@ -447,8 +448,8 @@ int launch(Server* s, Batch& b) {
   if (e != cudaSuccess) return cuda_fail(c, e, "server: cudaMemcpyAsync(batch frames)");
   cudaEventRecord(s->copied[b.slot], s->copy_stream);
   cudaStreamWaitEvent(c->stream, s->copied[b.slot], 0);
-  // the statistics pieces (zeroed by the statistics launch, which adds into them)
   const long long pieces_bytes = (long long)((const char*)b.rll - (const char*)b.part);
+  if (b.n_work > 0) cudaMemsetAsync(b.part, 0, (size_t)pieces_bytes, c->stream);
   TcBatch t;
   t.D = s->D;
   t.K = s->K;
@@ -486,7 +487,8 @@ int launch(Server* s, Batch& b) {
       const long long tot = (long long)b.R_map * s->M;
       srv_map_kernel<<<(unsigned)((tot + 7) / 8), 256, 0, c->stream>>>(
           b.R_map, s->M, s->D, s->K, s->n_chunks, b.m_model, b.m_piece0, b.m_pieces, b.m_frames, b.m_par,
-          s->row_of_comp, s->cent, b.part, s->mw, s->mmu, s->mvar, c->min_var, b.ow, b.omu, b.ovar, b.oaw);
+          s->row_of_comp, gmm::tc_stats_centred(s->K, b.second_order) ? s->cent : nullptr, b.part, s->mw, s->mmu,
+          s->mvar, c->min_var, b.ow, b.omu, b.ovar, b.oaw);
     }
     {
       GMM_LAUNCH(c, "srv_norm_kernel");

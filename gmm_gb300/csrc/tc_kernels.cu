@@ -119,8 +119,11 @@ __global__ void model_kernel(int D, int K, int Mact, int Mpad, long long plane_r
   const int r = (int)(blk / KC) * 128 + rr;
   const int k = cchunk * 8 + e;
   if (k == 0) comp_of_row[r] = r < Mact ? act[r] : -1;
-  // the centres of the statistics kernel's sums: the row's mean (zero for padding rows)
-  if (k < D) cent[(size_t)(row0 + r) * D + k] = r < Mact ? mu[(size_t)act[r] * D + k] : 0.0f;
+  // the centres of the statistics kernel's sums: the row's mean rounded to bf16 (any centre will
+  // do; this one the statistics kernel holds in shared memory exactly), zero for padding rows
+  if (k < D)
+    cent[(size_t)(row0 + r) * D + k] =
+        r < Mact ? __bfloat162float(__float2bfloat16_rn(mu[(size_t)act[r] * D + k])) : 0.0f;
   if (k == D) return;  // the constant column: model_const_kernel
   double v = 0.0;
   if (r < Mact) {
@@ -621,7 +624,8 @@ struct Periods {
   }
 };
 
-// The statistics kernel: one CTA per (component chunk, frame range). The chunk's W planes sit in
+// Sparse statistics kernel (second-order statistics for K >= 96, where the dense kernel's split
+// accumulators do not fit in TMEM): one CTA per (component chunk, frame range). The chunk's W planes sit in
 // TMEM (A operand of the logits MMA); Z tiles and their frame LSE values stream through an
 // NZ-stage TMA ring; the logits S^T[128 comps x 128 frames] go into one of NS TMEM buffers.
 //
@@ -633,29 +637,31 @@ struct Periods {
 // over dimensions (two per lane, one packed FP32x2 instruction for both). Sums around the
 // centre carry no cancellation: the variance update S/n - mu^2 no longer magnifies their
 // rounding. The readers of the partials add the centre back in FP64 (tc_uncentre_*). x comes
-// from the frame's FP32 row in HBM through L1 (a coalesced line per pair): the Z tile's
-// core-matrix layout puts a frame's columns 2 KB apart, in the same four banks, and the shared
-// memory is already busy with the MMA's operand reads and the TMA fills.
+// from the frame's FP32 row in HBM (prefetched into L2 a few tiles ahead, read through L1).
 // A second tcgen05 GEMM (Gamma^T Z, five split-bf16 products per tile) did this before: the
 // tensor core's FP32 accumulation rounds toward zero, which biased F/n and S/n by -5e-8
 // relative, and the variance update magnified that up to 175 times (worst variance 2.1e-5
-// relative at N = 1M, M = 2048, D = 39, against 3.8e-6 now).
+// relative at N = 1M, M = 2048, D = 39, against 3.9e-6 now).
 //
 // Sixteen epilogue warps, four per TMEM lane quadrant. Scan: warp p of a quadrant reads frame
-// chunk p (32 frames) of the quadrant's 32 component rows (thread = row), compares each logit
-// with the frame's LSE in the log domain (a branch-free mask), and writes the kept pairs (frame,
-// posterior g = 2^(s - lse) > minGamma) to the row's list for that chunk (up to kAccList
-// entries; a longer list is marked overflowed and its chunk rescanned from TMEM by the
-// accumulating warp). Accumulate: warp p owns rows 8p .. 8p + 7 of the quadrant and walks their
-// lists, lanes over dimensions. Sums go to FP64 partials [slot][chunk][K cols][128 rows] (F'_d at
-// column d, n at D, S'_d at K/2 + d), zeroed before the launch, by fire-and-forget FP64
-// reductions at the end of every accumulation period (FLUSH tiles of one slot); each partial
-// has one writer thread, so its additions happen in a fixed order.
+// chunk p (32 frames) of the quadrant's 32 component rows (thread = row) and builds, without
+// branches, the mask of frames whose logit is within log2(minGamma) of the frame's LSE.
+// Accumulate: warp p owns rows 8p .. 8p + 7 of the quadrant; for each masked frame of a row it
+// reads that frame's logit column from TMEM (all 32 rows at once, the row's value taken by a
+// shuffle), forms g = 2^(s - lse), keeps the pair when g > minGamma, and adds it, lanes over
+// dimensions. Sums go to FP64 partials [slot][chunk][K cols][128 rows] (F'_d at column d, n at
+// D, S'_d at K/2 + d), zeroed before the launch, by fire-and-forget FP64 reductions (see
+// kRowFlushMass for when); each partial has one writer thread, so its additions happen in a
+// fixed order. A slot is a speaker piece (tile_slot) or the CTA's frame range.
 __host__ __device__ constexpr int acc_ft(int) { return 128; }
-constexpr int kAccList = 4;  // kept pairs per (row, 32-frame chunk) held in a list
+// A row's FP32 sums go to the FP64 partials when its posterior mass reaches this (so an FP32 sum
+// has at most ~2048 terms of weight 1: relative rounding ~2^-24 sqrt(2048)), at the end of its
+// slot, and at the end of the CTA's range; rows without kept pairs are never written.
+constexpr float kRowFlushMass = 2048.0f;
+constexpr int kNoPeriod = 1 << 30;  // slots end only at slot changes and range ends
 
 template <int K>
-struct AccCfg {
+struct SparseCfg {
   static constexpr int FT = acc_ft(K);
   static constexpr int DMAX = (K - 1) / 2;  // largest D with this K
   static_assert(DMAX <= 63, "two dimensions per lane, the 64th slot carries the count");
@@ -666,18 +672,17 @@ struct AccCfg {
   static constexpr int NS = cmin(3, (512 - WCOLS) / FT);  // logits buffers
   static constexpr int S_COL = 0;
   static constexpr int W_COL = NS * FT;
-  static constexpr int LIST_BYTES = 128 * 4 * kAccList * 8;  // [row][chunk][entry] {frame, g}
-  static constexpr int CNT_BYTES = 128 * 4 * 4;              // [row][chunk] entries (or overflow)
-  static constexpr int FIXED = LIST_BYTES + CNT_BYTES + 32 * 8 + 64 + 1024;
+  static constexpr int MASK_BYTES = 2 * 128 * 4 * 4;  // [tile parity][row][frame chunk]
+  static constexpr int CEN_BYTES = 128 * 64 * 2;      // [row][dimension] centres, bf16
+  static constexpr int FIXED = MASK_BYTES + CEN_BYTES + 32 * 8 + 64 + 1024;
   static constexpr int NZ = cmin(3, (227 * 1024 - FIXED) / (Z_STAGE + LL_STAGE));
   static constexpr int OFF_Z = 0;
   static constexpr int OFF_LL = OFF_Z + NZ * Z_STAGE;
-  static constexpr int OFF_LIST = OFF_LL + NZ * LL_STAGE;
-  static constexpr int OFF_CNT = OFF_LIST + LIST_BYTES;
-  static constexpr int OFF_BAR = OFF_CNT + CNT_BYTES;
+  static constexpr int OFF_MASK = OFF_LL + NZ * LL_STAGE;
+  static constexpr int OFF_CEN = OFF_MASK + MASK_BYTES;
+  static constexpr int OFF_BAR = OFF_CEN + CEN_BYTES;
   static constexpr int OFF_MISC = OFF_BAR + 32 * 8;
   static constexpr int SMEM = OFF_MISC + 64 + 1024;
-  static constexpr int FLUSH = 64 * 128 / FT;  // tiles per FP64 flush (8192 frames)
   static_assert(NS >= 2, "logits buffers");
   static_assert(NZ >= 2, "Z ring");
   static_assert(W_COL + WCOLS <= 512, "TMEM budget");
@@ -689,15 +694,15 @@ constexpr int kAccThreads = 32 * (2 + kAccEpiWarps);  // warp 0 TMA, warp 1 logi
 // SO: second-order statistics wanted (else n and F only).
 template <int K, bool SO>
 __global__ void __launch_bounds__(kAccThreads, 1)
-    acc_kernel(const __grid_constant__ CUtensorMap zmap, const uint16_t* __restrict__ wplanes,
-               const float* __restrict__ cent, const float* __restrict__ X,
+    acc_sparse_kernel(const __grid_constant__ CUtensorMap zmap, const uint16_t* __restrict__ wplanes,
+               const float* __restrict__ cent, const float* __restrict__ X, long long N,
                const long long* __restrict__ row_frame, int D, int nTz, int nTw, const float* __restrict__ ll2,
                int n_tiles, int n_chunks, int slices, const int* __restrict__ tile_slot,
                const int4* __restrict__ work, float minGamma, int single_comp, const int* __restrict__ mact_dev,
                double* __restrict__ part, int* __restrict__ err) {
   if (mact_dev) single_comp = *mact_dev == 1;
-  using C = AccCfg<K>;
-  constexpr int FT = C::FT, NZ = C::NZ, NS = C::NS, FLUSH = C::FLUSH, EW = kAccEpiWarps;
+  using C = SparseCfg<K>;
+  constexpr int FT = C::FT, NZ = C::NZ, NS = C::NS, EW = kAccEpiWarps;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + C::OFF_BAR);
@@ -711,8 +716,8 @@ __global__ void __launch_bounds__(kAccThreads, 1)
   volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + C::OFF_MISC + 8);
   volatile int* stop_s = reinterpret_cast<volatile int*>(smem + C::OFF_MISC + 16);  // [4]
   float* ll_s = reinterpret_cast<float*>(smem + C::OFF_LL);
-  float2* list_s = reinterpret_cast<float2*>(smem + C::OFF_LIST);
-  int* cnt_s = reinterpret_cast<int*>(smem + C::OFF_CNT);
+  const uint32_t ll_sa = smem_u32(ll_s), mask_sa = smem_u32(smem + C::OFF_MASK);
+  const uint32_t cen_sa = smem_u32(smem + C::OFF_CEN);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int chunk = (int)blockIdx.x % n_chunks, slice = (int)blockIdx.x / n_chunks;
@@ -731,8 +736,7 @@ __global__ void __launch_bounds__(kAccThreads, 1)
     nt = max(0, min(n_tiles, t0 + per) - t0);
   }
   // Statistics go to "slots": one per speaker piece with tile_slot (work items never split a
-  // piece, so each (slot, chunk) has one owner), else one per slice. An accumulation period ends
-  // at a slot change or after FLUSH tiles of the same slot.
+  // piece, so each (slot, chunk) has one owner), else one per slice.
   Periods per(tile_slot, t0, nt, slice);
 
   if (threadIdx.x == 0) {
@@ -761,16 +765,30 @@ __global__ void __launch_bounds__(kAccThreads, 1)
   if (warp == 0) {
     if (lane == 0 && nt > 0) {
       prefetch_tmap(&zmap);
+      // the features' whole 16-byte pieces (the L2 prefetch wants an aligned base)
+      const long long xbytes = (N * D * 4) & ~15LL;
+      const bool xpf = (reinterpret_cast<uintptr_t>(X) & 15) == 0;
       int issued = 0;
       for (int i = 0; i < nt; ++i) {
         const int s = i % NZ;
-        if (!mbar_wait(&z_empty[s], ((i / NZ) & 1) ^ 1, abort_flag, kWaitLimit)) break;
+        if (!mbar_wait_sleep(&z_empty[s], ((i / NZ) & 1) ^ 1, abort_flag, kWaitLimit)) break;
         mbar_arrive_expect_tx(&z_full[s], C::Z_STAGE + C::LL_STAGE);
         uint8_t* zs = smem + C::OFF_Z + s * C::Z_STAGE;
         const int t = t0 + i;
         for (int p = 0; p < 3; ++p) load_image(zs + p * C::Z_PLANE, &zmap, p, nTz, K, t, &z_full[s]);
         bulk_load(ll_s + s * FT, ll2 + (size_t)t * FT, FT * 4, &z_full[s]);
         issued = i + 1;
+        // the tile's frames into L2 for the epilogue's reads of x, a few tiles ahead of them (a
+        // tile's rows are one contiguous run of frames)
+        if (xpf) {
+          const long long fb = row_frame ? row_frame[(long long)t * FT] : (long long)t * FT;
+          if (fb >= 0 && fb < N) {
+            const long long fe = fb + FT < N ? fb + FT : N;
+            const long long b0 = (fb * D * 4) & ~15LL, b1 = (fe * D * 4 + 15) & ~15LL;
+            const long long e1 = b1 < xbytes ? b1 : xbytes;
+            if (e1 > b0) bulk_prefetch_l2(reinterpret_cast<const char*>(X) + b0, (uint32_t)(e1 - b0));
+          }
+        }
       }
       if (*abort_flag)  // drain the copies still in flight
         for (int i = max(0, issued - NZ); i < issued; ++i) mbar_drain(&z_full[i % NZ], (i / NZ) & 1);
@@ -781,10 +799,10 @@ __global__ void __launch_bounds__(kAccThreads, 1)
       const uint32_t zb0 = smem_u32(smem + C::OFF_Z);
       const uint32_t idesc_l = idesc_bf16(128, FT, false, false);
       const uint32_t wa = tmem + C::W_COL;
-      bool ok = mbar_wait(w_full, 0, abort_flag, kWaitLimit);
+      bool ok = mbar_wait_sleep(w_full, 0, abort_flag, kWaitLimit);
       for (int i = 0; i < nt && ok; ++i) {
-        if (!mbar_wait(&z_full[i % NZ], (i / NZ) & 1, abort_flag, kWaitLimit)) break;
-        if (i >= NS && !mbar_wait(&s_free[i % NS], ((i - NS) / NS) & 1, abort_flag, kWaitLimit)) break;
+        if (!mbar_wait_sleep(&z_full[i % NZ], (i / NZ) & 1, abort_flag, kWaitLimit)) break;
+        if (i >= NS && !mbar_wait_sleep(&s_free[i % NS], ((i - NS) / NS) & 1, abort_flag, kWaitLimit)) break;
         tc_fence_after();
         const uint64_t zd = smem_desc(zb0 + (i % NZ) * C::Z_STAGE, FT * 16, 128);
         const uint32_t d = tmem + C::S_COL + (i % NS) * FT;
@@ -827,173 +845,164 @@ __global__ void __launch_bounds__(kAccThreads, 1)
     // lane = dimensions (lane, lane + 32); dimension 63 (lane 31's second one, unused since
     // D <= 63) carries the count: its x is 1 and its centre 0, so F'_63 = n
     const bool d0 = lane < D, d1 = lane + 32 < D, dn = lane == 31;
-    const int rowa0 = q4 * 32 + 8 * pw;  // first row this warp accumulates
-    const float* crow = cent + ((size_t)wchunk * 128 + rowa0) * D;
+    const int rowq0 = 8 * pw;                    // first row (within the quadrant) this warp owns
+    {
+      // this warp's rows' centres into shared memory as bf16 (exact: the centres are bf16 values)
+      const float* crow = cent + ((size_t)wchunk * 128 + q4 * 32 + rowq0) * D;
+      for (int j = 0; j < 8; ++j) {
+        const uint32_t a = cen_sa + (uint32_t)(((q4 * 32 + rowq0 + j) * 64) * 2);
+        const float c0 = d0 ? __ldg(crow + (size_t)j * D + lane) : 0.0f;
+        const float c1 = d1 ? __ldg(crow + (size_t)j * D + lane + 32) : 0.0f;
+        asm volatile("st.shared.u16 [%0], %1;" ::"r"(a + lane * 2), "h"(__bfloat16_as_ushort(__float2bfloat16_rn(c0))) : "memory");
+        asm volatile("st.shared.u16 [%0], %1;" ::"r"(a + (lane + 32) * 2), "h"(__bfloat16_as_ushort(__float2bfloat16_rn(c1))) : "memory");
+      }
+      __syncwarp();
+    }
     float2 Fs[8], Ss[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       Fs[j] = make_float2(0.0f, 0.0f);
       Ss[j] = make_float2(0.0f, 0.0f);
     }
+    uint32_t dirty = 0;  // rows with sums not yet in the partials
+    // row j's sums into the FP64 partials [col][row] of a slot, by reductions (no value comes
+    // back, so the warp does not wait); every partial has this one writer thread
+    auto flush_row = [&](int j, int slot) {
+      double* dst = part + ((size_t)slot * n_chunks + chunk) * K * 128 + q4 * 32 + rowq0 + j;
+      if (d0) atomicAdd(dst + (size_t)lane * 128, (double)Fs[j].x);
+      if (d1) atomicAdd(dst + (size_t)(lane + 32) * 128, (double)Fs[j].y);
+      if (SO && d0) atomicAdd(dst + (size_t)(K / 2 + lane) * 128, (double)Ss[j].x);
+      if (SO && d1) atomicAdd(dst + (size_t)(K / 2 + lane + 32) * 128, (double)Ss[j].y);
+      if (dn) atomicAdd(dst + (size_t)D * 128, (double)Fs[j].y);
+      Fs[j] = make_float2(0.0f, 0.0f);
+      Ss[j] = make_float2(0.0f, 0.0f);
+    };
     // candidates: posterior above minGamma within a margin (log2 domain), then the exact test
     const float thr = log2f(minGamma) - 0.01f;
     for (int i = 0; i < nt; ++i) {
-      const int s = i % NZ, b = i % NS;
-      per.begin(i, FLUSH);
-      const bool okw = mbar_wait(&z_full[s], (i / NZ) & 1, abort_flag, kWaitLimit) &&
-                       mbar_wait(&s_full[b], (i / NS) & 1, abort_flag, kWaitLimit);
-      const float* lls = ll_s + s * FT;
+      const int s = i % NZ, b = i % NS, mb = i & 1;
+      per.begin(i, kNoPeriod);
+      const bool okw = mbar_wait_sleep(&z_full[s], (i / NZ) & 1, abort_flag, kWaitLimit) &&
+                       mbar_wait_sleep(&s_full[b], (i / NS) & 1, abort_flag, kWaitLimit);
+      const uint32_t lla = ll_sa + (uint32_t)(s * FT * 4);
       const uint32_t sbuf = tmem + lane_off + C::S_COL + b * FT;
       const long long tile = (long long)(t0 + i);
       if (okw) {
-        // scan frame chunk pw of the quadrant's rows: a candidate mask without branches, then the
-        // few kept pairs (frame, posterior) into the row's list for this chunk
+        // scan frame chunk pw of the quadrant's rows: the candidate mask, without branches
         tc_fence_after();
-        float2* lst = list_s + (row_l * 4 + pw) * kAccList;
-        int cnt = 0;
+        uint32_t v[32];
+        tmem_ld32(sbuf + 32 * pw, v);
+        tmem_ld_wait();
+        uint32_t m = 0;
         if (!single_comp) {
-#pragma unroll 1
-          for (int h = 0; h < 32; h += 8) {  // 8 logits at a time (registers)
-            uint32_t v[8];
-            tmem_ld8(sbuf + 32 * pw + h, v);
-            tmem_ld_wait();
-            const float4 la = *reinterpret_cast<const float4*>(lls + 32 * pw + h);
-            const float4 lb = *reinterpret_cast<const float4*>(lls + 32 * pw + h + 4);
-            const float dl[8] = {__uint_as_float(v[0]) - la.x, __uint_as_float(v[1]) - la.y,
-                                 __uint_as_float(v[2]) - la.z, __uint_as_float(v[3]) - la.w,
-                                 __uint_as_float(v[4]) - lb.x, __uint_as_float(v[5]) - lb.y,
-                                 __uint_as_float(v[6]) - lb.z, __uint_as_float(v[7]) - lb.w};
-            // NaN (padding frame) and -inf (a trouble frame's +inf LSE) are never candidates
-            uint32_t m = 0;
 #pragma unroll
-            for (int k = 0; k < 8; ++k) m |= (dl[k] > thr ? 1u : 0u) << k;
-            while (m) {
-              const int k = __ffs(m) - 1;
-              m &= m - 1;
-              float dk;
-              switch (k) {  // register k of dl (k is this lane's own)
-                case 0: dk = dl[0]; break;
-                case 1: dk = dl[1]; break;
-                case 2: dk = dl[2]; break;
-                case 3: dk = dl[3]; break;
-                case 4: dk = dl[4]; break;
-                case 5: dk = dl[5]; break;
-                case 6: dk = dl[6]; break;
-                default: dk = dl[7]; break;
-              }
-              const float g = ex2(dk);
-              if (g > minGamma) {
-                if (cnt < kAccList) lst[cnt] = make_float2(__int_as_float(32 * pw + h + k), g);
-                ++cnt;
-              }
-            }
+          for (int q = 0; q < 8; ++q) {
+            const float4 l = lds_f4(lla + (uint32_t)((32 * pw + 4 * q) * 4));
+            // NaN (padding frame) and -inf (a trouble frame's +inf LSE) are never candidates
+            if (__uint_as_float(v[4 * q + 0]) - l.x > thr) m |= 1u << (4 * q + 0);
+            if (__uint_as_float(v[4 * q + 1]) - l.y > thr) m |= 1u << (4 * q + 1);
+            if (__uint_as_float(v[4 * q + 2]) - l.z > thr) m |= 1u << (4 * q + 2);
+            if (__uint_as_float(v[4 * q + 3]) - l.w > thr) m |= 1u << (4 * q + 3);
           }
         } else if (row_l == 0) {
           // one component: every real frame has posterior 1
-#pragma unroll 1
-          for (int k = 0; k < 32; ++k) {
-            if (!isnan(lls[32 * pw + k])) {
-              if (cnt < kAccList) lst[cnt] = make_float2(__int_as_float(32 * pw + k), 1.0f);
-              ++cnt;
-            }
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const float4 l = lds_f4(lla + (uint32_t)((32 * pw + 4 * q) * 4));
+            if (!isnan(l.x)) m |= 1u << (4 * q + 0);
+            if (!isnan(l.y)) m |= 1u << (4 * q + 1);
+            if (!isnan(l.z)) m |= 1u << (4 * q + 2);
+            if (!isnan(l.w)) m |= 1u << (4 * q + 3);
           }
         }
-        cnt_s[row_l * 4 + pw] = cnt;
+        sts_u32(mask_sa + (uint32_t)(((mb * 128 + row_l) * 4 + pw) * 4), m);
       }
-      // The quadrant's four warps reach every barrier on every path; the stop decision is one
-      // snapshot of the abort flag (raised by any failed wait) taken between two of them.
+      // The quadrant's four warps reach both barriers on every path; the stop decision is one
+      // snapshot of the abort flag (raised by any failed wait) taken between them. The masks are
+      // double-buffered by tile parity: a warp passes the next tile's first barrier only after
+      // all four finished this tile's accumulation.
       named_sync(1 + q4, 128);
       if (pw == 0 && lane == 0) stop_s[q4] = *abort_flag;
       named_sync(1 + q4, 128);
       if (stop_s[q4]) break;
-      // the Z stage and its LSE values are no longer needed: the lists carry the posteriors
-      if (lane == 0) mbar_arrive(&z_empty[s]);
-      // the kept pairs of this warp's rows; x from the frame's row (L2 / L1, coalesced), two
-      // pairs' loads in flight
-      auto frame_of = [&](int f) -> long long { return row_frame ? row_frame[tile * 128 + f] : tile * 128 + f; };
+      // the masked frames of this warp's rows
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
-        const int r = rowa0 + j;
-        const int4 cn = *reinterpret_cast<const int4*>(&cnt_s[r * 4]);
-        if ((cn.x | cn.y | cn.z | cn.w) == 0) continue;
-        // the row's centre, negated (through L1: the chunk's centres are a few KB)
-        const float2 wc = make_float2(d0 ? -__ldg(crow + (size_t)j * D + lane) : 0.0f,
-                                      d1 ? -__ldg(crow + (size_t)j * D + lane + 32) : 0.0f);
-        // list slots in use, kAccList per chunk; an overflowed chunk is rescanned from TMEM
-        uint32_t slots = 0, over = 0;
+        const int rq = rowq0 + j;  // row within the quadrant (= its TMEM lane)
+        const uint4 mk = lds_u4(mask_sa + (uint32_t)(((mb * 128 + q4 * 32 + rq) * 4) * 4));
+        if ((mk.x | mk.y | mk.z | mk.w) == 0) continue;
+        // the row's centre, negated
+        float2 wc;
         {
-          const int cc[4] = {cn.x, cn.y, cn.z, cn.w};
-#pragma unroll
-          for (int c = 0; c < 4; ++c) {
-            if (cc[c] > kAccList) over |= 1u << c;
-            else slots |= ((1u << cc[c]) - 1u) << (kAccList * c);
-          }
+          const uint32_t a = cen_sa + (uint32_t)(((q4 * 32 + rq) * 64) * 2);
+          unsigned short h0, h1;
+          asm volatile("ld.shared.u16 %0, [%1];" : "=h"(h0) : "r"(a + lane * 2));
+          asm volatile("ld.shared.u16 %0, [%1];" : "=h"(h1) : "r"(a + (lane + 32) * 2));
+          wc = make_float2(-__uint_as_float((uint32_t)h0 << 16), -__uint_as_float((uint32_t)h1 << 16));
         }
-        while (slots) {
-          float g[2];
-          float2 x[2];
-#pragma unroll
-          for (int u = 0; u < 2; ++u) {
-            g[u] = 0.0f;
-            x[u] = make_float2(0.0f, 0.0f);
-            if (slots) {
-              const int e = __ffs(slots) - 1;
-              slots &= slots - 1;
-              const float2 fg = list_s[r * 4 * kAccList + e];
-              g[u] = fg.y;
-              const float* xr = X + frame_of(__float_as_int(fg.x)) * D;
-              x[u] = make_float2(d0 ? __ldg(xr + lane) : 0.0f, d1 ? __ldg(xr + lane + 32) : (dn ? 1.0f : 0.0f));
-            }
+        // frames as one 128-bit set, walked two at a time: both logit columns read from TMEM
+        // (the row's value by a shuffle), then both frames' rows loaded, then both sums
+        uint64_t lo = ((uint64_t)mk.y << 32) | mk.x, hi = ((uint64_t)mk.w << 32) | mk.z;
+        auto next = [&]() -> int {
+          if (lo) { const int f = __ffsll((long long)lo) - 1; lo &= lo - 1; return f; }
+          if (hi) { const int f = __ffsll((long long)hi) - 1; hi &= hi - 1; return 64 + f; }
+          return -1;
+        };
+        while (lo | hi) {
+          const int f0 = next(), f1 = next();
+          const uint32_t r0 = tmem_ld1(sbuf + f0);
+          const uint32_t r1 = tmem_ld1(sbuf + (f1 >= 0 ? f1 : f0));
+          tmem_ld_wait();
+          const float s0 = __shfl_sync(0xffffffffu, __uint_as_float(r0), rq);
+          const float s1 = __shfl_sync(0xffffffffu, __uint_as_float(r1), rq);
+          float g0 = 1.0f, g1 = f1 >= 0 ? 1.0f : 0.0f;
+          if (!single_comp) {
+            g0 = ex2(s0 - lds_f(lla + (uint32_t)(f0 * 4)));
+            g1 = f1 >= 0 ? ex2(s1 - lds_f(lla + (uint32_t)(f1 * 4))) : 0.0f;
           }
-#pragma unroll
-          for (int u = 0; u < 2; ++u) {
-            const float2 dx = __fadd2_rn(x[u], wc);
-            const float2 t = __fmul2_rn(make_float2(g[u], g[u]), dx);
+          const bool k0 = g0 > minGamma, k1 = g1 > minGamma;
+          float2 x0 = make_float2(0.0f, 0.0f), x1 = make_float2(0.0f, 0.0f);
+          if (k0) {
+            const float* xr = X + (row_frame ? row_frame[tile * 128 + f0] : tile * 128 + f0) * D;
+            x0 = make_float2(d0 ? __ldg(xr + lane) : 0.0f, d1 ? __ldg(xr + lane + 32) : (dn ? 1.0f : 0.0f));
+          }
+          if (k1) {
+            const float* xr = X + (row_frame ? row_frame[tile * 128 + f1] : tile * 128 + f1) * D;
+            x1 = make_float2(d0 ? __ldg(xr + lane) : 0.0f, d1 ? __ldg(xr + lane + 32) : (dn ? 1.0f : 0.0f));
+          }
+          if (k0) {
+            const float2 dx = __fadd2_rn(x0, wc);
+            const float2 t = __fmul2_rn(make_float2(g0, g0), dx);
+            Fs[j] = __fadd2_rn(Fs[j], t);
+            if (SO) Ss[j] = __ffma2_rn(t, dx, Ss[j]);
+          }
+          if (k1) {
+            const float2 dx = __fadd2_rn(x1, wc);
+            const float2 t = __fmul2_rn(make_float2(g1, g1), dx);
             Fs[j] = __fadd2_rn(Fs[j], t);
             if (SO) Ss[j] = __ffma2_rn(t, dx, Ss[j]);
           }
         }
-        while (over) {
-          // overflowed chunk c: its 32 frames again, from TMEM (same arithmetic)
-          const int c = __ffs(over) - 1;
-          over &= over - 1;
-#pragma unroll 1
-          for (int k = 0; k < 32; ++k) {
-            const int f = 32 * c + k;
-            const uint32_t raw = tmem_ld1(sbuf + f);
-            tmem_ld_wait();
-            const float sv = __shfl_sync(0xffffffffu, __uint_as_float(raw), 8 * pw + j);
-            const float l = ll2[tile * 128 + f];
-            float g = 0.0f;
-            if (single_comp) g = (r == 0 && !isnan(l)) ? 1.0f : 0.0f;
-            else if (sv - l > thr) g = ex2(sv - l);
-            if (g > minGamma) {
-              const float* xr = X + frame_of(f) * D;
-              const float2 xx = make_float2(d0 ? __ldg(xr + lane) : 0.0f, d1 ? __ldg(xr + lane + 32) : (dn ? 1.0f : 0.0f));
-              const float2 dx = __fadd2_rn(xx, wc);
-              const float2 t = __fmul2_rn(make_float2(g, g), dx);
-              Fs[j] = __fadd2_rn(Fs[j], t);
-              if (SO) Ss[j] = __ffma2_rn(t, dx, Ss[j]);
-            }
-          }
+        // a row whose FP32 sums hold kRowFlushMass of posterior mass goes to FP64 now
+        dirty |= 1u << j;
+        if (__shfl_sync(0xffffffffu, Fs[j].y, 31) >= kRowFlushMass) {
+          flush_row(j, per.slot_of(i));
+          dirty &= ~(1u << j);
         }
       }
       tc_fence_before();
-      named_sync(1 + q4, 128);  // the quadrant's lists are read: the next scan may overwrite them
-      if (lane == 0) mbar_arrive(&s_free[b]);
-      if (per.end(i, FLUSH)) {
-        // the period's sums into the FP64 partials [col][row] (reductions: no value comes back)
-        double* mypart = part + ((size_t)per.slot_of(i) * n_chunks + chunk) * K * 128 + rowa0;
+      __syncwarp();
+      if (lane == 0) {
+        mbar_arrive(&s_free[b]);
+        mbar_arrive(&z_empty[s]);
+      }
+      if (dirty && per.end(i, kNoPeriod)) {
+        // the slot ends here (a speaker piece, or this CTA's frame range)
+        const int slot = per.slot_of(i);
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          if (d0) atomicAdd(mypart + (size_t)lane * 128 + j, (double)Fs[j].x);
-          if (d1) atomicAdd(mypart + (size_t)(lane + 32) * 128 + j, (double)Fs[j].y);
-          if (SO && d0) atomicAdd(mypart + (size_t)(K / 2 + lane) * 128 + j, (double)Ss[j].x);
-          if (SO && d1) atomicAdd(mypart + (size_t)(K / 2 + lane + 32) * 128 + j, (double)Ss[j].y);
-          if (dn) atomicAdd(mypart + (size_t)D * 128 + j, (double)Fs[j].y);
-          Fs[j] = make_float2(0.0f, 0.0f);
-          Ss[j] = make_float2(0.0f, 0.0f);
-        }
+        for (int j = 0; j < 8; ++j)
+          if (dirty & (1u << j)) flush_row(j, slot);
+        dirty = 0;
       }
     }
   }
@@ -1005,8 +1014,425 @@ __global__ void __launch_bounds__(kAccThreads, 1)
   }
 }
 
-// part [slice][chunk][K][128] (centred) -> stats (caller order): thread = (chunk, d, row) sums
-// n, F'_d and S'_d over the slices in order and adds the centre back.
+constexpr int kThreads = 352;  // dense kernel: warp 0 TMA, warp 1 logits MMA, warps 2-9 epilogue, warp 10 statistics MMA
+
+// Dense statistics kernel. The component chunk's W planes are stored into TMEM once (A operand of
+// the logits MMA); Z tiles stream through an NZ-stage shared-memory ring; posteriors go from the
+// logits accumulator into TMEM in place and feed the statistics MMA, flushed to FP64 partials
+// every FLUSH tiles.
+//
+// With second-order statistics (SPLIT) the statistics MMA writes two accumulators: A takes the
+// hi x Z1 product alone and B the four smaller ones (lo x Z2, hi x Z3, lo x Z1, hi x Z2). The
+// tensor core's FP32 accumulation rounds toward zero; a bf16 x bf16 product has 16 significant
+// bits, so a component's A sum over a tile is exact as long as its frames' products lie within
+// 8 binades of each other (always so for one frame), and B's rounding is 2^-8 smaller again.
+// With one accumulator the truncation of every frame's five-product sum biased F/n and S/n by
+// -5e-8 relative, which the variance update S/n - mu^2 magnified up to 175 times (worst variance
+// 2.1e-5 relative at N = 1M, M = 2048, D = 39). The epilogue adds A + B per tile in FP32 with
+// round-to-nearest and moves the sums into FP64 every FLUSH = 8 tiles.
+
+// Statistics columns without second-order statistics: the [x | 1] columns rounded up to the MMA
+// granularity. For every D with this K (K = 2D + 1 rounded up to 16) that is the same number.
+__host__ __device__ constexpr int acc_mean_cols(int K) { return ((K - 1) / 2 + 1 + 15) / 16 * 16; }
+
+// Resources of the statistics kernel for K and SO (second-order statistics wanted). Tiles are
+// FT = 128 frames: a tcgen05.mma with M = 128 and K = 16 costs max(45.5, N / 2) cycles on GB300
+// (measured), so the logits MMA (N = frames) reaches the full rate only from N = 96 on; 64-frame
+// tiles would cost the logits 42% more. TMEM holds two 128-column posterior buffers, the W planes
+// (K/2 columns each) and ND statistics accumulators of N2 columns. Two accumulators let the
+// statistics MMAs of tile j + 1 queue behind those of tile j before the epilogue has read tile j
+// out; W plane 2 (one of the six logits products) moves to shared memory, where that product
+// reads both operands, when that makes room. Plans in order of preference: (3 W planes in TMEM,
+// 2 accumulators), (2, 2), (3, 1), (2, 1). The Z ring takes as many stages (2 or 3) as the
+// shared memory left holds.
+template <int K, bool SO>
+struct AccCfg {
+  static constexpr int FT = acc_ft(K);
+  static_assert(FT == 128, "the epilogue converts two 32-frame chunks per warp");
+  static constexpr int N2 = SO ? K : acc_mean_cols(K);
+  static constexpr bool SPLIT = SO && K <= 80;    // A and B accumulators (see above)
+  static constexpr int NSET = SPLIT ? 2 : 1;       // accumulators of N2 columns per tile
+  static constexpr int Z_PLANE = FT * K * 2;
+  static constexpr int Z_STAGE = 3 * Z_PLANE;
+  static constexpr int LL_STAGE = FT * 4;
+  static constexpr int WC3 = (3 * K / 2 + 15) / 16 * 16, WC2 = (K + 15) / 16 * 16;
+  static constexpr bool P1 = 2 * FT + WC3 + 2 * NSET * N2 <= 512;
+  static constexpr bool P2 = !P1 && 2 * FT + WC2 + 2 * NSET * N2 <= 512;
+  static constexpr bool P3 = !P1 && !P2 && 2 * FT + WC3 + NSET * N2 <= 512;
+  static constexpr int WT = (P1 || P3) ? 3 : 2;   // W planes in TMEM
+  static constexpr int ND = (P1 || P2) ? 2 : 1;   // statistics accumulators
+  static constexpr int NS = 2;                    // posterior buffers
+  static constexpr int S_COL = 0;
+  static constexpr int W_COL = NS * FT;
+  static constexpr int D_COL = (W_COL + WT * K / 2 + 15) / 16 * 16;
+  static constexpr int W2_BYTES = WT == 2 ? K * 256 : 0;  // W plane 2 image in shared memory
+  static constexpr int FIXED = W2_BYTES + 32 * 8 + 64 + 1024;
+  static constexpr int NZ = cmin(3, (227 * 1024 - FIXED) / (Z_STAGE + LL_STAGE));
+  static constexpr int OFF_Z = 0;
+  static constexpr int OFF_W2 = OFF_Z + NZ * Z_STAGE;
+  static constexpr int OFF_LL = OFF_W2 + W2_BYTES;
+  static constexpr int OFF_BAR = OFF_LL + NZ * LL_STAGE;
+  static constexpr int OFF_MISC = OFF_BAR + 32 * 8;
+  static constexpr int SMEM = cmax(OFF_MISC + 64 + 1024, 120 * 1024);
+  static constexpr int FLUSH = SPLIT ? 8 : 64 * 128 / FT;  // tiles per FP64 flush
+  static constexpr int PIECE = 64 * 128 / FT;                // tiles per speaker piece (batched calls)
+  static_assert(NZ >= 2 && NZ <= 4, "Z ring");
+  static_assert(D_COL + ND * NSET * N2 <= 512, "TMEM budget");
+  static_assert(SMEM <= 227 * 1024, "shared memory budget");
+};
+
+// SO: second-order statistics wanted. The statistics MMA multiplies and the epilogue reads N2
+// columns: all K, or the leading [x | 1] ones.
+template <int K, bool SO>
+__global__ void __launch_bounds__(kThreads, 1)
+    acc_dense_kernel(const __grid_constant__ CUtensorMap zmap, const uint16_t* __restrict__ wplanes,
+               int nTz, int nTw, const float* __restrict__ ll2, int n_tiles, int n_chunks, int slices,
+               const int* __restrict__ tile_slot, const int4* __restrict__ work, float minGamma,
+               int single_comp, const int* __restrict__ mact_dev,
+               double* __restrict__ part, int* __restrict__ err) {
+  if (mact_dev) single_comp = *mact_dev == 1;
+  using C = AccCfg<K, SO>;
+  constexpr int FT = C::FT, NZ = C::NZ, NS = C::NS, ND = C::ND, N2 = C::N2, FLUSH = C::FLUSH;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = align1024(smem_raw);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + C::OFF_BAR);
+  uint64_t* w_full = bars + 0;
+  uint64_t* z_full = bars + 1;   // [NZ <= 4]
+  uint64_t* z_empty = bars + 5;  // [NZ]
+  uint64_t* s_full = bars + 9;   // [NS <= 4]
+  uint64_t* g_full = bars + 13;  // [NS buffers][2 frame halves]
+  uint64_t* d_full = bars + 21;     // [ND]
+  uint64_t* d_empty = bars + 23;    // [ND]
+  uint64_t* mma_done = bars + 25;   // [2]: one per MMA-issuing thread
+  uint64_t* s_free = bars + 27;     // [NS]: the statistics MMAs are done with a posterior buffer
+  uint64_t* w2_full = bars + 31;    // W plane 2 in shared memory (WT == 2)
+  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(smem + C::OFF_MISC);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + C::OFF_MISC + 8);
+  float* ll_s = reinterpret_cast<float*>(smem + C::OFF_LL);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int chunk = (int)blockIdx.x % n_chunks, slice = (int)blockIdx.x / n_chunks;
+  int wchunk = chunk;  // W chunk in the planes (several models may share them)
+  int t0, nt;
+  if (work) {
+    // explicit work item: {W chunk in the planes, chunk within its model, first tile, tiles}
+    const int4 wi = work[blockIdx.x];
+    wchunk = wi.x;
+    chunk = wi.y;
+    t0 = wi.z;
+    nt = wi.w;
+  } else {
+    const int per = (n_tiles + slices - 1) / slices;
+    t0 = slice * per;
+    nt = max(0, min(n_tiles, t0 + per) - t0);
+  }
+  // Statistics go to "slots": one per speaker with tile_slot (slices never split a speaker, so
+  // each (slot, chunk) has one owner), else one per slice. An accumulation period ends at a
+  // slot change or after FLUSH tiles of the same slot.
+  Periods per(tile_slot, t0, nt, slice);
+
+  if (threadIdx.x == 0) {
+    mbar_init(w_full, 8);
+    for (int i = 0; i < NZ; ++i) {
+      mbar_init(&z_full[i], 1);
+      mbar_init(&z_empty[i], 1);
+    }
+    for (int i = 0; i < NS; ++i) {
+      mbar_init(&s_full[i], 1);
+      mbar_init(&g_full[2 * i], 8);
+      mbar_init(&g_full[2 * i + 1], 8);
+      mbar_init(&s_free[i], 1);
+    }
+    for (int i = 0; i < ND; ++i) {
+      mbar_init(&d_full[i], 1);
+      mbar_init(&d_empty[i], 8);
+    }
+    mbar_init(w2_full, 1);
+    mbar_init(&mma_done[0], 1);
+    mbar_init(&mma_done[1], 1);
+    *abort_flag = 0;
+    fence_mbar_init();
+  }
+  if (warp == 1) {
+    tmem_alloc(tmem_holder, 512);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_holder;
+
+  if (warp == 0) {
+    if (lane == 0 && nt > 0) {
+      prefetch_tmap(&zmap);
+      if (C::WT == 2) {  // W plane 2: its image is already the operand layout, one bulk copy
+        mbar_arrive_expect_tx(w2_full, C::W2_BYTES);
+        bulk_load(smem + C::OFF_W2, wplanes + (size_t)(2 * nTw + wchunk) * (K / 8) * 1024, C::W2_BYTES, w2_full);
+      }
+      int issued = 0;
+      for (int i = 0; i < nt; ++i) {
+        const int s = i % NZ;
+        if (!mbar_wait(&z_empty[s], ((i / NZ) & 1) ^ 1, abort_flag, kWaitLimit)) break;
+        mbar_arrive_expect_tx(&z_full[s], C::Z_STAGE + C::LL_STAGE);
+        uint8_t* zs = smem + C::OFF_Z + s * C::Z_STAGE;
+        const int t = t0 + i;
+        for (int p = 0; p < 3; ++p) load_image(zs + p * C::Z_PLANE, &zmap, p, nTz, K, t, &z_full[s]);
+        bulk_load(ll_s + s * FT, ll2 + (size_t)t * FT, FT * 4, &z_full[s]);
+        issued = i + 1;
+      }
+      if (*abort_flag) {  // drain the copies still in flight
+        for (int i = max(0, issued - NZ); i < issued; ++i) mbar_drain(&z_full[i % NZ], (i / NZ) & 1);
+        if (C::WT == 2) mbar_drain(w2_full, 0);
+      }
+    }
+  } else if (warp == 1 || warp == 10) {
+    // Two MMA-issuing threads on different SM sub-partitions: the logits (warp 1) and the
+    // statistics (warp 10). Each shares its sub-partition with two busy epilogue warps; split
+    // this way each needs half the issue slots. A posterior buffer is reused by the logits of
+    // tile i + NS only after the statistics of tile i released it (s_free).
+    if (lane == 0 && nt > 0) {
+      const uint32_t zb0 = smem_u32(smem + C::OFF_Z);
+      bool ok = true;
+      if (warp == 1) {
+        const uint32_t idesc_l = idesc_bf16(128, FT, false, false);
+        const uint32_t wa = tmem + C::W_COL;
+        ok = mbar_wait(w_full, 0, abort_flag, kWaitLimit);
+        if (ok && C::WT == 2) ok = mbar_wait(w2_full, 0, abort_flag, kWaitLimit);
+        const uint64_t w2d = smem_desc(smem_u32(smem + C::OFF_W2), 128 * 16, 128);
+        for (int i = 0; i < nt && ok; ++i) {
+          if (!mbar_wait(&z_full[i % NZ], (i / NZ) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
+          if (i >= NS && !mbar_wait(&s_free[i % NS], ((i - NS) / NS) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
+          tc_fence_after();
+          const uint64_t zd = smem_desc(zb0 + (i % NZ) * C::Z_STAGE, FT * 16, 128);
+          const uint32_t d = tmem + C::S_COL + (i % NS) * FT;
+#pragma unroll
+          for (int pr = 0; pr < 6; ++pr) {
+#pragma unroll
+            for (int q = 0; q < K / 16; ++q) {
+              const uint64_t bd = desc_add(zd, prod_z(pr) * C::Z_PLANE + q * 2 * FT * 16);
+              const uint32_t a = wa + prod_w(pr) * (K / 2) + q * 8;
+              if (prod_w(pr) >= C::WT) mma_ss_c<true>(d, desc_add(w2d, q * 2 * 128 * 16), bd, idesc_l);
+              else if (pr == 0 && q == 0) mma_ts_c<false>(d, a, bd, idesc_l);
+              else mma_ts_c<true>(d, a, bd, idesc_l);
+            }
+          }
+          mma_commit(&s_full[i % NS]);
+        }
+        mma_commit(&mma_done[0]);
+        mbar_drain(&mma_done[0], 0);
+      } else {
+        const uint32_t idesc_s = idesc_bf16(128, N2, false, true);
+        for (int j = 0; j < nt && ok; ++j) {
+          const int b = j % NS;
+          const uint32_t dcol = tmem + C::D_COL + (j % ND) * (C::NSET * N2);
+          const uint32_t dsmall = C::SPLIT ? dcol + N2 : dcol;  // B (the small products)
+          // the tile's operands are in its stage; an accumulator holds one tile: wait until the
+          // epilogue has read out tile j - ND
+          if (!mbar_wait(&z_full[j % NZ], (j / NZ) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
+          if (j >= ND && !mbar_wait(&d_empty[j % ND], ((j - ND) / ND) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
+          const uint32_t gb = tmem + C::S_COL + b * FT;
+          // B = Z as [N = K columns] x [K' = frames], MN-major: LBO along frames, SBO along columns
+          const uint64_t zd = smem_desc(zb0 + (j % NZ) * C::Z_STAGE, 128, FT * 16);
+#pragma unroll
+          for (int q = 0; q < FT / 16; ++q) {
+            // the posteriors of each half of the tile's frames are signalled separately, so the
+            // statistics of the first half run while the epilogue converts the second
+            if (q % (FT / 32) == 0) {
+              if (!mbar_wait(&g_full[2 * b + q / (FT / 32)], (j / NS) & 1, abort_flag, kWaitLimit)) {
+                ok = false;
+                break;
+              }
+              tc_fence_after();
+            }
+            const uint32_t hi = gb + 32 * (q >> 1) + 8 * (q & 1);
+            const uint32_t lo = hi + 16;
+            const uint64_t z1 = desc_add(zd, 0 * C::Z_PLANE + q * 2 * 128);
+            const uint64_t z2 = desc_add(zd, 1 * C::Z_PLANE + q * 2 * 128);
+            const uint64_t z3 = desc_add(zd, 2 * C::Z_PLANE + q * 2 * 128);
+            // gamma (hi + lo) x Z (z1 + z2 + z3): the five products above 2^-18, smallest first;
+            // hi x Z1 into its own accumulator when SPLIT
+            if (q == 0) mma_ts_c<false>(dsmall, lo, z2, idesc_s);
+            else mma_ts_c<true>(dsmall, lo, z2, idesc_s);
+            mma_ts_c<true>(dsmall, hi, z3, idesc_s);
+            mma_ts_c<true>(dsmall, lo, z1, idesc_s);
+            mma_ts_c<true>(dsmall, hi, z2, idesc_s);
+            if (C::SPLIT && q == 0) mma_ts_c<false>(dcol, hi, z1, idesc_s);
+            else mma_ts_c<true>(dcol, hi, z1, idesc_s);
+          }
+          if (!ok) break;
+          mma_commit(&z_empty[j % NZ]);
+          mma_commit(&d_full[j % ND]);
+          mma_commit(&s_free[b]);
+        }
+        mma_commit(&mma_done[1]);
+        mbar_drain(&mma_done[1], 0);
+      }
+    }
+  } else if (warp < 10 && nt > 0) {
+    // epilogue: thread = component row; the two warps of a lane quadrant split the work
+    const int q4 = warp & 3;
+    const int hf = (warp - 2) >> 2;
+    const int row = q4 * 32 + lane;
+    const uint32_t lane_off = (uint32_t)(q4 * 32) << 16;
+    // the chunk's W planes into TMEM (A operand of the logits MMA): planes 0-1 by one warp of
+    // the pair, plane 2 by the other; with two planes in TMEM one each
+    {
+      const int KC = K / 8;
+      const int p0 = C::WT == 2 ? hf : (hf ? 2 : 0), p1 = C::WT == 2 ? hf + 1 : (hf ? 3 : 2);
+      for (int p = p0; p < p1; ++p) {
+        const uint4* src = reinterpret_cast<const uint4*>(wplanes + ((size_t)(p * nTw + wchunk) * KC) * 1024 + (size_t)row * 8);
+        for (int c = 0; c < KC; c += 2) {
+          const uint4 u0 = __ldg(src + (size_t)c * 128), u1 = __ldg(src + (size_t)(c + 1) * 128);
+          const uint32_t w[8] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z, u1.w};
+          tmem_st8(tmem + lane_off + C::W_COL + p * (K / 2) + c * 4, w);
+        }
+      }
+      tmem_st_wait();
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(w_full);
+    }
+    constexpr int NCH = FT / 64;         // 32-frame chunks per warp (2)
+    constexpr int KCH = N2 / 16;         // 16-column chunks of the statistics
+    constexpr int KH = (KCH + 1) / 2;    // chunks per warp of a pair
+    const int kc0 = hf ? KH : 0, kc1 = hf ? KCH : KH;
+    // The statistics MMA leaves one tile's sums in D2. The epilogue reads them one tile late
+    // (after the next tile's posteriors, so that it never waits on the MMA), adds them into
+    // FP32 registers with round-to-nearest, and moves the registers into the FP64 partials at
+    // the end of each accumulation period (FLUSH tiles of one slot).
+    float dacc[KH * 16];
+#pragma unroll
+    for (int k = 0; k < KH * 16; ++k) dacc[k] = 0.0f;
+    int last_slot = -1;
+    auto readout = [&](int t, bool flush, int slot) -> bool {
+      if (!mbar_wait(&d_full[t % ND], (t / ND) & 1, abort_flag, kWaitLimit)) return false;
+      tc_fence_after();
+      const uint32_t dbase = tmem + lane_off + C::D_COL + (t % ND) * (C::NSET * N2);
+      if constexpr (C::SPLIT) {
+        // A + B per column, then into the running sums (both in FP32, round to nearest)
+#pragma unroll
+        for (int g = 0; g < KH; ++g) {
+          if (kc0 + g < kc1) {
+            uint32_t ra[16], rb[16];
+            tmem_ld16(dbase + 16 * (kc0 + g), ra);
+            tmem_ld16(dbase + N2 + 16 * (kc0 + g), rb);
+            tmem_ld_wait();
+#pragma unroll
+            for (int k = 0; k < 16; ++k)
+              dacc[g * 16 + k] += __uint_as_float(ra[k]) + __uint_as_float(rb[k]);
+          }
+        }
+      } else {
+        constexpr int RB = KH <= 3 ? KH : 2;  // loads in flight before each wait
+#pragma unroll
+        for (int g = 0; g < KH; g += RB) {
+          uint32_t r[RB][16];
+#pragma unroll
+          for (int u = 0; u < RB; ++u)
+            if (g + u < KH && kc0 + g + u < kc1) tmem_ld16(dbase + 16 * (kc0 + g + u), r[u]);
+          tmem_ld_wait();
+#pragma unroll
+          for (int u = 0; u < RB; ++u) {
+            if (g + u < KH && kc0 + g + u < kc1) {
+#pragma unroll
+              for (int k = 0; k < 16; ++k) dacc[(g + u) * 16 + k] += __uint_as_float(r[u][k]);
+            }
+          }
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&d_empty[t % ND]);
+      if (flush) {
+        double* mypart = part + ((size_t)slot * n_chunks + chunk) * K * 128 + row;  // [col][row]
+        const bool first_flush = slot != last_slot;
+        last_slot = slot;
+#pragma unroll
+        for (int cc = 0; cc < KH; ++cc) {
+          if (kc0 + cc < kc1) {
+#pragma unroll
+            for (int k = 0; k < 16; ++k) {
+              double* dst = mypart + (size_t)(16 * (kc0 + cc) + k) * 128;
+              if (first_flush) *dst = (double)dacc[cc * 16 + k];
+              else *dst += (double)dacc[cc * 16 + k];
+              dacc[cc * 16 + k] = 0.0f;
+            }
+          }
+        }
+      }
+      return true;
+    };
+    bool ok = true;
+    for (int i = 0; i < nt; ++i) {
+      const int b = i % NS;
+      // period bookkeeping of the previous tile, before begin(i) moves the run start
+      const bool end_prev = i > 0 && per.end(i - 1, FLUSH);
+      const int slot_prev = i > 0 ? per.slot_of(i - 1) : 0;
+      per.begin(i, FLUSH);
+      if (!mbar_wait(&z_full[i % NZ], (i / NZ) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
+      if (!mbar_wait(&s_full[b], (i / NS) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
+      tc_fence_after();
+      const float* lls = ll_s + (i % NZ) * FT;
+      // pass cc converts 32-frame chunk 2 cc + hf: the two warps of a quadrant finish the first
+      // half of the tile's frames together and signal it before the second half
+#pragma unroll 1
+      for (int cc = 0; cc < NCH; ++cc) {
+        const int c = 2 * cc + hf;
+        const uint32_t col = tmem + lane_off + C::S_COL + b * FT + 32 * c;
+        uint32_t v[32];
+        tmem_ld32(col, v);
+        tmem_ld_wait();
+        uint32_t hi[16], lo[16];
+        if (!single_comp) {
+#pragma unroll
+          for (int k = 0; k < 32; k += 4) {
+            const float4 l4 = *reinterpret_cast<const float4*>(lls + 32 * c + k);
+            float g0 = ex2(__uint_as_float(v[k + 0]) - l4.x);
+            float g1 = ex2(__uint_as_float(v[k + 1]) - l4.y);
+            float g2 = ex2(__uint_as_float(v[k + 2]) - l4.z);
+            float g3 = ex2(__uint_as_float(v[k + 3]) - l4.w);
+            g0 = g0 > minGamma ? g0 : 0.0f;  // NaN (padding) and 0 (trouble: +inf LSE) prune
+            g1 = g1 > minGamma ? g1 : 0.0f;
+            g2 = g2 > minGamma ? g2 : 0.0f;
+            g3 = g3 > minGamma ? g3 : 0.0f;
+            const uint32_t h01 = pack_bf16(g0, g1), h23 = pack_bf16(g2, g3);
+            hi[k >> 1] = h01;
+            hi[(k >> 1) + 1] = h23;
+            lo[k >> 1] = pack_bf16(g0 - __uint_as_float(h01 << 16), g1 - __uint_as_float(h01 & 0xffff0000u));
+            lo[(k >> 1) + 1] = pack_bf16(g2 - __uint_as_float(h23 << 16), g3 - __uint_as_float(h23 & 0xffff0000u));
+          }
+        } else {
+          // one component: every real frame has posterior 1 (padding 0)
+#pragma unroll
+          for (int k = 0; k < 32; k += 2) {
+            const float g0 = isnan(lls[32 * c + k]) ? 0.0f : 1.0f;
+            const float g1 = isnan(lls[32 * c + k + 1]) ? 0.0f : 1.0f;
+            hi[k >> 1] = pack_bf16(g0, g1);
+            lo[k >> 1] = 0u;
+          }
+        }
+        tmem_st16(col, hi);
+        tmem_st16(col + 16, lo);
+        tmem_st_wait();
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&g_full[2 * b + cc]);
+      }
+      if (i > 0 && !readout(i - 1, end_prev, slot_prev)) { ok = false; break; }
+    }
+    if (ok && !*abort_flag) readout(nt - 1, true, per.slot_of(nt - 1));
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && *abort_flag) atomicExch(err, 1);
+  if (warp == 1) {
+    tc_fence_after();
+    tmem_dealloc(tmem, 512);
+  }
+}
+
+// part [slice][chunk][K][128] -> stats (caller order): thread = (chunk, d, row) sums n, F_d and
+// S_d over the slices in order; with cent (the sparse kernel's centred sums) it adds the centre
+// back.
 __global__ void reduce_kernel(int M, int D, int K, int Mact, int n_chunks, int slices, int n_tiles,
                               const int* __restrict__ comp_of_row, const float* __restrict__ cent,
                               const double* __restrict__ part, int flags, double* __restrict__ stats) {
@@ -1027,7 +1453,7 @@ __global__ void reduce_kernel(int M, int D, int K, int Mact, int n_chunks, int s
     Fc += p[(size_t)d * 128];
     if (sv) Sc += p[(size_t)(K / 2 + d) * 128];
   }
-  const double c = (double)cent[(size_t)r * D + d];
+  const double c = cent ? (double)cent[(size_t)r * D + d] : 0.0;
   if (d == 0) stats[m] += n;
   if (flags & GMM_ACC_MEAN) stats[(size_t)M + (size_t)m * D + d] += tc_uncentre_F(Fc, n, c);
   if (sv) stats[(size_t)M + (size_t)M * D + (size_t)m * D + d] += tc_uncentre_S(Sc, Fc, n, c);
@@ -1174,12 +1600,16 @@ int launch_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev, bool bui
 
 template <int K>
 int launch_acc_part(Ctx* c, int flags) {
-  using AC = AccCfg<K>;
+  using DA = AccCfg<K, true>;
+  using DM = AccCfg<K, false>;
+  using SC = SparseCfg<K>;
   const long long Npad = c->tcx.Npad;
   const int nTz = (int)(Npad / 128), nTw = c->tcm.Mpad / 128;
   const int n_chunks = nTw;
   static bool attr_set_acc = false;
-  const int n_tiles = (int)(Npad / AC::FT);
+  const int n_tiles = (int)(Npad / DA::FT);
+  const bool so = (flags & GMM_ACC_VAR) != 0;  // second-order statistics
+  const bool sparse = tc_stats_centred(K, so);
   // CTAs = component chunks x frame slices, one CTA per SM at a time: `waves` full waves of the
   // SMs (more waves = finer slices, which fill the SMs that a single wave leaves idle, at the
   // cost of more CTA start-ups). The autotuner measures 1-3 waves once per shape.
@@ -1194,20 +1624,26 @@ int launch_acc_part(Ctx* c, int flags) {
     c->tcpart_cap = pneed;
   }
   if (!attr_set_acc) {
-    cudaFuncSetAttribute(acc_kernel<K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, AC::SMEM);
-    cudaFuncSetAttribute(acc_kernel<K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, AC::SMEM);
+    cudaFuncSetAttribute(acc_dense_kernel<K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, DA::SMEM);
+    cudaFuncSetAttribute(acc_dense_kernel<K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, DM::SMEM);
+    cudaFuncSetAttribute(acc_sparse_kernel<K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SC::SMEM);
     attr_set_acc = true;
   }
   const CUtensorMap& zm = c->tm_zfull;
-  const bool so = (flags & GMM_ACC_VAR) != 0;  // second-order statistics
+  const int* mact_dev = c->static_shapes ? c->flag + 4 : nullptr;
   auto launch_acc = [&](int sl) {
-    // the kernel adds into its partials
-    cudaMemsetAsync(c->tcpart, 0, (size_t)n_chunks * sl * 128 * K * sizeof(double), c->stream);
-    auto kern = so ? acc_kernel<K, true> : acc_kernel<K, false>;
-    kern<<<n_chunks * sl, kAccThreads, AC::SMEM, c->stream>>>(
-        zm, c->tcm.planes, c->tcm.cent, c->X, nullptr, c->D, nTz, nTw, c->tcm.ll2, n_tiles, n_chunks, sl,
-        nullptr, nullptr, c->minGamma, c->Mact == 1, c->static_shapes ? c->flag + 4 : nullptr, c->tcpart,
-        c->tc_err);
+    if (sparse) {
+      // the sparse kernel adds into its partials
+      cudaMemsetAsync(c->tcpart, 0, (size_t)n_chunks * sl * 128 * K * sizeof(double), c->stream);
+      acc_sparse_kernel<K, true><<<n_chunks * sl, kAccThreads, SC::SMEM, c->stream>>>(
+          zm, c->tcm.planes, c->tcm.cent, c->X, c->N, nullptr, c->D, nTz, nTw, c->tcm.ll2, n_tiles, n_chunks, sl,
+          nullptr, nullptr, c->minGamma, c->Mact == 1, mact_dev, c->tcpart, c->tc_err);
+    } else {
+      auto kern = so ? acc_dense_kernel<K, true> : acc_dense_kernel<K, false>;
+      kern<<<n_chunks * sl, kThreads, so ? DA::SMEM : DM::SMEM, c->stream>>>(
+          zm, c->tcm.planes, nTz, nTw, c->tcm.ll2, n_tiles, n_chunks, sl, nullptr, nullptr, c->minGamma,
+          c->Mact == 1, mact_dev, c->tcpart, c->tc_err);
+    }
   };
   int waves = 1;
   {
@@ -1248,7 +1684,7 @@ int launch_acc_part(Ctx* c, int flags) {
     long long tot = (long long)n_chunks * c->D * 128;
     reduce_kernel<<<(int)((tot + 255) / 256), 256, 0, c->stream>>>(
         c->M, c->D, K, c->static_shapes ? c->tcm.Mpad : c->Mact, n_chunks, slices, n_tiles, c->tcm.comp_of_row,
-        c->tcm.cent, c->tcpart, flags, c->stats);
+        sparse ? c->tcm.cent : nullptr, c->tcpart, flags, c->stats);
   }
   return GMM_OK;
 }
@@ -1535,7 +1971,7 @@ int tc_speaker_stats(Ctx* c, int S, const long long* offs, const long long* d_of
   int* d_ts = nullptr;
   int4* d_wk = nullptr;
   ss->S = S;
-  ss->cent = c->tcm.cent;
+  ss->cent = tc_stats_centred(K, second_order) ? c->tcm.cent : nullptr;
   ss->n_chunks = n_chunks;
   ss->K = K;
   ss->pieces = pieces;
@@ -1692,6 +2128,7 @@ int tc_map_batch(Ctx* c, const MapBatch& b) {
 
 int tc_stats_ft(int K) { return acc_ft(K); }
 int tc_flush_tiles(int K) { return 64 * 128 / acc_ft(K); }
+bool tc_stats_centred(int K, bool second_order) { return second_order && K > 80; }
 int tc_k(int D) { return tc_K(D); }
 
 int tc_make_wmap(Ctx* c, CUtensorMap* map, const uint16_t* planes, long long rows, int K) {
@@ -1711,12 +2148,15 @@ template <int K>
 // the whole batch
 void run_batch_k(Ctx* c, const TcBatch& b, const CUtensorMap& zfull, int tile0, int ntl, int stages) {
   using LC = LlCfg<K>;
-  using AC = AccCfg<K>;
+  using DA = AccCfg<K, true>;
+  using DM = AccCfg<K, false>;
+  using SC = SparseCfg<K>;
   const int nTz = (int)(b.Rpad / 128);
   const int grid_ll = std::max(1, std::min(ntl, c->sms));
   cudaFuncSetAttribute(ll_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, LC::SMEM);
-  cudaFuncSetAttribute(acc_kernel<K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, AC::SMEM);
-  cudaFuncSetAttribute(acc_kernel<K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, AC::SMEM);
+  cudaFuncSetAttribute(acc_dense_kernel<K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, DA::SMEM);
+  cudaFuncSetAttribute(acc_dense_kernel<K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, DM::SMEM);
+  cudaFuncSetAttribute(acc_sparse_kernel<K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SC::SMEM);
   if ((stages & 1) && ntl > 0) {
     GMM_LAUNCH(c, "tc_ll_kernel");
     ll_kernel<K><<<grid_ll, kLlThreads, LC::SMEM, c->stream>>>(
@@ -1727,12 +2167,17 @@ void run_batch_k(Ctx* c, const TcBatch& b, const CUtensorMap& zfull, int tile0, 
   if ((stages & 2) && b.n_work > 0) {
     GMM_LAUNCH(c, "tc_acc_kernel");
     const CUtensorMap& zm = zfull;
-    auto kern = b.second_order ? acc_kernel<K, true> : acc_kernel<K, false>;
-    if (b.part_bytes) cudaMemsetAsync(b.part, 0, b.part_bytes, c->stream);  // the kernel adds into it
-    kern<<<b.n_work, kAccThreads, AC::SMEM, c->stream>>>(
-        zm, b.wplanes, b.cent, b.X, b.row_frame, b.D, nTz, b.w_chunks_total, b.ll2, (int)(b.Rpad / AC::FT),
-        b.n_chunks, 1, b.tile_slot,
-        b.work, c->minGamma, b.single_comp, nullptr, b.part, c->tc_err);
+    if (tc_stats_centred(K, b.second_order)) {
+      if (b.part_bytes) cudaMemsetAsync(b.part, 0, b.part_bytes, c->stream);  // the kernel adds into it
+      acc_sparse_kernel<K, true><<<b.n_work, kAccThreads, SC::SMEM, c->stream>>>(
+          zm, b.wplanes, b.cent, b.X, b.N, b.row_frame, b.D, nTz, b.w_chunks_total, b.ll2, (int)(b.Rpad / SC::FT),
+          b.n_chunks, 1, b.tile_slot, b.work, c->minGamma, b.single_comp, nullptr, b.part, c->tc_err);
+    } else {
+      auto kern = b.second_order ? acc_dense_kernel<K, true> : acc_dense_kernel<K, false>;
+      kern<<<b.n_work, kThreads, b.second_order ? DA::SMEM : DM::SMEM, c->stream>>>(
+          zm, b.wplanes, nTz, b.w_chunks_total, b.ll2, (int)(b.Rpad / DA::FT), b.n_chunks, 1, b.tile_slot,
+          b.work, c->minGamma, b.single_comp, nullptr, b.part, c->tc_err);
+    }
   }
 }
 }  // namespace

@@ -163,18 +163,21 @@ def test_tc_autotune_choice_and_results(glib):
 def test_accumulate_host_streams_features(glib, N):
     """gmm_accumulate_host (chunked host-to-device copies overlapping the E-step) gives the same
     statistics as gmm_upload_features + gmm_accumulate: n, F, S bit-identical (the same
-    statistics kernel over the same planes), total LL within 1e-12 rel (the LL partials are
+    statistics kernel over the same planes and the same decomposition -- the autotuner is off in
+    both, as its choice regroups the FP32 sums), total LL within 1e-12 rel (the LL partials are
     grouped per chunk); the features stay resident for the next E-step."""
     from gmm_gb300 import synth
     X, w, mu, var = synth.config_em(5, N, 39, 32, 64)
     a = glib.Handle(0)
     a.set_precision(glib.PREC_TC)
+    a.set_autotune(False)
     a.upload_model(w, mu, var)
     a.upload_features(X)
     ref = a.accumulate()
     a.close()
     b = glib.Handle(0)
     b.set_precision(glib.PREC_TC)
+    b.set_autotune(False)
     b.upload_model(w, mu, var)
     b.accumulate_host(X)
     st = b.read_stats()
