@@ -448,8 +448,8 @@ int launch(Server* s, Batch& b) {
   if (e != cudaSuccess) return cuda_fail(c, e, "server: cudaMemcpyAsync(batch frames)");
   cudaEventRecord(s->copied[b.slot], s->copy_stream);
   cudaStreamWaitEvent(c->stream, s->copied[b.slot], 0);
+  // the statistics pieces (zeroed by the statistics launch, which adds into them)
   const long long pieces_bytes = (long long)((const char*)b.rll - (const char*)b.part);
-  if (b.n_work > 0) cudaMemsetAsync(b.part, 0, (size_t)pieces_bytes, c->stream);
   TcBatch t;
   t.D = s->D;
   t.K = s->K;

@@ -1029,7 +1029,7 @@ constexpr int kThreads = 352;  // dense kernel: warp 0 TMA, warp 1 logits MMA, w
 // With one accumulator the truncation of every frame's five-product sum biased F/n and S/n by
 // -5e-8 relative, which the variance update S/n - mu^2 magnified up to 175 times (worst variance
 // 2.1e-5 relative at N = 1M, M = 2048, D = 39). The epilogue adds A + B per tile in FP32 with
-// round-to-nearest and moves the sums into FP64 every FLUSH = 8 tiles.
+// round-to-nearest and moves the sums into FP64 every FLUSH = 16 tiles.
 
 // Statistics columns without second-order statistics: the [x | 1] columns rounded up to the MMA
 // granularity. For every D with this K (K = 2D + 1 rounded up to 16) that is the same number.
@@ -1074,7 +1074,7 @@ struct AccCfg {
   static constexpr int OFF_BAR = OFF_LL + NZ * LL_STAGE;
   static constexpr int OFF_MISC = OFF_BAR + 32 * 8;
   static constexpr int SMEM = cmax(OFF_MISC + 64 + 1024, 120 * 1024);
-  static constexpr int FLUSH = SPLIT ? 8 : 64 * 128 / FT;  // tiles per FP64 flush
+  static constexpr int FLUSH = SPLIT ? 16 : 64 * 128 / FT;  // tiles per FP64 flush
   static constexpr int PIECE = 64 * 128 / FT;                // tiles per speaker piece (batched calls)
   static_assert(NZ >= 2 && NZ <= 4, "Z ring");
   static_assert(D_COL + ND * NSET * N2 <= 512, "TMEM budget");
@@ -1303,7 +1303,6 @@ __global__ void __launch_bounds__(kThreads, 1)
     float dacc[KH * 16];
 #pragma unroll
     for (int k = 0; k < KH * 16; ++k) dacc[k] = 0.0f;
-    int last_slot = -1;
     auto readout = [&](int t, bool flush, int slot) -> bool {
       if (!mbar_wait(&d_full[t % ND], (t / ND) & 1, abort_flag, kWaitLimit)) return false;
       tc_fence_after();
@@ -1344,17 +1343,15 @@ __global__ void __launch_bounds__(kThreads, 1)
       __syncwarp();
       if (lane == 0) mbar_arrive(&d_empty[t % ND]);
       if (flush) {
-        double* mypart = part + ((size_t)slot * n_chunks + chunk) * K * 128 + row;  // [col][row]
-        const bool first_flush = slot != last_slot;
-        last_slot = slot;
+        // into the zeroed FP64 partials [col][row] by reductions: no value comes back, so the
+        // warp does not wait; each partial has this one writer thread (a fixed order of additions)
+        double* mypart = part + ((size_t)slot * n_chunks + chunk) * K * 128 + row;
 #pragma unroll
         for (int cc = 0; cc < KH; ++cc) {
           if (kc0 + cc < kc1) {
 #pragma unroll
             for (int k = 0; k < 16; ++k) {
-              double* dst = mypart + (size_t)(16 * (kc0 + cc) + k) * 128;
-              if (first_flush) *dst = (double)dacc[cc * 16 + k];
-              else *dst += (double)dacc[cc * 16 + k];
+              atomicAdd(mypart + (size_t)(16 * (kc0 + cc) + k) * 128, (double)dacc[cc * 16 + k]);
               dacc[cc * 16 + k] = 0.0f;
             }
           }
@@ -1632,9 +1629,9 @@ int launch_acc_part(Ctx* c, int flags) {
   const CUtensorMap& zm = c->tm_zfull;
   const int* mact_dev = c->static_shapes ? c->flag + 4 : nullptr;
   auto launch_acc = [&](int sl) {
+    // both kernels add into their partials
+    cudaMemsetAsync(c->tcpart, 0, (size_t)n_chunks * sl * 128 * K * sizeof(double), c->stream);
     if (sparse) {
-      // the sparse kernel adds into its partials
-      cudaMemsetAsync(c->tcpart, 0, (size_t)n_chunks * sl * 128 * K * sizeof(double), c->stream);
       acc_sparse_kernel<K, true><<<n_chunks * sl, kAccThreads, SC::SMEM, c->stream>>>(
           zm, c->tcm.planes, c->tcm.cent, c->X, c->N, nullptr, c->D, nTz, nTw, c->tcm.ll2, n_tiles, n_chunks, sl,
           nullptr, nullptr, c->minGamma, c->Mact == 1, mact_dev, c->tcpart, c->tc_err);
@@ -2167,8 +2164,8 @@ void run_batch_k(Ctx* c, const TcBatch& b, const CUtensorMap& zfull, int tile0, 
   if ((stages & 2) && b.n_work > 0) {
     GMM_LAUNCH(c, "tc_acc_kernel");
     const CUtensorMap& zm = zfull;
+    if (b.part_bytes) cudaMemsetAsync(b.part, 0, b.part_bytes, c->stream);  // the kernels add into it
     if (tc_stats_centred(K, b.second_order)) {
-      if (b.part_bytes) cudaMemsetAsync(b.part, 0, b.part_bytes, c->stream);  // the kernel adds into it
       acc_sparse_kernel<K, true><<<b.n_work, kAccThreads, SC::SMEM, c->stream>>>(
           zm, b.wplanes, b.cent, b.X, b.N, b.row_frame, b.D, nTz, b.w_chunks_total, b.ll2, (int)(b.Rpad / SC::FT),
           b.n_chunks, 1, b.tile_slot, b.work, c->minGamma, b.single_comp, nullptr, b.part, c->tc_err);
