@@ -5,11 +5,12 @@ and exact-in-FP32 operand splits, so it is compared with the FP64 oracle (not wi
 replica). Tolerances, written per quantity:
   per-frame log-likelihood   |diff| <= 2e-4 + 2e-6 |ll|
   total log-likelihood       rel <= 1e-6
-  statistics                 |diff| <= 1e-3 * (scale of the component's statistic) -- posteriors
+  statistics                 |diff| <= 1e-4 * (scale of the component's statistic) -- posteriors
                              near the minGamma cut may land on the other side, which moves a
                              statistic by at most minGamma * |x| per frame
-  EM update (means/vars)     rel <= 1e-4 after one iteration at these small sizes (the 1e-5
-                             target of the full-size workload is measured by bench.py)
+  EM update                  weights rel <= 1e-5, means |diff| <= 1e-5 of the standard deviation,
+                             variances rel <= 1e-5 (as at the full UBM size,
+                             tests/test_tc_accuracy_gpu.py)
 """
 import numpy as np
 import pytest
@@ -23,7 +24,7 @@ def tc_handle(glib):
     return h
 
 
-def check_stats(s, o, rel=1e-3):
+def check_stats(s, o, rel=1e-4):
     for k in ("n", "F", "S"):
         scale = np.maximum(np.abs(o[k]), np.abs(o["n"])[:, None] if k != "n" else 1.0) + 1.0
         err = np.abs(s[k] - o[k]) / scale
@@ -89,9 +90,10 @@ def test_tc_em_iteration_close_to_fp64(glib, oracle, golden):
     ow, omu, ovar, _ = oracle.em_update64(g["w"], o)
     w, mu, var = h.read_model()
     assert abs(ll[0] - o["totLL"]) <= 1e-6 * abs(o["totLL"])
-    assert np.allclose(w, ow, rtol=1e-4)
-    assert np.allclose(mu, omu, rtol=1e-4, atol=1e-4)
-    assert np.allclose(var, ovar, rtol=1e-4)
+    live = ow > 0
+    assert (np.abs(w - ow) / np.where(live, ow, 1.0))[live].max() <= 1e-5
+    assert (np.abs(mu - omu) / np.sqrt(ovar))[live].max() <= 1e-5
+    assert (np.abs(var - ovar) / ovar)[live].max() <= 1e-5
     h.close()
 
 
