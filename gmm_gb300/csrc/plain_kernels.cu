@@ -510,13 +510,8 @@ namespace {
 constexpr size_t kNoAllocScratchBytes = (size_t)32 << 20;  // 32 MiB per device
 constexpr int kNoAllocMaxMix = 4096;
 constexpr int kNoAllocMaxDim = 128;
-constexpr size_t kNoAllocPartBytes = (size_t)4 << 20;       // per-slice partial statistics
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
-
-constexpr int kMaxDevices = 64;
-static void* g_noalloc_ptr[kMaxDevices];
-static bool g_noalloc_ready[kMaxDevices];
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
@@ -536,21 +531,18 @@ extern "C" int gmm_accumulate_noalloc(const float* dX, long long N, int D, int M
                 "(fixed 32 MiB scratch)");
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+  if (e != cudaSuccess)
     return fail(nullptr, GMM_ERR_CUDA, "gmm_accumulate_noalloc: no current CUDA device");
-  // once per device, with that device current: the device address of the scratch array
-  if (!g_noalloc_ready[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) {
-      cudaGetLastError();
-      return fail(nullptr, GMM_ERR_CUDA,
-                  std::string("gmm_accumulate_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-    }
-    g_noalloc_ptr[dev] = p;
-    g_noalloc_ready[dev] = true;
+  // The scratch array's address in the current device's context, looked up on every call (no
+  // cache): it is valid for this context only, and a cudaDeviceReset gives the device a new one.
+  void* scratch = nullptr;
+  e = cudaGetSymbolAddress(&scratch, g_noalloc_scratch);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(nullptr, GMM_ERR_CUDA,
+                std::string("gmm_accumulate_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
   }
-  unsigned char* base = static_cast<unsigned char*>(g_noalloc_ptr[dev]);
+  unsigned char* base = static_cast<unsigned char*>(scratch);
   const int E = 1 + 2 * D;
 
   // carve the scratch: flags | active list | icov | logG | logW | partials | LL | LL partials | posteriors
@@ -577,8 +569,6 @@ extern "C" int gmm_accumulate_noalloc(const float* dX, long long N, int D, int M
   c.icov = reinterpret_cast<float*>(base + off); off = align_up(off + sizeof(float) * (size_t)M * D, 256);
   c.logG = reinterpret_cast<float*>(base + off); off = align_up(off + sizeof(float) * M, 256);
   c.logW = reinterpret_cast<float*>(base + off); off = align_up(off + sizeof(float) * M, 256);
-  c.part = reinterpret_cast<double*>(base + off); off = align_up(off + kNoAllocPartBytes, 256);
-  const size_t rest = kNoAllocScratchBytes - off;
 
   // calls share the scratch: clear what must start at zero (flags) and the caller's output
   e = cudaMemsetAsync(c.flag, 0, 16 * sizeof(int), c.stream);
@@ -589,10 +579,25 @@ extern "C" int gmm_accumulate_noalloc(const float* dX, long long N, int D, int M
   if (rc) return fail(nullptr, rc, c.err);
   if (c.Mact <= 0) return fail(nullptr, GMM_ERR_STATE, "gmm_accumulate_noalloc: no component with non-zero weight");
 
-  // frame chunk: posteriors [Mact][chunk] + LL [chunk] + LL partials [chunk / 256] in `rest`
-  long long chunk = (long long)(rest / (sizeof(float) * (size_t)c.Mact + sizeof(float) + sizeof(double)));
-  chunk = chunk / 256 * 256 - 256;
-  if (chunk < 256) return fail(nullptr, GMM_ERR_UNSUPPORTED, "gmm_accumulate_noalloc: model too large for the scratch");
+  // The rest of the scratch: per-slice partial statistics [slices][Mact][E] (FP64), then a frame
+  // chunk of posteriors [Mact][chunk] + LL [chunk] + LL partials [chunk / 256]. The partials get
+  // as many slices as the frames want (as gmm_accumulate picks them), at most half of what is
+  // left and at least one; the model must leave room for one slice and 256 frames.
+  const size_t avail = kNoAllocScratchBytes - off;
+  const size_t slice_bytes = sizeof(double) * (size_t)c.Mact * E;
+  const size_t frame_bytes = sizeof(float) * (size_t)c.Mact + sizeof(float) + sizeof(double);
+  const size_t min_chunk_bytes = frame_bytes * 256 + 3 * 256;
+  if (align_up(slice_bytes, 256) + min_chunk_bytes > avail)
+    return fail(nullptr, GMM_ERR_UNSUPPORTED,
+                "gmm_accumulate_noalloc: model too large for the 32 MiB scratch (one slice of statistics "
+                "and 256 frames of posteriors do not fit)");
+  long long slice_cap = (long long)((avail - min_chunk_bytes) / slice_bytes);
+  const long long half_cap = (long long)((avail / 2) / slice_bytes);
+  if (half_cap >= 1 && half_cap < slice_cap) slice_cap = half_cap;
+  c.part = reinterpret_cast<double*>(base + off);
+  off = align_up(off + slice_bytes * (size_t)slice_cap, 256);
+  long long chunk = (long long)((kNoAllocScratchBytes - off - 3 * 256) / frame_bytes);
+  chunk = chunk / 256 * 256;
   if (chunk > N) chunk = (N + 255) / 256 * 256;
   if (chunk < 256) chunk = 256;
   c.logits = reinterpret_cast<float*>(base + off); off = align_up(off + sizeof(float) * (size_t)c.Mact * chunk, 256);
@@ -613,12 +618,13 @@ extern "C" int gmm_accumulate_noalloc(const float* dX, long long N, int D, int M
     else if (D <= 64) launch_ll<64>(&c, f0, nf, c.logits, chunk, llbuf, blocks);
     else launch_ll<128>(&c, f0, nf, c.logits, chunk, llbuf, blocks);
     ll_total_kernel<<<1, 1024, 0, c.stream>>>(blocks, c.llpart, c.stats + (size_t)M * E);
+    // frame slices as gmm_accumulate picks them (about 64 warps per SM, at least 256 frames
+    // each, a multiple of 4), then at most what the carved partials hold
     long long slices = 152LL * 64 / c.Mact;
     if (slices > nf / 256) slices = nf / 256;
-    const long long max_slices = (long long)(kNoAllocPartBytes / (sizeof(double) * (size_t)c.Mact * E));
-    if (slices > max_slices) slices = max_slices;
     if (slices < 1) slices = 1;
-    slices = slices / 4 * 4 > 0 ? slices / 4 * 4 : slices;
+    slices = (slices + 3) / 4 * 4;
+    if (slices > slice_cap) slices = slice_cap;
     long long slice_len = (nf + slices - 1) / slices;
     slice_len = (slice_len + 31) / 32 * 32;
     // the statistics kernel reads LL as ll[f0 + i] from c.ll

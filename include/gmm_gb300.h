@@ -243,13 +243,17 @@ int gmm_mllr_apply(gmm_handle h, const double* W);
  * gmm_accumulate computes with the plain FP32 path, from caller-owned device arrays
  * (dX [N][D], dw [M], dmu [M][D], dvar [M][D]) into the caller-owned device array
  * d_stats = n[M] | F[M*D] | S[M*D] | total log-likelihood (FP64, zeroed first), on `stream`
- * (a cudaStream_t; NULL = legacy default stream), and returns after the work finished.
+ * (a cudaStream_t; NULL = legacy default stream). The call is synchronous: it synchronises
+ * `stream` before it returns, so the statistics are ready on return.
  * Working memory is one fixed 32 MiB array compiled into the library; every GPU that loads the
- * library keeps it until the process exits. Limits: M <= 4096, D <= 128 (GMM_ERR_UNSUPPORTED
- * beyond). The first call on a device looks up the array's device address (no allocation); make
- * that first call before any stream capture. All calls share the array, so calls that overlap
- * on the GPU (different streams or threads at the same time) race; serialise them. Errors are
- * reported through gmm_last_error(NULL). */
+ * library keeps it until the process exits. Limits: M <= 4096, D <= 128, and one slice of
+ * statistics (8 * M_active * (1 + 2D) bytes) plus 256 frames of posteriors must fit beside the
+ * model tables (GMM_ERR_UNSUPPORTED beyond; every M <= 4096, D <= 128 fits). Each call looks up
+ * the array's address in the current context (no allocation, so a cudaDeviceReset between calls
+ * is harmless); the first call on a device may load the library's device code, so make that
+ * first call before any stream capture. All calls share the array, so calls that overlap on the
+ * GPU (different streams or threads at the same time) race; serialise them. Errors are reported
+ * through gmm_last_error(NULL). */
 int gmm_accumulate_noalloc(const float* dX, long long N, int D, int M, const float* dw,
                            const float* dmu, const float* dvar, float min_loglike, float min_gamma,
                            float min_var, int flags, double* d_stats, void* stream);

@@ -46,6 +46,29 @@ def test_noalloc_matches_accumulate_twice(glib):
             assert np.allclose(got[k], ref[k], rtol=1e-12, atol=1e-9), k
 
 
+@pytest.mark.parametrize("M,D,N", [(4096, 64, 5000), (2048, 128, 5000), (4096, 128, 6000),
+                                   (4096, 128, 300)])
+def test_noalloc_largest_models(glib, M, D, N):
+    """The largest models the scratch takes: the per-slice partial statistics are sized from
+    M * (1 + 2D), so at M = 4096, D = 128 one slice fills 8.4 MB and a frame chunk holds about
+    1300 frames -- N = 6000 runs several chunks through the same scratch, N = 300 one short
+    chunk. Two calls in a row, against gmm_accumulate on the same inputs."""
+    torch = pytest.importorskip("torch")
+    from gmm_gb300 import synth
+    X, w, mu, var = synth.config_em(43 + D, N, D, 16, M)
+    h = glib.Handle(0)
+    h.upload_model(w, mu, var)
+    h.upload_features(X)
+    ref = h.accumulate(glib.ACC_MEAN | glib.ACC_VAR)
+    h.close()
+    for _ in range(2):
+        got = run_noalloc(glib, torch, X, w, mu, var, glib.ACC_MEAN | glib.ACC_VAR)
+        assert abs(got["totLL"] - ref["totLL"]) <= 1e-12 * abs(ref["totLL"])
+        for k in ("n", "F", "S"):
+            assert np.all(np.isfinite(got[k])), k
+            assert np.allclose(got[k], ref[k], rtol=1e-12, atol=1e-9), k
+
+
 def test_noalloc_rejects_oversize(glib):
     torch = pytest.importorskip("torch")
     lib = glib.load()
