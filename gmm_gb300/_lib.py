@@ -69,6 +69,7 @@ SIGNATURES = {
     "gmm_launch_count": (_ll, [_vp]),
     "gmm_accumulate_noalloc": (_i, [_vp, _ll, _i, _i, _vp, _vp, _vp, _f, _f, _f, _i, _vp, _vp]),
     "gmm_set_autotune": (_i, [_vp, _i]),
+    "gmm_set_wait_limit": (_i, [_vp, _ll]),
     "gmm_autotune_choice": (_i, [_vp, C.POINTER(_i), _vp, _vp, _i]),
     "gmm_read_param": (_i, [C.c_char_p, _i, C.c_uint, _vp, _ll, C.POINTER(_ll), C.POINTER(_i)]),
     "gmm_accumulate_files": (_i, [_vp, _i, _i, C.POINTER(C.c_char_p), _i, C.c_uint, _d, C.POINTER(_i)]),
@@ -172,6 +173,10 @@ class Handle:
 
     def set_autotune(self, on: bool):
         self.check(self.lib.gmm_set_autotune(self.h, int(on)))
+
+    def set_wait_limit(self, cycles: int):
+        """Test hook: clock cycles a tensor-core pipeline wait may take (<= 0: the default)."""
+        self.check(self.lib.gmm_set_wait_limit(self.h, int(cycles)))
 
     def autotune_choices(self) -> dict:
         n = C.c_int()

@@ -231,10 +231,10 @@ __global__ void __launch_bounds__(kFtThreads, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_holder;
+  int issued = 0;  // B stage copies issued (loader thread)
 
   if (warp == 0) {
     if (lane == 0) {
-      int issued = 0;
       for (int sidx = 0; sidx < steps; ++sidx) {
         const int st = sidx % NB, g = sidx % ng;
         if (!mbar_wait(&b_empty[st], ((sidx / NB) & 1) ^ 1, abort_flag, kFtWait)) break;
@@ -242,12 +242,6 @@ __global__ void __launch_bounds__(kFtThreads, 1)
         bulk_load(smem + st * C::B_STAGE, Bimg + (size_t)g * 3 * N * KX, C::B_STAGE, &b_full[st]);
         issued = sidx + 1;
       }
-      if (*abort_flag)
-        for (int sidx = max(0, issued - NB); sidx < issued; ++sidx) {
-          const long long t0 = clock64();
-          while (!mbar_try_wait(&b_full[sidx % NB], (sidx / NB) & 1))
-            if (clock64() - t0 > kFtWait) break;
-        }
     }
   } else if (warp == 1) {
     if (lane == 0) {
@@ -375,6 +369,15 @@ __global__ void __launch_bounds__(kFtThreads, 1)
     if (lane == 0) s_red[q4] = v;
   }
   __syncthreads();
+  if (*abort_flag && warp == 0 && lane == 0) {
+    // Every role has stopped. The loader's last NB copies may still be in flight (a consumer
+    // that gave up never waited for them): let them land before the CTA's shared memory goes.
+    for (int sidx = max(0, issued - NB); sidx < issued; ++sidx) {
+      const long long t0 = clock64();
+      while (!mbar_try_wait(&b_full[sidx % NB], (sidx / NB) & 1))
+        if (clock64() - t0 > kFtWait) break;
+    }
+  }
   if (threadIdx.x == 0) {
     if (*abort_flag) atomicExch(err, 1);
     llpart[blockIdx.x] = s_red[0] + s_red[1] + s_red[2] + s_red[3];

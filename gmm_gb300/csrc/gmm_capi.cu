@@ -339,6 +339,15 @@ int gmm_set_autotune(gmm_handle h, int on) {
   return GMM_OK;
 }
 
+int gmm_set_wait_limit(gmm_handle h, long long cycles) {
+  if (!h) return GMM_ERR_ARG;
+  h->wait_limit = cycles > 0 ? cycles : kDefaultWaitLimit;
+  // the captured EM iteration holds the old limit as a kernel argument
+  if (h->em_graph) cudaGraphExecDestroy(h->em_graph);
+  h->em_graph = nullptr;
+  return GMM_OK;
+}
+
 int gmm_autotune_choice(gmm_handle h, int* n, long long* keys, int* waves, int cap) {
   if (!h || !n) return GMM_ERR_ARG;
   int k = 0;
@@ -1021,6 +1030,7 @@ static int em_iterate_graph(Ctx* c, int iters, int upW, int upM, int upV, double
     rc = sync(c, "gmm_em_iterate");
   }
   if (!rc && herr) {
+    c->tcx_valid = false;  // kernels that gave up may have left the feature planes half built
     cudaMemsetAsync(c->tc_err, 0, sizeof(int), c->stream);
     rc = fail(c, GMM_ERR_TIMEOUT, "tensor-core E-step: a bounded device wait expired");
   }

@@ -16,6 +16,9 @@ namespace gmm {
 constexpr double kMinusLog2Pi = -1.837877066409345;  // OL_GMMStatsEstimator.h:280
 constexpr int kMaxMix = 32767;                        // GMModel::NumMixes is __int16
 constexpr int kMaxDim = 1024;
+// How long (clock cycles, ~2 s) a tensor-core pipeline role may wait on an mbarrier before it
+// gives up, raises the CTA's abort flag and the kernel reports GMM_ERR_TIMEOUT.
+constexpr long long kDefaultWaitLimit = 4000000000LL;
 
 // ------------------------------------------------------------------ error plumbing
 struct Error {
@@ -106,6 +109,7 @@ struct Ctx {
   size_t tcpart_cap = 0;
   CUtensorMap tm_zfull, tm_wfull;  // TMA maps over the operand images (box = one 128-row tile)
   int* tc_err = nullptr;                          // bounded-wait expiry flag
+  long long wait_limit = kDefaultWaitLimit;       // clock cycles a pipeline wait may take
   double* tc_llpart = nullptr;                    // per-thread log-likelihood partials
   size_t tc_llpart_cap = 0;
   int sms = 0;

@@ -170,10 +170,10 @@ __global__ void __launch_bounds__(kThreadsG, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_holder;
+  int issued = 0;  // stage copies issued (loader thread)
 
   if (warp == 0) {
     if (lane == 0) {
-      int issued = 0;
       for (int j = 0; j < nst; ++j) {
         const int sg = j % kStages;
         if (!mbar_wait(&z_empty[sg], ((j / kStages) & 1) ^ 1, abort_flag, kWait)) break;
@@ -184,8 +184,6 @@ __global__ void __launch_bounds__(kThreadsG, 1)
         for (int p = 0; p < 3; ++p) bulk_load(dst + 3 * A_P + p * B_P, b_img + p * b_plane + off_b, B_P, &z_full[sg]);
         issued = j + 1;
       }
-      if (*abort_flag)
-        for (int j = max(0, issued - kStages); j < issued; ++j) mbar_drain_g(&z_full[j % kStages], (j / kStages) & 1);
     }
   } else if (warp == 1) {
     if (lane == 0) {
@@ -268,7 +266,14 @@ __global__ void __launch_bounds__(kThreadsG, 1)
     }
   }
   __syncthreads();
-  if (threadIdx.x == 0 && *abort_flag) atomicExch(err, 1);
+  if (*abort_flag) {
+    // Every role has stopped. The loader's last kStages copies may still be in flight (a
+    // consumer that gave up never waited for them): let them land before the CTA's shared
+    // memory goes.
+    if (warp == 0 && lane == 0)
+      for (int j = max(0, issued - kStages); j < issued; ++j) mbar_drain_g(&z_full[j % kStages], (j / kStages) & 1);
+    if (threadIdx.x == 0) atomicExch(err, 1);
+  }
   if (warp == 1) {
     tc_fence_after();
     tmem_dealloc(tmem, 512);

@@ -66,7 +66,7 @@ namespace {
 
 constexpr double kLog2e = 1.4426950408889634;
 constexpr float kLn2 = 0.69314718055994531f;
-constexpr long long kWaitLimit = 4000000000LL;  // clock cycles (~2 s)
+constexpr long long kWaitLimit = kDefaultWaitLimit;  // the exit-path drains always use it
 
 // ------------------------------------------------------------------ operand preparation
 
@@ -372,7 +372,7 @@ __global__ void __launch_bounds__(kLlThreads, 1)
               long long N, const long long* __restrict__ row_frame, const int* __restrict__ tile_wbase,
               int nTz, int nTw, int tile0, int n_tiles, int n_chunks, float trouble2, float minLL,
               float* __restrict__ ll2_out, float* __restrict__ ll_out, double* __restrict__ llpart,
-              int* __restrict__ err, const float* __restrict__ X, int D) {
+              int* __restrict__ err, const float* __restrict__ X, int D, long long wait_limit) {
   // frame tiles tile0 .. tile0 + n_tiles - 1, strided over the CTAs. With X the loaders build
   // the Z tiles from the raw features (and write the plane images for the statistics kernel);
   // without, they copy them from the plane images.
@@ -426,6 +426,7 @@ __global__ void __launch_bounds__(kLlThreads, 1)
   tc_fence_after();
   const uint32_t tmem = *tmem_holder;
   const int my_tiles = (n_tiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
+  int w_issued = 0;  // W chunk copies issued (loader thread)
 
   if (warp == 0) {
     if (lane == 0 && my_tiles > 0) {
@@ -437,16 +438,13 @@ __global__ void __launch_bounds__(kLlThreads, 1)
         const int wbase = tile_wbase ? tile_wbase[tile0 + (int)blockIdx.x + it * (int)gridDim.x] : 0;
         for (int ch = 0; ch < n_chunks; ++ch, ++j) {
           const int ws = j % NW;
-          if (!mbar_wait(&w_empty[ws], ((j / NW) & 1) ^ 1, abort_flag, kWaitLimit)) { ok = false; break; }
+          if (!mbar_wait(&w_empty[ws], ((j / NW) & 1) ^ 1, abort_flag, wait_limit)) { ok = false; break; }
           mbar_arrive_expect_tx(&w_full[ws], C::W_STAGE);
           uint8_t* dst = smem + C::OFF_W + ws * C::W_STAGE;
           for (int p = 0; p < 3; ++p)
             load_image(dst + p * C::W_PLANE, &wfull, p, nTw, K, wbase + ch, &w_full[ws]);
+          w_issued = j + 1;
         }
-      }
-      if (!ok) {  // drain the copies still in flight
-        const int last = j;
-        for (int k = max(0, last - NW); k < last; ++k) mbar_drain(&w_full[k % NW], (k / NW) & 1);
       }
     }
   } else if (warp == 1 || warp == 14) {
@@ -458,13 +456,13 @@ __global__ void __launch_bounds__(kLlThreads, 1)
       bool ok = true;
       for (int it = 0; it < my_tiles && ok; ++it) {
         const int zb = it % ZB;
-        if (!mbar_wait(&z_full[zb], (it / ZB) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
+        if (!mbar_wait(&z_full[zb], (it / ZB) & 1, abort_flag, wait_limit)) { ok = false; break; }
         const uint32_t za = tmem + C::Z_COL + zb * C::ZCOLS;
         for (int ch = 0; ch < n_chunks; ++ch, ++j) {
           if (two_issuers && (ch & 1) != role) continue;
           const int ws = j % NW, b = j & 1;
-          if (!mbar_wait(&w_full[ws], (j / NW) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
-          if (!mbar_wait(&s_empty[b], ((j >> 1) & 1) ^ 1, abort_flag, kWaitLimit)) { ok = false; break; }
+          if (!mbar_wait(&w_full[ws], (j / NW) & 1, abort_flag, wait_limit)) { ok = false; break; }
+          if (!mbar_wait(&s_empty[b], ((j >> 1) & 1) ^ 1, abort_flag, wait_limit)) { ok = false; break; }
           tc_fence_after();
           const uint64_t wd = smem_desc(wb0 + ws * C::W_STAGE, 128 * 16, 128);
           const uint32_t d = tmem + C::S_COL + b * 128;
@@ -494,7 +492,7 @@ __global__ void __launch_bounds__(kLlThreads, 1)
     for (int it = 0; it < my_tiles; ++it) {
       const int zb = it % ZB;
       const int tile = tile0 + (int)blockIdx.x + it * (int)gridDim.x;
-      if (!mbar_wait(&z_empty[zb], ((it / ZB) & 1) ^ 1, abort_flag, kWaitLimit)) break;
+      if (!mbar_wait(&z_empty[zb], ((it / ZB) & 1) ^ 1, abort_flag, wait_limit)) break;
       tc_fence_after();
       const uint32_t zaddr = tmem + lane_off + C::Z_COL + zb * C::ZCOLS;
       auto frame_of = [&](int t) -> long long {
@@ -535,7 +533,7 @@ __global__ void __launch_bounds__(kLlThreads, 1)
       float m = -INFINITY, sum = 0.0f;
       for (int ch = 0; ch < n_chunks && ok; ++ch, ++j) {
         const int b = j & 1;
-        if (!mbar_wait(&s_full[b], (j >> 1) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
+        if (!mbar_wait(&s_full[b], (j >> 1) & 1, abort_flag, wait_limit)) { ok = false; break; }
         tc_fence_after();
         // read both 32-column halves, then hand the accumulator back to the MMA issuer before
         // doing the arithmetic: the issuer waits on this release, so it comes as early as possible
@@ -596,7 +594,14 @@ __global__ void __launch_bounds__(kLlThreads, 1)
     if (hf == 0) llpart[(size_t)blockIdx.x * 128 + row] = llsum;
   }
   __syncthreads();
-  if (threadIdx.x == 0 && *abort_flag) atomicExch(err, 1);
+  if (*abort_flag) {
+    // Every role has stopped. The loader's last NW copies may still be in flight (a consumer
+    // that gave up never waited for them): let them land before the CTA's shared memory goes.
+    // Earlier copies were consumed, so they have landed.
+    if (warp == 0 && lane == 0)
+      for (int k = max(0, w_issued - NW); k < w_issued; ++k) mbar_drain(&w_full[k % NW], (k / NW) & 1);
+    if (threadIdx.x == 0) atomicExch(err, 1);
+  }
   if (warp == 1) {
     tc_fence_after();
     tmem_dealloc(tmem, 512);
@@ -699,7 +704,7 @@ __global__ void __launch_bounds__(kAccThreads, 1)
                const long long* __restrict__ row_frame, int D, int nTz, int nTw, const float* __restrict__ ll2,
                int n_tiles, int n_chunks, int slices, const int* __restrict__ tile_slot,
                const int4* __restrict__ work, float minGamma, int single_comp, const int* __restrict__ mact_dev,
-               double* __restrict__ part, int* __restrict__ err) {
+               double* __restrict__ part, int* __restrict__ err, long long wait_limit) {
   if (mact_dev) single_comp = *mact_dev == 1;
   using C = SparseCfg<K>;
   constexpr int FT = C::FT, NZ = C::NZ, NS = C::NS, EW = kAccEpiWarps;
@@ -761,6 +766,7 @@ __global__ void __launch_bounds__(kAccThreads, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_holder;
+  int issued = 0;  // Z tile copies issued (loader thread)
 
   if (warp == 0) {
     if (lane == 0 && nt > 0) {
@@ -768,10 +774,9 @@ __global__ void __launch_bounds__(kAccThreads, 1)
       // the features' whole 16-byte pieces (the L2 prefetch wants an aligned base)
       const long long xbytes = (N * D * 4) & ~15LL;
       const bool xpf = (reinterpret_cast<uintptr_t>(X) & 15) == 0;
-      int issued = 0;
       for (int i = 0; i < nt; ++i) {
         const int s = i % NZ;
-        if (!mbar_wait_sleep(&z_empty[s], ((i / NZ) & 1) ^ 1, abort_flag, kWaitLimit)) break;
+        if (!mbar_wait_sleep(&z_empty[s], ((i / NZ) & 1) ^ 1, abort_flag, wait_limit)) break;
         mbar_arrive_expect_tx(&z_full[s], C::Z_STAGE + C::LL_STAGE);
         uint8_t* zs = smem + C::OFF_Z + s * C::Z_STAGE;
         const int t = t0 + i;
@@ -790,8 +795,6 @@ __global__ void __launch_bounds__(kAccThreads, 1)
           }
         }
       }
-      if (*abort_flag)  // drain the copies still in flight
-        for (int i = max(0, issued - NZ); i < issued; ++i) mbar_drain(&z_full[i % NZ], (i / NZ) & 1);
     }
   } else if (warp == 1) {
     // the logits MMAs: S^T[comps x frames] = W Z^T, six split-bf16 plane products
@@ -799,10 +802,10 @@ __global__ void __launch_bounds__(kAccThreads, 1)
       const uint32_t zb0 = smem_u32(smem + C::OFF_Z);
       const uint32_t idesc_l = idesc_bf16(128, FT, false, false);
       const uint32_t wa = tmem + C::W_COL;
-      bool ok = mbar_wait_sleep(w_full, 0, abort_flag, kWaitLimit);
+      bool ok = mbar_wait_sleep(w_full, 0, abort_flag, wait_limit);
       for (int i = 0; i < nt && ok; ++i) {
-        if (!mbar_wait_sleep(&z_full[i % NZ], (i / NZ) & 1, abort_flag, kWaitLimit)) break;
-        if (i >= NS && !mbar_wait_sleep(&s_free[i % NS], ((i - NS) / NS) & 1, abort_flag, kWaitLimit)) break;
+        if (!mbar_wait_sleep(&z_full[i % NZ], (i / NZ) & 1, abort_flag, wait_limit)) break;
+        if (i >= NS && !mbar_wait_sleep(&s_free[i % NS], ((i - NS) / NS) & 1, abort_flag, wait_limit)) break;
         tc_fence_after();
         const uint64_t zd = smem_desc(zb0 + (i % NZ) * C::Z_STAGE, FT * 16, 128);
         const uint32_t d = tmem + C::S_COL + (i % NS) * FT;
@@ -882,8 +885,8 @@ __global__ void __launch_bounds__(kAccThreads, 1)
     for (int i = 0; i < nt; ++i) {
       const int s = i % NZ, b = i % NS, mb = i & 1;
       per.begin(i, kNoPeriod);
-      const bool okw = mbar_wait_sleep(&z_full[s], (i / NZ) & 1, abort_flag, kWaitLimit) &&
-                       mbar_wait_sleep(&s_full[b], (i / NS) & 1, abort_flag, kWaitLimit);
+      const bool okw = mbar_wait_sleep(&z_full[s], (i / NZ) & 1, abort_flag, wait_limit) &&
+                       mbar_wait_sleep(&s_full[b], (i / NS) & 1, abort_flag, wait_limit);
       const uint32_t lla = ll_sa + (uint32_t)(s * FT * 4);
       const uint32_t sbuf = tmem + lane_off + C::S_COL + b * FT;
       const long long tile = (long long)(t0 + i);
@@ -1007,7 +1010,14 @@ __global__ void __launch_bounds__(kAccThreads, 1)
     }
   }
   __syncthreads();
-  if (threadIdx.x == 0 && *abort_flag) atomicExch(err, 1);
+  if (*abort_flag) {
+    // Every role has stopped. The loader's last NZ copies may still be in flight (a consumer
+    // that gave up never waited for them): let them land before the CTA's shared memory goes.
+    // Earlier copies were consumed, so they have landed.
+    if (warp == 0 && lane == 0)
+      for (int i = max(0, issued - NZ); i < issued; ++i) mbar_drain(&z_full[i % NZ], (i / NZ) & 1);
+    if (threadIdx.x == 0) atomicExch(err, 1);
+  }
   if (warp == 1) {
     tc_fence_after();
     tmem_dealloc(tmem, 512);
@@ -1089,7 +1099,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                int nTz, int nTw, const float* __restrict__ ll2, int n_tiles, int n_chunks, int slices,
                const int* __restrict__ tile_slot, const int4* __restrict__ work, float minGamma,
                int single_comp, const int* __restrict__ mact_dev,
-               double* __restrict__ part, int* __restrict__ err) {
+               double* __restrict__ part, int* __restrict__ err, long long wait_limit) {
   if (mact_dev) single_comp = *mact_dev == 1;
   using C = AccCfg<K, SO>;
   constexpr int FT = C::FT, NZ = C::NZ, NS = C::NS, ND = C::ND, N2 = C::N2, FLUSH = C::FLUSH;
@@ -1161,6 +1171,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_holder;
+  int issued = 0;  // Z tile copies issued (loader thread)
 
   if (warp == 0) {
     if (lane == 0 && nt > 0) {
@@ -1169,20 +1180,15 @@ __global__ void __launch_bounds__(kThreads, 1)
         mbar_arrive_expect_tx(w2_full, C::W2_BYTES);
         bulk_load(smem + C::OFF_W2, wplanes + (size_t)(2 * nTw + wchunk) * (K / 8) * 1024, C::W2_BYTES, w2_full);
       }
-      int issued = 0;
       for (int i = 0; i < nt; ++i) {
         const int s = i % NZ;
-        if (!mbar_wait(&z_empty[s], ((i / NZ) & 1) ^ 1, abort_flag, kWaitLimit)) break;
+        if (!mbar_wait(&z_empty[s], ((i / NZ) & 1) ^ 1, abort_flag, wait_limit)) break;
         mbar_arrive_expect_tx(&z_full[s], C::Z_STAGE + C::LL_STAGE);
         uint8_t* zs = smem + C::OFF_Z + s * C::Z_STAGE;
         const int t = t0 + i;
         for (int p = 0; p < 3; ++p) load_image(zs + p * C::Z_PLANE, &zmap, p, nTz, K, t, &z_full[s]);
         bulk_load(ll_s + s * FT, ll2 + (size_t)t * FT, FT * 4, &z_full[s]);
         issued = i + 1;
-      }
-      if (*abort_flag) {  // drain the copies still in flight
-        for (int i = max(0, issued - NZ); i < issued; ++i) mbar_drain(&z_full[i % NZ], (i / NZ) & 1);
-        if (C::WT == 2) mbar_drain(w2_full, 0);
       }
     }
   } else if (warp == 1 || warp == 10) {
@@ -1196,12 +1202,12 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (warp == 1) {
         const uint32_t idesc_l = idesc_bf16(128, FT, false, false);
         const uint32_t wa = tmem + C::W_COL;
-        ok = mbar_wait(w_full, 0, abort_flag, kWaitLimit);
-        if (ok && C::WT == 2) ok = mbar_wait(w2_full, 0, abort_flag, kWaitLimit);
+        ok = mbar_wait(w_full, 0, abort_flag, wait_limit);
+        if (ok && C::WT == 2) ok = mbar_wait(w2_full, 0, abort_flag, wait_limit);
         const uint64_t w2d = smem_desc(smem_u32(smem + C::OFF_W2), 128 * 16, 128);
         for (int i = 0; i < nt && ok; ++i) {
-          if (!mbar_wait(&z_full[i % NZ], (i / NZ) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
-          if (i >= NS && !mbar_wait(&s_free[i % NS], ((i - NS) / NS) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
+          if (!mbar_wait(&z_full[i % NZ], (i / NZ) & 1, abort_flag, wait_limit)) { ok = false; break; }
+          if (i >= NS && !mbar_wait(&s_free[i % NS], ((i - NS) / NS) & 1, abort_flag, wait_limit)) { ok = false; break; }
           tc_fence_after();
           const uint64_t zd = smem_desc(zb0 + (i % NZ) * C::Z_STAGE, FT * 16, 128);
           const uint32_t d = tmem + C::S_COL + (i % NS) * FT;
@@ -1228,8 +1234,8 @@ __global__ void __launch_bounds__(kThreads, 1)
           const uint32_t dsmall = C::SPLIT ? dcol + N2 : dcol;  // B (the small products)
           // the tile's operands are in its stage; an accumulator holds one tile: wait until the
           // epilogue has read out tile j - ND
-          if (!mbar_wait(&z_full[j % NZ], (j / NZ) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
-          if (j >= ND && !mbar_wait(&d_empty[j % ND], ((j - ND) / ND) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
+          if (!mbar_wait(&z_full[j % NZ], (j / NZ) & 1, abort_flag, wait_limit)) { ok = false; break; }
+          if (j >= ND && !mbar_wait(&d_empty[j % ND], ((j - ND) / ND) & 1, abort_flag, wait_limit)) { ok = false; break; }
           const uint32_t gb = tmem + C::S_COL + b * FT;
           // B = Z as [N = K columns] x [K' = frames], MN-major: LBO along frames, SBO along columns
           const uint64_t zd = smem_desc(zb0 + (j % NZ) * C::Z_STAGE, 128, FT * 16);
@@ -1238,7 +1244,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             // the posteriors of each half of the tile's frames are signalled separately, so the
             // statistics of the first half run while the epilogue converts the second
             if (q % (FT / 32) == 0) {
-              if (!mbar_wait(&g_full[2 * b + q / (FT / 32)], (j / NS) & 1, abort_flag, kWaitLimit)) {
+              if (!mbar_wait(&g_full[2 * b + q / (FT / 32)], (j / NS) & 1, abort_flag, wait_limit)) {
                 ok = false;
                 break;
               }
@@ -1304,7 +1310,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
     for (int k = 0; k < KH * 16; ++k) dacc[k] = 0.0f;
     auto readout = [&](int t, bool flush, int slot) -> bool {
-      if (!mbar_wait(&d_full[t % ND], (t / ND) & 1, abort_flag, kWaitLimit)) return false;
+      if (!mbar_wait(&d_full[t % ND], (t / ND) & 1, abort_flag, wait_limit)) return false;
       tc_fence_after();
       const uint32_t dbase = tmem + lane_off + C::D_COL + (t % ND) * (C::NSET * N2);
       if constexpr (C::SPLIT) {
@@ -1366,8 +1372,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       const bool end_prev = i > 0 && per.end(i - 1, FLUSH);
       const int slot_prev = i > 0 ? per.slot_of(i - 1) : 0;
       per.begin(i, FLUSH);
-      if (!mbar_wait(&z_full[i % NZ], (i / NZ) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
-      if (!mbar_wait(&s_full[b], (i / NS) & 1, abort_flag, kWaitLimit)) { ok = false; break; }
+      if (!mbar_wait(&z_full[i % NZ], (i / NZ) & 1, abort_flag, wait_limit)) { ok = false; break; }
+      if (!mbar_wait(&s_full[b], (i / NS) & 1, abort_flag, wait_limit)) { ok = false; break; }
       tc_fence_after();
       const float* lls = ll_s + (i % NZ) * FT;
       // pass cc converts 32-frame chunk 2 cc + hf: the two warps of a quadrant finish the first
@@ -1420,7 +1426,16 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (ok && !*abort_flag) readout(nt - 1, true, per.slot_of(nt - 1));
   }
   __syncthreads();
-  if (threadIdx.x == 0 && *abort_flag) atomicExch(err, 1);
+  if (*abort_flag) {
+    // Every role has stopped. The loader's last NZ copies (and the W plane 2 copy) may still be
+    // in flight (a consumer that gave up never waited for them): let them land before the CTA's
+    // shared memory goes. Earlier copies were consumed, so they have landed.
+    if (warp == 0 && lane == 0 && nt > 0) {
+      for (int i = max(0, issued - NZ); i < issued; ++i) mbar_drain(&z_full[i % NZ], (i / NZ) & 1);
+      if (C::WT == 2) mbar_drain(w2_full, 0);
+    }
+    if (threadIdx.x == 0) atomicExch(err, 1);
+  }
   if (warp == 1) {
     tc_fence_after();
     tmem_dealloc(tmem, 512);
@@ -1574,7 +1589,7 @@ int launch_ll_part(Ctx* c, int tile0, int n_tiles_ll, float* ll_out_dev, bool wa
     ll_kernel<K><<<grid_ll, kLlThreads, LC::SMEM, c->stream>>>(
         c->tm_wfull, c->tcx.planes, c->N, nullptr, nullptr, nTz, nTw, tile0, n_tiles_ll, n_chunks, trouble2,
         c->minLL, c->tcm.ll2, ll_out_dev, c->tc_llpart, c->tc_err,
-        build_planes ? c->X : nullptr, c->D);
+        build_planes ? c->X : nullptr, c->D, c->wait_limit);
   }
   if (!want_total) return GMM_OK;
   {
@@ -1634,12 +1649,12 @@ int launch_acc_part(Ctx* c, int flags) {
     if (sparse) {
       acc_sparse_kernel<K, true><<<n_chunks * sl, kAccThreads, SC::SMEM, c->stream>>>(
           zm, c->tcm.planes, c->tcm.cent, c->X, c->N, nullptr, c->D, nTz, nTw, c->tcm.ll2, n_tiles, n_chunks, sl,
-          nullptr, nullptr, c->minGamma, c->Mact == 1, mact_dev, c->tcpart, c->tc_err);
+          nullptr, nullptr, c->minGamma, c->Mact == 1, mact_dev, c->tcpart, c->tc_err, c->wait_limit);
     } else {
       auto kern = so ? acc_dense_kernel<K, true> : acc_dense_kernel<K, false>;
       kern<<<n_chunks * sl, kThreads, so ? DA::SMEM : DM::SMEM, c->stream>>>(
           zm, c->tcm.planes, nTz, nTw, c->tcm.ll2, n_tiles, n_chunks, sl, nullptr, nullptr, c->minGamma,
-          c->Mact == 1, mact_dev, c->tcpart, c->tc_err);
+          c->Mact == 1, mact_dev, c->tcpart, c->tc_err, c->wait_limit);
     }
   };
   int waves = 1;
@@ -1650,7 +1665,7 @@ int launch_acc_part(Ctx* c, int flags) {
     auto it = c->tuned_waves.find(key);
     if (it != c->tuned_waves.end()) {
       waves = it->second;
-    } else if (c->autotune && !c->profile) {
+    } else if (c->autotune && !c->profile && c->wait_limit == kDefaultWaitLimit) {
       // each candidate launch rewrites the partials it uses, so the timed runs are harmless
       cudaEvent_t e0, e1;
       cudaEventCreate(&e0);
@@ -1850,6 +1865,8 @@ int tc_estep_streamed(Ctx* c, const float* Xh, int flags, int nchunks) {
   rc = sync(c, "tensor-core E-step");
   if (rc) return rc;
   if (herr) {
+    // kernels that gave up may have left the feature planes half built
+    c->tcx_valid = false;
     cudaMemsetAsync(c->tc_err, 0, sizeof(int), c->stream);
     return fail(c, GMM_ERR_TIMEOUT, "tensor-core E-step: a bounded device wait expired");
   }
@@ -1895,6 +1912,8 @@ int tc_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
   rc = sync(c, "tensor-core E-step");
   if (rc) return rc;
   if (herr) {
+    // kernels that gave up may have left the feature planes half built
+    c->tcx_valid = false;
     cudaMemsetAsync(c->tc_err, 0, sizeof(int), c->stream);
     return fail(c, GMM_ERR_TIMEOUT, "tensor-core E-step: a bounded device wait expired");
   }
@@ -2159,7 +2178,7 @@ void run_batch_k(Ctx* c, const TcBatch& b, const CUtensorMap& zfull, int tile0, 
     ll_kernel<K><<<grid_ll, kLlThreads, LC::SMEM, c->stream>>>(
         *b.wmap, b.zplanes, b.N, b.row_frame, b.tile_wbase, nTz, b.w_chunks_total, tile0, ntl, b.n_chunks,
         (float)(c->minLL * kLog2e), c->minLL, b.ll2, b.ll, b.llpart, c->tc_err,
-        b.X, b.D);
+        b.X, b.D, c->wait_limit);
   }
   if ((stages & 2) && b.n_work > 0) {
     GMM_LAUNCH(c, "tc_acc_kernel");
@@ -2168,12 +2187,13 @@ void run_batch_k(Ctx* c, const TcBatch& b, const CUtensorMap& zfull, int tile0, 
     if (tc_stats_centred(K, b.second_order)) {
       acc_sparse_kernel<K, true><<<b.n_work, kAccThreads, SC::SMEM, c->stream>>>(
           zm, b.wplanes, b.cent, b.X, b.N, b.row_frame, b.D, nTz, b.w_chunks_total, b.ll2, (int)(b.Rpad / SC::FT),
-          b.n_chunks, 1, b.tile_slot, b.work, c->minGamma, b.single_comp, nullptr, b.part, c->tc_err);
+          b.n_chunks, 1, b.tile_slot, b.work, c->minGamma, b.single_comp, nullptr, b.part, c->tc_err,
+          c->wait_limit);
     } else {
       auto kern = b.second_order ? acc_dense_kernel<K, true> : acc_dense_kernel<K, false>;
       kern<<<b.n_work, kThreads, b.second_order ? DA::SMEM : DM::SMEM, c->stream>>>(
           zm, b.wplanes, nTz, b.w_chunks_total, b.ll2, (int)(b.Rpad / DA::FT), b.n_chunks, 1, b.tile_slot,
-          b.work, c->minGamma, b.single_comp, nullptr, b.part, c->tc_err);
+          b.work, c->minGamma, b.single_comp, nullptr, b.part, c->tc_err, c->wait_limit);
     }
   }
 }

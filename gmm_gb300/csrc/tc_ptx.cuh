@@ -43,14 +43,33 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
+// Non-blocking test of a phase (never suspends the thread).
+__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Wait limits below this many clock cycles poll with test_wait, so that the limit holds to
+// within a few hundred cycles (try_wait may suspend the thread for a system-dependent time,
+// long enough for a phase to complete inside one test). Only tests set such limits.
+constexpr long long kPollingWaitLimit = 1000000;
+
 // Bounded wait: gives up after ~`limit` clock cycles or when another role aborted.
 // Returns false on give-up (and raises the abort flag).
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
                                           long long limit) {
-  if (mbar_try_wait(bar, parity)) return true;
+  const bool poll = limit < kPollingWaitLimit;
+  if (poll ? mbar_test_wait(bar, parity) : mbar_try_wait(bar, parity)) return true;
   const long long t0 = clock64();
   while (true) {
-    if (mbar_try_wait(bar, parity)) return true;
+    if (poll ? mbar_test_wait(bar, parity) : mbar_try_wait(bar, parity)) return true;
     if (*abort_flag) return false;
     if (clock64() - t0 > limit) {
       *abort_flag = 1;
@@ -76,6 +95,7 @@ __device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t* bar, uint32_t pari
 // mbar_wait with suspension between the tests (for roles that have nothing else to do)
 __device__ __forceinline__ bool mbar_wait_sleep(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
                                                 long long limit) {
+  if (limit < kPollingWaitLimit) return mbar_wait(bar, parity, abort_flag, limit);
   if (mbar_try_wait(bar, parity)) return true;
   const long long t0 = clock64();
   while (true) {

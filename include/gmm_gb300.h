@@ -172,6 +172,14 @@ int gmm_read_aux(gmm_handle h, int full, double* aux, double* aux2, double* aux3
 int gmm_set_autotune(gmm_handle h, int on);
 int gmm_autotune_choice(gmm_handle h, int* n, long long* keys, int* waves, int cap);
 
+/* Test hook (no counterpart in the reference): the number of clock cycles (default 4e9, about
+ * 2 s) a tensor-core pipeline role waits on a barrier before it gives up; the kernel then lets
+ * its copies and MMAs in flight finish (always with the default limit), frees its tensor memory
+ * and the call returns GMM_ERR_TIMEOUT with the handle still usable. A limit of a few hundred
+ * cycles makes the waits of any tensor-core E-step expire, so tests can check that path without
+ * a fault. cycles <= 0 restores the default. Not meant for production use. */
+int gmm_set_wait_limit(gmm_handle h, long long cycles);
+
 /* M-step on the device statistics (FP64 math, float model), in place on the resident model:
  * CModelAdapt::UpdateModelEM (OL_ModelAdapt.cpp:823-949). *alive = components left with
  * non-zero weight. */
