@@ -23,7 +23,11 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libgmmref.so")
-REF_SRC = "/root/reference/GMM/lib_bmssr"
+# The reference GMM project (its lib_bmssr sources and example/): $GMM_REF_ROOT, else the
+# checkout named "reference" beside this repository. Absent on machines without it.
+REF_ROOT = os.environ.get("GMM_REF_ROOT") or os.path.join(os.path.dirname(os.path.dirname(HERE)),
+                                                           "reference", "GMM")
+REF_SRC = os.path.join(REF_ROOT, "lib_bmssr")
 
 ACC_MEAN, ACC_VAR, ACC_PROBS_ONLY = 1, 2, 4
 

@@ -2,7 +2,7 @@
 
 Run where the reference sources are present (they are read in place, never copied):
 
-    python tests/golden/make_golden.py [--ref-root /root/reference/GMM]
+    python tests/golden/make_golden.py [--ref-root <reference GMM project root>]
 
 It builds ``oracle/_ref/libgmmref.so`` (the reference CPU estimator and CModelAdapt compiled
 from their own sources, see oracle/Makefile) and records its outputs on small inputs:
@@ -54,7 +54,7 @@ from gmm_gb300 import formats, synth  # noqa: E402
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref-root", default="/root/reference/GMM")
+    ap.add_argument("--ref-root", default=O.REF_ROOT)
     a = ap.parse_args()
     O.REF_SRC = os.path.join(a.ref_root, "lib_bmssr")
     O.build(ref=True)
@@ -225,7 +225,7 @@ def train_fixture():
 if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "--full-only":
         O.build(ref=True)
-        full_fixture("/root/reference/GMM")
+        full_fixture(O.REF_ROOT)
     elif len(sys.argv) > 1 and sys.argv[1] == "--train-full-only":
         O.build(ref=True)
         train_full_fixture()
