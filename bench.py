@@ -37,6 +37,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -45,6 +46,16 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 UNIT = "frame·comp/s"
+
+# DRAM traffic of one statistics launch (tc_acc_kernel<80, second order) at M = 2048, D = 39:
+# dram__bytes_read.sum + dram__bytes_write.sum from an ncu capture at N = 1M frames, split into a
+# part that grows with the frames (operand planes + frame LSE) and the FP64 partial statistics
+# (independent of N).
+TRAFFIC_PER_FRAME = 484.0
+TRAFFIC_FIXED = 68.96e6
+TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of acc_dense_kernel<80,1> at N=1M, "
+                  "M=2048, D=39: 552.96 MB = 484 B per frame (three bf16 K=80 operand planes + the "
+                  "frame LSE, scaled by N) + 68.96 MB independent of N (FP64 partials, W planes)")
 
 
 def parse():
@@ -70,6 +81,8 @@ def parse():
     ap.add_argument("--tau", type=int, default=16)
     ap.add_argument("--seed", type=int, default=None)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="ubm-em: skip the plain FP32 leg")
+    ap.add_argument("--no-secondary", action="store_true", help="ubm-em: skip map-batch / mllr-batch")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     a = ap.parse_args()
     big = a.workload in ("ubm-em", "mllr-batch")  # M = 2048, D = 39 workloads
@@ -96,10 +109,9 @@ class ClockSampler:
     def __init__(self, gpu_index: int):
         self.idx = gpu_index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        self.path = os.path.join(tempfile.mkdtemp(prefix="gmm_bench_clocks_"), "clocks.csv")
 
     def __enter__(self):
-        os.makedirs(os.path.dirname(self.path), exist_ok=True)
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -223,7 +235,7 @@ class UbmEm:
         oracle.em_update(w, mu, var, st)
         dt = time.perf_counter() - t
         return n * self.M / dt, (f"{n} frames x {self.M} components (E-step + EM update) of the "
-                                  f"same workload, {dt:.1f} s")
+                                  f"same workload, {dt:.1f} s"), n, dt
 
 
 class MapBatch:
@@ -298,7 +310,7 @@ class MapBatch:
             s += 1
         dt = time.perf_counter() - t
         return frames * self.M / dt, (f"first {s} speakers ({frames} frames) x {self.M} components "
-                                      f"(mean-only MAP: E-step + update), {dt:.1f} s")
+                                      f"(mean-only MAP: E-step + update), {dt:.1f} s"), frames, dt
 
 
 class MllrBatch:
@@ -369,7 +381,7 @@ class MllrBatch:
             s += 1
         dt = time.perf_counter() - t
         return frames * self.M / dt, (f"first {s} speakers ({frames} frames) x {self.M} components "
-                                      f"(MLLR: E-step + G/k + solves), {dt:.1f} s")
+                                      f"(MLLR: E-step + G/k + solves), {dt:.1f} s"), frames, dt
 
 
 def tc_mma_flop_per_fc(kernel, D, second_order=True):
@@ -468,7 +480,7 @@ class FullEm:
         oracle.full_em_update(w, mu, cov, st)
         dt = time.perf_counter() - t
         return n * self.M / dt, (f"{n} frames x {self.M} components (full-covariance E-step + EM update) "
-                                 f"of the same workload, {dt:.1f} s, one thread")
+                                 f"of the same workload, {dt:.1f} s, one thread"), n, dt
 
 
 WORKLOADS = {"ubm-em": UbmEm, "map-batch": MapBatch, "mllr-batch": MllrBatch, "full-em": FullEm}
@@ -638,20 +650,27 @@ def run_reference(args):
         return run_serve_reference(args, threads)
     wl = (UbmEm(args, 0, gen_frames=400_000) if args.workload == "ubm-em" else
           FullEm(args, 0, gen_frames=200_000) if args.workload == "full-em" else WORKLOADS[args.workload](args, 0))
+    # Each step is a bounded sample of the workload (a full 10M-frame CPU iteration takes
+    # minutes): ms_per_step is the measured time of one sample, sample_frames its size, and the
+    # full-step time is the extrapolation fc / value, labelled as such.
     per_step = max(1.0, 60.0 / max(1, args.steps + args.warmup))
     rates = []
     for i in range(args.warmup + args.steps):
-        r, sample = wl.cpu_rate(per_step, threads)
+        r, sample, frames, dt = wl.cpu_rate(per_step, threads)
         if i >= args.warmup:
-            rates.append((r, sample))
-    value = statistics.median([r for r, _ in rates])
-    cfg = {k: v for k, v in wl.describe().items() if k != "l2"}
+            rates.append((r, sample, frames, dt))
+    value = statistics.median([x[0] for x in rates])
     out = {
         "impl": "reference", "metric": wl.metric, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * wl.fc / value, "higher_is_better": True,
+        "ms_per_step": 1e3 * statistics.median([x[3] for x in rates]),
+        "sample_frames": int(statistics.median([x[2] for x in rates])),
+        "extrapolated": True,
+        "full_step_ms_extrapolated": 1e3 * wl.fc / value,
+        "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": cfg,
+        "precision": "fp32 (CPU)",
+        "config": workload_config(wl, world),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1 if args.workload == "full-em" else threads,
                          "kind": "port",
                          "sample": rates[-1][1] + " per step; reference CPU algorithm (oracle port)" +
@@ -704,6 +723,98 @@ def run_serve_reference(args, threads):
 
 # ------------------------------------------------------------------ GPU arm
 
+def timed_region(dev, step, steps, warmup, torch, stream, gpu, world):
+    """W untimed steps, then K steps between CUDA events on the engine's stream, bracketed by a
+    synchronize (and a barrier across ranks); max over ranks. Returns (ms per step, launches of
+    this library's kernels, per-kernel profile, clock record)."""
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(warmup):
+        step()
+    dev.profile(True)
+    dev.profile_reset()
+    launches0 = dev.launch_count()
+    barrier()
+    with ClockSampler(gpu) as clk:
+        with torch.cuda.stream(stream):
+            t0 = torch.cuda.Event(enable_timing=True)
+            t1 = torch.cuda.Event(enable_timing=True)
+            t0.record(stream)
+            for _ in range(steps):
+                step()
+            t1.record(stream)
+        barrier()
+    ms = t0.elapsed_time(t1) / steps
+    launches = dev.launch_count() - launches0
+    prof = dev.profile_read()
+    dev.profile(False)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, launches, prof, clk.summary()
+
+
+def timed_e2e(wl, steps, torch, world):
+    """The same steps end to end through the public API: pinned host inputs to the device and the
+    results back to the host inside the timed region, every step (wall clock, max over ranks)."""
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    h2d, d2h = wl.e2e_prepare(torch)
+    for _ in range(2):
+        wl.e2e_step()
+    barrier()
+    te = time.perf_counter()
+    ke = max(2, steps // 2)
+    for _ in range(ke):
+        wl.e2e_step()
+    barrier()
+    e2e_ms = (time.perf_counter() - te) * 1e3 / ke
+    if world > 1:
+        t = torch.tensor([e2e_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    return {"value": world * wl.fc / (e2e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms, "steps": ke}
+
+
+def workload_config(wl, world):
+    """The config dict both arms print for a workload."""
+    cfg = wl.describe()
+    cfg["parallelism"] = f"replicas x{world}"
+    return cfg
+
+
+def secondary(name, args, rank, world, gpu, torch, _lib):
+    """A second workload measured in the same process (tensor-core path): device-timed value and
+    the end-to-end value, each over its own timed region."""
+    sa = argparse.Namespace(**vars(args))
+    sa.workload = name
+    big = name == "mllr-batch"
+    sa.mix, sa.dim = (2048, 39) if big else (1024, 60)
+    sa.speakers = 500 if big else 1000
+    sa.seed = {"map-batch": 3, "mllr-batch": 4}[name]
+    wl = WORKLOADS[name](sa, rank)
+    dev = _lib.Handle(gpu)
+    dev.set_precision(_lib.PREC_TC)
+    wl.setup(dev, _lib, torch, f"cuda:{gpu}")
+    stream = torch.cuda.ExternalStream(dev.stream())
+    steps = max(3, min(args.steps, 10))
+    ms, launches, prof, clocks = timed_region(dev, wl.step, steps, max(3, args.warmup), torch, stream, gpu, world)
+    e2e = None if args.no_e2e else timed_e2e(wl, steps, torch, world)
+    dev.close()
+    return {"metric": wl.metric, "value": world * wl.fc / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
+            "steps": steps, "warmup": max(3, args.warmup), "config": workload_config(wl, world),
+            "gpu_launches": launches, "clocks": clocks, "e2e": e2e,
+            "kernels": {k: {"ms": v[0], "launches": v[1]} for k, v in prof.items()}}
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -727,57 +838,35 @@ def main():
     wl.setup(dev, _lib, torch, f"cuda:{gpu}")
     stream = torch.cuda.ExternalStream(dev.stream())
 
-    def barrier():
-        torch.cuda.synchronize()
-        if world > 1:
-            torch.distributed.barrier()
-
-    for _ in range(args.warmup):
-        wl.step()
-    # kernel timing (CUDA events on the engine's stream) over the timed region
-    dev.profile(True)
-    dev.profile_reset()
-    launches0 = dev.launch_count()
-    barrier()
-    with ClockSampler(gpu) as clk:
-        with torch.cuda.stream(stream):
-            t0 = torch.cuda.Event(enable_timing=True)
-            t1 = torch.cuda.Event(enable_timing=True)
-            t0.record(stream)
-            for _ in range(args.steps):
-                wl.step()
-            t1.record(stream)
-        barrier()
-    ms = t0.elapsed_time(t1) / args.steps
-    launches = dev.launch_count() - launches0
-    prof = dev.profile_read()
-    dev.profile(False)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms, launches, prof, clocks = timed_region(dev, wl.step, args.steps, args.warmup, torch, stream, gpu, world)
     value = world * wl.fc / (ms / 1e3)
+
+    # the other half of the headline metric: the same EM iteration on the plain FP32 kernels
+    # (the reference's GPU E-step design), from the same initial model, in this process
+    plain = None
+    if args.workload == "ubm-em" and prec == _lib.PREC_TC and not args.no_plain:
+        dev.set_precision(_lib.PREC_FP32)
+        dev.upload_model(wl.w, wl.mu, wl.var)
+        psteps = max(3, min(args.steps, 10))
+        pms, plaunches, _, pclocks = timed_region(dev, wl.step, psteps, args.warmup, torch, stream, gpu, world)
+        plain = {"ms_per_step": pms, "value": world * wl.fc / (pms / 1e3), "unit": UNIT, "steps": psteps,
+                 "warmup": args.warmup, "gpu_launches": plaunches, "clocks": pclocks,
+                 "dtype": "f32 (the reference's operation order)"}
+        dev.set_precision(prec)
+        dev.upload_model(wl.w, wl.mu, wl.var)
 
     # end-to-end through the public API: pinned host features -> device, the step, the result
     # back to the host, every step
-    e2e = None
-    if not args.no_e2e:
-        h2d, d2h = wl.e2e_prepare(torch)
-        for _ in range(2):
-            wl.e2e_step()
-        barrier()
-        te = time.perf_counter()
-        ke = max(2, args.steps // 2)
-        for _ in range(ke):
-            wl.e2e_step()
-        barrier()
-        e2e_ms = (time.perf_counter() - te) * 1e3 / ke
-        if world > 1:
-            t = torch.tensor([e2e_ms], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            e2e_ms = float(t.item())
-        e2e = {"value": world * wl.fc / (e2e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
-               "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms}
+    e2e = None if args.no_e2e else timed_e2e(wl, args.steps, torch, world)
+    dev.close()
+
+    # batched MAP and MLLR (the speaker-adaptation workloads), measured in the same process
+    sec = {}
+    if args.workload == "ubm-em" and prec == _lib.PREC_TC and not args.no_secondary:
+        wl.Xpin = wl.dX = None
+        torch.cuda.empty_cache()
+        for name in ("map-batch", "mllr-batch"):
+            sec[name] = secondary(name, args, rank, world, gpu, torch, _lib)
 
     if rank != 0:
         if world > 1:
@@ -792,14 +881,13 @@ def main():
     flop_fc = wl.flop_per_fc(name)
     achieved = flop_fc * (wl.fc / launches_per_step) / (per_launch_ms / 1e3) / 1e12 if kcnt else 0.0
     peak = bf16s if bf16s else bf16
-    # DRAM bytes per launch of the dominant kernel from an ncu capture of a smaller case of the
-    # same workload, scaled by the frames a launch processes (the operand planes are read once)
-    traffic = None
+    # DRAM bytes per launch of the dominant kernel: not measurable inside this process (no
+    # counters without a profiler); taken from an ncu capture of the same kernel on a 1M-frame
+    # case of this workload and scaled by the frames a launch processes (traffic_source)
+    traffic, traffic_source = None, None
     if args.workload == "ubm-em" and name == "tc_acc_kernel" and args.dim == 39 and args.mix == 2048:
-        # reads 509.5 MB per 1M frames (operand planes + frame LSE, scaled by N) and the FP64
-        # partial write-back, 39.1 MB at 1M frames (it does not grow with N):
-        # profiles/acc_kernel_ubm_em_1Mx2048x39.md
-        traffic = 509.5 * wl.N + 39.1e6
+        traffic = TRAFFIC_PER_FRAME * wl.N + TRAFFIC_FIXED
+        traffic_source = TRAFFIC_SOURCE
     peak_source = f"{peak_kind} (bf16 sustained, MEASURED_PEAKS.json)"
     bound = wl.bound_for(name) if hasattr(wl, "bound_for") else getattr(wl, "bound", "tensor")
     if bound == "fp32":  # SIMT FP32 kernels: nominal FMA rate (no measured FP32 peak in the file)
@@ -811,6 +899,7 @@ def main():
     executed = mma_fc * (wl.fc / launches_per_step) / (per_launch_ms / 1e3) / 1e12 if mma_fc else None
     roofline = {"bound": bound, "kernel": name, "achieved": achieved, "peak": peak,
                 "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
+                "traffic_source": traffic_source,
                 "algorithmic_flop_per_fc": flop_fc,
                 "mma_flop_per_fc": mma_fc,
                 "executed_tflops": executed,
@@ -820,22 +909,26 @@ def main():
                 "kernel_share": kms / max(1e-9, sum(v[0] for v in prof.values()))}
 
     threads = os.cpu_count() or 1
-    r, sample = wl.cpu_rate(args.cpu_seconds, threads)
+    r, sample, _, _ = wl.cpu_rate(args.cpu_seconds, threads)
     cpu = {"value": r, "unit": UNIT, "cores": 1 if args.workload == "full-em" else threads, "kind": "port",
            "sample": sample + "; reference CPU algorithm (oracle port)"}
 
-    cfg = wl.describe()
-    cfg.update({"precision": args.precision, "parallelism": f"replicas x{world}"})
     out = {
         "metric": wl.metric, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None,
         "dtype": ("f32 FMA, f64 Cholesky, double-float sums" if args.workload == "full-em" else
                   "f32" if prec == _lib.PREC_FP32 else "bf16x3 split (tcgen05), f32 accumulate, f64 reduce"),
-        "data": "synthetic", "config": cfg, "clocks": clk.summary(), "e2e": e2e,
+        "precision": args.precision,
+        "data": "synthetic", "config": workload_config(wl, world), "clocks": clocks, "e2e": e2e,
         "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
         "kernels": {k: {"ms": v[0], "launches": v[1]} for k, v in prof.items()},
     }
+    if plain:
+        out["plain_fp32"] = plain
+        out["tc_over_plain"] = plain["ms_per_step"] / ms
+    if sec:
+        out["secondary"] = sec
     print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
