@@ -143,6 +143,7 @@ class GMMStatsEstimatorGB300:
     def insertModel(self, model: GMModel, first: bool = True):
         if first:
             self._models = []
+            self._dev.clear_model_slots()
         elif self._models and model.D != self._models[0].D:
             raise RuntimeError("Models (GMMs) have to have same dimensions")
         model.rearrange()
@@ -151,15 +152,20 @@ class GMMStatsEstimatorGB300:
             raise RuntimeError("insertModel(): model contains very low variances "
                                f"[{float(model.var[model.w > 0][bad].min())}]!")
         self._models.append(model)
-        self.setModelToBeUsed(len(self._models) - 1)
+        n = len(self._models) - 1
+        if not model.full:  # the group's diagonal models stay resident on the device
+            self._dev.upload_model_slot(n, model.w, model.mu, model.var)
+        self.setModelToBeUsed(n)
 
     def setModelToBeUsed(self, n: int):
+        """OL_GMMStatsEstimator.cpp:318-325: switch to model n of the group (a device-to-device
+        copy of its resident slot; a full-covariance model is uploaded again)."""
         self._model = self._models[n]
         self._dev.set_options(self._minLogLike, self._minGamma, self._min_var)
         if self._model.full:  # GMM_ERR_MODEL (RuntimeError) if a covariance is not positive definite
             self._dev.upload_model_full(self._model.w, self._model.mu, self._model.var)
         else:
-            self._dev.upload_model(self._model.w, self._model.mu, self._model.var)
+            self._dev.select_model(n)
 
     def setAccFlags(self, mixProbsOnly, meanStats, varStats, varFull=False, auxStats=False):
         if auxStats:

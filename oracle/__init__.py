@@ -46,6 +46,17 @@ def build(ref: bool | None = None) -> None:
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_ROOT={REF_SRC}"], check=True)
 
 
+def build_adapter(engine_dir: str) -> None:
+    """Compile the reference-side binding (ref/gb300_adapter.hpp) against the reference headers,
+    linked against the engine in `engine_dir` and against the CPU stand-in of its C ABI
+    (ref/fake_engine.c): _ref/libadapter_gb300.so and _ref/libadapter_fake.so."""
+    subprocess.run(["make", "-s", "-C", HERE, "adapter", f"REF_ROOT={REF_SRC}", f"ENGINE_DIR={engine_dir}"],
+                   check=True)
+
+
+ADAPTER_FAKE = os.path.join(HERE, "_ref", "libadapter_fake.so")
+ADAPTER_GB300 = os.path.join(HERE, "_ref", "libadapter_gb300.so")
+
 _lib = None
 _ref = None
 
