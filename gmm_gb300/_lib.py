@@ -70,6 +70,10 @@ SIGNATURES = {
     "gmm_accumulate_noalloc": (_i, [_vp, _ll, _i, _i, _vp, _vp, _vp, _f, _f, _f, _i, _vp, _vp]),
     "gmm_set_autotune": (_i, [_vp, _i]),
     "gmm_set_wait_limit": (_i, [_vp, _ll]),
+    "gmm_set_tile_schedule": (_i, [_vp, _i]),
+    "gmm_upload_model_slot": (_i, [_vp, _i, _i, _i, _vp, _vp, _vp]),
+    "gmm_select_model": (_i, [_vp, _i]),
+    "gmm_clear_model_slots": (_i, [_vp]),
     "gmm_autotune_choice": (_i, [_vp, C.POINTER(_i), _vp, _vp, _i]),
     "gmm_read_param": (_i, [C.c_char_p, _i, C.c_uint, _vp, _ll, C.POINTER(_ll), C.POINTER(_i)]),
     "gmm_accumulate_files": (_i, [_vp, _i, _i, C.POINTER(C.c_char_p), _i, C.c_uint, _d, C.POINTER(_i)]),
@@ -174,6 +178,10 @@ class Handle:
     def set_autotune(self, on: bool):
         self.check(self.lib.gmm_set_autotune(self.h, int(on)))
 
+    def set_tile_schedule(self, on: bool):
+        """Sparse tile schedule of the tensor-core statistics (default on)."""
+        self.check(self.lib.gmm_set_tile_schedule(self.h, int(on)))
+
     def set_wait_limit(self, cycles: int):
         """Test hook: clock cycles a tensor-core pipeline wait may take (<= 0: the default)."""
         self.check(self.lib.gmm_set_wait_limit(self.h, int(cycles)))
@@ -199,6 +207,27 @@ class Handle:
         M, D = mu.shape
         self.check(self.lib.gmm_upload_model(self.h, M, D, ptr(w), ptr(mu), ptr(var)))
         self.M, self.D = M, D
+
+    def upload_model_slot(self, slot, w, mu, var):
+        """Stores a model in a device-resident slot of the handle's group (the model in use is
+        unchanged)."""
+        w = np.ascontiguousarray(w, np.float32)
+        mu = np.ascontiguousarray(mu, np.float32)
+        var = np.ascontiguousarray(var, np.float32)
+        M, D = mu.shape
+        self.check(self.lib.gmm_upload_model_slot(self.h, int(slot), M, D, ptr(w), ptr(mu), ptr(var)))
+        if not hasattr(self, "_slot_shapes"):
+            self._slot_shapes = {}
+        self._slot_shapes[int(slot)] = (M, D)
+
+    def select_model(self, slot):
+        """Makes the model of `slot` the resident model (device-to-device)."""
+        self.check(self.lib.gmm_select_model(self.h, int(slot)))
+        self.M, self.D = self._slot_shapes[int(slot)]
+
+    def clear_model_slots(self):
+        self.check(self.lib.gmm_clear_model_slots(self.h))
+        self._slot_shapes = {}
 
     def set_prior(self, w=None, mu=None, var=None):
         if w is None:

@@ -113,6 +113,14 @@ static void drain_timers(Ctx* c) {
   }
 }
 
+static void free_slot(Ctx* c, ModelSlot& s) {
+  const size_t md = sizeof(float) * (size_t)s.M * s.D, m1 = sizeof(float) * (size_t)s.M;
+  dfree(c, s.w, m1);
+  dfree(c, s.mu, md);
+  dfree(c, s.var, md);
+  s = ModelSlot();
+}
+
 static void free_model(Ctx* c) {
   size_t md = sizeof(float) * (size_t)c->M * c->D, m1 = sizeof(float) * (size_t)c->M;
   dfree(c, c->w, m1); dfree(c, c->mu, md); dfree(c, c->var, md);
@@ -283,6 +291,8 @@ int gmm_destroy(gmm_handle h) {
   cudaStreamSynchronize(c->stream);
   drain_timers(c);
   full_destroy(c);
+  sched_free(c);
+  for (auto& s : c->slots) free_slot(c, s);
   dfree(c, c->aux, c->aux_cap);
   dfree(c, c->gs, c->gs_cap * sizeof(float));
   dfree(c, c->gprev, c->gprev_cap * sizeof(float));
@@ -348,6 +358,14 @@ int gmm_set_wait_limit(gmm_handle h, long long cycles) {
   return GMM_OK;
 }
 
+int gmm_set_tile_schedule(gmm_handle h, int on) {
+  if (!h) return GMM_ERR_ARG;
+  h->sched.on = on != 0;
+  if (h->em_graph) cudaGraphExecDestroy(h->em_graph);  // the captured iteration has the old schedule
+  h->em_graph = nullptr;
+  return GMM_OK;
+}
+
 int gmm_autotune_choice(gmm_handle h, int* n, long long* keys, int* waves, int cap) {
   if (!h || !n) return GMM_ERR_ARG;
   int k = 0;
@@ -390,6 +408,73 @@ int gmm_upload_model(gmm_handle h, int M, int D, const float* w, const float* mu
   c->stats_valid = false;
   c->model_dirty = true;
   return plain_precompute(c);
+}
+
+int gmm_upload_model_slot(gmm_handle h, int slot, int M, int D, const float* w, const float* mu,
+                          const float* var) {
+  if (!h) return GMM_ERR_ARG;
+  Ctx* c = h;
+  if (!w || !mu || !var) return fail(c, GMM_ERR_ARG, "gmm_upload_model_slot: null array");
+  if (slot < 0 || slot >= kMaxModelSlots)
+    return fail(c, GMM_ERR_ARG, "gmm_upload_model_slot: slot must be in [0, 4096)");
+  if (M < 1 || M > kMaxMix || D < 1 || D > kMaxDim)
+    return fail(c, GMM_ERR_ARG, "gmm_upload_model_slot: M must be in [1, 32767] and D in [1, 1024]");
+  for (size_t i = 0; i < c->slots.size(); ++i)
+    if ((int)i != slot && c->slots[i].w && c->slots[i].D != D)
+      return fail(c, GMM_ERR_ARG, "gmm_upload_model_slot: models of a group must have the same dimension");
+  cudaSetDevice(c->device);
+  if ((size_t)slot >= c->slots.size()) c->slots.resize(slot + 1);
+  ModelSlot& s = c->slots[slot];
+  if (s.w && (s.M != M || s.D != D)) free_slot(c, s);
+  if (!s.w) {
+    const size_t md = sizeof(float) * (size_t)M * D, m1 = sizeof(float) * (size_t)M;
+    int rc = dalloc(c, (void**)&s.w, m1, "model slot weights");
+    if (!rc) rc = dalloc(c, (void**)&s.mu, md, "model slot means");
+    if (!rc) rc = dalloc(c, (void**)&s.var, md, "model slot variances");
+    if (rc) {
+      s.M = M;
+      s.D = D;
+      free_slot(c, s);
+      return rc;
+    }
+    s.M = M;
+    s.D = D;
+  }
+  const size_t md = sizeof(float) * (size_t)M * D;
+  cudaMemcpyAsync(s.w, w, sizeof(float) * M, cudaMemcpyHostToDevice, c->stream);
+  cudaMemcpyAsync(s.mu, mu, md, cudaMemcpyHostToDevice, c->stream);
+  cudaMemcpyAsync(s.var, var, md, cudaMemcpyHostToDevice, c->stream);
+  return sync(c, "gmm_upload_model_slot");
+}
+
+int gmm_select_model(gmm_handle h, int slot) {
+  if (!h) return GMM_ERR_ARG;
+  Ctx* c = h;
+  if (slot < 0 || (size_t)slot >= c->slots.size() || !c->slots[slot].w)
+    return fail(c, GMM_ERR_ARG, "gmm_select_model: no model in slot " + std::to_string(slot));
+  const ModelSlot& s = c->slots[slot];
+  if (c->precision == GMM_PREC_TC && !tc_supported(s.D))
+    return fail(c, GMM_ERR_UNSUPPORTED, "tensor-core path supports 1 <= D <= 63");
+  cudaSetDevice(c->device);
+  int rc = ensure_model(c, s.M, s.D);
+  if (rc) return rc;
+  const size_t md = sizeof(float) * (size_t)s.M * s.D;
+  cudaMemcpyAsync(c->w, s.w, sizeof(float) * s.M, cudaMemcpyDeviceToDevice, c->stream);
+  cudaMemcpyAsync(c->mu, s.mu, md, cudaMemcpyDeviceToDevice, c->stream);
+  cudaMemcpyAsync(c->var, s.var, md, cudaMemcpyDeviceToDevice, c->stream);
+  c->stats_valid = false;
+  c->model_dirty = true;
+  return plain_precompute(c);
+}
+
+int gmm_clear_model_slots(gmm_handle h) {
+  if (!h) return GMM_ERR_ARG;
+  Ctx* c = h;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  for (auto& s : c->slots) free_slot(c, s);
+  c->slots.clear();
+  return GMM_OK;
 }
 
 int gmm_set_prior(gmm_handle h, const float* w, const float* mu, const float* var) {
@@ -997,7 +1082,8 @@ static int em_iterate_graph(Ctx* c, int iters, int upW, int upM, int upV, double
                            (long long)(size_t)c->tcx.planes, (long long)(size_t)c->tcpart,
                            (long long)(size_t)c->tc_llpart, (long long)(size_t)c->tc_err,
                            (long long)(size_t)c->ll_hist, (long long)c->ll_hist_cap,
-                           (long long)c->tcpart_cap, (long long)c->tc_llpart_cap};
+                           (long long)c->tcpart_cap, (long long)c->tc_llpart_cap,
+                           (long long)(size_t)c->sched.planes, (long long)(size_t)c->sched.lists};
   static_assert(sizeof(key) == sizeof(c->em_graph_key), "graph key size");
   if (!rc && iters > 1 && (c->em_graph == nullptr || std::memcmp(key, c->em_graph_key, sizeof(key)) != 0)) {
     if (c->em_graph) cudaGraphExecDestroy(c->em_graph);

@@ -16,6 +16,7 @@ namespace gmm {
 constexpr double kMinusLog2Pi = -1.837877066409345;  // OL_GMMStatsEstimator.h:280
 constexpr int kMaxMix = 32767;                        // GMModel::NumMixes is __int16
 constexpr int kMaxDim = 1024;
+constexpr int kMaxModelSlots = 4096;  // models in one handle's group
 // How long (clock cycles, ~2 s) a tensor-core pipeline role may wait on an mbarrier before it
 // gives up, raises the CTA's abort flag and the kernel reports GMM_ERR_TIMEOUT.
 constexpr long long kDefaultWaitLimit = 4000000000LL;
@@ -54,6 +55,46 @@ struct TcFeatures {
   uint16_t* planes = nullptr;  // 3 bf16 planes of Z = [x, x^2, 1, ...] per frame tile
 };
 
+// Sparse tile schedule of the tensor-core statistics kernel (tc_schedule.cu): device buffers.
+constexpr int kSchedGridMax = 1024;  // work items (CTAs of the statistics launch) at most
+constexpr int kSchedChunksMax = 32;  // component chunks the frame masks cover
+// A chunk is active for a frame when one of its logits lies within log2(minGamma) - margin of
+// the frame's log2-LSE; the margin (log2 units) covers the rounding difference between the
+// logits kernel's and the statistics kernel's logits of the same pair (~1e-5).
+constexpr double kSchedMargin2 = 0.25;
+struct TileSched {
+  bool on = false;                // handle option (gmm_set_tile_schedule)
+  long long Npad = 0;             // frame rows the frame buffers hold
+  int K = 0;
+  int chunks = 0;                 // component chunks the lists cover
+  long long lists_nT = 0;         // tiles per chunk list
+  uint32_t* fmask = nullptr;      // [Npad] chunks with a kept posterior, per frame row
+  uint32_t* kbuf = nullptr;       // [2][Npad] sort keys (ping-pong)
+  int* vbuf = nullptr;            // [2][Npad] sort values
+  int* perm = nullptr;            // sorted row -> original row (inside vbuf)
+  long long* srow = nullptr;      // [Npad] sorted row -> frame (-1: padding)
+  int* hist = nullptr;            // [256][sort blocks], then [256] digit offsets
+  uint16_t* planes = nullptr;     // 3 bf16 planes of the sorted frames (tile images)
+  uint16_t* cplanes = nullptr;    // 2 bf16 planes of the statistics operand, centred per tile
+  float* cen = nullptr;           // [Npad / 128][K / 2] the tile centres
+  float* ll2 = nullptr;           // [Npad] log2-LSE of the sorted frames
+  uint32_t* tmask = nullptr;      // [Npad / 128] union of the masks of a sorted tile
+  int* lists = nullptr;           // [chunks][tiles] active tiles of each chunk
+  int* counts = nullptr;          // [chunks] list lengths
+  int4* work = nullptr;           // [kSchedGridMax] {W chunk, 0, list offset, tiles}
+  int* item_off = nullptr;        // [chunks + 1] first work item of each chunk, then the count
+  int* gact = nullptr;            // [M] active list grouped into spatially coherent chunks
+  int gact_cap = 0;
+  CUtensorMap zmap;               // over `planes`
+  CUtensorMap cmap;               // over `cplanes`
+};
+
+// One device-resident model of a handle's model group (caller order, as uploaded).
+struct ModelSlot {
+  int M = 0, D = 0;
+  float *w = nullptr, *mu = nullptr, *var = nullptr;
+};
+
 struct Ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -74,6 +115,9 @@ struct Ctx {
   float *pw = nullptr, *pmu = nullptr, *pvar = nullptr;  // MAP prior
   bool have_prior = false;
   bool model_dirty = true;  // precompute needed
+  std::vector<ModelSlot> slots;  // model group: gmm_upload_model_slot / gmm_select_model
+  TileSched sched;               // sparse tile schedule of the tensor-core statistics
+  bool sched_active = false;     // the current model planes are grouped for the schedule
 
   // features
   long long N = 0;
@@ -120,7 +164,7 @@ struct Ctx {
   bool autotune = true;
   std::map<long long, int> tuned_waves;  // key: K, component chunks, frame tiles (bucket)
   cudaGraphExec_t em_graph = nullptr;
-  long long em_graph_key[29] = {};
+  long long em_graph_key[31] = {};
   double* ll_hist = nullptr;  // [ll_hist_cap + 1]: per-iteration total LL, then a counter
   int ll_hist_cap = 0;
 
@@ -197,7 +241,7 @@ int mstep_mllr_apply(Ctx* c, const double* W_host);
 // ------------------------------------------------------------------ tensor-core path
 int tc_supported(int D);
 int tc_prepare_features(Ctx* c);
-int tc_prepare_model(Ctx* c);
+int tc_prepare_model(Ctx* c, bool sched_ok);
 int tc_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev);
 int tc_estep_streamed(Ctx* c, const float* Xh, int flags, int nchunks);
 
@@ -322,6 +366,15 @@ int tc_flush_tiles(int K);  // statistics tiles per speaker piece (one FP64 slot
 // The statistics kernel's partials are centred (tc_uncentre) for second-order statistics with
 // K > 80 (the sparse kernel); otherwise they are plain sums.
 bool tc_stats_centred(int K, bool second_order);
+// sparse tile schedule (tc_schedule.cu)
+bool sched_supported(int chunks, int Mact);
+int sched_prepare(Ctx* c, long long Npad, int K, int chunks);
+void sched_free(Ctx* c);
+void sched_group(Ctx* c, const int* act, int Mact, const int* mact_dev, int chunks, int D, const float* mu);
+void sched_sort(Ctx* c, long long Npad, int chunks);
+void sched_lists(Ctx* c, long long Npad, int chunks, int grid);
+void sched_reduce(Ctx* c, int K, int Mrows, int chunks, const int* comp_of_row, const float* cent,
+                  const double* part, int flags);
 int tc_k(int D);
 int tc_run_batch(Ctx* c, const TcBatch& b);
 int tc_run_batch_part(Ctx* c, const TcBatch& b, int tile0, int ntl, int stages);

@@ -71,6 +71,19 @@ int gmm_get_stream(gmm_handle h, void** stream);
 /* Model upload and precompute: insertModel (OL_GMMStatsEstimator.cpp:234-313) +
  * GMMStatsEstimator_GPU::uploadModel (CU_GMMStatsEstimator_CUDA.cu:284-318). */
 int gmm_upload_model(gmm_handle h, int M, int D, const float* w, const float* mu, const float* var);
+
+/* Model group (GMMStatsEstimator::insertModel with first = false and setModelToBeUsed,
+ * OL_GMMStatsEstimator.cpp:234-325): models kept resident on the device in numbered slots, so a
+ * switch between them copies nothing from the host. gmm_upload_model_slot stores a model (host
+ * arrays as for gmm_upload_model) in `slot` (0 <= slot < 4096; every model of the group must
+ * have the same D, as the reference requires) without changing the model in use;
+ * gmm_select_model makes slot n the resident model (a device-to-device copy and the same
+ * precompute and variance check as gmm_upload_model; the statistics of the previous model are
+ * dropped); gmm_clear_model_slots frees the group (insertModel with first = true). */
+int gmm_upload_model_slot(gmm_handle h, int slot, int M, int D, const float* w, const float* mu,
+                          const float* var);
+int gmm_select_model(gmm_handle h, int slot);
+int gmm_clear_model_slots(gmm_handle h);
 /* Prior model for MAP (the UBM argument of CModelAdapt::UpdateModelMAP, OL_ModelAdapt.cpp:993). */
 int gmm_set_prior(gmm_handle h, const float* w, const float* mu, const float* var);
 /* Copy the device-resident model back (w[M], mu[M*D], var[M*D]). */
@@ -171,6 +184,16 @@ int gmm_read_aux(gmm_handle h, int full, double* aux, double* aux2, double* aux3
  * and waves up to cap). */
 int gmm_set_autotune(gmm_handle h, int on);
 int gmm_autotune_choice(gmm_handle h, int* n, long long* keys, int* waves, int cap);
+
+/* Sparse tile schedule of the tensor-core statistics (no counterpart in the reference). A frame
+ * keeps posteriors above minGamma for a handful of components, so the E-step of the resident
+ * features (D <= 39, at most 32 chunks of 128 active components) groups the
+ * components into chunks that lie together in feature space, has the logits kernel record per
+ * frame the chunks holding a posterior that can survive the pruning, sorts the frames by that
+ * record, and runs the statistics only on the (128-frame tile, chunk) pairs that have one. The
+ * skipped pairs' posteriors are all pruned, so the statistics are the same up to the order of
+ * the additions. Off by default (on = 0 runs every pair: the dense schedule). */
+int gmm_set_tile_schedule(gmm_handle h, int on);
 
 /* Test hook (no counterpart in the reference): the number of clock cycles (default 4e9, about
  * 2 s) a tensor-core pipeline role waits on a barrier before it gives up; the kernel then lets

@@ -147,6 +147,7 @@ def test_tc_autotune_choice_and_results(glib):
     from gmm_gb300 import synth
     X, w, mu, var = synth.config_em(23, 200_000, 20, 16, 300)
     h = tc_handle(glib)
+    h.set_tile_schedule(False)  # the autotuner decomposes the dense schedule
     h.upload_model(w, mu, var)
     h.upload_features(X)
     a = h.accumulate()
