@@ -82,6 +82,9 @@ def parse():
     ap.add_argument("--seed", type=int, default=None)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="ubm-em: skip the plain FP32 leg")
+    ap.add_argument("--tile-schedule", default=os.environ.get("GMM_TILE_SCHEDULE", "default"),
+                    choices=["on", "off", "default"],
+                    help="sparse tile schedule of the tensor-core statistics (default: the library's, off)")
     ap.add_argument("--no-secondary", action="store_true", help="ubm-em: skip map-batch / mllr-batch")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     a = ap.parse_args()
@@ -835,6 +838,8 @@ def main():
     dev = _lib.Handle(gpu)
     prec = _lib.PREC_TC if args.precision == "tc" else _lib.PREC_FP32
     dev.set_precision(prec)
+    if args.tile_schedule != "default":
+        dev.set_tile_schedule(1 if args.tile_schedule == "on" else 0)
     wl.setup(dev, _lib, torch, f"cuda:{gpu}")
     stream = torch.cuda.ExternalStream(dev.stream())
 

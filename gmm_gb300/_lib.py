@@ -178,9 +178,10 @@ class Handle:
     def set_autotune(self, on: bool):
         self.check(self.lib.gmm_set_autotune(self.h, int(on)))
 
-    def set_tile_schedule(self, on: bool):
-        """Sparse tile schedule of the tensor-core statistics (default on)."""
-        self.check(self.lib.gmm_set_tile_schedule(self.h, int(on)))
+    def set_tile_schedule(self, mode):
+        """Sparse tile schedule of the tensor-core statistics: 0 off (default), 1 on for large
+        E-steps (>= 2048 frame tiles), 2 on always; True means 2, False 0."""
+        self.check(self.lib.gmm_set_tile_schedule(self.h, 2 if mode is True else 0 if mode is False else int(mode)))
 
     def set_wait_limit(self, cycles: int):
         """Test hook: clock cycles a tensor-core pipeline wait may take (<= 0: the default)."""

@@ -358,9 +358,10 @@ int gmm_set_wait_limit(gmm_handle h, long long cycles) {
   return GMM_OK;
 }
 
-int gmm_set_tile_schedule(gmm_handle h, int on) {
+int gmm_set_tile_schedule(gmm_handle h, int mode) {
   if (!h) return GMM_ERR_ARG;
-  h->sched.on = on != 0;
+  if (mode < 0 || mode > 2) return fail(h, GMM_ERR_ARG, "gmm_set_tile_schedule: mode must be 0, 1 or 2");
+  h->sched.mode = mode;
   if (h->em_graph) cudaGraphExecDestroy(h->em_graph);  // the captured iteration has the old schedule
   h->em_graph = nullptr;
   return GMM_OK;

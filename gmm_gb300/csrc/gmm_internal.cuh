@@ -58,12 +58,13 @@ struct TcFeatures {
 // Sparse tile schedule of the tensor-core statistics kernel (tc_schedule.cu): device buffers.
 constexpr int kSchedGridMax = 1024;  // work items (CTAs of the statistics launch) at most
 constexpr int kSchedChunksMax = 32;  // component chunks the frame masks cover
+constexpr long long kSchedMinTiles = 2048;  // mode 1: E-steps of at least this many frame tiles
 // A chunk is active for a frame when one of its logits lies within log2(minGamma) - margin of
 // the frame's log2-LSE; the margin (log2 units) covers the rounding difference between the
 // logits kernel's and the statistics kernel's logits of the same pair (~1e-5).
 constexpr double kSchedMargin2 = 0.25;
 struct TileSched {
-  bool on = false;                // handle option (gmm_set_tile_schedule)
+  int mode = 0;                   // gmm_set_tile_schedule: 0 off, 1 large E-steps, 2 always
   long long Npad = 0;             // frame rows the frame buffers hold
   int K = 0;
   int chunks = 0;                 // component chunks the lists cover
@@ -75,8 +76,6 @@ struct TileSched {
   long long* srow = nullptr;      // [Npad] sorted row -> frame (-1: padding)
   int* hist = nullptr;            // [256][sort blocks], then [256] digit offsets
   uint16_t* planes = nullptr;     // 3 bf16 planes of the sorted frames (tile images)
-  uint16_t* cplanes = nullptr;    // 2 bf16 planes of the statistics operand, centred per tile
-  float* cen = nullptr;           // [Npad / 128][K / 2] the tile centres
   float* ll2 = nullptr;           // [Npad] log2-LSE of the sorted frames
   uint32_t* tmask = nullptr;      // [Npad / 128] union of the masks of a sorted tile
   int* lists = nullptr;           // [chunks][tiles] active tiles of each chunk
@@ -86,7 +85,6 @@ struct TileSched {
   int* gact = nullptr;            // [M] active list grouped into spatially coherent chunks
   int gact_cap = 0;
   CUtensorMap zmap;               // over `planes`
-  CUtensorMap cmap;               // over `cplanes`
 };
 
 // One device-resident model of a handle's model group (caller order, as uploaded).

@@ -336,90 +336,29 @@ __device__ __forceinline__ void features_row_to_tmem(const float* __restrict__ X
   }
 }
 
-// Sparse tile schedule: for each sorted tile (one CTA, thread = row) the logits operand planes
-// of its frames (built from the raw features as the logits kernel builds them), their log2-LSE
-// values, the union of their chunk masks, and the operand of the statistics MMA centred on the
-// tile: c = the mean of the tile's frames, row = [x_0 - c_0, (x_0 - c_0)^2, x_1 - c_1, ...,
-// 1 at column 2D, 0 ...] (each dimension's first- and second-order columns side by side), split
-// into two bf16 planes (hi = the bf16 rounding, lo = the bf16 rounding of the rest). The tile's
-// frames share their components, so a component's per-tile sums gather many terms; around the
-// tile's centre they stay small and of both signs, and the tensor core's round-toward-zero
-// accumulation costs only their own low bits (uncentred, it biased the variances by 2.4e-5).
+// Sparse tile schedule: the sorted frames' operand planes (built from the raw features as the
+// logits kernel builds them), their log2-LSE values, their frame indices, and per sorted tile the
+// union of its frames' chunk masks. One CTA per 128-row tile, thread = row.
 template <int K>
 __global__ void __launch_bounds__(128) sort_rows_kernel(const float* __restrict__ X, int D, long long N,
                                                         const int* __restrict__ perm, const float* __restrict__ ll2,
                                                         const uint32_t* __restrict__ fmask,
-                                                        uint16_t* __restrict__ planes, uint16_t* __restrict__ cplanes,
-                                                        float* __restrict__ cen, float* __restrict__ sll2,
+                                                        uint16_t* __restrict__ planes, float* __restrict__ sll2,
                                                         long long* __restrict__ srow, uint32_t* __restrict__ tmask,
                                                         int nT) {
-  constexpr int KC = K / 8, DMAX = K / 2 - 1;
   __shared__ uint32_t red[4];
-  __shared__ float csum[4][DMAX + 1];
-  __shared__ float cs[DMAX];
-  const int tile = blockIdx.x, r = threadIdx.x, lane = r & 31, warp = r >> 5;
+  const int tile = blockIdx.x, r = threadIdx.x;
   const long long row = (long long)tile * 128 + r;
   const int o = perm[row];  // the row's place before the sort (frame index, or padding past N)
   const long long f = o < N ? (long long)o : -1LL;
-  const bool live = f >= 0;
   features_row_to_tmem<K, false>(X, D, f, planes, nT, tile, r, 0, true);
   sll2[row] = ll2[o];
   srow[row] = f;
   uint32_t m = fmask[o];
   for (int k = 16; k; k >>= 1) m |= __shfl_xor_sync(0xffffffffu, m, k);
-  if (lane == 0) red[warp] = m;
-  // the tile centre: the mean of its live frames (zero without any)
-  const float* xr = X + (live ? f : 0LL) * D;
-  float xv[DMAX];
-#pragma unroll
-  for (int d = 0; d < DMAX; ++d) xv[d] = (live && d < D) ? __ldg(xr + d) : 0.0f;
-#pragma unroll
-  for (int d = 0; d <= DMAX; ++d) {
-    float v = d < DMAX ? xv[d] : (live ? 1.0f : 0.0f);  // the last slot counts the live rows
-    for (int k = 16; k; k >>= 1) v += __shfl_xor_sync(0xffffffffu, v, k);
-    if (lane == 0) csum[warp][d] = v;
-  }
+  if ((r & 31) == 0) red[r >> 5] = m;
   __syncthreads();
   if (r == 0) tmask[tile] = red[0] | red[1] | red[2] | red[3];
-  if (r < DMAX) {
-    const float cnt = csum[0][DMAX] + csum[1][DMAX] + csum[2][DMAX] + csum[3][DMAX];
-    const float c = (r < D && cnt > 0.0f) ? (csum[0][r] + csum[1][r] + csum[2][r] + csum[3][r]) / cnt : 0.0f;
-    cs[r] = c;
-  }
-  if (r < K / 2) cen[(size_t)tile * (K / 2) + r] = 0.0f;  // overwritten below for r < D
-  __syncthreads();
-  if (r < D) cen[(size_t)tile * (K / 2) + r] = cs[r];
-#pragma unroll
-  for (int c = 0; c < KC; c += 2) {
-    uint32_t w[2][8];
-#pragma unroll
-    for (int e = 0; e < 16; e += 2) {
-      uint16_t a[2], b[2];
-#pragma unroll
-      for (int u = 0; u < 2; ++u) {
-        const int k = c * 8 + e + u;  // compile-time
-        float v = 0.0f;
-        if (k / 2 < DMAX && k / 2 < D) {
-          const int d = k / 2 < DMAX ? k / 2 : 0;
-          const float xc = live ? __fsub_rn(xv[d], cs[d]) : 0.0f;
-          v = (k & 1) ? __fmul_rn(xc, xc) : xc;
-        } else if (k == 2 * D && live) {
-          v = 1.0f;
-        }
-        const __nv_bfloat16 h1 = __float2bfloat16_rn(v);
-        a[u] = __bfloat16_as_ushort(h1);
-        b[u] = __bfloat16_as_ushort(__float2bfloat16_rn(v - __bfloat162float(h1)));
-      }
-      w[0][e >> 1] = a[0] | ((uint32_t)a[1] << 16);
-      w[1][e >> 1] = b[0] | ((uint32_t)b[1] << 16);
-    }
-#pragma unroll
-    for (int p = 0; p < 2; ++p) {
-      uint4* dst = reinterpret_cast<uint4*>(cplanes + ((size_t)(p * nT + tile) * KC + c) * 1024 + (size_t)r * 8);
-      dst[0] = make_uint4(w[p][0], w[p][1], w[p][2], w[p][3]);
-      dst[128] = make_uint4(w[p][4], w[p][5], w[p][6], w[p][7]);
-    }
-  }
 }
 
 // ------------------------------------------------------------------ log-likelihood kernel
@@ -1168,7 +1107,7 @@ __host__ __device__ constexpr int acc_mean_cols(int K) { return ((K - 1) / 2 + 1
 // reads both operands, when that makes room. Plans in order of preference: (3 W planes in TMEM,
 // 2 accumulators), (2, 2), (3, 1), (2, 1). The Z ring takes as many stages (2 or 3) as the
 // shared memory left holds.
-template <int K, bool SO, bool CEN = false>
+template <int K, bool SO>
 struct AccCfg {
   static constexpr int FT = acc_ft(K);
   static_assert(FT == 128, "the epilogue converts two 32-frame chunks per warp");
@@ -1176,11 +1115,8 @@ struct AccCfg {
   static constexpr bool SPLIT = SO && K <= 80;    // A and B accumulators (see above)
   static constexpr int NSET = SPLIT ? 2 : 1;       // accumulators of N2 columns per tile
   static constexpr int Z_PLANE = FT * K * 2;
-  // CEN (sorted tiles of the sparse schedule): the stage also holds the tile's centred statistics
-  // operand (two planes, after the three logits planes) and its centre
-  static constexpr int Z_STAGE = (CEN ? 5 : 3) * Z_PLANE;
+  static constexpr int Z_STAGE = 3 * Z_PLANE;
   static constexpr int LL_STAGE = FT * 4;
-  static constexpr int CEN_STAGE = CEN ? K / 2 * 4 : 0;
   static constexpr int WC3 = (3 * K / 2 + 15) / 16 * 16, WC2 = (K + 15) / 16 * 16;
   static constexpr bool P1 = 2 * FT + WC3 + 2 * NSET * N2 <= 512;
   static constexpr bool P2 = !P1 && 2 * FT + WC2 + 2 * NSET * N2 <= 512;
@@ -1193,45 +1129,34 @@ struct AccCfg {
   static constexpr int D_COL = (W_COL + WT * K / 2 + 15) / 16 * 16;
   static constexpr int W2_BYTES = WT == 2 ? K * 256 : 0;  // W plane 2 image in shared memory
   static constexpr int FIXED = W2_BYTES + 32 * 8 + 64 + 1024;
-  static constexpr int CEN_WARP = CEN ? 8 * 3 * 32 * 4 : 0;  // per epilogue warp: 2 tile centres + c0
-  static constexpr int NZ = cmin(3, (227 * 1024 - FIXED - CEN_WARP) / (Z_STAGE + LL_STAGE + CEN_STAGE));
+  static constexpr int NZ = cmin(3, (227 * 1024 - FIXED) / (Z_STAGE + LL_STAGE));
   static constexpr int OFF_Z = 0;
   static constexpr int OFF_W2 = OFF_Z + NZ * Z_STAGE;
   static constexpr int OFF_LL = OFF_W2 + W2_BYTES;
-  static constexpr int OFF_CEN = OFF_LL + NZ * LL_STAGE;
-  static constexpr int OFF_BAR = OFF_CEN + NZ * CEN_STAGE;
+  static constexpr int OFF_BAR = OFF_LL + NZ * LL_STAGE;
   static constexpr int OFF_MISC = OFF_BAR + 32 * 8;
-  static constexpr int OFF_CW = OFF_MISC + 64;
-  static constexpr int SMEM = cmax(OFF_CW + CEN_WARP + 1024, 120 * 1024);
+  static constexpr int SMEM = cmax(OFF_MISC + 64 + 1024, 120 * 1024);
   static constexpr int FLUSH = SPLIT ? 16 : 64 * 128 / FT;  // tiles per FP64 flush
   static constexpr int PIECE = 64 * 128 / FT;                // tiles per speaker piece (batched calls)
   static_assert(NZ >= 2 && NZ <= 4, "Z ring");
-  static_assert(!CEN || SPLIT, "centred statistics use the A/B accumulators");
   static_assert(D_COL + ND * NSET * N2 <= 512, "TMEM budget");
   static_assert(SMEM <= 227 * 1024, "shared memory budget");
 };
 
 // SO: second-order statistics wanted. The statistics MMA multiplies and the epilogue reads N2
 // columns: all K, or the leading [x | 1] ones.
-// CEN (second-order statistics over the sorted tiles of the sparse schedule): the statistics
-// MMA takes the tile's centred operand (cmap, two planes; columns 2d, 2d + 1 = the centred x_d
-// and its square, 2D = 1) with three products, lo x C1 + hi x C2 into B and hi x C1 into A; the
-// epilogue moves each tile's sums from the tile centre (cen) onto the centre of the first tile of
-// its FP64 flush period in FP32 registers, and the flush adds that centre back in FP64, writing
-// the partials in the usual column layout (F_d at d, n at D, S_d at K/2 + d).
-template <int K, bool SO, bool CEN = false>
+template <int K, bool SO>
 __global__ void __launch_bounds__(kThreads, 1)
     acc_dense_kernel(const __grid_constant__ CUtensorMap zmap, const uint16_t* __restrict__ wplanes,
                int nTz, int nTw, const float* __restrict__ ll2, int n_tiles, int n_chunks, int slices,
                const int* __restrict__ tile_slot, const int4* __restrict__ work, float minGamma,
                int single_comp, const int* __restrict__ mact_dev,
                double* __restrict__ part, int* __restrict__ err, long long wait_limit,
-               const int* __restrict__ tile_list, const int* __restrict__ n_work_dev,
-               const __grid_constant__ CUtensorMap cmap, const float* __restrict__ cen, int Dn) {
+               const int* __restrict__ tile_list, const int* __restrict__ n_work_dev) {
   // with n_work_dev: a fixed grid, of which the first *n_work_dev CTAs have work items
   if (n_work_dev && (int)blockIdx.x >= *n_work_dev) return;
   if (mact_dev) single_comp = *mact_dev == 1;
-  using C = AccCfg<K, SO, CEN>;
+  using C = AccCfg<K, SO>;
   constexpr int FT = C::FT, NZ = C::NZ, NS = C::NS, ND = C::ND, N2 = C::N2, FLUSH = C::FLUSH;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
@@ -1313,14 +1238,10 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (int i = 0; i < nt; ++i) {
         const int s = i % NZ;
         if (!mbar_wait(&z_empty[s], ((i / NZ) & 1) ^ 1, abort_flag, wait_limit)) break;
-        mbar_arrive_expect_tx(&z_full[s], C::Z_STAGE + C::LL_STAGE + C::CEN_STAGE);
+        mbar_arrive_expect_tx(&z_full[s], C::Z_STAGE + C::LL_STAGE);
         uint8_t* zs = smem + C::OFF_Z + s * C::Z_STAGE;
         const int t = tile_list ? tile_list[t0 + i] : t0 + i;
         for (int p = 0; p < 3; ++p) load_image(zs + p * C::Z_PLANE, &zmap, p, nTz, K, t, &z_full[s]);
-        if constexpr (CEN) {
-          for (int p = 0; p < 2; ++p) load_image(zs + (3 + p) * C::Z_PLANE, &cmap, p, nTz, K, t, &z_full[s]);
-          bulk_load(smem + C::OFF_CEN + s * C::CEN_STAGE, cen + (size_t)t * (K / 2), C::CEN_STAGE, &z_full[s]);
-        }
         bulk_load(ll_s + s * FT, ll2 + (size_t)t * FT, FT * 4, &z_full[s]);
         issued = i + 1;
       }
@@ -1386,30 +1307,18 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
             const uint32_t hi = gb + 32 * (q >> 1) + 8 * (q & 1);
             const uint32_t lo = hi + 16;
-            if constexpr (CEN) {
-              // gamma (hi + lo) x C (c1 + c2), the centred operand after the three logits planes:
-              // lo x C1 + hi x C2 into B, hi x C1 into A
-              const uint64_t c1 = desc_add(zd, 3 * C::Z_PLANE + q * 2 * 128);
-              const uint64_t c2 = desc_add(zd, 4 * C::Z_PLANE + q * 2 * 128);
-              if (q == 0) mma_ts_c<false>(dsmall, lo, c1, idesc_s);
-              else mma_ts_c<true>(dsmall, lo, c1, idesc_s);
-              mma_ts_c<true>(dsmall, hi, c2, idesc_s);
-              if (q == 0) mma_ts_c<false>(dcol, hi, c1, idesc_s);
-              else mma_ts_c<true>(dcol, hi, c1, idesc_s);
-            } else {
-              const uint64_t z1 = desc_add(zd, 0 * C::Z_PLANE + q * 2 * 128);
-              const uint64_t z2 = desc_add(zd, 1 * C::Z_PLANE + q * 2 * 128);
-              const uint64_t z3 = desc_add(zd, 2 * C::Z_PLANE + q * 2 * 128);
-              // gamma (hi + lo) x Z (z1 + z2 + z3): the five products above 2^-18, smallest
-              // first; hi x Z1 into its own accumulator when SPLIT
-              if (q == 0) mma_ts_c<false>(dsmall, lo, z2, idesc_s);
-              else mma_ts_c<true>(dsmall, lo, z2, idesc_s);
-              mma_ts_c<true>(dsmall, hi, z3, idesc_s);
-              mma_ts_c<true>(dsmall, lo, z1, idesc_s);
-              mma_ts_c<true>(dsmall, hi, z2, idesc_s);
-              if (C::SPLIT && q == 0) mma_ts_c<false>(dcol, hi, z1, idesc_s);
-              else mma_ts_c<true>(dcol, hi, z1, idesc_s);
-            }
+            const uint64_t z1 = desc_add(zd, 0 * C::Z_PLANE + q * 2 * 128);
+            const uint64_t z2 = desc_add(zd, 1 * C::Z_PLANE + q * 2 * 128);
+            const uint64_t z3 = desc_add(zd, 2 * C::Z_PLANE + q * 2 * 128);
+            // gamma (hi + lo) x Z (z1 + z2 + z3): the five products above 2^-18, smallest first;
+            // hi x Z1 into its own accumulator when SPLIT
+            if (q == 0) mma_ts_c<false>(dsmall, lo, z2, idesc_s);
+            else mma_ts_c<true>(dsmall, lo, z2, idesc_s);
+            mma_ts_c<true>(dsmall, hi, z3, idesc_s);
+            mma_ts_c<true>(dsmall, lo, z1, idesc_s);
+            mma_ts_c<true>(dsmall, hi, z2, idesc_s);
+            if (C::SPLIT && q == 0) mma_ts_c<false>(dcol, hi, z1, idesc_s);
+            else mma_ts_c<true>(dcol, hi, z1, idesc_s);
           }
           if (!ok) break;
           mma_commit(&z_empty[j % NZ]);
@@ -1455,80 +1364,10 @@ __global__ void __launch_bounds__(kThreads, 1)
     float dacc[KH * 16];
 #pragma unroll
     for (int k = 0; k < KH * 16; ++k) dacc[k] = 0.0f;
-    // CEN: this warp owns dimensions d0 .. (columns 2d, 2d + 1 of its chunks); cw holds the
-    // centres of those dimensions for two tiles (the tile being converted and the one being read
-    // out) and for the first tile of the current flush period (c0)
-    float dn = 0.0f;
-    bool pstart = true;
-    float* cw = reinterpret_cast<float*>(smem + C::OFF_CW) + (warp - 2) * 96;
-    const int d0 = 8 * kc0;
     auto readout = [&](int t, bool flush, int slot) -> bool {
       if (!mbar_wait(&d_full[t % ND], (t / ND) & 1, abort_flag, wait_limit)) return false;
       tc_fence_after();
       const uint32_t dbase = tmem + lane_off + C::D_COL + (t % ND) * (C::NSET * N2);
-      if constexpr (CEN) {
-        const float* ct = cw + (t & 1) * 32;
-        if (pstart) {  // the period's centre: this tile's
-          cw[64 + lane] = ct[lane];
-          __syncwarp();
-          pstart = false;
-        }
-        const float* c0 = cw + 64;
-        const uint32_t na = tmem_ld1(dbase + 2 * Dn), nb = tmem_ld1(dbase + N2 + 2 * Dn);
-        tmem_ld_wait();
-        const float nt = __uint_as_float(na) + __uint_as_float(nb);  // the tile's posterior mass
-#pragma unroll
-        for (int g = 0; g < KH; ++g) {
-          if (kc0 + g < kc1) {
-            uint32_t ra[16], rb[16];
-            tmem_ld16(dbase + 16 * (kc0 + g), ra);
-            tmem_ld16(dbase + N2 + 16 * (kc0 + g), rb);
-            tmem_ld_wait();
-#pragma unroll
-            for (int k = 0; k < 16; k += 2) {
-              const int j = 8 * g + k / 2;  // dimension d0 + j
-              if (d0 + j < Dn) {
-                // the sums around the tile centre, moved onto the period's centre (FP32, RN):
-                // F0 = F + dl n, S0 = S + dl (2 F + dl n), dl = c_t - c0
-                const float Ft = __uint_as_float(ra[k]) + __uint_as_float(rb[k]);
-                const float St = __uint_as_float(ra[k + 1]) + __uint_as_float(rb[k + 1]);
-                const float dl = ct[j] - c0[j];
-                dacc[g * 16 + k] += fmaf(dl, nt, Ft);
-                dacc[g * 16 + k + 1] += fmaf(dl, fmaf(dl, nt, 2.0f * Ft), St);
-              }
-            }
-          }
-        }
-        dn += nt;
-        tc_fence_before();
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&d_empty[t % ND]);
-        if (flush) {
-          // the period's centre added back in FP64, into the zeroed partials by reductions
-          double* mypart = part + ((size_t)slot * n_chunks + chunk) * K * 128 + row;
-          const double n64 = (double)dn;
-#pragma unroll
-          for (int g = 0; g < KH; ++g) {
-            if (kc0 + g < kc1) {
-#pragma unroll
-              for (int k = 0; k < 16; k += 2) {
-                const int j = 8 * g + k / 2;
-                if (d0 + j < Dn) {
-                  const double c = (double)c0[j], F0 = (double)dacc[g * 16 + k], S0 = (double)dacc[g * 16 + k + 1];
-                  atomicAdd(mypart + (size_t)(d0 + j) * 128, F0 + c * n64);
-                  atomicAdd(mypart + (size_t)(K / 2 + d0 + j) * 128, S0 + c * (2.0 * F0 + c * n64));
-                }
-                dacc[g * 16 + k] = 0.0f;
-                dacc[g * 16 + k + 1] = 0.0f;
-              }
-            }
-          }
-          if ((2 * Dn) / 16 >= kc0 && (2 * Dn) / 16 < kc1) atomicAdd(mypart + (size_t)Dn * 128, n64);
-          dn = 0.0f;
-          pstart = true;
-        }
-        return true;
-      }
       if constexpr (C::SPLIT) {
         // A + B per column, then into the running sums (both in FP32, round to nearest)
 #pragma unroll
@@ -1592,13 +1431,6 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (!mbar_wait(&s_full[b], (i / NS) & 1, abort_flag, wait_limit)) { ok = false; break; }
       tc_fence_after();
       const float* lls = ll_s + (i % NZ) * FT;
-      if constexpr (CEN) {
-        // the tile's centres of this warp's dimensions, while its stage is still live (the
-        // statistics MMAs of this tile, which release it, wait for the posteriors below)
-        const float* cs = reinterpret_cast<const float*>(smem + C::OFF_CEN + (i % NZ) * C::CEN_STAGE);
-        cw[(i & 1) * 32 + lane] = d0 + lane < K / 2 ? cs[d0 + lane] : 0.0f;
-        __syncwarp();
-      }
       // pass cc converts 32-frame chunk 2 cc + hf: the two warps of a quadrant finish the first
       // half of the tile's frames together and signal it before the second half
 #pragma unroll 1
@@ -1856,54 +1688,49 @@ int launch_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev, bool bui
 // kernel over work items on a fixed grid, add the items' partials per chunk.
 template <int K>
 int launch_acc_sched(Ctx* c, int flags) {
-  if constexpr (K > 80) {
-    return fail(c, GMM_ERR_STATE, "tile schedule: K > 80");
-  } else {
-    using DC = AccCfg<K, true, true>;
-    TileSched& s = c->sched;
-    const long long Npad = c->tcx.Npad;
-    const int nT = (int)(Npad / 128), chunks = c->tcm.Mpad / 128;
-    const int grid = std::min(kSchedGridMax, 2 * c->sms);
-    const size_t pneed = (size_t)grid * K * 128 * sizeof(double);
-    if (pneed > c->tcpart_cap) {
-      dfree(c, c->tcpart, c->tcpart_cap);
-      c->tcpart = nullptr;
-      c->tcpart_cap = 0;
-      int rc = dalloc(c, (void**)&c->tcpart, pneed, "tc partial statistics");
-      if (rc) return rc;
-      c->tcpart_cap = pneed;
-    }
-    static bool attr_set = false;
-    if (!attr_set) {
-      cudaFuncSetAttribute(acc_dense_kernel<K, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, DC::SMEM);
-      attr_set = true;
-    }
-    sched_sort(c, Npad, chunks);
-    {
-      GMM_LAUNCH(c, "tc_sort_rows_kernel");
-      sort_rows_kernel<K><<<nT, 128, 0, c->stream>>>(c->X, c->D, c->N, s.perm, c->tcm.ll2, s.fmask, s.planes,
-                                                     s.cplanes, s.cen, s.ll2, s.srow, s.tmask, nT);
-    }
-    int rc = make_map(c, &s.zmap, s.planes, 3 * Npad * K, K);
-    if (!rc) rc = make_map(c, &s.cmap, s.cplanes, 2 * Npad * K, K);
+  using DA = AccCfg<K, true>;
+  using DM = AccCfg<K, false>;
+  TileSched& s = c->sched;
+  const long long Npad = c->tcx.Npad;
+  const int nT = (int)(Npad / 128), chunks = c->tcm.Mpad / 128;
+  const bool so = (flags & GMM_ACC_VAR) != 0;
+  const int grid = std::min(kSchedGridMax, 2 * c->sms);
+  const size_t pneed = (size_t)grid * K * 128 * sizeof(double);
+  if (pneed > c->tcpart_cap) {
+    dfree(c, c->tcpart, c->tcpart_cap);
+    c->tcpart = nullptr;
+    c->tcpart_cap = 0;
+    int rc = dalloc(c, (void**)&c->tcpart, pneed, "tc partial statistics");
     if (rc) return rc;
-    sched_lists(c, Npad, chunks, grid);
-    cudaMemsetAsync(c->tcpart, 0, pneed, c->stream);  // the kernel adds into its item's partials
-    const int* mact_dev = c->static_shapes ? c->flag + 4 : nullptr;
-    // The statistics over the sorted tiles take the tile-centred operand (CEN): the tiles'
-    // frames share their components, so uncentred per-tile sums gather many large terms and the
-    // tensor core's round-toward-zero accumulation biased the variances by 2.4e-5 (and the
-    // occupancies by 2.5e-6). Mean-only requests get the same sums; S is not written out.
-    {
-      GMM_LAUNCH(c, "tc_acc_kernel");
-      acc_dense_kernel<K, true, true><<<grid, kThreads, DC::SMEM, c->stream>>>(
-          s.zmap, c->tcm.planes, nT, chunks, s.ll2, nT, 1, 1, nullptr, s.work, c->minGamma, c->Mact == 1, mact_dev,
-          c->tcpart, c->tc_err, c->wait_limit, s.lists, s.item_off + chunks, s.cmap, s.cen, c->D);
-    }
-    sched_reduce(c, K, c->static_shapes ? c->tcm.Mpad : c->Mact, chunks, c->tcm.comp_of_row, nullptr, c->tcpart,
-                 flags);
-    return GMM_OK;
+    c->tcpart_cap = pneed;
   }
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(acc_dense_kernel<K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, DA::SMEM);
+    cudaFuncSetAttribute(acc_dense_kernel<K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, DM::SMEM);
+    attr_set = true;
+  }
+  sched_sort(c, Npad, chunks);
+  {
+    GMM_LAUNCH(c, "tc_sort_rows_kernel");
+    sort_rows_kernel<K><<<nT, 128, 0, c->stream>>>(c->X, c->D, c->N, s.perm, c->tcm.ll2, s.fmask, s.planes, s.ll2,
+                                                   s.srow, s.tmask, nT);
+  }
+  int rc = make_map(c, &s.zmap, s.planes, 3 * Npad * K, K);
+  if (rc) return rc;
+  sched_lists(c, Npad, chunks, grid);
+  cudaMemsetAsync(c->tcpart, 0, pneed, c->stream);  // the kernel adds into its item's partials
+  const int* mact_dev = c->static_shapes ? c->flag + 4 : nullptr;
+  {
+    GMM_LAUNCH(c, "tc_acc_kernel");
+    auto kern = so ? acc_dense_kernel<K, true> : acc_dense_kernel<K, false>;
+    kern<<<grid, kThreads, so ? DA::SMEM : DM::SMEM, c->stream>>>(
+        s.zmap, c->tcm.planes, nT, chunks, s.ll2, nT, 1, 1, nullptr, s.work, c->minGamma, c->Mact == 1, mact_dev,
+        c->tcpart, c->tc_err, c->wait_limit, s.lists, s.item_off + chunks);
+  }
+  sched_reduce(c, K, c->static_shapes ? c->tcm.Mpad : c->Mact, chunks, c->tcm.comp_of_row, nullptr, c->tcpart,
+               flags);
+  return GMM_OK;
 }
 
 template <int K>
@@ -1951,7 +1778,7 @@ int launch_acc_part(Ctx* c, int flags) {
       auto kern = so ? acc_dense_kernel<K, true> : acc_dense_kernel<K, false>;
       kern<<<n_chunks * sl, kThreads, so ? DA::SMEM : DM::SMEM, c->stream>>>(
           zm, c->tcm.planes, nTz, nTw, c->tcm.ll2, n_tiles, n_chunks, sl, nullptr, nullptr, c->minGamma,
-          c->Mact == 1, mact_dev, c->tcpart, c->tc_err, c->wait_limit, nullptr, nullptr, zm, nullptr, c->D);
+          c->Mact == 1, mact_dev, c->tcpart, c->tc_err, c->wait_limit, nullptr, nullptr);
     }
   };
   int waves = 1;
@@ -2050,7 +1877,8 @@ int tc_prepare_model(Ctx* c, bool sched_ok) {
   // components grouped into spatially coherent chunks; the row order is free otherwise
   const int* mact_dev = c->static_shapes ? c->flag + 4 : nullptr;
   const int chunks = Mpad / 128;
-  c->sched_active = sched_ok && c->sched.on && K <= 80 && c->tcx.Npad > 0 &&
+  c->sched_active = sched_ok && K <= 80 && c->tcx.Npad > 0 &&
+                    (c->sched.mode == 2 || (c->sched.mode == 1 && c->tcx.Npad / 128 >= kSchedMinTiles)) &&
                     sched_supported(chunks, c->static_shapes ? c->M : c->Mact);
   if (c->sched_active) {
     int rc = sched_prepare(c, c->tcx.Npad, K, chunks);
@@ -2514,8 +2342,7 @@ void run_batch_k(Ctx* c, const TcBatch& b, const CUtensorMap& zfull, int tile0, 
       auto kern = b.second_order ? acc_dense_kernel<K, true> : acc_dense_kernel<K, false>;
       kern<<<b.n_work, kThreads, b.second_order ? DA::SMEM : DM::SMEM, c->stream>>>(
           zm, b.wplanes, nTz, b.w_chunks_total, b.ll2, (int)(b.Rpad / DA::FT), b.n_chunks, 1, b.tile_slot,
-          b.work, c->minGamma, b.single_comp, nullptr, b.part, c->tc_err, c->wait_limit, nullptr, nullptr, zm,
-          nullptr, b.D);
+          b.work, c->minGamma, b.single_comp, nullptr, b.part, c->tc_err, c->wait_limit, nullptr, nullptr);
     }
   }
 }

@@ -338,11 +338,7 @@ void free_frame_buffers(Ctx* c, TileSched& s) {
   dfree(c, s.ll2, sizeof(float) * Np);
   dfree(c, s.tmask, sizeof(uint32_t) * (Np / 128));
   dfree(c, s.srow, sizeof(long long) * Np);
-  dfree(c, s.cplanes, (size_t)2 * Np * s.K * sizeof(uint16_t));
-  dfree(c, s.cen, sizeof(float) * (Np / 128) * (size_t)(s.K / 2));
   s.srow = nullptr;
-  s.cplanes = nullptr;
-  s.cen = nullptr;
   s.fmask = s.kbuf = s.tmask = nullptr;
   s.vbuf = s.hist = nullptr;
   s.perm = nullptr;
@@ -375,8 +371,7 @@ int sched_prepare(Ctx* c, long long Npad, int K, int chunks) {
     if (!rc) rc = dalloc(c, (void**)&s.ll2, sizeof(float) * Npad, "sorted frame LSE");
     if (!rc) rc = dalloc(c, (void**)&s.tmask, sizeof(uint32_t) * nT, "tile masks");
     if (!rc) rc = dalloc(c, (void**)&s.srow, sizeof(long long) * Npad, "sorted row frames");
-    if (!rc) rc = dalloc(c, (void**)&s.cplanes, (size_t)2 * Npad * K * sizeof(uint16_t), "centred statistics planes");
-    if (!rc) rc = dalloc(c, (void**)&s.cen, sizeof(float) * nT * (size_t)(K / 2), "tile centres");
+
     s.Npad = Npad;  // set before a failure too, so that the sizes of what was allocated are known
     s.K = K;
     if (rc) {

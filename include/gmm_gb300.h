@@ -187,13 +187,18 @@ int gmm_autotune_choice(gmm_handle h, int* n, long long* keys, int* waves, int c
 
 /* Sparse tile schedule of the tensor-core statistics (no counterpart in the reference). A frame
  * keeps posteriors above minGamma for a handful of components, so the E-step of the resident
- * features (D <= 39, at most 32 chunks of 128 active components) groups the
- * components into chunks that lie together in feature space, has the logits kernel record per
- * frame the chunks holding a posterior that can survive the pruning, sorts the frames by that
- * record, and runs the statistics only on the (128-frame tile, chunk) pairs that have one. The
- * skipped pairs' posteriors are all pruned, so the statistics are the same up to the order of
- * the additions. Off by default (on = 0 runs every pair: the dense schedule). */
-int gmm_set_tile_schedule(gmm_handle h, int on);
+ * features (D <= 39, at most 32 chunks of 128 active components) can group the components into
+ * chunks that lie together in feature space, have the logits kernel record per frame the chunks
+ * holding a posterior that can survive the pruning, sort the frames by that record, and run the
+ * statistics only on the (128-frame tile, chunk) pairs that have one: 1.85 of 16 chunks per
+ * tile in UBM EM at M = 2048, D = 39, where it takes an EM iteration over 10M frames from 31.8
+ * to 13.6 ms. The skipped pairs' posteriors are all pruned, so nothing is dropped; but a sorted
+ * tile gathers a component's posterior mass, and the tensor core's round-toward-zero
+ * accumulation of a tile's sums then loses more low bits: variances within 2.4e-5 relative of
+ * FP64 after one UBM EM iteration (1e-5 with the dense schedule; 1.1e-5 for the reference's own
+ * FP32 arithmetic). mode 0: off (the default, every pair); 1: on for E-steps of at least 2048
+ * frame tiles; 2: on for every E-step. */
+int gmm_set_tile_schedule(gmm_handle h, int mode);
 
 /* Test hook (no counterpart in the reference): the number of clock cycles (default 4e9, about
  * 2 s) a tensor-core pipeline role waits on a barrier before it gives up; the kernel then lets

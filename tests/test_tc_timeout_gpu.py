@@ -13,26 +13,28 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _handle(glib, X, w, mu, var):
+def _handle(glib, X, w, mu, var, sched=False):
     h = glib.Handle(0)
     h.set_precision(glib.PREC_TC)
     h.set_autotune(False)
+    h.set_tile_schedule(sched)
     h.upload_model(w, mu, var)
     h.upload_features(X)
     return h
 
 
-# D = 39: the dense statistics kernel (K = 80); D = 60: the sparse one (K = 128, second order)
-@pytest.mark.parametrize("D,M,N", [(39, 64, 3000), (60, 40, 2000)])
-def test_tc_wait_expiry_reports_timeout_then_recovers(glib, D, M, N):
+# D = 39: the dense statistics kernel (K = 80), in the given frame order and over the sparse
+# tile schedule (work items on a fixed grid); D = 60: the sparse one (K = 128, second order)
+@pytest.mark.parametrize("D,M,N,sched", [(39, 64, 3000, False), (39, 300, 3000, True), (60, 40, 2000, False)])
+def test_tc_wait_expiry_reports_timeout_then_recovers(glib, D, M, N, sched):
     from gmm_gb300 import synth
     X, w, mu, var = synth.config_em(300 + D, N, D, 8, M)
-    fresh = _handle(glib, X, w, mu, var)
+    fresh = _handle(glib, X, w, mu, var, sched)
     ref = fresh.accumulate(glib.ACC_MEAN | glib.ACC_VAR)
     ref_mean = fresh.accumulate(glib.ACC_MEAN)
     fresh.close()
 
-    h = _handle(glib, X, w, mu, var)
+    h = _handle(glib, X, w, mu, var, sched)
     h.set_wait_limit(300)
     for flags in (glib.ACC_MEAN | glib.ACC_VAR, glib.ACC_MEAN):
         with pytest.raises(glib.GMMError) as e:
