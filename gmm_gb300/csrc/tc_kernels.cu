@@ -40,11 +40,14 @@
 //              S/n - mu^2 magnifies), i.e. n, F and S in one product (N2 = K), or only the leading
 //              [x | 1] columns when no second-order statistics are wanted. Posteriors never
 //              leave TMEM. An accumulator holds one tile's sums: the tensor core's FP32
-//              accumulation over many tiles loses low bits steadily, so the epilogue reads it
-//              every tile (one tile late, off the MMA's critical path; two accumulators where
-//              TMEM allows, so the next tile's statistics MMAs queue meanwhile), sums tiles in
-//              FP32 registers with round-to-nearest and moves them into FP64 partials every 8192
-//              frames; a final kernel reduces the partials over CTAs in a fixed order.
+//              accumulation over many tiles loses low bits steadily, so eight readout warps
+//              (apart from the eight posterior warps) read it as soon as the tile's MMAs are
+//              done (two accumulators where TMEM allows, so the next tile's statistics MMAs queue
+//              meanwhile), sum tiles in FP32 registers with round-to-nearest and move them into
+//              FP64 partials every 8192 frames; a final kernel reduces the partials over CTAs in
+//              a fixed order. Both MMA streams are issued by whole warps (one elected lane):
+//              issued from a one-thread branch, the MMAs came slower than the tensor pipe runs
+//              them whenever the posterior warps on the same sub-partition were busy.
 // Every mbarrier wait is bounded (~2 s); on expiry the kernel raises an error flag, drains its
 // own copies and MMAs (bounded), frees TMEM and returns.
 #include <cuda.h>
@@ -478,6 +481,8 @@ __global__ void __launch_bounds__(kLlThreads, 1)
       }
     }
   } else if (warp == 1 || warp == 14) {
+    // one thread issues (here the warp-issued form of the statistics kernel measured slower:
+    // 6.0 ms against 3.6 ms at N = 4M, M = 2048, D = 39)
     const int role = warp == 14;  // parity of the chunks this thread issues
     if (lane == 0 && my_tiles > 0 && (two_issuers || role == 0)) {
       const uint32_t idesc = idesc_bf16(128, 128, false, false);
@@ -1076,7 +1081,10 @@ __global__ void __launch_bounds__(kAccThreads, 1)
   }
 }
 
-constexpr int kThreads = 352;  // dense kernel: warp 0 TMA, warp 1 logits MMA, warps 2-9 epilogue, warp 10 statistics MMA
+// dense kernel: warp 0 TMA, warp 1 logits MMA, warps 2-9 posteriors, warp 10 statistics MMA,
+// warps 11-18 statistics readout
+constexpr int kAccReadWarp0 = 11;
+constexpr int kThreads = 32 * (kAccReadWarp0 + 8);
 
 // Dense statistics kernel. The component chunk's W planes are stored into TMEM once (A operand of
 // the logits MMA); Z tiles stream through an NZ-stage shared-memory ring; posteriors go from the
@@ -1247,22 +1255,24 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
     }
   } else if (warp == 1 || warp == 10) {
-    // Two MMA-issuing threads on different SM sub-partitions: the logits (warp 1) and the
-    // statistics (warp 10). Each shares its sub-partition with two busy epilogue warps; split
-    // this way each needs half the issue slots. A posterior buffer is reused by the logits of
-    // tile i + NS only after the statistics of tile i released it (s_free).
-    if (lane == 0 && nt > 0) {
+    // Two MMA-issuing warps on different SM sub-partitions: the logits (warp 1) and the
+    // statistics (warp 10). Each shares its sub-partition with two posterior warps and two
+    // readout warps; a whole converged warp runs each issue loop and one elected lane issues
+    // (mma_ts_e), which keeps the issue rate up while those warps are busy. A posterior buffer
+    // is reused by the logits of tile i + NS only after the statistics of tile i released it
+    // (s_free).
+    if (nt > 0) {
       const uint32_t zb0 = smem_u32(smem + C::OFF_Z);
       bool ok = true;
       if (warp == 1) {
         const uint32_t idesc_l = idesc_bf16(128, FT, false, false);
         const uint32_t wa = tmem + C::W_COL;
-        ok = mbar_wait(w_full, 0, abort_flag, wait_limit);
-        if (ok && C::WT == 2) ok = mbar_wait(w2_full, 0, abort_flag, wait_limit);
+        ok = mbar_wait_warp(w_full, 0, abort_flag, wait_limit);
+        if (ok && C::WT == 2) ok = mbar_wait_warp(w2_full, 0, abort_flag, wait_limit);
         const uint64_t w2d = smem_desc(smem_u32(smem + C::OFF_W2), 128 * 16, 128);
         for (int i = 0; i < nt && ok; ++i) {
-          if (!mbar_wait(&z_full[i % NZ], (i / NZ) & 1, abort_flag, wait_limit)) { ok = false; break; }
-          if (i >= NS && !mbar_wait(&s_free[i % NS], ((i - NS) / NS) & 1, abort_flag, wait_limit)) { ok = false; break; }
+          if (!mbar_wait_warp(&z_full[i % NZ], (i / NZ) & 1, abort_flag, wait_limit)) break;
+          if (i >= NS && !mbar_wait_warp(&s_free[i % NS], ((i - NS) / NS) & 1, abort_flag, wait_limit)) break;
           tc_fence_after();
           const uint64_t zd = smem_desc(zb0 + (i % NZ) * C::Z_STAGE, FT * 16, 128);
           const uint32_t d = tmem + C::S_COL + (i % NS) * FT;
@@ -1272,15 +1282,15 @@ __global__ void __launch_bounds__(kThreads, 1)
             for (int q = 0; q < K / 16; ++q) {
               const uint64_t bd = desc_add(zd, prod_z(pr) * C::Z_PLANE + q * 2 * FT * 16);
               const uint32_t a = wa + prod_w(pr) * (K / 2) + q * 8;
-              if (prod_w(pr) >= C::WT) mma_ss_c<true>(d, desc_add(w2d, q * 2 * 128 * 16), bd, idesc_l);
-              else if (pr == 0 && q == 0) mma_ts_c<false>(d, a, bd, idesc_l);
-              else mma_ts_c<true>(d, a, bd, idesc_l);
+              if (prod_w(pr) >= C::WT) mma_ss_e<true>(d, desc_add(w2d, q * 2 * 128 * 16), bd, idesc_l);
+              else if (pr == 0 && q == 0) mma_ts_e<false>(d, a, bd, idesc_l);
+              else mma_ts_e<true>(d, a, bd, idesc_l);
             }
           }
-          mma_commit(&s_full[i % NS]);
+          mma_commit_e(&s_full[i % NS]);
         }
-        mma_commit(&mma_done[0]);
-        mbar_drain(&mma_done[0], 0);
+        mma_commit_e(&mma_done[0]);
+        if (lane == 0) mbar_drain(&mma_done[0], 0);
       } else {
         const uint32_t idesc_s = idesc_bf16(128, N2, false, true);
         for (int j = 0; j < nt && ok; ++j) {
@@ -1288,9 +1298,9 @@ __global__ void __launch_bounds__(kThreads, 1)
           const uint32_t dcol = tmem + C::D_COL + (j % ND) * (C::NSET * N2);
           const uint32_t dsmall = C::SPLIT ? dcol + N2 : dcol;  // B (the small products)
           // the tile's operands are in its stage; an accumulator holds one tile: wait until the
-          // epilogue has read out tile j - ND
-          if (!mbar_wait(&z_full[j % NZ], (j / NZ) & 1, abort_flag, wait_limit)) { ok = false; break; }
-          if (j >= ND && !mbar_wait(&d_empty[j % ND], ((j - ND) / ND) & 1, abort_flag, wait_limit)) { ok = false; break; }
+          // readout of tile j - ND
+          if (!mbar_wait_warp(&z_full[j % NZ], (j / NZ) & 1, abort_flag, wait_limit)) break;
+          if (j >= ND && !mbar_wait_warp(&d_empty[j % ND], ((j - ND) / ND) & 1, abort_flag, wait_limit)) break;
           const uint32_t gb = tmem + C::S_COL + b * FT;
           // B = Z as [N = K columns] x [K' = frames], MN-major: LBO along frames, SBO along columns
           const uint64_t zd = smem_desc(zb0 + (j % NZ) * C::Z_STAGE, 128, FT * 16);
@@ -1299,7 +1309,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             // the posteriors of each half of the tile's frames are signalled separately, so the
             // statistics of the first half run while the epilogue converts the second
             if (q % (FT / 32) == 0) {
-              if (!mbar_wait(&g_full[2 * b + q / (FT / 32)], (j / NS) & 1, abort_flag, wait_limit)) {
+              if (!mbar_wait_warp(&g_full[2 * b + q / (FT / 32)], (j / NS) & 1, abort_flag, wait_limit)) {
                 ok = false;
                 break;
               }
@@ -1312,21 +1322,21 @@ __global__ void __launch_bounds__(kThreads, 1)
             const uint64_t z3 = desc_add(zd, 2 * C::Z_PLANE + q * 2 * 128);
             // gamma (hi + lo) x Z (z1 + z2 + z3): the five products above 2^-18, smallest first;
             // hi x Z1 into its own accumulator when SPLIT
-            if (q == 0) mma_ts_c<false>(dsmall, lo, z2, idesc_s);
-            else mma_ts_c<true>(dsmall, lo, z2, idesc_s);
-            mma_ts_c<true>(dsmall, hi, z3, idesc_s);
-            mma_ts_c<true>(dsmall, lo, z1, idesc_s);
-            mma_ts_c<true>(dsmall, hi, z2, idesc_s);
-            if (C::SPLIT && q == 0) mma_ts_c<false>(dcol, hi, z1, idesc_s);
-            else mma_ts_c<true>(dcol, hi, z1, idesc_s);
+            if (q == 0) mma_ts_e<false>(dsmall, lo, z2, idesc_s);
+            else mma_ts_e<true>(dsmall, lo, z2, idesc_s);
+            mma_ts_e<true>(dsmall, hi, z3, idesc_s);
+            mma_ts_e<true>(dsmall, lo, z1, idesc_s);
+            mma_ts_e<true>(dsmall, hi, z2, idesc_s);
+            if (C::SPLIT && q == 0) mma_ts_e<false>(dcol, hi, z1, idesc_s);
+            else mma_ts_e<true>(dcol, hi, z1, idesc_s);
           }
           if (!ok) break;
-          mma_commit(&z_empty[j % NZ]);
-          mma_commit(&d_full[j % ND]);
-          mma_commit(&s_free[b]);
+          mma_commit_e(&z_empty[j % NZ]);
+          mma_commit_e(&d_full[j % ND]);
+          mma_commit_e(&s_free[b]);
         }
-        mma_commit(&mma_done[1]);
-        mbar_drain(&mma_done[1], 0);
+        mma_commit_e(&mma_done[1]);
+        if (lane == 0) mbar_drain(&mma_done[1], 0);
       }
     }
   } else if (warp < 10 && nt > 0) {
@@ -1353,14 +1363,75 @@ __global__ void __launch_bounds__(kThreads, 1)
       __syncwarp();
       if (lane == 0) mbar_arrive(w_full);
     }
-    constexpr int NCH = FT / 64;         // 32-frame chunks per warp (2)
+    constexpr int NCH = FT / 64;  // 32-frame chunks per warp (2)
+    for (int i = 0; i < nt; ++i) {
+      const int b = i % NS;
+      if (!mbar_wait(&z_full[i % NZ], (i / NZ) & 1, abort_flag, wait_limit)) break;
+      if (!mbar_wait(&s_full[b], (i / NS) & 1, abort_flag, wait_limit)) break;
+      tc_fence_after();
+      const float* lls = ll_s + (i % NZ) * FT;
+      // pass cc converts 32-frame chunk 2 cc + hf: the two warps of a quadrant finish the first
+      // half of the tile's frames together and signal it before the second half
+#pragma unroll 1
+      for (int cc = 0; cc < NCH; ++cc) {
+        const int c = 2 * cc + hf;
+        const uint32_t col = tmem + lane_off + C::S_COL + b * FT + 32 * c;
+        uint32_t v[32];
+        tmem_ld32(col, v);
+        tmem_ld_wait();
+        uint32_t hi[16], lo[16];
+        if (!single_comp) {
+#pragma unroll
+          for (int k = 0; k < 32; k += 4) {
+            const float4 l4 = *reinterpret_cast<const float4*>(lls + 32 * c + k);
+            float g0 = ex2(__uint_as_float(v[k + 0]) - l4.x);
+            float g1 = ex2(__uint_as_float(v[k + 1]) - l4.y);
+            float g2 = ex2(__uint_as_float(v[k + 2]) - l4.z);
+            float g3 = ex2(__uint_as_float(v[k + 3]) - l4.w);
+            g0 = g0 > minGamma ? g0 : 0.0f;  // NaN (padding) and 0 (trouble: +inf LSE) prune
+            g1 = g1 > minGamma ? g1 : 0.0f;
+            g2 = g2 > minGamma ? g2 : 0.0f;
+            g3 = g3 > minGamma ? g3 : 0.0f;
+            const uint32_t h01 = pack_bf16(g0, g1), h23 = pack_bf16(g2, g3);
+            hi[k >> 1] = h01;
+            hi[(k >> 1) + 1] = h23;
+            lo[k >> 1] = pack_bf16(g0 - __uint_as_float(h01 << 16), g1 - __uint_as_float(h01 & 0xffff0000u));
+            lo[(k >> 1) + 1] = pack_bf16(g2 - __uint_as_float(h23 << 16), g3 - __uint_as_float(h23 & 0xffff0000u));
+          }
+        } else {
+          // one component: every real frame has posterior 1 (padding 0)
+#pragma unroll
+          for (int k = 0; k < 32; k += 2) {
+            const float g0 = isnan(lls[32 * c + k]) ? 0.0f : 1.0f;
+            const float g1 = isnan(lls[32 * c + k + 1]) ? 0.0f : 1.0f;
+            hi[k >> 1] = pack_bf16(g0, g1);
+            lo[k >> 1] = 0u;
+          }
+        }
+        tmem_st16(col, hi);
+        tmem_st16(col + 16, lo);
+        tmem_st_wait();
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&g_full[2 * b + cc]);
+      }
+    }
+  } else if (warp >= kAccReadWarp0 && nt > 0) {
+    // statistics readout: thread = component row; the two warps of a lane quadrant split the
+    // columns
+    const int q4 = warp & 3;
+    const int hf = (warp - kAccReadWarp0) >> 2;
+    const int row = q4 * 32 + lane;
+    const uint32_t lane_off = (uint32_t)(q4 * 32) << 16;
     constexpr int KCH = N2 / 16;         // 16-column chunks of the statistics
     constexpr int KH = (KCH + 1) / 2;    // chunks per warp of a pair
     const int kc0 = hf ? KH : 0, kc1 = hf ? KCH : KH;
-    // The statistics MMA leaves one tile's sums in D2. The epilogue reads them one tile late
-    // (after the next tile's posteriors, so that it never waits on the MMA), adds them into
-    // FP32 registers with round-to-nearest, and moves the registers into the FP64 partials at
-    // the end of each accumulation period (FLUSH tiles of one slot).
+    // The statistics MMA leaves one tile's sums in the accumulator. These warps read them as
+    // soon as the MMA is done, add them into FP32 registers with round-to-nearest and move the
+    // registers into the FP64 partials at the end of each accumulation period (FLUSH tiles of one
+    // slot). Being separate from the warps that form the posteriors, the readout of tile j never
+    // waits behind the conversion of tile j + 1, and the statistics MMAs of tile j + 1 (one
+    // accumulator set: they wait for that readout) start as soon as their posteriors are there.
     float dacc[KH * 16];
 #pragma unroll
     for (int k = 0; k < KH * 16; ++k) dacc[k] = 0.0f;
@@ -1420,65 +1491,10 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       return true;
     };
-    bool ok = true;
-    for (int i = 0; i < nt; ++i) {
-      const int b = i % NS;
-      // period bookkeeping of the previous tile, before begin(i) moves the run start
-      const bool end_prev = i > 0 && per.end(i - 1, FLUSH);
-      const int slot_prev = i > 0 ? per.slot_of(i - 1) : 0;
-      per.begin(i, FLUSH);
-      if (!mbar_wait(&z_full[i % NZ], (i / NZ) & 1, abort_flag, wait_limit)) { ok = false; break; }
-      if (!mbar_wait(&s_full[b], (i / NS) & 1, abort_flag, wait_limit)) { ok = false; break; }
-      tc_fence_after();
-      const float* lls = ll_s + (i % NZ) * FT;
-      // pass cc converts 32-frame chunk 2 cc + hf: the two warps of a quadrant finish the first
-      // half of the tile's frames together and signal it before the second half
-#pragma unroll 1
-      for (int cc = 0; cc < NCH; ++cc) {
-        const int c = 2 * cc + hf;
-        const uint32_t col = tmem + lane_off + C::S_COL + b * FT + 32 * c;
-        uint32_t v[32];
-        tmem_ld32(col, v);
-        tmem_ld_wait();
-        uint32_t hi[16], lo[16];
-        if (!single_comp) {
-#pragma unroll
-          for (int k = 0; k < 32; k += 4) {
-            const float4 l4 = *reinterpret_cast<const float4*>(lls + 32 * c + k);
-            float g0 = ex2(__uint_as_float(v[k + 0]) - l4.x);
-            float g1 = ex2(__uint_as_float(v[k + 1]) - l4.y);
-            float g2 = ex2(__uint_as_float(v[k + 2]) - l4.z);
-            float g3 = ex2(__uint_as_float(v[k + 3]) - l4.w);
-            g0 = g0 > minGamma ? g0 : 0.0f;  // NaN (padding) and 0 (trouble: +inf LSE) prune
-            g1 = g1 > minGamma ? g1 : 0.0f;
-            g2 = g2 > minGamma ? g2 : 0.0f;
-            g3 = g3 > minGamma ? g3 : 0.0f;
-            const uint32_t h01 = pack_bf16(g0, g1), h23 = pack_bf16(g2, g3);
-            hi[k >> 1] = h01;
-            hi[(k >> 1) + 1] = h23;
-            lo[k >> 1] = pack_bf16(g0 - __uint_as_float(h01 << 16), g1 - __uint_as_float(h01 & 0xffff0000u));
-            lo[(k >> 1) + 1] = pack_bf16(g2 - __uint_as_float(h23 << 16), g3 - __uint_as_float(h23 & 0xffff0000u));
-          }
-        } else {
-          // one component: every real frame has posterior 1 (padding 0)
-#pragma unroll
-          for (int k = 0; k < 32; k += 2) {
-            const float g0 = isnan(lls[32 * c + k]) ? 0.0f : 1.0f;
-            const float g1 = isnan(lls[32 * c + k + 1]) ? 0.0f : 1.0f;
-            hi[k >> 1] = pack_bf16(g0, g1);
-            lo[k >> 1] = 0u;
-          }
-        }
-        tmem_st16(col, hi);
-        tmem_st16(col + 16, lo);
-        tmem_st_wait();
-        tc_fence_before();
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&g_full[2 * b + cc]);
-      }
-      if (i > 0 && !readout(i - 1, end_prev, slot_prev)) { ok = false; break; }
+    for (int t = 0; t < nt; ++t) {
+      per.begin(t, FLUSH);
+      if (!readout(t, per.end(t, FLUSH), per.slot_of(t))) break;
     }
-    if (ok && !*abort_flag) readout(nt - 1, true, per.slot_of(nt - 1));
   }
   __syncthreads();
   if (*abort_flag) {
