@@ -1293,6 +1293,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (lane == 0) mbar_drain(&mma_done[0], 0);
       } else {
         const uint32_t idesc_s = idesc_bf16(128, N2, false, true);
+        const uint32_t idesc_s2 = idesc_bf16(128, C::SPLIT ? 2 * N2 : N2, false, true);  // [A | B]
         for (int j = 0; j < nt && ok; ++j) {
           const int b = j % NS;
           const uint32_t dcol = tmem + C::D_COL + (j % ND) * (C::NSET * N2);
@@ -1320,15 +1321,31 @@ __global__ void __launch_bounds__(kThreads, 1)
             const uint64_t z1 = desc_add(zd, 0 * C::Z_PLANE + q * 2 * 128);
             const uint64_t z2 = desc_add(zd, 1 * C::Z_PLANE + q * 2 * 128);
             const uint64_t z3 = desc_add(zd, 2 * C::Z_PLANE + q * 2 * 128);
-            // gamma (hi + lo) x Z (z1 + z2 + z3): the five products above 2^-18, smallest first;
-            // hi x Z1 into its own accumulator when SPLIT
-            if (q == 0) mma_ts_e<false>(dsmall, lo, z2, idesc_s);
-            else mma_ts_e<true>(dsmall, lo, z2, idesc_s);
-            mma_ts_e<true>(dsmall, hi, z3, idesc_s);
-            mma_ts_e<true>(dsmall, lo, z1, idesc_s);
-            mma_ts_e<true>(dsmall, hi, z2, idesc_s);
-            if (C::SPLIT && q == 0) mma_ts_e<false>(dcol, hi, z1, idesc_s);
-            else mma_ts_e<true>(dcol, hi, z1, idesc_s);
+            // gamma (hi + lo) x Z (z1 + z2 + z3): the five products above 2^-18
+            if constexpr (C::SPLIT) {
+              // hi x Z1 into accumulator A, the four smaller products into B (right after A).
+              // Planes Z1 and Z2 are adjacent column groups of one MN-major operand and B
+              // follows A in TMEM, so one MMA of N = 2 N2 computes hi x [Z1 | Z2] into [A | B].
+              if (q == 0) {
+                mma_ts_e<false>(dcol, hi, z1, idesc_s2);
+                mma_ts_e<true>(dsmall, lo, z2, idesc_s);
+                mma_ts_e<true>(dsmall, hi, z3, idesc_s);
+                mma_ts_e<true>(dsmall, lo, z1, idesc_s);
+              } else {
+                mma_ts_e<true>(dsmall, lo, z2, idesc_s);
+                mma_ts_e<true>(dsmall, hi, z3, idesc_s);
+                mma_ts_e<true>(dsmall, lo, z1, idesc_s);
+                mma_ts_e<true>(dcol, hi, z1, idesc_s2);
+              }
+            } else {
+              // one accumulator, smallest products first
+              if (q == 0) mma_ts_e<false>(dcol, lo, z2, idesc_s);
+              else mma_ts_e<true>(dcol, lo, z2, idesc_s);
+              mma_ts_e<true>(dcol, hi, z3, idesc_s);
+              mma_ts_e<true>(dcol, lo, z1, idesc_s);
+              mma_ts_e<true>(dcol, hi, z2, idesc_s);
+              mma_ts_e<true>(dcol, hi, z1, idesc_s);
+            }
           }
           if (!ok) break;
           mma_commit_e(&z_empty[j % NZ]);
