@@ -818,6 +818,57 @@ def secondary(name, args, rank, world, gpu, torch, _lib):
             "kernels": {k: {"ms": v[0], "launches": v[1]} for k, v in prof.items()}}
 
 
+
+def _parse_cpulist(text):
+    cpus = set()
+    for part in text.strip().split(","):
+        if not part:
+            continue
+        if "-" in part:
+            a, b = part.split("-")
+            cpus.update(range(int(a), int(b) + 1))
+        else:
+            cpus.add(int(part))
+    return cpus
+
+
+def bind_local_cpus(torch, gpu):
+    """Run on the host cores attached to this GPU (its NUMA-local cores, from sysfs or
+    nvidia-smi topo), so that the pinned host buffers of the end-to-end leg are allocated in the
+    GPU's local memory. Returns (previous affinity, a description)."""
+    prev = os.sched_getaffinity(0)
+    local = set()
+    try:
+        p = torch.cuda.get_device_properties(gpu)
+        bdf = f"{p.pci_domain_id:04x}:{p.pci_bus_id:02x}:{p.pci_device_id:02x}.0"
+        with open(f"/sys/bus/pci/devices/{bdf}/local_cpulist") as f:
+            local = _parse_cpulist(f.read())
+        src = "sysfs " + bdf
+    except Exception:
+        src = "unknown"
+    cpus = local & prev
+    if cpus and cpus != prev:
+        os.sched_setaffinity(0, cpus)
+        return prev, f"{len(cpus)} of {len(prev)} cores, GPU-local ({src})"
+    return prev, f"{len(prev)} cores, unchanged ({src})"
+
+
+def h2d_rate(torch, gpu, nbytes=512 << 20):
+    """Host-to-device copy rate from pinned memory (GB/s), median of 3."""
+    h = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    d = torch.empty(nbytes, dtype=torch.uint8, device=f"cuda:{gpu}")
+    rates = []
+    for _ in range(4):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        d.copy_(h, non_blocking=True)
+        e1.record()
+        e1.synchronize()
+        rates.append(nbytes / (e0.elapsed_time(e1) * 1e-3) / 1e9)
+    del h, d
+    return round(statistics.median(rates[1:]), 1)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -834,6 +885,7 @@ def main():
     _lib.load()
 
     gpu = local if world > 1 else 0
+    prev_cpus, cpu_note = bind_local_cpus(torch, gpu)
     wl = WORKLOADS[args.workload](args, rank)
     dev = _lib.Handle(gpu)
     prec = _lib.PREC_TC if args.precision == "tc" else _lib.PREC_FP32
@@ -848,6 +900,7 @@ def main():
 
     # end-to-end through the public API: pinned host features -> device, the step, the result
     # back to the host, every step
+    h2d_before = h2d_rate(torch, gpu)
     e2e = None if args.no_e2e else timed_e2e(wl, args.steps, torch, world)
 
     # the opt-in sparse tile schedule of the statistics on the same workload (its accuracy cost is
@@ -931,6 +984,8 @@ def main():
                 "kernel_ms_per_launch": per_launch_ms,
                 "kernel_share": kms / max(1e-9, sum(v[0] for v in prof.values()))}
 
+    host_link = {"cpus": cpu_note, "h2d_gbs_pinned": [h2d_before, h2d_rate(torch, gpu)]}
+    os.sched_setaffinity(0, prev_cpus)  # the CPU baseline runs on every host core
     threads = os.cpu_count() or 1
     r, sample, _, _ = wl.cpu_rate(args.cpu_seconds, threads)
     cpu = {"value": r, "unit": UNIT, "cores": 1 if args.workload == "full-em" else threads, "kind": "port",
@@ -946,6 +1001,7 @@ def main():
         "data": "synthetic", "config": workload_config(wl, world), "clocks": clocks, "e2e": e2e,
         "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
         "kernels": {k: {"ms": v[0], "launches": v[1]} for k, v in prof.items()},
+        "host_link": host_link,
     }
     if plain:
         out["plain_fp32"] = plain

@@ -41,7 +41,7 @@
 //              [x | 1] columns when no second-order statistics are wanted. Posteriors never
 //              leave TMEM. An accumulator holds one tile's sums: the tensor core's FP32
 //              accumulation over many tiles loses low bits steadily, so eight readout warps
-//              (apart from the eight posterior warps) read it as soon as the tile's MMAs are
+//              (apart from the four posterior warps) read it as soon as the tile's MMAs are
 //              done (two accumulators where TMEM allows, so the next tile's statistics MMAs queue
 //              meanwhile), sum tiles in FP32 registers with round-to-nearest and move them into
 //              FP64 partials every 8192 frames; a final kernel reduces the partials over CTAs in
@@ -1081,9 +1081,33 @@ __global__ void __launch_bounds__(kAccThreads, 1)
   }
 }
 
-// dense kernel: warp 0 TMA, warp 1 logits MMA, warps 2-9 posteriors, warp 10 statistics MMA,
-// warps 11-18 statistics readout
-constexpr int kAccReadWarp0 = 11;
+// Statistics MMAs issued by a whole warp (one elected lane) or by one thread; the forms below
+// pick one at compile time.
+template <int K>
+constexpr bool kWarpIssue = K <= 80;
+
+template <bool WARPED>
+__device__ __forceinline__ bool mbar_wait_x(uint64_t* bar, uint32_t parity, volatile int* abort_flag, long long limit) {
+  if constexpr (WARPED) return mbar_wait_warp(bar, parity, abort_flag, limit);
+  else return mbar_wait(bar, parity, abort_flag, limit);
+}
+
+template <bool WARPED, bool ACC>
+__device__ __forceinline__ void mma_ts_x(uint32_t d, uint32_t a, uint64_t b, uint32_t idesc) {
+  if constexpr (WARPED) mma_ts_e<ACC>(d, a, b, idesc);
+  else mma_ts_c<ACC>(d, a, b, idesc);
+}
+
+template <bool WARPED>
+__device__ __forceinline__ void mma_commit_x(uint64_t* bar) {
+  if constexpr (WARPED) mma_commit_e(bar);
+  else mma_commit(bar);
+}
+
+// dense kernel: warp 0 TMA, warp 1 logits MMA, warps 2-5 posteriors (one per TMEM lane
+// quadrant), warp 6 statistics MMA, warps 7-14 statistics readout
+constexpr int kAccStatsWarp = 6;
+constexpr int kAccReadWarp0 = 7;
 constexpr int kThreads = 32 * (kAccReadWarp0 + 8);
 
 // Dense statistics kernel. The component chunk's W planes are stored into TMEM once (A operand of
@@ -1118,7 +1142,7 @@ __host__ __device__ constexpr int acc_mean_cols(int K) { return ((K - 1) / 2 + 1
 template <int K, bool SO>
 struct AccCfg {
   static constexpr int FT = acc_ft(K);
-  static_assert(FT == 128, "the epilogue converts two 32-frame chunks per warp");
+  static_assert(FT == 128, "a posterior warp converts four 32-frame chunks, signalled in two halves");
   static constexpr int N2 = SO ? K : acc_mean_cols(K);
   static constexpr bool SPLIT = SO && K <= 80;    // A and B accumulators (see above)
   static constexpr int NSET = SPLIT ? 2 : 1;       // accumulators of N2 columns per tile
@@ -1205,15 +1229,15 @@ __global__ void __launch_bounds__(kThreads, 1)
   Periods per(tile_slot, t0, nt, slice);
 
   if (threadIdx.x == 0) {
-    mbar_init(w_full, 8);
+    mbar_init(w_full, 4);
     for (int i = 0; i < NZ; ++i) {
       mbar_init(&z_full[i], 1);
       mbar_init(&z_empty[i], 1);
     }
     for (int i = 0; i < NS; ++i) {
       mbar_init(&s_full[i], 1);
-      mbar_init(&g_full[2 * i], 8);
-      mbar_init(&g_full[2 * i + 1], 8);
+      mbar_init(&g_full[2 * i], 4);
+      mbar_init(&g_full[2 * i + 1], 4);
       mbar_init(&s_free[i], 1);
     }
     for (int i = 0; i < ND; ++i) {
@@ -1254,25 +1278,28 @@ __global__ void __launch_bounds__(kThreads, 1)
         issued = i + 1;
       }
     }
-  } else if (warp == 1 || warp == 10) {
-    // Two MMA-issuing warps on different SM sub-partitions: the logits (warp 1) and the
-    // statistics (warp 10). Each shares its sub-partition with two posterior warps and two
-    // readout warps; a whole converged warp runs each issue loop and one elected lane issues
-    // (mma_ts_e), which keeps the issue rate up while those warps are busy. A posterior buffer
-    // is reused by the logits of tile i + NS only after the statistics of tile i released it
-    // (s_free).
-    if (nt > 0) {
+  } else if (warp == 1 || warp == kAccStatsWarp) {
+    // Two MMA-issuing roles on different SM sub-partitions: the logits (warp 1) and the
+    // statistics (warp 6). Each shares its sub-partition with a posterior warp and two readout
+    // warps. The logits come from one thread; the statistics for K <= 80 from a whole converged
+    // warp with one elected lane issuing (kWarpIssue), which keeps their issue rate up while the
+    // posterior warp is busy (measured: 8.15 against 8.50 ms at N = 4M, M = 2048, D = 39). The
+    // warp-issued forms measured slower for the logits stream (8.41 ms there) and for K = 128
+    // (batched MAP, D = 60: 10.7 against 6.8 ms). A posterior buffer is reused by the logits of
+    // tile i + NS only after the statistics of tile i released it (s_free).
+    constexpr bool WARPED = kWarpIssue<K>;
+    if (nt > 0 && (warp == kAccStatsWarp ? (WARPED || lane == 0) : lane == 0)) {
       const uint32_t zb0 = smem_u32(smem + C::OFF_Z);
       bool ok = true;
       if (warp == 1) {
         const uint32_t idesc_l = idesc_bf16(128, FT, false, false);
         const uint32_t wa = tmem + C::W_COL;
-        ok = mbar_wait_warp(w_full, 0, abort_flag, wait_limit);
-        if (ok && C::WT == 2) ok = mbar_wait_warp(w2_full, 0, abort_flag, wait_limit);
+        ok = mbar_wait(w_full, 0, abort_flag, wait_limit);
+        if (ok && C::WT == 2) ok = mbar_wait(w2_full, 0, abort_flag, wait_limit);
         const uint64_t w2d = smem_desc(smem_u32(smem + C::OFF_W2), 128 * 16, 128);
         for (int i = 0; i < nt && ok; ++i) {
-          if (!mbar_wait_warp(&z_full[i % NZ], (i / NZ) & 1, abort_flag, wait_limit)) break;
-          if (i >= NS && !mbar_wait_warp(&s_free[i % NS], ((i - NS) / NS) & 1, abort_flag, wait_limit)) break;
+          if (!mbar_wait(&z_full[i % NZ], (i / NZ) & 1, abort_flag, wait_limit)) break;
+          if (i >= NS && !mbar_wait(&s_free[i % NS], ((i - NS) / NS) & 1, abort_flag, wait_limit)) break;
           tc_fence_after();
           const uint64_t zd = smem_desc(zb0 + (i % NZ) * C::Z_STAGE, FT * 16, 128);
           const uint32_t d = tmem + C::S_COL + (i % NS) * FT;
@@ -1282,15 +1309,15 @@ __global__ void __launch_bounds__(kThreads, 1)
             for (int q = 0; q < K / 16; ++q) {
               const uint64_t bd = desc_add(zd, prod_z(pr) * C::Z_PLANE + q * 2 * FT * 16);
               const uint32_t a = wa + prod_w(pr) * (K / 2) + q * 8;
-              if (prod_w(pr) >= C::WT) mma_ss_e<true>(d, desc_add(w2d, q * 2 * 128 * 16), bd, idesc_l);
-              else if (pr == 0 && q == 0) mma_ts_e<false>(d, a, bd, idesc_l);
-              else mma_ts_e<true>(d, a, bd, idesc_l);
+              if (prod_w(pr) >= C::WT) mma_ss_c<true>(d, desc_add(w2d, q * 2 * 128 * 16), bd, idesc_l);
+              else if (pr == 0 && q == 0) mma_ts_c<false>(d, a, bd, idesc_l);
+              else mma_ts_c<true>(d, a, bd, idesc_l);
             }
           }
-          mma_commit_e(&s_full[i % NS]);
+          mma_commit(&s_full[i % NS]);
         }
-        mma_commit_e(&mma_done[0]);
-        if (lane == 0) mbar_drain(&mma_done[0], 0);
+        mma_commit(&mma_done[0]);
+        mbar_drain(&mma_done[0], 0);
       } else {
         const uint32_t idesc_s = idesc_bf16(128, N2, false, true);
         const uint32_t idesc_s2 = idesc_bf16(128, C::SPLIT ? 2 * N2 : N2, false, true);  // [A | B]
@@ -1300,8 +1327,8 @@ __global__ void __launch_bounds__(kThreads, 1)
           const uint32_t dsmall = C::SPLIT ? dcol + N2 : dcol;  // B (the small products)
           // the tile's operands are in its stage; an accumulator holds one tile: wait until the
           // readout of tile j - ND
-          if (!mbar_wait_warp(&z_full[j % NZ], (j / NZ) & 1, abort_flag, wait_limit)) break;
-          if (j >= ND && !mbar_wait_warp(&d_empty[j % ND], ((j - ND) / ND) & 1, abort_flag, wait_limit)) break;
+          if (!mbar_wait_x<WARPED>(&z_full[j % NZ], (j / NZ) & 1, abort_flag, wait_limit)) break;
+          if (j >= ND && !mbar_wait_x<WARPED>(&d_empty[j % ND], ((j - ND) / ND) & 1, abort_flag, wait_limit)) break;
           const uint32_t gb = tmem + C::S_COL + b * FT;
           // B = Z as [N = K columns] x [K' = frames], MN-major: LBO along frames, SBO along columns
           const uint64_t zd = smem_desc(zb0 + (j % NZ) * C::Z_STAGE, 128, FT * 16);
@@ -1310,7 +1337,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             // the posteriors of each half of the tile's frames are signalled separately, so the
             // statistics of the first half run while the epilogue converts the second
             if (q % (FT / 32) == 0) {
-              if (!mbar_wait_warp(&g_full[2 * b + q / (FT / 32)], (j / NS) & 1, abort_flag, wait_limit)) {
+              if (!mbar_wait_x<WARPED>(&g_full[2 * b + q / (FT / 32)], (j / NS) & 1, abort_flag, wait_limit)) {
                 ok = false;
                 break;
               }
@@ -1327,47 +1354,45 @@ __global__ void __launch_bounds__(kThreads, 1)
               // Planes Z1 and Z2 are adjacent column groups of one MN-major operand and B
               // follows A in TMEM, so one MMA of N = 2 N2 computes hi x [Z1 | Z2] into [A | B].
               if (q == 0) {
-                mma_ts_e<false>(dcol, hi, z1, idesc_s2);
-                mma_ts_e<true>(dsmall, lo, z2, idesc_s);
-                mma_ts_e<true>(dsmall, hi, z3, idesc_s);
-                mma_ts_e<true>(dsmall, lo, z1, idesc_s);
+                mma_ts_x<WARPED, false>(dcol, hi, z1, idesc_s2);
+                mma_ts_x<WARPED, true>(dsmall, lo, z2, idesc_s);
+                mma_ts_x<WARPED, true>(dsmall, hi, z3, idesc_s);
+                mma_ts_x<WARPED, true>(dsmall, lo, z1, idesc_s);
               } else {
-                mma_ts_e<true>(dsmall, lo, z2, idesc_s);
-                mma_ts_e<true>(dsmall, hi, z3, idesc_s);
-                mma_ts_e<true>(dsmall, lo, z1, idesc_s);
-                mma_ts_e<true>(dcol, hi, z1, idesc_s2);
+                mma_ts_x<WARPED, true>(dsmall, lo, z2, idesc_s);
+                mma_ts_x<WARPED, true>(dsmall, hi, z3, idesc_s);
+                mma_ts_x<WARPED, true>(dsmall, lo, z1, idesc_s);
+                mma_ts_x<WARPED, true>(dcol, hi, z1, idesc_s2);
               }
             } else {
               // one accumulator, smallest products first
-              if (q == 0) mma_ts_e<false>(dcol, lo, z2, idesc_s);
-              else mma_ts_e<true>(dcol, lo, z2, idesc_s);
-              mma_ts_e<true>(dcol, hi, z3, idesc_s);
-              mma_ts_e<true>(dcol, lo, z1, idesc_s);
-              mma_ts_e<true>(dcol, hi, z2, idesc_s);
-              mma_ts_e<true>(dcol, hi, z1, idesc_s);
+              if (q == 0) mma_ts_x<WARPED, false>(dcol, lo, z2, idesc_s);
+              else mma_ts_x<WARPED, true>(dcol, lo, z2, idesc_s);
+              mma_ts_x<WARPED, true>(dcol, hi, z3, idesc_s);
+              mma_ts_x<WARPED, true>(dcol, lo, z1, idesc_s);
+              mma_ts_x<WARPED, true>(dcol, hi, z2, idesc_s);
+              mma_ts_x<WARPED, true>(dcol, hi, z1, idesc_s);
             }
           }
           if (!ok) break;
-          mma_commit_e(&z_empty[j % NZ]);
-          mma_commit_e(&d_full[j % ND]);
-          mma_commit_e(&s_free[b]);
+          mma_commit_x<WARPED>(&z_empty[j % NZ]);
+          mma_commit_x<WARPED>(&d_full[j % ND]);
+          mma_commit_x<WARPED>(&s_free[b]);
         }
-        mma_commit_e(&mma_done[1]);
+        mma_commit_x<WARPED>(&mma_done[1]);
         if (lane == 0) mbar_drain(&mma_done[1], 0);
       }
     }
-  } else if (warp < 10 && nt > 0) {
-    // epilogue: thread = component row; the two warps of a lane quadrant split the work
+  } else if (warp >= 2 && warp < kAccStatsWarp && nt > 0) {
+    // posteriors: thread = component row, one warp per TMEM lane quadrant (measured 1.7% faster
+    // than two warps per quadrant: fewer busy warps beside the MMA-issuing ones)
     const int q4 = warp & 3;
-    const int hf = (warp - 2) >> 2;
     const int row = q4 * 32 + lane;
     const uint32_t lane_off = (uint32_t)(q4 * 32) << 16;
-    // the chunk's W planes into TMEM (A operand of the logits MMA): planes 0-1 by one warp of
-    // the pair, plane 2 by the other; with two planes in TMEM one each
+    // the chunk's W planes into TMEM (A operand of the logits MMA)
     {
       const int KC = K / 8;
-      const int p0 = C::WT == 2 ? hf : (hf ? 2 : 0), p1 = C::WT == 2 ? hf + 1 : (hf ? 3 : 2);
-      for (int p = p0; p < p1; ++p) {
+      for (int p = 0; p < C::WT; ++p) {
         const uint4* src = reinterpret_cast<const uint4*>(wplanes + ((size_t)(p * nTw + wchunk) * KC) * 1024 + (size_t)row * 8);
         for (int c = 0; c < KC; c += 2) {
           const uint4 u0 = __ldg(src + (size_t)c * 128), u1 = __ldg(src + (size_t)(c + 1) * 128);
@@ -1380,18 +1405,17 @@ __global__ void __launch_bounds__(kThreads, 1)
       __syncwarp();
       if (lane == 0) mbar_arrive(w_full);
     }
-    constexpr int NCH = FT / 64;  // 32-frame chunks per warp (2)
+    constexpr int NCH = FT / 32;  // 32-frame chunks per warp (4)
     for (int i = 0; i < nt; ++i) {
       const int b = i % NS;
       if (!mbar_wait(&z_full[i % NZ], (i / NZ) & 1, abort_flag, wait_limit)) break;
       if (!mbar_wait(&s_full[b], (i / NS) & 1, abort_flag, wait_limit)) break;
       tc_fence_after();
       const float* lls = ll_s + (i % NZ) * FT;
-      // pass cc converts 32-frame chunk 2 cc + hf: the two warps of a quadrant finish the first
-      // half of the tile's frames together and signal it before the second half
+      // pass c converts 32-frame chunk c; the first half of the tile's frames is signalled
+      // before the second is converted
 #pragma unroll 1
-      for (int cc = 0; cc < NCH; ++cc) {
-        const int c = 2 * cc + hf;
+      for (int c = 0; c < NCH; ++c) {
         const uint32_t col = tmem + lane_off + C::S_COL + b * FT + 32 * c;
         uint32_t v[32];
         tmem_ld32(col, v);
@@ -1430,7 +1454,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         tmem_st_wait();
         tc_fence_before();
         __syncwarp();
-        if (lane == 0) mbar_arrive(&g_full[2 * b + cc]);
+        if (lane == 0 && (c & 1)) mbar_arrive(&g_full[2 * b + (c >> 1)]);
       }
     }
   } else if (warp >= kAccReadWarp0 && nt > 0) {
