@@ -191,7 +191,7 @@ int gmm_autotune_choice(gmm_handle h, int* n, long long* keys, int* waves, int c
  * chunks that lie together in feature space, have the logits kernel record per frame the chunks
  * holding a posterior that can survive the pruning, sort the frames by that record, and run the
  * statistics only on the (128-frame tile, chunk) pairs that have one: 1.85 of 16 chunks per
- * tile in UBM EM at M = 2048, D = 39, where it takes an EM iteration over 10M frames from 31.8
+ * tile in UBM EM at M = 2048, D = 39, where it takes an EM iteration over 10M frames from 29.8
  * to 13.6 ms. The skipped pairs' posteriors are all pruned, so nothing is dropped; but a sorted
  * tile gathers a component's posterior mass, and the tensor core's round-toward-zero
  * accumulation of a tile's sums then loses more low bits: variances within 2.4e-5 relative of
