@@ -728,8 +728,11 @@ def run_serve_reference(args, threads):
 
 def timed_region(dev, step, steps, warmup, torch, stream, gpu, world):
     """W untimed steps, then K steps between CUDA events on the engine's stream, bracketed by a
-    synchronize (and a barrier across ranks); max over ranks. Returns (ms per step, launches of
-    this library's kernels, per-kernel profile, clock record)."""
+    synchronize (and a barrier across ranks); max over ranks. Then a short second pass with the
+    library's per-kernel timing events (outside the timed region: replayed CUDA graphs carry no
+    per-kernel events, so the library runs those calls eagerly while profiling). Returns (ms per
+    step, launches of this library's kernels in the timed steps, per-kernel profile, clock
+    record)."""
     def barrier():
         torch.cuda.synchronize()
         if world > 1:
@@ -737,8 +740,6 @@ def timed_region(dev, step, steps, warmup, torch, stream, gpu, world):
 
     for _ in range(warmup):
         step()
-    dev.profile(True)
-    dev.profile_reset()
     launches0 = dev.launch_count()
     barrier()
     with ClockSampler(gpu) as clk:
@@ -752,6 +753,11 @@ def timed_region(dev, step, steps, warmup, torch, stream, gpu, world):
         barrier()
     ms = t0.elapsed_time(t1) / steps
     launches = dev.launch_count() - launches0
+    dev.profile(True)
+    dev.profile_reset()
+    for _ in range(min(steps, 3)):
+        step()
+    barrier()
     prof = dev.profile_read()
     dev.profile(False)
     if world > 1:

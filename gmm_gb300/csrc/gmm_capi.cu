@@ -307,6 +307,7 @@ int gmm_destroy(gmm_handle h) {
   dfree(c, c->tcm.comp_of_row, 0);
   dfree(c, c->tcm.cent, 0);
   if (c->em_graph) cudaGraphExecDestroy(c->em_graph);
+  if (c->map_graph) cudaGraphExecDestroy(c->map_graph);
   dfree(c, c->ll_hist, 0);
   dfree(c, c->tcm.ll2, 0);
   dfree(c, c->tcx.planes, 0);
@@ -352,9 +353,11 @@ int gmm_set_autotune(gmm_handle h, int on) {
 int gmm_set_wait_limit(gmm_handle h, long long cycles) {
   if (!h) return GMM_ERR_ARG;
   h->wait_limit = cycles > 0 ? cycles : kDefaultWaitLimit;
-  // the captured EM iteration holds the old limit as a kernel argument
+  // the captured EM iteration and batched MAP hold the old limit as a kernel argument
   if (h->em_graph) cudaGraphExecDestroy(h->em_graph);
   h->em_graph = nullptr;
+  if (h->map_graph) cudaGraphExecDestroy(h->map_graph);
+  h->map_graph = nullptr;
   return GMM_OK;
 }
 

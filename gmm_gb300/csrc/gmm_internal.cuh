@@ -163,6 +163,11 @@ struct Ctx {
   std::map<long long, int> tuned_waves;  // key: K, component chunks, frame tiles (bucket)
   cudaGraphExec_t em_graph = nullptr;
   long long em_graph_key[31] = {};
+  // batched MAP over the resident frames replayed from a CUDA graph while the batch layout (and
+  // every buffer the kernels read or write) stays the same: the kernels of one call, captured
+  cudaGraphExec_t map_graph = nullptr;
+  long long map_graph_key[48] = {};
+  int map_graph_launches = 0;  // kernel launches inside the graph (the launch count adds them)
   double* ll_hist = nullptr;  // [ll_hist_cap + 1]: per-iteration total LL, then a counter
   int ll_hist_cap = 0;
 

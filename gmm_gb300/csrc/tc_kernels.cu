@@ -56,6 +56,7 @@
 #include <math.h>
 
 #include <algorithm>
+#include <cstring>
 #include <vector>
 
 #include "gmm_internal.cuh"
@@ -2130,8 +2131,20 @@ int tc_estep(Ctx* c, int flags, bool want_stats, float* ll_out_dev) {
 // layout; its frames are cut into pieces of one FP64 flush period (8192 frames), each piece with
 // its own FP64 slot, and the statistics kernel runs over work items (component chunk x range of
 // whole pieces) of about equal size. A speaker's sums are the piece slots added in piece order.
-int tc_speaker_stats(Ctx* c, int S, const long long* offs, const long long* d_offs, double* d_ll,
-                     bool second_order, const float* Xh, SpeakerStats* ss) {
+namespace {
+// A speaker batch between its host preparation and its launches.
+struct SpeakerBatch {
+  TcBatch t;
+  long long* d_pad = nullptr;     // padded speaker offsets (device)
+  std::vector<long long> pad;     // the same on the host
+};
+
+// Host side of a speaker batch: the padded row layout, pieces and work items, the scratch
+// buffers, every host-to-device copy of the batch, and the row map (row_frame_kernel, launched
+// between the copies: issued after all of them, it cost the host-frames path its overlap of
+// frame copies and logits kernels -- batched MAP end to end 16.4 -> 21-29 ms).
+int speaker_prepare(Ctx* c, int S, const long long* offs, const long long* d_offs, bool second_order,
+                    SpeakerStats* ss, SpeakerBatch* sb) {
   *ss = SpeakerStats();
   if (!tc_supported(c->D)) return fail(c, GMM_ERR_UNSUPPORTED, "tensor-core path supports 1 <= D <= 63");
   if (!d_offs) return fail(c, GMM_ERR_ARG, "per-speaker statistics: device speaker offsets missing");
@@ -2149,7 +2162,8 @@ int tc_speaker_stats(Ctx* c, int S, const long long* offs, const long long* d_of
   const int FT = acc_ft(K), FLUSH = 64 * 128 / FT;
   const int n_chunks = c->tcm.Mpad / 128;
   // padded row layout (the row map itself is built on the device) and pieces
-  std::vector<long long> pad((size_t)S + 1, 0);
+  std::vector<long long>& pad = sb->pad;
+  pad.assign((size_t)S + 1, 0);
   for (int s = 0; s < S; ++s) pad[s + 1] = pad[s] + (offs[s + 1] - offs[s] + 127) / 128 * 128;
   const long long Rpad = pad[S] > 0 ? pad[S] : 128;
   const long long ntiles = Rpad / FT;
@@ -2187,7 +2201,7 @@ int tc_speaker_stats(Ctx* c, int S, const long long* offs, const long long* d_of
   const size_t wk_bytes = sizeof(int4) * std::max<size_t>(1, work.size());
   const size_t pad_bytes = sizeof(long long) * ((size_t)S + 1);
   long long* d_rf = nullptr;
-  long long* d_pad = nullptr;
+  long long*& d_pad = sb->d_pad;
   int* d_ts = nullptr;
   int4* d_wk = nullptr;
   ss->S = S;
@@ -2243,7 +2257,8 @@ int tc_speaker_stats(Ctx* c, int S, const long long* offs, const long long* d_of
       cudaMemcpyAsync(ss->piece0, piece0.data(), sizeof(int) * S, cudaMemcpyHostToDevice, c->stream);
       cudaMemcpyAsync(ss->npieces, npieces.data(), sizeof(int) * S, cudaMemcpyHostToDevice, c->stream);
     }
-    TcBatch t;
+    TcBatch& t = sb->t;
+    t = TcBatch();
     t.D = D;
     t.K = K;
     t.n_chunks = n_chunks;
@@ -2267,66 +2282,97 @@ int tc_speaker_stats(Ctx* c, int S, const long long* offs, const long long* d_of
     t.part_bytes = ss->part_bytes;
     t.single_comp = c->Mact == 1;
     t.second_order = second_order;
-    if (!Xh) {
-      rc = tc_run_batch(c, t);
-    } else {
-      // Frames from host memory: copied in chunks of whole speakers on the copy stream (the first
-      // chunks growing geometrically from 1/64 of the frames, then 1/8), each chunk's rows going
-      // through the logits kernel as soon as its frames land; then the statistics in one launch
-      // (statistics launches per chunk measured slower: a partial wave per chunk).
-      const long long f_all = offs[S] - offs[0];
-      const long long steady = std::max(1LL, (f_all + 7) / 8);
-      std::vector<int> cuts{0};  // chunk boundaries (speaker indices)
-      for (long long target = std::max(1LL, steady / 8); cuts.back() < S; target = std::min(steady, 2 * target)) {
-        int sb = cuts.back() + 1;
-        while (sb < S && offs[sb] - offs[cuts.back()] < target) ++sb;
-        cuts.push_back(sb);
-      }
-      rc = ensure_copy_stream(c, (int)cuts.size());
-      int k = 0;
-      if (!rc) {
-        cudaEventRecord(c->copy_events[k], c->stream);  // frames a previous call may still read
-        cudaStreamWaitEvent(c->copy_stream, c->copy_events[k], 0);
-        ++k;
-      }
-      for (size_t ci = 0; !rc && ci + 1 < cuts.size(); ++ci) {
-        const int sa = cuts[ci], sb = cuts[ci + 1];
-        const long long fa = offs[sa], fb = offs[sb];
-        if (fb > fa) {
-          cudaError_t e = cudaMemcpyAsync(const_cast<float*>(c->X) + fa * c->D, Xh + fa * c->D,
-                                          sizeof(float) * (size_t)(fb - fa) * c->D, cudaMemcpyHostToDevice,
-                                          c->copy_stream);
-          if (e != cudaSuccess) rc = cuda_fail(c, e, "cudaMemcpyAsync(speaker frames)");
-        }
-        if (!rc) {
-          cudaEventRecord(c->copy_events[k], c->copy_stream);
-          cudaStreamWaitEvent(c->stream, c->copy_events[k], 0);
-          ++k;
-          const int ta = (int)(pad[sa] / 128), tb = (int)(pad[sb] / 128);
-          if (tb > ta) rc = tc_run_batch_part(c, t, ta, tb - ta, 1);
-        }
-      }
-      if (!rc) rc = tc_run_batch_part(c, t, 0, (int)(Rpad / 128), 2);
+  }
+  return rc;
+}
+
+// The launches of a prepared speaker batch: the logits and statistics kernels (over the
+// resident frames, or over Xh copied in chunks of speakers on the copy stream), the component
+// rows and the per-speaker log-likelihoods. Over resident frames these are stream operations
+// only (a CUDA graph can capture them).
+int speaker_launch(Ctx* c, int S, const long long* offs, const long long* d_offs, double* d_ll, const float* Xh,
+                   SpeakerBatch* sb, SpeakerStats* ss) {
+  const TcBatch& t = sb->t;
+  const std::vector<long long>& pad = sb->pad;
+  const long long Rpad = t.Rpad;
+  int rc = GMM_OK;
+  if (!Xh) {
+    rc = tc_run_batch(c, t);
+  } else {
+    // Frames from host memory: copied in chunks of whole speakers on the copy stream (the first
+    // chunks growing geometrically from 1/64 of the frames, then 1/8), each chunk's rows going
+    // through the logits kernel as soon as its frames land; then the statistics in one launch
+    // (statistics launches per chunk measured slower: a partial wave per chunk).
+    const long long f_all = offs[S] - offs[0];
+    const long long steady = std::max(1LL, (f_all + 7) / 8);
+    std::vector<int> cuts{0};  // chunk boundaries (speaker indices)
+    for (long long target = std::max(1LL, steady / 8); cuts.back() < S; target = std::min(steady, 2 * target)) {
+      int sb_ = cuts.back() + 1;
+      while (sb_ < S && offs[sb_] - offs[cuts.back()] < target) ++sb_;
+      cuts.push_back(sb_);
     }
+    rc = ensure_copy_stream(c, (int)cuts.size());
+    int k = 0;
+    if (!rc) {
+      cudaEventRecord(c->copy_events[k], c->stream);  // frames a previous call may still read
+      cudaStreamWaitEvent(c->copy_stream, c->copy_events[k], 0);
+      ++k;
+    }
+    for (size_t ci = 0; !rc && ci + 1 < cuts.size(); ++ci) {
+      const int sa = cuts[ci], sz = cuts[ci + 1];
+      const long long fa = offs[sa], fb = offs[sz];
+      if (fb > fa) {
+        cudaError_t e = cudaMemcpyAsync(const_cast<float*>(c->X) + fa * c->D, Xh + fa * c->D,
+                                        sizeof(float) * (size_t)(fb - fa) * c->D, cudaMemcpyHostToDevice,
+                                        c->copy_stream);
+        if (e != cudaSuccess) rc = cuda_fail(c, e, "cudaMemcpyAsync(speaker frames)");
+      }
+      if (!rc) {
+        cudaEventRecord(c->copy_events[k], c->copy_stream);
+        cudaStreamWaitEvent(c->stream, c->copy_events[k], 0);
+        ++k;
+        const int ta = (int)(pad[sa] / 128), tb = (int)(pad[sz] / 128);
+        if (tb > ta) rc = tc_run_batch_part(c, t, ta, tb - ta, 1);
+      }
+    }
+    if (!rc) rc = tc_run_batch_part(c, t, 0, (int)(Rpad / 128), 2);
   }
   if (!rc) {
     {
       GMM_LAUNCH(c, "row_of_comp_kernel");
-      row_of_comp_kernel<<<1, 1024, 0, c->stream>>>(M, c->tcm.Mpad, c->tcm.comp_of_row, ss->row_of_comp);
+      row_of_comp_kernel<<<1, 1024, 0, c->stream>>>(c->M, c->tcm.Mpad, c->tcm.comp_of_row, ss->row_of_comp);
     }
     if (S > 0 && d_ll) {
       GMM_LAUNCH(c, "seg_sum_kernel");
       seg_sum_kernel<<<S, 256, 0, c->stream>>>(d_offs, c->ll, d_ll);
     }
+  }
+  return rc;
+}
+
+// After the launches: a bounded wait that gave up shows in the error flag.
+int speaker_finish(Ctx* c, const char* what, int rc) {
+  if (!rc) {
     int herr = 0;
     cudaMemcpyAsync(&herr, c->tc_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
-    rc = sync(c, "per-speaker statistics (tensor-core path)");
+    rc = sync(c, what);
     if (!rc && herr) {
+      c->tcx_valid = false;
       cudaMemsetAsync(c->tc_err, 0, sizeof(int), c->stream);
-      rc = fail(c, GMM_ERR_TIMEOUT, "per-speaker statistics: a bounded device wait expired");
+      rc = fail(c, GMM_ERR_TIMEOUT, std::string(what) + ": a bounded device wait expired");
     }
   }
   cudaStreamSynchronize(c->stream);
+  return rc;
+}
+}  // namespace
+
+int tc_speaker_stats(Ctx* c, int S, const long long* offs, const long long* d_offs, double* d_ll,
+                     bool second_order, const float* Xh, SpeakerStats* ss) {
+  SpeakerBatch sb;
+  int rc = speaker_prepare(c, S, offs, d_offs, second_order, ss, &sb);
+  if (!rc) rc = speaker_launch(c, S, offs, d_offs, d_ll, Xh, &sb, ss);
+  rc = speaker_finish(c, "per-speaker statistics (tensor-core path)", rc);
   if (rc) tc_free_speaker_stats(c, ss);
   return rc;
 }
@@ -2334,12 +2380,77 @@ int tc_speaker_stats(Ctx* c, int S, const long long* offs, const long long* d_of
 // The buffers belong to the handle's scratch (reused by the next batch).
 void tc_free_speaker_stats(Ctx*, SpeakerStats* ss) { *ss = SpeakerStats(); }
 
+// Batched MAP. Over the resident frames the kernels of a call after the row map (logits,
+// statistics, component rows, speaker log-likelihoods, the MAP update) are captured into a CUDA
+// graph after an eager run, and a later call with the same batch layout and the same buffers
+// replays it; its host-to-device copies (offsets, pieces, work items) and the row map stay
+// outside the graph and are issued every call, so a replay sees the call's own speaker offsets.
+// With per-kernel profiling on, calls run eagerly (a graph has no per-kernel timing events).
 int tc_map_batch(Ctx* c, const MapBatch& b) {
   SpeakerStats ss;
-  int rc = tc_speaker_stats(c, b.S, b.offs, b.d_offs, b.ll, b.upV != 0, b.Xh, &ss);
+  SpeakerBatch sb;
+  int rc = speaker_prepare(c, b.S, b.offs, b.d_offs, b.upV != 0, &ss, &sb);
   if (rc) return rc;
-  rc = mstep_map_batch(c, b, nullptr, &ss);
-  if (!rc) rc = sync(c, "batched MAP update");
+  auto run = [&]() -> int {
+    int r = speaker_launch(c, b.S, b.offs, b.d_offs, b.ll, b.Xh, &sb, &ss);
+    if (!r) r = mstep_map_batch(c, b, nullptr, &ss);
+    return r;
+  };
+  if (b.Xh || c->profile) {
+    rc = run();
+  } else {
+    const TcBatch& t = sb.t;
+    auto bits = [](float v) { uint32_t u; std::memcpy(&u, &v, 4); return (long long)u; };
+    const long long key[] = {b.S, t.Rpad, t.n_work, c->N, c->M, c->D, t.K, t.n_chunks, c->tcm.Mpad, c->Mact,
+                             b.tau, b.upW | b.upM << 1 | b.upV << 2 | (t.second_order ? 8 : 0),
+                             bits(c->minGamma), bits((float)c->minLL), bits(c->min_var), c->wait_limit,
+                             (long long)(size_t)b.d_offs, (long long)(size_t)b.w, (long long)(size_t)b.mu,
+                             (long long)(size_t)b.var, (long long)(size_t)b.aw, (long long)(size_t)b.ll,
+                             (long long)(size_t)sb.d_pad, (long long)(size_t)t.row_frame,
+                             (long long)(size_t)t.tile_slot, (long long)(size_t)t.work, (long long)(size_t)t.part,
+                             (long long)(size_t)ss.piece0, (long long)(size_t)ss.npieces,
+                             (long long)(size_t)ss.row_of_comp, (long long)(size_t)ss.cent,
+                             (long long)(size_t)t.zplanes, (long long)(size_t)t.ll2, (long long)(size_t)t.ll,
+                             (long long)(size_t)t.llpart, (long long)(size_t)t.wplanes, (long long)(size_t)c->X,
+                             (long long)(size_t)c->w, (long long)(size_t)c->mu, (long long)(size_t)c->var,
+                             (long long)(size_t)c->tc_err, (long long)(size_t)c->tcm.comp_of_row, 0, 0, 0, 0, 0, 0};
+    static_assert(sizeof(key) == sizeof(c->map_graph_key), "graph key size");
+    if (c->map_graph && std::memcmp(key, c->map_graph_key, sizeof(key)) == 0) {
+      cudaError_t e = cudaGraphLaunch(c->map_graph, c->stream);
+      if (e != cudaSuccess) rc = cuda_fail(c, e, "cudaGraphLaunch(batched MAP)");
+      c->launches += c->map_graph_launches;
+    } else {
+      if (c->map_graph) cudaGraphExecDestroy(c->map_graph);
+      c->map_graph = nullptr;
+      rc = run();  // eager (also sets the kernels' attributes before any capture)
+      if (!rc) {
+        const bool prof = c->profile;
+        const long long l0 = c->launches;
+        c->profile = false;  // no timing events inside the graph
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed);
+        if (e == cudaSuccess) {
+          const int r = run();
+          e = cudaStreamEndCapture(c->stream, &g);
+          if (!r && e == cudaSuccess) e = cudaGraphInstantiate(&c->map_graph, g, 0);
+          if (r && e == cudaSuccess) e = cudaErrorUnknown;
+          if (g) cudaGraphDestroy(g);
+        }
+        c->map_graph_launches = (int)(c->launches - l0);
+        c->launches = l0;
+        c->profile = prof;
+        if (e != cudaSuccess) {
+          // no graph this time: the eager run stands, the next call tries again
+          if (c->map_graph) cudaGraphExecDestroy(c->map_graph);
+          c->map_graph = nullptr;
+          cudaGetLastError();
+        } else {
+          std::memcpy(c->map_graph_key, key, sizeof(key));
+        }
+      }
+    }
+  }
+  rc = speaker_finish(c, "batched MAP update", rc);
   tc_free_speaker_stats(c, &ss);
   return rc;
 }

@@ -125,6 +125,49 @@ def test_batch_mean_only_two_calls_repeat(glib):
     h.close()
 
 
+@pytest.mark.parametrize("upW,upM,upV", [(0, 1, 0), (1, 1, 1)])
+def test_batch_graph_replay_equals_eager(glib, upW, upM, upV):
+    """Over the resident frames the second call with the same batch layout replays the kernels
+    captured after the first one. Replays with the same offsets, and with other speaker lengths
+    of the same padded layout (same speaker count, tiles and work items; the offsets, pieces and
+    work items are uploaded every call), equal a fresh handle's eager call bit for bit, and the
+    launch count grows by the same number of kernels per call."""
+    X, offs, ubm = workload(seed=57)
+    lens = np.diff(offs)
+    # other lengths of the same tile layout: move frames within each speaker's last tile
+    lens2 = lens.copy()
+    for s in range(len(lens2)):
+        if lens2[s] % 128 not in (0, 1):
+            lens2[s] -= 1
+    offs2 = offs[0] + np.concatenate([[0], np.cumsum(lens2)]).astype(np.int64)
+
+    def fresh(o):
+        h = glib.Handle(0)
+        h.set_precision(glib.PREC_TC)
+        h.upload_model(*ubm)
+        h.upload_features(X)
+        r = h.map_batch(o, 16, upW, upM, upV)
+        h.close()
+        return r
+
+    h = glib.Handle(0)
+    h.set_precision(glib.PREC_TC)
+    h.upload_model(*ubm)
+    h.upload_features(X)
+    first = h.map_batch(offs, 16, upW, upM, upV)
+    n1 = h.launch_count()
+    again = h.map_batch(offs, 16, upW, upM, upV)  # replay
+    n2 = h.launch_count()
+    other = h.map_batch(offs2, 16, upW, upM, upV)  # replay with new offsets
+    n3 = h.launch_count()
+    h.close()
+    for x, y in zip(first, again):
+        assert np.array_equal(x, y)
+    for x, y in zip(other, fresh(offs2)):
+        assert np.array_equal(x, y)
+    assert n2 - n1 == n3 - n2 > 0
+
+
 def test_batch_bad_offsets_are_errors(glib):
     X, offs, ubm = workload(seed=56)
     h = glib.Handle(0)
