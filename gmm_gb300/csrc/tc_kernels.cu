@@ -292,10 +292,14 @@ __device__ __forceinline__ void own_image_row_to_tmem(const uint16_t* planes, in
 
 // Row `r` of tile `tile` built from the raw features instead: the operand columns of
 // frame f (zeros when f < 0 or !valid), split into three bf16 planes, stored into TMEM (laid out
-// as image_row_to_tmem does) and into the plane images, which the statistics kernel reads next.
+// as image_row_to_tmem does) and, with TO_IMAGES, into the plane images, which the statistics
+// kernel reads next. Building from the 4D bytes of a frame is cheaper than copying its 6K bytes
+// of images (at N = 10M, M = 2048, D = 39: 8.65 ms for the logits kernel that builds and writes
+// the images, 9.31 ms for one that copies them), so the logits kernel builds from the frames on
+// every pass where it has two Z buffers.
 // The row's D <= K/2 - 1 features are loaded into registers first (independent loads, one
 // latency); the squares sit at the constant column K/2 + d, so every register index is static.
-template <int K, bool TO_TMEM = true>
+template <int K, bool TO_TMEM = true, bool TO_IMAGES = true>
 __device__ __forceinline__ void features_row_to_tmem(const float* __restrict__ X, int D, long long f,
                                                      uint16_t* __restrict__ planes, int nT, int tile, int r,
                                                      uint32_t taddr, bool valid) {
@@ -331,7 +335,7 @@ __device__ __forceinline__ void features_row_to_tmem(const float* __restrict__ X
 #pragma unroll
     for (int p = 0; p < 3; ++p) {
       if constexpr (TO_TMEM) tmem_st8(taddr + p * (K / 2) + c * 4, w[p]);
-      if (valid) {
+      if (TO_IMAGES && valid) {
         uint4* dst = reinterpret_cast<uint4*>(planes + ((size_t)(p * nT + tile) * KC + c) * 1024 + (size_t)r * 8);
         dst[0] = make_uint4(w[p][0], w[p][1], w[p][2], w[p][3]);
         dst[128] = make_uint4(w[p][4], w[p][5], w[p][6], w[p][7]);  // chunk c + 1: 1024 elements on
@@ -404,11 +408,12 @@ __global__ void __launch_bounds__(kLlThreads, 1)
               long long N, const long long* __restrict__ row_frame, const int* __restrict__ tile_wbase,
               int nTz, int nTw, int tile0, int n_tiles, int n_chunks, float trouble2, float minLL,
               float* __restrict__ ll2_out, float* __restrict__ ll_out, double* __restrict__ llpart,
-              int* __restrict__ err, const float* __restrict__ X, int D, long long wait_limit,
+              int* __restrict__ err, const float* __restrict__ X, int D, int write_images, long long wait_limit,
               uint32_t* __restrict__ fmask, float mask_thr2, int single_comp, const int* __restrict__ mact_dev) {
   // frame tiles tile0 .. tile0 + n_tiles - 1, strided over the CTAs. With X the loaders build
-  // the Z tiles from the raw features (and write the plane images for the statistics kernel);
-  // without, they copy them from the plane images.
+  // the Z tiles from the raw features (and, with write_images, write the plane images for the
+  // statistics kernel; with one Z buffer they always do); without, they copy them from the plane
+  // images.
   using C = LlCfg<K>;
   constexpr int ZB = C::ZB, NW = C::NW;
   extern __shared__ uint8_t smem_raw[];
@@ -538,7 +543,8 @@ __global__ void __launch_bounds__(kLlThreads, 1)
       if (!X) {
         image_row_to_tmem(zplanes, nTz, K, tile, row, zaddr, tile < nTz);
       } else if constexpr (ZB == 2) {
-        features_row_to_tmem<K>(X, D, frame_of(tile), zplanes, nTz, tile, row, zaddr, tile < nTz);
+        if (write_images) features_row_to_tmem<K>(X, D, frame_of(tile), zplanes, nTz, tile, row, zaddr, tile < nTz);
+        else features_row_to_tmem<K, true, false>(X, D, frame_of(tile), zplanes, nTz, tile, row, zaddr, tile < nTz);
       } else {
         if (it == 0) features_row_to_tmem<K, false>(X, D, frame_of(tile), zplanes, nTz, tile, row, 0, tile < nTz);
         own_image_row_to_tmem<K>(zplanes, nTz, tile, row, zaddr, tile < nTz);
@@ -1674,7 +1680,8 @@ int make_map(Ctx* c, CUtensorMap* map, const uint16_t* base, long long total_ele
   return GMM_OK;
 }
 
-// build_planes: the logits kernel builds the feature planes of its tiles from c->X on the way
+// build_planes: the logits kernel writes the feature planes of its tiles, built from c->X on the
+// way (with two Z buffers, K <= 80, it builds its Z tiles from c->X on every pass)
 // Largest dynamic shared memory of the logits kernel: room for the chunk maxima of 32 chunks
 // where that fits (the frame masks of the sparse tile schedule), else the plain layout.
 template <int K>
@@ -1714,7 +1721,8 @@ int launch_ll_part(Ctx* c, int tile0, int n_tiles_ll, float* ll_out_dev, bool wa
     ll_kernel<K><<<grid_ll, kLlThreads, smem, c->stream>>>(
         c->tm_wfull, c->tcx.planes, c->N, nullptr, nullptr, nTz, nTw, tile0, n_tiles_ll, n_chunks, trouble2,
         c->minLL, c->tcm.ll2, ll_out_dev, c->tc_llpart, c->tc_err,
-        build_planes ? c->X : nullptr, c->D, c->wait_limit, masks ? c->sched.fmask : nullptr,
+        (build_planes || LC::ZB == 2) ? c->X : nullptr, c->D, build_planes ? 1 : 0, c->wait_limit,
+        masks ? c->sched.fmask : nullptr,
         (float)(log2((double)c->minGamma) - kSchedMargin2), c->Mact == 1,
         c->static_shapes ? c->flag + 4 : nullptr);
   }
@@ -2495,7 +2503,7 @@ void run_batch_k(Ctx* c, const TcBatch& b, const CUtensorMap& zfull, int tile0, 
     ll_kernel<K><<<grid_ll, kLlThreads, LC::SMEM, c->stream>>>(
         *b.wmap, b.zplanes, b.N, b.row_frame, b.tile_wbase, nTz, b.w_chunks_total, tile0, ntl, b.n_chunks,
         (float)(c->minLL * kLog2e), c->minLL, b.ll2, b.ll, b.llpart, c->tc_err,
-        b.X, b.D, c->wait_limit, nullptr, 0.0f, 0, nullptr);
+        b.X, b.D, 1, c->wait_limit, nullptr, 0.0f, 0, nullptr);
   }
   if ((stages & 2) && b.n_work > 0) {
     GMM_LAUNCH(c, "tc_acc_kernel");
