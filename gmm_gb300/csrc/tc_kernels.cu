@@ -23,9 +23,9 @@
 // accepts only a few MMAs ahead, and an issuing warp shares its sub-partition with busy epilogue
 // warps: two issuers and fully unrolled issue loops (descriptor = per-stage base + constant).
 //   ll_kernel  (frame-tile major, persistent): four loader warps fill the 128-frame Z tile in
-//              TMEM -- built from the raw frames (and written to the plane images) on the first
-//              pass for K <= 80, copied from the plane images otherwise -- double-buffered where
-//              it fits; 128-component W chunks stream through a TMA ring; S[128 frames x 128
+//              TMEM -- for K <= 80 built from the raw frames on every pass (and written to the
+//              plane images on the first), for larger K copied from the plane images --
+//              double-buffered where it fits; 128-component W chunks stream through a TMA ring; S[128 frames x 128
 //              comps] accumulates in one of two TMEM buffers; the epilogue releases each buffer
 //              as soon as it has read it and runs an online log2-sum-exp over all chunks ->
 //              per-frame log-likelihood.
