@@ -939,6 +939,7 @@ def main():
     # back to the host, every step
     h2d_before = h2d_rate(torch, gpu)
     e2e = None if args.no_e2e else timed_e2e(wl, args.steps, torch, world)
+    h2d_after = h2d_rate(torch, gpu)
 
     # the opt-in sparse tile schedule of the statistics on the same workload (its accuracy cost is
     # stated in the header: variances within 2.4e-5 of FP64 instead of 1e-5)
@@ -1021,7 +1022,7 @@ def main():
                 "kernel_ms_per_launch": per_launch_ms,
                 "kernel_share": kms / max(1e-9, sum(v[0] for v in prof.values()))}
 
-    host_link = {"cpus": cpu_note, "h2d_gbs_pinned": [h2d_before, h2d_rate(torch, gpu)]}
+    host_link = {"cpus": cpu_note, "h2d_gbs_pinned": [h2d_before, h2d_after]}
     os.sched_setaffinity(0, prev_cpus)  # the CPU baseline runs on every host core
     threads = os.cpu_count() or 1
     r, sample, _, _ = wl.cpu_rate(args.cpu_seconds, threads)
