@@ -308,99 +308,128 @@ __global__ void mllr_apply_kernel(int M, int D, float* __restrict__ mu, const do
 // CModelAdapt::UpdateModelMAP (OL_ModelAdapt.cpp:1024-1099) for every (speaker, component),
 // with the resident model as both the starting point and the prior: AdaptModelMAP copies the UBM
 // (:1259-1260) and the first MAP iteration adapts that copy towards the statistics. Same
-// expression order as map_comp_kernel. One thread per (speaker, component) (see below).
+// expression order as map_comp_kernel. A block takes kMapPairs (speaker, component) pairs: first
+// one thread per pair forms the pair's scalars (occupation, alpha, 1 - alpha, 1 / occupation)
+// and its weight; then the block's threads take the (pair, dimension) elements, pairs fastest
+// (consecutive components are consecutive rows of the partials: coalesced reads), so that the
+// FP64 work of the D dimensions runs in parallel instead of in one thread per pair (1.47 ms for
+// C3's 1000 x 1024 pairs with one thread per pair). Means and variances are staged in shared
+// memory ([pair][D + 1], an odd stride) and written out as one contiguous range.
 // Statistics come in one of two layouts (kStatsSlots / kStatsPlain); in the plain layout the
 // speaker's total log-likelihood is copied out as well.
-constexpr int kMapThreads = 64;  // (speaker, component) pairs per block
+constexpr int kMapPairs = 32;     // (speaker, component) pairs per block
+constexpr int kMapThreads = 256;
 __global__ void __launch_bounds__(kMapThreads) map_batch_kernel(
     int S, int M, int D, const double* __restrict__ plain, const double* __restrict__ part, int K, int n_chunks,
     const int* __restrict__ piece0, const int* __restrict__ npieces, const int* __restrict__ row_of_comp,
     const float* __restrict__ cent, const long long* __restrict__ offs, const float* __restrict__ uw, const float* __restrict__ umu,
     const float* __restrict__ uvar, int tau, int upW, int upM, int upV, float min_var, float* __restrict__ ow,
     float* __restrict__ omu, float* __restrict__ ovar, float* __restrict__ adapted_w, double* __restrict__ ll) {
-  // thread = (speaker, component) pair t = s M + m: the partials of consecutive components are
-  // consecutive rows (coalesced reads); the block's means and variances are staged in shared
-  // memory ([pair][D + 1], an odd stride) and written out as one contiguous range.
   extern __shared__ float s_out[];
+  __shared__ double s_mp[kMapPairs], s_alfa[kMapPairs], s_one[kMapPairs], s_rmp[kMapPairs];
+  __shared__ float s_alfa_f[kMapPairs], s_one_f[kMapPairs], s_rmp_f[kMapPairs];  // FP32 copies
+  __shared__ int s_adapt[kMapPairs], s_spk[kMapPairs], s_comp[kMapPairs];
   const int SD = D + 1;
   float* s_mu = s_out;
-  float* s_var = s_out + kMapThreads * SD;
+  float* s_var = s_out + kMapPairs * SD;
   const long long tot_pairs = (long long)S * M;
-  const long long t0 = (long long)blockIdx.x * kMapThreads, t = t0 + threadIdx.x;
-  if (t < tot_pairs) {
+  const long long t0 = (long long)blockIdx.x * kMapPairs;
+  const int n_here = (int)(tot_pairs - t0 < kMapPairs ? tot_pairs - t0 : kMapPairs);
+  // statistic e (n / F / S order; operand-layout columns of the tensor-core partials) of
+  // component m for speaker s
+  auto stat = [&](int s, int m, int e) -> double {  // e in [0, 2D]: F_k = e < D, S_k = D + k, n = 2D
+    if (plain) {
+      const double* pst = plain + (size_t)s * ((size_t)M * (1 + 2 * D) + 2);
+      if (e == 2 * D) return pst[m];
+      if (e < D) return pst[M + (size_t)m * D + e];
+      return pst[M + (size_t)M * D + (size_t)m * D + (e - D)];
+    }
+    const int row = row_of_comp[m];
+    if (row < 0) return 0.0;  // inactive components were never accumulated
+    const int np = npieces[s], p0 = piece0[s];
+    double v = 0.0;
+    const int col = tc_stat_col(D, K, e);
+    for (int p = 0; p < np; ++p) {
+      const double x = part[((size_t)(p0 + p) * n_chunks + row / 128) * K * 128 + (size_t)col * 128 + (row % 128)];
+      v = p == 0 ? x : __dadd_rn(v, x);
+    }
+    return v;
+  };
+  if (threadIdx.x < n_here) {
+    const long long t = t0 + threadIdx.x;
     const int s = (int)(t / M), m = (int)(t - (long long)s * M);
-    const float* um = umu + (size_t)m * D;
-    const float* uv = uvar + (size_t)m * D;
-    // statistic e (n / F / S order; operand-layout columns of the tensor-core partials) of
-    // component m for speaker s
-    const int row = plain ? 0 : row_of_comp[m];
-    const double* pst = plain ? plain + (size_t)s * ((size_t)M * (1 + 2 * D) + 2) : nullptr;
-    if (plain && m == 0) ll[s] = pst[(size_t)M * (1 + 2 * D)];
-    const int np = plain ? 0 : npieces[s], p0 = plain ? 0 : piece0[s];
-    auto stat = [&](int e) -> double {  // e in [0, 2D]: F_k = e < D, S_k = D + k, n = 2D
-      if (plain) {
-        if (e == 2 * D) return pst[m];
-        if (e < D) return pst[M + (size_t)m * D + e];
-        return pst[M + (size_t)M * D + (size_t)m * D + (e - D)];
-      }
-      if (row < 0) return 0.0;  // inactive components were never accumulated
-      double v = 0.0;
-      const int col = tc_stat_col(D, K, e);
-      for (int p = 0; p < np; ++p) {
-        const double x = part[((size_t)(p0 + p) * n_chunks + row / 128) * K * 128 + (size_t)col * 128 + (row % 128)];
-        v = p == 0 ? x : __dadd_rn(v, x);
-      }
-      return v;
-    };
-    const double mp = stat(2 * D);
+    if (plain && m == 0) ll[s] = plain[(size_t)s * ((size_t)M * (1 + 2 * D) + 2) + (size_t)M * (1 + 2 * D)];
+    const double mp = stat(s, m, 2 * D);
     const bool adapt = uw[m] != 0.0f && mp > 0.0;
     const unsigned int tot = (unsigned int)(offs[s + 1] - offs[s]);
     const double alfa = adapt ? __ddiv_rn(mp, __dadd_rn(mp, (double)tau)) : 0.0;
     const double one_m = __dsub_rn(1.0, alfa);
-    {
-      float aw = 0.0f;
-      const bool wset = adapt && upW && tot > 0;
-      if (wset) {
-        const double t1 = __dmul_rn(alfa, __ddiv_rn(mp, (double)tot));
-        aw = (float)__dadd_rn(t1, __dmul_rn(one_m, (double)uw[m]));
-      }
-      ow[t] = wset ? aw : uw[m];
-      adapted_w[t] = aw;
+    float aw = 0.0f;
+    const bool wset = adapt && upW && tot > 0;
+    if (wset) {
+      const double t1 = __dmul_rn(alfa, __ddiv_rn(mp, (double)tot));
+      aw = (float)__dadd_rn(t1, __dmul_rn(one_m, (double)uw[m]));
     }
-    const double rmp = adapt ? __drcp_rn(mp) : 0.0;  // the D quotients below share the divisor mp
-    // the sparse statistics kernel's partials are centred on the component's mean (cr): tc_uncentre
-    const float* cr = (plain || !cent) ? nullptr : cent + (size_t)(row >= 0 ? row : 0) * D;
-    for (int k = 0; k < D; ++k) {
-      float am = um[k], av = uv[k];
-      if (adapt && (upM || upV)) {
-        const double Fk = stat(k);
-        const double c = cr ? (double)cr[k] : 0.0;
-        const double a1 = div_by_rcp(__dmul_rn(alfa, plain ? Fk : tc_uncentre_F(Fk, mp, c)), mp, rmp);
-        const double amd = __dadd_rn(a1, __dmul_rn(one_m, (double)um[k]));
-        am = (float)amd;
-        if (upV && plain) {
-          // the reference's expression: second moment and squared mean in float
-          const float second = __fadd_rn(uv[k], __fmul_rn(um[k], um[k]));
-          const float msq = __fmul_rn(am, am);
-          const double b1 = div_by_rcp(__dmul_rn(alfa, stat(D + k)), mp, rmp);
-          const double b2 = __dadd_rn(b1, __dmul_rn(one_m, (double)second));
-          av = (float)__dsub_rn(b2, (double)msq);
-          if (av < min_var) av = min_var;
-        } else if (upV) {
-          // tensor-core path: the variance in FP64 throughout
-          const double second = __dadd_rn((double)uv[k], __dmul_rn((double)um[k], (double)um[k]));
-          const double b1 = div_by_rcp(__dmul_rn(alfa, tc_uncentre_S(stat(D + k), Fk, mp, c)), mp, rmp);
-          const double b2 = __dadd_rn(b1, __dmul_rn(one_m, second));
-          av = (float)__dsub_rn(b2, __dmul_rn(amd, amd));
-          if (av < min_var) av = min_var;
-        }
-      }
-      s_mu[threadIdx.x * SD + k] = am;
-      s_var[threadIdx.x * SD + k] = av;
-    }
+    ow[t] = wset ? aw : uw[m];
+    adapted_w[t] = aw;
+    s_mp[threadIdx.x] = mp;
+    s_alfa[threadIdx.x] = alfa;
+    s_one[threadIdx.x] = one_m;
+    s_rmp[threadIdx.x] = adapt ? __drcp_rn(mp) : 0.0;  // the D quotients share the divisor mp
+    s_alfa_f[threadIdx.x] = (float)alfa;
+    s_one_f[threadIdx.x] = (float)one_m;
+    s_rmp_f[threadIdx.x] = (float)s_rmp[threadIdx.x];
+    s_adapt[threadIdx.x] = adapt ? 1 : 0;
+    s_spk[threadIdx.x] = s;
+    s_comp[threadIdx.x] = m;
   }
   __syncthreads();
-  const long long n_here = tot_pairs - t0 < kMapThreads ? tot_pairs - t0 : kMapThreads;
+  for (int i = threadIdx.x; i < kMapPairs * D; i += kMapThreads) {
+    const int j = i % kMapPairs, k = i / kMapPairs;
+    if (j >= n_here) continue;
+    const int s = s_spk[j], m = s_comp[j];  // (one 64-bit division per pair, in the first phase)
+    const float* um = umu + (size_t)m * D;
+    const float* uv = uvar + (size_t)m * D;
+    const bool adapt = s_adapt[j] != 0;
+    const double mp = s_mp[j], alfa = s_alfa[j], one_m = s_one[j], rmp = s_rmp[j];
+    // the sparse statistics kernel's partials are centred on the component's mean (cr): tc_uncentre
+    const int row = plain ? 0 : row_of_comp[m];
+    const float* cr = (plain || !cent) ? nullptr : cent + (size_t)(row >= 0 ? row : 0) * D;
+    float am = um[k], av = uv[k];
+    if (adapt && !plain && upM && !upV) {
+      // tensor-core path, means only: FP32 arithmetic (GB300's FP64 rate -- conversions
+      // included -- is 1/64 of FP32); the statistics already carry ~1e-6 relative error, FP32
+      // adds ~1e-7 of the mean. FP64 stays for the variance update.
+      const double Fd = stat(s, m, k);
+      const float Ff = cr ? (float)tc_uncentre_F(Fd, mp, (double)cr[k]) : (float)Fd;
+      am = __fmaf_rn(s_alfa_f[j], __fmul_rn(Ff, s_rmp_f[j]), __fmul_rn(s_one_f[j], um[k]));
+    } else if (adapt && (upM || upV)) {
+      const double Fk = stat(s, m, k);
+      const double c = cr ? (double)cr[k] : 0.0;
+      const double a1 = div_by_rcp(__dmul_rn(alfa, plain ? Fk : tc_uncentre_F(Fk, mp, c)), mp, rmp);
+      const double amd = __dadd_rn(a1, __dmul_rn(one_m, (double)um[k]));
+      am = (float)amd;
+      if (upV && plain) {
+        // the reference's expression: second moment and squared mean in float
+        const float second = __fadd_rn(uv[k], __fmul_rn(um[k], um[k]));
+        const float msq = __fmul_rn(am, am);
+        const double b1 = div_by_rcp(__dmul_rn(alfa, stat(s, m, D + k)), mp, rmp);
+        const double b2 = __dadd_rn(b1, __dmul_rn(one_m, (double)second));
+        av = (float)__dsub_rn(b2, (double)msq);
+        if (av < min_var) av = min_var;
+      } else if (upV) {
+        // tensor-core path: the variance in FP64 throughout
+        const double second = __dadd_rn((double)uv[k], __dmul_rn((double)um[k], (double)um[k]));
+        const double b1 = div_by_rcp(__dmul_rn(alfa, tc_uncentre_S(stat(s, m, D + k), Fk, mp, c)), mp, rmp);
+        const double b2 = __dadd_rn(b1, __dmul_rn(one_m, second));
+        av = (float)__dsub_rn(b2, __dmul_rn(amd, amd));
+        if (av < min_var) av = min_var;
+      }
+    }
+    s_mu[j * SD + k] = am;
+    s_var[j * SD + k] = av;
+  }
+  __syncthreads();
   for (int i = threadIdx.x; i < n_here * D; i += kMapThreads) {
     const int j = i / D, k = i - j * D;
     if (omu) omu[(size_t)t0 * D + i] = s_mu[j * SD + k];
@@ -1000,9 +1029,9 @@ int mstep_map_batch(Ctx* c, const MapBatch& b, const double* plain, const Speake
   if (tot == 0) return GMM_OK;
   {
     GMM_LAUNCH(c, "map_batch_kernel");
-    const size_t smem = sizeof(float) * 2 * kMapThreads * (size_t)(c->D + 1);
+    const size_t smem = sizeof(float) * 2 * kMapPairs * (size_t)(c->D + 1);
     cudaFuncSetAttribute(map_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    map_batch_kernel<<<(unsigned)((tot + kMapThreads - 1) / kMapThreads), kMapThreads, smem, c->stream>>>(
+    map_batch_kernel<<<(unsigned)((tot + kMapPairs - 1) / kMapPairs), kMapThreads, smem, c->stream>>>(
         b.S, c->M, c->D, plain, ss ? ss->part : nullptr, ss ? ss->K : 0, ss ? ss->n_chunks : 0,
         ss ? ss->piece0 : nullptr, ss ? ss->npieces : nullptr, ss ? ss->row_of_comp : nullptr,
         ss ? ss->cent : nullptr, b.d_offs, c->w, c->mu, c->var, b.tau, b.upW, b.upM, b.upV, c->min_var, b.w, b.mu, b.var, b.aw, b.ll);
