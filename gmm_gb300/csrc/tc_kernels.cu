@@ -2315,9 +2315,9 @@ int speaker_launch(Ctx* c, int S, const long long* offs, const long long* d_offs
     const long long steady = std::max(1LL, (f_all + 7) / 8);
     std::vector<int> cuts{0};  // chunk boundaries (speaker indices)
     for (long long target = std::max(1LL, steady / 8); cuts.back() < S; target = std::min(steady, 2 * target)) {
-      int sb_ = cuts.back() + 1;
-      while (sb_ < S && offs[sb_] - offs[cuts.back()] < target) ++sb_;
-      cuts.push_back(sb_);
+      int next = cuts.back() + 1;
+      while (next < S && offs[next] - offs[cuts.back()] < target) ++next;
+      cuts.push_back(next);
     }
     rc = ensure_copy_stream(c, (int)cuts.size());
     int k = 0;
@@ -2327,8 +2327,8 @@ int speaker_launch(Ctx* c, int S, const long long* offs, const long long* d_offs
       ++k;
     }
     for (size_t ci = 0; !rc && ci + 1 < cuts.size(); ++ci) {
-      const int sa = cuts[ci], sz = cuts[ci + 1];
-      const long long fa = offs[sa], fb = offs[sz];
+      const int sa = cuts[ci], se = cuts[ci + 1];  // speakers [sa, se)
+      const long long fa = offs[sa], fb = offs[se];
       if (fb > fa) {
         cudaError_t e = cudaMemcpyAsync(const_cast<float*>(c->X) + fa * c->D, Xh + fa * c->D,
                                         sizeof(float) * (size_t)(fb - fa) * c->D, cudaMemcpyHostToDevice,
@@ -2339,7 +2339,7 @@ int speaker_launch(Ctx* c, int S, const long long* offs, const long long* d_offs
         cudaEventRecord(c->copy_events[k], c->copy_stream);
         cudaStreamWaitEvent(c->stream, c->copy_events[k], 0);
         ++k;
-        const int ta = (int)(pad[sa] / 128), tb = (int)(pad[sz] / 128);
+        const int ta = (int)(pad[sa] / 128), tb = (int)(pad[se] / 128);
         if (tb > ta) rc = tc_run_batch_part(c, t, ta, tb - ta, 1);
       }
     }
