@@ -167,6 +167,7 @@ struct Ctx {
   // every buffer the kernels read or write) stays the same: the kernels of one call, captured
   cudaGraphExec_t map_graph = nullptr;
   long long map_graph_key[48] = {};
+  long long map_last_key[48] = {};  // the previous call's key: a layout is captured when it repeats
   int map_graph_launches = 0;  // kernel launches inside the graph (the launch count adds them)
   double* ll_hist = nullptr;  // [ll_hist_cap + 1]: per-iteration total LL, then a counter
   int ll_hist_cap = 0;

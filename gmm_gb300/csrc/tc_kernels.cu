@@ -2390,8 +2390,8 @@ void tc_free_speaker_stats(Ctx*, SpeakerStats* ss) { *ss = SpeakerStats(); }
 
 // Batched MAP. Over the resident frames the kernels of a call after the row map (logits,
 // statistics, component rows, speaker log-likelihoods, the MAP update) are captured into a CUDA
-// graph after an eager run, and a later call with the same batch layout and the same buffers
-// replays it; its host-to-device copies (offsets, pieces, work items) and the row map stay
+// graph after an eager run of a batch layout seen on the previous call too, and a later call
+// with the same batch layout and the same buffers replays it; its host-to-device copies (offsets, pieces, work items) and the row map stay
 // outside the graph and are issued every call, so a replay sees the call's own speaker offsets.
 // With per-kernel profiling on, calls run eagerly (a graph has no per-kernel timing events).
 int tc_map_batch(Ctx* c, const MapBatch& b) {
@@ -2428,10 +2428,14 @@ int tc_map_batch(Ctx* c, const MapBatch& b) {
       if (e != cudaSuccess) rc = cuda_fail(c, e, "cudaGraphLaunch(batched MAP)");
       c->launches += c->map_graph_launches;
     } else {
-      if (c->map_graph) cudaGraphExecDestroy(c->map_graph);
-      c->map_graph = nullptr;
+      // a layout is captured the second time in a row it comes (calls whose layouts keep
+      // changing run eagerly and pay no capture)
+      const bool repeat = std::memcmp(key, c->map_last_key, sizeof(key)) == 0;
+      std::memcpy(c->map_last_key, key, sizeof(key));
       rc = run();  // eager (also sets the kernels' attributes before any capture)
-      if (!rc) {
+      if (!rc && repeat) {
+        if (c->map_graph) cudaGraphExecDestroy(c->map_graph);
+        c->map_graph = nullptr;
         const bool prof = c->profile;
         const long long l0 = c->launches;
         c->profile = false;  // no timing events inside the graph

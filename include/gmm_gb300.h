@@ -225,11 +225,11 @@ int gmm_map_update(gmm_handle h, int tau, int up_weight, int up_mean, int up_var
  * total log-likelihood under the UBM). tau >= 1. The resident model is not changed. The batched
  * calls (gmm_map_batch[_device], gmm_mllr_batch) keep their device working buffers on the handle
  * between calls, grown to the largest batch seen and released by gmm_destroy; they count against
- * the handle's memory budget. With GMM_PREC_TC over the resident frames, a call whose batch layout
- * (speaker count, padded tiles, work items) and buffers equal the previous call's replays that
- * call's kernels from a CUDA graph (captured after it ran); the speaker offsets and the per-call
- * tables are uploaded every call, so the results equal an eager call's bit for bit. Per-kernel
- * profiling (gmm_profile_enable) runs calls eagerly. */
+ * the handle's memory budget. With GMM_PREC_TC over the resident frames, a batch layout (speaker
+ * count, padded tiles, work items, buffers) that comes on two calls in a row is captured into a
+ * CUDA graph after the second call ran, and later calls with that layout replay it; the speaker
+ * offsets and the per-call tables are uploaded every call, so the results equal an eager call's
+ * bit for bit. Per-kernel profiling (gmm_profile_enable) runs calls eagerly. */
 int gmm_map_batch(gmm_handle h, int S, const long long* offs, int tau, int up_weight, int up_mean,
                   int up_var, float* w, float* mu, float* var, double* ll);
 /* Global MLLR mean transforms for S speakers in one call (one regression class, one iteration):

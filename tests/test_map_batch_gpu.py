@@ -127,11 +127,11 @@ def test_batch_mean_only_two_calls_repeat(glib):
 
 @pytest.mark.parametrize("upW,upM,upV", [(0, 1, 0), (1, 1, 1)])
 def test_batch_graph_replay_equals_eager(glib, upW, upM, upV):
-    """Over the resident frames the second call with the same batch layout replays the kernels
-    captured after the first one. Replays with the same offsets, and with other speaker lengths
-    of the same padded layout (same speaker count, tiles and work items; the offsets, pieces and
-    work items are uploaded every call), equal a fresh handle's eager call bit for bit, and the
-    launch count grows by the same number of kernels per call."""
+    """Over the resident frames a batch layout that comes twice in a row is captured (after the
+    second call's eager run) and replayed by later calls with the same layout. Replays with the
+    same offsets, and with other speaker lengths of the same padded layout (same speaker count,
+    tiles and work items; the offsets, pieces and work items are uploaded every call), equal the
+    eager calls bit for bit, and every call adds the same number of kernel launches."""
     X, offs, ubm = workload(seed=57)
     lens = np.diff(offs)
     # other lengths of the same tile layout: move frames within each speaker's last tile
@@ -154,18 +154,20 @@ def test_batch_graph_replay_equals_eager(glib, upW, upM, upV):
     h.set_precision(glib.PREC_TC)
     h.upload_model(*ubm)
     h.upload_features(X)
-    first = h.map_batch(offs, 16, upW, upM, upV)
-    n1 = h.launch_count()
-    again = h.map_batch(offs, 16, upW, upM, upV)  # replay
-    n2 = h.launch_count()
-    other = h.map_batch(offs2, 16, upW, upM, upV)  # replay with new offsets
-    n3 = h.launch_count()
+    counts = [h.launch_count()]
+    results = []
+    for o in (offs, offs, offs2, offs):  # eager, eager + capture, replay, replay
+        results.append(h.map_batch(o, 16, upW, upM, upV))
+        counts.append(h.launch_count())
     h.close()
-    for x, y in zip(first, again):
+    first, again, other, last = results
+    for x, y, z in zip(first, again, last):
         assert np.array_equal(x, y)
+        assert np.array_equal(x, z)
     for x, y in zip(other, fresh(offs2)):
         assert np.array_equal(x, y)
-    assert n2 - n1 == n3 - n2 > 0
+    steps = np.diff(counts)
+    assert steps[0] > 0 and np.all(steps == steps[0]), steps
 
 
 def test_batch_bad_offsets_are_errors(glib):
