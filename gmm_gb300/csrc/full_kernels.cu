@@ -314,7 +314,7 @@ __global__ void __launch_bounds__(kFtThreads, 1)
       float maxLL = minLL, sumLL = minLL;
       for (int g = 0; g < ng && ok; ++g) {
         const int sidx = it * ng + g, b = sidx & 1;
-        if (!mbar_wait(&d_full[b], (sidx >> 1) & 1, abort_flag, kFtWait)) { ok = false; break; }
+        if (!mbar_wait_all(&d_full[b], (sidx >> 1) & 1, abort_flag, kFtWait)) { ok = false; break; }
         tc_fence_after();
         const int nt = min(GC, Mact - g * GC);
         float2 cp[GC];  // the group's constants, loaded before the accumulator

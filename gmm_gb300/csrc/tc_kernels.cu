@@ -17,8 +17,8 @@
 //
 // A tcgen05.mma with M = 128 and K = 16 costs max(45.5, N / 2) cycles on GB300 (measured), so
 // both kernels use N >= 128 for the logits. Two kernels per E-step. Each has one TMA-producer
-// warp, two MMA-issuing threads in warps on different SM sub-partitions and eight epilogue warps
-// (two per TMEM lane quadrant); the logits MMAs take their A operand from TMEM
+// warp, MMA-issuing threads in warps on different SM sub-partitions and epilogue warps that each
+// own one TMEM lane quadrant (32 rows); the logits MMAs take their A operand from TMEM
 // (tcgen05.mma ... [a_tmem], b_desc), so mostly B is read from shared memory. The tensor pipe
 // accepts only a few MMAs ahead, and an issuing warp shares its sub-partition with busy epilogue
 // warps: two issuers and fully unrolled issue loops (descriptor = per-stage base + constant).
@@ -391,16 +391,15 @@ struct LlCfg {
   static constexpr int S_COL = 0;          // 2 accumulator buffers of 128 columns
   static constexpr int Z_COL = 256;        // Z buffers
   static constexpr int OFF_W = 0;
-  static constexpr int OFF_RED = OFF_W + NW * W_STAGE;  // [128] max, [128] sum, [4] stop flags
-  static constexpr int OFF_BAR = OFF_RED + 2 * 128 * 4 + 64;
+  static constexpr int OFF_BAR = OFF_W + NW * W_STAGE;
   static constexpr int OFF_MISC = OFF_BAR + 16 * 8;
   static constexpr int SMEM = cmax(OFF_MISC + 64 + 1024, 120 * 1024);
-  // with frame masks: [2 column halves][chunks][128 rows] chunk maxima of the logits
+  // with frame masks: [chunks][128 rows] chunk maxima of the logits
   static constexpr int OFF_CM = OFF_MISC + 64;
-  static constexpr int smem_with_masks(int chunks) { return cmax(SMEM, OFF_CM + 2 * chunks * 128 * 4 + 1024); }
+  static constexpr int smem_with_masks(int chunks) { return cmax(SMEM, OFF_CM + chunks * 128 * 4 + 1024); }
   static_assert(Z_COL + ZB * ZCOLS <= 512, "TMEM budget");
 };
-constexpr int kLlThreads = 480;  // warp 0 TMA, 1 and 14 MMA, 2-9 epilogue, 10-13 Z loaders
+constexpr int kLlThreads = 352;  // warp 0 TMA, 1 and 10 MMA, 2-5 epilogue, 6-9 Z loaders
 
 template <int K>
 __global__ void __launch_bounds__(kLlThreads, 1)
@@ -428,9 +427,6 @@ __global__ void __launch_bounds__(kLlThreads, 1)
   uint64_t* mma_done = bars + 14;  // [2]: one per MMA-issuing thread
   uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(smem + C::OFF_MISC);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + C::OFF_MISC + 8);
-  float* red_m = reinterpret_cast<float*>(smem + C::OFF_RED);
-  float* red_s = red_m + 128;
-  volatile int* stop_s = reinterpret_cast<volatile int*>(red_m + 256);
   float* cmax_s = reinterpret_cast<float*>(smem + C::OFF_CM);  // with fmask: chunk maxima
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -449,7 +445,7 @@ __global__ void __launch_bounds__(kLlThreads, 1)
     }
     for (int i = 0; i < 2; ++i) {
       mbar_init(&s_full[i], 1);
-      mbar_init(&s_empty[i], 8);
+      mbar_init(&s_empty[i], 4);
     }
     mbar_init(&mma_done[0], 1);
     mbar_init(&mma_done[1], 1);
@@ -486,10 +482,10 @@ __global__ void __launch_bounds__(kLlThreads, 1)
         }
       }
     }
-  } else if (warp == 1 || warp == 14) {
+  } else if (warp == 1 || warp == 10) {
     // one thread issues (here the warp-issued form of the statistics kernel measured slower:
     // 6.0 ms against 3.6 ms at N = 4M, M = 2048, D = 39)
-    const int role = warp == 14;  // parity of the chunks this thread issues
+    const int role = warp == 10;  // parity of the chunks this thread issues
     if (lane == 0 && my_tiles > 0 && (two_issuers || role == 0)) {
       const uint32_t idesc = idesc_bf16(128, 128, false, false);
       const uint32_t wb0 = smem_u32(smem + C::OFF_W);
@@ -525,7 +521,7 @@ __global__ void __launch_bounds__(kLlThreads, 1)
       mma_commit(&mma_done[role]);
       mbar_drain(&mma_done[role], 0);
     }
-  } else if (warp >= 10) {
+  } else if (warp >= 6) {
     // Z loaders: thread = frame row of the tile; fill the next TMEM Z buffer from HBM
     const int q4 = warp & 3;
     const int row = q4 * 32 + lane;
@@ -533,7 +529,7 @@ __global__ void __launch_bounds__(kLlThreads, 1)
     for (int it = 0; it < my_tiles; ++it) {
       const int zb = it % ZB;
       const int tile = tile0 + (int)blockIdx.x + it * (int)gridDim.x;
-      if (!mbar_wait(&z_empty[zb], ((it / ZB) & 1) ^ 1, abort_flag, wait_limit)) break;
+      if (!mbar_wait_all(&z_empty[zb], ((it / ZB) & 1) ^ 1, abort_flag, wait_limit)) break;
       tc_fence_after();
       const uint32_t zaddr = tmem + lane_off + C::Z_COL + zb * C::ZCOLS;
       auto frame_of = [&](int t) -> long long {
@@ -561,10 +557,10 @@ __global__ void __launch_bounds__(kLlThreads, 1)
       }
     }
   } else {
-    // epilogue: thread = frame row; the two warps of a lane quadrant take the two 64-column
-    // halves of each chunk and merge their partial sums at the end of the tile
+    // epilogue: thread = frame row, one warp per lane quadrant taking all 128 columns of a chunk
+    // (two warps per quadrant, each taking a 64-column half and merging the halves at the end of
+    // the tile, measured 4.5% slower: more busy warps beside the MMA-issuing threads)
     const int q4 = warp & 3;
-    const int hf = (warp - 2) >> 2;
     const int row = q4 * 32 + lane;
     const uint32_t lane_off = (uint32_t)(q4 * 32) << 16;
     double llsum = 0.0;
@@ -575,20 +571,20 @@ __global__ void __launch_bounds__(kLlThreads, 1)
       float m = -INFINITY, sum = 0.0f;
       for (int ch = 0; ch < n_chunks && ok; ++ch, ++j) {
         const int b = j & 1;
-        if (!mbar_wait(&s_full[b], (j >> 1) & 1, abort_flag, wait_limit)) { ok = false; break; }
+        if (!mbar_wait_all(&s_full[b], (j >> 1) & 1, abort_flag, wait_limit)) { ok = false; break; }
         tc_fence_after();
-        // read both 32-column halves, then hand the accumulator back to the MMA issuer before
+        // read the whole row of the chunk, then hand the accumulator back to the MMA issuer before
         // doing the arithmetic: the issuer waits on this release, so it comes as early as possible
-        uint32_t vv[2][32];
-        tmem_ld32(tmem + lane_off + C::S_COL + b * 128 + hf * 64, vv[0]);
-        tmem_ld32(tmem + lane_off + C::S_COL + b * 128 + hf * 64 + 32, vv[1]);
+        uint32_t vv[4][32];
+#pragma unroll
+        for (int sub = 0; sub < 4; ++sub) tmem_ld32(tmem + lane_off + C::S_COL + b * 128 + 32 * sub, vv[sub]);
         tmem_ld_wait();
         tc_fence_before();
         __syncwarp();
         if (lane == 0) mbar_arrive(&s_empty[b]);
-        float cm = -INFINITY;  // this half's largest logit of the chunk
+        float cm = -INFINITY;
 #pragma unroll
-        for (int sub = 0; sub < 2; ++sub) {
+        for (int sub = 0; sub < 4; ++sub) {
           const uint32_t* v = vv[sub];
           float mx = __uint_as_float(v[0]);
 #pragma unroll
@@ -606,25 +602,18 @@ __global__ void __launch_bounds__(kLlThreads, 1)
             m = mn;
           }
         }
-        if (fmask) cmax_s[(hf * n_chunks + ch) * 128 + row] = cm;
+        if (fmask) cmax_s[ch * 128 + row] = cm;  // the chunk's largest logit of the row
       }
-      // merge the two column halves of each row. Both warps of the pair reach both barriers on
-      // every path and leave the tile loop together: the stop decision is one snapshot of the
-      // abort flag (raised by any failed wait) taken between the barriers.
-      if (hf == 1) { red_m[row] = m; red_s[row] = sum; }
-      named_sync(1 + q4, 64);
-      if (hf == 0 && lane == 0) stop_s[q4] = *abort_flag;
-      if (hf == 0 && ok && !*abort_flag) {
-        const float m1 = red_m[row], s1 = red_s[row];
-        const float M2 = fmaxf(m, m1);
-        float S2 = 0.0f;
-        if (M2 > -INFINITY) S2 = sum * ex2(m - M2) + s1 * ex2(m1 - M2);
+      if (ok && !*abort_flag) {
+        const float M2 = m, S2 = sum;
+        // the chunks holding a logit within mask_thr2 of the frame's LSE (one component: every
+        // real frame keeps it; trouble frames and padding keep nothing); trouble frames carry
+        // +inf (every posterior prunes to 0), padding carries NaN
         const long long f = (long long)tile * 128 + row;  // padded row
         const long long fr = row_frame ? row_frame[f] : (f < N ? f : -1);
         float l2 = M2 + lg2(S2);
         const bool trouble = !(M2 > trouble2) || !isfinite(l2);
         if (fr >= 0) {
-          // trouble frames carry +inf (every posterior prunes to 0), padding carries NaN
           ll2_out[f] = trouble ? INFINITY : l2;
           const float lnat = trouble ? minLL : l2 * kLn2;
           if (ll_out) ll_out[fr] = lnat;
@@ -633,26 +622,21 @@ __global__ void __launch_bounds__(kLlThreads, 1)
           ll2_out[f] = __int_as_float(0x7fc00000);
         }
         if (fmask) {
-          // the chunks holding a logit within mask_thr2 of the frame's LSE (one component: every
-          // real frame keeps it; trouble frames and padding keep nothing)
           uint32_t msk = 0;
           if (fr >= 0 && !trouble) {
             if (mact_dev ? *mact_dev == 1 : single_comp != 0) {
               msk = 1u;
             } else {
-              for (int q = 0; q < n_chunks; ++q) {
-                const float cq = fmaxf(cmax_s[q * 128 + row], cmax_s[(n_chunks + q) * 128 + row]);
-                if (cq - l2 > mask_thr2) msk |= 1u << q;
-              }
+              for (int q = 0; q < n_chunks; ++q)
+                if (cmax_s[q * 128 + row] - l2 > mask_thr2) msk |= 1u << q;
             }
           }
           fmask[f] = msk;
         }
       }
-      named_sync(1 + q4, 64);
-      if (stop_s[q4]) break;
+      if (__any_sync(0xffffffffu, !ok || *abort_flag != 0)) break;  // the warp leaves together
     }
-    if (hf == 0) llpart[(size_t)blockIdx.x * 128 + row] = llsum;
+    llpart[(size_t)blockIdx.x * 128 + row] = llsum;
   }
   __syncthreads();
   if (*abort_flag) {
@@ -949,8 +933,8 @@ __global__ void __launch_bounds__(kAccThreads, 1)
     for (int i = 0; i < nt; ++i) {
       const int s = i % NZ, b = i % NS, mb = i & 1;
       per.begin(i, kNoPeriod);
-      const bool okw = mbar_wait_sleep(&z_full[s], (i / NZ) & 1, abort_flag, wait_limit) &&
-                       mbar_wait_sleep(&s_full[b], (i / NS) & 1, abort_flag, wait_limit);
+      const bool okw = mbar_wait_sleep_all(&z_full[s], (i / NZ) & 1, abort_flag, wait_limit) &&
+                       mbar_wait_sleep_all(&s_full[b], (i / NS) & 1, abort_flag, wait_limit);
       const uint32_t lla = ll_sa + (uint32_t)(s * FT * 4);
       const uint32_t sbuf = tmem + lane_off + C::S_COL + b * FT;
       const long long tile = tile_list ? (long long)tile_list[t0 + i] : (long long)(t0 + i);
@@ -1415,8 +1399,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     constexpr int NCH = FT / 32;  // 32-frame chunks per warp (4)
     for (int i = 0; i < nt; ++i) {
       const int b = i % NS;
-      if (!mbar_wait(&z_full[i % NZ], (i / NZ) & 1, abort_flag, wait_limit)) break;
-      if (!mbar_wait(&s_full[b], (i / NS) & 1, abort_flag, wait_limit)) break;
+      if (!mbar_wait_all(&z_full[i % NZ], (i / NZ) & 1, abort_flag, wait_limit)) break;
+      if (!mbar_wait_all(&s_full[b], (i / NS) & 1, abort_flag, wait_limit)) break;
       tc_fence_after();
       const float* lls = ll_s + (i % NZ) * FT;
       // pass c converts 32-frame chunk c; the first half of the tile's frames is signalled
@@ -1484,7 +1468,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
     for (int k = 0; k < KH * 16; ++k) dacc[k] = 0.0f;
     auto readout = [&](int t, bool flush, int slot) -> bool {
-      if (!mbar_wait(&d_full[t % ND], (t / ND) & 1, abort_flag, wait_limit)) return false;
+      if (!mbar_wait_all(&d_full[t % ND], (t / ND) & 1, abort_flag, wait_limit)) return false;
       tc_fence_after();
       const uint32_t dbase = tmem + lane_off + C::D_COL + (t % ND) * (C::NSET * N2);
       if constexpr (C::SPLIT) {

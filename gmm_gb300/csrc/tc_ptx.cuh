@@ -117,6 +117,19 @@ __device__ __forceinline__ bool mbar_wait_sleep(uint64_t* bar, uint32_t parity, 
   }
 }
 
+// Waits for every lane of a warp with one outcome for the whole warp: each lane waits, then the
+// lanes vote. A wait that gave up in one lane (its limit, or the abort flag seen earlier than by
+// the others) makes the whole warp leave together, so the warp-collective tcgen05.ld / st that
+// follow never run in part of a warp. Call with all 32 lanes converged.
+__device__ __forceinline__ bool mbar_wait_all(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
+                                              long long limit) {
+  return __all_sync(0xffffffffu, mbar_wait(bar, parity, abort_flag, limit));
+}
+__device__ __forceinline__ bool mbar_wait_sleep_all(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
+                                                    long long limit) {
+  return __all_sync(0xffffffffu, mbar_wait_sleep(bar, parity, abort_flag, limit));
+}
+
 // shared-memory accesses by shared-window address (the compiler cannot always tell that a
 // pointer derived from the aligned dynamic shared memory is shared)
 __device__ __forceinline__ float4 lds_f4(uint32_t a) {
