@@ -381,6 +381,13 @@ __host__ __device__ constexpr int ll_zb(int K) { return K <= 80 ? 2 : 1; }
 // plane images) while the MMAs run on the previous one. With one, they build the next tile's
 // plane images while the MMAs run on the current tile and copy them into TMEM when it is done.
 __host__ __device__ constexpr int ll_nw(int K) { return K <= 96 ? 3 : 2; }
+// With three W stages the TMA ring holds whole chunks (three planes each). With two, the two
+// chunks in flight (one per MMA-issuing thread, their MMAs interleaved in the tensor pipe) end
+// together, and a chunk-granular ring would refill both stages at once while the pipe waits. So
+// two stages become six plane slots, filled in order of first use and released as soon as a
+// plane's last product is issued: the MMAs order the products plane by plane (lo, then mid,
+// then hi weight plane), which leaves each plane's slot half a chunk or more to refill.
+__host__ __device__ constexpr bool ll_plane_ring(int K) { return ll_nw(K) == 2; }
 
 template <int K>
 struct LlCfg {
@@ -392,7 +399,7 @@ struct LlCfg {
   static constexpr int Z_COL = 256;        // Z buffers
   static constexpr int OFF_W = 0;
   static constexpr int OFF_BAR = OFF_W + NW * W_STAGE;
-  static constexpr int OFF_MISC = OFF_BAR + 16 * 8;
+  static constexpr int OFF_MISC = OFF_BAR + 24 * 8;
   static constexpr int SMEM = cmax(OFF_MISC + 64 + 1024, 120 * 1024);
   // with frame masks: [chunks][128 rows] chunk maxima of the logits
   static constexpr int OFF_CM = OFF_MISC + 64;
@@ -415,16 +422,18 @@ __global__ void __launch_bounds__(kLlThreads, 1)
   // images.
   using C = LlCfg<K>;
   constexpr int ZB = C::ZB, NW = C::NW;
+  constexpr bool PR = ll_plane_ring(K);
+  constexpr int NSLOT = PR ? 3 * NW : NW;  // W ring slots: planes or whole chunks
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + C::OFF_BAR);
   uint64_t* z_full = bars + 0;   // [ZB <= 2]
   uint64_t* z_empty = bars + 2;  // [ZB]
-  uint64_t* w_full = bars + 4;   // [NW <= 3]
-  uint64_t* w_empty = bars + 7;  // [NW]
-  uint64_t* s_full = bars + 10;  // [2]
-  uint64_t* s_empty = bars + 12; // [2]
-  uint64_t* mma_done = bars + 14;  // [2]: one per MMA-issuing thread
+  uint64_t* w_full = bars + 4;   // [NSLOT <= 6]
+  uint64_t* w_empty = bars + 10; // [NSLOT]
+  uint64_t* s_full = bars + 16;  // [2]
+  uint64_t* s_empty = bars + 18; // [2]
+  uint64_t* mma_done = bars + 20;  // [2]: one per MMA-issuing thread
   uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(smem + C::OFF_MISC);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + C::OFF_MISC + 8);
   float* cmax_s = reinterpret_cast<float*>(smem + C::OFF_CM);  // with fmask: chunk maxima
@@ -439,7 +448,7 @@ __global__ void __launch_bounds__(kLlThreads, 1)
       mbar_init(&z_full[i], 4);
       mbar_init(&z_empty[i], two_issuers ? 2 : 1);
     }
-    for (int i = 0; i < NW; ++i) {
+    for (int i = 0; i < NSLOT; ++i) {
       mbar_init(&w_full[i], 1);
       mbar_init(&w_empty[i], 1);
     }
@@ -461,7 +470,13 @@ __global__ void __launch_bounds__(kLlThreads, 1)
   tc_fence_after();
   const uint32_t tmem = *tmem_holder;
   const int my_tiles = (n_tiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
-  int w_issued = 0;  // W chunk copies issued (loader thread)
+  int w_issued = 0;  // W ring fills issued (loader thread)
+  // plane ring: position of fill u (0 = the lo weight plane, 1 = mid, 2 = hi) of chunk j (counted
+  // over the CTA's tiles) in the fill order. Two issuers take the chunks of a pair (j even, j + 1)
+  // together, so their fills interleave; the slot is position % 6, its use count position / 6.
+  auto wpos = [two_issuers = (n_chunks % 2) == 0](int j, int u) -> int {
+    return two_issuers ? 6 * (j >> 1) + 2 * u + (j & 1) : 3 * j + u;
+  };
 
   if (warp == 0) {
     if (lane == 0 && my_tiles > 0) {
@@ -471,14 +486,30 @@ __global__ void __launch_bounds__(kLlThreads, 1)
       for (int it = 0; it < my_tiles && ok; ++it) {
         // first W chunk of the tile's model (one model unless a per-tile base is given)
         const int wbase = tile_wbase ? tile_wbase[tile0 + (int)blockIdx.x + it * (int)gridDim.x] : 0;
-        for (int ch = 0; ch < n_chunks; ++ch, ++j) {
-          const int ws = j % NW;
-          if (!mbar_wait(&w_empty[ws], ((j / NW) & 1) ^ 1, abort_flag, wait_limit)) { ok = false; break; }
-          mbar_arrive_expect_tx(&w_full[ws], C::W_STAGE);
-          uint8_t* dst = smem + C::OFF_W + ws * C::W_STAGE;
-          for (int p = 0; p < 3; ++p)
-            load_image(dst + p * C::W_PLANE, &wfull, p, nTw, K, wbase + ch, &w_full[ws]);
-          w_issued = j + 1;
+        if constexpr (PR) {
+          // fills in position order: a pair of chunks (two issuers) or one chunk at a time
+          const int group = two_issuers ? 2 : 1;
+          for (int ch = 0; ch < n_chunks && ok; ch += group, j += group) {
+            for (int u = 0; u < 3 && ok; ++u) {
+              for (int g = 0; g < group; ++g) {
+                const int pos = wpos(j + g, u), ws = pos % NSLOT;
+                if (!mbar_wait(&w_empty[ws], ((pos / NSLOT) & 1) ^ 1, abort_flag, wait_limit)) { ok = false; break; }
+                mbar_arrive_expect_tx(&w_full[ws], C::W_PLANE);
+                load_image(smem + C::OFF_W + ws * C::W_PLANE, &wfull, 2 - u, nTw, K, wbase + ch + g, &w_full[ws]);
+                w_issued = pos + 1;
+              }
+            }
+          }
+        } else {
+          for (int ch = 0; ch < n_chunks; ++ch, ++j) {
+            const int ws = j % NW;
+            if (!mbar_wait(&w_empty[ws], ((j / NW) & 1) ^ 1, abort_flag, wait_limit)) { ok = false; break; }
+            mbar_arrive_expect_tx(&w_full[ws], C::W_STAGE);
+            uint8_t* dst = smem + C::OFF_W + ws * C::W_STAGE;
+            for (int p = 0; p < 3; ++p)
+              load_image(dst + p * C::W_PLANE, &wfull, p, nTw, K, wbase + ch, &w_full[ws]);
+            w_issued = j + 1;
+          }
         }
       }
     }
@@ -495,26 +526,54 @@ __global__ void __launch_bounds__(kLlThreads, 1)
         const int zb = it % ZB;
         if (!mbar_wait(&z_full[zb], (it / ZB) & 1, abort_flag, wait_limit)) { ok = false; break; }
         const uint32_t za = tmem + C::Z_COL + zb * C::ZCOLS;
-        for (int ch = 0; ch < n_chunks; ++ch, ++j) {
+        for (int ch = 0; ch < n_chunks && ok; ++ch, ++j) {
           if (two_issuers && (ch & 1) != role) continue;
-          const int ws = j % NW, b = j & 1;
-          if (!mbar_wait(&w_full[ws], (j / NW) & 1, abort_flag, wait_limit)) { ok = false; break; }
+          const int b = j & 1;
           if (!mbar_wait(&s_empty[b], ((j >> 1) & 1) ^ 1, abort_flag, wait_limit)) { ok = false; break; }
-          tc_fence_after();
-          const uint64_t wd = smem_desc(wb0 + ws * C::W_STAGE, 128 * 16, 128);
           const uint32_t d = tmem + C::S_COL + b * 128;
+          if constexpr (PR) {
+            // products plane by plane: (hi, lo) | (mid, mid) (hi, mid) | (lo, hi) (mid, hi) (hi, hi)
+            // as (Z plane, W plane); each W plane is waited for before its first product and
+            // released after its last
+            constexpr int kOrder[6] = {2, 1, 4, 0, 3, 5};
 #pragma unroll
-          for (int pr = 0; pr < 6; ++pr) {
+            for (int st = 0; st < 6; ++st) {
+              const int pr = kOrder[st];
+              const int u = 2 - prod_w(pr);  // fill of the chunk that holds the product's W plane
+              const int pos = wpos(j, u), ws = pos % NSLOT;
+              if (st == 0 || st == 1 || st == 3) {
+                if (!mbar_wait(&w_full[ws], (pos / NSLOT) & 1, abort_flag, wait_limit)) { ok = false; break; }
+                tc_fence_after();
+              }
+              const uint64_t wd = smem_desc(wb0 + ws * C::W_PLANE, 128 * 16, 128);
 #pragma unroll
-            for (int q = 0; q < K / 16; ++q) {
-              const uint64_t bd = desc_add(wd, prod_w(pr) * C::W_PLANE + q * 2 * 128 * 16);
-              const uint32_t a = za + prod_z(pr) * (K / 2) + q * 8;
-              if (pr == 0 && q == 0) mma_ts_c<false>(d, a, bd, idesc);
-              else mma_ts_c<true>(d, a, bd, idesc);
+              for (int q = 0; q < K / 16; ++q) {
+                const uint64_t bd = desc_add(wd, q * 2 * 128 * 16);
+                const uint32_t a = za + prod_z(pr) * (K / 2) + q * 8;
+                if (st == 0 && q == 0) mma_ts_c<false>(d, a, bd, idesc);
+                else mma_ts_c<true>(d, a, bd, idesc);
+              }
+              if (st == 0 || st == 2 || st == 5) mma_commit(&w_empty[ws]);
             }
+            if (!ok) break;
+          } else {
+            const int ws = j % NW;
+            if (!mbar_wait(&w_full[ws], (j / NW) & 1, abort_flag, wait_limit)) { ok = false; break; }
+            tc_fence_after();
+            const uint64_t wd = smem_desc(wb0 + ws * C::W_STAGE, 128 * 16, 128);
+#pragma unroll
+            for (int pr = 0; pr < 6; ++pr) {
+#pragma unroll
+              for (int q = 0; q < K / 16; ++q) {
+                const uint64_t bd = desc_add(wd, prod_w(pr) * C::W_PLANE + q * 2 * 128 * 16);
+                const uint32_t a = za + prod_z(pr) * (K / 2) + q * 8;
+                if (pr == 0 && q == 0) mma_ts_c<false>(d, a, bd, idesc);
+                else mma_ts_c<true>(d, a, bd, idesc);
+              }
+            }
+            mma_commit(&w_empty[ws]);
           }
           mma_commit(&s_full[b]);
-          mma_commit(&w_empty[ws]);
           if (ch >= n_chunks - (two_issuers ? 2 : 1)) mma_commit(&z_empty[zb]);  // each issuer's last chunk
         }
       }
@@ -640,11 +699,11 @@ __global__ void __launch_bounds__(kLlThreads, 1)
   }
   __syncthreads();
   if (*abort_flag) {
-    // Every role has stopped. The loader's last NW copies may still be in flight (a consumer
+    // Every role has stopped. The loader's last NSLOT fills may still be in flight (a consumer
     // that gave up never waited for them): let them land before the CTA's shared memory goes.
-    // Earlier copies were consumed, so they have landed.
+    // Earlier fills were consumed, so they have landed.
     if (warp == 0 && lane == 0)
-      for (int k = max(0, w_issued - NW); k < w_issued; ++k) mbar_drain(&w_full[k % NW], (k / NW) & 1);
+      for (int k = max(0, w_issued - NSLOT); k < w_issued; ++k) mbar_drain(&w_full[k % NSLOT], (k / NSLOT) & 1);
     if (threadIdx.x == 0) atomicExch(err, 1);
   }
   if (warp == 1) {
