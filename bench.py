@@ -818,13 +818,14 @@ def workload_config(wl, world):
 
 def secondary(name, args, rank, world, gpu, torch, _lib):
     """A second workload measured in the same process (tensor-core path): device-timed value and
-    the end-to-end value, each over its own timed region. "serve": the served loop at two
-    offered rates for 1 s each (the full sweep is `--workload serve`)."""
+    the end-to-end value, each over its own timed region. "serve": the served loop at three
+    offered rates for 1 s each (the full sweep is `--workload serve`); 15000 req/s is close to
+    the loop's capacity, where one backlog can push p99 past 50 ms, and 10000 is not."""
     sa = argparse.Namespace(**vars(args))
     sa.workload = name
     if name == "serve":
         sa.mix, sa.dim, sa.seed = 1024, 60, 5
-        sa.rates, sa.duration, sa.serial_requests = "5000,15000", 1.0, min(args.serial_requests, 200)
+        sa.rates, sa.duration, sa.serial_requests = "5000,10000,15000", 1.0, min(args.serial_requests, 200)
         _, pool, sweep, serial_plain, serial_tc, st, clocks = serve_measure(sa, gpu, torch, _lib)
         best = serve_best(sweep)
         value = best["achieved_rps"] if best else 0.0
