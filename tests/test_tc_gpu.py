@@ -31,8 +31,11 @@ def check_stats(s, o, rel=1e-4):
         assert err.max() <= rel, (k, err.max())
 
 
+# K = 112 and 128 (D = 52, 55, 60) run the logits kernel's plane-granular W ring: with an even
+# chunk count (M = 130, 256: two MMA-issuing threads) and an odd one (M = 300, 384: one)
 @pytest.mark.parametrize("D,M,N", [(39, 16, 2048), (39, 200, 3000), (6, 8, 1000), (20, 4, 777),
-                                   (60, 130, 2500), (1, 5, 640), (47, 64, 1536)])
+                                   (60, 130, 2500), (1, 5, 640), (47, 64, 1536), (52, 300, 2000),
+                                   (60, 384, 1800), (55, 256, 1500)])
 def test_tc_matches_fp64(glib, oracle, D, M, N):
     from gmm_gb300 import synth
     X, w, mu, var = synth.config_em(100 + D, N, D, max(2, M // 2), M)
