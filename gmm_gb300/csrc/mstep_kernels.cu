@@ -14,6 +14,24 @@ namespace gmm {
 
 namespace {
 
+// FP64 -> FP32, round to nearest even, on the integer pipes. GB300 runs the conversion
+// instruction on its FP64 pipe (1/64 of the FP32 rate), where it was most of the batched MAP
+// update's FP64 work. This is the IEEE 754 rounding of the 52-bit significand to 23 bits for
+// results in the normal FP32 range; zero, subnormal, overflowing and non-finite inputs take the
+// conversion instruction. A round-up carry out of the significand increments the exponent (up to
+// infinity), which is the correctly rounded result.
+__device__ __forceinline__ float f64_to_f32_rn(double d) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const unsigned int hi = (unsigned int)(b >> 32), lo = (unsigned int)b;
+  const int e = (int)((hi >> 20) & 0x7ffu) - 1023;  // unbiased exponent
+  if (e < -126 || e > 127) return __double2float_rn(d);
+  const unsigned int keep = ((hi & 0xfffffu) << 3) | (lo >> 29);  // top 23 significand bits
+  const unsigned int rest = lo & 0x1fffffffu;                     // the 29 bits rounded away
+  unsigned int f = (hi & 0x80000000u) | ((unsigned int)(e + 127) << 23) | keep;
+  if (rest > 0x10000000u || (rest == 0x10000000u && (keep & 1u))) f += 1u;
+  return __uint_as_float(f);
+}
+
 __device__ __forceinline__ float reset_var_value() {
   // GMMMixture::Reset (OL_GMModel.cpp:73-83) fills diagonal variances with memset(.., 1, ..)
   return __int_as_float(0x01010101);
@@ -319,7 +337,7 @@ __global__ void mllr_apply_kernel(int M, int D, float* __restrict__ mu, const do
 // speaker's total log-likelihood is copied out as well.
 constexpr int kMapPairs = 32;     // (speaker, component) pairs per block
 constexpr int kMapThreads = 256;
-__global__ void __launch_bounds__(kMapThreads) map_batch_kernel(
+__global__ void __launch_bounds__(kMapThreads, 5) map_batch_kernel(
     int S, int M, int D, const double* __restrict__ plain, const double* __restrict__ part, int K, int n_chunks,
     const int* __restrict__ piece0, const int* __restrict__ npieces, const int* __restrict__ row_of_comp,
     const float* __restrict__ cent, const long long* __restrict__ offs, const float* __restrict__ uw, const float* __restrict__ umu,
@@ -401,7 +419,7 @@ __global__ void __launch_bounds__(kMapThreads) map_batch_kernel(
       // included -- is 1/64 of FP32); the statistics already carry ~1e-6 relative error, FP32
       // adds ~1e-7 of the mean. FP64 stays for the variance update.
       const double Fd = stat(s, m, k);
-      const float Ff = cr ? (float)tc_uncentre_F(Fd, mp, (double)cr[k]) : (float)Fd;
+      const float Ff = f64_to_f32_rn(cr ? tc_uncentre_F(Fd, mp, (double)cr[k]) : Fd);
       am = __fmaf_rn(s_alfa_f[j], __fmul_rn(Ff, s_rmp_f[j]), __fmul_rn(s_one_f[j], um[k]));
     } else if (adapt && (upM || upV)) {
       const double Fk = stat(s, m, k);
