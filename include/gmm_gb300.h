@@ -304,7 +304,7 @@ int gmm_accumulate_noalloc(const float* dX, long long N, int D, int M, const flo
 int gmm_profile_enable(gmm_handle h, int on);
 int gmm_profile_reset(gmm_handle h);
 int gmm_profile_read(gmm_handle h, int cap, const char** names, double* ms, long long* launches);
-/* Number of kernel launches this handle issued since creation (all kernels). */
+/* Number of kernel launches this handle issued since creation (all kernels); 0 for a null handle. */
 long long gmm_launch_count(gmm_handle h);
 
 /* ------------------------------------------------------------------ feature files
