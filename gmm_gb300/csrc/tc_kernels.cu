@@ -474,7 +474,7 @@ __global__ void __launch_bounds__(kLlThreads, 1)
   // plane ring: position of fill u (0 = the lo weight plane, 1 = mid, 2 = hi) of chunk j (counted
   // over the CTA's tiles) in the fill order. Two issuers take the chunks of a pair (j even, j + 1)
   // together, so their fills interleave; the slot is position % 6, its use count position / 6.
-  auto wpos = [two_issuers = (n_chunks % 2) == 0](int j, int u) -> int {
+  auto wpos = [two_issuers](int j, int u) -> int {
     return two_issuers ? 6 * (j >> 1) + 2 * u + (j & 1) : 3 * j + u;
   };
 
